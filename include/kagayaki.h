@@ -1,0 +1,294 @@
+/*
+ * kagayaki.h - C ABI of the GB300 render path (sm_103a).
+ *
+ * A drop-in for the render path of the kagayaki CUDA path tracer: scene
+ * upload, BVH build, closest-hit traversal, the path-traced frame, the SVGF
+ * denoiser, the learned radiance cache and PNG output.  Every entry point is
+ * plain C: pointers and sizes, no C++ or torch types, no exceptions and no
+ * exit() across the boundary.  Each returns a kgk_status; kgk_last_error()
+ * gives the message of the last failure on the calling thread.
+ *
+ * Buffer convention: every array argument may be a host pointer or a device
+ * pointer (cudaMalloc / managed).  The library inspects the pointer and stages
+ * host buffers through its own device memory.  The caller owns its buffers;
+ * the library owns all device memory it allocates until kgk_scene_destroy().
+ * A scene handle is single-threaded and uses one CUDA stream of its own.
+ *
+ * Reference citations (file:line) are paths inside RunningOutRate/kagayaki.
+ */
+#ifndef KAGAYAKI_H_
+#define KAGAYAKI_H_
+
+#include <stddef.h>
+#include <stdint.h>
+#include <stdbool.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define KGK_ABI_VERSION 1
+
+typedef enum kgk_status {
+    KGK_OK = 0,
+    KGK_ERR_INVALID_ARGUMENT = 1, /* null pointer, size out of range, bad enum   */
+    KGK_ERR_OUT_OF_MEMORY = 2,    /* device or host allocation failed            */
+    KGK_ERR_CUDA = 3,             /* a CUDA runtime call failed                  */
+    KGK_ERR_NO_DEVICE = 4,        /* no CUDA device, or not an sm_103 part       */
+    KGK_ERR_IO = 5,               /* file could not be opened / written          */
+    KGK_ERR_PARSE = 6,            /* malformed OBJ / MTL / image                 */
+    KGK_ERR_NOT_BUILT = 7,        /* trace/render before kgk_build_bvh()         */
+    KGK_ERR_DEVICE_CHECK = 8,     /* a kernel's own bounds/iteration check fired */
+    KGK_ERR_UNSUPPORTED = 9
+} kgk_status;
+
+/* ------------------------------------------------------------------------- */
+/* Scene structs, byte-compatible with the reference (sizes and offsets are    */
+/* static_asserted below and in the library).                                  */
+/* ------------------------------------------------------------------------- */
+
+/* struct_Vec.cuh:4-8 `Vec` (x, y, z + pad), 16 B. */
+typedef struct kgk_vec {
+    float x, y, z, align;
+} kgk_vec;
+
+/* struct_Triangle.cuh:8-20 `Triangle`, 156 B.  vn = per-vertex normals,
+ * vt = per-vertex texture coordinates (x = u, y = v). */
+typedef struct kgk_triangle {
+    kgk_vec v0, v1, v2;
+    kgk_vec v0_vn, v1_vn, v2_vn;
+    kgk_vec v0_vt, v1_vt, v2_vt;
+    int32_t material_id;
+    bool is_SmoothNormal;
+    int32_t shape_id;
+} kgk_triangle;
+
+/* struct_Material.cuh:6-11 `Material`, 96 B.  MATERIAL_TYPE_ID 0 = Lambert,
+ * 1 = Disney BRDF; TEXTURE_BASECOLOR_ID -1 = none.  The field name
+ * `cloearcoatGloss` keeps the reference's spelling. */
+typedef struct kgk_material {
+    int32_t MATERIAL_TYPE_ID;
+    int32_t TEXTURE_BASECOLOR_ID;
+    kgk_vec diffuse, emission;
+    float subsurface, metallic, specular, specularTint, roughness, anisotropic,
+          sheen, sheenTint, clearcoat, cloearcoatGloss, IOR, mu_a, mu_s, scatter_g;
+} kgk_material;
+
+/* struct_Texture.cuh:6-8 `Texture`, 24 B: float pixels, bpp channels. */
+typedef struct kgk_texture {
+    float *pixels;
+    int32_t width, height, bpp;
+} kgk_texture;
+
+/* struct_Camera.cuh:12-18 `Camera`, 72 B. */
+typedef struct kgk_camera {
+    kgk_vec CamOrg;
+    kgk_vec CamDir;
+    float CamToScreenDist;
+    kgk_vec ScreenXDir;
+    kgk_vec ScreenYDir;
+    float PixelSize;
+} kgk_camera;
+
+/* struct_Ray.cuh:12-15 `Ray`, 40 B (dir first, then org). */
+typedef struct kgk_ray {
+    kgk_vec dir;
+    kgk_vec org;
+    double _dummy;
+} kgk_ray;
+
+typedef struct kgk_scene kgk_scene; /* opaque */
+
+/* ------------------------------------------------------------------------- */
+/* Render configuration (replaces the compile-time constants of                */
+/* global_values.cuh:17-24, RayTrace.cuh:95 and SVGF.cuh).                     */
+/* ------------------------------------------------------------------------- */
+
+typedef enum kgk_estimator {
+    /* The reference's estimator, quirks included (radiance starts at 1e-4,
+     * un-weighted environment on miss, emission only at depth 0 and on
+     * Russian-roulette termination, pixel-corner environment samples, xorshift
+     * seeding of render.cuh:29).  Used for image parity with the reference. */
+    KGK_ESTIMATOR_COMPAT = 0,
+    /* Unbiased path tracing with NEE + MIS (balance heuristic over BSDF, face
+     * light and environment sampling), pixel jitter, max-depth cap. */
+    KGK_ESTIMATOR_UNBIASED = 1
+} kgk_estimator;
+
+typedef struct kgk_render_config {
+    int32_t width, height;   /* image size (global_values.cuh:17-18)              */
+    int32_t spp;             /* samples per pixel in this call                    */
+    int32_t max_depth;       /* max path vertices; <= 0 = unlimited (compat)      */
+    int32_t rr_start_depth;  /* Russian roulette may kill from this depth on (3)  */
+    int32_t estimator;       /* kgk_estimator                                     */
+    uint64_t seed;           /* stream seed (unbiased); ignored by compat         */
+    int32_t frame_index;     /* frame number, decorrelates frames                 */
+    int32_t accumulate;      /* 1: add this call's samples into the scene's FP64
+                                accumulator (converged references)              */
+    int32_t wave_paths;      /* paths in flight per wave; 0 = automatic            */
+    int32_t count_work;      /* 1: count BVH nodes visited / triangles tested      */
+    int32_t write_gbuffer;   /* 1: write the SVGF G-buffer from primary hits       */
+    int32_t use_cache;       /* 1: terminate paths into the radiance cache         */
+    int32_t reserved[6];
+} kgk_render_config;
+
+/* Work counters of one call.  Rays follow the reference's counting rule: one
+ * ray per traversal call (closest, shadow, MIS, reprojection). */
+typedef struct kgk_stats {
+    uint64_t rays_closest;        /* primary + extension rays                    */
+    uint64_t rays_shadow;         /* shadow / occlusion rays                     */
+    uint64_t traversal_overflows; /* rays whose traversal stack overflowed      */
+    uint64_t nodes_visited;       /* wide nodes intersected (count_work only)   */
+    uint64_t tris_tested;         /* triangles tested (count_work only)         */
+    uint64_t paths;               /* camera paths traced                         */
+    double ms_device;             /* device time of the call (CUDA events)       */
+    double reserved[4];
+} kgk_stats;
+
+typedef struct kgk_bvh_info {
+    uint64_t n_triangles;
+    uint64_t n_wide_nodes;        /* 8-wide compressed nodes                     */
+    uint64_t n_binary_nodes;      /* nodes of the binned-SAH binary tree         */
+    uint32_t max_depth;           /* of the wide tree                            */
+    uint32_t max_leaf_size;
+    double sah_cost;              /* SAH cost of the binary tree                 */
+    double ms_build;              /* device time of the build                    */
+    uint64_t device_bytes;        /* wide nodes + triangle records               */
+} kgk_bvh_info;
+
+/* ------------------------------------------------------------------------- */
+/* Library                                                                     */
+/* ------------------------------------------------------------------------- */
+
+/* Version string of the library. */
+const char *kgk_version(void);
+/* Human-readable name of a status code. */
+const char *kgk_status_string(kgk_status status);
+/* Copies the message of the calling thread's last failure into buf. */
+kgk_status kgk_last_error(char *buf, size_t len);
+/* Selects the CUDA device for handles created afterwards on this thread. */
+kgk_status kgk_set_device(int device);
+
+/* ------------------------------------------------------------------------- */
+/* Scene (replaces render_prepare.cuh:33-51, main.cu:110-175 and the device    */
+/* symbols ObjectsNum / Light_strength_sum_size / Exists_NoLight / NoHDR set   */
+/* through cudaGetSymbolAddress at main.cu:154-175)                             */
+/* ------------------------------------------------------------------------- */
+
+/* Uploads triangles, materials, textures (host float pixels) and an optional
+ * HDR environment (hdr may be NULL: the reference's HOST_Exists_NoHDR case,
+ * background = (1,1,1)).  Also builds the face-light CDF
+ * (NextEventEstimation_FaceLight.cuh:8-21) and the environment CDF
+ * (ImageBasedLighting.cuh:59-73).  n_tris >= 1, n_mats >= 1. */
+kgk_status kgk_scene_create(const kgk_triangle *tris, size_t n_tris,
+                            const kgk_material *mats, size_t n_mats,
+                            const kgk_texture *textures, size_t n_textures,
+                            const kgk_texture *hdr, kgk_scene **out);
+
+/* Loads a Wavefront OBJ (+ MTL in mtl_dir) and an optional Radiance .hdr
+ * environment: the loader semantics of load_object
+ * (FileIO/IO_load_WavefrontObj.cuh:10-127) and load_HDR
+ * (FileIO/IO_load_images.cuh:17-19).  Missing vn/vt are tolerated (flat
+ * normal, zero uv) where the reference would crash. */
+kgk_status kgk_scene_load_obj(const char *obj_path, const char *hdr_path, kgk_scene **out);
+
+void kgk_scene_destroy(kgk_scene *scene);
+
+/* Builds the acceleration structure on the GPU: binned SAH into a binary tree,
+ * collapsed into 8-wide compressed nodes.  Replaces construct_BVH
+ * (ConstructBVH.cuh:204) and MallocAndSetBVHtreeOnDevice
+ * (struct_BVH_node.cuh:72-83).  info may be NULL. */
+kgk_status kgk_build_bvh(kgk_scene *scene, kgk_bvh_info *info);
+
+/* Structural check of the built BVH on the host (every triangle referenced
+ * once, child boxes enclose their contents).  Returns KGK_ERR_DEVICE_CHECK and
+ * a message when an invariant fails. */
+kgk_status kgk_bvh_validate(kgk_scene *scene);
+
+/* ------------------------------------------------------------------------- */
+/* Traversal (replaces willIntersectWithTriangle_nonRecursive,                 */
+/* ConstructBVH.cuh:286-368)                                                   */
+/* ------------------------------------------------------------------------- */
+
+/* Closest hit of n rays: face_id[i] = index of the hit triangle in the scene's
+ * input order or -1 on a miss, t[i] = hit distance (1e38 on a miss).  A hit
+ * needs t >= 1e-5 (struct_Triangle.cuh:57); equal distances resolve to the
+ * smaller face id.  Intersection is watertight FP32. */
+kgk_status kgk_trace_closest(kgk_scene *scene, const kgk_ray *rays, size_t n,
+                             int32_t *face_id, float *t, kgk_stats *stats);
+
+/* Occlusion of n rays: occluded[i] = 1 when any triangle is hit with
+ * 1e-5 <= t < t_max[i] (t_max may be NULL: unbounded). */
+kgk_status kgk_trace_any(kgk_scene *scene, const kgk_ray *rays, const float *t_max,
+                         size_t n, uint8_t *occluded, kgk_stats *stats);
+
+/* ------------------------------------------------------------------------- */
+/* Camera and frame                                                            */
+/* ------------------------------------------------------------------------- */
+
+/* Camera_SetUpCamera (struct_Camera.cuh:27-35): Euler rotation in degrees
+ * (X then Y then Z), PixelSize = 36 / image_height. */
+kgk_status kgk_camera_setup(kgk_vec origin, float cam_to_screen_dist, float rotate_x_deg,
+                            float rotate_y_deg, float rotate_z_deg, int32_t image_height,
+                            kgk_camera *out);
+
+/* Renders one frame: spp paths per pixel, out[y*width+x] = mean radiance of
+ * this call's samples (x,y,z; align = 1).  Replaces render<<<>>>
+ * (render.cuh:21-49, main.cu:199) with a wavefront pipeline.  prev_cam may be
+ * NULL (no reprojection).  When cfg->accumulate is set, the samples are also
+ * added to the scene's FP64 accumulator (see kgk_accum_*). */
+kgk_status kgk_render(kgk_scene *scene, const kgk_camera *cam, const kgk_camera *prev_cam,
+                      const kgk_render_config *cfg, kgk_vec *out, kgk_stats *stats);
+
+/* FP64 accumulator of kgk_render(accumulate=1): resets it for width x height. */
+kgk_status kgk_accum_reset(kgk_scene *scene, int32_t width, int32_t height);
+/* Reads the accumulator: mean[p] (x,y,z) and, when var != NULL, the per-pixel
+ * sample variance of the mean, both in FP64.  n_samples may be NULL. */
+kgk_status kgk_accum_read(kgk_scene *scene, double *mean_rgb, double *var_rgb,
+                          uint64_t *n_samples);
+
+/* ------------------------------------------------------------------------- */
+/* SVGF (replaces ApplySVGF, SVGF.cuh:495-522)                                  */
+/* ------------------------------------------------------------------------- */
+
+typedef enum kgk_svgf_mode {
+    /* The reference's filter in its race-free reading: temporal accumulation,
+     * moments, 3x3 variance blur and 5x5 a-trous passes with full-image
+     * barriers between phases, the reference's constants and quirks. */
+    KGK_SVGF_COMPAT = 0,
+    /* Standard SVGF: working reprojection from the previous camera, temporal
+     * alpha, n a-trous iterations with edge-stopping sigmas. */
+    KGK_SVGF_STANDARD = 1
+} kgk_svgf_mode;
+
+typedef struct kgk_svgf_config {
+    int32_t mode;            /* kgk_svgf_mode                                   */
+    int32_t width, height;
+    int32_t frame_index;     /* 0 resets history (SVGF.cuh:502-504)            */
+    int32_t atrous_iterations;   /* 5                                          */
+    int32_t atrous_repeats;      /* compat: 5 (the k-loop of SVGF.cuh:486)     */
+    float alpha;             /* temporal blend of the new frame (0.2)          */
+    float sigma_z, sigma_n, sigma_l; /* 1, 128, 4                              */
+    int32_t reserved[6];
+} kgk_svgf_config;
+
+/* Filters the frame last rendered with write_gbuffer=1.  noisy is read and
+ * filtered is written (both width*height kgk_vec, host or device). */
+kgk_status kgk_svgf(kgk_scene *scene, const kgk_svgf_config *cfg, const kgk_vec *noisy,
+                    kgk_vec *filtered);
+
+/* ------------------------------------------------------------------------- */
+/* Image output (replaces save_png, FileIO/IO_save_png.cuh:34-56)              */
+/* ------------------------------------------------------------------------- */
+
+/* gamma 1/2.2, then clamp to [0,1], then x255 truncated, alpha 255
+ * (IO_save_png.cuh:26,7,47-52): out = width*height*4 bytes. */
+kgk_status kgk_tonemap_rgba8(const kgk_vec *img, int32_t width, int32_t height, uint8_t *out);
+/* Writes the tone-mapped image as an RGBA8 PNG. */
+kgk_status kgk_save_png(const kgk_vec *img, int32_t width, int32_t height, const char *path);
+
+#ifdef __cplusplus
+} /* extern "C" */
+#endif
+
+#endif /* KAGAYAKI_H_ */

@@ -1,0 +1,197 @@
+"""Python bindings of the CPU oracle (orc.c) and of the reference's own code
+built for the host (oracle/_ref).  TEST INFRASTRUCTURE ONLY: imported by
+tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg, never by the
+product package.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ORC_SO = os.path.join(HERE, "_build", "liborc.so")
+REF_SO = os.path.join(HERE, "_ref", "libkgkref.so")
+
+_vp = ctypes.c_void_p
+_i64 = ctypes.c_int64
+_i32 = ctypes.c_int
+_f32 = ctypes.c_float
+
+
+def build(ref=False):
+    """Builds liborc.so (and the reference library when ref=True and the
+    reference checkout exists)."""
+    subprocess.run(["make", "-s", "-C", HERE, "orc"], check=True)
+    if ref:
+        subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
+
+
+def _ptr(a):
+    return a.ctypes.data_as(_vp) if a is not None else None
+
+
+_orc = None
+
+
+def orc():
+    global _orc
+    if _orc is None:
+        if not os.path.exists(ORC_SO):
+            build()
+        L = ctypes.CDLL(ORC_SO)
+        L.orc_intersect_ref.argtypes = [_vp, _vp, _vp, _vp, _vp]
+        L.orc_intersect_ref.restype = _i32
+        L.orc_closest_brute.argtypes = [_vp, _i64, _vp, _i64, _vp, _vp, _i32]
+        L.orc_classify.argtypes = [_vp, _i64, _vp, _i64, _vp, _vp, _vp, _i32]
+        L.orc_bvh_build.argtypes = [_vp, _i64]
+        L.orc_bvh_build.restype = _vp
+        L.orc_bvh_closest.argtypes = [_vp, _vp, _i64, _vp, _vp, _i32]
+        L.orc_bvh_free.argtypes = [_vp]
+        L.orc_xorshift.argtypes = [ctypes.c_uint64]
+        L.orc_xorshift.restype = ctypes.c_uint64
+        L.orc_camera_setup.argtypes = [_vp, _f32, _f32, _f32, _f32, _i32, _vp]
+        L.orc_tonemap_rgba8.argtypes = [_vp, _i64, _vp]
+        L.orc_light_cdf.argtypes = [_vp, _i64, _vp, _vp]
+        L.orc_env_cdf.argtypes = [_vp, _i32, _i32, _i32, _vp]
+        L.orc_render_compat.argtypes = [_vp, _i64, _vp, _i64, _vp, _i32, _vp, _i32, _i32, _i32,
+                                        _vp, _i32, _i32, _i32, _i32, _vp]
+        L.orc_render_compat.restype = _i64
+        L.orc_set_point_arg_order.argtypes = [_i32]
+        _orc = L
+    return _orc
+
+
+def nthreads():
+    return max(1, os.cpu_count() or 1)
+
+
+def closest_brute(tris, rays):
+    n = len(rays)
+    ids = np.empty(n, np.int32)
+    t = np.empty(n, np.float32)
+    orc().orc_closest_brute(_ptr(tris), len(tris), _ptr(rays), n, _ptr(ids), _ptr(t), nthreads())
+    return ids, t
+
+
+def classify(tris, rays, ids, t):
+    flags = np.empty(len(rays), np.uint8)
+    orc().orc_classify(_ptr(tris), len(tris), _ptr(rays), len(rays), _ptr(ids), _ptr(t),
+                       _ptr(flags), nthreads())
+    return flags
+
+
+def closest_bvh(tris, rays):
+    L = orc()
+    b = L.orc_bvh_build(_ptr(tris), len(tris))
+    try:
+        n = len(rays)
+        ids = np.empty(n, np.int32)
+        t = np.empty(n, np.float32)
+        L.orc_bvh_closest(b, _ptr(rays), n, _ptr(ids), _ptr(t), nthreads())
+    finally:
+        L.orc_bvh_free(b)
+    return ids, t
+
+
+def camera_setup(org, dist, rot, image_height):
+    out = np.zeros(18, np.float32)
+    o = np.asarray(org, np.float32)
+    orc().orc_camera_setup(_ptr(o), dist, rot[0], rot[1], rot[2], image_height, _ptr(out))
+    return out
+
+
+def tonemap(img_vec4):
+    img = np.ascontiguousarray(img_vec4, np.float32).reshape(-1, 4)
+    out = np.empty((len(img), 4), np.uint8)
+    orc().orc_tonemap_rgba8(_ptr(img), len(img), _ptr(out))
+    return out
+
+
+def light_cdf(tris, mats):
+    out = np.empty(len(tris), np.float32)
+    orc().orc_light_cdf(_ptr(tris), len(tris), _ptr(mats), _ptr(out))
+    return out
+
+
+def env_cdf(env):
+    env = np.ascontiguousarray(env, np.float32)
+    h, w, bpp = env.shape
+    out = np.empty(w * h, np.float32)
+    orc().orc_env_cdf(_ptr(env), w, h, bpp, _ptr(out))
+    return out
+
+
+def render_compat(tris, mats, cam, width, height, frames, env=None, threads=None):
+    """Returns (frames, height*width, 3) float32 samples and the traversal
+    count.  Pixel 0 is NaN (the reference's seed divides by zero there)."""
+    out = np.empty((frames, width * height, 3), np.float32)
+    env_p, hw, hh, hb = None, 0, 0, 0
+    if env is not None:
+        env = np.ascontiguousarray(env, np.float32)
+        hh, hw, hb = env.shape
+        env_p = _ptr(env)
+    cam = np.ascontiguousarray(cam, np.float32)
+    n = orc().orc_render_compat(_ptr(tris), len(tris), _ptr(mats), len(mats), None, 0, env_p, hw,
+                                hh, hb, _ptr(cam), width, height, frames,
+                                threads or nthreads(), _ptr(out))
+    return out, n
+
+
+# ---------------------------------------------------------------------------
+# The reference's own code (host build, this container only)
+# ---------------------------------------------------------------------------
+_ref = None
+
+
+def ref_available():
+    return os.path.exists(REF_SO)
+
+
+def ref():
+    global _ref
+    if _ref is None:
+        L = ctypes.CDLL(REF_SO)
+        L.ref_trace_closest.argtypes = [_vp, _i32, _vp, ctypes.c_longlong, _vp, _vp, _vp, _i32, _vp]
+        L.ref_trace_closest.restype = ctypes.c_longlong
+        L.ref_bvh_stats.argtypes = [_vp]
+        L.ref_render.argtypes = [_vp, _i32, _vp, _i32, _vp, _i32, _vp, _i32, _i32, _i32, _vp, _vp,
+                                 _i32, _i32, _i32, _i32, _vp, _vp]
+        L.ref_render.restype = ctypes.c_longlong
+        L.ref_svgf.argtypes = [_i32, _i32, _vp, _vp, _vp, _vp, _i32]
+        L.ref_svgf.restype = _i32
+        L.ref_sizeof_svgfbuffer.restype = _i32
+        L.ref_disney_eval.argtypes = [_vp, _i32, _vp, _vp, _vp, _vp, _vp]
+        L.ref_camera_setup.argtypes = [_vp, _f32, _f32, _f32, _f32, _vp]
+        L.ref_light_cdf.argtypes = [_vp, _i32, _vp, _i32, _vp]
+        L.ref_env_cdf.argtypes = [_vp, _i32, _i32, _i32, _vp]
+        _ref = L
+    return _ref
+
+
+def ref_trace(tris, rays, threads=None):
+    n = len(rays)
+    ids = np.empty(n, np.int32)
+    t = np.empty(n, np.float32)
+    ok = np.empty(n, np.uint8)
+    bs = ctypes.c_double()
+    nodes = ref().ref_trace_closest(_ptr(tris), len(tris), _ptr(rays), n, _ptr(ids), _ptr(t),
+                                    _ptr(ok), threads or nthreads(), ctypes.byref(bs))
+    return ids, t, ok, nodes, bs.value
+
+
+def ref_render(tris, mats, cam, width, height, frames, env=None, threads=None, gbuf=False):
+    out = np.empty((frames, width * height, 3), np.float32)
+    env_p, hw, hh, hb = None, 0, 0, 0
+    if env is not None:
+        env = np.ascontiguousarray(env, np.float32)
+        hh, hw, hb = env.shape
+        env_p = _ptr(env)
+    cam = np.ascontiguousarray(cam, np.float32)
+    gb = None
+    if gbuf:
+        gb = np.zeros(width * height * ref().ref_sizeof_svgfbuffer(), np.uint8)
+    n = ref().ref_render(_ptr(tris), len(tris), _ptr(mats), len(mats), None, 0, env_p, hw, hh, hb,
+                         _ptr(cam), _ptr(cam), width, height, frames, threads or nthreads(),
+                         _ptr(out), _ptr(gb))
+    return (out, n, gb) if gbuf else (out, n)
