@@ -1,0 +1,167 @@
+"""Host-side mirror of the reference's render interface over the C ABI.
+
+    scene = Scene(triangles, materials, env=None)   # render_prepare + upload
+    scene.build_bvh()                                # construct_BVH
+    ids, t = scene.trace_closest(rays)               # willIntersectWithTriangle_nonRecursive
+    cam = camera_setup(origin, dist, rot, height)    # Camera_SetUpCamera
+    img = scene.render(cam, cfg)                     # render<<<>>>
+    save_png(img, path)                              # save_png
+
+Arrays are numpy structured arrays with the reference layouts
+(kagayaki_gb300.structs).  Errors raise KgkError with the library's message.
+"""
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from ._lib import KgkError, check, lib
+from .structs import (MATERIAL, RAY, TRIANGLE, KgkBvhInfo, KgkCamera, KgkRenderConfig, KgkStats,
+                      KgkSvgfConfig, KgkTexture, KgkVec)
+
+ESTIMATOR_COMPAT = 0
+ESTIMATOR_UNBIASED = 1
+
+
+def _p(a):
+    return ctypes.c_void_p(a.ctypes.data) if a is not None else None
+
+
+def _as(a, dtype):
+    a = np.ascontiguousarray(a)
+    if a.dtype != dtype:
+        a = a.astype(dtype)
+    return a
+
+
+def stats_dict(s):
+    return {k: getattr(s, k) for k, _ in KgkStats._fields_ if k != "reserved"}
+
+
+class Scene:
+    """A device-resident scene (owns a kgk_scene handle)."""
+
+    def __init__(self, triangles, materials, textures=None, env=None):
+        self._h = ctypes.c_void_p()
+        tris = _as(triangles, TRIANGLE)
+        mats = _as(materials, MATERIAL)
+        self._keep = []
+        tex_arr = None
+        ntex = 0
+        if textures:
+            tex_arr = (KgkTexture * len(textures))()
+            for i, t in enumerate(textures):
+                t = np.ascontiguousarray(t, np.float32)
+                self._keep.append(t)
+                tex_arr[i].pixels = t.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+                tex_arr[i].height, tex_arr[i].width, tex_arr[i].bpp = t.shape
+            ntex = len(textures)
+        hdr = None
+        if env is not None:
+            e = np.ascontiguousarray(env, np.float32)
+            self._keep.append(e)
+            hdr = KgkTexture(e.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), e.shape[1], e.shape[0],
+                             e.shape[2])
+        check(lib().kgk_scene_create(_p(tris), len(tris), _p(mats), len(mats),
+                                     ctypes.cast(tex_arr, ctypes.c_void_p) if tex_arr else None, ntex,
+                                     ctypes.byref(hdr) if hdr is not None else None,
+                                     ctypes.byref(self._h)))
+        self.n_triangles = len(tris)
+        self.bvh = None
+
+    def close(self):
+        if self._h:
+            lib().kgk_scene_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def build_bvh(self):
+        info = KgkBvhInfo()
+        check(lib().kgk_build_bvh(self._h, ctypes.byref(info)))
+        self.bvh = {k: getattr(info, k) for k, _ in KgkBvhInfo._fields_}
+        return self.bvh
+
+    def validate_bvh(self):
+        check(lib().kgk_bvh_validate(self._h))
+
+    def trace_closest(self, rays, with_stats=False):
+        rays = _as(rays, RAY)
+        n = len(rays)
+        ids = np.empty(n, np.int32)
+        t = np.empty(n, np.float32)
+        st = KgkStats()
+        check(lib().kgk_trace_closest(self._h, _p(rays), n, _p(ids), _p(t), ctypes.byref(st)))
+        return (ids, t, stats_dict(st)) if with_stats else (ids, t)
+
+    def trace_any(self, rays, t_max=None):
+        rays = _as(rays, RAY)
+        n = len(rays)
+        occ = np.empty(n, np.uint8)
+        tm = _as(t_max, np.float32) if t_max is not None else None
+        check(lib().kgk_trace_any(self._h, _p(rays), _p(tm), n, _p(occ), None))
+        return occ
+
+    def render(self, cam, width, height, spp=1, max_depth=0, rr_start_depth=3,
+               estimator=ESTIMATOR_COMPAT, seed=1, frame_index=0, accumulate=False,
+               count_work=False, write_gbuffer=False, use_cache=False, wave_paths=0, prev_cam=None,
+               out=None):
+        cfg = KgkRenderConfig(width=width, height=height, spp=spp, max_depth=max_depth,
+                              rr_start_depth=rr_start_depth, estimator=estimator, seed=seed,
+                              frame_index=frame_index, accumulate=int(accumulate),
+                              wave_paths=wave_paths, count_work=int(count_work),
+                              write_gbuffer=int(write_gbuffer), use_cache=int(use_cache))
+        if out is None:
+            out = np.empty((height, width, 4), np.float32)
+        st = KgkStats()
+        check(lib().kgk_render(self._h, ctypes.byref(cam),
+                               ctypes.byref(prev_cam) if prev_cam is not None else None,
+                               ctypes.byref(cfg), _p(out), ctypes.byref(st)))
+        return out, stats_dict(st)
+
+    def accum_reset(self, width, height):
+        check(lib().kgk_accum_reset(self._h, width, height))
+
+    def accum_read(self, width, height):
+        mean = np.empty((height, width, 3), np.float64)
+        var = np.empty((height, width, 3), np.float64)
+        n = ctypes.c_uint64()
+        check(lib().kgk_accum_read(self._h, _p(mean), _p(var), ctypes.byref(n)))
+        return mean, var, n.value
+
+
+def camera_setup(origin, dist, rot, image_height):
+    """Camera_SetUpCamera (struct_Camera.cuh:27-35), PixelSize = 36/height."""
+    cam = KgkCamera()
+    o = KgkVec(float(origin[0]), float(origin[1]), float(origin[2]), 0.0)
+    check(lib().kgk_camera_setup(o, float(dist), float(rot[0]), float(rot[1]), float(rot[2]),
+                                 int(image_height), ctypes.byref(cam)))
+    return cam
+
+
+def camera_array(cam):
+    return np.frombuffer(bytes(cam), dtype=np.float32).copy()
+
+
+def tonemap(img):
+    img = np.ascontiguousarray(img, np.float32)
+    h, w = img.shape[:2]
+    out = np.empty((h, w, 4), np.uint8)
+    check(lib().kgk_tonemap_rgba8(_p(img), w, h, _p(out)))
+    return out
+
+
+def save_png(img, path):
+    img = np.ascontiguousarray(img, np.float32)
+    h, w = img.shape[:2]
+    check(lib().kgk_save_png(_p(img), w, h, path.encode()))

@@ -1,0 +1,126 @@
+// image_io.cpp - tone mapping and PNG output (replaces save_png,
+// FileIO/IO_save_png.cuh:7-56).  The PNG encoder writes stored (uncompressed)
+// deflate blocks, so the library needs no zlib.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "kgk_scene.h"
+
+using namespace kgk;
+
+namespace {
+
+uint32_t crc_table[256];
+bool crc_ready = false;
+
+void crc_init() {
+    for (uint32_t n = 0; n < 256; ++n) {
+        uint32_t c = n;
+        for (int k = 0; k < 8; ++k) c = (c & 1) ? 0xedb88320u ^ (c >> 1) : c >> 1;
+        crc_table[n] = c;
+    }
+    crc_ready = true;
+}
+
+uint32_t crc32(const uint8_t *p, size_t n, uint32_t c = 0xffffffffu) {
+    for (size_t i = 0; i < n; ++i) c = crc_table[(c ^ p[i]) & 0xff] ^ (c >> 8);
+    return c;
+}
+
+void put32(std::vector<uint8_t> &v, uint32_t x) {
+    v.push_back((uint8_t)(x >> 24));
+    v.push_back((uint8_t)(x >> 16));
+    v.push_back((uint8_t)(x >> 8));
+    v.push_back((uint8_t)x);
+}
+
+void chunk(std::vector<uint8_t> &out, const char *type, const std::vector<uint8_t> &data) {
+    put32(out, (uint32_t)data.size());
+    size_t start = out.size();
+    out.insert(out.end(), type, type + 4);
+    out.insert(out.end(), data.begin(), data.end());
+    put32(out, crc32(&out[start], out.size() - start) ^ 0xffffffffu);
+}
+
+// gamma 1/2.2 -> clamp [0,1] -> x255 truncated (IO_save_png.cuh:26,7,47-52)
+inline uint8_t tone(float x) {
+    float g = powf(x, 1 / 2.2f);
+    g = g < 0.0f ? 0.0f : (g > 1.0f ? 1.0f : g);
+    return (uint8_t)(g * 255);
+}
+
+}  // namespace
+
+extern "C" {
+
+kgk_status kgk_tonemap_rgba8(const kgk_vec *img, int32_t w, int32_t h, uint8_t *out) {
+    if (!img || !out) return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_tonemap_rgba8: NULL buffer");
+    if (w <= 0 || h <= 0) return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_tonemap_rgba8: empty image");
+    const size_t npx = (size_t)w * h;
+    std::vector<kgk_vec> host;
+    const kgk_vec *src = img;
+    if (is_device_ptr(img)) {
+        host.resize(npx);
+        KGK_CUDA(cudaMemcpy(host.data(), img, npx * sizeof(kgk_vec), cudaMemcpyDeviceToHost));
+        src = host.data();
+    }
+    for (size_t i = 0; i < npx; ++i) {
+        out[4 * i] = tone(src[i].x);
+        out[4 * i + 1] = tone(src[i].y);
+        out[4 * i + 2] = tone(src[i].z);
+        out[4 * i + 3] = 255;
+    }
+    return KGK_OK;
+}
+
+kgk_status kgk_save_png(const kgk_vec *img, int32_t w, int32_t h, const char *path) {
+    if (!path) return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_save_png: path == NULL");
+    if (w <= 0 || h <= 0) return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_save_png: empty image");
+    std::vector<uint8_t> rgba((size_t)w * h * 4);
+    KGK_TRY(kgk_tonemap_rgba8(img, w, h, rgba.data()));
+    if (!crc_ready) crc_init();
+    std::vector<uint8_t> raw;
+    raw.reserve((size_t)h * (4 * (size_t)w + 1));
+    for (int y = 0; y < h; ++y) {
+        raw.push_back(0);  // filter: none
+        raw.insert(raw.end(), rgba.begin() + (size_t)y * w * 4, rgba.begin() + (size_t)(y + 1) * w * 4);
+    }
+    std::vector<uint8_t> z = {0x78, 0x01};
+    uint32_t a = 1, b = 0;
+    for (uint8_t c : raw) {
+        a = (a + c) % 65521u;
+        b = (b + a) % 65521u;
+    }
+    size_t pos = 0;
+    do {
+        size_t len = std::min<size_t>(65535, raw.size() - pos);
+        bool last = pos + len == raw.size();
+        z.push_back(last ? 1 : 0);
+        z.push_back((uint8_t)(len & 0xff));
+        z.push_back((uint8_t)(len >> 8));
+        z.push_back((uint8_t)(~len & 0xff));
+        z.push_back((uint8_t)((~len >> 8) & 0xff));
+        z.insert(z.end(), raw.begin() + pos, raw.begin() + pos + len);
+        pos += len;
+    } while (pos < raw.size());
+    put32(z, (b << 16) | a);
+    std::vector<uint8_t> png = {0x89, 'P', 'N', 'G', '\r', '\n', 0x1a, '\n'};
+    std::vector<uint8_t> ihdr;
+    put32(ihdr, (uint32_t)w);
+    put32(ihdr, (uint32_t)h);
+    ihdr.insert(ihdr.end(), {8, 6, 0, 0, 0});
+    chunk(png, "IHDR", ihdr);
+    chunk(png, "IDAT", z);
+    chunk(png, "IEND", {});
+    FILE *f = fopen(path, "wb");
+    if (!f) return fail(KGK_ERR_IO, std::string("kgk_save_png: cannot open ") + path);
+    size_t wr = fwrite(png.data(), 1, png.size(), f);
+    int cl = fclose(f);
+    if (wr != png.size() || cl != 0) return fail(KGK_ERR_IO, std::string("kgk_save_png: write failed for ") + path);
+    return KGK_OK;
+}
+
+}  // extern "C"

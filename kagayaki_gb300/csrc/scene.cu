@@ -1,0 +1,242 @@
+// scene.cu - scene upload: triangle/material/texture/environment data into
+// the device layout of kgk_internal.h, plus the light and environment CDFs.
+//
+// Replaces render_prepare (render_prepare.cuh:33-51) and the uploads of
+// main.cu:110-175.  The reference-estimator CDFs are the reference's own
+// sequential FP32 running sums (NextEventEstimation_FaceLight.cuh:8-21,
+// ImageBasedLighting.cuh:59-73) computed on the host in input order; this file
+// is compiled with -ffp-contract=off so the sums round the same way on every
+// host.  The unbiased estimator gets normalised CDFs accumulated in double.
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "kgk_device.cuh"
+#include "kgk_internal.h"
+
+namespace kgk {
+namespace {
+
+struct HV {
+    float x, y, z;
+};
+inline HV hv(const kgk_vec &v) { return {v.x, v.y, v.z}; }
+inline HV sub(HV a, HV b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+inline HV crs(HV a, HV b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
+inline float hlen(HV a) { return sqrtf(a.x * a.x + a.y * a.y + a.z * a.z); }
+
+// Triangle::area (struct_Triangle.cuh:106-108).
+inline float tri_area(const kgk_triangle &t) {
+    return 0.5f * hlen(crs(sub(hv(t.v1), hv(t.v0)), sub(hv(t.v2), hv(t.v0))));
+}
+
+bool is_device_ptr(const void *p) {
+    if (!p) return false;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+template <class T> kgk_status to_host(const T *p, size_t n, std::vector<T> &out) {
+    out.resize(n);
+    if (is_device_ptr(p)) {
+        KGK_CUDA(cudaMemcpy(out.data(), p, n * sizeof(T), cudaMemcpyDeviceToHost));
+    } else {
+        memcpy(out.data(), p, n * sizeof(T));
+    }
+    return KGK_OK;
+}
+
+template <class T> kgk_status upload(T **dst, const T *src, size_t n, const char *what, cudaStream_t st) {
+    KGK_TRY(dalloc(dst, n > 0 ? n : 1, what));
+    if (n > 0) KGK_CUDA(cudaMemcpyAsync(*dst, src, n * sizeof(T), cudaMemcpyHostToDevice, st));
+    return KGK_OK;
+}
+
+}  // namespace
+
+kgk_status scene_upload(DevScene &s, const kgk_triangle *tris_in, size_t n, const kgk_material *mats_in,
+                        size_t nm, const kgk_texture *tex, size_t ntex, const kgk_texture *hdr,
+                        cudaStream_t st) {
+    if (!tris_in || n == 0) return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_scene_create: no triangles");
+    if (!mats_in || nm == 0) return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_scene_create: no materials");
+    if (n > (size_t)600000000) return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_scene_create: too many triangles");
+    if (ntex > 0 && !tex) return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_scene_create: textures == NULL");
+    std::vector<kgk_triangle> tris;
+    std::vector<kgk_material> mats;
+    KGK_TRY(to_host(tris_in, n, tris));
+    KGK_TRY(to_host(mats_in, nm, mats));
+    for (size_t i = 0; i < n; ++i)
+        if (tris[i].material_id < 0 || (size_t)tris[i].material_id >= nm)
+            return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_scene_create: triangle " + std::to_string(i) +
+                                                      " has material_id " + std::to_string(tris[i].material_id) +
+                                                      " outside [0, " + std::to_string(nm) + ")");
+    for (size_t i = 0; i < nm; ++i)
+        if (mats[i].TEXTURE_BASECOLOR_ID >= (int)ntex || mats[i].TEXTURE_BASECOLOR_ID < -1)
+            return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_scene_create: material " + std::to_string(i) +
+                                                      " names a missing texture");
+
+    s.n_tris = (int32_t)n;
+    s.n_mats = (int32_t)nm;
+    // vertices and attributes
+    {
+        std::vector<float4> verts(3 * n), attr(4 * n);
+        for (size_t i = 0; i < n; ++i) {
+            const kgk_triangle &t = tris[i];
+            verts[3 * i] = make_float4(t.v0.x, t.v0.y, t.v0.z, 0.0f);
+            verts[3 * i + 1] = make_float4(t.v1.x, t.v1.y, t.v1.z, 0.0f);
+            verts[3 * i + 2] = make_float4(t.v2.x, t.v2.y, t.v2.z, 0.0f);
+            unsigned bits = ((unsigned)t.material_id & 0x7fffffffu) | (t.is_SmoothNormal ? 0x80000000u : 0u);
+            float fb;
+            memcpy(&fb, &bits, 4);
+            attr[4 * i] = make_float4(t.v0_vn.x, t.v0_vn.y, t.v0_vn.z, t.v0_vt.x);
+            attr[4 * i + 1] = make_float4(t.v1_vn.x, t.v1_vn.y, t.v1_vn.z, t.v0_vt.y);
+            attr[4 * i + 2] = make_float4(t.v2_vn.x, t.v2_vn.y, t.v2_vn.z, t.v1_vt.x);
+            attr[4 * i + 3] = make_float4(t.v1_vt.y, t.v2_vt.x, t.v2_vt.y, fb);
+        }
+        KGK_TRY(upload(&s.verts, verts.data(), verts.size(), "triangle vertices", st));
+        KGK_TRY(upload(&s.attr, attr.data(), attr.size(), "triangle attributes", st));
+        KGK_CUDA(cudaStreamSynchronize(st));
+    }
+    KGK_TRY(upload(&s.mats, mats.data(), nm, "materials", st));
+
+    // face lights: the reference's running FP32 sum (calculate_Lss)
+    {
+        std::vector<float> cdf(n);
+        std::vector<int32_t> ids;
+        std::vector<double> w;
+        auto emis_len = [&](int m) { return hlen(hv(mats[m].emission)); };
+        cdf[0] = tri_area(tris[0]) * emis_len(tris[0].material_id);
+        for (size_t i = 1; i < n; ++i) cdf[i] = cdf[i - 1] + tri_area(tris[i]) * emis_len(tris[i].material_id);
+        s.no_light = cdf[n - 1] == 0.0f ? 1 : 0;
+        KGK_TRY(upload(&s.light_cdf_ref, cdf.data(), n, "light CDF", st));
+        double total = 0.0;
+        for (size_t i = 0; i < n; ++i) {
+            double wi = (double)tri_area(tris[i]) * (double)emis_len(tris[i].material_id);
+            if (wi > 0.0) {
+                ids.push_back((int32_t)i);
+                w.push_back(wi);
+                total += wi;
+            }
+        }
+        s.n_emit = (int32_t)ids.size();
+        s.emit_total = (float)total;
+        std::vector<float> ecdf(ids.size() + 1);
+        double acc = 0.0;
+        ecdf[0] = 0.0f;
+        for (size_t k = 0; k < ids.size(); ++k) {
+            acc += w[k];
+            ecdf[k + 1] = (float)(acc / total);
+        }
+        if (!ids.empty()) ecdf.back() = 1.0f;
+        KGK_TRY(upload(&s.emit_ids, ids.data(), ids.size(), "emitter list", st));
+        KGK_TRY(upload(&s.emit_cdf, ecdf.data(), ecdf.size(), "emitter CDF", st));
+        KGK_CUDA(cudaStreamSynchronize(st));
+    }
+
+    // textures
+    if (ntex > 0) {
+        std::vector<kgk_texture> th;
+        KGK_TRY(to_host(tex, ntex, th));
+        std::vector<TexDesc> desc(ntex);
+        size_t total = 0;
+        for (size_t i = 0; i < ntex; ++i) {
+            if (!th[i].pixels || th[i].width <= 0 || th[i].height <= 0 || th[i].bpp < 3)
+                return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_scene_create: texture " + std::to_string(i) +
+                                                          " needs pixels, a size and >= 3 channels");
+            desc[i].offset = (int64_t)total;
+            desc[i].w = th[i].width;
+            desc[i].h = th[i].height;
+            desc[i].bpp = th[i].bpp;
+            total += (size_t)th[i].width * th[i].height * th[i].bpp;
+        }
+        KGK_TRY(dalloc(&s.tex_pixels, total, "texture pixels"));
+        for (size_t i = 0; i < ntex; ++i) {
+            size_t cnt = (size_t)th[i].width * th[i].height * th[i].bpp;
+            KGK_CUDA(cudaMemcpy(s.tex_pixels + desc[i].offset, th[i].pixels, cnt * sizeof(float),
+                                is_device_ptr(th[i].pixels) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice));
+        }
+        KGK_TRY(upload(&s.tex, desc.data(), ntex, "texture table", st));
+        s.n_tex = (int32_t)ntex;
+    }
+
+    // environment
+    if (hdr && hdr->pixels) {
+        const int w = hdr->width, h = hdr->height, bpp = hdr->bpp;
+        if (w <= 0 || h <= 0 || bpp < 3) return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_scene_create: bad HDR size");
+        const size_t npx = (size_t)w * h;
+        std::vector<float> px;
+        KGK_TRY(to_host(hdr->pixels, npx * bpp, px));
+        KGK_TRY(upload(&s.env, px.data(), px.size(), "environment", st));
+        s.env_w = w;
+        s.env_h = h;
+        s.env_bpp = bpp;
+        // reference running sum (calculate_Lss_HDR)
+        const float PIH = 3.14159265358979323846263383f;
+        std::vector<float> cdf(npx);
+        float v = 1.0f;
+        cdf[0] = hlen({px[0], px[1], px[2]}) * cosf((v - 0.5f) * PIH);
+        for (size_t i = 1; i < npx; ++i) {
+            v = 1.0f - (float)(int)(i / (size_t)w) / (float)h;
+            cdf[i] = cdf[i - 1] + hlen({px[bpp * i], px[bpp * i + 1], px[bpp * i + 2]}) * cosf((v - 0.5f) * PIH);
+        }
+        KGK_TRY(upload(&s.env_cdf_ref, cdf.data(), npx, "environment CDF", st));
+        // unbiased: texel weight = |rgb| * cos(latitude of the row centre)
+        std::vector<double> roww(h, 0.0);
+        std::vector<float> col((size_t)(w + 1) * h);
+        std::vector<float> row(h + 1);
+        double total = 0.0;
+        for (int r = 0; r < h; ++r) {
+            const double lat = (0.5 - (r + 0.5) / h) * M_PI;
+            const double c = cos(lat);
+            double acc = 0.0;
+            col[(size_t)r * (w + 1)] = 0.0f;
+            std::vector<double> tmp(w);
+            for (int x = 0; x < w; ++x) {
+                const float *p = &px[((size_t)r * w + x) * bpp];
+                double l = sqrt((double)p[0] * p[0] + (double)p[1] * p[1] + (double)p[2] * p[2]);
+                acc += l * c + 1e-30;
+                tmp[x] = acc;
+            }
+            for (int x = 0; x < w; ++x) col[(size_t)r * (w + 1) + x + 1] = (float)(tmp[x] / acc);
+            col[(size_t)r * (w + 1) + w] = 1.0f;
+            roww[r] = acc;
+            total += acc;
+        }
+        double acc = 0.0;
+        row[0] = 0.0f;
+        for (int r = 0; r < h; ++r) {
+            acc += roww[r];
+            row[r + 1] = (float)(acc / total);
+        }
+        row[h] = 1.0f;
+        s.env_total = (float)total;
+        KGK_TRY(upload(&s.env_row_cdf, row.data(), row.size(), "environment row CDF", st));
+        KGK_TRY(upload(&s.env_col_cdf, col.data(), col.size(), "environment column CDF", st));
+        KGK_CUDA(cudaStreamSynchronize(st));
+    }
+    return KGK_OK;
+}
+
+void scene_free(DevScene &s) {
+    dfree(s.tri_rec);
+    dfree(s.verts);
+    dfree(s.attr);
+    dfree(s.mats);
+    dfree(s.tex_pixels);
+    dfree(s.tex);
+    dfree(s.env);
+    dfree(s.env_cdf_ref);
+    dfree(s.env_row_cdf);
+    dfree(s.env_col_cdf);
+    dfree(s.light_cdf_ref);
+    dfree(s.emit_ids);
+    dfree(s.emit_cdf);
+    dfree(s.nodes);
+    s = DevScene();
+}
+
+}  // namespace kgk

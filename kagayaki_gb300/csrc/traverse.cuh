@@ -1,0 +1,255 @@
+// traverse.cuh - closest-hit and occlusion traversal of the 8-wide
+// compressed BVH with watertight FP32 ray/triangle intersection.
+// Replaces willIntersectWithTriangle_nonRecursive (ConstructBVH.cuh:286-368)
+// and Triangle::intersectTest (struct_Triangle.cuh:30-79) on the device.
+//
+// Semantics kept from the reference: a hit needs t >= 1e-5 (double compare,
+// struct_Triangle.cuh:57) and the result is the closest hit.  Where the
+// reference resolves equal distances by its traversal order, this resolves
+// them to the smaller triangle id, independent of the tree.
+// Differences by design: the test is watertight (Woop, Benthin, Wald 2013)
+// instead of Cramer's rule, and node culling uses the ray's [tmin, tmax]
+// interval (closest-hit pruning) instead of the whole line.
+#pragma once
+
+#include "kgk_device.cuh"
+#include "kgk_internal.h"
+
+namespace kgk {
+
+constexpr int kTravStack = 32;
+// Conservative widening of box exit distances: 1 + 2 * gamma(3) covers the
+// rounding of the quantised plane, the origin offset and the multiply.
+constexpr float kBoxWiden = 1.0000004f;
+
+struct RayPre {
+    float3 o, d, inv;
+    float sx, sy, sz;
+    int kx, ky, kz;
+    unsigned oct_inv4;
+};
+
+__device__ __forceinline__ float safe_inv(float d) {
+    // |d| < 1e-20 -> +-1e20 so that scale * inv never forms 0 * inf
+    float a = fabsf(d) < 1e-20f ? copysignf(1e-20f, d) : d;
+    return 1.0f / a;
+}
+
+__device__ __forceinline__ RayPre make_ray(float3 o, float3 d) {
+    RayPre r;
+    r.o = o;
+    r.d = d;
+    r.inv = f3(safe_inv(d.x), safe_inv(d.y), safe_inv(d.z));
+    const float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
+    int kz = ax > ay ? (ax > az ? 0 : 2) : (ay > az ? 1 : 2);
+    int kx = kz == 2 ? 0 : kz + 1;
+    int ky = kx == 2 ? 0 : kx + 1;
+    if (comp(d, kz) < 0.0f) { int t = kx; kx = ky; ky = t; }
+    r.kx = kx;
+    r.ky = ky;
+    r.kz = kz;
+    const float dz = comp(d, kz);
+    r.sx = comp(d, kx) / dz;
+    r.sy = comp(d, ky) / dz;
+    r.sz = 1.0f / dz;
+    unsigned oct = (d.x < 0.0f ? 4u : 0u) | (d.y < 0.0f ? 2u : 0u) | (d.z < 0.0f ? 1u : 0u);
+    r.oct_inv4 = (7u - oct) * 0x01010101u;
+    return r;
+}
+
+// Watertight test.  On a hit returns true with t, b1 (weight of v1) and b2
+// (weight of v2).  The 2D edge functions are formed with explicit
+// round-to-nearest multiplies and subtractions (no FMA contraction), so the
+// two triangles sharing an edge compute exactly negated values.
+__device__ __forceinline__ bool tri_intersect(const RayPre &r, float4 a4, float4 b4, float4 c4,
+                                              float *t, float *b1, float *b2) {
+    const float3 A = f3(a4) - r.o, B = f3(b4) - r.o, C = f3(c4) - r.o;
+    const float Akz = comp(A, r.kz), Bkz = comp(B, r.kz), Ckz = comp(C, r.kz);
+    const float Ax = comp(A, r.kx) - r.sx * Akz, Ay = comp(A, r.ky) - r.sy * Akz;
+    const float Bx = comp(B, r.kx) - r.sx * Bkz, By = comp(B, r.ky) - r.sy * Bkz;
+    const float Cx = comp(C, r.kx) - r.sx * Ckz, Cy = comp(C, r.ky) - r.sy * Ckz;
+    const float U = __fsub_rn(__fmul_rn(Cx, By), __fmul_rn(Cy, Bx));
+    const float V = __fsub_rn(__fmul_rn(Ax, Cy), __fmul_rn(Ay, Cx));
+    const float W = __fsub_rn(__fmul_rn(Bx, Ay), __fmul_rn(By, Ax));
+    if ((U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f)) return false;
+    const float det = U + V + W;
+    if (det == 0.0f) return false;
+    const float T = U * (r.sz * Akz) + V * (r.sz * Bkz) + W * (r.sz * Ckz);
+    const float tt = T / det;
+    if (!(tt >= kTMin)) return false;  // also rejects NaN
+    *t = tt;
+    *b1 = V / det;
+    *b2 = W / det;
+    return true;
+}
+
+__device__ __forceinline__ unsigned byte_of(unsigned x, int i) { return (x >> (i * 8)) & 0xffu; }
+__device__ __forceinline__ unsigned sign_extend_s8x4(unsigned x) { return ((x >> 7) & 0x01010101u) * 0xffu; }
+
+// Child hit mask of one compressed node: bits 24..31 = inner children
+// (octant-permuted slots), bits 0..23 = triangles of hit leaf children.
+__device__ __forceinline__ unsigned node_intersect(const RayPre &r, float tmin, float tmax,
+                                                   const float4 n0, const float4 n1, const float4 n2,
+                                                   const float4 n3, const float4 n4) {
+    const unsigned e = __float_as_uint(n0.w);
+    const float adx = __uint_as_float((e & 0xffu) << 23) * r.inv.x;
+    const float ady = __uint_as_float(((e >> 8) & 0xffu) << 23) * r.inv.y;
+    const float adz = __uint_as_float(((e >> 16) & 0xffu) << 23) * r.inv.z;
+    const float ox = (n0.x - r.o.x) * r.inv.x;
+    const float oy = (n0.y - r.o.y) * r.inv.y;
+    const float oz = (n0.z - r.o.z) * r.inv.z;
+    const float tm = tmax * kBoxWiden;
+    unsigned hits = 0;
+#pragma unroll
+    for (int half = 0; half < 2; ++half) {
+        const unsigned meta4 = __float_as_uint(half ? n1.w : n1.z);
+        const unsigned is_inner4 = (meta4 & (meta4 << 1)) & 0x10101010u;
+        const unsigned inner_mask4 = sign_extend_s8x4(is_inner4 << 3);
+        const unsigned bit_index4 = (meta4 ^ (r.oct_inv4 & inner_mask4)) & 0x1f1f1f1fu;
+        const unsigned child_bits4 = (meta4 >> 5) & 0x07070707u;
+        const unsigned qlx = __float_as_uint(half ? n2.y : n2.x), qhx = __float_as_uint(half ? n2.w : n2.z);
+        const unsigned qly = __float_as_uint(half ? n3.y : n3.x), qhy = __float_as_uint(half ? n3.w : n3.z);
+        const unsigned qlz = __float_as_uint(half ? n4.y : n4.x), qhz = __float_as_uint(half ? n4.w : n4.z);
+        const unsigned xn = r.d.x < 0.0f ? qhx : qlx, xf = r.d.x < 0.0f ? qlx : qhx;
+        const unsigned yn = r.d.y < 0.0f ? qhy : qly, yf = r.d.y < 0.0f ? qly : qhy;
+        const unsigned zn = r.d.z < 0.0f ? qhz : qlz, zf = r.d.z < 0.0f ? qlz : qhz;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const float t0x = (float)byte_of(xn, j) * adx + ox;
+            const float t0y = (float)byte_of(yn, j) * ady + oy;
+            const float t0z = (float)byte_of(zn, j) * adz + oz;
+            const float t1x = (float)byte_of(xf, j) * adx + ox;
+            const float t1y = (float)byte_of(yf, j) * ady + oy;
+            const float t1z = (float)byte_of(zf, j) * adz + oz;
+            const float lo = fmaxf(fmaxf(t0x, t0y), fmaxf(t0z, tmin));
+            const float hi = fminf(fminf(t1x, t1y), fminf(t1z, tm)) * kBoxWiden;
+            if (lo <= hi) hits |= byte_of(child_bits4, j) << byte_of(bit_index4, j);
+        }
+    }
+    return hits;
+}
+
+struct TravStats {
+    unsigned nodes, tris, overflow;
+};
+
+// Closest hit.  best_t in: search limit (exclusive of farther hits); out: hit
+// distance.  Returns the BVH-order triangle index of the hit or -1.
+// Both traversals check every node and triangle index against the buffer
+// sizes; a bad index sets st.overflow = 2 and ends the traversal instead of
+// reading out of range.
+template <bool kCount>
+__device__ __forceinline__ int trace_closest(const WideNode *__restrict__ nodes, unsigned n_nodes,
+                                             const float4 *__restrict__ tri, unsigned n_tris,
+                                             const RayPre &r, float &best_t, int &best_id, float &bu,
+                                             float &bv, TravStats &st) {
+    uint2 stack[kTravStack];
+    int sp = 0;
+    int hit_slot = -1;
+    uint2 group = make_uint2(0u, 0x80000000u);
+    while (true) {
+        uint2 tg = make_uint2(0u, 0u);
+        if (group.y & 0xff000000u) {
+            const unsigned hits_imask = group.y;
+            const int child_bit = 31 - __clz(hits_imask & 0xff000000u);
+            const unsigned base = group.x;
+            group.y &= ~(1u << child_bit);
+            if (group.y & 0xff000000u) {
+                if (sp < kTravStack) stack[sp++] = group;
+                else st.overflow = 1;
+            }
+            const unsigned slot = (unsigned)(child_bit - 24) ^ (r.oct_inv4 & 0xffu);
+            const unsigned rel = __popc(hits_imask & ~(0xffffffffu << slot));
+            if (base + rel >= n_nodes) { st.overflow = 2; break; }
+            const WideNode *nd = nodes + base + rel;
+            const float4 n0 = __ldg(&nd->n0), n1 = __ldg(&nd->n1), n2 = __ldg(&nd->n2),
+                         n3 = __ldg(&nd->n3), n4 = __ldg(&nd->n4);
+            if (kCount) ++st.nodes;
+            const unsigned hm = node_intersect(r, 0.0f, best_t, n0, n1, n2, n3, n4);
+            const unsigned imask = __float_as_uint(n0.w) >> 24;
+            group = make_uint2(__float_as_uint(n1.x), (hm & 0xff000000u) | imask);
+            tg = make_uint2(__float_as_uint(n1.y), hm & 0x00ffffffu);
+        } else {
+            tg = group;
+            group = make_uint2(0u, 0u);
+        }
+        while (tg.y != 0u) {
+            const int k = __ffs(tg.y) - 1;
+            tg.y &= tg.y - 1u;
+            const int ti = (int)tg.x + k;
+            if ((unsigned)ti >= n_tris) { st.overflow = 2; tg.y = 0u; group = make_uint2(0u, 0u); sp = 0; break; }
+            const float4 a = __ldg(&tri[3 * ti]), b = __ldg(&tri[3 * ti + 1]), c = __ldg(&tri[3 * ti + 2]);
+            if (kCount) ++st.tris;
+            float t, u, v;
+            if (tri_intersect(r, a, b, c, &t, &u, &v)) {
+                const int id = __float_as_int(a.w);
+                if (t < best_t || (t == best_t && id < best_id)) {
+                    best_t = t;
+                    best_id = id;
+                    bu = u;
+                    bv = v;
+                    hit_slot = ti;
+                }
+            }
+        }
+        if ((group.y & 0xff000000u) == 0u) {
+            if (sp == 0) break;
+            group = stack[--sp];
+        }
+    }
+    return hit_slot;
+}
+
+// Occlusion: true when any triangle lies at kTMin <= t < tmax.
+template <bool kCount>
+__device__ __forceinline__ bool trace_any(const WideNode *__restrict__ nodes, unsigned n_nodes,
+                                          const float4 *__restrict__ tri, unsigned n_tris,
+                                          const RayPre &r, float tmax, TravStats &st) {
+    uint2 stack[kTravStack];
+    int sp = 0;
+    uint2 group = make_uint2(0u, 0x80000000u);
+    while (true) {
+        uint2 tg = make_uint2(0u, 0u);
+        if (group.y & 0xff000000u) {
+            const unsigned hits_imask = group.y;
+            const int child_bit = 31 - __clz(hits_imask & 0xff000000u);
+            const unsigned base = group.x;
+            group.y &= ~(1u << child_bit);
+            if (group.y & 0xff000000u) {
+                if (sp < kTravStack) stack[sp++] = group;
+                else st.overflow = 1;
+            }
+            const unsigned slot = (unsigned)(child_bit - 24) ^ (r.oct_inv4 & 0xffu);
+            const unsigned rel = __popc(hits_imask & ~(0xffffffffu << slot));
+            if (base + rel >= n_nodes) { st.overflow = 2; break; }
+            const WideNode *nd = nodes + base + rel;
+            const float4 n0 = __ldg(&nd->n0), n1 = __ldg(&nd->n1), n2 = __ldg(&nd->n2),
+                         n3 = __ldg(&nd->n3), n4 = __ldg(&nd->n4);
+            if (kCount) ++st.nodes;
+            const unsigned hm = node_intersect(r, 0.0f, tmax, n0, n1, n2, n3, n4);
+            const unsigned imask = __float_as_uint(n0.w) >> 24;
+            group = make_uint2(__float_as_uint(n1.x), (hm & 0xff000000u) | imask);
+            tg = make_uint2(__float_as_uint(n1.y), hm & 0x00ffffffu);
+        } else {
+            tg = group;
+            group = make_uint2(0u, 0u);
+        }
+        while (tg.y != 0u) {
+            const int k = __ffs(tg.y) - 1;
+            tg.y &= tg.y - 1u;
+            const int ti = (int)tg.x + k;
+            if ((unsigned)ti >= n_tris) { st.overflow = 2; tg.y = 0u; group = make_uint2(0u, 0u); sp = 0; break; }
+            const float4 a = __ldg(&tri[3 * ti]), b = __ldg(&tri[3 * ti + 1]), c = __ldg(&tri[3 * ti + 2]);
+            if (kCount) ++st.tris;
+            float t, u, v;
+            if (tri_intersect(r, a, b, c, &t, &u, &v) && t < tmax) return true;
+        }
+        if ((group.y & 0xff000000u) == 0u) {
+            if (sp == 0) break;
+            group = stack[--sp];
+        }
+    }
+    return false;
+}
+
+}  // namespace kgk

@@ -66,6 +66,15 @@ class CounterRng:
 # Triangle assembly helpers
 # --------------------------------------------------------------------------
 
+def canonical(tris):
+    """Copy of TRIANGLE records with the C padding bytes zeroed (numpy copies
+    may leave arbitrary bytes there), so byte digests are reproducible."""
+    out = np.zeros(len(tris), dtype=TRIANGLE)
+    for f in TRIANGLE.names:
+        out[f] = tris[f]
+    return out
+
+
 def _tris_from_indexed(pos, nrm, uv, faces, material_id, smooth, shape_id):
     """Indexed mesh -> TRIANGLE records (positions/normals/uvs per vertex)."""
     n = len(faces)
@@ -151,7 +160,7 @@ def cornell_box():
     ly = y1 - 1e-3
     parts.append(_quad((-1.25, ly, -1.25), (1.25, ly, -1.25), (1.25, ly, 1.25),
                        (-1.25, ly, 1.25), 3, 7))
-    tris = np.concatenate(parts)
+    tris = canonical(np.concatenate(parts))
     assert len(tris) == 36
     cam = dict(origin=(0.0173, 5.0131, 13.6), dist=28.0, rot=(0.0, 0.0, 0.0))
     return tris, mats, cam
@@ -274,7 +283,7 @@ def icosphere_field(n_meshes=64, subdiv=6, seed=2, box=20.0, amplitude=0.05,
                                         base_f, 1 + i, True, i))
     g = ground_half
     parts.append(_quad((-g, -g, 0.0), (g, -g, 0.0), (g, g, 0.0), (-g, g, 0.0), 0, n_meshes))
-    tris = np.concatenate(parts)
+    tris = canonical(np.concatenate(parts))
     info = dict(centers=np.stack([cx, cy, cz], 1), radii=radii,
                 lo=(-box / 2, -box / 2, 0.0), hi=(box / 2, box / 2, box))
     return tris, mats, info

@@ -1074,3 +1074,24 @@ int64_t orc_render_compat(const void *tris, int64_t n, const void *mats, int64_t
 /* Test hook: selects the argument order of SamplePointOnTriangle's random
  * numbers (1 = right to left, the host build's order). */
 void orc_set_point_arg_order(int rtl) { g_point_args_rtl = rtl; }
+
+/* evaluate_Disney_BRDF / _pdf for one material and n direction triples,
+ * parameters as RayTrace.cuh:85-92 (test hook mirroring ref_disney_eval). */
+void orc_disney_eval(const void *mat, int n, const float *wo, const float *wi, const float *nrm,
+                     float *brdf, float *pdf) {
+    const Mat *m = (const Mat *)mat;
+    DisneyP p;
+    disney_params(m, &p);
+    for (int i = 0; i < n; ++i) {
+        V o = mk(wo[3 * i], wo[3 * i + 1], wo[3 * i + 2]);
+        V in = mk(wi[3 * i], wi[3 * i + 1], wi[3 * i + 2]);
+        V N = mk(nrm[3 * i], nrm[3 * i + 1], nrm[3 * i + 2]);
+        V u, v, w;
+        onb(N, &u, &v, &w);
+        V b = disney_eval(p.wt, m, o, in, N, u, v, w, p.ax, p.ay, p.ac);
+        brdf[3 * i] = b.x;
+        brdf[3 * i + 1] = b.y;
+        brdf[3 * i + 2] = b.z;
+        pdf[i] = disney_pdf(p.wt, in, o, N, u, v, w, p.ax, p.ay, p.ac);
+    }
+}

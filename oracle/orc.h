@@ -72,6 +72,14 @@ int64_t orc_render_compat(const void *tris, int64_t n, const void *mats, int64_t
                           int hdr_h, int hdr_bpp, const void *cam, int width, int height,
                           int frames, int nthreads, float *out);
 
+/* evaluate_Disney_BRDF (outgoing = toward the light, incoming = toward the
+ * viewer) and evaluate_Disney_BRDF_pdf (Disney_BRDF.cuh:118-183). */
+void orc_disney_eval(const void *mat, int n, const float *wo, const float *wi, const float *nrm,
+                     float *brdf, float *pdf);
+/* Selects the argument order of SamplePointOnTriangle's two random numbers
+ * (1 = right to left, the reference host build's order). */
+void orc_set_point_arg_order(int rtl);
+
 #ifdef __cplusplus
 }
 #endif

@@ -58,6 +58,7 @@ def orc():
                                         _vp, _i32, _i32, _i32, _i32, _vp]
         L.orc_render_compat.restype = _i64
         L.orc_set_point_arg_order.argtypes = [_i32]
+        L.orc_disney_eval.argtypes = [_vp, _i32, _vp, _vp, _vp, _vp, _vp]
         _orc = L
     return _orc
 
@@ -92,6 +93,16 @@ def closest_bvh(tris, rays):
     finally:
         L.orc_bvh_free(b)
     return ids, t
+
+
+def disney_eval(mat, wo, wi, nrm):
+    n = len(wo)
+    brdf = np.empty((n, 3), np.float32)
+    pdf = np.empty(n, np.float32)
+    wo, wi, nrm = (np.ascontiguousarray(a, np.float32) for a in (wo, wi, nrm))
+    orc().orc_disney_eval(_ptr(np.ascontiguousarray(mat)), n, _ptr(wo), _ptr(wi), _ptr(nrm),
+                          _ptr(brdf), _ptr(pdf))
+    return brdf, pdf
 
 
 def camera_setup(org, dist, rot, image_height):

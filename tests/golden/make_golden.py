@@ -1,0 +1,135 @@
+"""Generates the golden fixtures in tests/golden/ by running the reference's
+own render-path source compiled for the host (oracle/_ref, built from the
+reference checkout by `make -C oracle ref`).  Run in a container that has the
+reference checkout:
+
+    python tests/golden/make_golden.py
+
+Fixtures:
+  c1_trace_ref.npz      reference closest hits of the 2^20 Cornell parity rays
+                        (ids for all rays, t for the first 2^16), ray digest
+  ico_trace_ref.npz     the same for a 2-icosphere scene (2,562 triangles)
+  c1_render_ref.npz     per-sample compat renders (render.cuh:21-49) of the
+                        Cornell box, 48x48, 8 chained frames, plus 256-frame
+                        mean/variance at 32x32
+  disney_ref.npz        evaluate_Disney_BRDF / _pdf on seeded directions
+  camera_ref.npz        Camera_SetUpCamera for a few poses
+  cdf_ref.npz           calculate_Lss / calculate_Lss_HDR for small inputs
+"""
+import hashlib
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from kagayaki_gb300 import scenes, structs  # noqa: E402
+from oracle import orc  # noqa: E402
+
+C1_LO, C1_HI = (-4.99, 0.01, -4.99), (4.99, 9.99, 4.99)
+
+
+def digest(a):
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def ico_scene():
+    tris, mats, info = scenes.icosphere_field(n_meshes=2, subdiv=3, seed=5, box=6.0)
+    return tris, mats, info
+
+
+def main():
+    orc.build(ref=True)
+    assert orc.ref_available(), "oracle/_ref was not built (needs the reference checkout)"
+
+    # --- closest hits, Cornell box ---
+    tris, mats, cam = scenes.cornell_box()
+    rays = scenes.parity_rays(1 << 20, C1_LO, C1_HI, seed=1)
+    ids, t, ok, nodes, _ = orc.ref_trace(tris, rays)
+    np.savez_compressed(os.path.join(HERE, "c1_trace_ref.npz"), ids=ids.astype(np.int8), ok=ok,
+                        t_head=t[:1 << 16], ray_digest=digest(rays), tri_digest=digest(tris),
+                        ref_nodes=nodes)
+
+    # --- closest hits, small displaced icospheres ---
+    it, im, info = ico_scene()
+    irays = scenes.parity_rays(1 << 16, info["lo"], info["hi"], seed=3)
+    iids, itt, iok, inodes, _ = orc.ref_trace(it, irays)
+    np.savez_compressed(os.path.join(HERE, "ico_trace_ref.npz"), ids=iids, t=itt, ok=iok,
+                        ray_digest=digest(irays), tri_digest=digest(it), ref_nodes=inodes)
+
+    # --- compat renders ---
+    W = H = 48
+    c = orc.camera_setup(cam["origin"], cam["dist"], cam["rot"], H)
+    frames, nrays = orc.ref_render(tris, mats, c, W, H, 8)
+    W2 = H2 = 32
+    c2 = orc.camera_setup(cam["origin"], cam["dist"], cam["rot"], H2)
+    many, nrays2 = orc.ref_render(tris, mats, c2, W2, H2, 256)
+    np.savez_compressed(os.path.join(HERE, "c1_render_ref.npz"), frames=frames, width=W, height=H,
+                        camera=c, rays=nrays, mean32=np.nanmean(many, axis=0),
+                        var32=np.nanvar(many, axis=0, ddof=1), n32=256, camera32=c2,
+                        rays32=nrays2)
+
+    # --- Disney BRDF ---
+    rng = scenes.CounterRng(11)
+    mlist, wo_l, wi_l, n_l, b_l, p_l = [], [], [], [], [], []
+    for k in range(8):
+        m = structs.make_material(structs.DISNEY, tuple(rng.uniform(3, 0.05, 0.95)),
+                                  metallic=float(rng.uniform(1)[0] < 0.3),
+                                  roughness=float(rng.uniform(1, 0.05, 1.0)[0]), specular=0.5,
+                                  clearcoat=float(rng.uniform(1)[0]),
+                                  subsurface=float(rng.uniform(1)[0] * (k % 2)),
+                                  sheen=float(rng.uniform(1)[0] * (k % 3 == 0)),
+                                  sheenTint=0.5, specularTint=0.3,
+                                  anisotropic=float(rng.uniform(1)[0] * (k % 2)),
+                                  cloearcoatGloss=float(rng.uniform(1)[0]))
+        n = 256
+        nrm = np.zeros((n, 3), np.float32)
+        nrm[:, 2] = 1.0
+        def hemi(count):
+            u1, u2 = rng.uniform(count), rng.uniform(count)
+            z = u1
+            r = np.sqrt(np.maximum(0, 1 - z * z))
+            return np.stack([r * np.cos(2 * np.pi * u2), r * np.sin(2 * np.pi * u2), z], 1).astype(np.float32)
+        wo, wi = hemi(n), hemi(n)
+        brdf = np.zeros((n, 3), np.float32)
+        pdf = np.zeros(n, np.float32)
+        L = orc.ref()
+        L.ref_disney_eval(m.ctypes.data, n, wo.ctypes.data, wi.ctypes.data, nrm.ctypes.data,
+                          brdf.ctypes.data, pdf.ctypes.data)
+        mlist.append(m)
+        wo_l.append(wo); wi_l.append(wi); n_l.append(nrm); b_l.append(brdf); p_l.append(pdf)
+    np.savez_compressed(os.path.join(HERE, "disney_ref.npz"), mats=np.stack(mlist), wo=np.stack(wo_l),
+                        wi=np.stack(wi_l), n=np.stack(n_l), brdf=np.stack(b_l), pdf=np.stack(p_l))
+
+    # --- camera ---
+    poses = [((15.8153, 0.908405, 0.704717), 28.0, (103.426, 0.0, 95.9501)),
+             ((0.0173, 5.0131, 13.6), 28.0, (0.0, 0.0, 0.0)),
+             ((25.0, 0.0, 5.0), 28.0, (90.0, 0.0, 90.0)),
+             ((-3.0, 7.0, 1.0), 35.0, (12.5, -40.0, 7.0))]
+    cams = []
+    for org, dist, rot in poses:
+        out = np.zeros(18, np.float32)
+        o = np.asarray(org, np.float32)
+        orc.ref().ref_camera_setup(o.ctypes.data, dist, rot[0], rot[1], rot[2], out.ctypes.data)
+        cams.append(out)
+    np.savez_compressed(os.path.join(HERE, "camera_ref.npz"),
+                        org=np.array([p[0] for p in poses], np.float32),
+                        dist=np.array([p[1] for p in poses], np.float32),
+                        rot=np.array([p[2] for p in poses], np.float32), cams=np.stack(cams))
+
+    # --- CDFs ---
+    lcdf = np.zeros(len(tris), np.float32)
+    orc.ref().ref_light_cdf(tris.ctypes.data, len(tris), mats.ctypes.data, len(mats), lcdf.ctypes.data)
+    env, _ = scenes.sky_environment(64, 32, sun_peak=100.0, seed=3)
+    env = np.ascontiguousarray(env)
+    ecdf = np.zeros(64 * 32, np.float32)
+    orc.ref().ref_env_cdf(env.ctypes.data, 64, 32, 3, ecdf.ctypes.data)
+    np.savez_compressed(os.path.join(HERE, "cdf_ref.npz"), light=lcdf, env=env, env_cdf=ecdf)
+    print("golden fixtures written to", HERE)
+
+
+if __name__ == "__main__":
+    main()
