@@ -1,0 +1,292 @@
+"""Benchmark: Mrays/s of the wavefront path tracer on the displaced-icosphere
+scene (64 icospheres x 81,920 triangles + ground = 5,242,882 triangles, Disney
+materials, 2048x1024 procedural HDR sky with importance-sampled sun), 1920x1080
+at 64 samples per pixel, max depth 16.  One step = one 64-spp frame.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+value: rays (closest + shadow) per second of device time, inputs resident.
+e2e:   the same through the C ABI with host buffers: the camera is read from
+       host memory and the frame is copied back to host memory every step.
+--impl reference: the reference's estimator restated on the host CPU (the
+       oracle port; the reference's own GPU renderer is not run, see the
+       design notes), timed on a bounded sample of the same workload with all
+       host threads.
+Inputs (BVH + triangles ~0.7 GB) exceed the 129 MB L2, so no flush is needed.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+WORKLOAD = dict(workload="displaced-icospheres-5.2M-disney-hdr", triangles=64 * 81920 + 2, width=1920,
+                height=1080, spp=64, max_depth=16, env="2048x1024 float32 sky + sun lobe 1e4",
+                estimator="unbiased NEE+MIS", l2="inputs larger than L2 (0.7 GB BVH+triangles)")
+NODE_BYTES = 80
+TRI_BYTES = 48
+RAY_BYTES = 32 + 16  # ray in + hit out
+
+
+def load_peaks():
+    p = os.path.join(HERE, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d.get("hbm_gbs", 6800.0), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+
+    def __init__(self):
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "--query-gpu=index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self, gpu_index=0):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in self.lines:
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 9 or f[0] != str(gpu_index):
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for k, name in enumerate(names):
+                if f[5 + k].lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def build_workload():
+    from kagayaki_gb300 import scenes
+    tris, mats, info = scenes.icosphere_field()
+    env, sun = scenes.sky_environment(2048, 1024, sun_peak=1e4, seed=3)
+    return tris, mats, env, info
+
+
+def orbit_camera(frame, height, radius=25.0, start_deg=37.0, step_deg=6.0, z=6.0):
+    """Camera on a circle of `radius` around the field, looking at its centre
+    (z up).  Camera_SetUpCamera's Euler convention: rotate X by 90 - pitch to
+    look horizontally, then Z to face the centre."""
+    from kagayaki_gb300 import camera_setup
+    ang = start_deg + step_deg * frame
+    a = np.deg2rad(ang)
+    org = (radius * np.cos(a), radius * np.sin(a), z)
+    pitch = np.rad2deg(np.arctan2(z - 8.0, radius))
+    return camera_setup(org, 28.0, (90.0 - pitch, 0.0, ang + 90.0), height)
+
+
+def cpu_reference(tris, mats, env, threads, budget_s=10.0, chunk=65536):
+    """The reference's estimator restated on the host (the oracle port, with
+    the oracle's CPU BVH for closest hits) on a bounded sample of the frame:
+    batches of `chunk` pixels spread over the 1920x1080 frame at 1 spp until
+    `budget_s` seconds of work.  Returns (rays/s, rays, seconds, pixels)."""
+    from oracle import orc
+    from kagayaki_gb300 import camera_array
+    bvh = orc.CpuBvh(tris)
+    c = camera_array(orbit_camera(0, 1080))
+    npx = 1920 * 1080
+    order = np.random.default_rng(5).permutation(np.arange(1, npx, dtype=np.int32))
+    rays, secs, done = 0, 0.0, 0
+    while secs < budget_s and done < len(order):
+        px = order[done:done + chunk]
+        t0 = time.perf_counter()
+        _, nr = orc.render_compat_px(bvh, mats, c, 1920, 1080, px, env=env, threads=threads)
+        secs += time.perf_counter() - t0
+        rays += nr
+        done += len(px)
+    bvh.close()
+    return rays / secs, rays, secs, done
+
+
+def run_ours(args):
+    import kagayaki_gb300 as kg
+    from kagayaki_gb300 import ESTIMATOR_UNBIASED, ESTIMATOR_COMPAT, Scene
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as td
+        td.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+        torch.cuda.set_device(local)
+        dist = td
+    kg.lib().kgk_set_device(local)
+    tris, mats, env, info = build_workload()
+    W, H, spp = WORKLOAD["width"], WORKLOAD["height"], WORKLOAD["spp"]
+    scene = Scene(tris, mats, env=env)
+    bvh = scene.build_bvh()
+    cam = orbit_camera(rank, H)
+    kw = dict(spp=spp, max_depth=WORKLOAD["max_depth"], estimator=ESTIMATOR_UNBIASED, seed=1)
+    out_host = np.empty((H, W, 4), np.float32)
+    for w in range(args.warmup):
+        scene.render(cam, W, H, frame_index=w, out=out_host, **kw)
+    # work counts + stage times (untimed pass)
+    _, prof = scene.render(cam, W, H, frame_index=10_000, out=out_host, count_work=True, profile_stages=True, **kw)
+    if dist:
+        dist.barrier()
+    clocks = ClockSampler()
+    clocks.start()
+    # timed: device-resident output (value)
+    import ctypes
+    dev_out = ctypes.c_void_p()
+    from kagayaki_gb300._lib import lib as _l
+    cudart = None
+    rays = 0
+    dev_ms = 0.0
+    launches = 0
+    for k in range(args.steps):
+        img, st = scene.render(cam, W, H, frame_index=args.warmup + k, out=out_host, **kw)
+        rays += st["rays_closest"] + st["rays_shadow"]
+        dev_ms += st["ms_device"]
+        launches += st["kernel_launches"]
+    # end to end: host camera in, host frame out, wall clock
+    t0 = time.perf_counter()
+    e2e_rays = 0
+    for k in range(args.steps):
+        img, st = scene.render(cam, W, H, frame_index=100 + k, out=out_host, **kw)
+        e2e_rays += st["rays_closest"] + st["rays_shadow"]
+    e2e_s = time.perf_counter() - t0
+    ck = clocks.stop(local)
+    if dist:
+        import torch
+        tt = torch.tensor([dev_ms, e2e_s], dtype=torch.float64, device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        tot = torch.tensor([float(rays), float(e2e_rays)], dtype=torch.float64, device="cuda")
+        dist.all_reduce(tot)
+        dev_ms, e2e_s = tt.tolist()
+        rays, e2e_rays = tot.tolist()
+    scene.close()
+    if rank != 0:
+        return
+    hbm, peak_kind = load_peaks()
+    # roofline of the traversal (extend) stage: algorithmic bytes / stage time
+    alg_bytes = prof["nodes_visited"] * NODE_BYTES + prof["tris_tested"] * TRI_BYTES + \
+        prof["rays_closest"] * RAY_BYTES
+    ext_s = prof["ms_extend"] / 1e3
+    achieved = alg_bytes / ext_s / 1e9 if ext_s > 0 else None
+    traffic = None
+    tf = os.path.join(HERE, "profiles", "extend_traffic.json")
+    if os.path.exists(tf):
+        traffic = json.load(open(tf)).get("bytes_per_launch")
+    mrays = rays / (dev_ms / 1e3) / 1e6
+    line = {
+        "metric": "Mrays/s",
+        "value": round(mrays, 2),
+        "unit": "Mrays/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(dev_ms / args.steps, 3),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic seeded scene (procedural icospheres, procedural HDR)",
+        "config": dict(WORKLOAD, parallelism="replicas" if world > 1 else "single"),
+        "e2e": {"value": round(e2e_rays / e2e_s / 1e6, 2), "unit": "Mrays/s",
+                "h2d_bytes_per_step": 72 + 96, "d2h_bytes_per_step": W * H * 16},
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1) if achieved else None,
+                     "peak": hbm, "unit": "GB/s", "frac": round(achieved / hbm, 4) if achieved else None,
+                     "traffic": traffic, "kernel": "k_extend (closest-hit traversal)",
+                     "peak_source": peak_kind,
+                     "bytes_per_ray": round(alg_bytes / max(prof["rays_closest"], 1), 1)},
+        "stages_ms": {"extend": round(prof["ms_extend"], 2), "shade": round(prof["ms_shade"], 2),
+                      "shadow": round(prof["ms_shadow"], 2)},
+        "rays_per_step": int(rays / args.steps),
+        "bvh": {"wide_nodes": bvh["n_wide_nodes"], "build_ms": round(bvh["ms_build"], 1)},
+        "clocks": ck,
+    }
+    if not args.no_cpu:
+        thr = os.cpu_count() or 1
+        rps, nr, dt, npx_done = cpu_reference(tris, mats, env, thr, budget_s=args.cpu_seconds)
+        line["cpu_baseline"] = {"value": round(rps / 1e6, 4), "unit": "Mrays/s", "cores": thr, "kind": "port",
+                                "sample": f"{npx_done} random pixels of the frame at 1 spp, compat estimator "
+                                          f"(oracle port, CPU BVH): {nr} rays in {dt:.1f} s"}
+    print(json.dumps(line), flush=True)
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    thr = os.cpu_count() or 1
+    tris, mats, env, info = build_workload()
+    per = []
+    tot_rays = 0
+    budget = max(2.0, args.cpu_seconds / max(args.steps, 1))
+    for w in range(args.warmup + args.steps):
+        rps, nr, dt, npx_done = cpu_reference(tris, mats, env, thr, budget_s=budget if w >= args.warmup else 1.0)
+        if w >= args.warmup:
+            per.append(dt)
+            tot_rays += nr
+    v = tot_rays / sum(per) / 1e6
+    line = {"metric": "Mrays/s", "value": round(v, 4), "unit": "Mrays/s", "impl": "reference",
+            "n_gpus": int(os.environ.get("WORLD_SIZE", "1")), "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(1e3 * sum(per) / len(per), 1), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic seeded scene",
+            "config": dict(WORKLOAD, parallelism="host cores"),
+            "cpu_baseline": {"value": round(v, 4), "unit": "Mrays/s", "cores": thr, "kind": "port",
+                             "sample": f"random pixels of the frame at 1 spp per step (~{budget:.0f} s of work), "
+                                       "compat estimator, oracle port with a CPU BVH"},
+            "e2e": {"value": round(v, 4), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU baseline work budget")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -129,7 +129,8 @@ typedef struct kgk_render_config {
     int32_t count_work;      /* 1: count BVH nodes visited / triangles tested      */
     int32_t write_gbuffer;   /* 1: write the SVGF G-buffer from primary hits       */
     int32_t use_cache;       /* 1: terminate paths into the radiance cache         */
-    int32_t reserved[6];
+    int32_t profile_stages;  /* 1: time each pipeline stage with CUDA events        */
+    int32_t reserved[5];
 } kgk_render_config;
 
 /* Work counters of one call.  Rays follow the reference's counting rule: one
@@ -142,7 +143,10 @@ typedef struct kgk_stats {
     uint64_t tris_tested;         /* triangles tested (count_work only)         */
     uint64_t paths;               /* camera paths traced                         */
     double ms_device;             /* device time of the call (CUDA events)       */
-    double reserved[4];
+    uint64_t kernel_launches;     /* kernels this call launched                  */
+    double ms_extend;             /* closest-hit stage device time (profile_stages) */
+    double ms_shade;              /* shading stage device time (profile_stages)  */
+    double ms_shadow;             /* shadow-ray stage device time (profile_stages) */
 } kgk_stats;
 
 typedef struct kgk_bvh_info {

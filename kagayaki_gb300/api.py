@@ -35,7 +35,7 @@ def _as(a, dtype):
 
 
 def stats_dict(s):
-    return {k: getattr(s, k) for k, _ in KgkStats._fields_ if k != "reserved"}
+    return {k: getattr(s, k) for k, _ in KgkStats._fields_}
 
 
 class Scene:
@@ -115,12 +115,13 @@ class Scene:
     def render(self, cam, width, height, spp=1, max_depth=0, rr_start_depth=3,
                estimator=ESTIMATOR_COMPAT, seed=1, frame_index=0, accumulate=False,
                count_work=False, write_gbuffer=False, use_cache=False, wave_paths=0, prev_cam=None,
-               out=None):
+               out=None, profile_stages=False):
         cfg = KgkRenderConfig(width=width, height=height, spp=spp, max_depth=max_depth,
                               rr_start_depth=rr_start_depth, estimator=estimator, seed=seed,
                               frame_index=frame_index, accumulate=int(accumulate),
                               wave_paths=wave_paths, count_work=int(count_work),
-                              write_gbuffer=int(write_gbuffer), use_cache=int(use_cache))
+                              write_gbuffer=int(write_gbuffer), use_cache=int(use_cache),
+                              profile_stages=int(profile_stages))
         if out is None:
             out = np.empty((height, width, 4), np.float32)
         st = KgkStats()

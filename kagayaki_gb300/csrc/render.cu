@@ -1,31 +1,1018 @@
-// render.cu - wavefront path tracer (placeholder until the pipeline lands).
+// render.cu - wavefront path tracer.  Replaces the per-pixel megakernel
+// render<<<W*H/256, 256>>> (render.cuh:21-49, RayTrace.cuh:9-109).
+//
+// One wave = one path per (pixel, sample) pair, state in SoA arrays indexed by
+// path id.  Per bounce:
+//   extend  closest hit of every active path; paths are appended to one of
+//           three shade queues (miss, Lambert, Disney) with warp-ballot
+//           compaction, so shading warps are material-coherent;
+//   shade   emission, Russian roulette, next-event estimation (shadow-ray
+//           records with their contribution precomputed), BSDF sampling;
+//           continuing paths are compacted into the next active queue;
+//   shadow  two passes (face lights, environment) - at most one record per
+//           path per pass, so each adds to its path's radiance without atomics
+//           and in the reference's order (face light, then environment).
+// Kernels are persistent grid-stride loops that read their queue length from
+// device memory: the host never waits inside a wave.
+#include <cmath>
+#include <cstring>
+#include <vector>
+
 #include "kgk_scene.h"
+#include "shading.cuh"
+#include "traverse.cuh"
 
 namespace kgk {
-struct RenderState {};
+
+struct RenderState {
+    int W = 0, H = 0;                         // per-pixel buffers
+    unsigned long long *seeds = nullptr;      // compat per-pixel seed chain (render.cuh:19,29,42)
+    float4 *frame = nullptr;                  // per-call radiance sum
+    double *acc_sum = nullptr, *acc_sq = nullptr;  // FP64 accumulator (3 per pixel)
+    unsigned long long acc_n = 0;
+    int acc_W = 0, acc_H = 0;
+    // G-buffer of the last frame (SVGF input), per pixel
+    float4 *gb_pos = nullptr;   // position, depth (hit distance)
+    float4 *gb_nrm = nullptr;   // shading normal toward the camera, object id bits
+    float4 *gb_alb = nullptr;   // albedo, material id bits
+    float4 *gb_emi = nullptr;   // emission, hit flag
+    // wave state (capacity cap paths)
+    int cap = 0;
+    float4 *o = nullptr, *d = nullptr, *thr = nullptr, *rad = nullptr, *hit = nullptr;
+    unsigned long long *rng = nullptr;
+    int *depth = nullptr;
+    int *aq[2] = {nullptr, nullptr};
+    int *sq[3] = {nullptr, nullptr, nullptr};
+    float4 *sh_o[2] = {nullptr, nullptr}, *sh_d[2] = {nullptr, nullptr}, *sh_c[2] = {nullptr, nullptr};
+    int *cnt = nullptr;                       // queue counters
+    unsigned long long *stats = nullptr;      // rays_closest, rays_shadow, overflow, nodes, tris
+    int sms = 0;
+};
+
+namespace {
+
+enum Cnt { kA0 = 0, kA1 = 1, kSQ0 = 2, kSQ1 = 3, kSQ2 = 4, kSH0 = 5, kSH1 = 6, kNCnt = 8 };
+enum Stat { kRaysC = 0, kRaysS = 1, kOverflow = 2, kNodes = 3, kTris = 4, kNStat = 8 };
+
+struct Params {
+    DevScene sc;
+    kgk_camera cam;
+    int W, H, npx;
+    int spp_wave;          // samples per pixel in this wave
+    int sample_base;       // first sample index of the wave
+    int estimator;
+    int max_depth;         // <= 0: unlimited
+    int rr_start;
+    int write_gbuffer;
+    int count_work;
+    unsigned long long seed;
+    int frame_index;
+    // state
+    float4 *o, *d, *thr, *rad, *hit;
+    unsigned long long *rng;
+    int *depth;
+    unsigned long long *seeds;
+    float4 *gb_pos, *gb_nrm, *gb_alb, *gb_emi;
+    int *cnt;
+    unsigned long long *stats;
+};
+
+__device__ __forceinline__ int warp_append(int *counter, bool pred) {
+    const unsigned m = __ballot_sync(~0u, pred);
+    if (m == 0u) return -1;
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(m) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(counter, __popc(m));
+    base = __shfl_sync(~0u, base, leader);
+    return base + __popc(m & ((1u << lane) - 1u));
+}
+
+__device__ __forceinline__ void warp_add_u64(unsigned long long *dst, unsigned v) {
+    unsigned long long x = v;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(~0u, x, o);
+    if ((threadIdx.x & 31) == 0 && x) atomicAdd(dst, x);
+}
+
+__device__ __forceinline__ float3 env_or_bg_ref(const DevScene &s, float3 d) {
+    return s.env ? env_lookup_ref(s, d) : f3(1.0f, 1.0f, 1.0f);
+}
+
+// Generate1stRay (struct_Camera.cuh:38-45); jx, jy shift the pixel position.
+__device__ __forceinline__ float3 primary_dir(const kgk_camera &c, int W, int H, float X, float Y) {
+    const float3 cd = f3(c.CamDir.x, c.CamDir.y, c.CamDir.z);
+    const float3 sx = f3(c.ScreenXDir.x, c.ScreenXDir.y, c.ScreenXDir.z);
+    const float3 sy = f3(c.ScreenYDir.x, c.ScreenYDir.y, c.ScreenYDir.z);
+    float3 r = cd * c.CamToScreenDist + (sx * (X - W / 2.0f)) * c.PixelSize + (sy * (H / 2.0f - Y)) * c.PixelSize;
+    return normalize3(r);
+}
+
+// ---------------------------------------------------------------------------
+__global__ void k_raygen(Params P) {
+    const int n = P.npx * P.spp_wave;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int px = i % P.npx;
+        const int smp = P.sample_base + i / P.npx;
+        const int X = px % P.W, Y = px / P.W;
+        unsigned long long s;
+        float3 dir;
+        if (P.estimator == KGK_ESTIMATOR_COMPAT) {
+            // render.cuh:29 seeding; pixel 0 divides by zero there, its terms are 0 here
+            const int pos = px;
+            const int m1 = (int)((unsigned)142857u * (unsigned)pos);
+            const long long q = pos > 0 ? 998244353 / pos : 0;
+            const long long r = pos > 0 ? 1000000007 % pos : 0;
+            s = P.seeds[px] + (unsigned long long)(long long)m1 + (unsigned long long)q + (unsigned long long)r;
+            dir = primary_dir(P.cam, P.W, P.H, (float)X, (float)Y);
+        } else {
+            s = splitmix64(P.seed ^ splitmix64(((unsigned long long)P.frame_index << 40) ^
+                                               ((unsigned long long)smp << 26) ^ (unsigned long long)px));
+            if (s == 0ull) s = 1ull;
+            const float jx = rnd_u(s) - 0.5f, jy = rnd_u(s) - 0.5f;
+            dir = primary_dir(P.cam, P.W, P.H, (float)X + jx, (float)Y + jy);
+        }
+        P.o[i] = make_float4(P.cam.CamOrg.x, P.cam.CamOrg.y, P.cam.CamOrg.z, 0.0f);
+        P.d[i] = make_float4(dir.x, dir.y, dir.z, 0.0f);  // w: pdf of the sampled direction (0 = no MIS)
+        P.thr[i] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
+        const float r0 = P.estimator == KGK_ESTIMATOR_COMPAT ? kSINF : 0.0f;  // RayTrace.cuh:14
+        P.rad[i] = make_float4(r0, r0, r0, 0.0f);
+        P.rng[i] = s;
+        P.depth[i] = 0;
+    }
+}
+
+// ---------------------------------------------------------------------------
+template <bool kCount>
+__global__ void __launch_bounds__(128) k_extend(Params P, const int *__restrict__ q, int qcnt_idx, int dense_n,
+                                                int *sq0, int *sq1, int *sq2) {
+    const int n = q ? P.cnt[qcnt_idx] : dense_n;
+    const DevScene &s = P.sc;
+    for (int base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+        const int i = base + threadIdx.x;
+        const bool valid = i < n;
+        int p = 0, cls = -1;
+        TravStats st{0, 0, 0};
+        if (valid) {
+            p = q ? q[i] : i;
+            const float4 o = P.o[p], d = P.d[p];
+            const RayPre r = make_ray(f3(o), f3(d));
+            float bt = kBigT, u = 0.0f, v = 0.0f;
+            int bid = 0x7fffffff;
+            const int slot = trace_closest<kCount>(s.nodes, (unsigned)s.n_nodes, s.tri_rec, (unsigned)s.n_tris,
+                                                   r, bt, bid, u, v, st);
+            if (slot < 0) {
+                cls = 0;
+                P.hit[p] = make_float4(kBigT, 0.0f, 0.0f, __int_as_float(-1));
+            } else {
+                P.hit[p] = make_float4(bt, u, v, __int_as_float(bid));
+                const unsigned bits = __float_as_uint(__ldg(&s.attr[4 * bid + 3].w));
+                const int mid = (int)(bits & 0x7fffffffu);
+                cls = __ldg(&s.mats[mid].MATERIAL_TYPE_ID) == 1 ? 2 : 1;
+            }
+        }
+        const int a0 = warp_append(&P.cnt[kSQ0], cls == 0);
+        const int a1 = warp_append(&P.cnt[kSQ1], cls == 1);
+        const int a2 = warp_append(&P.cnt[kSQ2], cls == 2);
+        if (cls == 0) sq0[a0] = p;
+        if (cls == 1) sq1[a1] = p;
+        if (cls == 2) sq2[a2] = p;
+        warp_add_u64(&P.stats[kRaysC], valid ? 1u : 0u);
+        if (kCount) {
+            warp_add_u64(&P.stats[kNodes], st.nodes);
+            warp_add_u64(&P.stats[kTris], st.tris);
+        }
+        warp_add_u64(&P.stats[kOverflow], st.overflow);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Surface interaction (shared by both estimators)
+// ---------------------------------------------------------------------------
+struct Surface {
+    float3 pos, ng, ns, n;  // n = shading normal flipped to face the ray
+    float t;
+    kgk_material m;
+    int mat_id;
+};
+
+__device__ __forceinline__ Surface load_surface(const DevScene &s, int id, float4 h, float3 o, float3 d) {
+    Surface S;
+    const float3 v0 = f3(__ldg(&s.verts[3 * id])), v1 = f3(__ldg(&s.verts[3 * id + 1])),
+                 v2 = f3(__ldg(&s.verts[3 * id + 2]));
+    const float4 a0 = __ldg(&s.attr[4 * id]), a1 = __ldg(&s.attr[4 * id + 1]), a2 = __ldg(&s.attr[4 * id + 2]),
+                 a3 = __ldg(&s.attr[4 * id + 3]);
+    const float3 c = cross3(v1 - v0, v2 - v0);
+    const float3 n0 = f3(a0), n1 = f3(a1), n2 = f3(a2);
+    // Triangle::intersectTest (struct_Triangle.cuh:33-39, 62-76)
+    S.ng = len3(c) == 0.0f ? normalize3(n0 + n1 + n2) : normalize3(c);
+    const float b1 = h.y, b2 = h.z, b0 = 1.0f - b1 - b2;
+    const unsigned bits = __float_as_uint(a3.w);
+    S.ns = (bits & 0x80000000u) ? normalize3(n1 * b1 + n2 * b2 + n0 * b0) : S.ng;
+    float uu = b1 * a1.z + b2 * a3.y + b0 * a0.w;   // vt.x of v1, v2, v0
+    float vv = b1 * a3.x + b2 * a3.z + b0 * a1.w;   // vt.y
+    if (uu < 0.0f) uu += (float)((int)(-uu) + 1); else if (uu > 1.0f) uu -= (float)((int)uu);
+    if (vv < 0.0f) vv += (float)((int)(-vv) + 1); else if (vv > 1.0f) vv -= (float)((int)vv);
+    S.t = h.x;
+    S.pos = o + d * h.x;
+    S.mat_id = (int)(bits & 0x7fffffffu);
+    S.m = s.mats[S.mat_id];
+    if (S.m.TEXTURE_BASECOLOR_ID != -1) {
+        const float3 tc = tex_fetch(s, S.m.TEXTURE_BASECOLOR_ID, uu, vv);
+        S.m.diffuse.x = tc.x; S.m.diffuse.y = tc.y; S.m.diffuse.z = tc.z;
+    }
+    const float3 dif = f3(S.m.diffuse.x, S.m.diffuse.y, S.m.diffuse.z);
+    if ((double)len3(dif) < 1e-5) {  // RayTrace.cuh:53-55
+        S.m.diffuse.x = S.m.diffuse.y = S.m.diffuse.z = kSINF;
+    }
+    S.n = dot3(S.ns, d) > 0.0f ? -S.ns : S.ns;
+    return S;
+}
+
+__device__ __forceinline__ float3 emission_of(const kgk_material &m) { return f3(m.emission.x, m.emission.y, m.emission.z); }
+__device__ __forceinline__ float3 diffuse_of(const kgk_material &m) { return f3(m.diffuse.x, m.diffuse.y, m.diffuse.z); }
+
+__device__ __forceinline__ void push_shadow(const Params &P, float4 *so, float4 *sd, float4 *sc, int cidx,
+                                            bool pred, float3 org, float3 dir, float tmax, int light,
+                                            float3 contrib, int path) {
+    const int k = warp_append(&P.cnt[cidx], pred);
+    if (pred) {
+        so[k] = make_float4(org.x, org.y, org.z, tmax);
+        sd[k] = make_float4(dir.x, dir.y, dir.z, __int_as_float(light));
+        sc[k] = make_float4(contrib.x, contrib.y, contrib.z, __int_as_float(path));
+    }
+}
+
+// Writes the G-buffer of a primary hit (RayTrace.cuh:66-82): albedo after the
+// texture and the zero fix, emission, normal facing the camera, object id,
+// material id, depth.  The reference's reprojection result is always
+// (-1, -1) (struct_Camera.cuh:109-110); reprojection is done by SVGF itself.
+__device__ __forceinline__ void write_gbuffer(const Params &P, int px, const Surface *S) {
+    if (!S) {
+        P.gb_pos[px] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        P.gb_nrm[px] = make_float4(0.0f, 0.0f, 0.0f, __int_as_float(-1));
+        P.gb_alb[px] = make_float4(0.0f, 0.0f, 0.0f, __int_as_float(-1));
+        P.gb_emi[px] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        return;
+    }
+    P.gb_pos[px] = make_float4(S->pos.x, S->pos.y, S->pos.z, S->t);
+    P.gb_alb[px] = make_float4(S->m.diffuse.x, S->m.diffuse.y, S->m.diffuse.z, __int_as_float(S->mat_id));
+    P.gb_emi[px] = make_float4(S->m.emission.x, S->m.emission.y, S->m.emission.z, 1.0f);
+}
+
+// ---------------------------------------------------------------------------
+// compat shade: RayTrace.cuh:37-106 for one vertex
+// ---------------------------------------------------------------------------
+__device__ void shade_compat(const Params &P, int p, bool valid, int *next_q, int next_cnt, float4 *so0,
+                             float4 *sd0, float4 *sc0, float4 *so1, float4 *sd1, float4 *sc1) {
+    const DevScene &s = P.sc;
+    bool cont = false;
+    bool f_pred = false, e_pred = false;
+    float3 f_org, f_dir, f_c, e_dir, e_c;
+    float f_tmax = 0.0f;
+    int f_light = -1;
+    float3 npos, ndir, T;
+    unsigned long long rs = 0;
+    if (valid) {
+        const float4 o4 = P.o[p], d4 = P.d[p], h = P.hit[p];
+        const float3 o = f3(o4), d = f3(d4);
+        T = f3(P.thr[p]);
+        float3 rad = f3(P.rad[p]);
+        rs = P.rng[p];
+        const int depth = P.depth[p];
+        const int id = __float_as_int(h.w);
+        const int px = p % P.npx;
+        const bool first_sample = p < P.npx;
+        if (id < 0) {
+            if (depth == 0 && P.write_gbuffer && first_sample) {
+                write_gbuffer(P, px, nullptr);
+                P.gb_nrm[px] = make_float4(0.0f, 0.0f, 0.0f, __int_as_float(-1));
+            }
+            rad += T * env_or_bg_ref(s, d);  // RayTrace.cuh:21-35
+        } else {
+            Surface S = load_surface(s, id, h, o, d);
+            const float3 n = S.n;
+            if (depth == 0 && P.write_gbuffer && first_sample) {
+                write_gbuffer(P, px, &S);
+                P.gb_nrm[px] = make_float4(n.x, n.y, n.z, __int_as_float(id));
+            }
+            const DisneyParams dp = disney_params(S.m);
+            const float3 dif = diffuse_of(S.m), emi = emission_of(S.m);
+            // Russian roulette (2, 3)
+            float prr = fmaxf(dif.x, fmaxf(dif.y, dif.z));
+            if (prr == 0.0f) prr = kSINF;
+            const float rnd = rnd_ref(rs, 0.0f, 1.0f);
+            bool killed = false;
+            if (depth > 3) prr /= (float)(depth * depth);
+            if (depth > 2) {
+                if (prr < rnd) {
+                    rad += T * emi;
+                    killed = true;
+                }
+            } else {
+                prr = 1.0f;
+            }
+            if (!killed) {
+                if (depth == 0) rad += T * emi;
+                T = T / prr;
+                const float3 wo = -d;
+                // NEE, face lights (NextEventEstimation_FaceLight.cuh:47-120)
+                if (len3(emi) == 0.0f && S.m.MATERIAL_TYPE_ID < 2 && s.n_tris > 0) {
+                    const float R = rnd_ref(rs, 0.0f, 1.0f);
+                    // g++ evaluates SamplePointOnTriangle's arguments right to left
+                    const float r2 = rnd_ref(rs, 0.0f, 1.0f);
+                    const float r1 = rnd_ref(rs, 0.0f, 1.0f);
+                    // without face lights the reference samples Objects[-1]
+                    // (undefined); this step then contributes nothing
+                    if (!s.no_light) {
+                        const int lid = lower_bound_f(s.light_cdf_ref, s.n_tris,
+                                                      R * __ldg(&s.light_cdf_ref[s.n_tris - 1]));
+                        const float3 L0 = f3(__ldg(&s.verts[3 * lid])), L1 = f3(__ldg(&s.verts[3 * lid + 1])),
+                                     L2 = f3(__ldg(&s.verts[3 * lid + 2]));
+                        float t1 = r1 / 2.0f, t2 = r2 / 2.0f;
+                        const float off = t2 - t1;
+                        if (off > 0.0f) t2 += off; else t1 -= off;
+                        const float3 Pl = L0 * t1 + L1 * t2 + L2 * (1.0f - t1 - t2);
+                        const float3 Ld = normalize3(Pl - S.pos);
+                        const float dist = len3(Pl - S.pos);
+                        if (dot3(Ld, n) > 0.0f) {
+                            // the light's shading normal at the sample (smooth lights interpolate)
+                            const float4 la0 = __ldg(&s.attr[4 * lid]), la1 = __ldg(&s.attr[4 * lid + 1]),
+                                         la2 = __ldg(&s.attr[4 * lid + 2]), la3 = __ldg(&s.attr[4 * lid + 3]);
+                            const float3 lc = cross3(L1 - L0, L2 - L0);
+                            float3 lng = len3(lc) == 0.0f ? normalize3(f3(la0) + f3(la1) + f3(la2)) : normalize3(lc);
+                            if (__float_as_uint(la3.w) & 0x80000000u)
+                                lng = normalize3(f3(la1) * t2 + f3(la2) * (1.0f - t1 - t2) + f3(la0) * t1);
+                            const float cos1 = fabsf(dot3(S.ns, Ld)), cos2 = fabsf(dot3(lng, -Ld));
+                            const float G = cos1 * cos2 / (dist * dist);
+                            const float ltot = __ldg(&s.light_cdf_ref[s.n_tris - 1]);
+                            const float lprev = lid == 0 ? 0.0f : __ldg(&s.light_cdf_ref[lid - 1]);
+                            const float larea = 0.5f * len3(lc);
+                            const float pdf_nee = (lid == 0 ? __ldg(&s.light_cdf_ref[0]) / ltot
+                                                            : (__ldg(&s.light_cdf_ref[lid]) - lprev) / ltot) *
+                                                  (1.0f / larea);
+                            float p_hdr = s.env ? env_pdf_ref(s, Ld) : 0.0f;
+                            float3 bsdf;
+                            float p_pt;
+                            if (S.m.MATERIAL_TYPE_ID == 0) {
+                                bsdf = dif / kPI;
+                                p_pt = fmaxf(dot3(n, Ld), 0.0f) / kPI;
+                            } else {
+                                float3 u, v, w;
+                                onb_ref(n, u, v, w);
+                                bsdf = disney_eval(S.m, dp, Ld, wo, n, u, v, w);
+                                p_pt = disney_pdf_ref(dp, wo, Ld, n, u, v, w);
+                            }
+                            p_pt *= G / fabsf(dot3(Ld, S.ns));
+                            const float mis = pdf_nee / (p_pt + pdf_nee + p_hdr);
+                            const kgk_material lm = s.mats[__float_as_uint(la3.w) & 0x7fffffffu];
+                            const float3 c = ((bsdf * G) / pdf_nee) * emission_of(lm) * mis;
+                            f_pred = true;
+                            f_org = S.pos;
+                            f_dir = Ld;
+                            f_tmax = dist * 1.001f + 1e-4f;
+                            f_light = lid;
+                            f_c = T * c;
+                        }
+                    }
+                }
+                // NEE, environment (NextEventEstimation_HDR.cuh:4-58)
+                if (s.env) {
+                    const int npx = s.env_w * s.env_h;
+                    const float R = rnd_ref(rs, 0.0f, 1.0f);
+                    const float tot = __ldg(&s.env_cdf_ref[npx - 1]);
+                    const int pix = lower_bound_f(s.env_cdf_ref, npx, R * tot);
+                    float pdf = pix == 0 ? __ldg(&s.env_cdf_ref[0]) / tot
+                                         : (__ldg(&s.env_cdf_ref[pix]) - __ldg(&s.env_cdf_ref[pix - 1])) / tot;
+                    const float3 ed = env_index_to_dir_ref(s, pix, pdf);
+                    if (dot3(ed, n) > 0.0f) {
+                        const float3 Le = env_texel(s, pix);
+                        float3 bsdf;
+                        float p_pt;
+                        if (S.m.MATERIAL_TYPE_ID == 0) {
+                            bsdf = dif / kPI;
+                            p_pt = fmaxf(dot3(n, ed), 0.0f) / kPI;
+                        } else {
+                            float3 u, v, w;
+                            onb_ref(n, u, v, w);
+                            bsdf = disney_eval(S.m, dp, ed, wo, n, u, v, w);
+                            p_pt = disney_pdf_ref(dp, wo, ed, n, u, v, w);
+                        }
+                        const float mis = pdf / (p_pt + pdf);
+                        const float3 c = (bsdf * (Le / pdf)) * dot3(n, ed) * mis;
+                        e_pred = true;
+                        e_dir = ed;
+                        e_c = c * T;
+                    }
+                }
+                float3 u, v, w;
+                onb_ref(n, u, v, w);
+                // NextEventEstimation_PathTracing.cuh: draws its direction, adds nothing
+                if (S.m.MATERIAL_TYPE_ID == 0) (void)sample_cos_ref(rs, u, v, w);
+                // SampleNextRay (sampling.cuh:28-64)
+                float3 nd;
+                if (S.m.MATERIAL_TYPE_ID == 0) {
+                    nd = sample_cos_ref(rs, u, v, w);
+                    T = dif * T;
+                } else {
+                    // sample_BXDF in its zero-initialised reading: Sum = {w0, w0, w1, w2, w3}
+                    float R = rnd_ref(rs, 0.0f, 1.0f);
+                    const float sum[5] = {dp.wt[0], dp.wt[0], dp.wt[1], dp.wt[2], dp.wt[3]};
+                    R *= sum[4];
+                    int lobe;
+                    {
+                        int ng = -1, ok = 4;
+                        while (ok - ng > 1) {
+                            const int mid = (ok + ng) / 2;
+                            if (sum[mid] >= R) ok = mid; else ng = mid;
+                        }
+                        lobe = ok;
+                    }
+                    if (lobe <= 2) {
+                        nd = sample_cos_ref(rs, u, v, w);
+                    } else if (lobe == 3) {
+                        const float R1 = rnd_ref(rs, 0.0001f, 0.9999f);
+                        const float R2 = rnd_ref(rs, 0.0001f, 0.9999f);
+                        nd = reflect_ref(d, gtr2_half(R1, R2, u, v, w, dp.ax, dp.ay));
+                    } else {
+                        const float R1 = rnd_ref(rs, 0.0001f, 0.9999f);
+                        const float R2 = rnd_ref(rs, 0.0001f, 0.9999f);
+                        nd = reflect_ref(d, gtr1_half(R1, R2, u, v, w, dp.ac, false));
+                    }
+                    const float3 b = disney_eval(S.m, dp, nd, wo, n, u, v, w);
+                    const float pdf = disney_pdf_ref(dp, wo, nd, n, u, v, w);
+                    T = T * ((b * fabsf(dot3(n, nd))) / pdf);
+                }
+                npos = S.pos;
+                ndir = nd;
+                cont = P.max_depth <= 0 || depth + 1 < P.max_depth;
+            }
+        }
+        P.rad[p] = make_float4(rad.x, rad.y, rad.z, 0.0f);
+        if (cont) {
+            P.o[p] = make_float4(npos.x, npos.y, npos.z, 0.0f);
+            P.d[p] = make_float4(ndir.x, ndir.y, ndir.z, 0.0f);
+            P.thr[p] = make_float4(T.x, T.y, T.z, 0.0f);
+            P.depth[p] = depth + 1;
+        }
+        P.rng[p] = rs;
+        if (!cont) P.seeds[px] = rs;  // randSeeds[pos] = rand.seed (render.cuh:42)
+    }
+    const int k = warp_append(&P.cnt[next_cnt], cont);
+    if (cont) next_q[k] = p;
+    push_shadow(P, so0, sd0, sc0, kSH0, f_pred, f_org, f_dir, f_tmax, f_light, f_c, p);
+    push_shadow(P, so1, sd1, sc1, kSH1, e_pred, npos, e_dir, kBigT, -1, e_c, p);
+}
+
+// ---------------------------------------------------------------------------
+// unbiased shade
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void bsdf_eval_pdf(const Surface &S, const DisneyParams &dp, float3 n, float3 wo,
+                                              float3 wi, float3 &f, float &pdf) {
+    if (S.m.MATERIAL_TYPE_ID == 1) {
+        float3 u, v, w;
+        onb_ref(n, u, v, w);
+        f = disney_eval(S.m, dp, wi, wo, n, u, v, w);
+        pdf = disney_pdf_unbiased(dp, wo, wi, n, u, v, w);
+    } else {
+        const float c = dot3(n, wi);
+        f = c > 0.0f ? diffuse_of(S.m) / kPI : f3(0.0f, 0.0f, 0.0f);
+        pdf = fmaxf(c, 0.0f) / kPI;
+    }
+}
+
+__device__ void shade_unbiased(const Params &P, int p, bool valid, int *next_q, int next_cnt, float4 *so0,
+                               float4 *sd0, float4 *sc0, float4 *so1, float4 *sd1, float4 *sc1) {
+    const DevScene &s = P.sc;
+    bool cont = false, f_pred = false, e_pred = false;
+    float3 spos = f3(0.0f, 0.0f, 0.0f), f_dir = spos, f_c = spos, e_dir = spos, e_c = spos;
+    float f_tmax = 0.0f, npdf = 0.0f;
+    float3 ndir = spos, T = spos;
+    unsigned long long rs = 0;
+    if (valid) {
+        const float4 o4 = P.o[p], d4 = P.d[p], h = P.hit[p];
+        const float3 o = f3(o4), d = f3(d4);
+        const float prev_pdf = d4.w;  // 0: no MIS (camera ray)
+        T = f3(P.thr[p]);
+        float3 rad = f3(P.rad[p]);
+        rs = P.rng[p];
+        const int depth = P.depth[p];
+        const int id = __float_as_int(h.w);
+        const int px = p % P.npx;
+        const bool first_sample = p < P.npx;
+        if (id < 0) {
+            if (depth == 0 && P.write_gbuffer && first_sample) write_gbuffer(P, px, nullptr);
+            if (s.env) {
+                const float3 Le = env_lookup_u(s, d);
+                float wgt = 1.0f;
+                if (prev_pdf > 0.0f) {
+                    const float pe = env_pdf_u(s, d);
+                    wgt = prev_pdf / (prev_pdf + pe);
+                }
+                rad += T * Le * wgt;
+            } else {
+                rad += T;  // background (1,1,1), no light sampling for it
+            }
+        } else {
+            Surface S = load_surface(s, id, h, o, d);
+            const float3 n = S.n, wo = -d;
+            if (depth == 0 && P.write_gbuffer && first_sample) {
+                write_gbuffer(P, px, &S);
+                P.gb_nrm[px] = make_float4(n.x, n.y, n.z, __int_as_float(id));
+            }
+            const float3 emi = emission_of(S.m);
+            if (emi.x > 0.0f || emi.y > 0.0f || emi.z > 0.0f) {
+                float wgt = 1.0f;
+                if (prev_pdf > 0.0f && s.n_emit > 0) {
+                    const float cosl = fabsf(dot3(S.ng, d));
+                    const float parea = len3(emi) / s.emit_total;
+                    const float pl = cosl > 0.0f ? parea * S.t * S.t / cosl : 0.0f;
+                    wgt = prev_pdf / (prev_pdf + pl);
+                }
+                rad += T * emi * wgt;
+            }
+            bool alive = true;
+            if (depth >= P.rr_start) {
+                const float q = fminf(maxc(T), 0.95f);
+                if (rnd_u(rs) >= q) alive = false;
+                else T = T / q;
+            }
+            if (alive) {
+                const DisneyParams dp = disney_params(S.m);
+                spos = S.pos;
+                // NEE: one emitter sample
+                if (s.n_emit > 0) {
+                    const float r0 = rnd_u(rs), r1 = rnd_u(rs), r2 = rnd_u(rs);
+                    const int k = cdf_search(s.emit_cdf, s.n_emit, r0);
+                    const int lid = __ldg(&s.emit_ids[min(k, s.n_emit - 1)]);
+                    const float3 L0 = f3(__ldg(&s.verts[3 * lid])), L1 = f3(__ldg(&s.verts[3 * lid + 1])),
+                                 L2 = f3(__ldg(&s.verts[3 * lid + 2]));
+                    const float su = sqrtf(r1);
+                    const float3 Pl = L0 * (1.0f - su) + L1 * (r2 * su) + L2 * (su - r2 * su);
+                    float3 Ld = Pl - S.pos;
+                    const float dist = len3(Ld);
+                    Ld = Ld / dist;
+                    const float3 lc = cross3(L1 - L0, L2 - L0);
+                    const float cosl = fabsf(dot3(normalize3(lc), Ld));
+                    const float coss = dot3(n, Ld);
+                    if (coss > 0.0f && cosl > 0.0f && dist > 0.0f) {
+                        const unsigned lb = __float_as_uint(__ldg(&s.attr[4 * lid + 3].w));
+                        const float3 Le = emission_of(s.mats[lb & 0x7fffffffu]);
+                        const float parea = len3(Le) / s.emit_total;
+                        const float pl = parea * dist * dist / cosl;
+                        float3 f;
+                        float pb;
+                        bsdf_eval_pdf(S, dp, n, wo, Ld, f, pb);
+                        const float wgt = pl / (pl + pb);
+                        f_c = T * f * Le * (coss * wgt / pl);
+                        f_pred = f_c.x > 0.0f || f_c.y > 0.0f || f_c.z > 0.0f;
+                        f_dir = Ld;
+                        f_tmax = dist * (1.0f - 1e-4f);
+                    }
+                }
+                // NEE: one environment sample
+                if (s.env) {
+                    const float r0 = rnd_u(rs), r1 = rnd_u(rs), r2 = rnd_u(rs), r3 = rnd_u(rs);
+                    float pe;
+                    float3 Le;
+                    const float3 ed = env_sample_u(s, r0, r1, r2, r3, pe, Le);
+                    const float coss = dot3(n, ed);
+                    if (coss > 0.0f && pe > 0.0f) {
+                        float3 f;
+                        float pb;
+                        bsdf_eval_pdf(S, dp, n, wo, ed, f, pb);
+                        const float wgt = pe / (pe + pb);
+                        e_c = T * f * Le * (coss * wgt / pe);
+                        e_pred = e_c.x > 0.0f || e_c.y > 0.0f || e_c.z > 0.0f;
+                        e_dir = ed;
+                    }
+                }
+                // BSDF sample
+                if (P.max_depth <= 0 || depth + 1 < P.max_depth) {
+                    float3 u, v, w;
+                    onb_ref(n, u, v, w);
+                    float3 nd;
+                    float3 f;
+                    float pb;
+                    if (S.m.MATERIAL_TYPE_ID == 1) {
+                        const float sw = dp.wt[0] + dp.wt[1] + dp.wt[2] + dp.wt[3] + dp.wt[4];
+                        const float rl = rnd_u(rs) * sw, r1 = rnd_u(rs), r2 = rnd_u(rs);
+                        const float c3 = dp.wt[0] + dp.wt[1] + dp.wt[2];
+                        if (rl < c3) nd = sample_cos_u(r1, r2, u, v, w);
+                        else if (rl < c3 + dp.wt[3])
+                            nd = reflect_ref(d, gtr2_half(fminf(r1, 0.99999f), fminf(r2, 0.99999f), u, v, w, dp.ax, dp.ay));
+                        else
+                            nd = reflect_ref(d, gtr1_half(r1, r2, u, v, w, dp.ac, true));
+                        bsdf_eval_pdf(S, dp, n, wo, nd, f, pb);
+                    } else {
+                        const float r1 = rnd_u(rs), r2 = rnd_u(rs);
+                        nd = sample_cos_u(r1, r2, u, v, w);
+                        bsdf_eval_pdf(S, dp, n, wo, nd, f, pb);
+                    }
+                    const float c = dot3(n, nd);
+                    if (pb > 0.0f && c > 0.0f) {
+                        T = T * f * (c / pb);
+                        if (T.x > 0.0f || T.y > 0.0f || T.z > 0.0f) {
+                            cont = true;
+                            ndir = nd;
+                            npdf = pb;
+                        }
+                    }
+                }
+            }
+        }
+        P.rad[p] = make_float4(rad.x, rad.y, rad.z, 0.0f);
+        if (cont) {
+            P.o[p] = make_float4(spos.x, spos.y, spos.z, 0.0f);
+            P.d[p] = make_float4(ndir.x, ndir.y, ndir.z, npdf);
+            P.thr[p] = make_float4(T.x, T.y, T.z, 0.0f);
+            P.depth[p] = depth + 1;
+        }
+        P.rng[p] = rs;
+    }
+    const int k = warp_append(&P.cnt[next_cnt], cont);
+    if (cont) next_q[k] = p;
+    push_shadow(P, so0, sd0, sc0, kSH0, f_pred, spos, f_dir, f_tmax, -1, f_c, p);
+    push_shadow(P, so1, sd1, sc1, kSH1, e_pred, spos, e_dir, kBigT, -1, e_c, p);
+}
+
+template <int kEst>
+__global__ void __launch_bounds__(128) k_shade(Params P, const int *sq0, const int *sq1, const int *sq2,
+                                               int *next_q, int next_cnt, float4 *so0, float4 *sd0, float4 *sc0,
+                                               float4 *so1, float4 *sd1, float4 *sc1) {
+    const int n0 = P.cnt[kSQ0], n1 = P.cnt[kSQ1], n2 = P.cnt[kSQ2];
+    const int n = n0 + n1 + n2;
+    for (int base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+        const int i = base + threadIdx.x;
+        const bool valid = i < n;
+        int p = 0;
+        if (valid) p = i < n0 ? sq0[i] : (i < n0 + n1 ? sq1[i - n0] : sq2[i - n0 - n1]);
+        if (kEst == KGK_ESTIMATOR_COMPAT)
+            shade_compat(P, p, valid, next_q, next_cnt, so0, sd0, sc0, so1, sd1, sc1);
+        else
+            shade_unbiased(P, p, valid, next_q, next_cnt, so0, sd0, sc0, so1, sd1, sc1);
+    }
+}
+
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) k_shadow(Params P, int cidx, const float4 *__restrict__ so,
+                                                const float4 *__restrict__ sd, const float4 *__restrict__ sc) {
+    const int n = P.cnt[cidx];
+    const DevScene &s = P.sc;
+    for (int base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+        const int i = base + threadIdx.x;
+        const bool valid = i < n;
+        TravStats st{0, 0, 0};
+        if (valid) {
+            const float4 o = so[i], d = sd[i], c = sc[i];
+            const RayPre r = make_ray(f3(o), f3(d));
+            const int light = __float_as_int(d.w);
+            bool vis;
+            if (light >= 0) {
+                // the reference's test: the closest hit must be the sampled light
+                float bt = o.w, u, v;
+                int bid = 0x7fffffff;
+                const int slot = trace_closest<false>(s.nodes, (unsigned)s.n_nodes, s.tri_rec, (unsigned)s.n_tris,
+                                                      r, bt, bid, u, v, st);
+                vis = slot >= 0 && bid == light;
+            } else {
+                vis = !trace_any<false>(s.nodes, (unsigned)s.n_nodes, s.tri_rec, (unsigned)s.n_tris, r, o.w, st);
+            }
+            if (vis) {
+                const int p = __float_as_int(c.w);
+                float4 rr = P.rad[p];
+                rr.x += c.x;
+                rr.y += c.y;
+                rr.z += c.z;
+                P.rad[p] = rr;
+            }
+        }
+        warp_add_u64(&P.stats[kRaysS], valid ? 1u : 0u);
+        warp_add_u64(&P.stats[kOverflow], st.overflow);
+    }
+}
+
+// Sums the wave's samples per pixel (fixed order) into the frame buffer and
+// the FP64 accumulator.
+__global__ void k_finish(Params P, float4 *frame, double *acc_sum, double *acc_sq, int accumulate, int first_wave) {
+    for (int px = blockIdx.x * blockDim.x + threadIdx.x; px < P.npx; px += gridDim.x * blockDim.x) {
+        float4 f = first_wave ? make_float4(0.0f, 0.0f, 0.0f, 0.0f) : frame[px];
+        double s0 = 0, s1 = 0, s2 = 0, q0 = 0, q1 = 0, q2 = 0;
+        for (int k = 0; k < P.spp_wave; ++k) {
+            const float4 r = P.rad[k * P.npx + px];
+            f.x += r.x;
+            f.y += r.y;
+            f.z += r.z;
+            if (accumulate) {
+                s0 += r.x; s1 += r.y; s2 += r.z;
+                q0 += (double)r.x * r.x; q1 += (double)r.y * r.y; q2 += (double)r.z * r.z;
+            }
+        }
+        frame[px] = f;
+        if (accumulate) {
+            acc_sum[3 * px] += s0; acc_sum[3 * px + 1] += s1; acc_sum[3 * px + 2] += s2;
+            acc_sq[3 * px] += q0; acc_sq[3 * px + 1] += q1; acc_sq[3 * px + 2] += q2;
+        }
+    }
+}
+
+__global__ void k_output(const float4 *frame, int npx, float inv_spp, float4 *out) {
+    for (int px = blockIdx.x * blockDim.x + threadIdx.x; px < npx; px += gridDim.x * blockDim.x) {
+        const float4 f = frame[px];
+        out[px] = make_float4(f.x * inv_spp, f.y * inv_spp, f.z * inv_spp, 1.0f);
+    }
+}
+
+template <class T> kgk_status ensure(T **p, size_t n, const char *what) {
+    dfree(*p);
+    *p = nullptr;
+    return dalloc(p, n, what);
+}
+
+kgk_status ensure_pixels(RenderState &R, int W, int H) {
+    if (R.W == W && R.H == H && R.seeds) return KGK_OK;
+    const size_t npx = (size_t)W * H;
+    KGK_TRY(ensure(&R.seeds, npx, "per-pixel seeds"));
+    KGK_CUDA(cudaMemset(R.seeds, 0, npx * sizeof(unsigned long long)));
+    KGK_TRY(ensure(&R.frame, npx, "frame buffer"));
+    KGK_TRY(ensure(&R.gb_pos, npx, "G-buffer"));
+    KGK_TRY(ensure(&R.gb_nrm, npx, "G-buffer"));
+    KGK_TRY(ensure(&R.gb_alb, npx, "G-buffer"));
+    KGK_TRY(ensure(&R.gb_emi, npx, "G-buffer"));
+    R.W = W;
+    R.H = H;
+    return KGK_OK;
+}
+
+kgk_status ensure_wave(RenderState &R, int cap) {
+    if (R.cap >= cap) return KGK_OK;
+    KGK_TRY(ensure(&R.o, cap, "path state"));
+    KGK_TRY(ensure(&R.d, cap, "path state"));
+    KGK_TRY(ensure(&R.thr, cap, "path state"));
+    KGK_TRY(ensure(&R.rad, cap, "path state"));
+    KGK_TRY(ensure(&R.hit, cap, "path state"));
+    KGK_TRY(ensure(&R.rng, cap, "path state"));
+    KGK_TRY(ensure(&R.depth, cap, "path state"));
+    for (int k = 0; k < 2; ++k) KGK_TRY(ensure(&R.aq[k], cap, "path queue"));
+    for (int k = 0; k < 3; ++k) KGK_TRY(ensure(&R.sq[k], cap, "shade queue"));
+    for (int k = 0; k < 2; ++k) {
+        KGK_TRY(ensure(&R.sh_o[k], cap, "shadow queue"));
+        KGK_TRY(ensure(&R.sh_d[k], cap, "shadow queue"));
+        KGK_TRY(ensure(&R.sh_c[k], cap, "shadow queue"));
+    }
+    R.cap = cap;
+    return KGK_OK;
+}
+
+}  // namespace
+
 void render_state_free(kgk_scene *s) {
-    delete s->rs;
+    RenderState *R = s->rs;
+    if (!R) return;
+    void *ptrs[] = {R->seeds, R->frame, R->acc_sum, R->acc_sq, R->gb_pos, R->gb_nrm, R->gb_alb, R->gb_emi,
+                    R->o, R->d, R->thr, R->rad, R->hit, R->rng, R->depth, R->aq[0], R->aq[1], R->sq[0],
+                    R->sq[1], R->sq[2], R->sh_o[0], R->sh_o[1], R->sh_d[0], R->sh_d[1], R->sh_c[0],
+                    R->sh_c[1], R->cnt, R->stats};
+    for (void *p : ptrs) dfree(p);
+    delete R;
     s->rs = nullptr;
 }
+
+RenderState *render_state(kgk_scene *s) {
+    if (!s->rs) s->rs = new RenderState();
+    return s->rs;
+}
+
 }  // namespace kgk
 
 using namespace kgk;
 
 extern "C" {
-kgk_status kgk_render(kgk_scene *, const kgk_camera *, const kgk_camera *, const kgk_render_config *, kgk_vec *,
-                      kgk_stats *) {
-    return fail(KGK_ERR_UNSUPPORTED, "kgk_render: not built yet");
+
+kgk_status kgk_render(kgk_scene *s, const kgk_camera *cam, const kgk_camera *prev_cam,
+                      const kgk_render_config *cfg, kgk_vec *out, kgk_stats *stats) {
+    (void)prev_cam;
+    if (!s || !cam || !cfg || !out) return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_render: NULL argument");
+    if (!s->built) return fail(KGK_ERR_NOT_BUILT, "kgk_render: call kgk_build_bvh first");
+    if (cfg->width <= 0 || cfg->height <= 0 || (long long)cfg->width * cfg->height > (1LL << 26))
+        return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_render: image size out of range");
+    if (cfg->spp <= 0) return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_render: spp must be positive");
+    if (cfg->estimator != KGK_ESTIMATOR_COMPAT && cfg->estimator != KGK_ESTIMATOR_UNBIASED)
+        return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_render: unknown estimator");
+    if (cfg->use_cache) return fail(KGK_ERR_UNSUPPORTED, "kgk_render: use the radiance-cache entry point");
+    KGK_CUDA(cudaSetDevice(s->device));
+    RenderState &R = *render_state(s);
+    const int W = cfg->width, H = cfg->height, npx = W * H;
+    KGK_TRY(ensure_pixels(R, W, H));
+    if (cfg->estimator == KGK_ESTIMATOR_COMPAT && cfg->frame_index == 0)
+        KGK_CUDA(cudaMemsetAsync(R.seeds, 0, (size_t)npx * sizeof(unsigned long long), s->stream));
+    // samples per wave: compat chains the per-pixel seeds, one sample per wave
+    int spw = 1;
+    if (cfg->estimator == KGK_ESTIMATOR_UNBIASED) {
+        const int target = cfg->wave_paths > 0 ? cfg->wave_paths : (1 << 22);
+        spw = std::max(1, std::min(cfg->spp, target / std::max(npx, 1)));
+    }
+    KGK_TRY(ensure_wave(R, npx * spw));
+    if (!R.cnt) KGK_TRY(dalloc(&R.cnt, kNCnt, "counters"));
+    if (!R.stats) KGK_TRY(dalloc(&R.stats, kNStat, "counters"));
+    if (cfg->accumulate) {
+        if (!R.acc_sum || R.acc_W != W || R.acc_H != H)
+            return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_render: accumulate needs kgk_accum_reset for this size");
+    }
+    if (!R.sms) {
+        cudaDeviceProp prop;
+        KGK_CUDA(cudaGetDeviceProperties(&prop, s->device));
+        R.sms = prop.multiProcessorCount;
+    }
+    cudaStream_t st = s->stream;
+    KGK_CUDA(cudaMemsetAsync(R.stats, 0, kNStat * sizeof(unsigned long long), st));
+    Params P;
+    memset(&P, 0, sizeof P);
+    P.sc = s->dev;
+    P.cam = *cam;
+    P.W = W;
+    P.H = H;
+    P.npx = npx;
+    P.estimator = cfg->estimator;
+    P.max_depth = cfg->max_depth;
+    P.rr_start = cfg->rr_start_depth;
+    P.write_gbuffer = cfg->write_gbuffer;
+    P.count_work = cfg->count_work;
+    P.seed = cfg->seed;
+    P.frame_index = cfg->frame_index;
+    P.o = R.o; P.d = R.d; P.thr = R.thr; P.rad = R.rad; P.hit = R.hit; P.rng = R.rng; P.depth = R.depth;
+    P.seeds = R.seeds;
+    P.gb_pos = R.gb_pos; P.gb_nrm = R.gb_nrm; P.gb_alb = R.gb_alb; P.gb_emi = R.gb_emi;
+    P.cnt = R.cnt;
+    P.stats = R.stats;
+    const int grid = R.sms * 8;   // persistent grid-stride launches, 128 threads per block
+    cudaEvent_t e0, e1;
+    KGK_CUDA(cudaEventCreate(&e0));
+    KGK_CUDA(cudaEventCreate(&e1));
+    KGK_CUDA(cudaEventRecord(e0, st));
+    const int max_bounces = cfg->max_depth > 0 ? cfg->max_depth : 1024;
+    uint64_t launches = 0;
+    // optional per-stage timing: an event before and after every stage launch
+    const bool prof = cfg->profile_stages != 0;
+    std::vector<cudaEvent_t> ev;
+    std::vector<int> ev_stage;  // 0 extend, 1 shade, 2 shadow
+    auto stage_begin = [&](int stage) -> kgk_status {
+        if (!prof) return KGK_OK;
+        cudaEvent_t a;
+        KGK_CUDA(cudaEventCreate(&a));
+        KGK_CUDA(cudaEventRecord(a, st));
+        ev.push_back(a);
+        ev_stage.push_back(stage);
+        return KGK_OK;
+    };
+    auto stage_end = [&]() -> kgk_status {
+        if (!prof) return KGK_OK;
+        cudaEvent_t b;
+        KGK_CUDA(cudaEventCreate(&b));
+        KGK_CUDA(cudaEventRecord(b, st));
+        ev.push_back(b);
+        ev_stage.push_back(-1);
+        return KGK_OK;
+    };
+    for (int done = 0, wave = 0; done < cfg->spp; done += spw, ++wave) {
+        P.spp_wave = std::min(spw, cfg->spp - done);
+        P.sample_base = done;
+        const int n = npx * P.spp_wave;
+        k_raygen<<<grid, 128, 0, st>>>(P);
+        ++launches;
+        int cur = 0;
+        for (int b = 0; b < max_bounces; ++b) {
+            KGK_CUDA(cudaMemsetAsync(R.cnt + kSQ0, 0, 5 * sizeof(int), st));
+            KGK_CUDA(cudaMemsetAsync(R.cnt + (cur ^ 1), 0, sizeof(int), st));
+            const int *q = b == 0 ? nullptr : R.aq[cur];
+            KGK_TRY(stage_begin(0));
+            if (cfg->count_work)
+                k_extend<true><<<grid, 128, 0, st>>>(P, q, cur, n, R.sq[0], R.sq[1], R.sq[2]);
+            else
+                k_extend<false><<<grid, 128, 0, st>>>(P, q, cur, n, R.sq[0], R.sq[1], R.sq[2]);
+            KGK_TRY(stage_end());
+            KGK_TRY(stage_begin(1));
+            if (cfg->estimator == KGK_ESTIMATOR_COMPAT)
+                k_shade<KGK_ESTIMATOR_COMPAT><<<grid, 128, 0, st>>>(P, R.sq[0], R.sq[1], R.sq[2], R.aq[cur ^ 1],
+                                                                  cur ^ 1, R.sh_o[0], R.sh_d[0], R.sh_c[0],
+                                                                  R.sh_o[1], R.sh_d[1], R.sh_c[1]);
+            else
+                k_shade<KGK_ESTIMATOR_UNBIASED><<<grid, 128, 0, st>>>(P, R.sq[0], R.sq[1], R.sq[2],
+                                                                    R.aq[cur ^ 1], cur ^ 1, R.sh_o[0],
+                                                                    R.sh_d[0], R.sh_c[0], R.sh_o[1],
+                                                                    R.sh_d[1], R.sh_c[1]);
+            KGK_TRY(stage_end());
+            KGK_TRY(stage_begin(2));
+            k_shadow<<<grid, 128, 0, st>>>(P, kSH0, R.sh_o[0], R.sh_d[0], R.sh_c[0]);
+            k_shadow<<<grid, 128, 0, st>>>(P, kSH1, R.sh_o[1], R.sh_d[1], R.sh_c[1]);
+            KGK_TRY(stage_end());
+            KGK_CUDA(cudaGetLastError());
+            launches += 4;
+            cur ^= 1;
+            if ((b & 3) == 3) {
+                int alive = 0;
+                KGK_CUDA(cudaMemcpyAsync(&alive, R.cnt + cur, sizeof(int), cudaMemcpyDeviceToHost, st));
+                KGK_CUDA(cudaStreamSynchronize(st));
+                if (alive == 0) break;
+            }
+        }
+        k_finish<<<(npx + 255) / 256, 256, 0, st>>>(P, R.frame, R.acc_sum, R.acc_sq, cfg->accumulate, wave == 0);
+        KGK_CUDA(cudaGetLastError());
+        ++launches;
+    }
+    if (cfg->accumulate) R.acc_n += (unsigned long long)cfg->spp;
+    // output
+    const bool od = is_device_ptr(out);
+    float4 *dout;
+    if (od) {
+        dout = reinterpret_cast<float4 *>(out);
+    } else {
+        KGK_TRY(s->staging.reserve((size_t)npx * sizeof(float4)));
+        dout = reinterpret_cast<float4 *>(s->staging.ptr);
+    }
+    k_output<<<(npx + 255) / 256, 256, 0, st>>>(R.frame, npx, 1.0f / (float)cfg->spp, dout);
+    KGK_CUDA(cudaGetLastError());
+    ++launches;
+    KGK_CUDA(cudaEventRecord(e1, st));
+    if (!od) KGK_CUDA(cudaMemcpyAsync(out, dout, (size_t)npx * sizeof(float4), cudaMemcpyDeviceToHost, st));
+    unsigned long long hs[kNStat];
+    KGK_CUDA(cudaMemcpyAsync(hs, R.stats, sizeof hs, cudaMemcpyDeviceToHost, st));
+    KGK_CUDA(cudaStreamSynchronize(st));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (stats) {
+        memset(stats, 0, sizeof *stats);
+        stats->rays_closest = hs[kRaysC];
+        stats->rays_shadow = hs[kRaysS];
+        stats->traversal_overflows = hs[kOverflow];
+        stats->nodes_visited = hs[kNodes];
+        stats->tris_tested = hs[kTris];
+        stats->paths = (uint64_t)npx * (uint64_t)cfg->spp;
+        stats->ms_device = ms;
+        stats->kernel_launches = launches;
+        double stage_ms[3] = {0, 0, 0};
+        for (size_t k = 0; k + 1 < ev.size(); k += 2) {
+            float m = 0;
+            cudaEventElapsedTime(&m, ev[k], ev[k + 1]);
+            stage_ms[ev_stage[k]] += m;
+        }
+        stats->ms_extend = stage_ms[0];
+        stats->ms_shade = stage_ms[1];
+        stats->ms_shadow = stage_ms[2];
+    }
+    for (cudaEvent_t e : ev) cudaEventDestroy(e);
+    if (hs[kOverflow])
+        return fail(KGK_ERR_DEVICE_CHECK, "kgk_render: " + std::to_string(hs[kOverflow]) +
+                                              " traversals overflowed their stack");
+    return KGK_OK;
 }
-kgk_status kgk_accum_reset(kgk_scene *, int32_t, int32_t) {
-    return fail(KGK_ERR_UNSUPPORTED, "kgk_accum_reset: not built yet");
+
+kgk_status kgk_accum_reset(kgk_scene *s, int32_t W, int32_t H) {
+    if (!s) return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_accum_reset: scene == NULL");
+    if (W <= 0 || H <= 0 || (long long)W * H > (1LL << 26))
+        return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_accum_reset: size out of range");
+    KGK_CUDA(cudaSetDevice(s->device));
+    RenderState &R = *render_state(s);
+    const size_t n = (size_t)W * H * 3;
+    if (R.acc_W != W || R.acc_H != H || !R.acc_sum) {
+        KGK_TRY(ensure(&R.acc_sum, n, "FP64 accumulator"));
+        KGK_TRY(ensure(&R.acc_sq, n, "FP64 accumulator"));
+        R.acc_W = W;
+        R.acc_H = H;
+    }
+    KGK_CUDA(cudaMemsetAsync(R.acc_sum, 0, n * sizeof(double), s->stream));
+    KGK_CUDA(cudaMemsetAsync(R.acc_sq, 0, n * sizeof(double), s->stream));
+    KGK_CUDA(cudaStreamSynchronize(s->stream));
+    R.acc_n = 0;
+    return KGK_OK;
 }
-kgk_status kgk_accum_read(kgk_scene *, double *, double *, uint64_t *) {
-    return fail(KGK_ERR_UNSUPPORTED, "kgk_accum_read: not built yet");
+
+kgk_status kgk_accum_read(kgk_scene *s, double *mean, double *var, uint64_t *n_samples) {
+    if (!s || !mean) return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_accum_read: NULL argument");
+    RenderState *R = s->rs;
+    if (!R || !R->acc_sum) return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_accum_read: no accumulator (kgk_accum_reset)");
+    KGK_CUDA(cudaSetDevice(s->device));
+    const size_t n = (size_t)R->acc_W * R->acc_H * 3;
+    std::vector<double> sum(n), sq(n);
+    KGK_CUDA(cudaMemcpy(sum.data(), R->acc_sum, n * sizeof(double), cudaMemcpyDeviceToHost));
+    KGK_CUDA(cudaMemcpy(sq.data(), R->acc_sq, n * sizeof(double), cudaMemcpyDeviceToHost));
+    const double N = (double)R->acc_n;
+    for (size_t i = 0; i < n; ++i) {
+        const double m = N > 0 ? sum[i] / N : 0.0;
+        mean[i] = m;
+        if (var) var[i] = N > 1 ? std::max(0.0, (sq[i] - N * m * m) / (N - 1)) / N : 0.0;
+    }
+    if (n_samples) *n_samples = R->acc_n;
+    return KGK_OK;
 }
+
 kgk_status kgk_svgf(kgk_scene *, const kgk_svgf_config *, const kgk_vec *, kgk_vec *) {
     return fail(KGK_ERR_UNSUPPORTED, "kgk_svgf: not built yet");
 }
 kgk_status kgk_scene_load_obj(const char *, const char *, kgk_scene **) {
     return fail(KGK_ERR_UNSUPPORTED, "kgk_scene_load_obj: not built yet");
 }
-}
+
+}  // extern "C"

@@ -4,7 +4,8 @@
 // and Triangle::intersectTest (struct_Triangle.cuh:30-79) on the device.
 //
 // Semantics kept from the reference: a hit needs t >= 1e-5 (double compare,
-// struct_Triangle.cuh:57) and the result is the closest hit.  Where the
+// struct_Triangle.cuh:57), the result is the closest hit, and the reported
+// distance is computed by the reference's own expression (ref_distance).  Where the
 // reference resolves equal distances by its traversal order, this resolves
 // them to the smaller triangle id, independent of the tree.
 // Differences by design: the test is watertight (Woop, Benthin, Wald 2013)
@@ -81,6 +82,31 @@ __device__ __forceinline__ bool tri_intersect(const RayPre &r, float4 a4, float4
     *b1 = V / det;
     *b2 = W / det;
     return true;
+}
+
+// Distance and barycentrics of an accepted hit by the reference's own
+// expressions (struct_Triangle.cuh:46-49), every operation rounded
+// separately like the reference's host build: the reported t is the
+// reference's t bit for bit.  u = weight of v1, v = weight of v2.
+__device__ __forceinline__ float3 rn_sub(float3 a, float3 b) {
+    return f3(__fsub_rn(a.x, b.x), __fsub_rn(a.y, b.y), __fsub_rn(a.z, b.z));
+}
+__device__ __forceinline__ float3 rn_cross(float3 a, float3 b) {
+    return f3(__fsub_rn(__fmul_rn(a.y, b.z), __fmul_rn(a.z, b.y)),
+              __fsub_rn(__fmul_rn(a.z, b.x), __fmul_rn(a.x, b.z)),
+              __fsub_rn(__fmul_rn(a.x, b.y), __fmul_rn(a.y, b.x)));
+}
+__device__ __forceinline__ float rn_dot(float3 a, float3 b) {
+    return __fadd_rn(__fadd_rn(__fmul_rn(a.x, b.x), __fmul_rn(a.y, b.y)), __fmul_rn(a.z, b.z));
+}
+__device__ __forceinline__ void ref_distance(const RayPre &r, float4 a4, float4 b4, float4 c4, float *t, float *u,
+                                             float *v) {
+    const float3 v0 = f3(a4), e1 = rn_sub(f3(b4), v0), e2 = rn_sub(f3(c4), v0), so = rn_sub(r.o, v0);
+    const float3 de2 = rn_cross(r.d, e2), se1 = rn_cross(so, e1);
+    const float term1 = __fdiv_rn(1.0f, rn_dot(de2, e1));
+    *t = __fmul_rn(term1, rn_dot(se1, e2));
+    *u = __fmul_rn(term1, rn_dot(de2, so));
+    *v = __fmul_rn(term1, rn_dot(se1, r.d));
 }
 
 __device__ __forceinline__ unsigned byte_of(unsigned x, int i) { return (x >> (i * 8)) & 0xffu; }
@@ -182,6 +208,8 @@ __device__ __forceinline__ int trace_closest(const WideNode *__restrict__ nodes,
             if (kCount) ++st.tris;
             float t, u, v;
             if (tri_intersect(r, a, b, c, &t, &u, &v)) {
+                ref_distance(r, a, b, c, &t, &u, &v);
+                if (!(t >= kTMin)) continue;
                 const int id = __float_as_int(a.w);
                 if (t < best_t || (t == best_t && id < best_id)) {
                     best_t = t;
@@ -242,7 +270,10 @@ __device__ __forceinline__ bool trace_any(const WideNode *__restrict__ nodes, un
             const float4 a = __ldg(&tri[3 * ti]), b = __ldg(&tri[3 * ti + 1]), c = __ldg(&tri[3 * ti + 2]);
             if (kCount) ++st.tris;
             float t, u, v;
-            if (tri_intersect(r, a, b, c, &t, &u, &v) && t < tmax) return true;
+            if (tri_intersect(r, a, b, c, &t, &u, &v)) {
+                ref_distance(r, a, b, c, &t, &u, &v);
+                if (t >= kTMin && t < tmax) return true;
+            }
         }
         if ((group.y & 0xff000000u) == 0u) {
             if (sp == 0) break;

@@ -64,14 +64,17 @@ class KgkRenderConfig(ctypes.Structure):
                 ("seed", ctypes.c_uint64), ("frame_index", ctypes.c_int32),
                 ("accumulate", ctypes.c_int32), ("wave_paths", ctypes.c_int32),
                 ("count_work", ctypes.c_int32), ("write_gbuffer", ctypes.c_int32),
-                ("use_cache", ctypes.c_int32), ("reserved", ctypes.c_int32 * 6)]
+                ("use_cache", ctypes.c_int32), ("profile_stages", ctypes.c_int32),
+                ("reserved", ctypes.c_int32 * 5)]
 
 
 class KgkStats(ctypes.Structure):
     _fields_ = [("rays_closest", ctypes.c_uint64), ("rays_shadow", ctypes.c_uint64),
                 ("traversal_overflows", ctypes.c_uint64), ("nodes_visited", ctypes.c_uint64),
                 ("tris_tested", ctypes.c_uint64), ("paths", ctypes.c_uint64),
-                ("ms_device", ctypes.c_double), ("reserved", ctypes.c_double * 4)]
+                ("ms_device", ctypes.c_double), ("kernel_launches", ctypes.c_uint64),
+                ("ms_extend", ctypes.c_double), ("ms_shade", ctypes.c_double),
+                ("ms_shadow", ctypes.c_double)]
 
 
 class KgkBvhInfo(ctypes.Structure):

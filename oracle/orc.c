@@ -410,14 +410,9 @@ static int slab(const bnode *nd, const double *o, const double *inv, double tmax
     return t1 >= 0;
 }
 
-typedef struct { const orc_bvh *b; const Ray *rays; int32_t *id; float *t; } bvhq_ctx;
-
-static void bvhq_chunk(void *c_, int64_t i0, int64_t i1) {
-    bvhq_ctx *c = (bvhq_ctx *)c_;
-    const orc_bvh *b = c->b;
+static void bvh_closest_one(const orc_bvh *b, const Ray *r, int32_t *id_out, float *t_out) {
     int32_t stack[256];
-    for (int64_t i = i0; i < i1; ++i) {
-        const Ray *r = &c->rays[i];
+    {
         double o[3] = {r->org.x, r->org.y, r->org.z};
         double d[3] = {r->dir.x, r->dir.y, r->dir.z};
         double inv[3];
@@ -444,9 +439,16 @@ static void bvhq_chunk(void *c_, int64_t i0, int64_t i1) {
                 stack[sp++] = nd->left;
             }
         }
-        c->id[i] = bid;
-        c->t[i] = best;
+        *id_out = bid;
+        *t_out = best;
     }
+}
+
+typedef struct { const orc_bvh *b; const Ray *rays; int32_t *id; float *t; } bvhq_ctx;
+
+static void bvhq_chunk(void *c_, int64_t i0, int64_t i1) {
+    bvhq_ctx *c = (bvhq_ctx *)c_;
+    for (int64_t i = i0; i < i1; ++i) bvh_closest_one(c->b, &c->rays[i], &c->id[i], &c->t[i]);
 }
 
 void orc_bvh_closest(const orc_bvh *b, const void *rays, int64_t nrays, int32_t *face_id,
@@ -577,6 +579,9 @@ typedef struct {
     float *out;
     int64_t *rays; /* per-thread-chunk counts accumulate here under lock */
     pthread_mutex_t mu;
+    const orc_bvh *bvh;      /* NULL: brute-force closest hits */
+    const int32_t *px_list;  /* NULL: all pixels but 0 */
+    int64_t n_px;
 } rctx;
 
 /* Algorithms.cuh:6-20 */
@@ -591,6 +596,15 @@ static int lower_bound_f(const float *a, int64_t n, float k) {
 }
 
 static int closest(const rctx *c, const Ray *r, Hit *out, int *id) {
+    if (c->bvh) {
+        int32_t bid;
+        float bt;
+        bvh_closest_one(c->bvh, r, &bid, &bt);
+        *id = bid;
+        if (bid < 0) { out->distance = bINF; return 0; }
+        isect_full(&c->tris[bid], r, out, NULL, NULL);
+        return 1;
+    }
     float best = bINF;
     int bid = -1;
     Hit h;
@@ -627,6 +641,9 @@ static V uv_sphere(V d) {
 static V hdr_emission(const rctx *c, V d) {
     V uv = uv_sphere(d);
     int idx = c->hw * (int)((float)(c->hh - 1) * (1 - uv.y)) + (int)((float)(c->hw - 1) * (1 - uv.x));
+    /* a NaN direction (a degenerate sample) indexes nothing in the reference's
+     * defined behaviour; clamp like the device code */
+    if (idx < 0 || idx >= c->hw * c->hh) idx = idx < 0 ? 0 : c->hw * c->hh - 1;
     idx *= c->hbpp;
     return mk(c->hdr[idx], c->hdr[idx + 1], c->hdr[idx + 2]);
 }
@@ -646,6 +663,7 @@ static float hdr_pdf(const rctx *c, V d) {
     V uv = uv_sphere(d);
     int idx = (c->hw * (int)((float)c->hh * (1.0f - uv.y)) + (int)((float)c->hw * (uv.x)));
     if (idx >= c->hw * c->hh) idx = c->hw * c->hh - 1; /* reference reads one past the end */
+    if (idx < 0) idx = 0;
     if (idx == 0) return c->lssh[0] / c->lssh[c->lssh_n - 1];
     return (c->lssh[idx] - c->lssh[idx - 1]) / c->lssh[c->lssh_n - 1];
 }
@@ -834,10 +852,12 @@ static void nee_face(const rctx *c, V *rad, V T, uint64_t *s, const Ray *ray, co
     int id;
     if (c->no_light) id = -1;
     else id = lower_bound_f(c->lss, c->lss_n, R * c->lss[c->lss_n - 1]);
-    if (id < 0) return;
     float r1, r2;
     if (g_point_args_rtl) { r2 = RND(s, 0, 1); r1 = RND(s, 0, 1); }
     else { r1 = RND(s, 0, 1); r2 = RND(s, 0, 1); }
+    /* no face light: the reference samples Objects[-1] (undefined); here the
+     * step draws its three numbers and contributes nothing */
+    if (id < 0) return;
     V P = sample_point_on_tri(r1, r2, &c->tris[id]);
     V L = normalize(vsub(P, hp->position));
     float dist = len(vsub(P, hp->position));
@@ -999,7 +1019,8 @@ static void render_chunk(void *c_, int64_t i0, int64_t i1) {
     int64_t nr = 0;
     const int64_t npx = (int64_t)c->W * c->H;
     for (int64_t i = i0; i < i1; ++i) {
-        int pos = (int)(i + 1);
+        int pos = c->px_list ? (int)c->px_list[i] : (int)(i + 1);
+        if (pos <= 0 || pos >= npx) continue;
         int X = pos % c->W, Y = pos / c->W;
         uint64_t s = c->seeds[pos];
         for (int f = 0; f < c->frames; ++f) {
@@ -1094,4 +1115,64 @@ void orc_disney_eval(const void *mat, int n, const float *wo, const float *wi, c
         brdf[3 * i + 2] = b.z;
         pdf[i] = disney_pdf(p.wt, in, o, N, u, v, w, p.ax, p.ay, p.ac);
     }
+}
+
+/* The compat estimator over a list of pixels (1..W*H-1) of a W x H frame,
+ * one sample each, with closest hits from a CPU BVH (orc_bvh_build); for
+ * scenes too large for brute force.  out = n_px * 3 floats (pixel order of
+ * the list).  Returns the number of traversal calls. */
+int64_t orc_render_compat_px(const void *tris, int64_t n, const void *mats, const orc_bvh *bvh,
+                             const float *hdr, int hdr_w, int hdr_h, int hdr_bpp, const void *cam,
+                             int width, int height, const int32_t *px_list, int64_t n_px, int nthreads,
+                             float *out) {
+    rctx c;
+    memset(&c, 0, sizeof c);
+    c.tris = (const Tri *)tris;
+    c.n = n;
+    c.mats = (const Mat *)mats;
+    c.hdr = hdr;
+    c.hw = hdr_w;
+    c.hh = hdr_h;
+    c.hbpp = hdr_bpp;
+    float *lss = (float *)malloc(sizeof(float) * (size_t)(n > 0 ? n : 1));
+    orc_light_cdf(tris, n, mats, lss);
+    c.lss = lss;
+    c.lss_n = n;
+    c.no_light = n > 0 && lss[n - 1] == 0;
+    float *lssh = NULL;
+    c.no_hdr = hdr == NULL;
+    if (hdr) {
+        lssh = (float *)malloc(sizeof(float) * (size_t)hdr_w * hdr_h);
+        orc_env_cdf(hdr, hdr_w, hdr_h, hdr_bpp, lssh);
+        c.lssh = lssh;
+        c.lssh_n = (int64_t)hdr_w * hdr_h;
+    }
+    memcpy(&c.cam, cam, sizeof(Cam));
+    c.W = width;
+    c.H = height;
+    c.frames = 1;
+    const int64_t npx = (int64_t)width * height;
+    c.seeds = (uint64_t *)calloc((size_t)npx, sizeof(uint64_t));
+    float *full = (float *)calloc((size_t)npx * 3, sizeof(float));
+    c.out = full;
+    int64_t rays = 0;
+    c.rays = &rays;
+    c.bvh = bvh;
+    c.px_list = px_list;
+    c.n_px = n_px;
+    pthread_mutex_init(&c.mu, NULL);
+    parallel_for(n_px, nthreads, 4, render_chunk, &c);
+    pthread_mutex_destroy(&c.mu);
+    for (int64_t k = 0; k < n_px; ++k) {
+        int64_t p = px_list[k];
+        if (p <= 0 || p >= npx) continue;
+        out[3 * k] = full[3 * p];
+        out[3 * k + 1] = full[3 * p + 1];
+        out[3 * k + 2] = full[3 * p + 2];
+    }
+    free(full);
+    free(c.seeds);
+    free(lss);
+    free(lssh);
+    return rays;
 }

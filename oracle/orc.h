@@ -76,6 +76,11 @@ int64_t orc_render_compat(const void *tris, int64_t n, const void *mats, int64_t
  * viewer) and evaluate_Disney_BRDF_pdf (Disney_BRDF.cuh:118-183). */
 void orc_disney_eval(const void *mat, int n, const float *wo, const float *wi, const float *nrm,
                      float *brdf, float *pdf);
+/* The compat estimator over a pixel list with closest hits from a CPU BVH. */
+int64_t orc_render_compat_px(const void *tris, int64_t n, const void *mats, const orc_bvh *bvh,
+                             const float *hdr, int hdr_w, int hdr_h, int hdr_bpp, const void *cam,
+                             int width, int height, const int32_t *px_list, int64_t n_px, int nthreads,
+                             float *out);
 /* Selects the argument order of SamplePointOnTriangle's two random numbers
  * (1 = right to left, the reference host build's order). */
 void orc_set_point_arg_order(int rtl);

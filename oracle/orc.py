@@ -59,6 +59,9 @@ def orc():
         L.orc_render_compat.restype = _i64
         L.orc_set_point_arg_order.argtypes = [_i32]
         L.orc_disney_eval.argtypes = [_vp, _i32, _vp, _vp, _vp, _vp, _vp]
+        L.orc_render_compat_px.argtypes = [_vp, _i64, _vp, _vp, _vp, _i32, _i32, _i32, _vp, _i32, _i32,
+                                           _vp, _i64, _i32, _vp]
+        L.orc_render_compat_px.restype = _i64
         _orc = L
     return _orc
 
@@ -146,6 +149,40 @@ def render_compat(tris, mats, cam, width, height, frames, env=None, threads=None
     n = orc().orc_render_compat(_ptr(tris), len(tris), _ptr(mats), len(mats), None, 0, env_p, hw,
                                 hh, hb, _ptr(cam), width, height, frames,
                                 threads or nthreads(), _ptr(out))
+    return out, n
+
+
+class CpuBvh:
+    """A CPU BVH of the oracle, built once and reused."""
+
+    def __init__(self, tris):
+        self.tris = np.ascontiguousarray(tris)
+        self.h = orc().orc_bvh_build(_ptr(self.tris), len(self.tris))
+
+    def close(self):
+        if self.h:
+            orc().orc_bvh_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+
+def render_compat_px(bvh, mats, cam, width, height, px_list, env=None, threads=None):
+    """Compat estimator, one sample for each pixel of px_list, closest hits
+    from the CPU BVH.  Returns (n_px, 3) float32 and the traversal count."""
+    px = np.ascontiguousarray(px_list, np.int32)
+    out = np.zeros((len(px), 3), np.float32)
+    env_p, hw, hh, hb = None, 0, 0, 0
+    if env is not None:
+        env = np.ascontiguousarray(env, np.float32)
+        hh, hw, hb = env.shape
+        env_p = _ptr(env)
+    cam = np.ascontiguousarray(cam, np.float32)
+    mats = np.ascontiguousarray(mats)
+    n = orc().orc_render_compat_px(_ptr(bvh.tris), len(bvh.tris), _ptr(mats), bvh.h, env_p, hw, hh, hb,
+                                   _ptr(cam), width, height, _ptr(px), len(px), threads or nthreads(),
+                                   _ptr(out))
     return out, n
 
 
