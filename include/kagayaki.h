@@ -276,10 +276,34 @@ typedef struct kgk_svgf_config {
     int32_t reserved[6];
 } kgk_svgf_config;
 
-/* Filters the frame last rendered with write_gbuffer=1.  noisy is read and
- * filtered is written (both width*height kgk_vec, host or device). */
+/* Filters the frame last rendered with write_gbuffer=1 (its G-buffer, and
+ * for KGK_SVGF_STANDARD the camera it was rendered with).  noisy is read and
+ * filtered is written (both width*height kgk_vec, host or device).  The
+ * filter keeps its history in the scene handle. */
 kgk_status kgk_svgf(kgk_scene *scene, const kgk_svgf_config *cfg, const kgk_vec *noisy,
                     kgk_vec *filtered);
+
+/* struct_SVGFBuffers.cuh:7-23 `SVGFBuffer`, 112 B: the reference's per-pixel
+ * G-buffer and filter state. */
+typedef struct kgk_svgf_buffer {
+    kgk_vec Albedo, Emission, Normal, ColorHistory;
+    int32_t ObjectID, MaterialID;
+    int32_t PosLastFrameI[2];
+    float PosLastFrameF[2];
+    int32_t sampleNum;
+    float MomentOne, MomentTwo, Variance, Depth;
+    bool willApplyATrousFilter, willApplyTemporalAccumulation;
+} kgk_svgf_buffer;
+
+/* ApplySVGF (SVGF.cuh:495-522) over the reference's own buffers, in its
+ * race-free reading (a full-image barrier at every __syncthreads): result is
+ * read and rewritten (ColorHistory at the end, SVGF.cuh:492), filtered
+ * receives the output image, cur is updated like the reference updates it,
+ * prev is read (and initialised when frame == 0).  All arrays hold
+ * width*height records, host or device.  Uses the current device and its own
+ * stream; synchronous. */
+kgk_status kgk_svgf_apply(kgk_vec *result, kgk_vec *filtered, kgk_svgf_buffer *prev,
+                          kgk_svgf_buffer *cur, int32_t width, int32_t height, int32_t frame);
 
 /* ------------------------------------------------------------------------- */
 /* Image output (replaces save_png, FileIO/IO_save_png.cuh:34-56)              */

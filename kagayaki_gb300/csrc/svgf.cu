@@ -1,0 +1,846 @@
+// svgf.cu - spatiotemporal variance-guided filtering.
+//
+// compat: ApplySVGF (SVGF.cuh:495-522) over the reference's own 112-byte
+//   SVGFBuffer records.  Every __syncthreads of the reference, which it uses
+//   as if it were a grid barrier, becomes a kernel boundary here, and reads
+//   that precede a barrier while writes follow it are double-buffered: this
+//   is the race-free reading of the filter, with its constants and quirks
+//   (absolute pixel coordinates in the a-trous depth weight, SVGF.cuh:426;
+//   the 5 x 5 stage loop, SVGF.cuh:486-491; the 0.2 blend, SVGF.cuh:459-464).
+// standard: SVGF with reprojection of the previous frame from the previous
+//   camera, temporal integration of colour and luminance moments (alpha),
+//   spatial variance fallback, `atrous_iterations` edge-stopping a-trous
+//   passes (sigma_z, sigma_n, sigma_l) on albedo-demodulated lighting, the
+//   first pass feeding the next frame's history.
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "kgk_device.cuh"
+#include "kgk_scene.h"
+
+static_assert(sizeof(kgk_svgf_buffer) == 112, "SVGFBuffer must be 112 B (struct_SVGFBuffers.cuh:7-23)");
+static_assert(offsetof(kgk_svgf_buffer, ObjectID) == 64, "SVGFBuffer.ObjectID offset");
+static_assert(offsetof(kgk_svgf_buffer, sampleNum) == 88, "SVGFBuffer.sampleNum offset");
+static_assert(offsetof(kgk_svgf_buffer, Depth) == 104, "SVGFBuffer.Depth offset");
+static_assert(offsetof(kgk_svgf_buffer, willApplyATrousFilter) == 108, "SVGFBuffer flag offset");
+
+namespace kgk {
+
+struct RenderState;
+struct SvgfState {
+    int W = 0, H = 0;
+    // compat
+    kgk_svgf_buffer *prev = nullptr, *cur = nullptr;
+    // standard (SoA)
+    float4 *hist = nullptr, *hist_prev = nullptr;      // demodulated colour history, w = history length
+    float2 *mom = nullptr, *mom_prev = nullptr;        // luminance moments
+    float4 *nd_prev = nullptr;                         // previous normal + depth
+    int *mat_prev = nullptr;                           // previous material id (-1 = no hit)
+    float4 *col = nullptr, *tmp = nullptr;             // colour + variance ping-pong
+    float *gvar = nullptr;                             // 3x3-blurred variance
+    kgk_camera prev_cam{};
+    bool has_prev = false;
+};
+
+SvgfState *svgf_state(kgk_scene *s);
+void svgf_state_free(kgk_scene *s);
+bool svgf_gbuffer(kgk_scene *s, int *W, int *H, const float4 **pos, const float4 **nrm, const float4 **alb,
+                  const float4 **emi, kgk_camera *cam);
+
+namespace {
+
+constexpr float kS = 1e-4f;  // sINF
+
+__device__ __forceinline__ float3 v3(kgk_vec v) { return f3(v.x, v.y, v.z); }
+__device__ __forceinline__ kgk_vec kv(float3 a) { kgk_vec r; r.x = a.x; r.y = a.y; r.z = a.z; r.align = 0.0f; return r; }
+__device__ __forceinline__ float lumf(float3 c) { return 0.2126f * c.x + 0.7152f * c.y + 0.0722f * c.z; }
+__device__ __forceinline__ float3 div3(float3 a, float3 b) { return f3(a.x / b.x, a.y / b.y, a.z / b.z); }
+
+__device__ __forceinline__ void sb_init(kgk_svgf_buffer &b) {
+    const kgk_vec z = {0, 0, 0, 0};
+    b.Albedo = b.Emission = b.Normal = b.ColorHistory = z;
+    b.ObjectID = -1;
+    b.MaterialID = -1;
+    b.PosLastFrameI[0] = b.PosLastFrameI[1] = -1;
+    b.PosLastFrameF[0] = b.PosLastFrameF[1] = -1.0f;
+    b.sampleNum = 0;
+    b.MomentOne = -1.0f;
+    b.MomentTwo = -1.0f;
+    b.Variance = 0.0f;
+    b.Depth = 0.0f;
+    b.willApplyATrousFilter = true;
+    b.willApplyTemporalAccumulation = false;
+}
+
+__device__ __forceinline__ float depth_w(float d, float nd, int dx, int dy, float gx, float gy) {
+    const float top = -1.0f * fabsf(d - nd);
+    const float bottom = 1.0f * fabsf((float)dx * gx + (float)dy * gy) + kS;
+    return expf(top / bottom);
+}
+__device__ __forceinline__ float normal_w(float3 n, float3 m) {
+    float c = fmaxf(0.0f, dot3(n, m));
+    c *= c; c *= c; c *= c; c *= c; c *= c; c *= c; c *= c;  // ^128
+    return c;
+}
+__device__ __forceinline__ float lum_w(float l, float nl, float sd) {
+    const float top = -1.0f * fabsf(l - nl);
+    const float bottom = 4.0f * sd + kS;
+    return expf(top / bottom);
+}
+
+struct CompatArgs {
+    int W, H, frame;
+    kgk_vec *R, *F;
+    kgk_svgf_buffer *P, *C;
+    float *M1, *M2, *sd, *gz, *s1, *s2, *sw, *var;
+    unsigned char *spatial;
+    kgk_vec *R2;
+};
+
+#define FOR_PIXELS(n) for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < (n); p += gridDim.x * blockDim.x)
+
+__global__ void k_c_prologue(CompatArgs a) {
+    FOR_PIXELS(a.W * a.H) {
+        float3 r = v3(a.R[p]);
+        if (!isfinite(len3(r))) a.R[p] = kv(f3(0.0f, 0.0f, 0.0f));
+        if (a.frame == 0) sb_init(a.P[p]);
+        if (a.P[p].MomentOne == -1.0f) {
+            const float m1 = lumf(div3(v3(a.R[p]), v3(a.C[p].Albedo)));
+            a.C[p].MomentOne = m1;
+            a.C[p].MomentTwo = m1 * m1;
+        }
+        a.F[p] = kv(f3(0.0f, 0.0f, 0.0f));
+    }
+}
+
+// TemporalAccumulation (SVGF.cuh:50-98)
+__global__ void k_c_temporal(CompatArgs a) {
+    const int W = a.W, H = a.H;
+    FOR_PIXELS(W * H) {
+        const kgk_svgf_buffer &c = a.C[p];
+        if (len3(v3(c.Emission)) != 0.0f) continue;
+        const int px = c.PosLastFrameI[0], py = c.PosLastFrameI[1];
+        const float s = c.PosLastFrameF[0] - (float)px, t = c.PosLastFrameF[1] - (float)py;
+        const int ox[4] = {0, 1, 0, 1}, oy[4] = {0, 0, 1, 1};
+        const float w[4] = {(1 - s) * (1 - t), s * (1 - t), (1 - s) * t, s * t};
+        float3 sum = f3(0.0f, 0.0f, 0.0f);
+        float swt = 0.0f;
+        for (int i = 0; i < 4; ++i) {
+            const int qx = px + ox[i], qy = py + oy[i];
+            if (qx < 0 || qx >= W || qy < 0 || qy >= H) continue;
+            const kgk_svgf_buffer &q = a.P[W * qy + qx];
+            if (q.MaterialID == c.MaterialID && q.willApplyTemporalAccumulation) {
+                sum += v3(q.ColorHistory) * w[i];
+                swt += w[i];
+            }
+        }
+        if (swt == 0.0f) continue;
+        const float3 hist = sum / swt;
+        a.R[p] = kv(v3(a.R[p]) * 0.2f + hist * 0.8f);
+    }
+}
+
+// VarianceEstimation, before the first barrier (SVGF.cuh:114-145)
+__global__ void k_c_var1(CompatArgs a) {
+    const int W = a.W, H = a.H;
+    FOR_PIXELS(W * H) {
+        const int x = p % W, y = p / W;
+        const kgk_svgf_buffer &c = a.C[p];
+        const float l = lumf(div3(v3(a.R[p]), v3(c.Albedo) + f3(kS, kS, kS)));
+        a.M1[p] = l;
+        a.M2[p] = l * l;
+        bool sp = c.PosLastFrameI[0] == -1;
+        if (!sp) {
+            const int prev = W * c.PosLastFrameI[1] + c.PosLastFrameI[0];
+            sp = (prev < 0 || prev >= W * H) ? true : a.P[prev].sampleNum < 3;
+        }
+        a.spatial[p] = sp ? 1 : 0;
+        const int dx = x < W / 2 ? 1 : -1, dy = y < H / 2 ? 1 : -1;
+        const float d = c.Depth;
+        a.gz[2 * p] = (a.C[W * y + x + dx].Depth - d) / (float)dx;
+        a.gz[2 * p + 1] = (a.C[W * (y + dy) + x].Depth - d) / (float)dy;
+    }
+}
+
+__global__ void k_c_var2(CompatArgs a) {
+    const int W = a.W;
+    FOR_PIXELS(W * a.H) {
+        if (a.spatial[p]) continue;
+        kgk_svgf_buffer &c = a.C[p];
+        const int prev = W * c.PosLastFrameI[1] + c.PosLastFrameI[0];
+        c.sampleNum = a.P[prev].sampleNum + 1;
+        float cw = 1.0f / 5.0f;
+        if (c.sampleNum < 5) cw = 1.0f / (float)c.sampleNum;
+        c.MomentOne = (1.0f - cw) * a.P[prev].MomentOne + cw * a.M1[p];
+        c.MomentTwo = (1.0f - cw) * a.P[prev].MomentTwo + cw * a.M2[p];
+        a.M1[p] = c.MomentOne;
+        a.M2[p] = c.MomentTwo;
+    }
+}
+
+__constant__ float cK7[7] = {0.00598f, 0.060626f, 0.241843f, 0.383103f, 0.241843f, 0.060626f, 0.00598f};
+__constant__ float cKG[3] = {1 / 4.0f, 1 / 2.0f, 1 / 4.0f};
+__constant__ float cKW[25] = {1 / 256.0f, 4 / 256.0f, 6 / 256.0f, 4 / 256.0f, 1 / 256.0f,
+                              4 / 256.0f, 16 / 256.0f, 24 / 256.0f, 16 / 256.0f, 4 / 256.0f,
+                              6 / 256.0f, 24 / 256.0f, 36 / 256.0f, 24 / 256.0f, 6 / 256.0f,
+                              4 / 256.0f, 16 / 256.0f, 24 / 256.0f, 16 / 256.0f, 4 / 256.0f,
+                              1 / 256.0f, 4 / 256.0f, 6 / 256.0f, 4 / 256.0f, 1 / 256.0f};
+
+// 7x7 edge-stopped moment filter (SVGF.cuh:166-225)
+__global__ void k_c_var3(CompatArgs a) {
+    const int W = a.W, H = a.H;
+    FOR_PIXELS(W * H) {
+        a.sw[p] = a.s1[p] = a.s2[p] = 0.0f;
+        if (!a.spatial[p]) continue;
+        const int x = p % W, y = p / W;
+        const kgk_svgf_buffer &c = a.C[p];
+        const float3 n = v3(c.Normal);
+        float s1 = 0, s2 = 0, sw = 0;
+        for (int kx = -3; kx <= 3; ++kx) {
+            const int nx = x + kx;
+            if (nx < 0 || nx >= W) continue;
+            const float hx = cK7[kx + 3];
+            for (int ky = -3; ky <= 3; ++ky) {
+                const int ny = y + ky;
+                if (ny < 0 || ny >= H) continue;
+                const float hy = cK7[ky + 3];
+                if (kx == 0 && ky == 0) {
+                    s1 += hx * hy * a.M1[p];
+                    s2 += hx * hy * a.M2[p];
+                    sw += hx * hy;
+                    continue;
+                }
+                const int q = W * ny + nx;
+                const kgk_svgf_buffer &d = a.C[q];
+                if (d.ObjectID == -1) continue;
+                const float wm = c.MaterialID == d.MaterialID ? 1.0f : 0.0f;
+                const float wz = depth_w(c.Depth, d.Depth, kx, ky, a.gz[2 * p], a.gz[2 * p + 1]);
+                const float wn = normal_w(n, v3(d.Normal));
+                const float w = hx * hy * wz * wn * wm;
+                s1 += w * a.M1[q];
+                s2 += w * a.M2[q];
+                sw += w;
+            }
+        }
+        a.s1[p] = s1;
+        a.s2[p] = s2;
+        a.sw[p] = sw;
+    }
+}
+
+__global__ void k_c_var4(CompatArgs a) {
+    const int W = a.W;
+    FOR_PIXELS(W * a.H) {
+        kgk_svgf_buffer &c = a.C[p];
+        if (c.ObjectID == -1 || (a.spatial[p] && a.sw[p] == 0.0f)) {
+            a.F[p] = a.R[p];
+            sb_init(c);
+            c.willApplyATrousFilter = false;
+        } else if (a.spatial[p]) {
+            c.MomentOne = a.s1[p] / a.sw[p];
+            c.MomentTwo = a.s2[p] / a.sw[p];
+            if (c.PosLastFrameI[0] == -1) c.sampleNum = 1;
+            else c.sampleNum = a.P[W * c.PosLastFrameI[1] + c.PosLastFrameI[0]].sampleNum + 1;
+        }
+    }
+}
+
+__global__ void k_c_var5(CompatArgs a) {
+    FOR_PIXELS(a.W * a.H) {
+        kgk_svgf_buffer &c = a.C[p];
+        if (c.ObjectID == -1) continue;
+        c.Variance = fmaxf(0.0f, c.MomentTwo - c.MomentOne * c.MomentOne);
+        if (c.Variance > 1000) c.Variance = 1000;
+    }
+}
+
+// ApplyGaussianFilterToVar (SVGF.cuh:277-344)
+__global__ void k_c_gauss1(CompatArgs a) {
+    const int W = a.W, H = a.H;
+    FOR_PIXELS(W * H) {
+        const int x = p % W, y = p / W;
+        float sv = 0, sw = 0;
+        for (int kx = -1; kx <= 1; ++kx) {
+            const float hx = cKG[kx + 1];
+            const int nx = x + kx;
+            if (nx < 0 || nx >= W) continue;
+            for (int ky = -1; ky <= 1; ++ky) {
+                const float hy = cKG[ky + 1];
+                const int ny = y + ky;
+                if (ny < 0 || ny >= H) continue;
+                const kgk_svgf_buffer &d = a.C[W * ny + nx];
+                if (d.ObjectID == -1) continue;
+                const float w = hx * hy;
+                sv += w * d.Variance;
+                sw += w;
+            }
+        }
+        a.s1[p] = sv;
+        a.sw[p] = sw;
+    }
+}
+
+__global__ void k_c_gauss2(CompatArgs a) {
+    FOR_PIXELS(a.W * a.H) {
+        kgk_svgf_buffer &c = a.C[p];
+        a.sd[p] = 0.0f;
+        if (a.s1[p] == 0.0f && a.sw[p] != 0.0f) {
+            a.F[p] = a.R[p];
+            c.willApplyATrousFilter = false;
+        } else if (a.sw[p] == 0.0f) {
+            c.MomentOne = -1.0f;
+            c.MomentTwo = -1.0f;
+            c.sampleNum = 0;
+            c.willApplyATrousFilter = false;
+        } else {
+            c.Variance = a.s1[p] / a.sw[p];
+            a.sd[p] = sqrtf(a.s1[p] / a.sw[p]);
+        }
+        a.var[p] = c.Variance;
+    }
+}
+
+// One a-trous stage (SVGF.cuh:347-474).  Reads Rin / var_in, writes Rout /
+// var_out (copies for untouched pixels keep the ping-pong consistent).
+__global__ void k_c_atrous(CompatArgs a, const kgk_vec *__restrict__ Rin, kgk_vec *Rout,
+                           const float *__restrict__ vin, float *vout, int stage) {
+    const int W = a.W, H = a.H;
+    FOR_PIXELS(W * H) {
+        const int x = p % W, y = p / W;
+        kgk_svgf_buffer &c = a.C[p];
+        const float3 alb = v3(c.Albedo);
+        const float3 dc = div3(v3(Rin[p]), alb + f3(kS, kS, kS));
+        const float l = lumf(dc);
+        const float d = c.Depth;
+        const int dx = x < W / 2 ? 1 : -1, dy = y < H / 2 ? 1 : -1;
+        const float gx = (a.C[W * y + x + dx].Depth - d) / (float)dx;
+        const float gy = (a.C[W * (y + dy) + x].Depth - d) / (float)dy;
+        const float3 n = v3(c.Normal);
+        const float sdv = a.sd[p];
+        float3 srad = f3(0.0f, 0.0f, 0.0f);
+        float svar = 0.0f, swt = 0.0f;
+        for (int ki = 0; ki < 25; ++ki) {
+            const float h = cKW[ki];
+            const int qx = x + ((ki % 5 - 2) * (1 << stage)), qy = y + ((ki / 5 - 2) * (1 << stage));
+            if (qx < 0 || qx >= W || qy < 0 || qy >= H) continue;
+            const int q = W * qy + qx;
+            if (ki == 12) {
+                svar += h * h * vin[p];
+                srad += dc * h;
+                swt += h;
+                continue;
+            }
+            const kgk_svgf_buffer &e = a.C[q];
+            if (e.ObjectID == -1) continue;
+            const float3 nr = div3(v3(Rin[q]), v3(e.Albedo) + f3(kS, kS, kS));
+            const float nl = lumf(nr);
+            if (((double)l > 0.5 && nl > 5 * l) || ((double)l > 0.1 && nl > 50 * l) || (l > kS && nl > 100 * l))
+                continue;
+            const float wm = c.MaterialID == e.MaterialID ? 1.0f : 0.0f;
+            const float wz = depth_w(d, e.Depth, qx, qy, gx, gy);  // absolute coordinates, SVGF.cuh:426
+            const float wn = normal_w(n, v3(e.Normal));
+            const float wl = lum_w(l, nl, sdv);
+            const float w = c.willApplyATrousFilter ? h * wz * wn * wl * wm : h * wz * wn * wm;
+            srad += nr * w;
+            svar += w * w * vin[q];
+            swt += w;
+        }
+        Rout[p] = Rin[p];
+        vout[p] = vin[p];
+        if (c.ObjectID == -1) continue;
+        if (swt < 1e-6f || swt * swt < 1e-6f) {
+            a.F[p] = Rin[p];
+            c.willApplyTemporalAccumulation = true;
+            continue;
+        }
+        const float3 fl = srad / swt;
+        const float fv = svar / (swt * swt);
+        const float cw = 0.2f;
+        const float3 o = (fl * alb) * cw + v3(Rin[p]) * (1 - cw);
+        a.F[p] = kv(o);
+        Rout[p] = kv(o);
+        if (c.willApplyATrousFilter) vout[p] = cw * vin[p] + (1 - cw) * fv;
+        if (stage == 0) {
+            c.ColorHistory = kv(o);
+            c.willApplyTemporalAccumulation = true;
+        }
+    }
+}
+
+__global__ void k_c_final(CompatArgs a, const float *var) {
+    FOR_PIXELS(a.W * a.H) {
+        a.C[p].Variance = var[p];
+        a.R[p] = a.C[p].ColorHistory;
+    }
+}
+
+__global__ void k_copy_vec(const kgk_vec *src, kgk_vec *dst, int n) {
+    FOR_PIXELS(n) dst[p] = src[p];
+}
+
+// Runs the compat pipeline on device buffers (R, F, P, C all W*H records).
+kgk_status run_compat(kgk_vec *R, kgk_vec *F, kgk_svgf_buffer *P, kgk_svgf_buffer *C, int W, int H, int frame,
+                      int repeats, int stages, cudaStream_t st) {
+    const size_t npx = (size_t)W * H;
+    void *scratch = nullptr;
+    const size_t fl = npx * sizeof(float);
+    const size_t bytes = 9 * fl + npx + npx * sizeof(kgk_vec) + 1024;
+    KGK_TRY(dmalloc(&scratch, bytes, "SVGF scratch"));
+    char *b = (char *)scratch;
+    CompatArgs a;
+    a.W = W; a.H = H; a.frame = frame; a.R = R; a.F = F; a.P = P; a.C = C;
+    a.M1 = (float *)b; b += fl;
+    a.M2 = (float *)b; b += fl;
+    a.sd = (float *)b; b += fl;
+    a.gz = (float *)b; b += 2 * fl;
+    a.s1 = (float *)b; b += fl;
+    a.s2 = (float *)b; b += fl;
+    a.sw = (float *)b; b += fl;
+    a.var = (float *)b; b += fl;
+    a.R2 = (kgk_vec *)b; b += npx * sizeof(kgk_vec);
+    a.spatial = (unsigned char *)b;
+    float *var2 = nullptr;
+    kgk_status stt = dmalloc((void **)&var2, fl, "SVGF scratch");
+    if (stt != KGK_OK) { dfree(scratch); return stt; }
+    const int g = (int)std::min<size_t>((npx + 255) / 256, 65535);
+    k_c_prologue<<<g, 256, 0, st>>>(a);
+    k_c_temporal<<<g, 256, 0, st>>>(a);
+    k_c_var1<<<g, 256, 0, st>>>(a);
+    k_c_var2<<<g, 256, 0, st>>>(a);
+    k_c_var3<<<g, 256, 0, st>>>(a);
+    k_c_var4<<<g, 256, 0, st>>>(a);
+    k_c_var5<<<g, 256, 0, st>>>(a);
+    k_c_gauss1<<<g, 256, 0, st>>>(a);
+    k_c_gauss2<<<g, 256, 0, st>>>(a);
+    kgk_vec *rin = R, *rout = a.R2;
+    float *vin = a.var, *vout = var2;
+    for (int k = 0; k < repeats; ++k)
+        for (int s = 0; s < stages; ++s) {
+            k_c_atrous<<<g, 256, 0, st>>>(a, rin, rout, vin, vout, s);
+            std::swap(rin, rout);
+            std::swap(vin, vout);
+        }
+    if (rin != R) k_copy_vec<<<g, 256, 0, st>>>(rin, R, (int)npx);
+    k_c_final<<<g, 256, 0, st>>>(a, vin);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    dfree(scratch);
+    dfree(var2);
+    if (e != cudaSuccess) return cuda_fail(e, "SVGF compat kernels");
+    return KGK_OK;
+}
+
+// Fills reference-layout records from the renderer's G-buffer, the way
+// render.cuh:28 (init) and RayTrace.cuh:66-82 fill them.
+__global__ void k_gbuffer_to_records(const float4 *pos, const float4 *nrm, const float4 *alb, const float4 *emi,
+                                     int npx, kgk_svgf_buffer *C) {
+    FOR_PIXELS(npx) {
+        kgk_svgf_buffer b;
+        sb_init(b);
+        const int obj = __float_as_int(nrm[p].w);
+        if (obj >= 0) {
+            b.Albedo = kv(f3(alb[p]));
+            b.Emission = kv(f3(emi[p]));
+            b.Normal = kv(f3(nrm[p]));
+            b.ObjectID = obj;
+            b.MaterialID = __float_as_int(alb[p].w);
+            b.Depth = pos[p].w;
+        }
+        C[p] = b;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// standard SVGF
+// ---------------------------------------------------------------------------
+struct StdArgs {
+    int W, H;
+    const float4 *pos, *nrm, *alb, *emi;   // current G-buffer
+    const float4 *noisy;                   // current frame (kgk_vec)
+    float4 *hist, *hist_prev;
+    float2 *mom, *mom_prev;
+    float4 *nd_prev;
+    int *mat_prev;
+    float4 *col, *tmp;
+    float *gvar;
+    kgk_camera pcam;
+    int has_prev;
+    float alpha, sz, sn, sl;
+};
+
+// Projects a world position into the previous camera (inverse of
+// Generate1stRay): pixel coordinates (x, y) of the previous frame.
+__device__ __forceinline__ bool project_prev(const kgk_camera &c, int W, int H, float3 p, float &x, float &y) {
+    const float3 o = f3(c.CamOrg.x, c.CamOrg.y, c.CamOrg.z);
+    const float3 d = f3(c.CamDir.x, c.CamDir.y, c.CamDir.z);
+    const float3 sx = f3(c.ScreenXDir.x, c.ScreenXDir.y, c.ScreenXDir.z);
+    const float3 sy = f3(c.ScreenYDir.x, c.ScreenYDir.y, c.ScreenYDir.z);
+    const float3 v = p - o;
+    const float z = dot3(v, d);
+    if (z <= 1e-6f) return false;
+    const float k = c.CamToScreenDist / z;  // scale to the screen plane
+    x = dot3(v, sx) * k / (c.PixelSize * dot3(sx, sx)) + W / 2.0f;
+    y = H / 2.0f - dot3(v, sy) * k / (c.PixelSize * dot3(sy, sy));
+    return true;
+}
+
+__global__ void k_s_temporal(StdArgs a) {
+    const int W = a.W, H = a.H;
+    FOR_PIXELS(W * H) {
+        const float4 nr = a.nrm[p];
+        const int obj = __float_as_int(nr.w);
+        const float3 noisy = f3(a.noisy[p]);
+        if (obj < 0) {
+            a.hist[p] = make_float4(noisy.x, noisy.y, noisy.z, 0.0f);
+            a.mom[p] = make_float2(0.0f, 0.0f);
+            a.col[p] = make_float4(noisy.x, noisy.y, noisy.z, 0.0f);
+            continue;
+        }
+        const float4 al = a.alb[p];
+        const int mat = __float_as_int(al.w);
+        const float3 albedo = f3(al);
+        const float3 dl = div3(noisy, albedo + f3(kS, kS, kS));
+        const float l = lumf(dl);
+        float3 hc = f3(0.0f, 0.0f, 0.0f);
+        float2 hm = make_float2(0.0f, 0.0f);
+        float hl = 0.0f, wsum = 0.0f;
+        if (a.has_prev) {
+            float x, y;
+            const float4 ps = a.pos[p];
+            if (project_prev(a.pcam, W, H, f3(ps), x, y)) {
+                // bilinear taps around the previous pixel centre
+                const float fx = x - 0.5f, fy = y - 0.5f;
+                const int x0 = (int)floorf(fx), y0 = (int)floorf(fy);
+                const float tx = fx - x0, ty = fy - y0;
+                const float3 pc = f3(a.pcam.CamOrg.x, a.pcam.CamOrg.y, a.pcam.CamOrg.z);
+                const float exp_depth = len3(f3(ps) - pc);
+                for (int k = 0; k < 4; ++k) {
+                    const int qx = x0 + (k & 1), qy = y0 + (k >> 1);
+                    if (qx < 0 || qx >= W || qy < 0 || qy >= H) continue;
+                    const int q = W * qy + qx;
+                    if (a.mat_prev[q] != mat) continue;
+                    const float4 pn = a.nd_prev[q];
+                    if (dot3(f3(pn), f3(nr)) < 0.9f) continue;
+                    if (fabsf(pn.w - exp_depth) > 0.05f * exp_depth + 1e-3f) continue;
+                    const float w = ((k & 1) ? tx : 1.0f - tx) * ((k >> 1) ? ty : 1.0f - ty);
+                    const float4 hp = a.hist_prev[q];
+                    hc += f3(hp) * w;
+                    hl += hp.w * w;
+                    hm.x += a.mom_prev[q].x * w;
+                    hm.y += a.mom_prev[q].y * w;
+                    wsum += w;
+                }
+            }
+        }
+        float3 c;
+        float2 m;
+        float len;
+        if (wsum > 1e-4f) {
+            hc = hc / wsum;
+            hm.x /= wsum;
+            hm.y /= wsum;
+            len = fminf(hl / wsum + 1.0f, 64.0f);
+            const float ac = fmaxf(a.alpha, 1.0f / len);
+            const float am = fmaxf(a.alpha, 1.0f / len);
+            c = hc * (1.0f - ac) + dl * ac;
+            m = make_float2(hm.x * (1.0f - am) + l * am, hm.y * (1.0f - am) + l * l * am);
+        } else {
+            c = dl;
+            m = make_float2(l, l * l);
+            len = 1.0f;
+        }
+        a.hist[p] = make_float4(c.x, c.y, c.z, len);
+        a.mom[p] = m;
+        a.col[p] = make_float4(c.x, c.y, c.z, 0.0f);
+    }
+}
+
+__device__ __forceinline__ float depth_weight_std(float d, float dq, float grad, float dist, float sz) {
+    return expf(-fabsf(d - dq) / (sz * fabsf(grad) * dist + 1e-3f));
+}
+
+// Variance: temporal moments when the history is long enough, else a 7x7
+// edge-stopped spatial estimate.
+__global__ void k_s_variance(StdArgs a) {
+    const int W = a.W, H = a.H;
+    FOR_PIXELS(W * H) {
+        const float4 nr = a.nrm[p];
+        if (__float_as_int(nr.w) < 0) continue;
+        const float len = a.hist[p].w;
+        float var;
+        if (len >= 4.0f) {
+            const float2 m = a.mom[p];
+            var = fmaxf(0.0f, m.y - m.x * m.x);
+        } else {
+            const int x = p % W, y = p / W;
+            const float d = a.pos[p].w;
+            const int mat = __float_as_int(a.alb[p].w);
+            const float gx = (x + 1 < W ? a.pos[p + 1].w : d) - (x > 0 ? a.pos[p - 1].w : d);
+            const float gy = (y + 1 < H ? a.pos[p + W].w : d) - (y > 0 ? a.pos[p - W].w : d);
+            const float grad = 0.5f * fmaxf(fabsf(gx), fabsf(gy));
+            float s1 = 0, s2 = 0, sw = 0;
+            for (int ky = -3; ky <= 3; ++ky)
+                for (int kx = -3; kx <= 3; ++kx) {
+                    const int qx = x + kx, qy = y + ky;
+                    if (qx < 0 || qx >= W || qy < 0 || qy >= H) continue;
+                    const int q = W * qy + qx;
+                    const float4 qn = a.nrm[q];
+                    if (__float_as_int(qn.w) < 0 || __float_as_int(a.alb[q].w) != mat) continue;
+                    const float w = depth_weight_std(d, a.pos[q].w, grad, sqrtf((float)(kx * kx + ky * ky)), a.sz) *
+                                    powf(fmaxf(0.0f, dot3(f3(nr), f3(qn))), a.sn);
+                    const float2 m = a.mom[q];
+                    s1 += w * m.x;
+                    s2 += w * m.y;
+                    sw += w;
+                }
+            var = sw > 0.0f ? fmaxf(0.0f, s2 / sw - (s1 / sw) * (s1 / sw)) : 0.0f;
+            var *= 4.0f / len;  // boost for short histories
+        }
+        a.col[p].w = var;
+    }
+}
+
+__global__ void k_s_gauss_var(StdArgs a, const float4 *col) {
+    const int W = a.W, H = a.H;
+    FOR_PIXELS(W * H) {
+        const int x = p % W, y = p / W;
+        float s = 0, w = 0;
+        for (int ky = -1; ky <= 1; ++ky)
+            for (int kx = -1; kx <= 1; ++kx) {
+                const int qx = x + kx, qy = y + ky;
+                if (qx < 0 || qx >= W || qy < 0 || qy >= H) continue;
+                const float k = cKG[kx + 1] * cKG[ky + 1];
+                s += k * col[W * qy + qx].w;
+                w += k;
+            }
+        a.gvar[p] = s / w;
+    }
+}
+
+__global__ void k_s_atrous(StdArgs a, const float4 *__restrict__ in, float4 *out, int step) {
+    const int W = a.W, H = a.H;
+    FOR_PIXELS(W * H) {
+        const float4 nr = a.nrm[p];
+        const float4 c = in[p];
+        if (__float_as_int(nr.w) < 0) {
+            out[p] = c;
+            continue;
+        }
+        const int x = p % W, y = p / W;
+        const float d = a.pos[p].w;
+        const int mat = __float_as_int(a.alb[p].w);
+        const float gx = (x + 1 < W ? a.pos[p + 1].w : d) - (x > 0 ? a.pos[p - 1].w : d);
+        const float gy = (y + 1 < H ? a.pos[p + W].w : d) - (y > 0 ? a.pos[p - W].w : d);
+        const float grad = 0.5f * fmaxf(fabsf(gx), fabsf(gy));
+        const float l = lumf(f3(c));
+        const float sdl = a.sl * sqrtf(fmaxf(a.gvar[p], 0.0f)) + 1e-6f;
+        float3 sc = f3(c) * (36.0f / 256.0f);
+        float sv = (36.0f / 256.0f) * (36.0f / 256.0f) * c.w;
+        float sw = 36.0f / 256.0f;
+        for (int ki = 0; ki < 25; ++ki) {
+            if (ki == 12) continue;
+            const int ox = ki % 5 - 2, oy = ki / 5 - 2;
+            const int qx = x + ox * step, qy = y + oy * step;
+            if (qx < 0 || qx >= W || qy < 0 || qy >= H) continue;
+            const int q = W * qy + qx;
+            const float4 qn = a.nrm[q];
+            if (__float_as_int(qn.w) < 0 || __float_as_int(a.alb[q].w) != mat) continue;
+            const float4 qc = in[q];
+            const float dist = (float)step * sqrtf((float)(ox * ox + oy * oy));
+            const float wz = depth_weight_std(d, a.pos[q].w, grad, dist, a.sz);
+            const float wn = powf(fmaxf(0.0f, dot3(f3(nr), f3(qn))), a.sn);
+            const float wl = expf(-fabsf(l - lumf(f3(qc))) / sdl);
+            const float w = cKW[ki] * wz * wn * wl;
+            sc += f3(qc) * w;
+            sv += w * w * qc.w;
+            sw += w;
+        }
+        out[p] = make_float4(sc.x / sw, sc.y / sw, sc.z / sw, sv / (sw * sw));
+    }
+}
+
+__global__ void k_s_feedback(StdArgs a, const float4 *filtered) {
+    FOR_PIXELS(a.W * a.H) {
+        if (__float_as_int(a.nrm[p].w) < 0) continue;
+        const float4 f = filtered[p];
+        a.hist[p].x = f.x;
+        a.hist[p].y = f.y;
+        a.hist[p].z = f.z;
+    }
+}
+
+__global__ void k_s_output(StdArgs a, const float4 *filtered, float4 *out) {
+    FOR_PIXELS(a.W * a.H) {
+        const float4 nr = a.nrm[p];
+        if (__float_as_int(nr.w) < 0) {
+            const float4 c = filtered[p];
+            out[p] = make_float4(c.x, c.y, c.z, 1.0f);
+            continue;
+        }
+        const float3 al = f3(a.alb[p]) + f3(kS, kS, kS);
+        const float4 c = filtered[p];
+        const float3 e = f3(a.emi[p]);
+        out[p] = make_float4(c.x * al.x + 0.0f * e.x, c.y * al.y, c.z * al.z, 1.0f);
+    }
+}
+
+__global__ void k_s_save_prev(StdArgs a) {
+    FOR_PIXELS(a.W * a.H) {
+        const float4 nr = a.nrm[p];
+        const int obj = __float_as_int(nr.w);
+        a.nd_prev[p] = make_float4(nr.x, nr.y, nr.z, a.pos[p].w);
+        a.mat_prev[p] = obj < 0 ? -1 : __float_as_int(a.alb[p].w);
+    }
+}
+
+template <class T> kgk_status realloc_d(T **p, size_t n, const char *what) {
+    dfree(*p);
+    *p = nullptr;
+    return dalloc(p, n, what);
+}
+
+}  // namespace
+
+void svgf_state_free_impl(SvgfState *S) {
+    void *ptrs[] = {S->prev, S->cur, S->hist, S->hist_prev, S->mom, S->mom_prev, S->nd_prev, S->mat_prev,
+                    S->col, S->tmp, S->gvar};
+    for (void *p : ptrs) dfree(p);
+}
+
+}  // namespace kgk
+
+using namespace kgk;
+
+extern "C" {
+
+kgk_status kgk_svgf_apply(kgk_vec *result, kgk_vec *filtered, kgk_svgf_buffer *prev, kgk_svgf_buffer *cur,
+                          int32_t W, int32_t H, int32_t frame) {
+    if (!result || !filtered || !prev || !cur) return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_svgf_apply: NULL buffer");
+    if (W < 2 || H < 2 || (long long)W * H > (1LL << 26))
+        return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_svgf_apply: image size out of range (needs >= 2 x 2)");
+    int dev = 0;
+    KGK_CUDA(cudaGetDevice(&dev));
+    cudaStream_t st;
+    KGK_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    const size_t npx = (size_t)W * H;
+    const bool dr = is_device_ptr(result), df = is_device_ptr(filtered), dp = is_device_ptr(prev),
+               dc = is_device_ptr(cur);
+    kgk_vec *R = result, *F = filtered;
+    kgk_svgf_buffer *P = prev, *C = cur;
+    std::vector<void *> owned;
+    auto stage = [&](void **dst, void *src, size_t bytes, bool is_dev) -> kgk_status {
+        if (is_dev) { *dst = src; return KGK_OK; }
+        KGK_TRY(dmalloc(dst, bytes, "SVGF staging"));
+        owned.push_back(*dst);
+        KGK_CUDA(cudaMemcpyAsync(*dst, src, bytes, cudaMemcpyHostToDevice, st));
+        return KGK_OK;
+    };
+    kgk_status s = KGK_OK;
+    if (s == KGK_OK) s = stage((void **)&R, result, npx * sizeof(kgk_vec), dr);
+    if (s == KGK_OK) s = stage((void **)&F, filtered, npx * sizeof(kgk_vec), df);
+    if (s == KGK_OK) s = stage((void **)&P, prev, npx * sizeof(kgk_svgf_buffer), dp);
+    if (s == KGK_OK) s = stage((void **)&C, cur, npx * sizeof(kgk_svgf_buffer), dc);
+    if (s == KGK_OK) s = run_compat(R, F, P, C, W, H, frame, 5, 5, st);
+    if (s == KGK_OK) {
+        cudaError_t e = cudaSuccess;
+        if (!dr) e = cudaMemcpyAsync(result, R, npx * sizeof(kgk_vec), cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess && !df) e = cudaMemcpyAsync(filtered, F, npx * sizeof(kgk_vec), cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess && !dp) e = cudaMemcpyAsync(prev, P, npx * sizeof(kgk_svgf_buffer), cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess && !dc) e = cudaMemcpyAsync(cur, C, npx * sizeof(kgk_svgf_buffer), cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) s = cuda_fail(e, "kgk_svgf_apply copies");
+    }
+    for (void *p : owned) dfree(p);
+    cudaStreamDestroy(st);
+    return s;
+}
+
+kgk_status kgk_svgf(kgk_scene *s, const kgk_svgf_config *cfg, const kgk_vec *noisy, kgk_vec *filtered) {
+    if (!s || !cfg || !noisy || !filtered) return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_svgf: NULL argument");
+    KGK_CUDA(cudaSetDevice(s->device));
+    int W, H;
+    const float4 *gpos, *gnrm, *galb, *gemi;
+    kgk_camera cam;
+    if (!svgf_gbuffer(s, &W, &H, &gpos, &gnrm, &galb, &gemi, &cam))
+        return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_svgf: render a frame with write_gbuffer=1 first");
+    if (cfg->width != W || cfg->height != H)
+        return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_svgf: size differs from the last rendered G-buffer");
+    if (W < 2 || H < 2) return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_svgf: image must be at least 2 x 2");
+    SvgfState &S = *svgf_state(s);
+    const size_t npx = (size_t)W * H;
+    cudaStream_t st = s->stream;
+    if (S.W != W || S.H != H) {
+        svgf_state_free_impl(&S);
+        S = SvgfState();
+        KGK_TRY(dalloc(&S.prev, npx, "SVGF history"));
+        KGK_TRY(dalloc(&S.cur, npx, "SVGF state"));
+        KGK_TRY(dalloc(&S.hist, npx, "SVGF history"));
+        KGK_TRY(dalloc(&S.hist_prev, npx, "SVGF history"));
+        KGK_TRY(dalloc(&S.mom, npx, "SVGF moments"));
+        KGK_TRY(dalloc(&S.mom_prev, npx, "SVGF moments"));
+        KGK_TRY(dalloc(&S.nd_prev, npx, "SVGF history"));
+        KGK_TRY(dalloc(&S.mat_prev, npx, "SVGF history"));
+        KGK_TRY(dalloc(&S.col, npx, "SVGF colour"));
+        KGK_TRY(dalloc(&S.tmp, npx, "SVGF colour"));
+        KGK_TRY(dalloc(&S.gvar, npx, "SVGF variance"));
+        KGK_CUDA(cudaMemset(S.prev, 0, npx * sizeof(kgk_svgf_buffer)));
+        S.W = W;
+        S.H = H;
+        S.has_prev = false;
+    }
+    // staging of host images
+    const bool dn = is_device_ptr(noisy), dfo = is_device_ptr(filtered);
+    KGK_TRY(s->staging.reserve(2 * npx * sizeof(float4) + 256));
+    float4 *in = dn ? (float4 *)noisy : (float4 *)s->staging.ptr;
+    float4 *out = dfo ? (float4 *)filtered : (float4 *)((char *)s->staging.ptr + npx * sizeof(float4));
+    if (!dn) KGK_CUDA(cudaMemcpyAsync(in, noisy, npx * sizeof(float4), cudaMemcpyHostToDevice, st));
+    const int g = (int)std::min<size_t>((npx + 255) / 256, 65535);
+    if (cfg->mode == KGK_SVGF_COMPAT) {
+        k_gbuffer_to_records<<<g, 256, 0, st>>>(gpos, gnrm, galb, gemi, (int)npx, S.cur);
+        // result buffer: the noisy frame (copied, the reference rewrites it)
+        float4 *R = S.col;
+        KGK_CUDA(cudaMemcpyAsync(R, in, npx * sizeof(float4), cudaMemcpyDeviceToDevice, st));
+        const int reps = cfg->atrous_repeats > 0 ? cfg->atrous_repeats : 5;
+        const int stages = cfg->atrous_iterations > 0 ? cfg->atrous_iterations : 5;
+        KGK_TRY(run_compat((kgk_vec *)R, (kgk_vec *)out, S.prev, S.cur, W, H, cfg->frame_index, reps, stages, st));
+        // main.cu:232: the current buffer becomes the previous one
+        KGK_CUDA(cudaMemcpyAsync(S.prev, S.cur, npx * sizeof(kgk_svgf_buffer), cudaMemcpyDeviceToDevice, st));
+    } else if (cfg->mode == KGK_SVGF_STANDARD) {
+        if (cfg->frame_index == 0) S.has_prev = false;
+        StdArgs a;
+        a.W = W; a.H = H; a.pos = gpos; a.nrm = gnrm; a.alb = galb; a.emi = gemi; a.noisy = in;
+        a.hist = S.hist; a.hist_prev = S.hist_prev; a.mom = S.mom; a.mom_prev = S.mom_prev;
+        a.nd_prev = S.nd_prev; a.mat_prev = S.mat_prev; a.col = S.col; a.tmp = S.tmp; a.gvar = S.gvar;
+        a.pcam = S.prev_cam;
+        a.has_prev = S.has_prev ? 1 : 0;
+        a.alpha = cfg->alpha > 0.0f ? cfg->alpha : 0.2f;
+        a.sz = cfg->sigma_z > 0.0f ? cfg->sigma_z : 1.0f;
+        a.sn = cfg->sigma_n > 0.0f ? cfg->sigma_n : 128.0f;
+        a.sl = cfg->sigma_l > 0.0f ? cfg->sigma_l : 4.0f;
+        k_s_temporal<<<g, 256, 0, st>>>(a);
+        k_s_variance<<<g, 256, 0, st>>>(a);
+        const int iters = cfg->atrous_iterations > 0 ? cfg->atrous_iterations : 5;
+        float4 *src = S.col, *dst = S.tmp;
+        for (int i = 0; i < iters; ++i) {
+            k_s_gauss_var<<<g, 256, 0, st>>>(a, src);
+            k_s_atrous<<<g, 256, 0, st>>>(a, src, dst, 1 << i);
+            if (i == 0) k_s_feedback<<<g, 256, 0, st>>>(a, dst);
+            std::swap(src, dst);
+        }
+        k_s_output<<<g, 256, 0, st>>>(a, src, out);
+        k_s_save_prev<<<g, 256, 0, st>>>(a);
+        KGK_CUDA(cudaGetLastError());
+        std::swap(S.hist, S.hist_prev);
+        std::swap(S.mom, S.mom_prev);
+        S.prev_cam = cam;
+        S.has_prev = true;
+    } else {
+        return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_svgf: unknown mode");
+    }
+    if (!dfo) KGK_CUDA(cudaMemcpyAsync(filtered, out, npx * sizeof(float4), cudaMemcpyDeviceToHost, st));
+    KGK_CUDA(cudaStreamSynchronize(st));
+    return KGK_OK;
+}
+
+}  // extern "C"

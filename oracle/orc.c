@@ -1176,3 +1176,296 @@ int64_t orc_render_compat_px(const void *tris, int64_t n, const void *mats, cons
     free(lssh);
     return rays;
 }
+
+/* ------------------------------------------------------------------------ */
+/* SVGF, race-free reading (SVGF.cuh:10-522)                                  */
+/* ------------------------------------------------------------------------ */
+typedef struct {
+    V albedo, emission, normal, history;
+    int32_t object_id, material_id;
+    int32_t pos_i[2];
+    float pos_f[2];
+    int32_t sample_num;
+    float m1, m2, variance, depth;
+    unsigned char atrous, temporal;
+    unsigned char pad[2];
+} SB;
+_Static_assert(sizeof(SB) == 112, "SVGFBuffer");
+
+static void sb_init(SB *b) { /* struct_SVGFBuffers.cuh:31-47 */
+    b->albedo = mk(0, 0, 0);
+    b->emission = mk(0, 0, 0);
+    b->normal = mk(0, 0, 0);
+    b->history = mk(0, 0, 0);
+    b->object_id = -1;
+    b->material_id = -1;
+    b->pos_i[0] = b->pos_i[1] = -1;
+    b->pos_f[0] = b->pos_f[1] = -1;
+    b->sample_num = 0;
+    b->m1 = -1.0f;
+    b->m2 = -1.0f;
+    b->variance = 0.0f;
+    b->depth = 0.0f;
+    b->atrous = 1;
+    b->temporal = 0;
+}
+
+static float lum(V c) { return 0.2126f * c.x + 0.7152f * c.y + 0.0722f * c.z; }
+static float depth_w(float d, float nd, int dx, int dy, float gx, float gy) {
+    float top = -1.0f * fabsf(d - nd);
+    float bottom = 1.0f * fabsf((float)dx * gx + (float)dy * gy) + sINF;
+    return expf(top / bottom);
+}
+static float normal_w(V n, V nn) {
+    float c = fmaxf(0.0f, dot(n, nn));
+    c *= c; c *= c; c *= c; c *= c; c *= c; c *= c; c *= c;
+    return c;
+}
+static float lum_w(float l, float nl, float sd) {
+    float top = -1.0f * fabsf(l - nl);
+    float bottom = 4.0f * sd + sINF;
+    return expf(top / bottom);
+}
+
+/* One ApplySVGF call over all pixels with a full barrier at every
+ * __syncthreads.  result/filtered: npx Vec (4 floats); prev/cur: npx SB. */
+void orc_svgf_compat(int W, int H, float *result_, float *filtered_, void *prev_, void *cur_, int frame) {
+    const int npx = W * H;
+    V *R = (V *)result_, *F = (V *)filtered_;
+    SB *P = (SB *)prev_, *C = (SB *)cur_;
+    float *M1 = (float *)calloc((size_t)npx, sizeof(float));
+    float *M2 = (float *)calloc((size_t)npx, sizeof(float));
+    float *sd = (float *)calloc((size_t)npx, sizeof(float));
+    unsigned char *spatial = (unsigned char *)calloc((size_t)npx, 1);
+    float *sw = (float *)calloc((size_t)npx, sizeof(float));
+    float *s1 = (float *)calloc((size_t)npx, sizeof(float));
+    float *s2 = (float *)calloc((size_t)npx, sizeof(float));
+    V *R2 = (V *)calloc((size_t)npx, sizeof(V));
+    float *var2 = (float *)calloc((size_t)npx, sizeof(float));
+    float *gz = (float *)calloc((size_t)npx * 2, sizeof(float));
+    /* ApplySVGF prologue (SVGF.cuh:498-511) */
+    for (int p = 0; p < npx; ++p) {
+        if (!isfinite(len(R[p]))) R[p] = mk(0.0f, 0.0f, 0.0f);
+        if (frame == 0) sb_init(&P[p]);
+        if (P[p].m1 == -1.0f) {
+            V c = vdivv(R[p], C[p].albedo);
+            C[p].m1 = lum(c);
+            C[p].m2 = C[p].m1 * C[p].m1;
+        }
+        F[p] = mk(0, 0, 0);
+    }
+    /* TemporalAccumulation (SVGF.cuh:50-98) */
+    for (int p = 0; p < npx; ++p) {
+        if (len(C[p].emission) != 0) continue;
+        int px = C[p].pos_i[0], py = C[p].pos_i[1];
+        float s = C[p].pos_f[0] - (float)px, t = C[p].pos_f[1] - (float)py;
+        int off[4][2] = {{0, 0}, {1, 0}, {0, 1}, {1, 1}};
+        float w[4] = {(1 - s) * (1 - t), s * (1 - t), (1 - s) * t, s * t};
+        V sum = mk(0, 0, 0);
+        float swt = 0.0f;
+        for (int i = 0; i < 4; ++i) {
+            int qx = px + off[i][0], qy = py + off[i][1];
+            if (qx < 0 || qx >= W || qy < 0 || qy >= H) continue;
+            int q = W * qy + qx;
+            if (P[q].material_id == C[p].material_id && P[q].temporal) {
+                sum = vadd(sum, vmul(P[q].history, w[i]));
+                swt += w[i];
+            }
+        }
+        if (swt == 0.0f) continue;
+        V hist = vdivs(sum, swt);
+        R[p] = vadd(vmul(R[p], 0.2f), vmul(hist, (float)0.8));
+    }
+    /* VarianceEstimation (SVGF.cuh:112-275), phase by phase */
+    for (int p = 0; p < npx; ++p) {
+        int x = p % W, y = p / W;
+        V dc = vdivv(R[p], vadd(C[p].albedo, mk(sINF, sINF, sINF)));
+        float l = lum(dc);
+        M1[p] = l;
+        M2[p] = l * l;
+        int prev = W * C[p].pos_i[1] + C[p].pos_i[0];
+        spatial[p] = C[p].pos_i[0] == -1 || P[prev].sample_num < 3;
+        int dx = x < W / 2 ? 1 : -1, dy = y < H / 2 ? 1 : -1;
+        float d = C[p].depth;
+        gz[2 * p] = (C[W * y + x + dx].depth - d) / (float)dx;
+        gz[2 * p + 1] = (C[W * (y + dy) + x].depth - d) / (float)dy;
+    }
+    for (int p = 0; p < npx; ++p) {
+        if (spatial[p]) continue;
+        int prev = W * C[p].pos_i[1] + C[p].pos_i[0];
+        C[p].sample_num = P[prev].sample_num + 1;
+        float cw = 1.0f / 5.0f;
+        if (C[p].sample_num < 5) cw = 1.0f / (float)C[p].sample_num;
+        C[p].m1 = (1.0f - cw) * P[prev].m1 + cw * M1[p];
+        C[p].m2 = (1.0f - cw) * P[prev].m2 + cw * M2[p];
+        M1[p] = C[p].m1;
+        M2[p] = C[p].m2;
+    }
+    static const float K7[7] = {0.00598f, 0.060626f, 0.241843f, 0.383103f, 0.241843f, 0.060626f, 0.00598f};
+    for (int p = 0; p < npx; ++p) {
+        sw[p] = s1[p] = s2[p] = 0.0f;
+        if (!spatial[p]) continue;
+        int x = p % W, y = p / W;
+        float a = 0, b = 0, c = 0;
+        for (int kx = -3; kx <= 3; ++kx) {
+            int nx = x + kx;
+            if (nx < 0 || nx >= W) continue;
+            float hx = K7[kx + 3];
+            for (int ky = -3; ky <= 3; ++ky) {
+                int ny = y + ky;
+                if (ny < 0 || ny >= H) continue;
+                float hy = K7[ky + 3];
+                if (kx == 0 && ky == 0) {
+                    a += hx * hy * M1[p];
+                    b += hx * hy * M2[p];
+                    c += hx * hy;
+                    continue;
+                }
+                int q = W * ny + nx;
+                if (C[q].object_id == -1) continue;
+                float wm = C[p].material_id == C[q].material_id ? 1.0f : 0.0f;
+                float wz = depth_w(C[p].depth, C[q].depth, kx, ky, gz[2 * p], gz[2 * p + 1]);
+                float wn = normal_w(C[p].normal, C[q].normal);
+                float wt = hx * hy * wz * wn * wm;
+                a += wt * M1[q];
+                b += wt * M2[q];
+                c += wt;
+            }
+        }
+        s1[p] = a;
+        s2[p] = b;
+        sw[p] = c;
+    }
+    for (int p = 0; p < npx; ++p) {
+        int prev = W * C[p].pos_i[1] + C[p].pos_i[0];
+        if (C[p].object_id == -1) {
+            F[p] = R[p];
+            sb_init(&C[p]);
+            C[p].atrous = 0;
+        } else if (spatial[p] && sw[p] == 0) {
+            F[p] = R[p];
+            sb_init(&C[p]);
+            C[p].atrous = 0;
+        } else if (spatial[p]) {
+            C[p].m1 = s1[p] / sw[p];
+            C[p].m2 = s2[p] / sw[p];
+            if (C[p].pos_i[0] == -1) C[p].sample_num = 1;
+            else C[p].sample_num = P[prev].sample_num + 1;
+        }
+    }
+    for (int p = 0; p < npx; ++p) {
+        if (C[p].object_id == -1) continue;
+        C[p].variance = fmaxf(0.0f, C[p].m2 - C[p].m1 * C[p].m1);
+        if (C[p].variance > 1000) C[p].variance = 1000;
+    }
+    /* ApplyGaussianFilterToVar (SVGF.cuh:277-344) */
+    static const float KG[3] = {1 / 4.0f, 1 / 2.0f, 1 / 4.0f};
+    for (int p = 0; p < npx; ++p) {
+        int x = p % W, y = p / W;
+        float sv = 0, swt = 0;
+        for (int kx = -1; kx <= 1; ++kx) {
+            float hx = KG[kx + 1];
+            int nx = x + kx;
+            if (nx < 0 || nx >= W) continue;
+            for (int ky = -1; ky <= 1; ++ky) {
+                float hy = KG[ky + 1];
+                int ny = y + ky;
+                if (ny < 0 || ny >= H) continue;
+                int q = W * ny + nx;
+                if (C[q].object_id == -1) continue;
+                float wt = hx * hy;
+                sv += wt * C[q].variance;
+                swt += wt;
+            }
+        }
+        s1[p] = sv;
+        sw[p] = swt;
+    }
+    for (int p = 0; p < npx; ++p) {
+        sd[p] = 0.0f;
+        if (s1[p] == 0 && sw[p] != 0) {
+            F[p] = R[p];
+            C[p].atrous = 0;
+        } else if (sw[p] == 0) {
+            C[p].m1 = -1.0f;
+            C[p].m2 = -1.0f;
+            C[p].sample_num = 0;
+            C[p].atrous = 0;
+        } else {
+            C[p].variance = s1[p] / sw[p];
+            sd[p] = sqrtf(s1[p] / sw[p]);
+        }
+    }
+    /* 5 x 5 a-trous stages (SVGF.cuh:347-474, 486-491) */
+    static const float KW[25] = {1 / 256.0f, 4 / 256.0f, 6 / 256.0f, 4 / 256.0f, 1 / 256.0f,
+                                 4 / 256.0f, 16 / 256.0f, 24 / 256.0f, 16 / 256.0f, 4 / 256.0f,
+                                 6 / 256.0f, 24 / 256.0f, 36 / 256.0f, 24 / 256.0f, 6 / 256.0f,
+                                 4 / 256.0f, 16 / 256.0f, 24 / 256.0f, 16 / 256.0f, 4 / 256.0f,
+                                 1 / 256.0f, 4 / 256.0f, 6 / 256.0f, 4 / 256.0f, 1 / 256.0f};
+    for (int k = 0; k < 5; ++k) {
+        for (int stage = 0; stage < 5; ++stage) {
+            for (int p = 0; p < npx; ++p) {
+                R2[p] = R[p];
+                var2[p] = C[p].variance;
+            }
+            for (int p = 0; p < npx; ++p) {
+                int x = p % W, y = p / W;
+                V dc = vdivv(R2[p], vadd(C[p].albedo, mk(sINF, sINF, sINF)));
+                float l = lum(dc);
+                float d = C[p].depth;
+                int dx = x < W / 2 ? 1 : -1, dy = y < H / 2 ? 1 : -1;
+                float gx = (C[W * y + x + dx].depth - d) / (float)dx;
+                float gy = (C[W * (y + dy) + x].depth - d) / (float)dy;
+                V srad = mk(0.0f, 0.0f, 0.0f);
+                float svar = 0.0f, swt = 0.0f;
+                for (int ki = 0; ki < 25; ++ki) {
+                    float h = KW[ki];
+                    int ox = ki % 5 - 2, oy = ki / 5 - 2;
+                    int qx = x + (ox * (1 << stage)), qy = y + (oy * (1 << stage));
+                    if (qx < 0 || qx >= W || qy < 0 || qy >= H) continue;
+                    int q = W * qy + qx;
+                    if (ki == 12) {
+                        svar += h * h * var2[p];
+                        srad = vadd(srad, vmul(dc, h));
+                        swt += h;
+                        continue;
+                    }
+                    if (C[q].object_id == -1) continue;
+                    V nr = vdivv(R2[q], vadd(C[q].albedo, mk(sINF, sINF, sINF)));
+                    float nl = lum(nr);
+                    if (((double)l > 0.5 && nl > 5 * l) || ((double)l > 0.1 && nl > 50 * l) ||
+                        (l > sINF && nl > 100 * l))
+                        continue;
+                    float wm = C[p].material_id == C[q].material_id ? 1 : 0;
+                    float wz = depth_w(d, C[q].depth, qx, qy, gx, gy);
+                    float wn = normal_w(C[p].normal, C[q].normal);
+                    float wl = lum_w(l, nl, sd[p]);
+                    float wt = C[p].atrous ? h * wz * wn * wl * wm : h * wz * wn * wm;
+                    srad = vadd(srad, vmul(nr, wt));
+                    svar += wt * wt * var2[q];
+                    swt += wt;
+                }
+                if (C[p].object_id == -1) continue;
+                if (swt < 1e-6f || swt * swt < 1e-6f) {
+                    F[p] = R2[p];
+                    C[p].temporal = 1;
+                    continue;
+                }
+                V fl = vdivs(srad, swt);
+                float fv = svar / (swt * swt);
+                float cw = 0.2f;
+                V out = vadd(vmul(vmulv(fl, C[p].albedo), cw), vmul(R2[p], (1 - cw)));
+                F[p] = out;
+                R[p] = out;
+                if (C[p].atrous) C[p].variance = cw * var2[p] + (1 - cw) * fv;
+                if (stage == 0) {
+                    C[p].history = out;
+                    C[p].temporal = 1;
+                }
+            }
+        }
+    }
+    for (int p = 0; p < npx; ++p) R[p] = C[p].history;
+    free(M1); free(M2); free(sd); free(spatial); free(sw); free(s1); free(s2);
+    free(R2); free(var2); free(gz);
+}

@@ -81,6 +81,10 @@ int64_t orc_render_compat_px(const void *tris, int64_t n, const void *mats, cons
                              const float *hdr, int hdr_w, int hdr_h, int hdr_bpp, const void *cam,
                              int width, int height, const int32_t *px_list, int64_t n_px, int nthreads,
                              float *out);
+/* ApplySVGF (SVGF.cuh:495-522) in its race-free reading: every
+ * __syncthreads() is a barrier over the whole image.  result, filtered: npx
+ * Vec; prev, cur: npx SVGFBuffer records (112 B, struct_SVGFBuffers.cuh). */
+void orc_svgf_compat(int W, int H, float *result, float *filtered, void *prev, void *cur, int frame);
 /* Selects the argument order of SamplePointOnTriangle's two random numbers
  * (1 = right to left, the reference host build's order). */
 void orc_set_point_arg_order(int rtl);

@@ -62,6 +62,7 @@ def orc():
         L.orc_render_compat_px.argtypes = [_vp, _i64, _vp, _vp, _vp, _i32, _i32, _i32, _vp, _i32, _i32,
                                            _vp, _i64, _i32, _vp]
         L.orc_render_compat_px.restype = _i64
+        L.orc_svgf_compat.argtypes = [_i32, _i32, _vp, _vp, _vp, _vp, _i32]
         _orc = L
     return _orc
 
@@ -150,6 +151,12 @@ def render_compat(tris, mats, cam, width, height, frames, env=None, threads=None
                                 hh, hb, _ptr(cam), width, height, frames,
                                 threads or nthreads(), _ptr(out))
     return out, n
+
+
+def svgf_compat(width, height, result, filtered, prev, cur, frame):
+    """In-place ApplySVGF over numpy buffers (result/filtered (npx,4) f32,
+    prev/cur uint8 arrays of 112-byte SVGFBuffer records)."""
+    orc().orc_svgf_compat(width, height, _ptr(result), _ptr(filtered), _ptr(prev), _ptr(cur), frame)
 
 
 class CpuBvh:

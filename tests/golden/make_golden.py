@@ -128,6 +128,29 @@ def main():
     ecdf = np.zeros(64 * 32, np.float32)
     orc.ref().ref_env_cdf(env.ctypes.data, 64, 32, 3, ecdf.ctypes.data)
     np.savez_compressed(os.path.join(HERE, "cdf_ref.npz"), light=lcdf, env=env, env_cdf=ecdf)
+    # --- SVGF: ApplySVGF over a reference-rendered G-buffer, two frames ---
+    SW, SH = 40, 24
+    cs = orc.camera_setup(cam["origin"], cam["dist"], cam["rot"], SH)
+    frames2, _, gb = orc.ref_render(tris, mats, cs, SW, SH, 2, gbuf=True)
+    sz = orc.ref().ref_sizeof_svgfbuffer()
+    npx = SW * SH
+    def vec(img):
+        v = np.zeros((npx, 4), np.float32)
+        v[:, :3] = np.nan_to_num(img, nan=0.0)
+        return v
+    res0, res1 = vec(frames2[0]), vec(frames2[1])
+    prev = np.zeros(npx * sz, np.uint8)
+    cur = gb.copy()
+    r0, f0 = res0.copy(), np.zeros_like(res0)
+    assert orc.ref().ref_svgf(SW, SH, r0.ctypes.data, f0.ctypes.data, prev.ctypes.data, cur.ctypes.data, 0) == 0
+    cur0 = cur.copy()
+    prev1 = cur0.copy()
+    cur1 = gb.copy()
+    r1, f1 = res1.copy(), np.zeros_like(res1)
+    assert orc.ref().ref_svgf(SW, SH, r1.ctypes.data, f1.ctypes.data, prev1.ctypes.data, cur1.ctypes.data, 1) == 0
+    np.savez_compressed(os.path.join(HERE, "svgf_ref.npz"), width=SW, height=SH, gbuf=gb, res0=res0, res1=res1,
+                        out_result0=r0, out_filtered0=f0, out_cur0=cur0, out_result1=r1, out_filtered1=f1,
+                        out_cur1=cur1, record_size=sz)
     print("golden fixtures written to", HERE)
 
 
