@@ -36,6 +36,7 @@ PROTOTYPES = {
     "kgk_accum_reset": (_st, [_vp, _i32, _i32]),
     "kgk_accum_read": (_st, [_vp, _vp, _vp, ctypes.POINTER(ctypes.c_uint64)]),
     "kgk_svgf": (_st, [_vp, ctypes.POINTER(KgkSvgfConfig), _vp, _vp]),
+    "kgk_svgf_apply": (_st, [_vp, _vp, _vp, _vp, _i32, _i32, _i32]),
     "kgk_tonemap_rgba8": (_st, [_vp, _i32, _i32, _vp]),
     "kgk_save_png": (_st, [_vp, _i32, _i32, ctypes.c_char_p]),
 }

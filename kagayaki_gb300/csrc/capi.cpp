@@ -165,6 +165,7 @@ void kgk_scene_destroy(kgk_scene *s) {
     cudaSetDevice(s->device);
     if (s->stream) cudaStreamSynchronize(s->stream);
     render_state_free(s);
+    svgf_state_free(s);
     scene_free(s->dev);
     if (s->stream) cudaStreamDestroy(s->stream);
     delete s;

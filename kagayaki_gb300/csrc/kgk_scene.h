@@ -17,6 +17,24 @@ struct RenderState;  // render.cu
 void render_state_free(kgk_scene *s);
 bool is_device_ptr(const void *p);
 
+// SVGF history kept across frames (svgf.cu).
+struct SvgfState {
+    int W = 0, H = 0;
+    kgk_svgf_buffer *prev = nullptr, *cur = nullptr;   // compat: reference-layout records
+    float4 *hist = nullptr, *hist_prev = nullptr;      // standard: demodulated colour, w = history length
+    float2 *mom = nullptr, *mom_prev = nullptr;        // standard: luminance moments
+    float4 *nd_prev = nullptr;                         // previous normal + depth
+    int *mat_prev = nullptr;                           // previous material id (-1 = no hit)
+    float4 *col = nullptr, *tmp = nullptr;             // colour + variance ping-pong
+    float *gvar = nullptr;                             // 3x3-blurred variance
+    kgk_camera prev_cam{};
+    bool has_prev = false;
+};
+void svgf_state_free(kgk_scene *s);
+// The G-buffer and camera of the last frame rendered with write_gbuffer=1.
+bool svgf_gbuffer(kgk_scene *s, int *W, int *H, const float4 **pos, const float4 **nrm, const float4 **alb,
+                  const float4 **emi, kgk_camera *cam);
+
 }  // namespace kgk
 
 struct kgk_scene {
@@ -26,4 +44,5 @@ struct kgk_scene {
     bool built = false;
     kgk::Staging staging;
     kgk::RenderState *rs = nullptr;
+    kgk::SvgfState *svgf = nullptr;
 };

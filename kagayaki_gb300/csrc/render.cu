@@ -47,6 +47,8 @@ struct RenderState {
     int *cnt = nullptr;                       // queue counters
     unsigned long long *stats = nullptr;      // rays_closest, rays_shadow, overflow, nodes, tris
     int sms = 0;
+    bool gbuffer_valid = false;               // G-buffer written by the last frame
+    kgk_camera gbuffer_cam{};
 };
 
 namespace {
@@ -783,6 +785,20 @@ RenderState *render_state(kgk_scene *s) {
     return s->rs;
 }
 
+bool svgf_gbuffer(kgk_scene *s, int *W, int *H, const float4 **pos, const float4 **nrm, const float4 **alb,
+                  const float4 **emi, kgk_camera *cam) {
+    RenderState *R = s->rs;
+    if (!R || !R->gbuffer_valid) return false;
+    *W = R->W;
+    *H = R->H;
+    *pos = R->gb_pos;
+    *nrm = R->gb_nrm;
+    *alb = R->gb_alb;
+    *emi = R->gb_emi;
+    *cam = R->gbuffer_cam;
+    return true;
+}
+
 }  // namespace kgk
 
 using namespace kgk;
@@ -921,6 +937,10 @@ kgk_status kgk_render(kgk_scene *s, const kgk_camera *cam, const kgk_camera *pre
         ++launches;
     }
     if (cfg->accumulate) R.acc_n += (unsigned long long)cfg->spp;
+    if (cfg->write_gbuffer) {
+        R.gbuffer_valid = true;
+        R.gbuffer_cam = *cam;
+    }
     // output
     const bool od = is_device_ptr(out);
     float4 *dout;
@@ -1008,9 +1028,6 @@ kgk_status kgk_accum_read(kgk_scene *s, double *mean, double *var, uint64_t *n_s
     return KGK_OK;
 }
 
-kgk_status kgk_svgf(kgk_scene *, const kgk_svgf_config *, const kgk_vec *, kgk_vec *) {
-    return fail(KGK_ERR_UNSUPPORTED, "kgk_svgf: not built yet");
-}
 kgk_status kgk_scene_load_obj(const char *, const char *, kgk_scene **) {
     return fail(KGK_ERR_UNSUPPORTED, "kgk_scene_load_obj: not built yet");
 }

@@ -27,27 +27,6 @@ static_assert(offsetof(kgk_svgf_buffer, willApplyATrousFilter) == 108, "SVGFBuff
 
 namespace kgk {
 
-struct RenderState;
-struct SvgfState {
-    int W = 0, H = 0;
-    // compat
-    kgk_svgf_buffer *prev = nullptr, *cur = nullptr;
-    // standard (SoA)
-    float4 *hist = nullptr, *hist_prev = nullptr;      // demodulated colour history, w = history length
-    float2 *mom = nullptr, *mom_prev = nullptr;        // luminance moments
-    float4 *nd_prev = nullptr;                         // previous normal + depth
-    int *mat_prev = nullptr;                           // previous material id (-1 = no hit)
-    float4 *col = nullptr, *tmp = nullptr;             // colour + variance ping-pong
-    float *gvar = nullptr;                             // 3x3-blurred variance
-    kgk_camera prev_cam{};
-    bool has_prev = false;
-};
-
-SvgfState *svgf_state(kgk_scene *s);
-void svgf_state_free(kgk_scene *s);
-bool svgf_gbuffer(kgk_scene *s, int *W, int *H, const float4 **pos, const float4 **nrm, const float4 **alb,
-                  const float4 **emi, kgk_camera *cam);
-
 namespace {
 
 constexpr float kS = 1e-4f;  // sINF
@@ -706,6 +685,18 @@ void svgf_state_free_impl(SvgfState *S) {
     void *ptrs[] = {S->prev, S->cur, S->hist, S->hist_prev, S->mom, S->mom_prev, S->nd_prev, S->mat_prev,
                     S->col, S->tmp, S->gvar};
     for (void *p : ptrs) dfree(p);
+}
+
+void svgf_state_free(kgk_scene *s) {
+    if (!s->svgf) return;
+    svgf_state_free_impl(s->svgf);
+    delete s->svgf;
+    s->svgf = nullptr;
+}
+
+SvgfState *svgf_state(kgk_scene *s) {
+    if (!s->svgf) s->svgf = new SvgfState();
+    return s->svgf;
 }
 
 }  // namespace kgk

@@ -112,3 +112,21 @@ def test_tonemap_rule():
     exp = np.nan_to_num(exp, nan=0.0)
     assert np.array_equal(out[:, :3], (exp * 255).astype(np.uint8))
     assert (out[:, 3] == 255).all()
+
+
+def test_svgf_restatement_bit_exact_with_reference():
+    g = golden("svgf_ref.npz")
+    W, H = int(g["width"]), int(g["height"])
+    npx = W * H
+    prev = np.zeros(npx * 112, np.uint8)
+    cur = g["gbuf"].copy()
+    r0, f0 = g["res0"].copy(), np.zeros_like(g["res0"])
+    orc.svgf_compat(W, H, r0, f0, prev, cur, 0)
+    assert np.array_equal(f0, g["out_filtered0"])
+    assert np.array_equal(r0, g["out_result0"])
+    assert np.array_equal(cur, g["out_cur0"])
+    prev1, cur1 = cur.copy(), g["gbuf"].copy()
+    r1, f1 = g["res1"].copy(), np.zeros_like(g["res1"])
+    orc.svgf_compat(W, H, r1, f1, prev1, cur1, 1)
+    assert np.array_equal(f1, g["out_filtered1"])
+    assert np.array_equal(cur1, g["out_cur1"])
