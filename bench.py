@@ -152,6 +152,12 @@ def run_ours(args):
         dist = td
     kg.lib().kgk_set_device(local)
     tris, mats, env, info = build_workload()
+    if args.width:
+        WORKLOAD["width"] = args.width
+    if args.height:
+        WORKLOAD["height"] = args.height
+    if args.spp:
+        WORKLOAD["spp"] = args.spp
     W, H, spp = WORKLOAD["width"], WORKLOAD["height"], WORKLOAD["spp"]
     scene = Scene(tris, mats, env=env)
     bvh = scene.build_bvh()
@@ -166,11 +172,7 @@ def run_ours(args):
         dist.barrier()
     clocks = ClockSampler()
     clocks.start()
-    # timed: device-resident output (value)
-    import ctypes
-    dev_out = ctypes.c_void_p()
-    from kagayaki_gb300._lib import lib as _l
-    cudart = None
+    # timed: device time of each frame (CUDA events on the library's stream)
     rays = 0
     dev_ms = 0.0
     launches = 0
@@ -280,7 +282,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU baseline work budget")
-    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
+    ap.add_argument("--width", type=int, default=0, help="override the frame width (profiling cases)")
+    ap.add_argument("--height", type=int, default=0, help="override the frame height")
+    ap.add_argument("--spp", type=int, default=0, help="override the samples per pixel")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
