@@ -306,6 +306,47 @@ kgk_status kgk_svgf_apply(kgk_vec *result, kgk_vec *filtered, kgk_svgf_buffer *p
                           kgk_svgf_buffer *cur, int32_t width, int32_t height, int32_t frame);
 
 /* ------------------------------------------------------------------------- */
+/* Learned radiance cache (no counterpart in the reference)                    */
+/* ------------------------------------------------------------------------- */
+
+/* A small MLP (64 encoded inputs -> 5 hidden layers of 64, ReLU -> RGB) that
+ * kgk_render(use_cache=1) queries where a path's spread exceeds the pixel
+ * footprint, trained online every frame on the tracer's own radiance samples.
+ * BF16 weights and activations on the tensor cores, FP32 accumulation, FP32
+ * master weights, Adam, relative-L2 loss with dynamic loss scaling.
+ * Raw query = 13 floats: position normalised to the scene box (3), shading
+ * normal (3), direction toward the viewer (3), roughness, albedo (3). */
+typedef struct kgk_nrc_config {
+    int32_t width;              /* hidden width: 64                              */
+    int32_t hidden_layers;      /* 5                                             */
+    float learning_rate;        /* Adam, 1e-2                                    */
+    int32_t train_paths;        /* training paths per frame, 65,536              */
+    int32_t train_suffix_max;   /* bounces a training path runs past its query, 4 */
+    int32_t train_steps;        /* Adam steps per frame, 4                       */
+    float spread_c;             /* termination: path spread^2 > c * footprint^2  */
+    uint64_t seed;              /* weight initialisation                          */
+    int32_t reserved[8];
+} kgk_nrc_config;
+
+/* (Re)initialises the scene's cache with He-uniform weights. */
+kgk_status kgk_nrc_init(kgk_scene *scene, const kgk_nrc_config *cfg);
+/* FP32 master weights, layer by layer, each (out, in) row-major: 5 x (64 x 64)
+ * then 3 x 64 (20,672 floats). */
+kgk_status kgk_nrc_set_weights(kgk_scene *scene, const float *w, size_t n);
+kgk_status kgk_nrc_get_weights(kgk_scene *scene, float *w, size_t n);
+/* Predictions (n x 3) for n raw queries (n x 13). */
+kgk_status kgk_nrc_infer(kgk_scene *scene, const float *raw, size_t n, float *out);
+/* Gradient of the mean relative-L2 loss over the batch w.r.t. the weights
+ * (20,672 floats, loss scale removed) and the loss; weights unchanged. */
+kgk_status kgk_nrc_gradients(kgk_scene *scene, const float *raw, const float *target, size_t n,
+                             float *grad, float *loss);
+/* `steps` Adam steps on one batch; loss = the last step's loss. */
+kgk_status kgk_nrc_train(kgk_scene *scene, const float *raw, const float *target, size_t n,
+                         int32_t steps, float *loss);
+/* Current dynamic loss scale. */
+kgk_status kgk_nrc_loss_scale(kgk_scene *scene, float *scale);
+
+/* ------------------------------------------------------------------------- */
 /* Image output (replaces save_png, FileIO/IO_save_png.cuh:34-56)              */
 /* ------------------------------------------------------------------------- */
 

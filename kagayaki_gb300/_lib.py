@@ -37,6 +37,13 @@ PROTOTYPES = {
     "kgk_accum_read": (_st, [_vp, _vp, _vp, ctypes.POINTER(ctypes.c_uint64)]),
     "kgk_svgf": (_st, [_vp, ctypes.POINTER(KgkSvgfConfig), _vp, _vp]),
     "kgk_svgf_apply": (_st, [_vp, _vp, _vp, _vp, _i32, _i32, _i32]),
+    "kgk_nrc_init": (_st, [_vp, _vp]),
+    "kgk_nrc_set_weights": (_st, [_vp, _vp, _sz]),
+    "kgk_nrc_get_weights": (_st, [_vp, _vp, _sz]),
+    "kgk_nrc_infer": (_st, [_vp, _vp, _sz, _vp]),
+    "kgk_nrc_gradients": (_st, [_vp, _vp, _vp, _sz, _vp, _vp]),
+    "kgk_nrc_train": (_st, [_vp, _vp, _vp, _sz, _i32, _vp]),
+    "kgk_nrc_loss_scale": (_st, [_vp, _vp]),
     "kgk_tonemap_rgba8": (_st, [_vp, _i32, _i32, _vp]),
     "kgk_save_png": (_st, [_vp, _i32, _i32, ctypes.c_char_p]),
 }

@@ -16,8 +16,8 @@ import numpy as np
 
 from . import _lib
 from ._lib import KgkError, check, lib
-from .structs import (MATERIAL, RAY, TRIANGLE, KgkBvhInfo, KgkCamera, KgkRenderConfig, KgkStats,
-                      KgkSvgfConfig, KgkTexture, KgkVec)
+from .structs import (MATERIAL, RAY, TRIANGLE, KgkBvhInfo, KgkCamera, KgkNrcConfig, KgkRenderConfig,
+                      KgkStats, KgkSvgfConfig, KgkTexture, KgkVec)
 
 ESTIMATOR_COMPAT = 0
 ESTIMATOR_UNBIASED = 1
@@ -129,6 +129,13 @@ class Scene:
                                ctypes.byref(prev_cam) if prev_cam is not None else None,
                                ctypes.byref(cfg), _p(out), ctypes.byref(st)))
         return out, stats_dict(st)
+
+    def cache_init(self, **cfg):
+        """(Re)initialises the learned radiance cache used by
+        render(use_cache=True); keyword arguments are kgk_nrc_config fields
+        (0 / absent = the library default)."""
+        c = KgkNrcConfig(**cfg)
+        check(lib().kgk_nrc_init(self._h, ctypes.byref(c)))
 
     def accum_reset(self, width, height):
         check(lib().kgk_accum_reset(self._h, width, height))

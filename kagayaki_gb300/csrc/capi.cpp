@@ -166,6 +166,7 @@ void kgk_scene_destroy(kgk_scene *s) {
     if (s->stream) cudaStreamSynchronize(s->stream);
     render_state_free(s);
     svgf_state_free(s);
+    nrc_state_free(s);
     scene_free(s->dev);
     if (s->stream) cudaStreamDestroy(s->stream);
     delete s;

@@ -89,6 +89,8 @@ struct DevScene {
     float *emit_cdf = nullptr;       // unbiased: normalised CDF over emit_ids (n+1)
     int32_t n_emit = 0;
     float emit_total = 0.0f;         // sum of area * |emission| (double-summed)
+    // Bounding box of all vertices (normalises radiance-cache positions).
+    float lo[3] = {0, 0, 0}, hi[3] = {1, 1, 1};
     // BVH.
     WideNode *nodes = nullptr;
     int32_t n_nodes = 0;

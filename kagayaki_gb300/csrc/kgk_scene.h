@@ -14,6 +14,7 @@ struct Staging {
 };
 
 struct RenderState;  // render.cu
+struct NrcState;     // nrc.cu
 void render_state_free(kgk_scene *s);
 bool is_device_ptr(const void *p);
 
@@ -31,6 +32,7 @@ struct SvgfState {
     bool has_prev = false;
 };
 void svgf_state_free(kgk_scene *s);
+void nrc_state_free(kgk_scene *s);
 // The G-buffer and camera of the last frame rendered with write_gbuffer=1.
 bool svgf_gbuffer(kgk_scene *s, int *W, int *H, const float4 **pos, const float4 **nrm, const float4 **alb,
                   const float4 **emi, kgk_camera *cam);
@@ -45,4 +47,5 @@ struct kgk_scene {
     kgk::Staging staging;
     kgk::RenderState *rs = nullptr;
     kgk::SvgfState *svgf = nullptr;
+    kgk::NrcState *nrc = nullptr;
 };

@@ -1,0 +1,685 @@
+// nrc.cu - learned radiance cache: a fully fused MLP (64 -> 5 x 64 ReLU -> 3,
+// no biases) in BF16 on the tensor cores with FP32 accumulation.
+//
+// One warp carries 16 samples through every layer with mma.sync m16n8k16:
+// the FP32 accumulator fragment of one layer, rounded to BF16 after the
+// ReLU, is exactly the A-operand fragment of the next layer, so activations
+// stay in registers.  Weights live in shared memory as a BF16 image with a
+// 72-element row pitch (bank-conflict-free fragment loads).
+// Training fuses forward, relative-L2 loss (scaled by a dynamic loss scale),
+// backward and the weight-gradient GEMMs; each CTA accumulates dW in shared
+// memory (FP32) and adds it to the global gradient once.  Adam updates FP32
+// master weights and rewrites the BF16 image.
+// No counterpart in the reference.
+#include <cuda_bf16.h>
+
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "kgk_device.cuh"
+#include "kgk_nrc.h"
+#include "kgk_scene.h"
+
+namespace kgk {
+namespace nrc {
+
+__device__ __forceinline__ uint32_t pack2(float lo, float hi) {
+    __nv_bfloat162 h = __floats2bfloat162_rn(lo, hi);
+    return *reinterpret_cast<uint32_t *>(&h);
+}
+__device__ __forceinline__ uint32_t pack_raw(unsigned short lo, unsigned short hi) {
+    return (uint32_t)lo | ((uint32_t)hi << 16);
+}
+__device__ __forceinline__ float bf2f(unsigned short b) { return __uint_as_float((uint32_t)b << 16); }
+
+__device__ __forceinline__ void mma16816(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};\n"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// One input feature (column c of the 64-float encoding) of a raw query.
+__device__ __forceinline__ float encode_col(const float *raw, int c) {
+    if (c < 36) {
+        const int ax = c / 12, k = (c % 12) >> 1;
+        float s, co;
+        sincospif(raw[ax] * (float)(1 << k), &s, &co);
+        return (c & 1) ? co : s;
+    }
+    if (c < 42) return raw[3 + (c - 36)];  // normal, view
+    if (c < 54) {
+        const int j = c - 42;
+        const float x = raw[3 + (j / 6) * 3 + ((j % 6) >> 1)];
+        float s, co;
+        sincospif(x, &s, &co);
+        return (j & 1) ? co : s;
+    }
+    if (c < 58) return raw[9 + (c - 54)];  // roughness, albedo
+    return 1.0f;
+}
+
+// Input-layer A fragments of the warp's 16 samples (rows g and g + 8).
+__device__ __forceinline__ void encode_frags(const float *ra, const float *rb, uint32_t (&a)[4][4]) {
+    const int t = threadIdx.x & 3;
+#pragma unroll
+    for (int kt = 0; kt < 4; ++kt) {
+        const int c0 = kt * 16 + 2 * t;
+        a[kt][0] = pack2(encode_col(ra, c0), encode_col(ra, c0 + 1));
+        a[kt][1] = pack2(encode_col(rb, c0), encode_col(rb, c0 + 1));
+        a[kt][2] = pack2(encode_col(ra, c0 + 8), encode_col(ra, c0 + 9));
+        a[kt][3] = pack2(encode_col(rb, c0 + 8), encode_col(rb, c0 + 9));
+    }
+}
+
+// acc[nt] = A (16 x 64) * W^T (64 x 64) for one hidden layer; W row-major
+// [out][in] in shared memory with pitch kPitch.
+__device__ __forceinline__ void layer_fwd(const unsigned short *W, const uint32_t (&a)[4][4], float (&acc)[8][4]) {
+    const int g = (threadIdx.x & 31) >> 2, t = threadIdx.x & 3;
+#pragma unroll
+    for (int nt = 0; nt < 8; ++nt) {
+        acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.0f;
+        const unsigned short *row = W + (nt * 8 + g) * kPitch;
+#pragma unroll
+        for (int kt = 0; kt < 4; ++kt) {
+            const uint32_t b0 = *reinterpret_cast<const uint32_t *>(row + kt * 16 + 2 * t);
+            const uint32_t b1 = *reinterpret_cast<const uint32_t *>(row + kt * 16 + 8 + 2 * t);
+            mma16816(acc[nt], a[kt], b0, b1);
+        }
+    }
+}
+
+__device__ __forceinline__ void out_fwd(const unsigned short *W, const uint32_t (&a)[4][4], float (&acc)[4]) {
+    const int g = (threadIdx.x & 31) >> 2, t = threadIdx.x & 3;
+    acc[0] = acc[1] = acc[2] = acc[3] = 0.0f;
+    const unsigned short *row = W + g * kPitch;
+#pragma unroll
+    for (int kt = 0; kt < 4; ++kt) {
+        const uint32_t b0 = *reinterpret_cast<const uint32_t *>(row + kt * 16 + 2 * t);
+        const uint32_t b1 = *reinterpret_cast<const uint32_t *>(row + kt * 16 + 8 + 2 * t);
+        mma16816(acc, a[kt], b0, b1);
+    }
+}
+
+// C fragments (after ReLU) -> BF16 A fragments of the next layer.
+__device__ __forceinline__ void relu_to_frags(const float (&acc)[8][4], uint32_t (&a)[4][4]) {
+#pragma unroll
+    for (int kt = 0; kt < 4; ++kt) {
+        a[kt][0] = pack2(fmaxf(acc[2 * kt][0], 0.0f), fmaxf(acc[2 * kt][1], 0.0f));
+        a[kt][1] = pack2(fmaxf(acc[2 * kt][2], 0.0f), fmaxf(acc[2 * kt][3], 0.0f));
+        a[kt][2] = pack2(fmaxf(acc[2 * kt + 1][0], 0.0f), fmaxf(acc[2 * kt + 1][1], 0.0f));
+        a[kt][3] = pack2(fmaxf(acc[2 * kt + 1][2], 0.0f), fmaxf(acc[2 * kt + 1][3], 0.0f));
+    }
+}
+
+// Stores A fragments (16 x 64 BF16) into a [16][kPitch] shared tile.
+__device__ __forceinline__ void store_frags(unsigned short *T, const uint32_t (&a)[4][4]) {
+    const int g = (threadIdx.x & 31) >> 2, t = threadIdx.x & 3;
+#pragma unroll
+    for (int kt = 0; kt < 4; ++kt) {
+        const int c = kt * 16 + 2 * t;
+        *reinterpret_cast<uint32_t *>(T + g * kPitch + c) = a[kt][0];
+        *reinterpret_cast<uint32_t *>(T + (g + 8) * kPitch + c) = a[kt][1];
+        *reinterpret_cast<uint32_t *>(T + g * kPitch + c + 8) = a[kt][2];
+        *reinterpret_cast<uint32_t *>(T + (g + 8) * kPitch + c + 8) = a[kt][3];
+    }
+}
+
+__device__ __forceinline__ void load_image(unsigned short *dst, const unsigned short *src) {
+    const int n16 = kImgElems * 2 / 16;
+    const uint4 *s = reinterpret_cast<const uint4 *>(src);
+    uint4 *d = reinterpret_cast<uint4 *>(dst);
+    for (int i = threadIdx.x; i < n16; i += blockDim.x) d[i] = s[i];
+}
+
+// ---------------------------------------------------------------------------
+// inference
+// ---------------------------------------------------------------------------
+// Query record: raw[13], T[3] (path throughput), path id, pad -> 5 float4.
+__global__ void __launch_bounds__(256) k_infer(const unsigned short *__restrict__ img, const float *__restrict__ raw,
+                                               int stride_floats, int n, const int *n_dev, float *out, float4 *rad) {
+    extern __shared__ __align__(16) unsigned short sW[];
+    load_image(sW, img);
+    __syncthreads();
+    const int total = n_dev ? *n_dev : n;
+    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (int base = warp * 16; base < total; base += nwarps * 16) {
+        const int sa = base + g, sb = base + g + 8;
+        float ra[kRaw], rb[kRaw];
+#pragma unroll
+        for (int k = 0; k < kRaw; ++k) {
+            ra[k] = sa < total ? raw[(size_t)sa * stride_floats + k] : 0.0f;
+            rb[k] = sb < total ? raw[(size_t)sb * stride_floats + k] : 0.0f;
+        }
+        uint32_t a[4][4];
+        encode_frags(ra, rb, a);
+        float acc[8][4];
+#pragma unroll 1
+        for (int l = 0; l < kLayers; ++l) {
+            layer_fwd(sW + l * kWidth * kPitch, a, acc);
+            relu_to_frags(acc, a);
+        }
+        float y[4];
+        out_fwd(sW + kLayers * kWidth * kPitch, a, y);
+        // lanes t = 0, 1 hold outputs 0..3 of samples g and g + 8
+        if (t < 2) {
+            const int cols[2] = {2 * t, 2 * t + 1};
+            const int s2[2] = {sa, sb};
+            for (int r = 0; r < 2; ++r) {
+                const int s = s2[r];
+                if (s >= total) continue;
+                for (int k = 0; k < 2; ++k) {
+                    const int c = cols[k];
+                    if (c > 2) continue;
+                    const float v = y[2 * r + k];
+                    if (out) out[(size_t)s * 3 + c] = v;
+                    if (rad) {
+                        // cache termination: rad[path] += T * max(y, 0)
+                        const float *rec = raw + (size_t)s * stride_floats;
+                        const int path = __float_as_int(rec[16]);
+                        const float add = rec[13 + c] * fmaxf(v, 0.0f);
+                        float *rp = reinterpret_cast<float *>(rad + path) + c;
+                        *rp += add;
+                    }
+                }
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// training: forward + loss + backward + dW
+// ---------------------------------------------------------------------------
+struct TrainSmem {
+    // layout inside dynamic shared memory
+    static constexpr size_t img = 0;
+    static constexpr size_t dw = ((size_t)kImgElems * 2 + 15) & ~(size_t)15;
+    static constexpr size_t dw_floats = (size_t)kLayers * kWidth * kWidth + (size_t)kOutRows * kWidth;
+    static constexpr size_t warps = dw + dw_floats * 4;
+    static constexpr size_t per_warp = (size_t)(kLayers + 2) * 16 * kPitch * 2;  // acts 0..L, dZ stage
+    static constexpr size_t total(int nw) { return warps + per_warp * nw; }
+};
+
+__device__ __forceinline__ void dw_accumulate(float *dWl, const unsigned short *dZs, const unsigned short *A, int mtiles,
+                                              int valid_rows) {
+    const int g = (threadIdx.x & 31) >> 2, t = threadIdx.x & 3;
+    for (int mt = 0; mt < mtiles; ++mt) {
+        uint32_t a[4];
+        const int o0 = mt * 16 + g, o1 = o0 + 8;
+        a[0] = pack_raw(dZs[(2 * t) * kPitch + o0], dZs[(2 * t + 1) * kPitch + o0]);
+        a[1] = pack_raw(dZs[(2 * t) * kPitch + o1], dZs[(2 * t + 1) * kPitch + o1]);
+        a[2] = pack_raw(dZs[(2 * t + 8) * kPitch + o0], dZs[(2 * t + 9) * kPitch + o0]);
+        a[3] = pack_raw(dZs[(2 * t + 8) * kPitch + o1], dZs[(2 * t + 9) * kPitch + o1]);
+#pragma unroll
+        for (int nt = 0; nt < 8; ++nt) {
+            const int i = nt * 8 + g;
+            const uint32_t b0 = pack_raw(A[(2 * t) * kPitch + i], A[(2 * t + 1) * kPitch + i]);
+            const uint32_t b1 = pack_raw(A[(2 * t + 8) * kPitch + i], A[(2 * t + 9) * kPitch + i]);
+            float c[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+            mma16816(c, a, b0, b1);
+            const int col = nt * 8 + 2 * t;
+            if (o0 < valid_rows) {
+                atomicAdd(&dWl[o0 * kWidth + col], c[0]);
+                atomicAdd(&dWl[o0 * kWidth + col + 1], c[1]);
+            }
+            if (o1 < valid_rows) {
+                atomicAdd(&dWl[o1 * kWidth + col], c[2]);
+                atomicAdd(&dWl[o1 * kWidth + col + 1], c[3]);
+            }
+        }
+    }
+}
+
+// Stores C fragments (16 x 64, FP32) as a BF16 [16][kPitch] tile.
+__device__ __forceinline__ void store_acc(unsigned short *T, const float (&acc)[8][4]) {
+    const int g = (threadIdx.x & 31) >> 2, t = threadIdx.x & 3;
+#pragma unroll
+    for (int nt = 0; nt < 8; ++nt) {
+        const int c = nt * 8 + 2 * t;
+        *reinterpret_cast<uint32_t *>(T + g * kPitch + c) = pack2(acc[nt][0], acc[nt][1]);
+        *reinterpret_cast<uint32_t *>(T + (g + 8) * kPitch + c) = pack2(acc[nt][2], acc[nt][3]);
+    }
+}
+
+__global__ void __launch_bounds__(128) k_train(const unsigned short *__restrict__ img, const float *__restrict__ raw,
+                                               int raw_stride, const float *__restrict__ target, int tgt_stride,
+                                               int n, const int *n_dev, const float *scale_p, float *dW_glob,
+                                               float *loss_sum) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    unsigned short *sW = reinterpret_cast<unsigned short *>(smem + TrainSmem::img);
+    float *sdW = reinterpret_cast<float *>(smem + TrainSmem::dw);
+    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3, wid = threadIdx.x >> 5;
+    unsigned short *acts = reinterpret_cast<unsigned short *>(smem + TrainSmem::warps + TrainSmem::per_warp * wid);
+    unsigned short *dzs = acts + (kLayers + 1) * 16 * kPitch;
+    load_image(sW, img);
+    for (size_t i = threadIdx.x; i < TrainSmem::dw_floats; i += blockDim.x) sdW[i] = 0.0f;
+    __syncthreads();
+    const int total = n_dev ? *n_dev : n;
+    const float S = *scale_p;
+    const float inv_n = 1.0f / (3.0f * (float)max(total, 1));
+    float lsum = 0.0f;
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (int base = warp * 16; base < total; base += nwarps * 16) {
+        const int sa = base + g, sb = base + g + 8;
+        float ra[kRaw], rb[kRaw];
+#pragma unroll
+        for (int k = 0; k < kRaw; ++k) {
+            ra[k] = sa < total ? raw[(size_t)sa * raw_stride + k] : 0.0f;
+            rb[k] = sb < total ? raw[(size_t)sb * raw_stride + k] : 0.0f;
+        }
+        uint32_t a[4][4];
+        encode_frags(ra, rb, a);
+        store_frags(acts, a);
+        float acc[8][4];
+#pragma unroll 1
+        for (int l = 0; l < kLayers; ++l) {
+            layer_fwd(sW + l * kWidth * kPitch, a, acc);
+            relu_to_frags(acc, a);
+            store_frags(acts + (l + 1) * 16 * kPitch, a);
+        }
+        float y[4];
+        out_fwd(sW + kLayers * kWidth * kPitch, a, y);
+        // relative L2: d/dy (y - t)^2 / (y^2 + eps), denominator held constant
+        float dy[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+#pragma unroll
+        for (int r = 0; r < 2; ++r) {
+            const int s = r == 0 ? sa : sb;
+#pragma unroll
+            for (int k = 0; k < 2; ++k) {
+                const int c = 2 * t + k;
+                if (c > 2 || s >= total) continue;
+                const float yy = y[2 * r + k];
+                const float tt = target[(size_t)s * tgt_stride + c];
+                const float den = yy * yy + kEpsRel;
+                const float d = yy - tt;
+                lsum += d * d / den;
+                dy[2 * r + k] = 2.0f * d / den * inv_n * S;
+            }
+        }
+        // output layer: dZ_out (16 x 8, cols 0..2 live) staged as BF16
+        __syncwarp();
+        {
+            float tile[8][4];
+#pragma unroll
+            for (int nt = 0; nt < 8; ++nt) tile[nt][0] = tile[nt][1] = tile[nt][2] = tile[nt][3] = 0.0f;
+            tile[0][0] = dy[0]; tile[0][1] = dy[1]; tile[0][2] = dy[2]; tile[0][3] = dy[3];
+            store_acc(dzs, tile);
+        }
+        __syncwarp();
+        dw_accumulate(sdW + kLayers * kWidth * kWidth, dzs, acts + kLayers * 16 * kPitch, 1, 3);
+        // dA_L = dZ_out (16 x 16, cols >= 8 zero) * W_out (16 x 64)
+        uint32_t dza[4];
+        dza[0] = pack2(dy[0], dy[1]);
+        dza[1] = pack2(dy[2], dy[3]);
+        dza[2] = 0u;
+        dza[3] = 0u;
+        {
+            const unsigned short *Wo = sW + kLayers * kWidth * kPitch;
+#pragma unroll
+            for (int nt = 0; nt < 8; ++nt) {
+                acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.0f;
+                const int i = nt * 8 + g;
+                const uint32_t b0 = pack_raw(Wo[(2 * t) * kPitch + i], Wo[(2 * t + 1) * kPitch + i]);
+                const uint32_t b1 = pack_raw(Wo[(2 * t + 8) * kPitch + i], Wo[(2 * t + 9) * kPitch + i]);
+                mma16816(acc[nt], dza, b0, b1);
+            }
+        }
+#pragma unroll 1
+        for (int l = kLayers - 1; l >= 0; --l) {
+            // dZ_l = dA_l * relu'(h_l); h_l is activation l + 1 in `acts`
+            const unsigned short *H = acts + (l + 1) * 16 * kPitch;
+#pragma unroll
+            for (int nt = 0; nt < 8; ++nt) {
+                const int c = nt * 8 + 2 * t;
+                if (bf2f(H[g * kPitch + c]) <= 0.0f) acc[nt][0] = 0.0f;
+                if (bf2f(H[g * kPitch + c + 1]) <= 0.0f) acc[nt][1] = 0.0f;
+                if (bf2f(H[(g + 8) * kPitch + c]) <= 0.0f) acc[nt][2] = 0.0f;
+                if (bf2f(H[(g + 8) * kPitch + c + 1]) <= 0.0f) acc[nt][3] = 0.0f;
+            }
+            __syncwarp();
+            store_acc(dzs, acc);
+            __syncwarp();
+            dw_accumulate(sdW + (size_t)l * kWidth * kWidth, dzs, acts + l * 16 * kPitch, 4, kWidth);
+            if (l == 0) break;
+            // dA_{l-1} = dZ_l (16 x 64) * W_l (64 x 64)
+            uint32_t da[4][4];
+#pragma unroll
+            for (int kt = 0; kt < 4; ++kt) {
+                da[kt][0] = pack2(acc[2 * kt][0], acc[2 * kt][1]);
+                da[kt][1] = pack2(acc[2 * kt][2], acc[2 * kt][3]);
+                da[kt][2] = pack2(acc[2 * kt + 1][0], acc[2 * kt + 1][1]);
+                da[kt][3] = pack2(acc[2 * kt + 1][2], acc[2 * kt + 1][3]);
+            }
+            const unsigned short *Wl = sW + l * kWidth * kPitch;
+#pragma unroll
+            for (int nt = 0; nt < 8; ++nt) {
+                acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.0f;
+                const int i = nt * 8 + g;
+#pragma unroll
+                for (int kt = 0; kt < 4; ++kt) {
+                    const int o = kt * 16 + 2 * t;
+                    const uint32_t b0 = pack_raw(Wl[o * kPitch + i], Wl[(o + 1) * kPitch + i]);
+                    const uint32_t b1 = pack_raw(Wl[(o + 8) * kPitch + i], Wl[(o + 9) * kPitch + i]);
+                    mma16816(acc[nt], da[kt], b0, b1);
+                }
+            }
+        }
+        __syncwarp();
+    }
+    // loss
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) lsum += __shfl_xor_sync(~0u, lsum, o);
+    if (lane == 0 && loss_sum) atomicAdd(loss_sum, lsum * inv_n);
+    __syncthreads();
+    for (size_t i = threadIdx.x; i < TrainSmem::dw_floats; i += blockDim.x) {
+        const float v = sdW[i];
+        if (v != 0.0f) {
+            // global gradient is [l][out][in] with the output layer's 3 rows
+            if (i < (size_t)kLayers * kWidth * kWidth) atomicAdd(&dW_glob[i], v);
+            else {
+                const size_t j = i - (size_t)kLayers * kWidth * kWidth;
+                if (j / kWidth < 3) atomicAdd(&dW_glob[(size_t)kLayers * kWidth * kWidth + j], v);
+            }
+        }
+    }
+}
+
+// Master weights [l][out][in] -> padded BF16 image.
+__global__ void k_make_image(const float *w, unsigned short *img) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < kImgElems; i += gridDim.x * blockDim.x) {
+        float v = 0.0f;
+        const int hid = kLayers * kWidth * kPitch;
+        if (i < hid) {
+            const int l = i / (kWidth * kPitch), r = (i / kPitch) % kWidth, c = i % kPitch;
+            if (c < kWidth) v = w[(size_t)l * kWidth * kWidth + r * kWidth + c];
+        } else {
+            const int j = i - hid, r = j / kPitch, c = j % kPitch;
+            if (r < 3 && c < kWidth) v = w[(size_t)kLayers * kWidth * kWidth + r * kWidth + c];
+        }
+        __nv_bfloat16 b = __float2bfloat16_rn(v);
+        img[i] = *reinterpret_cast<unsigned short *>(&b);
+    }
+}
+
+__global__ void k_check_finite(const float *g, int n, int *bad) {
+    int local = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        if (!isfinite(g[i])) local = 1;
+    if (__any_sync(~0u, local) && (threadIdx.x & 31) == 0) atomicOr(bad, 1);
+}
+
+__global__ void k_adam(float *w, float *m, float *v, const float *g, int n, const int *bad, const float *scale_p,
+                       float lr, float b1, float b2, float eps, float bc1, float bc2) {
+    if (*bad) return;
+    const float inv_s = 1.0f / *scale_p;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float gi = g[i] * inv_s;
+        const float mi = b1 * m[i] + (1.0f - b1) * gi;
+        const float vi = b2 * v[i] + (1.0f - b2) * gi * gi;
+        m[i] = mi;
+        v[i] = vi;
+        w[i] -= lr * (mi / bc1) / (sqrtf(vi / bc2) + eps);
+    }
+}
+
+// Dynamic loss scaling: halve on a non-finite gradient, double after
+// kScaleGrowth clean steps.
+__global__ void k_scale_update(float *scale, int *good, const int *bad) {
+    if (*bad) {
+        *scale = fmaxf(*scale * 0.5f, 1.0f);
+        *good = 0;
+    } else if (++*good >= kScaleGrowth) {
+        *scale = fminf(*scale * 2.0f, 65536.0f);
+        *good = 0;
+    }
+}
+
+__global__ void k_unscale(const float *g, int n, const float *scale_p, float *out) {
+    const float inv = 1.0f / *scale_p;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) out[i] = g[i] * inv;
+}
+
+}  // namespace nrc
+
+// ---------------------------------------------------------------------------
+// state
+// ---------------------------------------------------------------------------
+using namespace nrc;
+
+kgk_status nrc_init(NrcState &N, const kgk_nrc_config *cfg, int device) {
+    nrc_free(N);
+    if (cfg) N.cfg = *cfg;
+    if (N.cfg.width == 0) N.cfg.width = kWidth;
+    if (N.cfg.hidden_layers == 0) N.cfg.hidden_layers = kLayers;
+    if (N.cfg.width != kWidth || N.cfg.hidden_layers != kLayers)
+        return fail(KGK_ERR_UNSUPPORTED, "radiance cache: this build has 5 hidden layers of width 64");
+    if (N.cfg.learning_rate <= 0.0f) N.cfg.learning_rate = 1e-2f;
+    if (N.cfg.train_paths <= 0) N.cfg.train_paths = 65536;
+    if (N.cfg.train_suffix_max <= 0) N.cfg.train_suffix_max = 4;
+    if (N.cfg.train_steps <= 0) N.cfg.train_steps = 4;
+    if (N.cfg.spread_c <= 0.0f) N.cfg.spread_c = 0.01f;
+    KGK_TRY(dalloc(&N.w, kParams, "cache weights"));
+    KGK_TRY(dalloc(&N.m, kParams, "cache Adam state"));
+    KGK_TRY(dalloc(&N.v, kParams, "cache Adam state"));
+    KGK_TRY(dalloc(&N.g, kParams, "cache gradient"));
+    KGK_TRY(dalloc(&N.img, (size_t)kImgElems, "cache BF16 weights"));
+    KGK_TRY(dalloc(&N.scal, 4, "cache scalars"));
+    KGK_TRY(dalloc(&N.ints, 4, "cache scalars"));
+    // He-uniform initialisation from a seeded stream
+    std::vector<float> h(kParams);
+    unsigned long long s = N.cfg.seed ? N.cfg.seed : 0x1234567ull;
+    auto nxt = [&]() {
+        s ^= s << 13; s ^= s >> 7; s ^= s << 17;
+        return (double)(s >> 11) * (1.0 / 9007199254740992.0);
+    };
+    const double lim = std::sqrt(6.0 / kWidth);
+    for (int i = 0; i < kParams; ++i) h[i] = (float)((2.0 * nxt() - 1.0) * lim);
+    KGK_CUDA(cudaMemcpy(N.w, h.data(), kParams * sizeof(float), cudaMemcpyHostToDevice));
+    KGK_CUDA(cudaMemset(N.m, 0, kParams * sizeof(float)));
+    KGK_CUDA(cudaMemset(N.v, 0, kParams * sizeof(float)));
+    const float sc[4] = {kInitScale, 0.0f, 0.0f, 0.0f};
+    KGK_CUDA(cudaMemcpy(N.scal, sc, sizeof sc, cudaMemcpyHostToDevice));
+    KGK_CUDA(cudaMemset(N.ints, 0, 4 * sizeof(int)));
+    k_make_image<<<64, 256>>>(N.w, N.img);
+    KGK_CUDA(cudaGetLastError());
+    KGK_CUDA(cudaDeviceSynchronize());
+    KGK_CUDA(cudaFuncSetAttribute(k_train, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TrainSmem::total(4)));
+    KGK_CUDA(cudaFuncSetAttribute(k_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, kImgElems * 2));
+    cudaDeviceProp p;
+    KGK_CUDA(cudaGetDeviceProperties(&p, device));
+    N.sms = p.multiProcessorCount;
+    N.step = 0;
+    N.ready = true;
+    return KGK_OK;
+}
+
+void nrc_free(NrcState &N) {
+    void *ptrs[] = {N.w, N.m, N.v, N.g, N.img, N.scal, N.ints};
+    for (void *p : ptrs) dfree(p);
+    N.w = N.m = N.v = N.g = N.scal = nullptr;
+    N.img = nullptr;
+    N.ints = nullptr;
+    N.ready = false;
+}
+
+kgk_status nrc_infer_dev(NrcState &N, const float *raw, int stride, int n, const int *n_dev, float *out, float4 *rad,
+                         cudaStream_t st) {
+    const int grid = N.sms * 4;
+    k_infer<<<grid, 256, kImgElems * 2, st>>>(N.img, raw, stride, n, n_dev, out, rad);
+    KGK_CUDA(cudaGetLastError());
+    return KGK_OK;
+}
+
+kgk_status nrc_grad_dev(NrcState &N, const float *raw, int raw_stride, const float *tgt, int tgt_stride, int n,
+                        const int *n_dev, cudaStream_t st) {
+    KGK_CUDA(cudaMemsetAsync(N.g, 0, kParams * sizeof(float), st));
+    KGK_CUDA(cudaMemsetAsync(N.scal + 1, 0, sizeof(float), st));  // loss
+    const int grid = N.sms;
+    k_train<<<grid, 128, TrainSmem::total(4), st>>>(N.img, raw, raw_stride, tgt, tgt_stride, n, n_dev, N.scal, N.g,
+                                                     N.scal + 1);
+    KGK_CUDA(cudaGetLastError());
+    return KGK_OK;
+}
+
+kgk_status nrc_step_dev(NrcState &N, cudaStream_t st) {
+    KGK_CUDA(cudaMemsetAsync(N.ints, 0, sizeof(int), st));  // bad flag
+    k_check_finite<<<64, 256, 0, st>>>(N.g, kParams, N.ints);
+    ++N.step;
+    const float b1 = 0.9f, b2 = 0.99f;
+    const float bc1 = 1.0f - std::pow(b1, (float)N.step), bc2 = 1.0f - std::pow(b2, (float)N.step);
+    k_adam<<<64, 256, 0, st>>>(N.w, N.m, N.v, N.g, kParams, N.ints, N.scal, N.cfg.learning_rate, b1, b2, 1e-10f,
+                               bc1, bc2);
+    k_scale_update<<<1, 1, 0, st>>>(N.scal, N.ints + 1, N.ints);
+    k_make_image<<<64, 256, 0, st>>>(N.w, N.img);
+    KGK_CUDA(cudaGetLastError());
+    return KGK_OK;
+}
+
+NrcState *nrc_state(kgk_scene *s) {
+    if (!s->nrc) s->nrc = new NrcState();
+    return s->nrc;
+}
+
+void nrc_state_free(kgk_scene *s) {
+    if (!s->nrc) return;
+    nrc_free(*s->nrc);
+    delete s->nrc;
+    s->nrc = nullptr;
+}
+
+}  // namespace kgk
+
+using namespace kgk;
+
+namespace {
+
+kgk_status stage_in(kgk_scene *s, const void *src, size_t bytes, void **dst, std::vector<void *> &owned) {
+    if (is_device_ptr(src)) {
+        *dst = const_cast<void *>(src);
+        return KGK_OK;
+    }
+    KGK_TRY(dmalloc(dst, bytes, "cache staging"));
+    owned.push_back(*dst);
+    KGK_CUDA(cudaMemcpyAsync(*dst, src, bytes, cudaMemcpyHostToDevice, s->stream));
+    return KGK_OK;
+}
+
+struct Owned {
+    std::vector<void *> v;
+    ~Owned() {
+        for (void *p : v) dfree(p);
+    }
+};
+
+kgk_status need(kgk_scene *s) {
+    if (!s) return fail(KGK_ERR_INVALID_ARGUMENT, "radiance cache: scene == NULL");
+    if (!s->nrc || !s->nrc->ready) return fail(KGK_ERR_INVALID_ARGUMENT, "radiance cache: call kgk_nrc_init first");
+    KGK_CUDA(cudaSetDevice(s->device));
+    return KGK_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+kgk_status kgk_nrc_init(kgk_scene *s, const kgk_nrc_config *cfg) {
+    if (!s) return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_nrc_init: scene == NULL");
+    KGK_CUDA(cudaSetDevice(s->device));
+    return nrc_init(*nrc_state(s), cfg, s->device);
+}
+
+kgk_status kgk_nrc_set_weights(kgk_scene *s, const float *w, size_t n) {
+    KGK_TRY(need(s));
+    if (!w || n != (size_t)kParams)
+        return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_nrc_set_weights: expected " + std::to_string(kParams) + " floats");
+    NrcState &N = *s->nrc;
+    KGK_CUDA(cudaMemcpy(N.w, w, n * sizeof(float), is_device_ptr(w) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice));
+    k_make_image<<<64, 256, 0, s->stream>>>(N.w, N.img);
+    KGK_CUDA(cudaGetLastError());
+    KGK_CUDA(cudaStreamSynchronize(s->stream));
+    return KGK_OK;
+}
+
+kgk_status kgk_nrc_get_weights(kgk_scene *s, float *w, size_t n) {
+    KGK_TRY(need(s));
+    if (!w || n != (size_t)kParams)
+        return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_nrc_get_weights: expected " + std::to_string(kParams) + " floats");
+    KGK_CUDA(cudaStreamSynchronize(s->stream));
+    KGK_CUDA(cudaMemcpy(w, s->nrc->w, n * sizeof(float), is_device_ptr(w) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost));
+    return KGK_OK;
+}
+
+kgk_status kgk_nrc_infer(kgk_scene *s, const float *raw, size_t n, float *out) {
+    KGK_TRY(need(s));
+    if (n == 0) return KGK_OK;
+    if (!raw || !out || n > (1u << 30)) return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_nrc_infer: bad arguments");
+    Owned o;
+    void *draw, *dout;
+    KGK_TRY(stage_in(s, raw, n * kRaw * sizeof(float), &draw, o.v));
+    const bool od = is_device_ptr(out);
+    if (od) dout = out;
+    else {
+        KGK_TRY(dmalloc(&dout, n * 3 * sizeof(float), "cache staging"));
+        o.v.push_back(dout);
+    }
+    KGK_TRY(nrc_infer_dev(*s->nrc, (const float *)draw, kRaw, (int)n, nullptr, (float *)dout, nullptr, s->stream));
+    if (!od) KGK_CUDA(cudaMemcpyAsync(out, dout, n * 3 * sizeof(float), cudaMemcpyDeviceToHost, s->stream));
+    KGK_CUDA(cudaStreamSynchronize(s->stream));
+    return KGK_OK;
+}
+
+kgk_status kgk_nrc_gradients(kgk_scene *s, const float *raw, const float *target, size_t n, float *grad, float *loss) {
+    KGK_TRY(need(s));
+    if (!raw || !target || !grad || n == 0 || n > (1u << 30))
+        return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_nrc_gradients: bad arguments");
+    Owned o;
+    void *draw, *dt;
+    KGK_TRY(stage_in(s, raw, n * kRaw * sizeof(float), &draw, o.v));
+    KGK_TRY(stage_in(s, target, n * 3 * sizeof(float), &dt, o.v));
+    NrcState &N = *s->nrc;
+    KGK_TRY(nrc_grad_dev(N, (const float *)draw, kRaw, (const float *)dt, 3, (int)n, nullptr, s->stream));
+    void *dg;
+    KGK_TRY(dmalloc(&dg, kParams * sizeof(float), "cache staging"));
+    o.v.push_back(dg);
+    k_unscale<<<64, 256, 0, s->stream>>>(N.g, kParams, N.scal, (float *)dg);
+    KGK_CUDA(cudaGetLastError());
+    KGK_CUDA(cudaMemcpyAsync(grad, dg, kParams * sizeof(float), cudaMemcpyDeviceToHost, s->stream));
+    float hl = 0.0f;
+    KGK_CUDA(cudaMemcpyAsync(&hl, N.scal + 1, sizeof(float), cudaMemcpyDeviceToHost, s->stream));
+    KGK_CUDA(cudaStreamSynchronize(s->stream));
+    if (loss) *loss = hl;
+    return KGK_OK;
+}
+
+kgk_status kgk_nrc_train(kgk_scene *s, const float *raw, const float *target, size_t n, int32_t steps, float *loss) {
+    KGK_TRY(need(s));
+    if (!raw || !target || n == 0 || n > (1u << 30) || steps <= 0)
+        return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_nrc_train: bad arguments");
+    Owned o;
+    void *draw, *dt;
+    KGK_TRY(stage_in(s, raw, n * kRaw * sizeof(float), &draw, o.v));
+    KGK_TRY(stage_in(s, target, n * 3 * sizeof(float), &dt, o.v));
+    NrcState &N = *s->nrc;
+    for (int k = 0; k < steps; ++k) {
+        KGK_TRY(nrc_grad_dev(N, (const float *)draw, kRaw, (const float *)dt, 3, (int)n, nullptr, s->stream));
+        KGK_TRY(nrc_step_dev(N, s->stream));
+    }
+    float hl = 0.0f;
+    KGK_CUDA(cudaMemcpyAsync(&hl, N.scal + 1, sizeof(float), cudaMemcpyDeviceToHost, s->stream));
+    KGK_CUDA(cudaStreamSynchronize(s->stream));
+    if (loss) *loss = hl;
+    return KGK_OK;
+}
+
+kgk_status kgk_nrc_loss_scale(kgk_scene *s, float *scale) {
+    KGK_TRY(need(s));
+    if (!scale) return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_nrc_loss_scale: NULL");
+    KGK_CUDA(cudaStreamSynchronize(s->stream));
+    KGK_CUDA(cudaMemcpy(scale, s->nrc->scal, sizeof(float), cudaMemcpyDeviceToHost));
+    return KGK_OK;
+}
+
+}  // extern "C"

@@ -18,6 +18,7 @@
 #include <cstring>
 #include <vector>
 
+#include "kgk_nrc.h"
 #include "kgk_scene.h"
 #include "shading.cuh"
 #include "traverse.cuh"
@@ -46,6 +47,13 @@ struct RenderState {
     float4 *sh_o[2] = {nullptr, nullptr}, *sh_d[2] = {nullptr, nullptr}, *sh_c[2] = {nullptr, nullptr};
     int *cnt = nullptr;                       // queue counters
     unsigned long long *stats = nullptr;      // rays_closest, rays_shadow, overflow, nodes, tris
+    // radiance cache (capacity cap paths)
+    float2 *spread = nullptr;                 // (sqrt-summed path spread, primary footprint)
+    int *pflags = nullptr;                    // bit 0 training path, bit 1 queried, bits 8.. suffix bounces
+    float *qrec = nullptr;                    // query records, kQRec floats each
+    float *trec = nullptr;                    // training records, kQRec floats each
+    float *ttgt = nullptr;                    // training targets (3 per record)
+    int tcap = 0;
     int sms = 0;
     bool gbuffer_valid = false;               // G-buffer written by the last frame
     kgk_camera gbuffer_cam{};
@@ -53,7 +61,18 @@ struct RenderState {
 
 namespace {
 
-enum Cnt { kA0 = 0, kA1 = 1, kSQ0 = 2, kSQ1 = 3, kSQ2 = 4, kSH0 = 5, kSH1 = 6, kNCnt = 8 };
+// Device counters: alive-queue sizes (double-buffered), shade-queue sizes,
+// shadow-queue sizes, dynamic-fetch cursors of the extend and shadow kernels
+// (zeroed before every bounce together with the queues), cache record counts.
+enum Cnt {
+    kA0 = 0, kA1 = 1, kSQ0 = 2, kSQ1 = 3, kSQ2 = 4, kSH0 = 5, kSH1 = 6, kFE = 7, kFS0 = 8, kFS1 = 9,
+    kQN = 10, kTN = 11, kNCnt = 12
+};
+// Lanes of a warp that must be idle before the warp fetches new rays.
+constexpr int kRefill = 8;
+// Cache record: raw query [13], T [3], path id (int bits), radiance before the
+// query vertex's scattering [3].
+constexpr int kQRec = 20;
 enum Stat { kRaysC = 0, kRaysS = 1, kOverflow = 2, kNodes = 3, kTris = 4, kNStat = 8 };
 
 struct Params {
@@ -77,6 +96,14 @@ struct Params {
     float4 *gb_pos, *gb_nrm, *gb_alb, *gb_emi;
     int *cnt;
     unsigned long long *stats;
+    // radiance cache
+    int use_cache;
+    float2 *spread;
+    int *pflags;
+    float *qrec, *trec;
+    int tcap;
+    int train_stride, train_offset, suffix_max;
+    float spread_c;
 };
 
 __device__ __forceinline__ int warp_append(int *counter, bool pred) {
@@ -141,51 +168,83 @@ __global__ void k_raygen(Params P) {
         P.rad[i] = make_float4(r0, r0, r0, 0.0f);
         P.rng[i] = s;
         P.depth[i] = 0;
+        if (P.use_cache) {
+            P.spread[i] = make_float2(0.0f, 0.0f);
+            const bool train = P.train_stride > 0 && i < P.npx && (i % P.train_stride) == P.train_offset;
+            P.pflags[i] = train ? 1 : 0;
+        }
     }
 }
 
 // ---------------------------------------------------------------------------
+// Closest hit for every ray of the queue (q == nullptr: paths 0..dense_n-1),
+// then the path goes to the miss, Lambert or Disney shade queue.  Each warp
+// keeps its lanes busy: when kRefill or more lanes have finished, they take
+// the next rays from the queue (one atomic per warp).
 template <bool kCount>
 __global__ void __launch_bounds__(128) k_extend(Params P, const int *__restrict__ q, int qcnt_idx, int dense_n,
                                                 int *sq0, int *sq1, int *sq2) {
     const int n = q ? P.cnt[qcnt_idx] : dense_n;
     const DevScene &s = P.sc;
-    for (int base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
-        const int i = base + threadIdx.x;
-        const bool valid = i < n;
-        int p = 0, cls = -1;
-        TravStats st{0, 0, 0};
-        if (valid) {
-            p = q ? q[i] : i;
-            const float4 o = P.o[p], d = P.d[p];
-            const RayPre r = make_ray(f3(o), f3(d));
-            float bt = kBigT, u = 0.0f, v = 0.0f;
-            int bid = 0x7fffffff;
-            const int slot = trace_closest<kCount>(s.nodes, (unsigned)s.n_nodes, s.tri_rec, (unsigned)s.n_tris,
-                                                   r, bt, bid, u, v, st);
-            if (slot < 0) {
+    int *fetch = &P.cnt[kFE];
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned lt = (1u << lane) - 1u;
+    bool active = false, exhausted = false;
+    int p = 0;
+    unsigned rays = 0;
+    RayPre r;
+    Trav c;
+    TravStack stk;
+    TravStats st{0, 0, 0};
+    while (true) {
+        const unsigned idle = __ballot_sync(~0u, !active);
+        if (!exhausted && __popc(idle) >= kRefill) {
+            int base = 0;
+            if (lane == 0) base = atomicAdd(fetch, __popc(idle));
+            base = __shfl_sync(~0u, base, 0);
+            if (base + __popc(idle) >= n) exhausted = true;
+            if (!active) {
+                const int i = base + __popc(idle & lt);
+                if (i < n) {
+                    p = q ? q[i] : i;
+                    const float4 o = P.o[p], d = P.d[p];
+                    r = make_ray(f3(o), f3(d));
+                    trav_init(c, kBigT);
+                    active = true;
+                }
+            }
+        }
+        if (!__any_sync(~0u, active)) break;
+        int cls = -1;
+        if (active && trav_step<kCount>(s.nodes, (unsigned)s.n_nodes, s.tri_rec, (unsigned)s.n_tris, r, c, stk,
+                                        false, st)) {
+            active = false;
+            ++rays;
+            if (c.hit_slot < 0) {
                 cls = 0;
                 P.hit[p] = make_float4(kBigT, 0.0f, 0.0f, __int_as_float(-1));
             } else {
-                P.hit[p] = make_float4(bt, u, v, __int_as_float(bid));
-                const unsigned bits = __float_as_uint(__ldg(&s.attr[4 * bid + 3].w));
+                P.hit[p] = make_float4(c.best_t, c.bu, c.bv, __int_as_float(c.best_id));
+                const unsigned bits = __float_as_uint(__ldg(&s.attr[4 * c.best_id + 3].w));
                 const int mid = (int)(bits & 0x7fffffffu);
                 cls = __ldg(&s.mats[mid].MATERIAL_TYPE_ID) == 1 ? 2 : 1;
             }
         }
-        const int a0 = warp_append(&P.cnt[kSQ0], cls == 0);
-        const int a1 = warp_append(&P.cnt[kSQ1], cls == 1);
-        const int a2 = warp_append(&P.cnt[kSQ2], cls == 2);
-        if (cls == 0) sq0[a0] = p;
-        if (cls == 1) sq1[a1] = p;
-        if (cls == 2) sq2[a2] = p;
-        warp_add_u64(&P.stats[kRaysC], valid ? 1u : 0u);
-        if (kCount) {
-            warp_add_u64(&P.stats[kNodes], st.nodes);
-            warp_add_u64(&P.stats[kTris], st.tris);
+        if (__any_sync(~0u, cls >= 0)) {
+            const int a0 = warp_append(&P.cnt[kSQ0], cls == 0);
+            const int a1 = warp_append(&P.cnt[kSQ1], cls == 1);
+            const int a2 = warp_append(&P.cnt[kSQ2], cls == 2);
+            if (cls == 0) sq0[a0] = p;
+            if (cls == 1) sq1[a1] = p;
+            if (cls == 2) sq2[a2] = p;
         }
-        warp_add_u64(&P.stats[kOverflow], st.overflow);
     }
+    warp_add_u64(&P.stats[kRaysC], rays);
+    if (kCount) {
+        warp_add_u64(&P.stats[kNodes], st.nodes);
+        warp_add_u64(&P.stats[kTris], st.tris);
+    }
+    warp_add_u64(&P.stats[kOverflow], st.overflow);
 }
 
 // ---------------------------------------------------------------------------
@@ -483,6 +542,26 @@ __device__ __forceinline__ void bsdf_eval_pdf(const Surface &S, const DisneyPara
     }
 }
 
+// Writes a cache record for the surface point of a path: normalised position,
+// shading normal, direction to the viewer, roughness, albedo, then T, the
+// path id and the radiance gathered so far.
+__device__ __forceinline__ void write_cache_record(const Params &P, float *rec, const Surface &S, float3 wo,
+                                                   float3 T, int path, float3 rad) {
+    const DevScene &s = P.sc;
+    const float3 lo = f3(s.lo[0], s.lo[1], s.lo[2]), hi = f3(s.hi[0], s.hi[1], s.hi[2]);
+    const float3 e = hi - lo;
+    rec[0] = fminf(fmaxf((S.pos.x - lo.x) / fmaxf(e.x, 1e-20f), 0.0f), 1.0f);
+    rec[1] = fminf(fmaxf((S.pos.y - lo.y) / fmaxf(e.y, 1e-20f), 0.0f), 1.0f);
+    rec[2] = fminf(fmaxf((S.pos.z - lo.z) / fmaxf(e.z, 1e-20f), 0.0f), 1.0f);
+    rec[3] = S.n.x; rec[4] = S.n.y; rec[5] = S.n.z;
+    rec[6] = wo.x; rec[7] = wo.y; rec[8] = wo.z;
+    rec[9] = S.m.MATERIAL_TYPE_ID == 1 ? S.m.roughness : 1.0f;
+    rec[10] = S.m.diffuse.x; rec[11] = S.m.diffuse.y; rec[12] = S.m.diffuse.z;
+    rec[13] = T.x; rec[14] = T.y; rec[15] = T.z;
+    rec[16] = __int_as_float(path);
+    rec[17] = rad.x; rec[18] = rad.y; rec[19] = rad.z;
+}
+
 __device__ void shade_unbiased(const Params &P, int p, bool valid, int *next_q, int next_cnt, float4 *so0,
                                float4 *sd0, float4 *sc0, float4 *so1, float4 *sd1, float4 *sc1) {
     const DevScene &s = P.sc;
@@ -534,7 +613,38 @@ __device__ void shade_unbiased(const Params &P, int p, bool valid, int *next_q, 
                 rad += T * emi * wgt;
             }
             bool alive = true;
-            if (depth >= P.rr_start) {
+            bool to_cache = false;
+            if (P.use_cache) {
+                // path spread (sqrt-summed) against the primary footprint
+                float2 sp = P.spread[p];
+                const float cosl = fmaxf(fabsf(dot3(S.ng, d)), 1e-4f);
+                if (depth == 0) sp.y = S.t * S.t / (4.0f * kPI * cosl);
+                else sp.x += sqrtf(S.t * S.t / (fmaxf(prev_pdf, 1e-8f) * cosl));
+                P.spread[p] = sp;
+                int fl = P.pflags[p];
+                const bool wide = depth >= 1 && sp.x * sp.x > P.spread_c * sp.y;
+                if (fl & 1) {
+                    if (!(fl & 2)) {
+                        if (wide) {  // training path: record the query vertex, keep going
+                            const int k = atomicAdd(&P.cnt[kTN], 1);
+                            if (k < P.tcap) write_cache_record(P, P.trec + (size_t)k * kQRec, S, -d, T, p, rad);
+                            fl |= 2;
+                        }
+                    } else {
+                        fl += 256;
+                        if ((fl >> 8) >= P.suffix_max) to_cache = true;  // suffix end: bootstrap from the cache
+                    }
+                    P.pflags[p] = fl;
+                } else if (wide) {
+                    to_cache = true;
+                }
+            }
+            if (to_cache) {
+                const int k = atomicAdd(&P.cnt[kQN], 1);
+                write_cache_record(P, P.qrec + (size_t)k * kQRec, S, -d, T, p, rad);
+                alive = false;
+            }
+            if (alive && depth >= P.rr_start) {
                 const float q = fminf(maxc(T), 0.95f);
                 if (rnd_u(rs) >= q) alive = false;
                 else T = T / q;
@@ -657,40 +767,75 @@ __global__ void __launch_bounds__(128) k_shade(Params P, const int *sq0, const i
 }
 
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(128) k_shadow(Params P, int cidx, const float4 *__restrict__ so,
+// Shadow rays of one queue: a face-light record (light id >= 0) is visible
+// when the closest hit within its range is that light (the reference's test,
+// NextEventEstimation_FaceLight.cuh:69-71); an environment record when nothing
+// lies in (kTMin, range).  Visible records add their contribution to the
+// path's radiance (one record per path per queue, so no atomics).  Lanes are
+// refilled like k_extend's.
+__global__ void __launch_bounds__(128) k_shadow(Params P, int cidx, int fidx, const float4 *__restrict__ so,
                                                 const float4 *__restrict__ sd, const float4 *__restrict__ sc) {
     const int n = P.cnt[cidx];
     const DevScene &s = P.sc;
-    for (int base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
-        const int i = base + threadIdx.x;
-        const bool valid = i < n;
-        TravStats st{0, 0, 0};
-        if (valid) {
-            const float4 o = so[i], d = sd[i], c = sc[i];
-            const RayPre r = make_ray(f3(o), f3(d));
-            const int light = __float_as_int(d.w);
-            bool vis;
-            if (light >= 0) {
-                // the reference's test: the closest hit must be the sampled light
-                float bt = o.w, u, v;
-                int bid = 0x7fffffff;
-                const int slot = trace_closest<false>(s.nodes, (unsigned)s.n_nodes, s.tri_rec, (unsigned)s.n_tris,
-                                                      r, bt, bid, u, v, st);
-                vis = slot >= 0 && bid == light;
-            } else {
-                vis = !trace_any<false>(s.nodes, (unsigned)s.n_nodes, s.tri_rec, (unsigned)s.n_tris, r, o.w, st);
+    int *fetch = &P.cnt[fidx];
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned lt = (1u << lane) - 1u;
+    bool active = false, exhausted = false;
+    int i = 0, light = -1;
+    unsigned rays = 0;
+    RayPre r;
+    Trav c;
+    TravStack stk;
+    TravStats st{0, 0, 0};
+    while (true) {
+        const unsigned idle = __ballot_sync(~0u, !active);
+        if (!exhausted && __popc(idle) >= kRefill) {
+            int base = 0;
+            if (lane == 0) base = atomicAdd(fetch, __popc(idle));
+            base = __shfl_sync(~0u, base, 0);
+            if (base + __popc(idle) >= n) exhausted = true;
+            if (!active) {
+                i = base + __popc(idle & lt);
+                if (i < n) {
+                    const float4 o = so[i], d = sd[i];
+                    r = make_ray(f3(o), f3(d));
+                    light = __float_as_int(d.w);
+                    trav_init(c, o.w);
+                    active = true;
+                }
             }
+        }
+        if (!__any_sync(~0u, active)) break;
+        if (active && trav_step<false>(s.nodes, (unsigned)s.n_nodes, s.tri_rec, (unsigned)s.n_tris, r, c, stk,
+                                       light < 0, st)) {
+            active = false;
+            ++rays;
+            const bool vis = light >= 0 ? (c.hit_slot >= 0 && c.best_id == light) : c.hit_slot < 0;
             if (vis) {
-                const int p = __float_as_int(c.w);
+                const float4 cc = sc[i];
+                const int p = __float_as_int(cc.w);
                 float4 rr = P.rad[p];
-                rr.x += c.x;
-                rr.y += c.y;
-                rr.z += c.z;
+                rr.x += cc.x;
+                rr.y += cc.y;
+                rr.z += cc.z;
                 P.rad[p] = rr;
             }
         }
-        warp_add_u64(&P.stats[kRaysS], valid ? 1u : 0u);
-        warp_add_u64(&P.stats[kOverflow], st.overflow);
+    }
+    warp_add_u64(&P.stats[kRaysS], rays);
+    warp_add_u64(&P.stats[kOverflow], st.overflow);
+}
+
+// Training targets: scattered radiance leaving each recorded query vertex,
+// (radiance at the end of the path - radiance before the vertex) / T.
+__global__ void k_cache_targets(const float *trec, const int *n_dev, int cap, const float4 *rad, float *tgt) {
+    const int n = min(*n_dev, cap);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float *r = trec + (size_t)i * kQRec;
+        const int path = __float_as_int(r[16]);
+        const float4 fin = rad[path];
+        const float f[3] = {fin.x, fin.y, fin.z};
+        for (int c = 0; c < 3; ++c) tgt[3 * i + c] = (f[c] - r[17 + c]) / fmaxf(r[13 + c], 1e-8f);
     }
 }
 
@@ -762,7 +907,18 @@ kgk_status ensure_wave(RenderState &R, int cap) {
         KGK_TRY(ensure(&R.sh_d[k], cap, "shadow queue"));
         KGK_TRY(ensure(&R.sh_c[k], cap, "shadow queue"));
     }
+    KGK_TRY(ensure(&R.spread, cap, "cache path state"));
+    KGK_TRY(ensure(&R.pflags, cap, "cache path state"));
+    KGK_TRY(ensure(&R.qrec, (size_t)cap * kQRec, "cache query records"));
     R.cap = cap;
+    return KGK_OK;
+}
+
+kgk_status ensure_train(RenderState &R, int tcap) {
+    if (R.tcap >= tcap) return KGK_OK;
+    KGK_TRY(ensure(&R.trec, (size_t)tcap * kQRec, "cache training records"));
+    KGK_TRY(ensure(&R.ttgt, (size_t)tcap * 3, "cache training targets"));
+    R.tcap = tcap;
     return KGK_OK;
 }
 
@@ -774,7 +930,7 @@ void render_state_free(kgk_scene *s) {
     void *ptrs[] = {R->seeds, R->frame, R->acc_sum, R->acc_sq, R->gb_pos, R->gb_nrm, R->gb_alb, R->gb_emi,
                     R->o, R->d, R->thr, R->rad, R->hit, R->rng, R->depth, R->aq[0], R->aq[1], R->sq[0],
                     R->sq[1], R->sq[2], R->sh_o[0], R->sh_o[1], R->sh_d[0], R->sh_d[1], R->sh_c[0],
-                    R->sh_c[1], R->cnt, R->stats};
+                    R->sh_c[1], R->cnt, R->stats, R->spread, R->pflags, R->qrec, R->trec, R->ttgt};
     for (void *p : ptrs) dfree(p);
     delete R;
     s->rs = nullptr;
@@ -815,7 +971,10 @@ kgk_status kgk_render(kgk_scene *s, const kgk_camera *cam, const kgk_camera *pre
     if (cfg->spp <= 0) return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_render: spp must be positive");
     if (cfg->estimator != KGK_ESTIMATOR_COMPAT && cfg->estimator != KGK_ESTIMATOR_UNBIASED)
         return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_render: unknown estimator");
-    if (cfg->use_cache) return fail(KGK_ERR_UNSUPPORTED, "kgk_render: use the radiance-cache entry point");
+    if (cfg->use_cache && cfg->estimator != KGK_ESTIMATOR_UNBIASED)
+        return fail(KGK_ERR_UNSUPPORTED, "kgk_render: the radiance cache works with the unbiased estimator");
+    if (cfg->use_cache && (!s->nrc || !s->nrc->ready))
+        return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_render: use_cache needs kgk_nrc_init");
     KGK_CUDA(cudaSetDevice(s->device));
     RenderState &R = *render_state(s);
     const int W = cfg->width, H = cfg->height, npx = W * H;
@@ -861,6 +1020,20 @@ kgk_status kgk_render(kgk_scene *s, const kgk_camera *cam, const kgk_camera *pre
     P.gb_pos = R.gb_pos; P.gb_nrm = R.gb_nrm; P.gb_alb = R.gb_alb; P.gb_emi = R.gb_emi;
     P.cnt = R.cnt;
     P.stats = R.stats;
+    P.use_cache = cfg->use_cache ? 1 : 0;
+    if (P.use_cache) {
+        const kgk_nrc_config &nc = s->nrc->cfg;
+        KGK_TRY(ensure_train(R, nc.train_paths));
+        P.spread = R.spread;
+        P.pflags = R.pflags;
+        P.qrec = R.qrec;
+        P.trec = R.trec;
+        P.tcap = R.tcap;
+        P.train_stride = std::max(1, npx / std::max(nc.train_paths, 1));
+        P.train_offset = (int)(((unsigned)cfg->frame_index * 2654435761u) % (unsigned)P.train_stride);
+        P.suffix_max = nc.train_suffix_max;
+        P.spread_c = nc.spread_c;
+    }
     const int grid = R.sms * 8;   // persistent grid-stride launches, 128 threads per block
     cudaEvent_t e0, e1;
     KGK_CUDA(cudaEventCreate(&e0));
@@ -894,11 +1067,15 @@ kgk_status kgk_render(kgk_scene *s, const kgk_camera *cam, const kgk_camera *pre
         P.spp_wave = std::min(spw, cfg->spp - done);
         P.sample_base = done;
         const int n = npx * P.spp_wave;
+        if (P.use_cache) {
+            KGK_CUDA(cudaMemsetAsync(R.cnt + kQN, 0, 2 * sizeof(int), st));
+            if (wave > 0) P.train_stride = 0;  // training paths only in the first wave
+        }
         k_raygen<<<grid, 128, 0, st>>>(P);
         ++launches;
         int cur = 0;
         for (int b = 0; b < max_bounces; ++b) {
-            KGK_CUDA(cudaMemsetAsync(R.cnt + kSQ0, 0, 5 * sizeof(int), st));
+            KGK_CUDA(cudaMemsetAsync(R.cnt + kSQ0, 0, (kFS1 + 1 - kSQ0) * sizeof(int), st));
             KGK_CUDA(cudaMemsetAsync(R.cnt + (cur ^ 1), 0, sizeof(int), st));
             const int *q = b == 0 ? nullptr : R.aq[cur];
             KGK_TRY(stage_begin(0));
@@ -919,8 +1096,8 @@ kgk_status kgk_render(kgk_scene *s, const kgk_camera *cam, const kgk_camera *pre
                                                                     R.sh_d[1], R.sh_c[1]);
             KGK_TRY(stage_end());
             KGK_TRY(stage_begin(2));
-            k_shadow<<<grid, 128, 0, st>>>(P, kSH0, R.sh_o[0], R.sh_d[0], R.sh_c[0]);
-            k_shadow<<<grid, 128, 0, st>>>(P, kSH1, R.sh_o[1], R.sh_d[1], R.sh_c[1]);
+            k_shadow<<<grid, 128, 0, st>>>(P, kSH0, kFS0, R.sh_o[0], R.sh_d[0], R.sh_c[0]);
+            k_shadow<<<grid, 128, 0, st>>>(P, kSH1, kFS1, R.sh_o[1], R.sh_d[1], R.sh_c[1]);
             KGK_TRY(stage_end());
             KGK_CUDA(cudaGetLastError());
             launches += 4;
@@ -930,6 +1107,27 @@ kgk_status kgk_render(kgk_scene *s, const kgk_camera *cam, const kgk_camera *pre
                 KGK_CUDA(cudaMemcpyAsync(&alive, R.cnt + cur, sizeof(int), cudaMemcpyDeviceToHost, st));
                 KGK_CUDA(cudaStreamSynchronize(st));
                 if (alive == 0) break;
+            }
+        }
+        if (P.use_cache) {
+            // terminate into the cache, then learn from this wave's training paths
+            NrcState &N = *s->nrc;
+            KGK_TRY(nrc_infer_dev(N, R.qrec, kQRec, R.cap, R.cnt + kQN, nullptr, R.rad, st));
+            k_cache_targets<<<64, 256, 0, st>>>(R.trec, R.cnt + kTN, R.tcap, R.rad, R.ttgt);
+            KGK_CUDA(cudaGetLastError());
+            launches += 2;
+            if (wave == 0) {
+                int ntr = 0;
+                KGK_CUDA(cudaMemcpyAsync(&ntr, R.cnt + kTN, sizeof(int), cudaMemcpyDeviceToHost, st));
+                KGK_CUDA(cudaStreamSynchronize(st));
+                ntr = std::min(ntr, R.tcap);
+                if (ntr > 0) {
+                    for (int k = 0; k < N.cfg.train_steps; ++k) {
+                        KGK_TRY(nrc_grad_dev(N, R.trec, kQRec, R.ttgt, 3, ntr, nullptr, st));
+                        KGK_TRY(nrc_step_dev(N, st));
+                        launches += 6;
+                    }
+                }
             }
         }
         k_finish<<<(npx + 255) / 256, 256, 0, st>>>(P, R.frame, R.acc_sum, R.acc_sq, cfg->accumulate, wave == 0);

@@ -81,6 +81,20 @@ kgk_status scene_upload(DevScene &s, const kgk_triangle *tris_in, size_t n, cons
 
     s.n_tris = (int32_t)n;
     s.n_mats = (int32_t)nm;
+    for (int a = 0; a < 3; ++a) {
+        s.lo[a] = INFINITY;
+        s.hi[a] = -INFINITY;
+    }
+    for (size_t i = 0; i < n; ++i) {
+        const kgk_vec *vs[3] = {&tris[i].v0, &tris[i].v1, &tris[i].v2};
+        for (const kgk_vec *v : vs) {
+            const float c[3] = {v->x, v->y, v->z};
+            for (int a = 0; a < 3; ++a) {
+                s.lo[a] = std::fmin(s.lo[a], c[a]);
+                s.hi[a] = std::fmax(s.hi[a], c[a]);
+            }
+        }
+    }
     // vertices and attributes
     {
         std::vector<float4> verts(3 * n), attr(4 * n);

@@ -488,8 +488,9 @@ __global__ void k_s_temporal(StdArgs a) {
             float x, y;
             const float4 ps = a.pos[p];
             if (project_prev(a.pcam, W, H, f3(ps), x, y)) {
-                // bilinear taps around the previous pixel centre
-                const float fx = x - 0.5f, fy = y - 0.5f;
+                // bilinear taps; pixel (X, Y)'s primary ray passes through
+                // integer screen coordinates (Generate1stRay)
+                const float fx = x, fy = y;
                 const int x0 = (int)floorf(fx), y0 = (int)floorf(fy);
                 const float tx = fx - x0, ty = fy - y0;
                 const float3 pc = f3(a.pcam.CamOrg.x, a.pcam.CamOrg.y, a.pcam.CamOrg.z);

@@ -283,4 +283,100 @@ __device__ __forceinline__ bool trace_any(const WideNode *__restrict__ nodes, un
     return false;
 }
 
+// ---------------------------------------------------------------------------
+// Resumable traversal, one node visit per call, for kernels that refill
+// finished lanes with new rays (dynamic ray fetch) instead of letting a warp
+// wait for its longest ray.  Same node order, culling and hit rules as
+// trace_closest / trace_any, so the results are the same.
+// ---------------------------------------------------------------------------
+// The stack lives in a separate local array (TravStack) so that the scalar
+// state stays in registers.
+struct TravStack {
+    uint2 e[kTravStack];
+};
+struct Trav {
+    uint2 group;
+    int sp;
+    float best_t, bu, bv;
+    int best_id, hit_slot;
+};
+
+__device__ __forceinline__ void trav_init(Trav &c, float tmax) {
+    c.sp = 0;
+    c.group = make_uint2(0u, 0x80000000u);
+    c.best_t = tmax;
+    c.bu = 0.0f;
+    c.bv = 0.0f;
+    c.best_id = 0x7fffffff;
+    c.hit_slot = -1;
+}
+
+// Visits one node and the triangles of its hit leaves.  any_mode: stop at the
+// first triangle with kTMin <= t < best_t (occlusion); otherwise keep the
+// closest hit (ties to the smaller id).  Returns true when the traversal is
+// finished; then c.hit_slot is the BVH-order triangle index hit, or -1.
+template <bool kCount>
+__device__ __forceinline__ bool trav_step(const WideNode *__restrict__ nodes, unsigned n_nodes,
+                                          const float4 *__restrict__ tri, unsigned n_tris, const RayPre &r,
+                                          Trav &c, TravStack &stk, bool any_mode, TravStats &st) {
+    uint2 tg = make_uint2(0u, 0u);
+    if (c.group.y & 0xff000000u) {
+        const unsigned hits_imask = c.group.y;
+        const int child_bit = 31 - __clz(hits_imask & 0xff000000u);
+        const unsigned base = c.group.x;
+        c.group.y &= ~(1u << child_bit);
+        if (c.group.y & 0xff000000u) {
+            if (c.sp < kTravStack) stk.e[c.sp++] = c.group;
+            else st.overflow = 1;
+        }
+        const unsigned slot = (unsigned)(child_bit - 24) ^ (r.oct_inv4 & 0xffu);
+        const unsigned rel = __popc(hits_imask & ~(0xffffffffu << slot));
+        if (base + rel >= n_nodes) { st.overflow = 2; return true; }
+        const WideNode *nd = nodes + base + rel;
+        const float4 n0 = __ldg(&nd->n0), n1 = __ldg(&nd->n1), n2 = __ldg(&nd->n2), n3 = __ldg(&nd->n3),
+                     n4 = __ldg(&nd->n4);
+        if (kCount) ++st.nodes;
+        const unsigned hm = node_intersect(r, 0.0f, c.best_t, n0, n1, n2, n3, n4);
+        const unsigned imask = __float_as_uint(n0.w) >> 24;
+        c.group = make_uint2(__float_as_uint(n1.x), (hm & 0xff000000u) | imask);
+        tg = make_uint2(__float_as_uint(n1.y), hm & 0x00ffffffu);
+    } else {
+        tg = c.group;
+        c.group = make_uint2(0u, 0u);
+    }
+    while (tg.y != 0u) {
+        const int k = __ffs(tg.y) - 1;
+        tg.y &= tg.y - 1u;
+        const int ti = (int)tg.x + k;
+        if ((unsigned)ti >= n_tris) { st.overflow = 2; return true; }
+        const float4 a = __ldg(&tri[3 * ti]), b = __ldg(&tri[3 * ti + 1]), cc = __ldg(&tri[3 * ti + 2]);
+        if (kCount) ++st.tris;
+        float t, u, v;
+        if (tri_intersect(r, a, b, cc, &t, &u, &v)) {
+            ref_distance(r, a, b, cc, &t, &u, &v);
+            if (!(t >= kTMin)) continue;
+            const int id = __float_as_int(a.w);
+            if (any_mode) {
+                if (t < c.best_t) {
+                    c.best_t = t;
+                    c.best_id = id;
+                    c.hit_slot = ti;
+                    return true;
+                }
+            } else if (t < c.best_t || (t == c.best_t && id < c.best_id)) {
+                c.best_t = t;
+                c.best_id = id;
+                c.bu = u;
+                c.bv = v;
+                c.hit_slot = ti;
+            }
+        }
+    }
+    if ((c.group.y & 0xff000000u) == 0u) {
+        if (c.sp == 0) return true;
+        c.group = stk.e[--c.sp];
+    }
+    return false;
+}
+
 }  // namespace kgk

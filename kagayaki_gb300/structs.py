@@ -92,6 +92,14 @@ class KgkSvgfConfig(ctypes.Structure):
                 ("sigma_l", ctypes.c_float), ("reserved", ctypes.c_int32 * 6)]
 
 
+class KgkNrcConfig(ctypes.Structure):
+    _fields_ = [("width", ctypes.c_int32), ("hidden_layers", ctypes.c_int32),
+                ("learning_rate", ctypes.c_float), ("train_paths", ctypes.c_int32),
+                ("train_suffix_max", ctypes.c_int32), ("train_steps", ctypes.c_int32),
+                ("spread_c", ctypes.c_float), ("seed", ctypes.c_uint64),
+                ("reserved", ctypes.c_int32 * 8)]
+
+
 assert ctypes.sizeof(KgkCamera) == 72
 assert ctypes.sizeof(KgkTexture) == 24
 

@@ -130,3 +130,29 @@ def test_svgf_restatement_bit_exact_with_reference():
     orc.svgf_compat(W, H, r1, f1, prev1, cur1, 1)
     assert np.array_equal(f1, g["out_filtered1"])
     assert np.array_equal(cur1, g["out_cur1"])
+
+
+def test_mlp_oracle_gradients_match_finite_differences():
+    """The FP64 MLP oracle's backward pass, checked by central differences of
+    the relative-L2 loss with its stop-gradient denominator held at the base
+    point."""
+    from oracle import mlp_oracle as mo
+    rng = np.random.default_rng(0)
+    w = [rng.uniform(-1, 1, (64, 64)) * 0.3 for _ in range(5)] + [rng.uniform(-1, 1, (3, 64)) * 0.3]
+    raw = rng.uniform(0, 1, (64, 13))
+    t = rng.uniform(0, 1, (64, 3))
+    _, g, y0 = mo.gradients(w, raw, t, quantize=False)
+    den0 = y0 * y0 + mo.EPS_REL
+
+    def frozen_loss(ws):
+        y, _, _ = mo.forward(ws, raw, quantize=False)
+        return np.sum((y - t) ** 2 / den0) / y.size
+
+    eps = 1e-6
+    for (l, i, j) in [(0, 3, 40), (2, 5, 7), (4, 63, 0), (5, 1, 17)]:
+        wp = [x.copy() for x in w]
+        wp[l][i, j] += eps
+        wm = [x.copy() for x in w]
+        wm[l][i, j] -= eps
+        fd = (frozen_loss(wp) - frozen_loss(wm)) / (2 * eps)
+        assert abs(fd - g[l][i, j]) <= 1e-6 + 1e-5 * abs(fd), (l, i, j, fd, g[l][i, j])

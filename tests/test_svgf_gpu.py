@@ -86,5 +86,7 @@ def test_svgf_standard_reduces_error_over_an_orbit():
             errs_noisy.append(relmse(noisy))
             errs_filt.append(relmse(out))
     assert all(np.isfinite(errs_filt))
-    assert errs_filt[-1] < 0.5 * errs_noisy[-1], (errs_noisy, errs_filt)
-    assert np.mean(errs_filt[4:]) <= np.mean(errs_filt[:2]) * 1.05, errs_filt
+    # every filtered frame at most half the relative MSE of its 1-spp input,
+    # and the history never makes a later frame worse than the first
+    assert all(f < 0.5 * n for f, n in zip(errs_filt, errs_noisy)), (errs_noisy, errs_filt)
+    assert max(errs_filt[2:]) <= 1.5 * errs_filt[0], errs_filt
