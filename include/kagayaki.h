@@ -305,6 +305,36 @@ typedef struct kgk_svgf_buffer {
 kgk_status kgk_svgf_apply(kgk_vec *result, kgk_vec *filtered, kgk_svgf_buffer *prev,
                           kgk_svgf_buffer *cur, int32_t width, int32_t height, int32_t frame);
 
+/* Largest image (width * height) kgk_svgf_apply_noalloc accepts. */
+#define KGK_SVGF_NOALLOC_MAX_PIXELS (512 * 512)
+
+/* kgk_svgf_apply without any device allocation, for callers that cannot call
+ * cudaMalloc: applications that hand all device memory to their own pool
+ * allocator at start-up, and per-frame loops that must not allocate because
+ * cudaMalloc / cudaFree synchronise the whole device.  No counterpart in the
+ * reference (its ApplySVGF allocates nothing because its scratch is fixed
+ * 1920x1920 globals, SVGF.cuh:109-110).
+ *
+ * Same filter and results as kgk_svgf_apply.  Differences:
+ *  - result, filtered, prev and cur must be device memory (host buffers are
+ *    rejected: staging them would allocate);
+ *  - width * height <= KGK_SVGF_NOALLOC_MAX_PIXELS, else
+ *    KGK_ERR_INVALID_ARGUMENT;
+ *  - the work runs on `cuda_stream` (a cudaStream_t, NULL = the default
+ *    stream) and the call returns when it has finished;
+ *  - scratch comes from one fixed device array of ~15 MB inside the library,
+ *    which every GPU that loads the library holds until the process exits.
+ *    All calls share it: calls that overlap on the GPU (for instance from two
+ *    host threads on two streams) race and give undefined results.  Each call
+ *    writes every scratch word it reads, so what an earlier call left there
+ *    does not matter.
+ * The first call on each device looks the array's device address up
+ * (cudaGetSymbolAddress) with that device current; make that first call
+ * before any stream capture. */
+kgk_status kgk_svgf_apply_noalloc(kgk_vec *result, kgk_vec *filtered, kgk_svgf_buffer *prev,
+                                  kgk_svgf_buffer *cur, int32_t width, int32_t height, int32_t frame,
+                                  void *cuda_stream);
+
 /* ------------------------------------------------------------------------- */
 /* Learned radiance cache (no counterpart in the reference)                    */
 /* ------------------------------------------------------------------------- */

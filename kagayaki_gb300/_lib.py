@@ -37,6 +37,7 @@ PROTOTYPES = {
     "kgk_accum_read": (_st, [_vp, _vp, _vp, ctypes.POINTER(ctypes.c_uint64)]),
     "kgk_svgf": (_st, [_vp, ctypes.POINTER(KgkSvgfConfig), _vp, _vp]),
     "kgk_svgf_apply": (_st, [_vp, _vp, _vp, _vp, _i32, _i32, _i32]),
+    "kgk_svgf_apply_noalloc": (_st, [_vp, _vp, _vp, _vp, _i32, _i32, _i32, _vp]),
     "kgk_nrc_init": (_st, [_vp, _vp]),
     "kgk_nrc_set_weights": (_st, [_vp, _vp, _sz]),
     "kgk_nrc_get_weights": (_st, [_vp, _vp, _sz]),

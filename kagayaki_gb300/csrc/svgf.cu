@@ -836,3 +836,113 @@ kgk_status kgk_svgf(kgk_scene *s, const kgk_svgf_config *cfg, const kgk_vec *noi
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Allocation-free ApplySVGF (kgk_svgf_apply_noalloc).
+//
+// Some callers cannot call cudaMalloc: applications that reserve all device
+// memory for their own pool allocator at start-up, and per-frame loops that
+// must not allocate because cudaMalloc / cudaFree synchronise the whole device
+// and stall the caller's other streams.  This entry point takes its scratch
+// from g_svgf_scratch, a file-scope device array sized for
+// KGK_SVGF_NOALLOC_MAX_PIXELS pixels (57 B per pixel, ~15 MB); every GPU that
+// loads the library holds that array until the process exits.
+// ---------------------------------------------------------------------------
+#include <mutex>
+
+namespace kgk {
+namespace {
+
+constexpr size_t kNaMax = (size_t)KGK_SVGF_NOALLOC_MAX_PIXELS;
+constexpr size_t kNaAlign = 256;
+constexpr size_t na_up(size_t x) { return (x + kNaAlign - 1) & ~(kNaAlign - 1); }
+constexpr size_t kNaFloats = na_up(kNaMax * sizeof(float));
+// M1, M2, sd, gz (x2), s1, s2, sw, var, var2 | R2 (kgk_vec) | spatial (bytes)
+constexpr size_t kNaBytes = 10 * kNaFloats + na_up(kNaMax * sizeof(kgk_vec)) + na_up(kNaMax);
+
+__device__ __align__(256) static unsigned char g_svgf_scratch[kNaBytes];
+
+constexpr int kNaMaxDevices = 64;
+std::mutex g_na_mu;
+unsigned char *g_na_addr[kNaMaxDevices] = {};
+
+// Device address of g_svgf_scratch on the current device; looked up once per
+// device (with that device current) and cached.
+kgk_status noalloc_scratch(unsigned char **out) {
+    int dev = 0;
+    KGK_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kNaMaxDevices) return fail(KGK_ERR_NO_DEVICE, "kgk_svgf_apply_noalloc: device index too large");
+    std::lock_guard<std::mutex> lock(g_na_mu);
+    if (!g_na_addr[dev]) {
+        unsigned char *ptr = nullptr;
+        cudaError_t e = cudaGetSymbolAddress((void **)&ptr, g_svgf_scratch);
+        if (e != cudaSuccess || !ptr) return cuda_fail(e, "cudaGetSymbolAddress(g_svgf_scratch)");
+        g_na_addr[dev] = ptr;
+    }
+    *out = g_na_addr[dev];
+    return KGK_OK;
+}
+
+}  // namespace
+}  // namespace kgk
+
+extern "C" kgk_status kgk_svgf_apply_noalloc(kgk_vec *result, kgk_vec *filtered, kgk_svgf_buffer *prev,
+                                             kgk_svgf_buffer *cur, int32_t W, int32_t H, int32_t frame,
+                                             void *cuda_stream) {
+    using namespace kgk;
+    if (!result || !filtered || !prev || !cur)
+        return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_svgf_apply_noalloc: NULL buffer");
+    if (W < 2 || H < 2) return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_svgf_apply_noalloc: image must be at least 2 x 2");
+    if ((long long)W * H > (long long)KGK_SVGF_NOALLOC_MAX_PIXELS)
+        return fail(KGK_ERR_INVALID_ARGUMENT,
+                    "kgk_svgf_apply_noalloc: " + std::to_string((long long)W * H) + " pixels exceed the maximum of " +
+                        std::to_string(KGK_SVGF_NOALLOC_MAX_PIXELS) + " (use kgk_svgf_apply)");
+    if (!is_device_ptr(result) || !is_device_ptr(filtered) || !is_device_ptr(prev) || !is_device_ptr(cur))
+        return fail(KGK_ERR_INVALID_ARGUMENT,
+                    "kgk_svgf_apply_noalloc: all four buffers must be device memory (host buffers would need staging)");
+    unsigned char *base = nullptr;
+    KGK_TRY(noalloc_scratch(&base));
+    cudaStream_t st = (cudaStream_t)cuda_stream;
+    const size_t npx = (size_t)W * H;
+    CompatArgs a;
+    a.W = W; a.H = H; a.frame = frame;
+    a.R = result; a.F = filtered; a.P = prev; a.C = cur;
+    unsigned char *b = base;
+    a.M1 = (float *)b; b += kNaFloats;
+    a.M2 = (float *)b; b += kNaFloats;
+    a.sd = (float *)b; b += kNaFloats;
+    a.gz = (float *)b; b += 2 * kNaFloats;
+    a.s1 = (float *)b; b += kNaFloats;
+    a.s2 = (float *)b; b += kNaFloats;
+    a.sw = (float *)b; b += kNaFloats;
+    a.var = (float *)b; b += kNaFloats;
+    float *var2 = (float *)b; b += kNaFloats;
+    a.R2 = (kgk_vec *)b; b += na_up(kNaMax * sizeof(kgk_vec));
+    a.spatial = b;
+    // Every scratch word is written by an earlier kernel of this call before
+    // any kernel reads it, so the previous call's leftovers never matter.
+    const int g = (int)std::min<size_t>((npx + 255) / 256, 65535);
+    k_c_prologue<<<g, 256, 0, st>>>(a);
+    k_c_temporal<<<g, 256, 0, st>>>(a);
+    k_c_var1<<<g, 256, 0, st>>>(a);
+    k_c_var2<<<g, 256, 0, st>>>(a);
+    k_c_var3<<<g, 256, 0, st>>>(a);
+    k_c_var4<<<g, 256, 0, st>>>(a);
+    k_c_var5<<<g, 256, 0, st>>>(a);
+    k_c_gauss1<<<g, 256, 0, st>>>(a);
+    k_c_gauss2<<<g, 256, 0, st>>>(a);
+    kgk_vec *rin = result, *rout = a.R2;
+    float *vin = a.var, *vout = var2;
+    for (int k = 0; k < 5; ++k)
+        for (int s = 0; s < 5; ++s) {
+            k_c_atrous<<<g, 256, 0, st>>>(a, rin, rout, vin, vout, s);
+            std::swap(rin, rout);
+            std::swap(vin, vout);
+        }
+    if (rin != result) k_copy_vec<<<g, 256, 0, st>>>(rin, result, (int)npx);
+    k_c_final<<<g, 256, 0, st>>>(a, vin);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_fail(e, "kgk_svgf_apply_noalloc kernels");
+    return KGK_OK;
+}
