@@ -12,6 +12,10 @@ e2e:   the same through the C ABI with host buffers: the camera is read from
        oracle port; the reference's own GPU renderer is not run, see the
        design notes), timed on a bounded sample of the same workload with all
        host threads.
+relmse: equal-time image error against a converged 4096-spp frame (FP64
+       accumulation on the GPU), plain path tracing vs the learned radiance
+       cache, at the first camera of the orbit (static camera, 1 spp per
+       cached frame, online training included in the cached frames' time).
 Inputs (BVH + triangles ~0.7 GB) exceed the 129 MB L2, so no flush is needed.
 """
 import argparse
@@ -176,11 +180,15 @@ def run_ours(args):
     rays = 0
     dev_ms = 0.0
     launches = 0
+    ext_ms = 0.0
+    ext_rays = 0
     for k in range(args.steps):
-        img, st = scene.render(cam, W, H, frame_index=args.warmup + k, out=out_host, **kw)
+        img, st = scene.render(cam, W, H, frame_index=args.warmup + k, out=out_host, profile_stages=True, **kw)
         rays += st["rays_closest"] + st["rays_shadow"]
         dev_ms += st["ms_device"]
         launches += st["kernel_launches"]
+        ext_ms += st["ms_extend"]
+        ext_rays += st["rays_closest"]
     # end to end: host camera in, host frame out, wall clock
     t0 = time.perf_counter()
     e2e_rays = 0
@@ -189,6 +197,9 @@ def run_ours(args):
         e2e_rays += st["rays_closest"] + st["rays_shadow"]
     e2e_s = time.perf_counter() - t0
     ck = clocks.stop(local)
+    study = None
+    if not args.no_relmse and rank == 0:
+        study = relmse_study(scene, W, H, WORKLOAD["max_depth"])
     if dist:
         import torch
         tt = torch.tensor([dev_ms, e2e_s], dtype=torch.float64, device="cuda")
@@ -201,15 +212,18 @@ def run_ours(args):
     if rank != 0:
         return
     hbm, peak_kind = load_peaks()
-    # roofline of the traversal (extend) stage: algorithmic bytes / stage time
-    alg_bytes = prof["nodes_visited"] * NODE_BYTES + prof["tris_tested"] * TRI_BYTES + \
-        prof["rays_closest"] * RAY_BYTES
-    ext_s = prof["ms_extend"] / 1e3
-    achieved = alg_bytes / ext_s / 1e9 if ext_s > 0 else None
+    # roofline of the traversal (extend) stage: algorithmic bytes per ray
+    # (counted in the untimed counting pass) x rays of the timed frames /
+    # the extend launches' event-timed duration in the timed frames
+    bytes_per_ray = (prof["nodes_visited"] * NODE_BYTES + prof["tris_tested"] * TRI_BYTES +
+                     prof["rays_closest"] * RAY_BYTES) / max(prof["rays_closest"], 1)
+    ext_s = ext_ms / 1e3
+    achieved = bytes_per_ray * ext_rays / ext_s / 1e9 if ext_s > 0 else None
+    n_ext = args.steps * prof["extend_launches"] if prof.get("extend_launches") else None
     traffic = None
-    tf = os.path.join(HERE, "profiles", "extend_traffic.json")
-    if os.path.exists(tf):
-        traffic = json.load(open(tf)).get("bytes_per_launch")
+    dram_per_ray = read_profile_value("k_extend_c2.md", "dram_bytes_per_ray")
+    if dram_per_ray is not None and n_ext:
+        traffic = round(dram_per_ray * ext_rays / n_ext)
     mrays = rays / (dev_ms / 1e3) / 1e6
     line = {
         "metric": "Mrays/s",
@@ -232,13 +246,16 @@ def run_ours(args):
                      "peak": hbm, "unit": "GB/s", "frac": round(achieved / hbm, 4) if achieved else None,
                      "traffic": traffic, "kernel": "k_extend (closest-hit traversal)",
                      "peak_source": peak_kind,
-                     "bytes_per_ray": round(alg_bytes / max(prof["rays_closest"], 1), 1)},
+                     "bytes_per_ray": round(bytes_per_ray, 1),
+                     "achieved_per_launch_bytes": round(bytes_per_ray * ext_rays / n_ext) if n_ext else None},
         "stages_ms": {"extend": round(prof["ms_extend"], 2), "shade": round(prof["ms_shade"], 2),
                       "shadow": round(prof["ms_shadow"], 2)},
         "rays_per_step": int(rays / args.steps),
         "bvh": {"wide_nodes": bvh["n_wide_nodes"], "build_ms": round(bvh["ms_build"], 1)},
         "clocks": ck,
     }
+    if study:
+        line["relmse"] = study
     if not args.no_cpu:
         thr = os.cpu_count() or 1
         rps, nr, dt, npx_done = cpu_reference(tris, mats, env, thr, budget_s=args.cpu_seconds)
@@ -246,6 +263,77 @@ def run_ours(args):
                                 "sample": f"{npx_done} random pixels of the frame at 1 spp, compat estimator "
                                           f"(oracle port, CPU BVH): {nr} rays in {dt:.1f} s"}
     print(json.dumps(line), flush=True)
+
+
+def read_profile_value(name, key):
+    """A `key = value` line of a committed ncu summary under profiles/."""
+    path = os.path.join(HERE, "profiles", name)
+    if not os.path.exists(path):
+        return None
+    for ln in open(path):
+        ln = ln.strip().strip("`")
+        if ln.startswith(key) and "=" in ln:
+            try:
+                return float(ln.split("=", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+def rel_mse(img, ref):
+    """Mean over pixels and channels of (x - ref)^2 / (ref^2 + 0.01)."""
+    return float(np.mean((img - ref) ** 2 / (ref ** 2 + 1e-2)))
+
+
+def relmse_study(scene, W, H, max_depth, ref_spp=4096, train_frames=32, eval_frames=16):
+    """Equal-time relMSE, plain vs learned radiance cache, against a converged
+    FP64-accumulated reference at the first camera of the orbit."""
+    from kagayaki_gb300 import ESTIMATOR_UNBIASED
+    cam = orbit_camera(0, H)
+    kw = dict(max_depth=max_depth, estimator=ESTIMATOR_UNBIASED)
+    out = np.empty((H, W, 4), np.float32)
+    t0 = time.perf_counter()
+    scene.accum_reset(W, H)
+    chunk = 64
+    for k in range(ref_spp // chunk):
+        scene.render(cam, W, H, spp=chunk, seed=7, frame_index=200_000 + k, accumulate=True, out=out, **kw)
+    ref, _, nref = scene.accum_read(W, H)
+    ref_s = time.perf_counter() - t0
+    # plain: device ms per sample per pixel, then the equal-time image
+    plain1, st1 = scene.render(cam, W, H, spp=1, seed=3, frame_index=300_000, out=out, **kw)
+    plain1 = plain1[..., :3].astype(np.float64)
+    _, st4 = scene.render(cam, W, H, spp=4, seed=3, frame_index=300_001, out=out, **kw)
+    ms_per_spp = st4["ms_device"] / 4
+    # cache: online training at 1 spp per frame, then eval_frames more frames
+    scene.cache_init(seed=1)
+    for f in range(train_frames):
+        scene.render(cam, W, H, spp=1, seed=5, frame_index=f, use_cache=True, out=out, **kw)
+    acc = np.zeros((H, W, 3))
+    cache_ms = 0.0
+    cache1 = None
+    for f in range(eval_frames):
+        img, st = scene.render(cam, W, H, spp=1, seed=5, frame_index=train_frames + f, use_cache=True, out=out,
+                               **kw)
+        acc += img[..., :3]
+        cache_ms += st["ms_device"]
+        if cache1 is None:
+            cache1 = img[..., :3].astype(np.float64)
+            cache1_ms = st["ms_device"]
+    cache_img = acc / eval_frames
+    spp_eq = max(1, int(round(cache_ms / ms_per_spp)))
+    plain_eq, stp = scene.render(cam, W, H, spp=spp_eq, seed=9, frame_index=300_002, out=out, **kw)
+    plain_eq = plain_eq[..., :3].astype(np.float64)
+    return {
+        "reference": {"spp": int(nref), "accumulation": "fp64", "seconds": round(ref_s, 1)},
+        "camera": "orbit frame 0 (static)",
+        "plain_1spp": {"relmse": round(rel_mse(plain1, ref), 5), "ms": round(st1["ms_device"], 2)},
+        "cache_1spp": {"relmse": round(rel_mse(cache1, ref), 5), "ms": round(cache1_ms, 2),
+                       "after_training_frames": train_frames},
+        "equal_time": {"ms": round(cache_ms, 2),
+                       "cache": {"relmse": round(rel_mse(cache_img, ref), 5), "frames": eval_frames, "spp": eval_frames},
+                       "plain": {"relmse": round(rel_mse(plain_eq, ref), 5), "spp": spp_eq,
+                                 "ms": round(stp["ms_device"], 2)}},
+    }
 
 
 def run_reference(args):
@@ -283,6 +371,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU baseline work budget")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
+    ap.add_argument("--no-relmse", action="store_true", help="skip the plain-vs-cache relMSE study")
     ap.add_argument("--width", type=int, default=0, help="override the frame width (profiling cases)")
     ap.add_argument("--height", type=int, default=0, help="override the frame height")
     ap.add_argument("--spp", type=int, default=0, help="override the samples per pixel")

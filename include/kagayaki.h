@@ -147,6 +147,7 @@ typedef struct kgk_stats {
     double ms_extend;             /* closest-hit stage device time (profile_stages) */
     double ms_shade;              /* shading stage device time (profile_stages)  */
     double ms_shadow;             /* shadow-ray stage device time (profile_stages) */
+    uint64_t extend_launches;     /* closest-hit (extend) kernel launches        */
 } kgk_stats;
 
 typedef struct kgk_bvh_info {
@@ -189,11 +190,38 @@ kgk_status kgk_scene_create(const kgk_triangle *tris, size_t n_tris,
                             const kgk_texture *textures, size_t n_textures,
                             const kgk_texture *hdr, kgk_scene **out);
 
-/* Loads a Wavefront OBJ (+ MTL in mtl_dir) and an optional Radiance .hdr
- * environment: the loader semantics of load_object
- * (FileIO/IO_load_WavefrontObj.cuh:10-127) and load_HDR
- * (FileIO/IO_load_images.cuh:17-19).  Missing vn/vt are tolerated (flat
- * normal, zero uv) where the reference would crash. */
+/* A scene read from files, in host memory (malloc'ed by the library; free it
+ * with kgk_host_scene_free).  hdr.pixels == NULL: no environment. */
+typedef struct kgk_host_scene {
+    kgk_triangle *triangles;
+    size_t n_triangles;
+    kgk_material *materials;   /* [0] = the reserved grey material (scene.cuh:14-18) */
+    size_t n_materials;
+    kgk_texture *textures;     /* float pixels, + 1e-4 as the reference loads them */
+    size_t n_textures;
+    kgk_texture hdr;
+} kgk_host_scene;
+
+/* Reads a Wavefront OBJ with its MTL files and diffuse textures, and an
+ * optional environment image (hdr_path may be NULL), into host arrays: the
+ * semantics of load_object (FileIO/IO_load_WavefrontObj.cuh:10-127, which
+ * parses with tinyobjloader v2.0.0rc10) and load_Textures / load_HDR
+ * (FileIO/IO_load_images.cuh:9-29).  MTL files and textures are looked up in
+ * the OBJ file's directory.  Vertices without vn take the face normal and
+ * without vt (0,0,0), where the reference would read past its arrays.
+ * Images: PNG, binary PNM and Radiance .hdr (KGK_ERR_UNSUPPORTED for JPEG and
+ * other formats). */
+kgk_status kgk_load_obj(const char *obj_path, const char *hdr_path, kgk_host_scene *out);
+void kgk_host_scene_free(kgk_host_scene *scene);
+
+/* stbi_loadf (FileIO/IO_load_images.cuh:10): the image as float pixels with
+ * its own channel count; 8-bit colour channels (v/255)^2.2, alpha v/255, .hdr
+ * as stored.  Free with kgk_image_free. */
+kgk_status kgk_load_image(const char *path, kgk_texture *out);
+void kgk_image_free(kgk_texture *image);
+
+/* kgk_load_obj followed by kgk_scene_create (render_prepare's load_object +
+ * load_HDR, render_prepare.cuh:35-37). */
 kgk_status kgk_scene_load_obj(const char *obj_path, const char *hdr_path, kgk_scene **out);
 
 void kgk_scene_destroy(kgk_scene *scene);

@@ -5,4 +5,4 @@ include/kagayaki.h); this package is its host-side mirror.
 """
 from ._lib import KgkError, lib, last_error  # noqa: F401
 from .api import (ESTIMATOR_COMPAT, ESTIMATOR_UNBIASED, Scene, camera_array,  # noqa: F401
-                  camera_setup, save_png, tonemap)
+                  camera_setup, load_image, load_obj, save_png, tonemap)

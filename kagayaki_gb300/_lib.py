@@ -45,6 +45,10 @@ PROTOTYPES = {
     "kgk_nrc_gradients": (_st, [_vp, _vp, _vp, _sz, _vp, _vp]),
     "kgk_nrc_train": (_st, [_vp, _vp, _vp, _sz, _i32, _vp]),
     "kgk_nrc_loss_scale": (_st, [_vp, _vp]),
+    "kgk_load_obj": (_st, [ctypes.c_char_p, ctypes.c_char_p, _vp]),
+    "kgk_host_scene_free": (None, [_vp]),
+    "kgk_load_image": (_st, [ctypes.c_char_p, _vp]),
+    "kgk_image_free": (None, [_vp]),
     "kgk_tonemap_rgba8": (_st, [_vp, _i32, _i32, _vp]),
     "kgk_save_png": (_st, [_vp, _i32, _i32, ctypes.c_char_p]),
 }

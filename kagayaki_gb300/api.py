@@ -16,8 +16,8 @@ import numpy as np
 
 from . import _lib
 from ._lib import KgkError, check, lib
-from .structs import (MATERIAL, RAY, TRIANGLE, KgkBvhInfo, KgkCamera, KgkNrcConfig, KgkRenderConfig,
-                      KgkStats, KgkSvgfConfig, KgkTexture, KgkVec)
+from .structs import (MATERIAL, RAY, TRIANGLE, KgkBvhInfo, KgkCamera, KgkHostScene, KgkNrcConfig,
+                      KgkRenderConfig, KgkStats, KgkSvgfConfig, KgkTexture, KgkVec)
 
 ESTIMATOR_COMPAT = 0
 ESTIMATOR_UNBIASED = 1
@@ -68,6 +68,18 @@ class Scene:
                                      ctypes.byref(self._h)))
         self.n_triangles = len(tris)
         self.bvh = None
+
+    @classmethod
+    def from_obj(cls, obj_path, hdr_path=None):
+        """kgk_scene_load_obj: an OBJ scene (and environment) straight to the device."""
+        self = cls.__new__(cls)
+        self._h = ctypes.c_void_p()
+        self._keep = []
+        check(lib().kgk_scene_load_obj(str(obj_path).encode(), str(hdr_path).encode() if hdr_path else None,
+                                       ctypes.byref(self._h)))
+        self.n_triangles = None
+        self.bvh = None
+        return self
 
     def close(self):
         if self._h:
@@ -146,6 +158,44 @@ class Scene:
         n = ctypes.c_uint64()
         check(lib().kgk_accum_read(self._h, _p(mean), _p(var), ctypes.byref(n)))
         return mean, var, n.value
+
+
+def _texture_array(t):
+    n = t.width * t.height * t.bpp
+    if not t.pixels or n == 0:
+        return None
+    return np.ctypeslib.as_array(ctypes.cast(t.pixels, ctypes.POINTER(ctypes.c_float)), (n,)).copy().reshape(
+        t.height, t.width, t.bpp)
+
+
+def load_image(path):
+    """stbi_loadf semantics (FileIO/IO_load_images.cuh:10): float pixels
+    (height, width, channels)."""
+    t = KgkTexture()
+    check(lib().kgk_load_image(str(path).encode(), ctypes.byref(t)))
+    try:
+        return _texture_array(t)
+    finally:
+        lib().kgk_image_free(ctypes.byref(t))
+
+
+def load_obj(obj_path, hdr_path=None):
+    """load_object + load_Textures + load_HDR (FileIO/IO_load_WavefrontObj.cuh:10-127,
+    FileIO/IO_load_images.cuh:9-29).  Returns (triangles, materials,
+    [texture arrays], environment array or None)."""
+    hs = KgkHostScene()
+    check(lib().kgk_load_obj(str(obj_path).encode(), str(hdr_path).encode() if hdr_path else None,
+                             ctypes.byref(hs)))
+    try:
+        tris = np.frombuffer(ctypes.string_at(hs.triangles, hs.n_triangles * TRIANGLE.itemsize),
+                             TRIANGLE).copy()
+        mats = np.frombuffer(ctypes.string_at(hs.materials, hs.n_materials * MATERIAL.itemsize),
+                             MATERIAL).copy()
+        texs = [_texture_array(hs.textures[i]) for i in range(hs.n_textures)]
+        env = _texture_array(hs.hdr)
+        return tris, mats, texs, env
+    finally:
+        lib().kgk_host_scene_free(ctypes.byref(hs))
 
 
 def camera_setup(origin, dist, rot, image_height):

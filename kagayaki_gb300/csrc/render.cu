@@ -1040,7 +1040,7 @@ kgk_status kgk_render(kgk_scene *s, const kgk_camera *cam, const kgk_camera *pre
     KGK_CUDA(cudaEventCreate(&e1));
     KGK_CUDA(cudaEventRecord(e0, st));
     const int max_bounces = cfg->max_depth > 0 ? cfg->max_depth : 1024;
-    uint64_t launches = 0;
+    uint64_t launches = 0, extend_launches = 0;
     // optional per-stage timing: an event before and after every stage launch
     const bool prof = cfg->profile_stages != 0;
     std::vector<cudaEvent_t> ev;
@@ -1084,6 +1084,7 @@ kgk_status kgk_render(kgk_scene *s, const kgk_camera *cam, const kgk_camera *pre
             else
                 k_extend<false><<<grid, 128, 0, st>>>(P, q, cur, n, R.sq[0], R.sq[1], R.sq[2]);
             KGK_TRY(stage_end());
+            ++extend_launches;
             KGK_TRY(stage_begin(1));
             if (cfg->estimator == KGK_ESTIMATOR_COMPAT)
                 k_shade<KGK_ESTIMATOR_COMPAT><<<grid, 128, 0, st>>>(P, R.sq[0], R.sq[1], R.sq[2], R.aq[cur ^ 1],
@@ -1170,6 +1171,7 @@ kgk_status kgk_render(kgk_scene *s, const kgk_camera *cam, const kgk_camera *pre
         stats->paths = (uint64_t)npx * (uint64_t)cfg->spp;
         stats->ms_device = ms;
         stats->kernel_launches = launches;
+        stats->extend_launches = extend_launches;
         double stage_ms[3] = {0, 0, 0};
         for (size_t k = 0; k + 1 < ev.size(); k += 2) {
             float m = 0;
@@ -1224,10 +1226,6 @@ kgk_status kgk_accum_read(kgk_scene *s, double *mean, double *var, uint64_t *n_s
     }
     if (n_samples) *n_samples = R->acc_n;
     return KGK_OK;
-}
-
-kgk_status kgk_scene_load_obj(const char *, const char *, kgk_scene **) {
-    return fail(KGK_ERR_UNSUPPORTED, "kgk_scene_load_obj: not built yet");
 }
 
 }  // extern "C"

@@ -74,7 +74,7 @@ class KgkStats(ctypes.Structure):
                 ("tris_tested", ctypes.c_uint64), ("paths", ctypes.c_uint64),
                 ("ms_device", ctypes.c_double), ("kernel_launches", ctypes.c_uint64),
                 ("ms_extend", ctypes.c_double), ("ms_shade", ctypes.c_double),
-                ("ms_shadow", ctypes.c_double)]
+                ("ms_shadow", ctypes.c_double), ("extend_launches", ctypes.c_uint64)]
 
 
 class KgkBvhInfo(ctypes.Structure):
@@ -90,6 +90,13 @@ class KgkSvgfConfig(ctypes.Structure):
                 ("atrous_repeats", ctypes.c_int32), ("alpha", ctypes.c_float),
                 ("sigma_z", ctypes.c_float), ("sigma_n", ctypes.c_float),
                 ("sigma_l", ctypes.c_float), ("reserved", ctypes.c_int32 * 6)]
+
+
+class KgkHostScene(ctypes.Structure):
+    _fields_ = [("triangles", ctypes.c_void_p), ("n_triangles", ctypes.c_size_t),
+                ("materials", ctypes.c_void_p), ("n_materials", ctypes.c_size_t),
+                ("textures", ctypes.POINTER(KgkTexture)), ("n_textures", ctypes.c_size_t),
+                ("hdr", KgkTexture)]
 
 
 class KgkNrcConfig(ctypes.Structure):

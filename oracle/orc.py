@@ -220,8 +220,44 @@ def ref():
         L.ref_camera_setup.argtypes = [_vp, _f32, _f32, _f32, _f32, _vp]
         L.ref_light_cdf.argtypes = [_vp, _i32, _vp, _i32, _vp]
         L.ref_env_cdf.argtypes = [_vp, _i32, _i32, _i32, _vp]
+        L.ref_load_obj.argtypes = [ctypes.c_char_p, _vp, _vp, _vp]
+        L.ref_load_obj.restype = _i32
+        L.ref_obj_copy.argtypes = [_vp, _vp]
+        L.ref_obj_texture.argtypes = [_i32, _vp, _vp, _vp, ctypes.POINTER(ctypes.POINTER(ctypes.c_float))]
+        L.ref_load_image.argtypes = [ctypes.c_char_p, _vp, _vp, _vp]
+        L.ref_load_image.restype = ctypes.POINTER(ctypes.c_float)
         _ref = L
     return _ref
+
+
+def ref_load_obj(directory):
+    """The reference's load_object run in `directory` (./OBJ.obj there).
+    Returns (triangles, materials, [texture arrays (h, w, bpp)])."""
+    from kagayaki_gb300.structs import MATERIAL, TRIANGLE
+    nt, nm, nx = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    rc = ref().ref_load_obj(directory.encode(), ctypes.byref(nt), ctypes.byref(nm), ctypes.byref(nx))
+    assert rc == 0
+    tris = np.zeros(nt.value, TRIANGLE)
+    mats = np.zeros(nm.value, MATERIAL)
+    ref().ref_obj_copy(_ptr(tris), _ptr(mats))
+    texs = []
+    for i in range(nx.value):
+        w, h, b = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        px = ctypes.POINTER(ctypes.c_float)()
+        ref().ref_obj_texture(i, ctypes.byref(w), ctypes.byref(h), ctypes.byref(b), ctypes.byref(px))
+        n = w.value * h.value * b.value
+        texs.append(np.ctypeslib.as_array(px, (n,)).copy().reshape(h.value, w.value, b.value))
+    return tris, mats, texs
+
+
+def ref_load_image(path):
+    """stbi_loadf(path, ..., 0) as the reference calls it: (h, w, bpp) floats or None."""
+    w, h, b = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    px = ref().ref_load_image(path.encode(), ctypes.byref(w), ctypes.byref(h), ctypes.byref(b))
+    if not px:
+        return None
+    n = w.value * h.value * b.value
+    return np.ctypeslib.as_array(px, (n,)).copy().reshape(h.value, w.value, b.value)
 
 
 def ref_trace(tris, rays, threads=None):

@@ -48,6 +48,9 @@ public:
 #include "struct_Xorshift.cuh"
 #include "NextEventEstimation.cuh"
 #include "render.cuh"
+#include "FileIO/IO_load_WavefrontObj.cuh"
+
+#include <unistd.h>
 
 thread_local kgk_uint3_ blockIdx, threadIdx, blockDim;
 static std::barrier<> *g_barrier = nullptr;
@@ -290,6 +293,41 @@ void ref_env_cdf(const float *pixels, int w, int h, int bpp, float *out) {
     HOST_Light_strength_sum_HDR.clear();
     calculate_Lss_HDR();
     std::memcpy(out, HOST_Light_strength_sum_HDR.data(), sizeof(float) * (size_t)w * h);
+}
+
+/* load_object (IO_load_WavefrontObj.cuh:10-127) + load_Textures run in
+ * directory `dir` (the reference reads ./OBJ.obj, its MTL files and textures
+ * from the working directory).  Counts out; ref_obj_copy fetches the arrays. */
+static std::vector<Material> g_reserved_materials;
+int ref_load_obj(const char *dir, int *n_tris, int *n_mats, int *n_tex) {
+    if (g_reserved_materials.empty()) g_reserved_materials = HOST_MaterialsData;
+    HOST_ObjectsData.clear();
+    HOST_MaterialsData = g_reserved_materials;
+    HOST_TexturesData.clear();
+    char cwd[4096];
+    if (!getcwd(cwd, sizeof cwd)) return -1;
+    if (chdir(dir) != 0) return -1;
+    load_object();
+    const int rc = chdir(cwd);
+    *n_tris = (int)HOST_ObjectsData.size();
+    *n_mats = (int)HOST_MaterialsData.size();
+    *n_tex = (int)HOST_TexturesData.size();
+    return rc;
+}
+void ref_obj_copy(Triangle *tris, Material *mats) {
+    std::memcpy(tris, HOST_ObjectsData.data(), sizeof(Triangle) * HOST_ObjectsData.size());
+    std::memcpy(mats, HOST_MaterialsData.data(), sizeof(Material) * HOST_MaterialsData.size());
+}
+void ref_obj_texture(int i, int *w, int *h, int *bpp, const float **pixels) {
+    *w = HOST_TexturesData[i].width;
+    *h = HOST_TexturesData[i].height;
+    *bpp = HOST_TexturesData[i].bpp;
+    *pixels = HOST_TexturesData[i].pixels;
+}
+
+/* stbi_loadf of one file (load_image without the +1e-4, and load_HDR). */
+const float *ref_load_image(const char *path, int *w, int *h, int *bpp) {
+    return stbi_loadf(path, w, h, bpp, 0);
 }
 
 } // extern "C"

@@ -15,6 +15,12 @@ Fixtures:
   disney_ref.npz        evaluate_Disney_BRDF / _pdf on seeded directions
   camera_ref.npz        Camera_SetUpCamera for a few poses
   cdf_ref.npz           calculate_Lss / calculate_Lss_HDR for small inputs
+  svgf_ref.npz          ApplySVGF (race-free reading) on two frames
+  loader_ref.npz        load_object + load_Textures on the seeded OBJ scene of
+                        tests/golden/scene_files.py, and stbi_loadf on its
+                        seeded PNG / PNM / .hdr images
+
+    python tests/golden/make_golden.py --only loader   # just loader_ref.npz
 """
 import hashlib
 import os
@@ -41,8 +47,35 @@ def ico_scene():
     return tris, mats, info
 
 
+def make_loader_golden():
+    """Reference loader outputs for the seeded files of scene_files.py."""
+    import tempfile
+    sys.path.insert(0, HERE)
+    import scene_files
+    out = {}
+    with tempfile.TemporaryDirectory() as d:
+        for name in scene_files.write_images(d):
+            img = orc.ref_load_image(os.path.join(d, name))
+            assert img is not None, name
+            out["img_" + name] = img
+        scene_files.write_obj_scene(d)
+        tris, mats, texs = orc.ref_load_obj(d)
+    out["obj_tris"] = scenes.canonical(tris)
+    out["obj_mats"] = mats
+    for i, t in enumerate(texs):
+        out[f"obj_tex{i}"] = t
+    out["obj_ntex"] = np.int32(len(texs))
+    np.savez_compressed(os.path.join(HERE, "loader_ref.npz"), **out)
+
+
 def main():
     orc.build(ref=True)
+    assert orc.ref_available(), "oracle/_ref was not built (needs the reference checkout)"
+    if "--only" in sys.argv and sys.argv[sys.argv.index("--only") + 1] == "loader":
+        make_loader_golden()
+        print("loader fixture written to", HERE)
+        return
+    make_loader_golden()
     assert orc.ref_available(), "oracle/_ref was not built (needs the reference checkout)"
 
     # --- closest hits, Cornell box ---

@@ -1,0 +1,100 @@
+"""Scene loading (kgk_load_obj, kgk_load_image) against the reference's own
+loader: load_object / load_Textures (FileIO/IO_load_WavefrontObj.cuh:10-127,
+tinyobjloader) and stbi_loadf (FileIO/IO_load_images.cuh:9-19, stb_image),
+compiled for the host.  The committed fixture tests/golden/loader_ref.npz
+holds the reference's outputs for the seeded files that
+tests/golden/scene_files.py writes; when oracle/_ref is built the reference
+is also run live.  Bar: bit-exact (triangles, materials, every float pixel).
+Host-only: no GPU needed.
+"""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, golden
+from kagayaki_gb300 import KgkError, load_image, load_obj, scenes
+
+sys.path.insert(0, GOLDEN)
+import scene_files  # noqa: E402
+
+
+def same_bits(a, b):
+    a, b = np.ascontiguousarray(a), np.ascontiguousarray(b)
+    return (a.shape == b.shape and a.dtype.itemsize == b.dtype.itemsize and
+            np.array_equal(a.view(np.uint8), b.view(np.uint8)))
+
+
+def test_images_match_stb_loadf(tmp_path):
+    g = golden("loader_ref.npz")
+    names = scene_files.write_images(str(tmp_path))
+    assert len(names) >= 30
+    for name in names:
+        ours = load_image(tmp_path / name)
+        assert same_bits(ours, g["img_" + name]), name
+
+
+def test_obj_scene_matches_reference_loader(tmp_path):
+    g = golden("loader_ref.npz")
+    path = scene_files.write_obj_scene(str(tmp_path))
+    tris, mats, texs, env = load_obj(path)
+    assert env is None
+    assert same_bits(scenes.canonical(tris), scenes.canonical(g["obj_tris"]))  # padding bytes zeroed
+    assert same_bits(mats, g["obj_mats"])
+    assert len(texs) == int(g["obj_ntex"])
+    for i, t in enumerate(texs):
+        assert same_bits(t, g[f"obj_tex{i}"]), i
+    # what the scene exercises
+    assert set(np.unique(tris["shape_id"])) == {0, 1, 2, 4}  # shape 3 has only lines, but it counts
+    assert set(np.unique(tris["material_id"])) >= {0, 1, 2, 3, 4, 5}
+    assert tris["is_SmoothNormal"].any() and not tris["is_SmoothNormal"].all()
+
+
+@pytest.mark.skipif(not os.path.exists(os.path.join(os.path.dirname(GOLDEN), "..", "oracle", "_ref",
+                                                    "libkgkref.so")), reason="reference build not present")
+def test_live_against_reference_build(tmp_path):
+    from oracle import orc
+    names = scene_files.write_images(str(tmp_path))
+    for name in names:
+        assert same_bits(load_image(tmp_path / name), orc.ref_load_image(str(tmp_path / name))), name
+    scene_files.write_obj_scene(str(tmp_path))
+    rt, rm, rx = orc.ref_load_obj(str(tmp_path))
+    tris, mats, texs, _ = load_obj(tmp_path / "OBJ.obj")
+    assert same_bits(scenes.canonical(tris), scenes.canonical(rt))
+    assert same_bits(mats, rm)
+    for a, b in zip(texs, rx):
+        assert same_bits(a, b)
+
+
+def test_environment_loaded_without_offset(tmp_path):
+    g = golden("loader_ref.npz")
+    scene_files.write_images(str(tmp_path))
+    path = scene_files.write_obj_scene(str(tmp_path))
+    _, _, _, env = load_obj(path, tmp_path / "rle.hdr")
+    assert same_bits(env, g["img_rle.hdr"])
+
+
+def test_missing_normals_and_texcoords_are_tolerated(tmp_path):
+    (tmp_path / "a.obj").write_text("v 0 0 0\nv 2 0 0\nv 0 3 0\nv 0 0 1\nf 1 2 3\nf 1 2/1 4\nvt 0.5 0.5\n")
+    tris, mats, texs, _ = load_obj(tmp_path / "a.obj")
+    assert len(tris) == 2 and len(mats) == 1 and not texs
+    np.testing.assert_array_equal(tris["verts"][0, 3:6, :3], [[0, 0, 1]] * 3)  # face normal
+    np.testing.assert_array_equal(tris["verts"][1, 3:6, :3], [[0, -1, 0]] * 3)
+    assert np.all(tris["verts"][0, 6:9] == 0)  # no texcoords
+    # a positive index may name a vt defined later in the file (resolved at the end)
+    np.testing.assert_array_equal(tris["verts"][1, 6:9, :3], [[0, 0, 0], [0.5, 0.5, 0], [0, 0, 0]])
+
+
+def test_errors(tmp_path):
+    with pytest.raises(KgkError, match="cannot open"):
+        load_obj(tmp_path / "missing.obj")
+    (tmp_path / "bad.obj").write_text("v 0 0 0\nf 0 1 2\n")
+    with pytest.raises(KgkError, match="bad face index"):
+        load_obj(tmp_path / "bad.obj")
+    (tmp_path / "oob.obj").write_text("v 0 0 0\nv 1 0 0\nf 1 2 7\n")
+    with pytest.raises(KgkError, match="out of range"):
+        load_obj(tmp_path / "oob.obj")
+    (tmp_path / "x.jpg").write_bytes(b"\xff\xd8\xff\xe0" + bytes(64))
+    with pytest.raises(KgkError, match="JPEG"):
+        load_image(tmp_path / "x.jpg")
