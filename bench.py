@@ -199,7 +199,10 @@ def run_ours(args):
     ck = clocks.stop(local)
     study = None
     if not args.no_relmse and rank == 0:
-        study = relmse_study(scene, W, H, WORKLOAD["max_depth"])
+        try:
+            study = relmse_study(scene, W, H, WORKLOAD["max_depth"])
+        except Exception as e:  # the throughput line is still printed
+            study = {"error": f"{type(e).__name__}: {e}"}
     if dist:
         import torch
         tt = torch.tensor([dev_ms, e2e_s], dtype=torch.float64, device="cuda")
