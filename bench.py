@@ -166,7 +166,8 @@ def run_ours(args):
     scene = Scene(tris, mats, env=env)
     bvh = scene.build_bvh()
     cam = orbit_camera(rank, H)
-    kw = dict(spp=spp, max_depth=WORKLOAD["max_depth"], estimator=ESTIMATOR_UNBIASED, seed=1)
+    kw = dict(spp=spp, max_depth=WORKLOAD["max_depth"], estimator=ESTIMATOR_UNBIASED, seed=1,
+              wave_paths=args.wave_paths)
     out_host = np.empty((H, W, 4), np.float32)
     for w in range(args.warmup):
         scene.render(cam, W, H, frame_index=w, out=out_host, **kw)
@@ -339,6 +340,63 @@ def relmse_study(scene, W, H, max_depth, ref_spp=4096, train_frames=32, eval_fra
     }
 
 
+def run_svgf_orbit(args):
+    """The 1-spp orbit with SVGF: 1920x1080, 60 frames (6 degrees per frame) of
+    the 5.2M-triangle scene, each rendered at 1 spp with its G-buffer and
+    filtered by the standard SVGF (alpha 0.2, 5 a-trous iterations, sigma_z 1,
+    sigma_n 128, sigma_l 4).  frames/s over the wall clock (host buffers);
+    relMSE of the last frame, noisy and filtered, against its converged
+    4096-spp (FP64-accumulated) render."""
+    import ctypes
+    from kagayaki_gb300 import ESTIMATOR_UNBIASED, Scene
+    from kagayaki_gb300._lib import check, lib
+    from kagayaki_gb300.structs import KgkSvgfConfig
+    tris, mats, env, info = build_workload()
+    W, H = args.width or 1920, args.height or 1080
+    frames = 60
+    scene = Scene(tris, mats, env=env)
+    scene.build_bvh()
+    kw = dict(spp=1, max_depth=WORKLOAD["max_depth"], estimator=ESTIMATOR_UNBIASED, write_gbuffer=True)
+    cfg = KgkSvgfConfig(mode=1, width=W, height=H, frame_index=0, atrous_iterations=5, alpha=0.2,
+                        sigma_z=1.0, sigma_n=128.0, sigma_l=4.0)
+    noisy = np.empty((H, W, 4), np.float32)
+    filt = np.empty((H, W, 4), np.float32)
+
+    def frame(f, prev):
+        cam = orbit_camera(f, H)
+        scene.render(cam, W, H, seed=3, frame_index=f, out=noisy, prev_cam=prev, **kw)
+        cfg.frame_index = f
+        check(lib().kgk_svgf(scene._h, ctypes.byref(cfg), ctypes.c_void_p(noisy.ctypes.data),
+                             ctypes.c_void_p(filt.ctypes.data)))
+        return cam
+
+    prev = None
+    for f in range(3):  # warm-up (history restarts at frame 0 below)
+        prev = frame(f, prev)
+    prev = None
+    t0 = time.perf_counter()
+    for f in range(frames):
+        prev = frame(f, prev)
+    secs = time.perf_counter() - t0
+    cam = orbit_camera(frames - 1, H)
+    scene.accum_reset(W, H)
+    for k in range(64):
+        scene.render(cam, W, H, spp=64, seed=7, frame_index=500_000 + k, accumulate=True,
+                     max_depth=WORKLOAD["max_depth"], estimator=ESTIMATOR_UNBIASED)
+    ref, _, nref = scene.accum_read(W, H)
+    scene.close()
+    line = {"metric": "frames/s", "value": round(frames / secs, 2), "unit": "frames/s", "n_gpus": 1,
+            "steps": frames, "warmup": 3, "ms_per_step": round(1e3 * secs / frames, 2), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic seeded scene",
+            "config": {"workload": "svgf-orbit-1spp", "width": W, "height": H, "frames": frames,
+                       "triangles": WORKLOAD["triangles"], "svgf": "standard, alpha 0.2, 5 a-trous, 1/128/4",
+                       "timing": "wall clock, host buffers (render + filter + copies)"},
+            "relmse_last_frame": {"reference_spp": int(nref),
+                                  "noisy_1spp": round(rel_mse(noisy[..., :3].astype(np.float64), ref), 5),
+                                  "svgf": round(rel_mse(filt[..., :3].astype(np.float64), ref), 5)}}
+    print(json.dumps(line), flush=True)
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -375,12 +433,17 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU baseline work budget")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
     ap.add_argument("--no-relmse", action="store_true", help="skip the plain-vs-cache relMSE study")
+    ap.add_argument("--wave-paths", type=int, default=0, help="paths per wave (0 = the library default)")
+    ap.add_argument("--workload", default="frame", choices=["frame", "svgf-orbit"],
+                    help="frame: the 64-spp Mrays/s benchmark; svgf-orbit: 60 frames at 1 spp + SVGF")
     ap.add_argument("--width", type=int, default=0, help="override the frame width (profiling cases)")
     ap.add_argument("--height", type=int, default=0, help="override the frame height")
     ap.add_argument("--spp", type=int, default=0, help="override the samples per pixel")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "svgf-orbit":
+        run_svgf_orbit(args)
     else:
         run_ours(args)
 

@@ -25,6 +25,12 @@
 
 namespace kgk {
 
+// Device bytes per path in flight (ensure_wave): 5 float4 of state, rng,
+// depth, two alive queues, three shade queues, two shadow queues of three
+// float4; with the cache also its spread, flags and query record.
+constexpr size_t kPathStateBytes = 5 * 16 + 8 + 4 + 2 * 4 + 3 * 4 + 2 * 3 * 16;
+constexpr size_t kCachePathBytes = 8 + 4 + 20 * 4;
+
 struct RenderState {
     int W = 0, H = 0;                         // per-pixel buffers
     unsigned long long *seeds = nullptr;      // compat per-pixel seed chain (render.cuh:19,29,42)
@@ -54,6 +60,9 @@ struct RenderState {
     float *trec = nullptr;                    // training records, kQRec floats each
     float *ttgt = nullptr;                    // training targets (3 per record)
     int tcap = 0;
+    int qrec_cap = 0;                         // paths the cache arrays above hold
+    // device bytes held for `cap` paths (they count as available when sizing the wave)
+    size_t cap_bytes_held() const { return (size_t)cap * kPathStateBytes + (size_t)qrec_cap * kCachePathBytes; }
     int sms = 0;
     bool gbuffer_valid = false;               // G-buffer written by the last frame
     kgk_camera gbuffer_cam{};
@@ -70,6 +79,7 @@ enum Cnt {
 };
 // Lanes of a warp that must be idle before the warp fetches new rays.
 constexpr int kRefill = 8;
+
 // Cache record: raw query [13], T [3], path id (int bits), radiance before the
 // query vertex's scattering [3].
 constexpr int kQRec = 20;
@@ -533,7 +543,7 @@ __device__ __forceinline__ void bsdf_eval_pdf(const Surface &S, const DisneyPara
     if (S.m.MATERIAL_TYPE_ID == 1) {
         float3 u, v, w;
         onb_ref(n, u, v, w);
-        f = disney_eval(S.m, dp, wi, wo, n, u, v, w);
+        f = disney_eval<false>(S.m, dp, wi, wo, n, u, v, w);
         pdf = disney_pdf_unbiased(dp, wo, wi, n, u, v, w);
     } else {
         const float c = dot3(n, wi);
@@ -891,7 +901,14 @@ kgk_status ensure_pixels(RenderState &R, int W, int H) {
     return KGK_OK;
 }
 
-kgk_status ensure_wave(RenderState &R, int cap) {
+kgk_status ensure_wave(RenderState &R, int cap, bool cache) {
+    if (R.cap >= cap && (!cache || R.qrec_cap >= cap)) return KGK_OK;
+    if (cache && R.qrec_cap < cap) {
+        KGK_TRY(ensure(&R.spread, cap, "cache path state"));
+        KGK_TRY(ensure(&R.pflags, cap, "cache path state"));
+        KGK_TRY(ensure(&R.qrec, (size_t)cap * kQRec, "cache query records"));
+        R.qrec_cap = cap;
+    }
     if (R.cap >= cap) return KGK_OK;
     KGK_TRY(ensure(&R.o, cap, "path state"));
     KGK_TRY(ensure(&R.d, cap, "path state"));
@@ -907,9 +924,6 @@ kgk_status ensure_wave(RenderState &R, int cap) {
         KGK_TRY(ensure(&R.sh_d[k], cap, "shadow queue"));
         KGK_TRY(ensure(&R.sh_c[k], cap, "shadow queue"));
     }
-    KGK_TRY(ensure(&R.spread, cap, "cache path state"));
-    KGK_TRY(ensure(&R.pflags, cap, "cache path state"));
-    KGK_TRY(ensure(&R.qrec, (size_t)cap * kQRec, "cache query records"));
     R.cap = cap;
     return KGK_OK;
 }
@@ -984,10 +998,21 @@ kgk_status kgk_render(kgk_scene *s, const kgk_camera *cam, const kgk_camera *pre
     // samples per wave: compat chains the per-pixel seeds, one sample per wave
     int spw = 1;
     if (cfg->estimator == KGK_ESTIMATOR_UNBIASED) {
-        const int target = cfg->wave_paths > 0 ? cfg->wave_paths : (1 << 22);
+        // Default: as many paths in flight as fit in half of the free device
+        // memory, up to 2^27 (a 1080p frame at 64 spp in one wave, ~28 GB of
+        // path state): each bounce's last, latency-bound rays then overlap
+        // with the bulk of the frame instead of ending every small wave.
+        int target = cfg->wave_paths;
+        if (target <= 0) {
+            size_t free_b = 0, total_b = 0;
+            KGK_CUDA(cudaMemGetInfo(&free_b, &total_b));
+            const size_t per_path = kPathStateBytes + (cfg->use_cache ? kCachePathBytes : 0);
+            const size_t fit = (free_b / 2 + R.cap_bytes_held()) / per_path;
+            target = (int)std::min<size_t>((size_t)1 << 27, std::max<size_t>(fit, (size_t)npx));
+        }
         spw = std::max(1, std::min(cfg->spp, target / std::max(npx, 1)));
     }
-    KGK_TRY(ensure_wave(R, npx * spw));
+    KGK_TRY(ensure_wave(R, npx * spw, cfg->use_cache != 0));
     if (!R.cnt) KGK_TRY(dalloc(&R.cnt, kNCnt, "counters"));
     if (!R.stats) KGK_TRY(dalloc(&R.stats, kNStat, "counters"));
     if (cfg->accumulate) {

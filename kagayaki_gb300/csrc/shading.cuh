@@ -118,8 +118,20 @@ __device__ __forceinline__ float smith_g(float ndv, float ag) {
     return 1.0f / (ndv + sqrtf(a + b - a * b));
 }
 
+// Smith Lambda of anisotropic GGX in the shading frame (u, v, n).
+__device__ __forceinline__ float g_lambda_n(float3 wd, float3 u, float3 v, float3 n, float ax, float ay) {
+    const float a = dot3(wd, u), b = dot3(wd, v), c = dot3(wd, n);
+    return 0.5f * (-1.0f + sqrtf(1.0f + (ax * ax * a * a + ay * ay * b * b) / (c * c)));
+}
+
 // evaluate_Disney_BRDF (Disney_BRDF.cuh:118-133): out = toward the light,
 // in = toward the viewer; both leave the surface.
+// kRefG = true: the reference's specular shadowing term, whose Lambda is taken
+// in a frame built around the half vector (so it does not fall off at grazing
+// view or light directions; compat mode reproduces it).  kRefG = false (the
+// unbiased estimator): height-correlated Smith G with Lambda in the shading
+// frame, which bounds the sampling weight f cos / pdf at grazing angles.
+template <bool kRefG = true>
 __device__ float3 disney_eval(const kgk_material &m, const DisneyParams &p, float3 out, float3 in,
                               float3 n, float3 u, float3 v, float3 w) {
     if (dot3(n, in) < 0.0f || dot3(n, out) < 0.0f) return f3(0.0f, 0.0f, 0.0f);
@@ -154,7 +166,9 @@ __device__ float3 disney_eval(const kgk_material &m, const DisneyParams &p, floa
         const float fw = pow5(1.0f - dot3(h, n));
         const float3 F = f0 + (f3(1.0f, 1.0f, 1.0f) - f0) * fw;
         const float D = d_gtr2(h, p.ax, p.ay, u, v, w);
-        const float G = 1.0f / (1.0f + g_lambda(in, h, p.ax, p.ay) + g_lambda(out, h, p.ax, p.ay));
+        const float G = kRefG ? 1.0f / (1.0f + g_lambda(in, h, p.ax, p.ay) + g_lambda(out, h, p.ax, p.ay))
+                              : 1.0f / (1.0f + g_lambda_n(in, u, v, w, p.ax, p.ay) +
+                                        g_lambda_n(out, u, v, w, p.ax, p.ay));
         b += F * (D * G / (4.0f * fabsf(ndi) * fabsf(ndo)) * p.wt[3]);
     }
     // clearcoat (GTR1 + Smith 0.25)
@@ -330,16 +344,15 @@ __device__ __forceinline__ float env_texel_weight(const DevScene &s, int row, in
     return (cdf1 - cdf0) * (r1 - r0);  // probability of the texel
 }
 
-// Solid-angle pdf of direction d under env importance sampling.
+// Solid-angle pdf of direction d under env importance sampling: the texel's
+// probability spread uniformly over (longitude, latitude) inside the texel,
+// divided by the solid-angle element cos(latitude) of d itself.
 __device__ __forceinline__ float env_pdf_u(const DevScene &s, float3 d) {
     int row, col;
     float cosl;
     env_dir_to_texel(s, d, row, col, cosl);
-    // texel latitude centre (the CDF weighted texels by this cosine)
-    const float lat = (0.5f - (row + 0.5f) / s.env_h) * kPI;
-    const float c = cosf(lat);
-    if (c <= 1e-7f) return 0.0f;
-    return env_texel_weight(s, row, col) * (float)s.env_w * (float)s.env_h / (2.0f * kPI * kPI * c);
+    if (cosl <= 1e-7f) return 0.0f;
+    return env_texel_weight(s, row, col) * (float)s.env_w * (float)s.env_h / (2.0f * kPI * kPI * cosl);
 }
 
 __device__ __forceinline__ float3 env_lookup_u(const DevScene &s, float3 d) {
@@ -350,8 +363,8 @@ __device__ __forceinline__ float3 env_lookup_u(const DevScene &s, float3 d) {
 }
 
 // Samples a direction; returns it with its solid-angle pdf and radiance.
-// Inside the texel the direction is uniform in (u, latitude) - constant
-// density per texel up to the cos(latitude) factor evaluated at its centre.
+// Inside the texel the direction is uniform in (longitude, latitude), so its
+// solid-angle density carries 1 / cos(latitude) of the sampled direction.
 __device__ __forceinline__ float3 env_sample_u(const DevScene &s, float r0, float r1, float r2, float r3,
                                                float &pdf, float3 &Le) {
     const int row = cdf_search(s.env_row_cdf, s.env_h, r0);
@@ -361,8 +374,8 @@ __device__ __forceinline__ float3 env_sample_u(const DevScene &s, float r0, floa
     const float phi = (v - 0.5f) * kPI, theta = (u - 0.5f) * 2.0f * kPI;
     const float cp = cosf(phi);
     const float3 d = f3(cp * cosf(theta), cp * sinf(theta), sinf(phi));
-    const float lat = (0.5f - (row + 0.5f) / s.env_h) * kPI;
-    pdf = env_texel_weight(s, row, col) * (float)s.env_w * (float)s.env_h / (2.0f * kPI * kPI * fmaxf(cosf(lat), 1e-7f));
+    pdf = cp > 1e-7f ? env_texel_weight(s, row, col) * (float)s.env_w * (float)s.env_h / (2.0f * kPI * kPI * cp)
+                     : 0.0f;
     Le = env_texel(s, row * s.env_w + col);
     return d;
 }
