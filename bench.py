@@ -225,7 +225,7 @@ def run_ours(args):
     achieved = bytes_per_ray * ext_rays / ext_s / 1e9 if ext_s > 0 else None
     n_ext = args.steps * prof["extend_launches"] if prof.get("extend_launches") else None
     traffic = None
-    dram_per_ray = read_profile_value("k_extend_c2.md", "dram_bytes_per_ray")
+    dram_per_ray = read_profile_value("k_extend_c2_traffic.md", "dram_bytes_per_ray")
     if dram_per_ray is not None and n_ext:
         traffic = round(dram_per_ray * ext_rays / n_ext)
     mrays = rays / (dev_ms / 1e3) / 1e6

@@ -130,7 +130,9 @@ typedef struct kgk_render_config {
     int32_t write_gbuffer;   /* 1: write the SVGF G-buffer from primary hits       */
     int32_t use_cache;       /* 1: terminate paths into the radiance cache         */
     int32_t profile_stages;  /* 1: time each pipeline stage with CUDA events        */
-    int32_t reserved[5];
+    int32_t texture_filter;  /* 0: nearest (Texture::get_Color, struct_Texture.cuh:
+                                12-18); 1: bilinear with wrap-around addressing  */
+    int32_t reserved[4];
 } kgk_render_config;
 
 /* Work counters of one call.  Rays follow the reference's counting rule: one
@@ -223,6 +225,20 @@ void kgk_image_free(kgk_texture *image);
 /* kgk_load_obj followed by kgk_scene_create (render_prepare's load_object +
  * load_HDR, render_prepare.cuh:35-37). */
 kgk_status kgk_scene_load_obj(const char *obj_path, const char *hdr_path, kgk_scene **out);
+
+/* An 8-bit RGBA texture, 4 bytes per texel, rows from the top.  Kept as bytes
+ * on the device (a quarter of the float texture's memory); a colour channel v
+ * reads as (v/255)^2.2 + 1e-4, the value the reference's loader
+ * (stbi_loadf + load_image, FileIO/IO_load_images.cuh:9-15) gives the same
+ * 8-bit file, so nearest-filtered renders equal those of the float texture. */
+typedef struct kgk_texture_rgba8 {
+    const uint8_t *pixels;
+    int32_t width, height;
+} kgk_texture_rgba8;
+
+/* Replaces the scene's textures with n RGBA8 textures (materials'
+ * TEXTURE_BASECOLOR_ID index them; n must cover every id in use). */
+kgk_status kgk_scene_set_textures_rgba8(kgk_scene *scene, const kgk_texture_rgba8 *textures, size_t n);
 
 void kgk_scene_destroy(kgk_scene *scene);
 

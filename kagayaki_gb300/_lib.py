@@ -45,6 +45,7 @@ PROTOTYPES = {
     "kgk_nrc_gradients": (_st, [_vp, _vp, _vp, _sz, _vp, _vp]),
     "kgk_nrc_train": (_st, [_vp, _vp, _vp, _sz, _i32, _vp]),
     "kgk_nrc_loss_scale": (_st, [_vp, _vp]),
+    "kgk_scene_set_textures_rgba8": (_st, [_vp, _vp, _sz]),
     "kgk_load_obj": (_st, [ctypes.c_char_p, ctypes.c_char_p, _vp]),
     "kgk_host_scene_free": (None, [_vp]),
     "kgk_load_image": (_st, [ctypes.c_char_p, _vp]),

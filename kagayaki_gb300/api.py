@@ -17,7 +17,7 @@ import numpy as np
 from . import _lib
 from ._lib import KgkError, check, lib
 from .structs import (MATERIAL, RAY, TRIANGLE, KgkBvhInfo, KgkCamera, KgkHostScene, KgkNrcConfig,
-                      KgkRenderConfig, KgkStats, KgkSvgfConfig, KgkTexture, KgkVec)
+                      KgkRenderConfig, KgkStats, KgkSvgfConfig, KgkTexture, KgkTextureRGBA8, KgkVec)
 
 ESTIMATOR_COMPAT = 0
 ESTIMATOR_UNBIASED = 1
@@ -127,13 +127,13 @@ class Scene:
     def render(self, cam, width, height, spp=1, max_depth=0, rr_start_depth=3,
                estimator=ESTIMATOR_COMPAT, seed=1, frame_index=0, accumulate=False,
                count_work=False, write_gbuffer=False, use_cache=False, wave_paths=0, prev_cam=None,
-               out=None, profile_stages=False):
+               out=None, profile_stages=False, texture_filter=0):
         cfg = KgkRenderConfig(width=width, height=height, spp=spp, max_depth=max_depth,
                               rr_start_depth=rr_start_depth, estimator=estimator, seed=seed,
                               frame_index=frame_index, accumulate=int(accumulate),
                               wave_paths=wave_paths, count_work=int(count_work),
                               write_gbuffer=int(write_gbuffer), use_cache=int(use_cache),
-                              profile_stages=int(profile_stages))
+                              profile_stages=int(profile_stages), texture_filter=int(texture_filter))
         if out is None:
             out = np.empty((height, width, 4), np.float32)
         st = KgkStats()
@@ -141,6 +141,18 @@ class Scene:
                                ctypes.byref(prev_cam) if prev_cam is not None else None,
                                ctypes.byref(cfg), _p(out), ctypes.byref(st)))
         return out, stats_dict(st)
+
+    def set_textures_rgba8(self, textures):
+        """Replaces the scene's textures with RGBA8 ones: (height, width, 4) uint8 arrays."""
+        arr = (KgkTextureRGBA8 * max(len(textures), 1))()
+        keep = []
+        for i, t in enumerate(textures):
+            t = np.ascontiguousarray(t, np.uint8)
+            assert t.ndim == 3 and t.shape[2] == 4
+            keep.append(t)
+            arr[i].pixels = t.ctypes.data
+            arr[i].height, arr[i].width = t.shape[:2]
+        check(lib().kgk_scene_set_textures_rgba8(self._h, ctypes.cast(arr, ctypes.c_void_p), len(textures)))
 
     def cache_init(self, **cfg):
         """(Re)initialises the learned radiance cache used by

@@ -160,6 +160,12 @@ kgk_status kgk_scene_create(const kgk_triangle *tris, size_t n_tris, const kgk_m
     KGK_GUARD_END
 }
 
+kgk_status kgk_scene_set_textures_rgba8(kgk_scene *s, const kgk_texture_rgba8 *textures, size_t n) {
+    if (!s) return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_scene_set_textures_rgba8: scene == NULL");
+    KGK_CUDA(cudaSetDevice(s->device));
+    return scene_set_textures_rgba8(s->dev, textures, n, s->stream);
+}
+
 void kgk_scene_destroy(kgk_scene *s) {
     if (!s) return;
     cudaSetDevice(s->device);

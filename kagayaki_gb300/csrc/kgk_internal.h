@@ -54,8 +54,8 @@ struct __align__(16) BinNode {
 };
 
 struct TexDesc {
-    int64_t offset;  // into the concatenated float pixel buffer
-    int32_t w, h, bpp, pad;
+    int64_t offset;  // float textures: floats into tex_pixels; RGBA8: texels into tex_rgba8
+    int32_t w, h, bpp, rgba8;
 };
 
 // Device-resident scene.
@@ -71,16 +71,21 @@ struct DevScene {
     float4 *verts = nullptr;
     float4 *attr = nullptr;
     kgk_material *mats = nullptr;
-    // Textures (float pixels, reference layout).
+    // Textures: float pixels (reference layout) or RGBA8 texels decoded
+    // through tex_lut (256 entries: (v/255)^2.2 + 1e-4, the reference loader's
+    // value for an 8-bit channel).
     float *tex_pixels = nullptr;
+    uchar4 *tex_rgba8 = nullptr;
+    float *tex_lut = nullptr;
     TexDesc *tex = nullptr;
     int32_t n_tex = 0;
+    int32_t tex_filter = 0;  // per render call: 0 nearest (Texture::get_Color), 1 bilinear
     // Environment (nullptr: none -> background (1,1,1)).
     float *env = nullptr;
     int32_t env_w = 0, env_h = 0, env_bpp = 0;
     float *env_cdf_ref = nullptr;    // reference running FP32 sum over w*h texels
-    float *env_row_cdf = nullptr;    // unbiased: marginal CDF over rows (h+1)
-    float *env_col_cdf = nullptr;    // unbiased: conditional CDFs ((w+1) per row)
+    float2 *env_alias = nullptr;     // unbiased: alias table over w*h texels (threshold, alias index bits)
+    float *env_prob = nullptr;       // unbiased: probability of each texel
     float env_total = 0.0f;          // sum of the unbiased weights
     // Face lights.
     float *light_cdf_ref = nullptr;  // reference running FP32 sum over all triangles
@@ -132,6 +137,7 @@ struct BvhBuildStats {
     double sah = 0, ms = 0;
 };
 
+kgk_status scene_set_textures_rgba8(DevScene &s, const kgk_texture_rgba8 *tex, size_t n, cudaStream_t st);
 kgk_status scene_upload(DevScene &s, const kgk_triangle *tris, size_t n, const kgk_material *mats,
                         size_t nm, const kgk_texture *tex, size_t ntex, const kgk_texture *hdr,
                         cudaStream_t st);

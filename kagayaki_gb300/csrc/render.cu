@@ -538,18 +538,27 @@ __device__ void shade_compat(const Params &P, int p, bool valid, int *next_q, in
 // ---------------------------------------------------------------------------
 // unbiased shade
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void bsdf_eval_pdf(const Surface &S, const DisneyParams &dp, float3 n, float3 wo,
-                                              float3 wi, float3 &f, float &pdf) {
-    if (S.m.MATERIAL_TYPE_ID == 1) {
+// Not inlined: the unbiased shader evaluates the BSDF at three call sites
+// (face-light NEE, environment NEE, BSDF sample); one copy of the Disney
+// code keeps the kernel inside the instruction cache.  The material is read
+// from its global record (diffuse passed in: it may come from a texture);
+// returns (f, pdf).
+__device__ __noinline__ float4 bsdf_eval_pdf(const kgk_material *__restrict__ mg, float3 diffuse, float3 n,
+                                             float3 wo, float3 wi) {
+    if (mg->MATERIAL_TYPE_ID == 1) {
+        kgk_material m = *mg;
+        m.diffuse.x = diffuse.x;
+        m.diffuse.y = diffuse.y;
+        m.diffuse.z = diffuse.z;
+        const DisneyParams dp = disney_params(m);
         float3 u, v, w;
         onb_ref(n, u, v, w);
-        f = disney_eval<false>(S.m, dp, wi, wo, n, u, v, w);
-        pdf = disney_pdf_unbiased(dp, wo, wi, n, u, v, w);
-    } else {
-        const float c = dot3(n, wi);
-        f = c > 0.0f ? diffuse_of(S.m) / kPI : f3(0.0f, 0.0f, 0.0f);
-        pdf = fmaxf(c, 0.0f) / kPI;
+        const float3 f = disney_eval<false>(m, dp, wi, wo, n, u, v, w);
+        return make_float4(f.x, f.y, f.z, disney_pdf_unbiased(dp, wo, wi, n, u, v, w));
     }
+    const float c = dot3(n, wi);
+    const float3 f = c > 0.0f ? diffuse / kPI : f3(0.0f, 0.0f, 0.0f);
+    return make_float4(f.x, f.y, f.z, fmaxf(c, 0.0f) / kPI);
 }
 
 // Writes a cache record for the surface point of a path: normalised position,
@@ -682,9 +691,9 @@ __device__ void shade_unbiased(const Params &P, int p, bool valid, int *next_q, 
                         const float3 Le = emission_of(s.mats[lb & 0x7fffffffu]);
                         const float parea = len3(Le) / s.emit_total;
                         const float pl = parea * dist * dist / cosl;
-                        float3 f;
-                        float pb;
-                        bsdf_eval_pdf(S, dp, n, wo, Ld, f, pb);
+                        const float4 fp = bsdf_eval_pdf(&s.mats[S.mat_id], diffuse_of(S.m), n, wo, Ld);
+                        const float3 f = f3(fp);
+                        const float pb = fp.w;
                         const float wgt = pl / (pl + pb);
                         f_c = T * f * Le * (coss * wgt / pl);
                         f_pred = f_c.x > 0.0f || f_c.y > 0.0f || f_c.z > 0.0f;
@@ -694,15 +703,14 @@ __device__ void shade_unbiased(const Params &P, int p, bool valid, int *next_q, 
                 }
                 // NEE: one environment sample
                 if (s.env) {
-                    const float r0 = rnd_u(rs), r1 = rnd_u(rs), r2 = rnd_u(rs), r3 = rnd_u(rs);
                     float pe;
                     float3 Le;
-                    const float3 ed = env_sample_u(s, r0, r1, r2, r3, pe, Le);
+                    const float3 ed = env_sample_u(s, rs, pe, Le);
                     const float coss = dot3(n, ed);
                     if (coss > 0.0f && pe > 0.0f) {
-                        float3 f;
-                        float pb;
-                        bsdf_eval_pdf(S, dp, n, wo, ed, f, pb);
+                        const float4 fp = bsdf_eval_pdf(&s.mats[S.mat_id], diffuse_of(S.m), n, wo, ed);
+                        const float3 f = f3(fp);
+                        const float pb = fp.w;
                         const float wgt = pe / (pe + pb);
                         e_c = T * f * Le * (coss * wgt / pe);
                         e_pred = e_c.x > 0.0f || e_c.y > 0.0f || e_c.z > 0.0f;
@@ -714,8 +722,6 @@ __device__ void shade_unbiased(const Params &P, int p, bool valid, int *next_q, 
                     float3 u, v, w;
                     onb_ref(n, u, v, w);
                     float3 nd;
-                    float3 f;
-                    float pb;
                     if (S.m.MATERIAL_TYPE_ID == 1) {
                         const float sw = dp.wt[0] + dp.wt[1] + dp.wt[2] + dp.wt[3] + dp.wt[4];
                         const float rl = rnd_u(rs) * sw, r1 = rnd_u(rs), r2 = rnd_u(rs);
@@ -725,12 +731,13 @@ __device__ void shade_unbiased(const Params &P, int p, bool valid, int *next_q, 
                             nd = reflect_ref(d, gtr2_half(fminf(r1, 0.99999f), fminf(r2, 0.99999f), u, v, w, dp.ax, dp.ay));
                         else
                             nd = reflect_ref(d, gtr1_half(r1, r2, u, v, w, dp.ac, true));
-                        bsdf_eval_pdf(S, dp, n, wo, nd, f, pb);
                     } else {
                         const float r1 = rnd_u(rs), r2 = rnd_u(rs);
                         nd = sample_cos_u(r1, r2, u, v, w);
-                        bsdf_eval_pdf(S, dp, n, wo, nd, f, pb);
                     }
+                    const float4 fp = bsdf_eval_pdf(&s.mats[S.mat_id], diffuse_of(S.m), n, wo, nd);
+                    const float3 f = f3(fp);
+                    const float pb = fp.w;
                     const float c = dot3(n, nd);
                     if (pb > 0.0f && c > 0.0f) {
                         T = T * f * (c / pb);
@@ -1029,6 +1036,7 @@ kgk_status kgk_render(kgk_scene *s, const kgk_camera *cam, const kgk_camera *pre
     Params P;
     memset(&P, 0, sizeof P);
     P.sc = s->dev;
+    P.sc.tex_filter = cfg->texture_filter == 1 ? 1 : 0;
     P.cam = *cam;
     P.W = W;
     P.H = H;

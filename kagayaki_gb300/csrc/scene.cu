@@ -17,6 +17,12 @@
 namespace kgk {
 namespace {
 
+inline float int_bits_as_float(int i) {
+    float f;
+    memcpy(&f, &i, sizeof f);
+    return f;
+}
+
 struct HV {
     float x, y, z;
 };
@@ -198,40 +204,92 @@ kgk_status scene_upload(DevScene &s, const kgk_triangle *tris_in, size_t n, cons
             cdf[i] = cdf[i - 1] + hlen({px[bpp * i], px[bpp * i + 1], px[bpp * i + 2]}) * cosf((v - 0.5f) * PIH);
         }
         KGK_TRY(upload(&s.env_cdf_ref, cdf.data(), npx, "environment CDF", st));
-        // unbiased: texel weight = |rgb| * cos(latitude of the row centre)
-        std::vector<double> roww(h, 0.0);
-        std::vector<float> col((size_t)(w + 1) * h);
-        std::vector<float> row(h + 1);
+        // unbiased: texel weight = |rgb| * cos(latitude of the row centre),
+        // sampled in O(1) through an alias table (Vose's construction)
+        std::vector<double> q(npx);
         double total = 0.0;
         for (int r = 0; r < h; ++r) {
-            const double lat = (0.5 - (r + 0.5) / h) * M_PI;
-            const double c = cos(lat);
-            double acc = 0.0;
-            col[(size_t)r * (w + 1)] = 0.0f;
-            std::vector<double> tmp(w);
+            const double c = cos((0.5 - (r + 0.5) / h) * M_PI);
             for (int x = 0; x < w; ++x) {
                 const float *p = &px[((size_t)r * w + x) * bpp];
-                double l = sqrt((double)p[0] * p[0] + (double)p[1] * p[1] + (double)p[2] * p[2]);
-                acc += l * c + 1e-30;
-                tmp[x] = acc;
+                const double l = sqrt((double)p[0] * p[0] + (double)p[1] * p[1] + (double)p[2] * p[2]);
+                q[(size_t)r * w + x] = l * c + 1e-30;
+                total += q[(size_t)r * w + x];
             }
-            for (int x = 0; x < w; ++x) col[(size_t)r * (w + 1) + x + 1] = (float)(tmp[x] / acc);
-            col[(size_t)r * (w + 1) + w] = 1.0f;
-            roww[r] = acc;
-            total += acc;
         }
-        double acc = 0.0;
-        row[0] = 0.0f;
-        for (int r = 0; r < h; ++r) {
-            acc += roww[r];
-            row[r + 1] = (float)(acc / total);
+        std::vector<float> prob(npx);
+        std::vector<float2> alias(npx);
+        std::vector<size_t> small, large;
+        for (size_t i = 0; i < npx; ++i) {
+            prob[i] = (float)(q[i] / total);
+            q[i] = q[i] / total * (double)npx;  // scaled: mean 1
+            (q[i] < 1.0 ? small : large).push_back(i);
         }
-        row[h] = 1.0f;
+        while (!small.empty() && !large.empty()) {
+            const size_t a = small.back(), l = large.back();
+            small.pop_back();
+            alias[a] = make_float2((float)q[a], int_bits_as_float((int)l));
+            q[l] = (q[l] + q[a]) - 1.0;
+            if (q[l] < 1.0) {
+                large.pop_back();
+                small.push_back(l);
+            }
+        }
+        for (size_t i : large) alias[i] = make_float2(1.0f, int_bits_as_float((int)i));
+        for (size_t i : small) alias[i] = make_float2(1.0f, int_bits_as_float((int)i));  // rounding leftovers
         s.env_total = (float)total;
-        KGK_TRY(upload(&s.env_row_cdf, row.data(), row.size(), "environment row CDF", st));
-        KGK_TRY(upload(&s.env_col_cdf, col.data(), col.size(), "environment column CDF", st));
+        KGK_TRY(upload(&s.env_alias, alias.data(), alias.size(), "environment alias table", st));
+        KGK_TRY(upload(&s.env_prob, prob.data(), prob.size(), "environment texel probabilities", st));
         KGK_CUDA(cudaStreamSynchronize(st));
     }
+    return KGK_OK;
+}
+
+kgk_status scene_set_textures_rgba8(DevScene &s, const kgk_texture_rgba8 *tex, size_t n, cudaStream_t st) {
+    if (n > 0 && !tex) return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_scene_set_textures_rgba8: textures == NULL");
+    std::vector<TexDesc> desc(n);
+    size_t total = 0;
+    for (size_t i = 0; i < n; ++i) {
+        if (!tex[i].pixels || tex[i].width <= 0 || tex[i].height <= 0)
+            return fail(KGK_ERR_INVALID_ARGUMENT,
+                        "kgk_scene_set_textures_rgba8: texture " + std::to_string(i) + " needs pixels and a size");
+        desc[i].offset = (int64_t)total;
+        desc[i].w = tex[i].width;
+        desc[i].h = tex[i].height;
+        desc[i].bpp = 4;
+        desc[i].rgba8 = 1;
+        total += (size_t)tex[i].width * tex[i].height;
+    }
+    // materials may only name textures that exist
+    std::vector<kgk_material> mats(s.n_mats);
+    KGK_CUDA(cudaMemcpy(mats.data(), s.mats, mats.size() * sizeof(kgk_material), cudaMemcpyDeviceToHost));
+    for (const kgk_material &m : mats)
+        if (m.TEXTURE_BASECOLOR_ID >= (int)n)
+            return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_scene_set_textures_rgba8: a material names texture " +
+                                                      std::to_string(m.TEXTURE_BASECOLOR_ID) + " of " +
+                                                      std::to_string(n));
+    dfree(s.tex_pixels);
+    dfree(s.tex_rgba8);
+    dfree(s.tex);
+    s.tex_pixels = nullptr;
+    s.tex_rgba8 = nullptr;
+    s.tex = nullptr;
+    s.n_tex = 0;
+    if (n == 0) return KGK_OK;
+    KGK_TRY(dalloc(&s.tex_rgba8, total, "RGBA8 texels"));
+    for (size_t i = 0; i < n; ++i) {
+        const size_t cnt = (size_t)tex[i].width * tex[i].height;
+        KGK_CUDA(cudaMemcpy(s.tex_rgba8 + desc[i].offset, tex[i].pixels, cnt * 4,
+                            is_device_ptr(tex[i].pixels) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice));
+    }
+    if (!s.tex_lut) {
+        float lut[256];
+        for (int v = 0; v < 256; ++v) lut[v] = (float)((double)powf(v / 255.0f, 2.2f) + 1e-4);
+        KGK_TRY(upload(&s.tex_lut, lut, 256, "texture decode table", st));
+    }
+    KGK_TRY(upload(&s.tex, desc.data(), n, "texture table", st));
+    s.n_tex = (int32_t)n;
+    KGK_CUDA(cudaStreamSynchronize(st));
     return KGK_OK;
 }
 
@@ -241,11 +299,13 @@ void scene_free(DevScene &s) {
     dfree(s.attr);
     dfree(s.mats);
     dfree(s.tex_pixels);
+    dfree(s.tex_rgba8);
+    dfree(s.tex_lut);
     dfree(s.tex);
     dfree(s.env);
     dfree(s.env_cdf_ref);
-    dfree(s.env_row_cdf);
-    dfree(s.env_col_cdf);
+    dfree(s.env_alias);
+    dfree(s.env_prob);
     dfree(s.light_cdf_ref);
     dfree(s.emit_ids);
     dfree(s.emit_cdf);

@@ -338,10 +338,7 @@ __device__ __forceinline__ void env_dir_to_texel(const DevScene &s, float3 d, in
 }
 
 __device__ __forceinline__ float env_texel_weight(const DevScene &s, int row, int col) {
-    const float cdf0 = col == 0 ? 0.0f : __ldg(&s.env_col_cdf[(size_t)row * (s.env_w + 1) + col]);
-    const float cdf1 = __ldg(&s.env_col_cdf[(size_t)row * (s.env_w + 1) + col + 1]);
-    const float r0 = __ldg(&s.env_row_cdf[row]), r1 = __ldg(&s.env_row_cdf[row + 1]);
-    return (cdf1 - cdf0) * (r1 - r0);  // probability of the texel
+    return __ldg(&s.env_prob[(size_t)row * s.env_w + col]);  // probability of the texel
 }
 
 // Solid-angle pdf of direction d under env importance sampling: the texel's
@@ -365,10 +362,16 @@ __device__ __forceinline__ float3 env_lookup_u(const DevScene &s, float3 d) {
 // Samples a direction; returns it with its solid-angle pdf and radiance.
 // Inside the texel the direction is uniform in (longitude, latitude), so its
 // solid-angle density carries 1 / cos(latitude) of the sampled direction.
-__device__ __forceinline__ float3 env_sample_u(const DevScene &s, float r0, float r1, float r2, float r3,
-                                               float &pdf, float3 &Le) {
-    const int row = cdf_search(s.env_row_cdf, s.env_h, r0);
-    const int col = cdf_search(s.env_col_cdf + (size_t)row * (s.env_w + 1), s.env_w, r1);
+// The texel comes from the alias table: a uniform index (from 64 random
+// bits, so every index is equally likely to within 2^-40) and one coin.
+__device__ __forceinline__ float3 env_sample_u(const DevScene &s, unsigned long long &rs, float &pdf, float3 &Le) {
+    const unsigned long long n = (unsigned long long)s.env_w * (unsigned long long)s.env_h;
+    rs = xorshift64(rs);
+    int t = (int)__umul64hi(rs, n);
+    const float coin = rnd_u(rs), r2 = rnd_u(rs), r3 = rnd_u(rs);
+    const float2 e = __ldg(&s.env_alias[t]);
+    if (coin >= e.x) t = __float_as_int(e.y);
+    const int row = t / s.env_w, col = t - row * s.env_w;
     const float v = 1.0f - (row + r2) / s.env_h;
     const float u = 1.0f - (col + r3) / s.env_w;
     const float phi = (v - 0.5f) * kPI, theta = (u - 0.5f) * 2.0f * kPI;
@@ -381,15 +384,37 @@ __device__ __forceinline__ float3 env_sample_u(const DevScene &s, float r0, floa
 }
 
 // ---------------------------------------------------------------------------
-// Textures: nearest fetch (Texture::get_Color, struct_Texture.cuh:12-18);
-// the row index is clamped where the reference reads past the end (v = 0).
+// Textures: nearest fetch (Texture::get_Color, struct_Texture.cuh:12-18;
+// the index is clamped where the reference reads past the end, v = 0) or
+// bilinear; float or RGBA8 texels.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ float3 tex_fetch(const DevScene &s, int tex, float u, float v) {
-    const TexDesc td = s.tex[tex];
-    int idx = td.w * (int)((float)td.h * (1.0f - v)) + (int)((float)td.w * u);
-    idx = min(max(idx, 0), td.w * td.h - 1);
+__device__ __forceinline__ float3 tex_texel(const DevScene &s, const TexDesc &td, int idx) {
+    if (td.rgba8) {
+        const uchar4 b = __ldg(&s.tex_rgba8[td.offset + idx]);
+        return f3(__ldg(&s.tex_lut[b.x]), __ldg(&s.tex_lut[b.y]), __ldg(&s.tex_lut[b.z]));
+    }
     const float *p = s.tex_pixels + td.offset + (size_t)idx * td.bpp;
     return f3(__ldg(p), __ldg(p + 1), __ldg(p + 2));
+}
+
+__device__ __forceinline__ float3 tex_fetch(const DevScene &s, int tex, float u, float v) {
+    const TexDesc td = s.tex[tex];
+    if (s.tex_filter == 1) {
+        // bilinear, texel centres at (i + 0.5) / w, wrap-around addressing
+        const float x = u * td.w - 0.5f, y = (1.0f - v) * td.h - 0.5f;
+        const float fx = floorf(x), fy = floorf(y);
+        const float ax = x - fx, ay = y - fy;
+        int x0 = (int)fx % td.w, y0 = (int)fy % td.h;
+        if (x0 < 0) x0 += td.w;
+        if (y0 < 0) y0 += td.h;
+        const int x1 = x0 + 1 == td.w ? 0 : x0 + 1, y1 = y0 + 1 == td.h ? 0 : y0 + 1;
+        const float3 c00 = tex_texel(s, td, y0 * td.w + x0), c10 = tex_texel(s, td, y0 * td.w + x1);
+        const float3 c01 = tex_texel(s, td, y1 * td.w + x0), c11 = tex_texel(s, td, y1 * td.w + x1);
+        return (c00 * (1.0f - ax) + c10 * ax) * (1.0f - ay) + (c01 * (1.0f - ax) + c11 * ax) * ay;
+    }
+    int idx = td.w * (int)((float)td.h * (1.0f - v)) + (int)((float)td.w * u);
+    idx = min(max(idx, 0), td.w * td.h - 1);
+    return tex_texel(s, td, idx);
 }
 
 }  // namespace kgk

@@ -110,6 +110,12 @@ __device__ __forceinline__ void ref_distance(const RayPre &r, float4 a4, float4 
 }
 
 __device__ __forceinline__ unsigned byte_of(unsigned x, int i) { return (x >> (i * 8)) & 0xffu; }
+// Byte i of x as a float, exactly: one byte permute builds the bits of
+// 2^23 + byte, one subtraction removes 2^23 (no integer-to-float conversion).
+__device__ __forceinline__ float byte_as_float(unsigned x, int i) {
+    const unsigned bits = __byte_perm(x, 0x4Bu, (unsigned)i | 0x4550u);
+    return __uint_as_float(bits) - 8388608.0f;
+}
 __device__ __forceinline__ unsigned sign_extend_s8x4(unsigned x) { return ((x >> 7) & 0x01010101u) * 0xffu; }
 
 // Child hit mask of one compressed node: bits 24..31 = inner children
@@ -141,12 +147,12 @@ __device__ __forceinline__ unsigned node_intersect(const RayPre &r, float tmin, 
         const unsigned zn = r.d.z < 0.0f ? qhz : qlz, zf = r.d.z < 0.0f ? qlz : qhz;
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
-            const float t0x = (float)byte_of(xn, j) * adx + ox;
-            const float t0y = (float)byte_of(yn, j) * ady + oy;
-            const float t0z = (float)byte_of(zn, j) * adz + oz;
-            const float t1x = (float)byte_of(xf, j) * adx + ox;
-            const float t1y = (float)byte_of(yf, j) * ady + oy;
-            const float t1z = (float)byte_of(zf, j) * adz + oz;
+            const float t0x = byte_as_float(xn, j) * adx + ox;
+            const float t0y = byte_as_float(yn, j) * ady + oy;
+            const float t0z = byte_as_float(zn, j) * adz + oz;
+            const float t1x = byte_as_float(xf, j) * adx + ox;
+            const float t1y = byte_as_float(yf, j) * ady + oy;
+            const float t1z = byte_as_float(zf, j) * adz + oz;
             const float lo = fmaxf(fmaxf(t0x, t0y), fmaxf(t0z, tmin));
             const float hi = fminf(fminf(t1x, t1y), fminf(t1z, tm)) * kBoxWiden;
             if (lo <= hi) hits |= byte_of(child_bits4, j) << byte_of(bit_index4, j);

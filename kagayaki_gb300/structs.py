@@ -65,7 +65,11 @@ class KgkRenderConfig(ctypes.Structure):
                 ("accumulate", ctypes.c_int32), ("wave_paths", ctypes.c_int32),
                 ("count_work", ctypes.c_int32), ("write_gbuffer", ctypes.c_int32),
                 ("use_cache", ctypes.c_int32), ("profile_stages", ctypes.c_int32),
-                ("reserved", ctypes.c_int32 * 5)]
+                ("texture_filter", ctypes.c_int32), ("reserved", ctypes.c_int32 * 4)]
+
+
+class KgkTextureRGBA8(ctypes.Structure):
+    _fields_ = [("pixels", ctypes.c_void_p), ("width", ctypes.c_int32), ("height", ctypes.c_int32)]
 
 
 class KgkStats(ctypes.Structure):
