@@ -22,7 +22,8 @@ struct NrcState {
     float *w = nullptr, *m = nullptr, *v = nullptr, *g = nullptr;  // FP32 master weights, Adam, gradient
     unsigned short *img = nullptr;   // BF16 weight image (shared-memory layout)
     float *scal = nullptr;           // [0] loss scale, [1] last loss
-    int *ints = nullptr;             // [0] non-finite flag, [1] clean steps since the last scale change
+    int *ints = nullptr;             // [0] non-finite flag, [1] clean steps since the last scale change,
+                                     // [2] inference timeout flag
     int step = 0;
     int sms = 0;
     bool ready = false;
@@ -35,6 +36,9 @@ void nrc_free(NrcState &N);
 // floats 13..15 and the path id (int bits) at float 16 of each record.
 kgk_status nrc_infer_dev(NrcState &N, const float *raw, int stride, int n, const int *n_dev, float *out, float4 *rad,
                          cudaStream_t st);
+// KGK_ERR_DEVICE_CHECK (and clears the flag) when an inference kernel gave up
+// a bounded wait; synchronous.
+kgk_status nrc_check_error(NrcState &N);
 // Gradient of the mean relative-L2 loss (times the loss scale) into N.g.
 kgk_status nrc_grad_dev(NrcState &N, const float *raw, int raw_stride, const float *tgt, int tgt_stride, int n,
                         const int *n_dev, cudaStream_t st);

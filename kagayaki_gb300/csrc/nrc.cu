@@ -191,6 +191,241 @@ __global__ void __launch_bounds__(256) k_infer(const unsigned short *__restrict_
 }
 
 // ---------------------------------------------------------------------------
+// inference on the 5th-generation tensor cores (tcgen05 + TMEM)
+//
+// One CTA of 128 threads carries tiles of 128 queries through the network:
+// thread r owns row r.  Per layer the CTA writes the BF16 activations
+// (128 x 64) to shared memory in the 128-byte-swizzled K-major layout, one
+// elected thread issues four tcgen05.mma (M=128, N=64, K=16 each) against the
+// layer's weights (64 x 64, same layout, resident in shared memory) into a
+// 128 x 64 FP32 accumulator in tensor memory, and commits to an mbarrier; the
+// threads then read their row back from tensor memory (tcgen05.ld 32x32b),
+// apply the ReLU and round to BF16 for the next layer.  The output layer uses
+// N=16 (3 live rows of the padded weights).
+// Every wait is bounded: on a timeout the CTA raises *err, stops issuing and
+// frees its tensor memory.
+// ---------------------------------------------------------------------------
+namespace tc {
+
+constexpr int kRows = 128;                       // M of every MMA, queries per tile
+constexpr uint32_t kLayerBytes = 64 * 128;       // 64 rows x 128 B (64 BF16)
+constexpr uint32_t kOutBytes = 16 * 128;         // padded output layer
+constexpr uint32_t kWOff = 0;                    // hidden layers at l * kLayerBytes
+constexpr uint32_t kOutOff = kLayers * kLayerBytes;
+constexpr uint32_t kAOff = kOutOff + kOutBytes;  // activation tile, 16 KB (1024-aligned)
+constexpr uint32_t kBarOff = kAOff + kRows * 128;
+constexpr uint32_t kSlotOff = kBarOff + 8;
+constexpr uint32_t kSmemBytes = kSlotOff + 8 + 1024;  // + room to align the base to 1024 B
+constexpr uint32_t kTmemCols = 64;
+static_assert(kAOff % 1024 == 0, "swizzle atoms need 1024-byte alignment");
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// Shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row atoms
+// 1024 B apart (stride byte offset), descriptor version 1.
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
+    return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)1u << 16) | ((uint64_t)(1024u >> 4) << 32) |
+           ((uint64_t)1u << 46) | ((uint64_t)2u << 61);
+}
+
+// Instruction descriptor, kind::f16: BF16 A and B (K-major), FP32 D, M x N.
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem_d),
+        "l"(a), "l"(b), "r"(idesc), "r"(acc));
+}
+
+__device__ __forceinline__ void commit(uint32_t bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool bar_try(uint32_t bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Waits for the barrier phase; false after ~1 s (2^31 SM cycles).
+__device__ __forceinline__ bool bar_wait(uint32_t bar, uint32_t parity) {
+    const long long t0 = clock64();
+    while (!bar_try(bar, parity))
+        if (clock64() - t0 > (1ll << 31)) return false;
+    return true;
+}
+
+__device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// 16 consecutive FP32 columns of this thread's TMEM lane.
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+// Row r of a 128B-swizzled K-major tile: 16-byte chunk c of the row.
+__device__ __forceinline__ uint32_t sw_off(int r, int c) { return (uint32_t)r * 128u + ((uint32_t)(c ^ (r & 7)) << 4); }
+
+}  // namespace tc
+
+__global__ void __launch_bounds__(128) k_infer_tc(const unsigned short *__restrict__ img, const float *__restrict__ raw,
+                                                  int stride_floats, int n, const int *n_dev, float *out, float4 *rad,
+                                                  int *err) {
+    using namespace tc;
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    const uint32_t pad = (1024u - (smem_u32(smem_raw) & 1023u)) & 1023u;
+    unsigned char *sm = smem_raw + pad;
+    const uint32_t s0 = smem_u32(sm);
+    const int tid = threadIdx.x, warp = tid >> 5;
+    // weights: BF16 image rows (pitch kPitch) -> swizzled K-major tiles
+    for (int i = tid; i < (kLayers * 64 + 16) * 8; i += blockDim.x) {
+        const int row = i >> 3, c = i & 7;  // row over all layers (64 per hidden layer, then 16)
+        const uint4 v = *reinterpret_cast<const uint4 *>(img + (size_t)row * kPitch + c * 8);
+        uint32_t dst;
+        if (row < kLayers * 64) dst = kWOff + (uint32_t)(row >> 6) * kLayerBytes + sw_off(row & 63, c);
+        else dst = kOutOff + sw_off(row - kLayers * 64, c);
+        *reinterpret_cast<uint4 *>(sm + dst) = v;
+    }
+    const uint32_t bar = s0 + kBarOff;
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(s0 + kSlotOff),
+                     "r"(kTmemCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    fence_async_smem();
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tmem = *reinterpret_cast<volatile uint32_t *>(sm + kSlotOff);
+    const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);  // this warp's 32 TMEM lanes
+    const int total = n_dev ? min(*n_dev, n) : n;
+    uint32_t phase = 0;
+    bool failed = false;
+    unsigned char *A = sm + kAOff;
+    for (int tile = blockIdx.x; tile * kRows < total; tile += gridDim.x) {
+        const int q = tile * kRows + tid;
+        const bool live = q < total;
+        // input encoding of row tid
+        {
+            float rw[kRaw];
+#pragma unroll
+            for (int k = 0; k < kRaw; ++k) rw[k] = live ? raw[(size_t)q * stride_floats + k] : 0.0f;
+#pragma unroll
+            for (int c = 0; c < 8; ++c) {
+                uint4 v;
+                v.x = pack2(encode_col(rw, 8 * c + 0), encode_col(rw, 8 * c + 1));
+                v.y = pack2(encode_col(rw, 8 * c + 2), encode_col(rw, 8 * c + 3));
+                v.z = pack2(encode_col(rw, 8 * c + 4), encode_col(rw, 8 * c + 5));
+                v.w = pack2(encode_col(rw, 8 * c + 6), encode_col(rw, 8 * c + 7));
+                *reinterpret_cast<uint4 *>(A + sw_off(tid, c)) = v;
+            }
+        }
+        float y[3] = {0.0f, 0.0f, 0.0f};
+        for (int l = 0; l <= kLayers; ++l) {
+            const bool last = l == kLayers;
+            fence_async_smem();
+            fence_before();
+            __syncthreads();
+            if (tid == 0) {
+                fence_after();
+                const uint64_t ad = sw128_desc(s0 + kAOff);
+                const uint64_t bd = sw128_desc(s0 + (last ? kOutOff : kWOff + (uint32_t)l * kLayerBytes));
+                const uint32_t id = last ? idesc_bf16(128, 16) : idesc_bf16(128, 64);
+#pragma unroll
+                for (int kk = 0; kk < 4; ++kk) mma_bf16(tmem, ad + 2 * kk, bd + 2 * kk, id, kk > 0 ? 1u : 0u);
+                commit(bar);
+            }
+            const bool ok = bar_wait(bar, phase);
+            phase ^= 1u;
+            if (__syncthreads_or(!ok)) {
+                failed = true;
+                break;
+            }
+            fence_after();
+            if (!last) {
+#pragma unroll
+                for (int cb = 0; cb < 4; ++cb) {  // 16 columns = two 16-byte chunks of BF16
+                    float v[16];
+                    tmem_ld16(trow + 16 * cb, v);
+                    tmem_wait_ld();
+                    uint4 lo, hi;
+                    lo.x = pack2(fmaxf(v[0], 0.0f), fmaxf(v[1], 0.0f));
+                    lo.y = pack2(fmaxf(v[2], 0.0f), fmaxf(v[3], 0.0f));
+                    lo.z = pack2(fmaxf(v[4], 0.0f), fmaxf(v[5], 0.0f));
+                    lo.w = pack2(fmaxf(v[6], 0.0f), fmaxf(v[7], 0.0f));
+                    hi.x = pack2(fmaxf(v[8], 0.0f), fmaxf(v[9], 0.0f));
+                    hi.y = pack2(fmaxf(v[10], 0.0f), fmaxf(v[11], 0.0f));
+                    hi.z = pack2(fmaxf(v[12], 0.0f), fmaxf(v[13], 0.0f));
+                    hi.w = pack2(fmaxf(v[14], 0.0f), fmaxf(v[15], 0.0f));
+                    *reinterpret_cast<uint4 *>(A + sw_off(tid, 2 * cb)) = lo;
+                    *reinterpret_cast<uint4 *>(A + sw_off(tid, 2 * cb + 1)) = hi;
+                }
+            } else {
+                float v[16];
+                tmem_ld16(trow, v);
+                tmem_wait_ld();
+                y[0] = v[0];
+                y[1] = v[1];
+                y[2] = v[2];
+            }
+        }
+        if (failed) break;
+        if (live) {
+            if (out) {
+                out[(size_t)q * 3 + 0] = y[0];
+                out[(size_t)q * 3 + 1] = y[1];
+                out[(size_t)q * 3 + 2] = y[2];
+            }
+            if (rad) {
+                // cache termination: rad[path] += T * max(y, 0)
+                const float *rec = raw + (size_t)q * stride_floats;
+                const int path = __float_as_int(rec[16]);
+                float4 r = rad[path];
+                r.x += rec[13] * fmaxf(y[0], 0.0f);
+                r.y += rec[14] * fmaxf(y[1], 0.0f);
+                r.z += rec[15] * fmaxf(y[2], 0.0f);
+                rad[path] = r;
+            }
+        }
+    }
+    if (failed) {
+        // the MMAs of the timed-out phase may still be in flight: wait once
+        // more (bounded) before the tensor memory is released
+        bar_wait(bar, phase ^ 1u);
+        if (tid == 0) atomicExch(err, 1);
+    }
+    fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
+    }
+}
+
+// ---------------------------------------------------------------------------
 // training: forward + loss + backward + dW
 // ---------------------------------------------------------------------------
 struct TrainSmem {
@@ -487,7 +722,7 @@ kgk_status nrc_init(NrcState &N, const kgk_nrc_config *cfg, int device) {
     KGK_CUDA(cudaGetLastError());
     KGK_CUDA(cudaDeviceSynchronize());
     KGK_CUDA(cudaFuncSetAttribute(k_train, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TrainSmem::total(4)));
-    KGK_CUDA(cudaFuncSetAttribute(k_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, kImgElems * 2));
+    KGK_CUDA(cudaFuncSetAttribute(k_infer_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc::kSmemBytes));
     cudaDeviceProp p;
     KGK_CUDA(cudaGetDeviceProperties(&p, device));
     N.sms = p.multiProcessorCount;
@@ -505,10 +740,20 @@ void nrc_free(NrcState &N) {
     N.ready = false;
 }
 
+kgk_status nrc_check_error(NrcState &N) {
+    int e = 0;
+    KGK_CUDA(cudaMemcpy(&e, N.ints + 2, sizeof(int), cudaMemcpyDeviceToHost));
+    if (e) {
+        KGK_CUDA(cudaMemset(N.ints + 2, 0, sizeof(int)));
+        return fail(KGK_ERR_DEVICE_CHECK, "radiance cache: a tensor-core wait timed out (inference abandoned)");
+    }
+    return KGK_OK;
+}
+
 kgk_status nrc_infer_dev(NrcState &N, const float *raw, int stride, int n, const int *n_dev, float *out, float4 *rad,
                          cudaStream_t st) {
-    const int grid = N.sms * 4;
-    k_infer<<<grid, 256, kImgElems * 2, st>>>(N.img, raw, stride, n, n_dev, out, rad);
+    const int grid = N.sms * 3;  // three ~60 KB CTAs fit an SM; 3 x 64 TMEM columns of 512
+    k_infer_tc<<<grid, 128, tc::kSmemBytes, st>>>(N.img, raw, stride, n, n_dev, out, rad, N.ints + 2);
     KGK_CUDA(cudaGetLastError());
     return KGK_OK;
 }
@@ -628,7 +873,7 @@ kgk_status kgk_nrc_infer(kgk_scene *s, const float *raw, size_t n, float *out) {
     KGK_TRY(nrc_infer_dev(*s->nrc, (const float *)draw, kRaw, (int)n, nullptr, (float *)dout, nullptr, s->stream));
     if (!od) KGK_CUDA(cudaMemcpyAsync(out, dout, n * 3 * sizeof(float), cudaMemcpyDeviceToHost, s->stream));
     KGK_CUDA(cudaStreamSynchronize(s->stream));
-    return KGK_OK;
+    return nrc_check_error(*s->nrc);
 }
 
 kgk_status kgk_nrc_gradients(kgk_scene *s, const float *raw, const float *target, size_t n, float *grad, float *loss) {

@@ -1216,6 +1216,7 @@ kgk_status kgk_render(kgk_scene *s, const kgk_camera *cam, const kgk_camera *pre
         stats->ms_shadow = stage_ms[2];
     }
     for (cudaEvent_t e : ev) cudaEventDestroy(e);
+    if (cfg->use_cache) KGK_TRY(nrc_check_error(*s->nrc));
     if (hs[kOverflow])
         return fail(KGK_ERR_DEVICE_CHECK, "kgk_render: " + std::to_string(hs[kOverflow]) +
                                               " traversals overflowed their stack");
