@@ -141,6 +141,19 @@ def cpu_reference(tris, mats, env, threads, budget_s=10.0, chunk=65536):
     return rays / secs, rays, secs, done
 
 
+def reduce_over_ranks(dist, dev_ms, e2e_s, rays, e2e_rays, device):
+    """Replicas: the job's time is the slowest rank's (max), its work the sum
+    of all ranks' rays.  Returns (dev_ms, e2e_s, rays, e2e_rays) for the job."""
+    import torch
+    tt = torch.tensor([dev_ms, e2e_s], dtype=torch.float64, device=device)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    tot = torch.tensor([float(rays), float(e2e_rays)], dtype=torch.float64, device=device)
+    dist.all_reduce(tot)
+    dev_ms, e2e_s = tt.tolist()
+    rays, e2e_rays = tot.tolist()
+    return dev_ms, e2e_s, rays, e2e_rays
+
+
 def run_ours(args):
     import kagayaki_gb300 as kg
     from kagayaki_gb300 import ESTIMATOR_UNBIASED, ESTIMATOR_COMPAT, Scene
@@ -205,13 +218,7 @@ def run_ours(args):
         except Exception as e:  # the throughput line is still printed
             study = {"error": f"{type(e).__name__}: {e}"}
     if dist:
-        import torch
-        tt = torch.tensor([dev_ms, e2e_s], dtype=torch.float64, device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        tot = torch.tensor([float(rays), float(e2e_rays)], dtype=torch.float64, device="cuda")
-        dist.all_reduce(tot)
-        dev_ms, e2e_s = tt.tolist()
-        rays, e2e_rays = tot.tolist()
+        dev_ms, e2e_s, rays, e2e_rays = reduce_over_ranks(dist, dev_ms, e2e_s, rays, e2e_rays, "cuda")
     scene.close()
     if rank != 0:
         return
@@ -397,6 +404,65 @@ def run_svgf_orbit(args):
     print(json.dumps(line), flush=True)
 
 
+def run_mlp(args):
+    """The radiance-cache MLP alone (64 -> 5 x 64 -> 3, BF16 in, FP32
+    accumulate): inference of 2^21 queries (tcgen05 kernel) and training
+    steps on 65,536 samples (forward + backward + dW + Adam), device buffers.
+    TFLOP/s over algorithmic FLOPs: 2 x 20,672 per query, 3 x that per
+    training sample."""
+    import ctypes
+    import torch
+    from kagayaki_gb300 import Scene, scenes
+    from kagayaki_gb300._lib import check, lib
+    tris, mats, _ = scenes.cornell_box()
+    scene = Scene(tris, mats)
+    check(lib().kgk_nrc_init(scene._h, None))
+    g = torch.Generator(device="cpu").manual_seed(1)
+    n = 1 << 21
+    raw = torch.rand((n, 13), generator=g).cuda()
+    out = torch.empty((n, 3), device="cuda")
+    nt = 65536
+    traw = torch.rand((nt, 13), generator=g).cuda()
+    tgt = torch.rand((nt, 3), generator=g).cuda()
+    loss = np.zeros(1, np.float32)  # host: the call returns the last step's loss
+    vp = lambda t: ctypes.c_void_p(t.data_ptr())  # noqa: E731
+
+    def infer():
+        check(lib().kgk_nrc_infer(scene._h, vp(raw), n, vp(out)))
+
+    def train(k):
+        check(lib().kgk_nrc_train(scene._h, vp(traw), vp(tgt), nt, k, ctypes.c_void_p(loss.ctypes.data)))
+
+    for _ in range(args.warmup):
+        infer()
+        train(4)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        infer()
+    ti = (time.perf_counter() - t0) / args.steps
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        train(4)
+    tt = (time.perf_counter() - t0) / args.steps / 4
+    scene.close()
+    peaks = json.load(open(os.path.join(HERE, "MEASURED_PEAKS.json"))) if os.path.exists(
+        os.path.join(HERE, "MEASURED_PEAKS.json")) else {}
+    peak = peaks.get("bf16_tflops", 1900.0)
+    fl = 2 * 20672
+    inf_tf = fl * n / ti / 1e12
+    trn_tf = 3 * fl * nt / tt / 1e12
+    line = {"metric": "Mqueries/s", "value": round(n / ti / 1e6, 1), "unit": "Mqueries/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ti * 1e3, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "bf16 (fp32 accumulate)", "data": "uniform random queries",
+            "config": {"workload": "cache-mlp", "queries": n, "train_batch": nt, "timing": "wall clock per call"},
+            "inference": {"tflops": round(inf_tf, 2), "frac_of_bf16_peak": round(inf_tf / peak, 4),
+                          "kernel": "k_infer_tc (tcgen05)"},
+            "training_step": {"ms": round(tt * 1e3, 3), "tflops": round(trn_tf, 2),
+                              "frac_of_bf16_peak": round(trn_tf / peak, 4), "kernel": "k_train (mma.sync)"}}
+    print(json.dumps(line), flush=True)
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -434,8 +500,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
     ap.add_argument("--no-relmse", action="store_true", help="skip the plain-vs-cache relMSE study")
     ap.add_argument("--wave-paths", type=int, default=0, help="paths per wave (0 = the library default)")
-    ap.add_argument("--workload", default="frame", choices=["frame", "svgf-orbit"],
-                    help="frame: the 64-spp Mrays/s benchmark; svgf-orbit: 60 frames at 1 spp + SVGF")
+    ap.add_argument("--workload", default="frame", choices=["frame", "svgf-orbit", "mlp"],
+                    help="frame: the 64-spp Mrays/s benchmark; svgf-orbit: 60 frames at 1 spp + SVGF; "
+                         "mlp: the radiance-cache network alone")
     ap.add_argument("--width", type=int, default=0, help="override the frame width (profiling cases)")
     ap.add_argument("--height", type=int, default=0, help="override the frame height")
     ap.add_argument("--spp", type=int, default=0, help="override the samples per pixel")
@@ -444,6 +511,8 @@ def main():
         run_reference(args)
     elif args.workload == "svgf-orbit":
         run_svgf_orbit(args)
+    elif args.workload == "mlp":
+        run_mlp(args)
     else:
         run_ours(args)
 

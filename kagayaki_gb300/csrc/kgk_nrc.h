@@ -21,6 +21,9 @@ struct NrcState {
     kgk_nrc_config cfg{};
     float *w = nullptr, *m = nullptr, *v = nullptr, *g = nullptr;  // FP32 master weights, Adam, gradient
     unsigned short *img = nullptr;   // BF16 weight image (shared-memory layout)
+    unsigned short *trH = nullptr;   // training scratch: activations H_l, [layer][row][64]
+    unsigned short *trD = nullptr;   // training scratch: output gradients dZ_l, [layer][row][64]
+    int tr_cap = 0;                  // rows the scratch holds
     float *scal = nullptr;           // [0] loss scale, [1] last loss
     int *ints = nullptr;             // [0] non-finite flag, [1] clean steps since the last scale change,
                                      // [2] inference timeout flag

@@ -426,78 +426,47 @@ __global__ void __launch_bounds__(128) k_infer_tc(const unsigned short *__restri
 }
 
 // ---------------------------------------------------------------------------
-// training: forward + loss + backward + dW
+// training, split form: k_train_fb runs forward, loss and backward for tiles
+// of 16 samples per warp and stores every layer's input activations H_l and
+// output gradients dZ_l (BF16 rows of 64) to global scratch; k_train_dw then
+// forms dW_l = dZ_l^T H_l over the batch as a split-K GEMM (each CTA a chunk
+// of samples, accumulating in registers, one atomic add per element per CTA).
+// Layer 5 is the output layer (dZ_5 has 3 live columns of 64).
 // ---------------------------------------------------------------------------
-struct TrainSmem {
-    // layout inside dynamic shared memory
-    static constexpr size_t img = 0;
-    static constexpr size_t dw = ((size_t)kImgElems * 2 + 15) & ~(size_t)15;
-    static constexpr size_t dw_floats = (size_t)kLayers * kWidth * kWidth + (size_t)kOutRows * kWidth;
-    static constexpr size_t warps = dw + dw_floats * 4;
-    static constexpr size_t per_warp = (size_t)(kLayers + 2) * 16 * kPitch * 2;  // acts 0..L, dZ stage
-    static constexpr size_t total(int nw) { return warps + per_warp * nw; }
-};
+constexpr int kFbWarps = 4;
+constexpr size_t kFbPerWarp = (size_t)(kLayers + 1) * 16 * kPitch * 2;  // H_0..H_5 tiles
+constexpr size_t kFbSmem = (((size_t)kImgElems * 2 + 15) & ~(size_t)15) + kFbPerWarp * kFbWarps;
 
-__device__ __forceinline__ void dw_accumulate(float *dWl, const unsigned short *dZs, const unsigned short *A, int mtiles,
-                                              int valid_rows) {
-    const int g = (threadIdx.x & 31) >> 2, t = threadIdx.x & 3;
-    for (int mt = 0; mt < mtiles; ++mt) {
-        uint32_t a[4];
-        const int o0 = mt * 16 + g, o1 = o0 + 8;
-        a[0] = pack_raw(dZs[(2 * t) * kPitch + o0], dZs[(2 * t + 1) * kPitch + o0]);
-        a[1] = pack_raw(dZs[(2 * t) * kPitch + o1], dZs[(2 * t + 1) * kPitch + o1]);
-        a[2] = pack_raw(dZs[(2 * t + 8) * kPitch + o0], dZs[(2 * t + 9) * kPitch + o0]);
-        a[3] = pack_raw(dZs[(2 * t + 8) * kPitch + o1], dZs[(2 * t + 9) * kPitch + o1]);
-#pragma unroll
-        for (int nt = 0; nt < 8; ++nt) {
-            const int i = nt * 8 + g;
-            const uint32_t b0 = pack_raw(A[(2 * t) * kPitch + i], A[(2 * t + 1) * kPitch + i]);
-            const uint32_t b1 = pack_raw(A[(2 * t + 8) * kPitch + i], A[(2 * t + 9) * kPitch + i]);
-            float c[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-            mma16816(c, a, b0, b1);
-            const int col = nt * 8 + 2 * t;
-            if (o0 < valid_rows) {
-                atomicAdd(&dWl[o0 * kWidth + col], c[0]);
-                atomicAdd(&dWl[o0 * kWidth + col + 1], c[1]);
-            }
-            if (o1 < valid_rows) {
-                atomicAdd(&dWl[o1 * kWidth + col], c[2]);
-                atomicAdd(&dWl[o1 * kWidth + col + 1], c[3]);
-            }
-        }
+// Copies a warp's [16][kPitch] BF16 tile (64 live columns) to global rows
+// dst[row * 64 + c], rows base..base+15 (16-byte stores).
+__device__ __forceinline__ void tile_to_global(const unsigned short *T, unsigned short *dst, int base) {
+    const int lane = threadIdx.x & 31;
+    for (int i = lane; i < 16 * 8; i += 32) {
+        const int r = i >> 3, c = i & 7;
+        const uint4 v = *reinterpret_cast<const uint4 *>(T + r * kPitch + c * 8);
+        *reinterpret_cast<uint4 *>(dst + (size_t)(base + r) * kWidth + c * 8) = v;
     }
 }
 
-// Stores C fragments (16 x 64, FP32) as a BF16 [16][kPitch] tile.
-__device__ __forceinline__ void store_acc(unsigned short *T, const float (&acc)[8][4]) {
-    const int g = (threadIdx.x & 31) >> 2, t = threadIdx.x & 3;
-#pragma unroll
-    for (int nt = 0; nt < 8; ++nt) {
-        const int c = nt * 8 + 2 * t;
-        *reinterpret_cast<uint32_t *>(T + g * kPitch + c) = pack2(acc[nt][0], acc[nt][1]);
-        *reinterpret_cast<uint32_t *>(T + (g + 8) * kPitch + c) = pack2(acc[nt][2], acc[nt][3]);
-    }
-}
-
-__global__ void __launch_bounds__(128) k_train(const unsigned short *__restrict__ img, const float *__restrict__ raw,
-                                               int raw_stride, const float *__restrict__ target, int tgt_stride,
-                                               int n, const int *n_dev, const float *scale_p, float *dW_glob,
-                                               float *loss_sum) {
+__global__ void __launch_bounds__(128) k_train_fb(const unsigned short *__restrict__ img, const float *__restrict__ raw,
+                                                  int raw_stride, const float *__restrict__ target, int tgt_stride,
+                                                  int n, const int *n_dev, const float *scale_p,
+                                                  unsigned short *Hs, unsigned short *Ds, size_t layer_stride,
+                                                  float *loss_sum) {
     extern __shared__ __align__(16) unsigned char smem[];
-    unsigned short *sW = reinterpret_cast<unsigned short *>(smem + TrainSmem::img);
-    float *sdW = reinterpret_cast<float *>(smem + TrainSmem::dw);
+    unsigned short *sW = reinterpret_cast<unsigned short *>(smem);
     const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3, wid = threadIdx.x >> 5;
-    unsigned short *acts = reinterpret_cast<unsigned short *>(smem + TrainSmem::warps + TrainSmem::per_warp * wid);
-    unsigned short *dzs = acts + (kLayers + 1) * 16 * kPitch;
+    unsigned short *acts = reinterpret_cast<unsigned short *>(smem + (((size_t)kImgElems * 2 + 15) & ~(size_t)15) +
+                                                              kFbPerWarp * wid);
     load_image(sW, img);
-    for (size_t i = threadIdx.x; i < TrainSmem::dw_floats; i += blockDim.x) sdW[i] = 0.0f;
     __syncthreads();
-    const int total = n_dev ? *n_dev : n;
+    const int total = n_dev ? min(*n_dev, n) : n;
+    const int padded = (total + 15) & ~15;
     const float S = *scale_p;
     const float inv_n = 1.0f / (3.0f * (float)max(total, 1));
     float lsum = 0.0f;
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nwarps = (gridDim.x * blockDim.x) >> 5;
-    for (int base = warp * 16; base < total; base += nwarps * 16) {
+    for (int base = warp * 16; base < padded; base += nwarps * 16) {
         const int sa = base + g, sb = base + g + 8;
         float ra[kRaw], rb[kRaw];
 #pragma unroll
@@ -517,6 +486,8 @@ __global__ void __launch_bounds__(128) k_train(const unsigned short *__restrict_
         }
         float y[4];
         out_fwd(sW + kLayers * kWidth * kPitch, a, y);
+        __syncwarp();
+        for (int l = 0; l <= kLayers; ++l) tile_to_global(acts + l * 16 * kPitch, Hs + l * layer_stride, base);
         // relative L2: d/dy (y - t)^2 / (y^2 + eps), denominator held constant
         float dy[4] = {0.0f, 0.0f, 0.0f, 0.0f};
 #pragma unroll
@@ -534,18 +505,20 @@ __global__ void __launch_bounds__(128) k_train(const unsigned short *__restrict_
                 dy[2 * r + k] = 2.0f * d / den * inv_n * S;
             }
         }
-        // output layer: dZ_out (16 x 8, cols 0..2 live) staged as BF16
-        __syncwarp();
+        // dZ of the output layer: columns 0..3 of the rows (3 live)
         {
-            float tile[8][4];
-#pragma unroll
-            for (int nt = 0; nt < 8; ++nt) tile[nt][0] = tile[nt][1] = tile[nt][2] = tile[nt][3] = 0.0f;
-            tile[0][0] = dy[0]; tile[0][1] = dy[1]; tile[0][2] = dy[2]; tile[0][3] = dy[3];
-            store_acc(dzs, tile);
+            unsigned short *drow = Ds + (size_t)kLayers * layer_stride;
+            const uint32_t d0 = pack2(dy[0], dy[1]), d1 = pack2(dy[2], dy[3]);
+            if (t < 2) {
+                *reinterpret_cast<uint32_t *>(drow + (size_t)sa * kWidth + 2 * t) = d0;
+                *reinterpret_cast<uint32_t *>(drow + (size_t)sb * kWidth + 2 * t) = d1;
+            } else {
+                *reinterpret_cast<uint32_t *>(drow + (size_t)sa * kWidth + 2 * t) = 0u;
+                *reinterpret_cast<uint32_t *>(drow + (size_t)sb * kWidth + 2 * t) = 0u;
+            }
+            // columns 8..63 of the output-layer rows stay zero (written once per call)
         }
-        __syncwarp();
-        dw_accumulate(sdW + kLayers * kWidth * kWidth, dzs, acts + kLayers * 16 * kPitch, 1, 3);
-        // dA_L = dZ_out (16 x 16, cols >= 8 zero) * W_out (16 x 64)
+        // dA_4 = dZ_out (16 x 16, cols >= 8 zero) * W_out (16 x 64)
         uint32_t dza[4];
         dza[0] = pack2(dy[0], dy[1]);
         dza[1] = pack2(dy[2], dy[3]);
@@ -565,19 +538,23 @@ __global__ void __launch_bounds__(128) k_train(const unsigned short *__restrict_
 #pragma unroll 1
         for (int l = kLayers - 1; l >= 0; --l) {
             // dZ_l = dA_l * relu'(h_l); h_l is activation l + 1 in `acts`
-            const unsigned short *H = acts + (l + 1) * 16 * kPitch;
+            const unsigned short *Hl = acts + (l + 1) * 16 * kPitch;
 #pragma unroll
             for (int nt = 0; nt < 8; ++nt) {
                 const int c = nt * 8 + 2 * t;
-                if (bf2f(H[g * kPitch + c]) <= 0.0f) acc[nt][0] = 0.0f;
-                if (bf2f(H[g * kPitch + c + 1]) <= 0.0f) acc[nt][1] = 0.0f;
-                if (bf2f(H[(g + 8) * kPitch + c]) <= 0.0f) acc[nt][2] = 0.0f;
-                if (bf2f(H[(g + 8) * kPitch + c + 1]) <= 0.0f) acc[nt][3] = 0.0f;
+                if (bf2f(Hl[g * kPitch + c]) <= 0.0f) acc[nt][0] = 0.0f;
+                if (bf2f(Hl[g * kPitch + c + 1]) <= 0.0f) acc[nt][1] = 0.0f;
+                if (bf2f(Hl[(g + 8) * kPitch + c]) <= 0.0f) acc[nt][2] = 0.0f;
+                if (bf2f(Hl[(g + 8) * kPitch + c + 1]) <= 0.0f) acc[nt][3] = 0.0f;
             }
-            __syncwarp();
-            store_acc(dzs, acc);
-            __syncwarp();
-            dw_accumulate(sdW + (size_t)l * kWidth * kWidth, dzs, acts + l * 16 * kPitch, 4, kWidth);
+            // dZ_l rows to global (BF16)
+            unsigned short *drow = Ds + (size_t)l * layer_stride;
+#pragma unroll
+            for (int nt = 0; nt < 8; ++nt) {
+                const int c = nt * 8 + 2 * t;
+                *reinterpret_cast<uint32_t *>(drow + (size_t)sa * kWidth + c) = pack2(acc[nt][0], acc[nt][1]);
+                *reinterpret_cast<uint32_t *>(drow + (size_t)sb * kWidth + c) = pack2(acc[nt][2], acc[nt][3]);
+            }
             if (l == 0) break;
             // dA_{l-1} = dZ_l (16 x 64) * W_l (64 x 64)
             uint32_t da[4][4];
@@ -604,20 +581,70 @@ __global__ void __launch_bounds__(128) k_train(const unsigned short *__restrict_
         }
         __syncwarp();
     }
-    // loss
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) lsum += __shfl_xor_sync(~0u, lsum, o);
     if (lane == 0 && loss_sum) atomicAdd(loss_sum, lsum * inv_n);
-    __syncthreads();
-    for (size_t i = threadIdx.x; i < TrainSmem::dw_floats; i += blockDim.x) {
-        const float v = sdW[i];
-        if (v != 0.0f) {
-            // global gradient is [l][out][in] with the output layer's 3 rows
-            if (i < (size_t)kLayers * kWidth * kWidth) atomicAdd(&dW_glob[i], v);
-            else {
-                const size_t j = i - (size_t)kLayers * kWidth * kWidth;
-                if (j / kWidth < 3) atomicAdd(&dW_glob[(size_t)kLayers * kWidth * kWidth + j], v);
-            }
+}
+
+// dW_l[o][i] += sum over a chunk of samples of dZ_l[s][o] * H_l[s][i].
+// blockIdx.y = layer (0..4 hidden, 5 output); blockIdx.x = sample chunk.
+// Warp w owns output rows 16w..16w+15 (the output layer only warp 0).
+constexpr int kDwChunk = 1024;
+__global__ void __launch_bounds__(128) k_train_dw(const unsigned short *__restrict__ Hs,
+                                                  const unsigned short *__restrict__ Ds, size_t layer_stride, int n,
+                                                  const int *n_dev, float *dW_glob) {
+    __shared__ __align__(16) unsigned short sD[16 * kPitch], sH[16 * kPitch];
+    const int l = blockIdx.y;
+    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3, wid = threadIdx.x >> 5;
+    const int total = n_dev ? min(*n_dev, n) : n;
+    const int padded = (total + 15) & ~15;
+    const int s0 = blockIdx.x * kDwChunk, s1 = min(s0 + kDwChunk, padded);
+    if (s0 >= s1) return;
+    const unsigned short *D = Ds + (size_t)l * layer_stride, *Hl = Hs + (size_t)l * layer_stride;
+    const bool active = l < kLayers || wid == 0;
+    float acc[8][4];
+#pragma unroll
+    for (int nt = 0; nt < 8; ++nt) acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.0f;
+    for (int sb = s0; sb < s1; sb += 16) {
+        __syncthreads();
+        {
+            const int r = threadIdx.x >> 3, c = threadIdx.x & 7;  // 128 threads = 16 rows x 8 chunks
+            *reinterpret_cast<uint4 *>(sD + r * kPitch + c * 8) =
+                *reinterpret_cast<const uint4 *>(D + (size_t)(sb + r) * kWidth + c * 8);
+            *reinterpret_cast<uint4 *>(sH + r * kPitch + c * 8) =
+                *reinterpret_cast<const uint4 *>(Hl + (size_t)(sb + r) * kWidth + c * 8);
+        }
+        __syncthreads();
+        if (!active) continue;
+        // A = dZ^T rows o (16 of them) x 16 samples; B = H samples x 64 inputs
+        uint32_t a[4];
+        const int o0 = wid * 16 + g, o1 = o0 + 8;
+        a[0] = pack_raw(sD[(2 * t) * kPitch + o0], sD[(2 * t + 1) * kPitch + o0]);
+        a[1] = pack_raw(sD[(2 * t) * kPitch + o1], sD[(2 * t + 1) * kPitch + o1]);
+        a[2] = pack_raw(sD[(2 * t + 8) * kPitch + o0], sD[(2 * t + 9) * kPitch + o0]);
+        a[3] = pack_raw(sD[(2 * t + 8) * kPitch + o1], sD[(2 * t + 9) * kPitch + o1]);
+#pragma unroll
+        for (int nt = 0; nt < 8; ++nt) {
+            const int i = nt * 8 + g;
+            const uint32_t b0 = pack_raw(sH[(2 * t) * kPitch + i], sH[(2 * t + 1) * kPitch + i]);
+            const uint32_t b1 = pack_raw(sH[(2 * t + 8) * kPitch + i], sH[(2 * t + 9) * kPitch + i]);
+            mma16816(acc[nt], a, b0, b1);
+        }
+    }
+    if (!active) return;
+    const int o0 = wid * 16 + g, o1 = o0 + 8;
+    const int rows = l < kLayers ? kWidth : 3;
+    float *dW = dW_glob + (size_t)l * kWidth * kWidth;
+#pragma unroll
+    for (int nt = 0; nt < 8; ++nt) {
+        const int col = nt * 8 + 2 * t;
+        if (o0 < rows) {
+            atomicAdd(&dW[o0 * kWidth + col], acc[nt][0]);
+            atomicAdd(&dW[o0 * kWidth + col + 1], acc[nt][1]);
+        }
+        if (o1 < rows) {
+            atomicAdd(&dW[o1 * kWidth + col], acc[nt][2]);
+            atomicAdd(&dW[o1 * kWidth + col + 1], acc[nt][3]);
         }
     }
 }
@@ -721,7 +748,7 @@ kgk_status nrc_init(NrcState &N, const kgk_nrc_config *cfg, int device) {
     k_make_image<<<64, 256>>>(N.w, N.img);
     KGK_CUDA(cudaGetLastError());
     KGK_CUDA(cudaDeviceSynchronize());
-    KGK_CUDA(cudaFuncSetAttribute(k_train, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TrainSmem::total(4)));
+    KGK_CUDA(cudaFuncSetAttribute(k_train_fb, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFbSmem));
     KGK_CUDA(cudaFuncSetAttribute(k_infer_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc::kSmemBytes));
     cudaDeviceProp p;
     KGK_CUDA(cudaGetDeviceProperties(&p, device));
@@ -732,10 +759,11 @@ kgk_status nrc_init(NrcState &N, const kgk_nrc_config *cfg, int device) {
 }
 
 void nrc_free(NrcState &N) {
-    void *ptrs[] = {N.w, N.m, N.v, N.g, N.img, N.scal, N.ints};
+    void *ptrs[] = {N.w, N.m, N.v, N.g, N.img, N.scal, N.ints, N.trH, N.trD};
     for (void *p : ptrs) dfree(p);
     N.w = N.m = N.v = N.g = N.scal = nullptr;
-    N.img = nullptr;
+    N.img = N.trH = N.trD = nullptr;
+    N.tr_cap = 0;
     N.ints = nullptr;
     N.ready = false;
 }
@@ -760,11 +788,26 @@ kgk_status nrc_infer_dev(NrcState &N, const float *raw, int stride, int n, const
 
 kgk_status nrc_grad_dev(NrcState &N, const float *raw, int raw_stride, const float *tgt, int tgt_stride, int n,
                         const int *n_dev, cudaStream_t st) {
+    const int rows = (n + 15) & ~15;
+    if (N.tr_cap < rows) {
+        // per-sample activations and output gradients of every layer (BF16 rows of 64)
+        dfree(N.trH);
+        dfree(N.trD);
+        N.trH = N.trD = nullptr;
+        N.tr_cap = 0;
+        const size_t cnt = (size_t)(kLayers + 1) * rows * kWidth;
+        KGK_TRY(dalloc(&N.trH, cnt, "cache training scratch"));
+        KGK_TRY(dalloc(&N.trD, cnt, "cache training scratch"));
+        KGK_CUDA(cudaMemset(N.trD, 0, cnt * sizeof(unsigned short)));  // output-layer columns >= 8 stay 0
+        N.tr_cap = rows;
+    }
+    const size_t ls = (size_t)N.tr_cap * kWidth;
     KGK_CUDA(cudaMemsetAsync(N.g, 0, kParams * sizeof(float), st));
     KGK_CUDA(cudaMemsetAsync(N.scal + 1, 0, sizeof(float), st));  // loss
-    const int grid = N.sms;
-    k_train<<<grid, 128, TrainSmem::total(4), st>>>(N.img, raw, raw_stride, tgt, tgt_stride, n, n_dev, N.scal, N.g,
-                                                     N.scal + 1);
+    k_train_fb<<<N.sms * 2, 32 * kFbWarps, kFbSmem, st>>>(N.img, raw, raw_stride, tgt, tgt_stride, n, n_dev, N.scal,
+                                                          N.trH, N.trD, ls, N.scal + 1);
+    const dim3 gdw((unsigned)((rows + kDwChunk - 1) / kDwChunk), kLayers + 1);
+    k_train_dw<<<gdw, 128, 0, st>>>(N.trH, N.trD, ls, n, n_dev, N.g);
     KGK_CUDA(cudaGetLastError());
     return KGK_OK;
 }

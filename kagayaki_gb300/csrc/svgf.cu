@@ -435,6 +435,7 @@ __global__ void k_gbuffer_to_records(const float4 *pos, const float4 *nrm, const
 // ---------------------------------------------------------------------------
 struct StdArgs {
     int W, H;
+    int sn_log2;                           // log2(sigma_n) when it is a power of two <= 2^16, else -1
     const float4 *pos, *nrm, *alb, *emi;   // current G-buffer
     const float4 *noisy;                   // current frame (kgk_vec)
     float4 *hist, *hist_prev;
@@ -537,7 +538,18 @@ __global__ void k_s_temporal(StdArgs a) {
 }
 
 __device__ __forceinline__ float depth_weight_std(float d, float dq, float grad, float dist, float sz) {
-    return expf(-fabsf(d - dq) / (sz * fabsf(grad) * dist + 1e-3f));
+    return __expf(-fabsf(d - dq) / (sz * fabsf(grad) * dist + 1e-3f));
+}
+
+// Normal weight max(0, n.nq)^sigma_n: repeated squaring when sigma_n is a
+// power of two (sn_log2 >= 0; 128 = seven squarings), else the fast power.
+__device__ __forceinline__ float normal_weight(float c, float sn, int sn_log2) {
+    c = fmaxf(0.0f, c);
+    if (sn_log2 >= 0) {
+        for (int i = 0; i < sn_log2; ++i) c *= c;
+        return c;
+    }
+    return c > 0.0f ? __powf(c, sn) : 0.0f;
 }
 
 // Variance: temporal moments when the history is long enough, else a 7x7
@@ -568,7 +580,7 @@ __global__ void k_s_variance(StdArgs a) {
                     const float4 qn = a.nrm[q];
                     if (__float_as_int(qn.w) < 0 || __float_as_int(a.alb[q].w) != mat) continue;
                     const float w = depth_weight_std(d, a.pos[q].w, grad, sqrtf((float)(kx * kx + ky * ky)), a.sz) *
-                                    powf(fmaxf(0.0f, dot3(f3(nr), f3(qn))), a.sn);
+                                    normal_weight(dot3(f3(nr), f3(qn)), a.sn, a.sn_log2);
                     const float2 m = a.mom[q];
                     s1 += w * m.x;
                     s2 += w * m.y;
@@ -629,8 +641,8 @@ __global__ void k_s_atrous(StdArgs a, const float4 *__restrict__ in, float4 *out
             const float4 qc = in[q];
             const float dist = (float)step * sqrtf((float)(ox * ox + oy * oy));
             const float wz = depth_weight_std(d, a.pos[q].w, grad, dist, a.sz);
-            const float wn = powf(fmaxf(0.0f, dot3(f3(nr), f3(qn))), a.sn);
-            const float wl = expf(-fabsf(l - lumf(f3(qc))) / sdl);
+            const float wn = normal_weight(dot3(f3(nr), f3(qn)), a.sn, a.sn_log2);
+            const float wl = __expf(-fabsf(l - lumf(f3(qc))) / sdl);
             const float w = cKW[ki] * wz * wn * wl;
             sc += f3(qc) * w;
             sv += w * w * qc.w;
@@ -809,6 +821,9 @@ kgk_status kgk_svgf(kgk_scene *s, const kgk_svgf_config *cfg, const kgk_vec *noi
         a.alpha = cfg->alpha > 0.0f ? cfg->alpha : 0.2f;
         a.sz = cfg->sigma_z > 0.0f ? cfg->sigma_z : 1.0f;
         a.sn = cfg->sigma_n > 0.0f ? cfg->sigma_n : 128.0f;
+        a.sn_log2 = -1;
+        for (int k = 0; k <= 16; ++k)
+            if (a.sn == (float)(1 << k)) a.sn_log2 = k;
         a.sl = cfg->sigma_l > 0.0f ? cfg->sigma_l : 4.0f;
         k_s_temporal<<<g, 256, 0, st>>>(a);
         k_s_variance<<<g, 256, 0, st>>>(a);
