@@ -106,7 +106,7 @@ def build_workload():
     return tris, mats, env, info
 
 
-def orbit_camera(frame, height, radius=25.0, start_deg=37.0, step_deg=6.0, z=6.0):
+def orbit_camera(frame, height, radius=25.0, start_deg=37.0, step_deg=6.0, z=6.0, target_z=8.0):
     """Camera on a circle of `radius` around the field, looking at its centre
     (z up).  Camera_SetUpCamera's Euler convention: rotate X by 90 - pitch to
     look horizontally, then Z to face the centre."""
@@ -114,7 +114,7 @@ def orbit_camera(frame, height, radius=25.0, start_deg=37.0, step_deg=6.0, z=6.0
     ang = start_deg + step_deg * frame
     a = np.deg2rad(ang)
     org = (radius * np.cos(a), radius * np.sin(a), z)
-    pitch = np.rad2deg(np.arctan2(z - 8.0, radius))
+    pitch = np.rad2deg(np.arctan2(z - target_z, radius))
     return camera_setup(org, 28.0, (90.0 - pitch, 0.0, ang + 90.0), height)
 
 
@@ -463,6 +463,87 @@ def run_mlp(args):
     print(json.dumps(line), flush=True)
 
 
+def run_c5(args):
+    """The scaled config: 10.6 M triangles (128 displaced icospheres on a
+    256 x 256-tile terrain), 64 RGBA8 1024^2 textures sampled bilinearly, a
+    4096 x 2048 HDR sky, 3840 x 2160 at 1 spp per frame over a 120-frame orbit
+    with the radiance cache (2^18 training paths per frame; the network is the
+    64-wide one), then plain vs cache at equal time and at equal relMSE against
+    a 4096-spp FP64-accumulated frame."""
+    from kagayaki_gb300 import ESTIMATOR_UNBIASED, Scene, scenes
+    W, H = args.width or 3840, args.height or 2160
+    frames = 120
+    t0 = time.perf_counter()
+    tris, mats, tex, info = scenes.c5_scene()
+    env, _ = scenes.sky_environment(4096, 2048, sun_peak=1e4, seed=3)
+    gen_s = time.perf_counter() - t0
+    scene = Scene(tris, mats, textures=[np.zeros((1, 1, 3), np.float32)] * len(tex), env=env)
+    scene.set_textures_rgba8(tex)
+    bvh = scene.build_bvh()
+    kw = dict(max_depth=WORKLOAD["max_depth"], estimator=ESTIMATOR_UNBIASED, texture_filter=1)
+    cam_of = lambda f: orbit_camera(f, H, radius=60.0, z=14.0, target_z=12.0)  # noqa: E731
+    out = np.empty((H, W, 4), np.float32)
+    res = {}
+    for mode in ("plain", "cache"):
+        if mode == "cache":
+            scene.cache_init(train_paths=1 << 18, seed=1)
+        for f in range(3):
+            scene.render(cam_of(f), W, H, spp=1, seed=1, frame_index=f, use_cache=mode == "cache", out=out, **kw)
+        dev = 0.0
+        t0 = time.perf_counter()
+        for f in range(frames):
+            _, st = scene.render(cam_of(f), W, H, spp=1, seed=1, frame_index=f, use_cache=mode == "cache", out=out,
+                                 **kw)
+            dev += st["ms_device"]
+        wall = time.perf_counter() - t0
+        res[mode] = {"frames_per_s_device": round(frames / (dev / 1e3), 2), "frames_per_s_wall": round(frames / wall, 2),
+                     "ms_per_frame_device": round(dev / frames, 2)}
+    # static camera: converged reference, cache after training, plain at equal time and at equal relMSE
+    cam = cam_of(0)
+    scene.accum_reset(W, H)
+    for k in range(64):
+        scene.render(cam, W, H, spp=64, seed=7, frame_index=900_000 + k, accumulate=True, **kw)
+    ref, _, nref = scene.accum_read(W, H)
+    scene.cache_init(train_paths=1 << 18, seed=1)
+    for f in range(32):
+        scene.render(cam, W, H, spp=1, seed=5, frame_index=f, use_cache=True, out=out, **kw)
+    acc = np.zeros((H, W, 3))
+    cache_ms = 0.0
+    nf = 8
+    for f in range(nf):
+        img, st = scene.render(cam, W, H, spp=1, seed=5, frame_index=32 + f, use_cache=True, out=out, **kw)
+        acc += img[..., :3]
+        cache_ms += st["ms_device"]
+    e_cache = rel_mse(acc / nf, ref)
+    _, st4 = scene.render(cam, W, H, spp=4, seed=3, frame_index=950_000, out=out, **kw)
+    spp_eq = max(1, int(round(cache_ms / (st4["ms_device"] / 4))))
+    img, stp = scene.render(cam, W, H, spp=spp_eq, seed=9, frame_index=950_001, out=out, **kw)
+    e_plain = rel_mse(img[..., :3].astype(np.float64), ref)
+    eq_relmse = None
+    for spp in (16, 32, 64, 128, 256, 512):
+        img, stq = scene.render(cam, W, H, spp=spp, seed=11, frame_index=960_000 + spp, out=out, **kw)
+        e = rel_mse(img[..., :3].astype(np.float64), ref)
+        if e <= e_cache:
+            eq_relmse = {"plain_spp": spp, "plain_ms": round(stq["ms_device"], 2), "plain_relmse": round(e, 5),
+                         "cache_ms": round(cache_ms, 2), "time_ratio": round(stq["ms_device"] / cache_ms, 2)}
+            break
+    scene.close()
+    line = {"metric": "frames/s", "value": res["cache"]["frames_per_s_device"], "unit": "frames/s", "n_gpus": 1,
+            "steps": frames, "warmup": 3, "ms_per_step": res["cache"]["ms_per_frame_device"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 (cache MLP bf16)",
+            "data": "synthetic seeded scene",
+            "config": {"workload": "c5-10.6M-4k-1spp-orbit", "triangles": int(len(tris)), "width": W, "height": H,
+                       "textures": "64 x 1024^2 RGBA8, bilinear", "env": "4096x2048 float32 sky + sun 1e4",
+                       "cache": "width 64, 2^18 training paths per frame", "scene_generation_s": round(gen_s, 1),
+                       "bvh_build_ms": round(bvh["ms_build"], 1)},
+            "orbit": res,
+            "relmse_static": {"reference_spp": int(nref),
+                              "equal_time": {"ms": round(cache_ms, 2), "cache": round(e_cache, 5),
+                                             "plain": round(e_plain, 5), "plain_spp": spp_eq},
+                              "equal_relmse": eq_relmse}}
+    print(json.dumps(line), flush=True)
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -500,9 +581,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
     ap.add_argument("--no-relmse", action="store_true", help="skip the plain-vs-cache relMSE study")
     ap.add_argument("--wave-paths", type=int, default=0, help="paths per wave (0 = the library default)")
-    ap.add_argument("--workload", default="frame", choices=["frame", "svgf-orbit", "mlp"],
+    ap.add_argument("--workload", default="frame", choices=["frame", "svgf-orbit", "mlp", "c5"],
                     help="frame: the 64-spp Mrays/s benchmark; svgf-orbit: 60 frames at 1 spp + SVGF; "
-                         "mlp: the radiance-cache network alone")
+                         "mlp: the radiance-cache network alone; c5: 10.6M triangles, 4K, textures, cache")
     ap.add_argument("--width", type=int, default=0, help="override the frame width (profiling cases)")
     ap.add_argument("--height", type=int, default=0, help="override the frame height")
     ap.add_argument("--spp", type=int, default=0, help="override the samples per pixel")
@@ -513,6 +594,8 @@ def main():
         run_svgf_orbit(args)
     elif args.workload == "mlp":
         run_mlp(args)
+    elif args.workload == "c5":
+        run_c5(args)
     else:
         run_ours(args)
 

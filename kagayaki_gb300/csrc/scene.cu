@@ -164,9 +164,9 @@ kgk_status scene_upload(DevScene &s, const kgk_triangle *tris_in, size_t n, cons
         std::vector<TexDesc> desc(ntex);
         size_t total = 0;
         for (size_t i = 0; i < ntex; ++i) {
-            if (!th[i].pixels || th[i].width <= 0 || th[i].height <= 0 || th[i].bpp < 3)
+            if (!th[i].pixels || th[i].width <= 0 || th[i].height <= 0 || th[i].bpp < 1 || th[i].bpp > 4)
                 return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_scene_create: texture " + std::to_string(i) +
-                                                          " needs pixels, a size and >= 3 channels");
+                                                          " needs pixels, a size and 1 to 4 channels");
             desc[i].offset = (int64_t)total;
             desc[i].w = th[i].width;
             desc[i].h = th[i].height;

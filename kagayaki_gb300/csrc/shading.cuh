@@ -393,8 +393,13 @@ __device__ __forceinline__ float3 tex_texel(const DevScene &s, const TexDesc &td
         const uchar4 b = __ldg(&s.tex_rgba8[td.offset + idx]);
         return f3(__ldg(&s.tex_lut[b.x]), __ldg(&s.tex_lut[b.y]), __ldg(&s.tex_lut[b.z]));
     }
-    const float *p = s.tex_pixels + td.offset + (size_t)idx * td.bpp;
-    return f3(__ldg(p), __ldg(p + 1), __ldg(p + 2));
+    // three consecutive floats from the texel, as Texture::get_Color reads
+    // them: with fewer than 3 channels they run into the next texels (the
+    // reference's behaviour); clamped at the end of the texture
+    const int n_el = td.w * td.h * td.bpp;
+    const int e = idx * td.bpp;
+    const float *p = s.tex_pixels + td.offset;
+    return f3(__ldg(p + e), __ldg(p + min(e + 1, n_el - 1)), __ldg(p + min(e + 2, n_el - 1)));
 }
 
 __device__ __forceinline__ float3 tex_fetch(const DevScene &s, int tex, float u, float v) {

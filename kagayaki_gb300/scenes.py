@@ -12,6 +12,8 @@ Scenes:
                          2-triangle emissive ceiling light (17,12,4); Lambert.
   icosphere_field()    - N displaced icospheres (subdivision s) over a ground
                          quad; Disney materials drawn per mesh; z up.
+  c5_scene()           - 128 icospheres on a 256 x 256-tile heightfield with
+                         64 procedural RGBA8 textures (10.6 M triangles).
   sky_environment()    - lat-long float32 RGB environment in the reference's
                          mapping (ImageBasedLighting.cuh:6-56): sky gradient and
                          a sun lobe of a given peak radiance.
@@ -287,6 +289,96 @@ def icosphere_field(n_meshes=64, subdiv=6, seed=2, box=20.0, amplitude=0.05,
     info = dict(centers=np.stack([cx, cy, cz], 1), radii=radii,
                 lo=(-box / 2, -box / 2, 0.0), hi=(box / 2, box / 2, box))
     return tris, mats, info
+
+
+def value_noise2(x, y, seed, octaves=3, base_freq=4.0):
+    """2D value noise over arrays x, y in [0, 1): `octaves` bilinear octaves
+    (freq base_freq * 2^k, amplitude 0.5^k), smoothstep-interpolated,
+    normalised to [-1, 1]."""
+    total = np.zeros(np.broadcast(x, y).shape)
+    norm = 0.0
+    for k in range(octaves):
+        freq = base_freq * (2 ** k)
+        amp = 0.5 ** k
+        qx, qy = x * freq + 1000.0, y * freq + 1000.0
+        ix, iy = np.floor(qx).astype(np.int64), np.floor(qy).astype(np.int64)
+        fx, fy = qx - ix, qy - iy
+        fx, fy = fx * fx * (3.0 - 2.0 * fx), fy * fy * (3.0 - 2.0 * fy)
+        z = np.zeros_like(ix)
+        h00 = _lattice_hash(ix, iy, z, seed * 131 + k)
+        h10 = _lattice_hash(ix + 1, iy, z, seed * 131 + k)
+        h01 = _lattice_hash(ix, iy + 1, z, seed * 131 + k)
+        h11 = _lattice_hash(ix + 1, iy + 1, z, seed * 131 + k)
+        total += amp * ((h00 * (1 - fx) + h10 * fx) * (1 - fy) + (h01 * (1 - fx) + h11 * fx) * fy)
+        norm += amp
+    return total / norm
+
+
+def heightfield_terrain(tiles=256, half=150.0, height=6.0, seed=9, material_id=0, shape_id=0, uv_repeat=8.0):
+    """A tiles x tiles grid of quads (2 * tiles^2 triangles) over
+    [-half, half]^2 at z = height * noise (3-octave value noise), smooth
+    normals, uv repeating uv_repeat times across the terrain."""
+    n = tiles + 1
+    g = np.linspace(0.0, 1.0, n)
+    X, Y = np.meshgrid(g, g, indexing="xy")
+    Z = height * value_noise2(X, Y, seed, octaves=4, base_freq=3.0)
+    pos = np.stack([(X * 2 - 1) * half, (Y * 2 - 1) * half, Z], -1).reshape(-1, 3)
+    uv = np.stack([X * uv_repeat, Y * uv_repeat], -1).reshape(-1, 2).astype(np.float32)
+    i = np.arange(tiles)
+    I, J = np.meshgrid(i, i, indexing="xy")
+    v00 = (J * n + I).reshape(-1)
+    v10, v01, v11 = v00 + 1, v00 + n, v00 + n + 1
+    faces = np.concatenate([np.stack([v00, v10, v11], 1), np.stack([v00, v11, v01], 1)]).astype(np.int64)
+    fn = np.cross(pos[faces[:, 1]] - pos[faces[:, 0]], pos[faces[:, 2]] - pos[faces[:, 0]])
+    vn = np.zeros_like(pos)
+    for k in range(3):
+        for c in range(3):
+            vn[:, c] += np.bincount(faces[:, k], weights=fn[:, c], minlength=len(pos))
+    vn /= np.sqrt((vn * vn).sum(1, keepdims=True))
+    return _tris_from_indexed(pos.astype(np.float32), vn.astype(np.float32), uv, faces, material_id, True,
+                              shape_id)
+
+
+def procedural_textures_rgba8(n=64, size=1024, seed=21):
+    """n seeded RGBA8 textures (size x size): per texture a checker of a random
+    period blended with value noise between two random colours."""
+    rng = CounterRng(seed)
+    g = (np.arange(size) + 0.5) / size
+    X, Y = np.meshgrid(g, g, indexing="xy")
+    out = []
+    for t in range(n):
+        c0, c1 = rng.uniform(3, 0.05, 0.95), rng.uniform(3, 0.05, 0.95)
+        period = int(rng.uniform(1, 4, 33)[0])
+        mix = rng.uniform(1, 0.2, 0.8)[0]
+        checker = ((np.floor(X * period) + np.floor(Y * period)) % 2).astype(np.float64)
+        noise = 0.5 + 0.5 * value_noise2(X, Y, seed * 1000 + t, octaves=3, base_freq=6.0)
+        w = mix * checker + (1 - mix) * noise
+        rgb = c0[None, None, :] * (1 - w[..., None]) + c1[None, None, :] * w[..., None]
+        img = np.empty((size, size, 4), np.uint8)
+        img[..., :3] = np.clip(np.round(rgb * 255.0), 0, 255).astype(np.uint8)
+        img[..., 3] = 255
+        out.append(img)
+    return out
+
+
+def c5_scene(n_meshes=128, subdiv=6, n_textures=64, tex_size=1024, seed=5):
+    """Config-5 style scene: n_meshes displaced icospheres (as icosphere_field,
+    spread over a 40-unit box) on a 256 x 256-tile heightfield terrain, with
+    n_textures RGBA8 textures: the terrain (Lambert) and every other sphere
+    (Disney base colour) are textured.  Returns (triangles, materials,
+    textures, info)."""
+    tris, mats, info = icosphere_field(n_meshes=n_meshes, subdiv=subdiv, seed=seed, box=40.0, ground_half=1.0)
+    tris = tris[:-2]  # the field's ground quad is replaced by the terrain
+    mats = mats.copy()
+    for i in range(0, n_meshes, 2):
+        mats[1 + i]["TEXTURE_BASECOLOR_ID"] = (i // 2) % n_textures
+    mats[0] = make_material(LAMBERT, (0.7, 0.7, 0.7), tex=n_textures - 1)
+    terrain = heightfield_terrain(tiles=256, half=150.0, height=6.0, seed=seed + 1, material_id=0,
+                                  shape_id=n_meshes)
+    terrain["verts"][:, :3, 2] -= 8.0  # below the spheres (whose lowest point is z = 0)
+    tris = canonical(np.concatenate([tris, terrain]))
+    textures = procedural_textures_rgba8(n_textures, tex_size, seed + 2)
+    return tris, mats, textures, info
 
 
 def sky_environment(width=2048, height=1024, sun_peak=1e4, seed=3, sun_sigma_deg=1.0):

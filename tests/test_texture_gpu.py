@@ -95,3 +95,27 @@ def test_bilinear_reproduces_a_linear_ramp():
             assert np.all(np.abs(got - exp) <= 3 * sig + 2e-3), (x, y, got, exp, sig)
             checked += 1
     assert checked >= 9
+
+
+def test_scene_load_obj_renders_like_the_host_arrays(tmp_path):
+    """kgk_scene_load_obj (OBJ/MTL/PNG straight to the device) equals
+    kgk_load_obj + kgk_scene_create of the same files, frame for frame."""
+    import sys
+    from conftest import GOLDEN
+    sys.path.insert(0, GOLDEN)
+    import scene_files
+    from kagayaki_gb300 import ESTIMATOR_COMPAT, load_obj
+    path = scene_files.write_obj_scene(str(tmp_path))
+    scene_files.write_images(str(tmp_path))
+    hdr = str(tmp_path / "rle.hdr")
+    cam = camera_setup((0.5, 1.5, 14.0), 28.0, (0.0, 0.0, 0.0), 24)
+    with Scene.from_obj(path, hdr) as s:
+        s.build_bvh()
+        a, _ = s.render(cam, 24, 24, spp=4, estimator=ESTIMATOR_COMPAT, max_depth=4)
+        a = a.copy()
+    tris, mats, texs, env = load_obj(path, hdr)
+    with Scene(tris, mats, textures=texs, env=env) as s:
+        s.build_bvh()
+        b, _ = s.render(cam, 24, 24, spp=4, estimator=ESTIMATOR_COMPAT, max_depth=4)
+    assert np.array_equal(a, b)
+    assert a[..., :3].max() > 0
