@@ -204,7 +204,8 @@ __global__ void __launch_bounds__(128) k_extend(Params P, const int *__restrict_
     unsigned rays = 0;
     RayPre r;
     Trav c;
-    TravStack stk;
+    __shared__ uint2 s_stack[kSmemStack * kSmemStackStride];
+    TravStack stk{s_stack + threadIdx.x};
     TravStats st{0, 0, 0};
     while (true) {
         const unsigned idle = __ballot_sync(~0u, !active);
@@ -802,7 +803,8 @@ __global__ void __launch_bounds__(128) k_shadow(Params P, int cidx, int fidx, co
     unsigned rays = 0;
     RayPre r;
     Trav c;
-    TravStack stk;
+    __shared__ uint2 s_stack[kSmemStack * kSmemStackStride];
+    TravStack stk{s_stack + threadIdx.x};
     TravStats st{0, 0, 0};
     while (true) {
         const unsigned idle = __ballot_sync(~0u, !active);
