@@ -204,8 +204,7 @@ __global__ void __launch_bounds__(128) k_extend(Params P, const int *__restrict_
     unsigned rays = 0;
     RayPre r;
     Trav c;
-    __shared__ uint2 s_stack[kSmemStack * kSmemStackStride];
-    TravStack stk{s_stack + threadIdx.x};
+    TravStack stk;
     TravStats st{0, 0, 0};
     while (true) {
         const unsigned idle = __ballot_sync(~0u, !active);
@@ -803,8 +802,7 @@ __global__ void __launch_bounds__(128) k_shadow(Params P, int cidx, int fidx, co
     unsigned rays = 0;
     RayPre r;
     Trav c;
-    __shared__ uint2 s_stack[kSmemStack * kSmemStackStride];
-    TravStack stk{s_stack + threadIdx.x};
+    TravStack stk;
     TravStats st{0, 0, 0};
     while (true) {
         const unsigned idle = __ballot_sync(~0u, !active);

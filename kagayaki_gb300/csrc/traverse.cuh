@@ -297,14 +297,8 @@ __device__ __forceinline__ bool trace_any(const WideNode *__restrict__ nodes, un
 // ---------------------------------------------------------------------------
 // The stack lives in a separate local array (TravStack) so that the scalar
 // state stays in registers.
-// Shared-memory stack of the resumable traversal: entry i of thread t at
-// base[i * kSmemStackStride], base = stack + t, so a warp's accesses fall in
-// distinct banks whatever each lane's depth (128-thread CTAs, 8-byte entries).
-constexpr int kSmemStack = 24;        // entries per thread; an 8-wide BVH of 10^7 triangles is ~8-12 deep
-constexpr int kSmemStackStride = 128; // threads per CTA of the kernels that use it
 struct TravStack {
-    uint2 *base;
-    __device__ __forceinline__ uint2 &e(int i) { return base[i * kSmemStackStride]; }
+    uint2 e[kTravStack];
 };
 struct Trav {
     uint2 group;
@@ -338,7 +332,7 @@ __device__ __forceinline__ bool trav_step(const WideNode *__restrict__ nodes, un
         const unsigned base = c.group.x;
         c.group.y &= ~(1u << child_bit);
         if (c.group.y & 0xff000000u) {
-            if (c.sp < kSmemStack) stk.e(c.sp++) = c.group;
+            if (c.sp < kTravStack) stk.e[c.sp++] = c.group;
             else st.overflow = 1;
         }
         const unsigned slot = (unsigned)(child_bit - 24) ^ (r.oct_inv4 & 0xffu);
@@ -386,7 +380,7 @@ __device__ __forceinline__ bool trav_step(const WideNode *__restrict__ nodes, un
     }
     if ((c.group.y & 0xff000000u) == 0u) {
         if (c.sp == 0) return true;
-        c.group = stk.e(--c.sp);
+        c.group = stk.e[--c.sp];
     }
     return false;
 }
