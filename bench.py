@@ -196,13 +196,16 @@ def run_ours(args):
     launches = 0
     ext_ms = 0.0
     ext_rays = 0
+    stage_sum = {"extend": 0.0, "shade": 0.0, "shadow": 0.0, "tail": 0.0}
     for k in range(args.steps):
         img, st = scene.render(cam, W, H, frame_index=args.warmup + k, out=out_host, profile_stages=True, **kw)
         rays += st["rays_closest"] + st["rays_shadow"]
         dev_ms += st["ms_device"]
         launches += st["kernel_launches"]
         ext_ms += st["ms_extend"]
-        ext_rays += st["rays_closest"]
+        ext_rays += st["rays_closest"] - st["rays_tail"]  # the tail kernel's rays are not k_extend's
+        for key in stage_sum:
+            stage_sum[key] += st["ms_" + key]
     # end to end: host camera in, host frame out, wall clock
     t0 = time.perf_counter()
     e2e_rays = 0
@@ -226,8 +229,9 @@ def run_ours(args):
     # roofline of the traversal (extend) stage: algorithmic bytes per ray
     # (counted in the untimed counting pass) x rays of the timed frames /
     # the extend launches' event-timed duration in the timed frames
+    ext_rays_prof = prof["rays_closest"] - prof["rays_tail"]  # nodes / triangles are counted in k_extend only
     bytes_per_ray = (prof["nodes_visited"] * NODE_BYTES + prof["tris_tested"] * TRI_BYTES +
-                     prof["rays_closest"] * RAY_BYTES) / max(prof["rays_closest"], 1)
+                     ext_rays_prof * RAY_BYTES) / max(ext_rays_prof, 1)
     ext_s = ext_ms / 1e3
     achieved = bytes_per_ray * ext_rays / ext_s / 1e9 if ext_s > 0 else None
     n_ext = args.steps * prof["extend_launches"] if prof.get("extend_launches") else None
@@ -259,8 +263,7 @@ def run_ours(args):
                      "peak_source": peak_kind,
                      "bytes_per_ray": round(bytes_per_ray, 1),
                      "achieved_per_launch_bytes": round(bytes_per_ray * ext_rays / n_ext) if n_ext else None},
-        "stages_ms": {"extend": round(prof["ms_extend"], 2), "shade": round(prof["ms_shade"], 2),
-                      "shadow": round(prof["ms_shadow"], 2)},
+        "stages_ms": {k: round(v / args.steps, 2) for k, v in stage_sum.items()},
         "rays_per_step": int(rays / args.steps),
         "bvh": {"wide_nodes": bvh["n_wide_nodes"], "build_ms": round(bvh["ms_build"], 1)},
         "clocks": ck,

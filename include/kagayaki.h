@@ -150,6 +150,8 @@ typedef struct kgk_stats {
     double ms_shade;              /* shading stage device time (profile_stages)  */
     double ms_shadow;             /* shadow-ray stage device time (profile_stages) */
     uint64_t extend_launches;     /* closest-hit (extend) kernel launches        */
+    double ms_tail;               /* tail-kernel device time (profile_stages)    */
+    uint64_t rays_tail;           /* closest-hit rays traced by the tail kernel (part of rays_closest) */
 } kgk_stats;
 
 typedef struct kgk_bvh_info {

@@ -83,7 +83,9 @@ constexpr int kRefill = 8;
 // Cache record: raw query [13], T [3], path id (int bits), radiance before the
 // query vertex's scattering [3].
 constexpr int kQRec = 20;
-enum Stat { kRaysC = 0, kRaysS = 1, kOverflow = 2, kNodes = 3, kTris = 4, kNStat = 8 };
+enum Stat { kRaysC = 0, kRaysS = 1, kOverflow = 2, kNodes = 3, kTris = 4, kRaysT = 5, kNStat = 8 };
+// Paths few enough to finish in the tail kernel (one thread per path).
+constexpr int kTailPaths = 1 << 17;
 
 struct Params {
     DevScene sc;
@@ -581,15 +583,23 @@ __device__ __forceinline__ void write_cache_record(const Params &P, float *rec, 
     rec[17] = rad.x; rec[18] = rad.y; rec[19] = rad.z;
 }
 
-__device__ void shade_unbiased(const Params &P, int p, bool valid, int *next_q, int next_cnt, float4 *so0,
-                               float4 *sd0, float4 *sc0, float4 *so1, float4 *sd1, float4 *sc1) {
+// One unbiased shading event of path p (its hit is in P.hit): emission, the
+// cache decisions, Russian roulette, the two NEE samples (returned in `o` as
+// shadow-ray records, not traced) and the BSDF sample (path state updated).
+struct ShadeOut {
+    bool cont, f_pred, e_pred;
+    float3 spos, f_dir, f_c, e_dir, e_c;
+    float f_tmax;
+};
+
+__device__ __forceinline__ void shade_unbiased_core(const Params &P, int p, ShadeOut &out) {
     const DevScene &s = P.sc;
     bool cont = false, f_pred = false, e_pred = false;
     float3 spos = f3(0.0f, 0.0f, 0.0f), f_dir = spos, f_c = spos, e_dir = spos, e_c = spos;
     float f_tmax = 0.0f, npdf = 0.0f;
     float3 ndir = spos, T = spos;
     unsigned long long rs = 0;
-    if (valid) {
+    {
         const float4 o4 = P.o[p], d4 = P.d[p], h = P.hit[p];
         const float3 o = f3(o4), d = f3(d4);
         const float prev_pdf = d4.w;  // 0: no MIS (camera ray)
@@ -759,10 +769,77 @@ __device__ void shade_unbiased(const Params &P, int p, bool valid, int *next_q, 
         }
         P.rng[p] = rs;
     }
-    const int k = warp_append(&P.cnt[next_cnt], cont);
-    if (cont) next_q[k] = p;
-    push_shadow(P, so0, sd0, sc0, kSH0, f_pred, spos, f_dir, f_tmax, -1, f_c, p);
-    push_shadow(P, so1, sd1, sc1, kSH1, e_pred, spos, e_dir, kBigT, -1, e_c, p);
+    out.cont = cont;
+    out.f_pred = f_pred;
+    out.e_pred = e_pred;
+    out.spos = spos;
+    out.f_dir = f_dir;
+    out.f_c = f_c;
+    out.e_dir = e_dir;
+    out.e_c = e_c;
+    out.f_tmax = f_tmax;
+}
+
+__device__ void shade_unbiased(const Params &P, int p, bool valid, int *next_q, int next_cnt, float4 *so0,
+                               float4 *sd0, float4 *sc0, float4 *so1, float4 *sd1, float4 *sc1) {
+    ShadeOut o{};
+    if (valid) shade_unbiased_core(P, p, o);
+    const int k = warp_append(&P.cnt[next_cnt], o.cont);
+    if (o.cont) next_q[k] = p;
+    push_shadow(P, so0, sd0, sc0, kSH0, o.f_pred, o.spos, o.f_dir, o.f_tmax, -1, o.f_c, p);
+    push_shadow(P, so1, sd1, sc1, kSH1, o.e_pred, o.spos, o.e_dir, kBigT, -1, o.e_c, p);
+}
+
+// The tail of a wave: once few paths are alive, each thread carries one path
+// through all of its remaining bounces - closest hit, shading, then its
+// face-light and environment shadow rays in that order (the order of the
+// wavefront's passes, so the radiance sums are the same) - instead of four
+// kernel launches per bounce that each wait for their slowest ray.
+__global__ void __launch_bounds__(128) k_tail(Params P, const int *__restrict__ q, int qcnt_idx) {
+    const int n = P.cnt[qcnt_idx];
+    const DevScene &s = P.sc;
+    unsigned rays_c = 0, rays_s = 0, overflow = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int p = q[i];
+        for (;;) {
+            const float4 o4 = P.o[p], d4 = P.d[p];
+            const RayPre r = make_ray(f3(o4), f3(d4));
+            float bt = kBigT, u = 0.0f, v = 0.0f;
+            int bid = 0x7fffffff;
+            TravStats st{0, 0, 0};
+            const int slot = trace_closest<false>(s.nodes, (unsigned)s.n_nodes, s.tri_rec, (unsigned)s.n_tris, r, bt,
+                                                  bid, u, v, st);
+            P.hit[p] = slot < 0 ? make_float4(kBigT, 0.0f, 0.0f, __int_as_float(-1))
+                                : make_float4(bt, u, v, __int_as_float(bid));
+            ++rays_c;
+            ShadeOut so{};
+            shade_unbiased_core(P, p, so);
+            if (so.f_pred) {
+                const RayPre rs = make_ray(so.spos, so.f_dir);
+                if (!trace_any<false>(s.nodes, (unsigned)s.n_nodes, s.tri_rec, (unsigned)s.n_tris, rs, so.f_tmax, st)) {
+                    float4 rr = P.rad[p];
+                    rr.x += so.f_c.x; rr.y += so.f_c.y; rr.z += so.f_c.z;
+                    P.rad[p] = rr;
+                }
+                ++rays_s;
+            }
+            if (so.e_pred) {
+                const RayPre rs = make_ray(so.spos, so.e_dir);
+                if (!trace_any<false>(s.nodes, (unsigned)s.n_nodes, s.tri_rec, (unsigned)s.n_tris, rs, kBigT, st)) {
+                    float4 rr = P.rad[p];
+                    rr.x += so.e_c.x; rr.y += so.e_c.y; rr.z += so.e_c.z;
+                    P.rad[p] = rr;
+                }
+                ++rays_s;
+            }
+            overflow += st.overflow;
+            if (!so.cont) break;
+        }
+    }
+    warp_add_u64(&P.stats[kRaysC], rays_c);
+    warp_add_u64(&P.stats[kRaysS], rays_s);
+    warp_add_u64(&P.stats[kRaysT], rays_c);
+    warp_add_u64(&P.stats[kOverflow], overflow);
 }
 
 template <int kEst>
@@ -1077,7 +1154,7 @@ kgk_status kgk_render(kgk_scene *s, const kgk_camera *cam, const kgk_camera *pre
     // optional per-stage timing: an event before and after every stage launch
     const bool prof = cfg->profile_stages != 0;
     std::vector<cudaEvent_t> ev;
-    std::vector<int> ev_stage;  // 0 extend, 1 shade, 2 shadow
+    std::vector<int> ev_stage;  // 0 extend, 1 shade, 2 shadow, 3 tail
     auto stage_begin = [&](int stage) -> kgk_status {
         if (!prof) return KGK_OK;
         cudaEvent_t a;
@@ -1136,11 +1213,23 @@ kgk_status kgk_render(kgk_scene *s, const kgk_camera *cam, const kgk_camera *pre
             KGK_CUDA(cudaGetLastError());
             launches += 4;
             cur ^= 1;
-            if ((b & 3) == 3) {
+            // the unbiased estimator checks every bounce from the second on,
+            // to hand the last few paths to the tail kernel
+            const bool unbiased = cfg->estimator == KGK_ESTIMATOR_UNBIASED;
+            if ((b & 3) == 3 || (unbiased && b >= 1)) {
                 int alive = 0;
                 KGK_CUDA(cudaMemcpyAsync(&alive, R.cnt + cur, sizeof(int), cudaMemcpyDeviceToHost, st));
                 KGK_CUDA(cudaStreamSynchronize(st));
                 if (alive == 0) break;
+                if (unbiased && alive <= kTailPaths && b + 1 < max_bounces) {
+                    KGK_TRY(stage_begin(3));
+                    const int tg = std::max(1, std::min((alive + 127) / 128, R.sms * 16));
+                    k_tail<<<tg, 128, 0, st>>>(P, R.aq[cur], cur);
+                    KGK_TRY(stage_end());
+                    KGK_CUDA(cudaGetLastError());
+                    ++launches;
+                    break;
+                }
             }
         }
         if (P.use_cache) {
@@ -1205,7 +1294,7 @@ kgk_status kgk_render(kgk_scene *s, const kgk_camera *cam, const kgk_camera *pre
         stats->ms_device = ms;
         stats->kernel_launches = launches;
         stats->extend_launches = extend_launches;
-        double stage_ms[3] = {0, 0, 0};
+        double stage_ms[4] = {0, 0, 0, 0};
         for (size_t k = 0; k + 1 < ev.size(); k += 2) {
             float m = 0;
             cudaEventElapsedTime(&m, ev[k], ev[k + 1]);
@@ -1214,6 +1303,8 @@ kgk_status kgk_render(kgk_scene *s, const kgk_camera *cam, const kgk_camera *pre
         stats->ms_extend = stage_ms[0];
         stats->ms_shade = stage_ms[1];
         stats->ms_shadow = stage_ms[2];
+        stats->ms_tail = stage_ms[3];
+        stats->rays_tail = hs[kRaysT];
     }
     for (cudaEvent_t e : ev) cudaEventDestroy(e);
     if (cfg->use_cache) KGK_TRY(nrc_check_error(*s->nrc));

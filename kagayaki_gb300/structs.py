@@ -78,7 +78,8 @@ class KgkStats(ctypes.Structure):
                 ("tris_tested", ctypes.c_uint64), ("paths", ctypes.c_uint64),
                 ("ms_device", ctypes.c_double), ("kernel_launches", ctypes.c_uint64),
                 ("ms_extend", ctypes.c_double), ("ms_shade", ctypes.c_double),
-                ("ms_shadow", ctypes.c_double), ("extend_launches", ctypes.c_uint64)]
+                ("ms_shadow", ctypes.c_double), ("extend_launches", ctypes.c_uint64),
+                ("ms_tail", ctypes.c_double), ("rays_tail", ctypes.c_uint64)]
 
 
 class KgkBvhInfo(ctypes.Structure):
