@@ -547,6 +547,108 @@ def run_c5(args):
     print(json.dumps(line), flush=True)
 
 
+def run_c1(args, reference=False):
+    """The reference's CPU-runnable case: the 36-triangle Cornell box, 256 x 256,
+    16 spp, the reference's estimator (compat: one sample per pixel per pass
+    with its seed chain, Russian roulette only - the reference has no depth
+    cap).  Ours on the GPU, or (reference=True) the oracle port of the
+    reference's render on all host cores."""
+    from kagayaki_gb300 import ESTIMATOR_COMPAT, Scene, camera_array, camera_setup, scenes
+    tris, mats, c = scenes.cornell_box()
+    W = H = 256
+    spp = 16
+    cam = camera_setup(c["origin"], c["dist"], c["rot"], H)
+    if reference:
+        from oracle import orc
+        thr = os.cpu_count() or 1
+        ca = camera_array(cam)
+        orc.render_compat(tris, mats, ca, W, H, 1, threads=thr)  # warm-up
+        t0 = time.perf_counter()
+        rays = 0
+        for _ in range(args.steps):
+            _, n = orc.render_compat(tris, mats, ca, W, H, spp, threads=thr)
+            rays += n
+        secs = time.perf_counter() - t0
+        extra = {"impl": "reference",
+                 "cpu_baseline": {"value": round(rays / secs / 1e6, 3), "unit": "Mrays/s", "cores": thr,
+                                  "kind": "port", "sample": f"{args.steps} full frames"}}
+        ms = 1e3 * secs / args.steps
+    else:
+        scene = Scene(tris, mats)
+        scene.build_bvh()
+        out = np.empty((H, W, 4), np.float32)
+        for f in range(args.warmup):
+            scene.render(cam, W, H, spp=spp, estimator=ESTIMATOR_COMPAT, frame_index=f, out=out)
+        dev = 0.0
+        rays = 0
+        for f in range(args.steps):
+            _, st = scene.render(cam, W, H, spp=spp, estimator=ESTIMATOR_COMPAT, frame_index=args.warmup + f,
+                                 out=out)
+            dev += st["ms_device"]
+            rays += st["rays_closest"] + st["rays_shadow"]
+        scene.close()
+        secs = dev / 1e3
+        ms = dev / args.steps
+        extra = {}
+    line = {"metric": "Mrays/s", "value": round(rays / secs / 1e6, 3), "unit": "Mrays/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic seeded Cornell box",
+            "config": {"workload": "cornell-36tris-256x256-16spp-compat", "estimator": "reference (compat)",
+                       "depth": "Russian roulette only, as the reference"}}
+    line.update(extra)
+    print(json.dumps(line), flush=True)
+
+
+def run_c4(args):
+    """The cache along the SVGF orbit's cameras: 1920 x 1080, 1 spp, 60 frames,
+    online training (65,536 paths per frame); plain 1-spp frames and plain
+    frames of the same device time rendered beside it; relMSE at frames 20,
+    40 and 60 against 4096-spp FP64-accumulated references."""
+    from kagayaki_gb300 import ESTIMATOR_UNBIASED, Scene
+    tris, mats, env, info = build_workload()
+    W, H = args.width or 1920, args.height or 1080
+    frames = 60
+    evals = (19, 39, 59)
+    scene = Scene(tris, mats, env=env)
+    scene.build_bvh()
+    kw = dict(max_depth=WORKLOAD["max_depth"], estimator=ESTIMATOR_UNBIASED)
+    out = np.empty((H, W, 4), np.float32)
+    imgs = {}
+    times = {}
+    for mode in ("plain", "cache"):
+        if mode == "cache":
+            scene.cache_init(seed=1)
+        dev = 0.0
+        for f in range(frames):
+            img, st = scene.render(orbit_camera(f, H), W, H, spp=1, seed=3, frame_index=f, use_cache=mode == "cache",
+                                   out=out, **kw)
+            dev += st["ms_device"]
+            if f in evals:
+                imgs[(mode, f)] = img[..., :3].astype(np.float64)
+        times[mode] = dev / frames
+    res = []
+    for f in evals:
+        cam = orbit_camera(f, H)
+        scene.accum_reset(W, H)
+        for k in range(64):
+            scene.render(cam, W, H, spp=64, seed=7, frame_index=700_000 + 100 * f + k, accumulate=True, out=out, **kw)
+        ref, _, nref = scene.accum_read(W, H)
+        spp_eq = max(1, int(round(times["cache"] / times["plain"])))
+        eq, _ = scene.render(cam, W, H, spp=spp_eq, seed=9, frame_index=800_000 + f, out=out, **kw)
+        res.append({"frame": f + 1, "plain_1spp": round(rel_mse(imgs[("plain", f)], ref), 4),
+                    "cache_1spp": round(rel_mse(imgs[("cache", f)], ref), 4),
+                    "plain_equal_time": round(rel_mse(eq[..., :3].astype(np.float64), ref), 4),
+                    "plain_equal_time_spp": spp_eq})
+    scene.close()
+    line = {"metric": "frames/s", "value": round(1e3 / times["cache"], 2), "unit": "frames/s", "n_gpus": 1,
+            "steps": frames, "warmup": 0, "ms_per_step": round(times["cache"], 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 (cache MLP bf16)", "data": "synthetic seeded scene",
+            "config": {"workload": "cache-orbit-1080p-1spp", "frames": frames, "cache": "width 64, 65,536 training paths"},
+            "plain_frames_per_s": round(1e3 / times["plain"], 2),
+            "relmse": res}
+    print(json.dumps(line), flush=True)
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -584,19 +686,26 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
     ap.add_argument("--no-relmse", action="store_true", help="skip the plain-vs-cache relMSE study")
     ap.add_argument("--wave-paths", type=int, default=0, help="paths per wave (0 = the library default)")
-    ap.add_argument("--workload", default="frame", choices=["frame", "svgf-orbit", "mlp", "c5"],
-                    help="frame: the 64-spp Mrays/s benchmark; svgf-orbit: 60 frames at 1 spp + SVGF; "
-                         "mlp: the radiance-cache network alone; c5: 10.6M triangles, 4K, textures, cache")
+    ap.add_argument("--workload", default="frame", choices=["frame", "c1", "svgf-orbit", "c4", "mlp", "c5"],
+                    help="frame: the 64-spp Mrays/s benchmark; c1: the Cornell box with the reference's "
+                         "estimator (also with --impl reference); svgf-orbit: 60 frames at 1 spp + SVGF; c4: the "
+                         "cache along the orbit; mlp: the radiance-cache network alone; c5: 10.6M triangles, 4K, "
+                         "textures, cache")
     ap.add_argument("--width", type=int, default=0, help="override the frame width (profiling cases)")
     ap.add_argument("--height", type=int, default=0, help="override the frame height")
     ap.add_argument("--spp", type=int, default=0, help="override the samples per pixel")
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.workload == "c1":
+        if int(os.environ.get("RANK", "0")) == 0:
+            run_c1(args, reference=args.impl == "reference")
+    elif args.impl == "reference":
         run_reference(args)
     elif args.workload == "svgf-orbit":
         run_svgf_orbit(args)
     elif args.workload == "mlp":
         run_mlp(args)
+    elif args.workload == "c4":
+        run_c4(args)
     elif args.workload == "c5":
         run_c5(args)
     else:
