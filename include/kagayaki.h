@@ -141,8 +141,9 @@ typedef struct kgk_stats {
     uint64_t rays_closest;        /* primary + extension rays                    */
     uint64_t rays_shadow;         /* shadow / occlusion rays                     */
     uint64_t traversal_overflows; /* rays whose traversal stack overflowed      */
-    uint64_t nodes_visited;       /* wide nodes intersected (count_work only)   */
-    uint64_t tris_tested;         /* triangles tested (count_work only)         */
+    uint64_t nodes_visited;       /* wide nodes intersected by the wavefront's closest-hit
+                                     rays (count_work only; not the tail kernel's) */
+    uint64_t tris_tested;         /* triangles tested, likewise                 */
     uint64_t paths;               /* camera paths traced                         */
     double ms_device;             /* device time of the call (CUDA events)       */
     uint64_t kernel_launches;     /* kernels this call launched                  */

@@ -336,8 +336,19 @@ __device__ __forceinline__ void write_gbuffer(const Params &P, int px, const Sur
 // ---------------------------------------------------------------------------
 // compat shade: RayTrace.cuh:37-106 for one vertex
 // ---------------------------------------------------------------------------
-__device__ void shade_compat(const Params &P, int p, bool valid, int *next_q, int next_cnt, float4 *so0,
-                             float4 *sd0, float4 *sc0, float4 *so1, float4 *sd1, float4 *sc1) {
+// Result of one shading event: whether the path continues (its state is
+// updated in place) and its shadow-ray records (face light: origin, direction,
+// range, light id for the reference's closest-hit test or -1 for an occlusion
+// test; environment: from spos), which the caller traces or queues.
+struct ShadeOut {
+    bool cont, f_pred, e_pred;
+    float3 spos, f_org, f_dir, f_c, e_dir, e_c;
+    float f_tmax;
+    int f_light;
+};
+
+// One shading event of path p in the reference's estimator (see shade_unbiased_core).
+__device__ __forceinline__ void shade_compat_core(const Params &P, int p, ShadeOut &out) {
     const DevScene &s = P.sc;
     bool cont = false;
     bool f_pred = false, e_pred = false;
@@ -346,7 +357,7 @@ __device__ void shade_compat(const Params &P, int p, bool valid, int *next_q, in
     int f_light = -1;
     float3 npos, ndir, T;
     unsigned long long rs = 0;
-    if (valid) {
+    {
         const float4 o4 = P.o[p], d4 = P.d[p], h = P.hit[p];
         const float3 o = f3(o4), d = f3(d4);
         T = f3(P.thr[p]);
@@ -531,10 +542,27 @@ __device__ void shade_compat(const Params &P, int p, bool valid, int *next_q, in
         P.rng[p] = rs;
         if (!cont) P.seeds[px] = rs;  // randSeeds[pos] = rand.seed (render.cuh:42)
     }
-    const int k = warp_append(&P.cnt[next_cnt], cont);
-    if (cont) next_q[k] = p;
-    push_shadow(P, so0, sd0, sc0, kSH0, f_pred, f_org, f_dir, f_tmax, f_light, f_c, p);
-    push_shadow(P, so1, sd1, sc1, kSH1, e_pred, npos, e_dir, kBigT, -1, e_c, p);
+    out.cont = cont;
+    out.f_pred = f_pred;
+    out.e_pred = e_pred;
+    out.spos = npos;
+    out.f_org = f_org;
+    out.f_dir = f_dir;
+    out.f_c = f_c;
+    out.e_dir = e_dir;
+    out.e_c = e_c;
+    out.f_tmax = f_tmax;
+    out.f_light = f_light;
+}
+
+__device__ void shade_compat(const Params &P, int p, bool valid, int *next_q, int next_cnt, float4 *so0,
+                             float4 *sd0, float4 *sc0, float4 *so1, float4 *sd1, float4 *sc1) {
+    ShadeOut o{};
+    if (valid) shade_compat_core(P, p, o);
+    const int k = warp_append(&P.cnt[next_cnt], o.cont);
+    if (o.cont) next_q[k] = p;
+    push_shadow(P, so0, sd0, sc0, kSH0, o.f_pred, o.f_org, o.f_dir, o.f_tmax, o.f_light, o.f_c, p);
+    push_shadow(P, so1, sd1, sc1, kSH1, o.e_pred, o.spos, o.e_dir, kBigT, -1, o.e_c, p);
 }
 
 // ---------------------------------------------------------------------------
@@ -586,12 +614,6 @@ __device__ __forceinline__ void write_cache_record(const Params &P, float *rec, 
 // One unbiased shading event of path p (its hit is in P.hit): emission, the
 // cache decisions, Russian roulette, the two NEE samples (returned in `o` as
 // shadow-ray records, not traced) and the BSDF sample (path state updated).
-struct ShadeOut {
-    bool cont, f_pred, e_pred;
-    float3 spos, f_dir, f_c, e_dir, e_c;
-    float f_tmax;
-};
-
 __device__ __forceinline__ void shade_unbiased_core(const Params &P, int p, ShadeOut &out) {
     const DevScene &s = P.sc;
     bool cont = false, f_pred = false, e_pred = false;
@@ -778,6 +800,8 @@ __device__ __forceinline__ void shade_unbiased_core(const Params &P, int p, Shad
     out.e_dir = e_dir;
     out.e_c = e_c;
     out.f_tmax = f_tmax;
+    out.f_org = spos;
+    out.f_light = -1;
 }
 
 __device__ void shade_unbiased(const Params &P, int p, bool valid, int *next_q, int next_cnt, float4 *so0,
@@ -790,18 +814,22 @@ __device__ void shade_unbiased(const Params &P, int p, bool valid, int *next_q, 
     push_shadow(P, so1, sd1, sc1, kSH1, o.e_pred, o.spos, o.e_dir, kBigT, -1, o.e_c, p);
 }
 
-// The tail of a wave: once few paths are alive, each thread carries one path
-// through all of its remaining bounces - closest hit, shading, then its
-// face-light and environment shadow rays in that order (the order of the
-// wavefront's passes, so the radiance sums are the same) - instead of four
-// kernel launches per bounce that each wait for their slowest ray.
-__global__ void __launch_bounds__(128) k_tail(Params P, const int *__restrict__ q, int qcnt_idx) {
-    const int n = P.cnt[qcnt_idx];
+// The tail of a wave: once few paths are alive (or the whole wave is small),
+// each thread carries one path through all of its remaining bounces - closest
+// hit, shading, then its face-light and environment shadow rays in that order
+// (the order of the wavefront's passes, so the radiance sums are the same) -
+// instead of four kernel launches per bounce that each wait for their slowest
+// ray.  q == nullptr: paths 0..dense_n-1 from their primary rays.  A path
+// runs at most `bounces` more bounces, the wavefront's bounce limit.
+template <int kEst>
+__global__ void __launch_bounds__(128) k_tail(Params P, const int *__restrict__ q, int qcnt_idx, int dense_n,
+                                              int bounces) {
+    const int n = q ? P.cnt[qcnt_idx] : dense_n;
     const DevScene &s = P.sc;
     unsigned rays_c = 0, rays_s = 0, overflow = 0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const int p = q[i];
-        for (;;) {
+        const int p = q ? q[i] : i;
+        for (int k = 0; k < bounces; ++k) {
             const float4 o4 = P.o[p], d4 = P.d[p];
             const RayPre r = make_ray(f3(o4), f3(d4));
             float bt = kBigT, u = 0.0f, v = 0.0f;
@@ -813,10 +841,22 @@ __global__ void __launch_bounds__(128) k_tail(Params P, const int *__restrict__ 
                                 : make_float4(bt, u, v, __int_as_float(bid));
             ++rays_c;
             ShadeOut so{};
-            shade_unbiased_core(P, p, so);
+            if (kEst == KGK_ESTIMATOR_COMPAT) shade_compat_core(P, p, so);
+            else shade_unbiased_core(P, p, so);
             if (so.f_pred) {
-                const RayPre rs = make_ray(so.spos, so.f_dir);
-                if (!trace_any<false>(s.nodes, (unsigned)s.n_nodes, s.tri_rec, (unsigned)s.n_tris, rs, so.f_tmax, st)) {
+                const RayPre rs = make_ray(so.f_org, so.f_dir);
+                bool vis;
+                if (so.f_light >= 0) {  // the reference's test: the closest hit is the light
+                    float lt = so.f_tmax, lu, lv;
+                    int lid = 0x7fffffff;
+                    const int ls = trace_closest<false>(s.nodes, (unsigned)s.n_nodes, s.tri_rec, (unsigned)s.n_tris,
+                                                        rs, lt, lid, lu, lv, st);
+                    vis = ls >= 0 && lid == so.f_light;
+                } else {
+                    vis = !trace_any<false>(s.nodes, (unsigned)s.n_nodes, s.tri_rec, (unsigned)s.n_tris, rs,
+                                            so.f_tmax, st);
+                }
+                if (vis) {
                     float4 rr = P.rad[p];
                     rr.x += so.f_c.x; rr.y += so.f_c.y; rr.z += so.f_c.z;
                     P.rad[p] = rr;
@@ -1183,8 +1223,21 @@ kgk_status kgk_render(kgk_scene *s, const kgk_camera *cam, const kgk_camera *pre
         }
         k_raygen<<<grid, 128, 0, st>>>(P);
         ++launches;
+        // a small wave (the reference's estimator renders one sample per
+        // pixel per wave) runs in the tail kernel from its primary rays
+        if (n <= kTailPaths) {
+            KGK_TRY(stage_begin(3));
+            const int tg = std::max(1, std::min((n + 127) / 128, R.sms * 16));
+            if (cfg->estimator == KGK_ESTIMATOR_COMPAT)
+                k_tail<KGK_ESTIMATOR_COMPAT><<<tg, 128, 0, st>>>(P, nullptr, 0, n, max_bounces);
+            else
+                k_tail<KGK_ESTIMATOR_UNBIASED><<<tg, 128, 0, st>>>(P, nullptr, 0, n, max_bounces);
+            KGK_TRY(stage_end());
+            KGK_CUDA(cudaGetLastError());
+            ++launches;
+        }
         int cur = 0;
-        for (int b = 0; b < max_bounces; ++b) {
+        for (int b = 0; b < max_bounces && n > kTailPaths; ++b) {
             KGK_CUDA(cudaMemsetAsync(R.cnt + kSQ0, 0, (kFS1 + 1 - kSQ0) * sizeof(int), st));
             KGK_CUDA(cudaMemsetAsync(R.cnt + (cur ^ 1), 0, sizeof(int), st));
             const int *q = b == 0 ? nullptr : R.aq[cur];
@@ -1213,18 +1266,21 @@ kgk_status kgk_render(kgk_scene *s, const kgk_camera *cam, const kgk_camera *pre
             KGK_CUDA(cudaGetLastError());
             launches += 4;
             cur ^= 1;
-            // the unbiased estimator checks every bounce from the second on,
+            // from the second bounce on, check the alive count every bounce,
             // to hand the last few paths to the tail kernel
-            const bool unbiased = cfg->estimator == KGK_ESTIMATOR_UNBIASED;
-            if ((b & 3) == 3 || (unbiased && b >= 1)) {
+            if (b >= 1) {
                 int alive = 0;
                 KGK_CUDA(cudaMemcpyAsync(&alive, R.cnt + cur, sizeof(int), cudaMemcpyDeviceToHost, st));
                 KGK_CUDA(cudaStreamSynchronize(st));
                 if (alive == 0) break;
-                if (unbiased && alive <= kTailPaths && b + 1 < max_bounces) {
+                if (alive <= kTailPaths && b + 1 < max_bounces) {
                     KGK_TRY(stage_begin(3));
                     const int tg = std::max(1, std::min((alive + 127) / 128, R.sms * 16));
-                    k_tail<<<tg, 128, 0, st>>>(P, R.aq[cur], cur);
+                    if (cfg->estimator == KGK_ESTIMATOR_COMPAT)
+                        k_tail<KGK_ESTIMATOR_COMPAT><<<tg, 128, 0, st>>>(P, R.aq[cur], cur, 0, max_bounces - b - 1);
+                    else
+                        k_tail<KGK_ESTIMATOR_UNBIASED><<<tg, 128, 0, st>>>(P, R.aq[cur], cur, 0,
+                                                                          max_bounces - b - 1);
                     KGK_TRY(stage_end());
                     KGK_CUDA(cudaGetLastError());
                     ++launches;

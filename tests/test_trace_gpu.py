@@ -123,3 +123,36 @@ def test_displaced_icosphere_field_full_size_property():
     hit = (oids >= 0) & (ids == oids)
     rel = np.abs(t[hit] - ot[hit]) / ot[hit]
     assert np.quantile(rel, 0.9999) <= T_REL_TOL
+
+
+def test_watertight_closed_mesh():
+    """Rays from inside a closed, displaced icosphere aimed exactly at its
+    vertices and at the midpoints of its edges (where two or more triangles
+    meet) must all hit: the edge functions of neighbouring triangles are
+    computed with explicit rounding, so no ray slips through a shared edge."""
+    v, f = scenes.icosphere(4)
+    rng = np.random.default_rng(8)
+    v = (v * (1.0 + 0.03 * rng.uniform(-1, 1, (len(v), 1)))).astype(np.float32)
+    uv = np.zeros((len(v), 2), np.float32)
+    tris = scenes.canonical(scenes._tris_from_indexed(v, v, uv, f.astype(np.int64), 0, False, 0))
+    mats = np.stack([structs_lambert()])
+    edges = np.concatenate([f[:, [0, 1]], f[:, [1, 2]], f[:, [2, 0]]])
+    mids = (v[edges[:, 0]].astype(np.float64) + v[edges[:, 1]].astype(np.float64)) / 2
+    targets = np.concatenate([v.astype(np.float64), mids])
+    origins = rng.uniform(-0.2, 0.2, (len(targets), 3))
+    d = targets - origins
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    rays = np.zeros(len(targets), dtype=scenes.RAY)
+    rays["dir"][:, :3] = d.astype(np.float32)
+    rays["org"][:, :3] = origins.astype(np.float32)
+    with Scene(tris, mats) as s:
+        s.build_bvh()
+        ids, t = s.trace_closest(rays)
+        occ = s.trace_any(rays)
+    assert (ids >= 0).all(), f"{int((ids < 0).sum())} of {len(ids)} rays leaked"
+    assert occ.all()
+
+
+def structs_lambert():
+    from kagayaki_gb300 import structs
+    return structs.make_material(structs.LAMBERT, (0.5, 0.5, 0.5))
