@@ -219,6 +219,31 @@ typedef struct kgk_host_scene {
 kgk_status kgk_load_obj(const char *obj_path, const char *hdr_path, kgk_host_scene *out);
 void kgk_host_scene_free(kgk_host_scene *scene);
 
+/* Loading options (no counterpart in the reference, whose load_object has
+ * none).  material_model: KGK_MATERIALS_REFERENCE converts every MTL material
+ * as load_object does (Lambert, IO_load_WavefrontObj.cuh:90-124);
+ * KGK_MATERIALS_PBR makes a material that has any key of the MTL PBR
+ * extension (Pr, Pm, Ps, Pc, Pcr, aniso) a Disney material: roughness Pr,
+ * metallic Pm, sheen Ps, clearcoat Pc, clearcoat gloss 1 - Pcr, anisotropic
+ * aniso (each clamped to [0,1]), base colour Kd / map_Kd, emission Ke,
+ * specular ((Ni-1)/(Ni+1))^2 / 0.08 clamped (0.5 without Ni); the others stay
+ * as the reference converts them.  threads: parse and conversion threads
+ * (0 = all hardware threads, at most 64); the result is the same for every
+ * thread count.  A NULL options pointer means all zeros. */
+typedef enum kgk_material_model {
+    KGK_MATERIALS_REFERENCE = 0,
+    KGK_MATERIALS_PBR = 1
+} kgk_material_model;
+
+typedef struct kgk_load_options {
+    int32_t material_model;
+    int32_t threads;
+    int32_t reserved[6];
+} kgk_load_options;
+
+kgk_status kgk_load_obj_ex(const char *obj_path, const char *hdr_path, const kgk_load_options *options,
+                           kgk_host_scene *out);
+
 /* stbi_loadf (FileIO/IO_load_images.cuh:10): the image as float pixels with
  * its own channel count; 8-bit colour channels (v/255)^2.2, alpha v/255, .hdr
  * as stored.  Free with kgk_image_free. */
@@ -228,6 +253,8 @@ void kgk_image_free(kgk_texture *image);
 /* kgk_load_obj followed by kgk_scene_create (render_prepare's load_object +
  * load_HDR, render_prepare.cuh:35-37). */
 kgk_status kgk_scene_load_obj(const char *obj_path, const char *hdr_path, kgk_scene **out);
+kgk_status kgk_scene_load_obj_ex(const char *obj_path, const char *hdr_path, const kgk_load_options *options,
+                                 kgk_scene **out);
 
 /* An 8-bit RGBA texture, 4 bytes per texel, rows from the top.  Kept as bytes
  * on the device (a quarter of the float texture's memory); a colour channel v

@@ -25,6 +25,7 @@ PROTOTYPES = {
     "kgk_set_device": (_st, [ctypes.c_int]),
     "kgk_scene_create": (_st, [_vp, _sz, _vp, _sz, _vp, _sz, _vp, ctypes.POINTER(_vp)]),
     "kgk_scene_load_obj": (_st, [ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(_vp)]),
+    "kgk_scene_load_obj_ex": (_st, [ctypes.c_char_p, ctypes.c_char_p, _vp, ctypes.POINTER(_vp)]),
     "kgk_scene_destroy": (None, [_vp]),
     "kgk_build_bvh": (_st, [_vp, ctypes.POINTER(KgkBvhInfo)]),
     "kgk_bvh_validate": (_st, [_vp]),
@@ -47,6 +48,7 @@ PROTOTYPES = {
     "kgk_nrc_loss_scale": (_st, [_vp, _vp]),
     "kgk_scene_set_textures_rgba8": (_st, [_vp, _vp, _sz]),
     "kgk_load_obj": (_st, [ctypes.c_char_p, ctypes.c_char_p, _vp]),
+    "kgk_load_obj_ex": (_st, [ctypes.c_char_p, ctypes.c_char_p, _vp, _vp]),
     "kgk_host_scene_free": (None, [_vp]),
     "kgk_load_image": (_st, [ctypes.c_char_p, _vp]),
     "kgk_image_free": (None, [_vp]),

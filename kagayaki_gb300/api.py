@@ -16,8 +16,9 @@ import numpy as np
 
 from . import _lib
 from ._lib import KgkError, check, lib
-from .structs import (MATERIAL, RAY, TRIANGLE, KgkBvhInfo, KgkCamera, KgkHostScene, KgkNrcConfig,
-                      KgkRenderConfig, KgkStats, KgkSvgfConfig, KgkTexture, KgkTextureRGBA8, KgkVec)
+from .structs import (MATERIAL, MATERIALS_PBR, MATERIALS_REFERENCE, RAY, TRIANGLE, KgkBvhInfo,  # noqa: F401
+                      KgkCamera, KgkHostScene, KgkLoadOptions, KgkNrcConfig, KgkRenderConfig, KgkStats,
+                      KgkSvgfConfig, KgkTexture, KgkTextureRGBA8, KgkVec)
 
 ESTIMATOR_COMPAT = 0
 ESTIMATOR_UNBIASED = 1
@@ -70,13 +71,14 @@ class Scene:
         self.bvh = None
 
     @classmethod
-    def from_obj(cls, obj_path, hdr_path=None):
-        """kgk_scene_load_obj: an OBJ scene (and environment) straight to the device."""
+    def from_obj(cls, obj_path, hdr_path=None, materials=MATERIALS_REFERENCE, threads=0):
+        """kgk_scene_load_obj_ex: an OBJ scene (and environment) straight to the device."""
         self = cls.__new__(cls)
         self._h = ctypes.c_void_p()
         self._keep = []
-        check(lib().kgk_scene_load_obj(str(obj_path).encode(), str(hdr_path).encode() if hdr_path else None,
-                                       ctypes.byref(self._h)))
+        opt = _load_options(materials, threads)
+        check(lib().kgk_scene_load_obj_ex(str(obj_path).encode(), str(hdr_path).encode() if hdr_path else None,
+                                          ctypes.byref(opt), ctypes.byref(self._h)))
         self.n_triangles = None
         self.bvh = None
         return self
@@ -191,18 +193,32 @@ def load_image(path):
         lib().kgk_image_free(ctypes.byref(t))
 
 
-def load_obj(obj_path, hdr_path=None):
+def _host_array(ptr, n, dtype):
+    """A numpy copy of n records of dtype at the library-owned host pointer."""
+    raw = (ctypes.c_uint8 * (n * dtype.itemsize)).from_address(ptr)
+    return np.frombuffer(raw, np.uint8).view(dtype).copy()
+
+
+def _load_options(materials, threads):
+    opt = KgkLoadOptions()
+    opt.material_model = int(materials)
+    opt.threads = int(threads)
+    return opt
+
+
+def load_obj(obj_path, hdr_path=None, materials=MATERIALS_REFERENCE, threads=0):
     """load_object + load_Textures + load_HDR (FileIO/IO_load_WavefrontObj.cuh:10-127,
-    FileIO/IO_load_images.cuh:9-29).  Returns (triangles, materials,
-    [texture arrays], environment array or None)."""
+    FileIO/IO_load_images.cuh:9-29), through kgk_load_obj_ex.  materials:
+    MATERIALS_REFERENCE (the reference's Lambert conversion) or MATERIALS_PBR
+    (Disney from the MTL PBR keys); threads: 0 = all host threads.  Returns
+    (triangles, materials, [texture arrays], environment array or None)."""
     hs = KgkHostScene()
-    check(lib().kgk_load_obj(str(obj_path).encode(), str(hdr_path).encode() if hdr_path else None,
-                             ctypes.byref(hs)))
+    opt = _load_options(materials, threads)
+    check(lib().kgk_load_obj_ex(str(obj_path).encode(), str(hdr_path).encode() if hdr_path else None,
+                                ctypes.byref(opt), ctypes.byref(hs)))
     try:
-        tris = np.frombuffer(ctypes.string_at(hs.triangles, hs.n_triangles * TRIANGLE.itemsize),
-                             TRIANGLE).copy()
-        mats = np.frombuffer(ctypes.string_at(hs.materials, hs.n_materials * MATERIAL.itemsize),
-                             MATERIAL).copy()
+        tris = _host_array(hs.triangles, hs.n_triangles, TRIANGLE)
+        mats = _host_array(hs.materials, hs.n_materials, MATERIAL)
         texs = [_texture_array(hs.textures[i]) for i in range(hs.n_textures)]
         env = _texture_array(hs.hdr)
         return tris, mats, texs, env

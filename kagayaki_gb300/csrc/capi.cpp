@@ -19,6 +19,7 @@ static thread_local std::string g_last_error;
 static thread_local int g_device = 0;
 
 void set_error(const std::string &msg) { g_last_error = msg; }
+const std::string &last_error_message() { return g_last_error; }
 kgk_status fail(kgk_status st, const std::string &msg) {
     g_last_error = msg;
     return st;

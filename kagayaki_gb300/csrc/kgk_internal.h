@@ -106,6 +106,7 @@ struct DevScene {
 // Error handling inside the library: every failure records a message.
 // ---------------------------------------------------------------------------
 void set_error(const std::string &msg);
+const std::string &last_error_message();  // this thread's last error
 kgk_status fail(kgk_status st, const std::string &msg);
 kgk_status cuda_fail(cudaError_t e, const char *what);
 

@@ -34,9 +34,11 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <atomic>
 #include <map>
 #include <set>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "kgk_scene.h"
@@ -178,10 +180,6 @@ bool parse_triple(const char **t, int nv, int nvn, int nvt, VIdx *r) {
     return true;
 }
 
-struct Face {
-    std::vector<VIdx> vi;
-    unsigned smooth = 0;
-};
 struct Tri {
     VIdx a, b, c;
     int mat;
@@ -196,6 +194,10 @@ struct MtlMaterial {
     std::string name;
     float diffuse[3] = {0, 0, 0}, specular[3] = {0, 0, 0}, emission[3] = {0, 0, 0};
     float ior = 1.0f, roughness = 0.0f, metallic = 0.0f;
+    // PBR extension (Pr / Pm above, and Ps, Pc, Pcr, aniso): read for the
+    // Disney mapping only; has_pbr = any of Pr, Pm, Ps, Pc, Pcr, aniso given
+    float sheen = 0.0f, clearcoat = 0.0f, clearcoat_roughness = 0.0f, anisotropy = 0.0f;
+    bool has_pbr = false, has_ni = false;
     std::string diffuse_tex;
 };
 
@@ -222,6 +224,16 @@ struct Lines {
 bool read_text(const std::string &path, std::string &out) {
     FILE *f = fopen(path.c_str(), "rb");
     if (!f) return false;
+    // one read of the whole file when its size is known, then whatever follows
+    if (fseek(f, 0, SEEK_END) == 0) {
+        const long size = ftell(f);
+        if (size > 0 && fseek(f, 0, SEEK_SET) == 0) {
+            out.resize((size_t)size);
+            out.resize(fread(&out[0], 1, (size_t)size, f));
+        } else {
+            fseek(f, 0, SEEK_SET);
+        }
+    }
     char buf[1 << 16];
     size_t n;
     while ((n = fread(buf, 1, sizeof buf, f)) > 0) out.append(buf, n);
@@ -263,9 +275,23 @@ void parse_mtl(const std::string &text, std::vector<MtlMaterial> &mats, std::map
         if (t[0] == 'K' && t[1] == 'd' && is_space(t[2])) { rgb(m.diffuse); has_kd = true; continue; }
         if (t[0] == 'K' && t[1] == 's' && is_space(t[2])) { rgb(m.specular); continue; }
         if (t[0] == 'K' && t[1] == 'e' && is_space(t[2])) { rgb(m.emission); continue; }
-        if (t[0] == 'N' && t[1] == 'i' && is_space(t[2])) { t += 2; m.ior = read_real(&t); continue; }
-        if (t[0] == 'P' && t[1] == 'r' && is_space(t[2])) { t += 2; m.roughness = read_real(&t); continue; }
-        if (t[0] == 'P' && t[1] == 'm' && is_space(t[2])) { t += 2; m.metallic = read_real(&t); continue; }
+        if (t[0] == 'N' && t[1] == 'i' && is_space(t[2])) { t += 2; m.ior = read_real(&t); m.has_ni = true; continue; }
+        if (t[0] == 'P' && t[1] == 'r' && is_space(t[2])) { t += 2; m.roughness = read_real(&t); m.has_pbr = true; continue; }
+        if (t[0] == 'P' && t[1] == 'm' && is_space(t[2])) { t += 2; m.metallic = read_real(&t); m.has_pbr = true; continue; }
+        if (t[0] == 'P' && t[1] == 's' && is_space(t[2])) { t += 2; m.sheen = read_real(&t); m.has_pbr = true; continue; }
+        if (t[0] == 'P' && t[1] == 'c' && is_space(t[2])) { t += 2; m.clearcoat = read_real(&t); m.has_pbr = true; continue; }
+        if (!strncmp(t, "Pcr", 3) && is_space(t[3])) {
+            t += 3;
+            m.clearcoat_roughness = read_real(&t);
+            m.has_pbr = true;
+            continue;
+        }
+        if (!strncmp(t, "aniso", 5) && is_space(t[5])) {
+            t += 5;
+            m.anisotropy = read_real(&t);
+            m.has_pbr = true;
+            continue;
+        }
         if (!strncmp(t, "map_Kd", 6) && is_space(t[6])) {
             t += 7;
             // texture options (-name values) precede the file name, which runs to the line end
@@ -310,17 +336,19 @@ int pnpoly3(const float *vx, const float *vy, float tx, float ty) {
     return c;
 }
 
-// Emits the triangles of one polygon (tinyobjloader's "simple" triangulation).
-void triangulate(const Face &f, int mat, const std::vector<float> &v, std::vector<Tri> &out) {
-    const size_t n = f.vi.size();
+// Emits the triangles of one polygon (tinyobjloader's "simple" triangulation)
+// of n corners.  Only the first `vsize` floats of v (the vertices read before
+// the polygon's group ended) are visible to it.
+void triangulate(const VIdx *fv, size_t n, unsigned smooth, int mat, const std::vector<float> &v, size_t vsize,
+                 std::vector<Tri> &out) {
     if (n < 3) return;
     if (n == 3) {
-        out.push_back({f.vi[0], f.vi[1], f.vi[2], mat, f.smooth});
+        out.push_back({fv[0], fv[1], fv[2], mat, smooth});
         return;
     }
-    auto valid = [&](const VIdx &x) { return x.v >= 0 && (size_t)(3 * x.v + 2) < v.size(); };
+    auto valid = [&](const VIdx &x) { return x.v >= 0 && (size_t)(3 * x.v + 2) < vsize; };
     if (n == 4) {
-        const VIdx &i0 = f.vi[0], &i1 = f.vi[1], &i2 = f.vi[2], &i3 = f.vi[3];
+        const VIdx &i0 = fv[0], &i1 = fv[1], &i2 = fv[2], &i3 = fv[3];
         if (!valid(i0) || !valid(i1) || !valid(i2) || !valid(i3)) return;
         const float *p0 = &v[3 * i0.v], *p1 = &v[3 * i1.v], *p2 = &v[3 * i2.v], *p3 = &v[3 * i3.v];
         const float e02x = p2[0] - p0[0], e02y = p2[1] - p0[1], e02z = p2[2] - p0[2];
@@ -328,18 +356,18 @@ void triangulate(const Face &f, int mat, const std::vector<float> &v, std::vecto
         const float s02 = e02x * e02x + e02y * e02y + e02z * e02z;
         const float s13 = e13x * e13x + e13y * e13y + e13z * e13z;
         if (s02 < s13) {
-            out.push_back({i0, i1, i2, mat, f.smooth});
-            out.push_back({i0, i2, i3, mat, f.smooth});
+            out.push_back({i0, i1, i2, mat, smooth});
+            out.push_back({i0, i2, i3, mat, smooth});
         } else {
-            out.push_back({i0, i1, i3, mat, f.smooth});
-            out.push_back({i1, i2, i3, mat, f.smooth});
+            out.push_back({i0, i1, i3, mat, smooth});
+            out.push_back({i1, i2, i3, mat, smooth});
         }
         return;
     }
     // ear clipping in the plane of two axes
     size_t axes[2] = {1, 2};
     for (size_t k = 0; k < n; ++k) {
-        const VIdx &a = f.vi[k % n], &b = f.vi[(k + 1) % n], &c = f.vi[(k + 2) % n];
+        const VIdx &a = fv[k % n], &b = fv[(k + 1) % n], &c = fv[(k + 2) % n];
         if (!valid(a) || !valid(b) || !valid(c)) continue;
         const float *p0 = &v[3 * a.v], *p1 = &v[3 * b.v], *p2 = &v[3 * c.v];
         const float e0x = p1[0] - p0[0], e0y = p1[1] - p0[1], e0z = p1[2] - p0[2];
@@ -356,10 +384,10 @@ void triangulate(const Face &f, int mat, const std::vector<float> &v, std::vecto
             break;
         }
     }
-    std::vector<VIdx> rem = f.vi;
+    std::vector<VIdx> rem(fv, fv + n);
     size_t guess = 0, iters = rem.size(), prev_n = rem.size();
     auto coord = [&](const VIdx &x, size_t ax) {
-        return (x.v < 0 || (size_t)(x.v * 3 + ax) >= v.size()) ? 0.0f : v[x.v * 3 + ax];
+        return (x.v < 0 || (size_t)(x.v * 3 + ax) >= vsize) ? 0.0f : v[x.v * 3 + ax];
     };
     while (rem.size() > 3 && iters > 0) {
         const size_t np = rem.size();
@@ -388,7 +416,7 @@ void triangulate(const Face &f, int mat, const std::vector<float> &v, std::vecto
         for (size_t o = 3; o < np; ++o) {
             const size_t idx = (guess + o) % np;
             const VIdx &x = rem[idx];
-            if (x.v < 0 || (size_t)(x.v * 3 + axes[0]) >= v.size() || (size_t)(x.v * 3 + axes[1]) >= v.size())
+            if (x.v < 0 || (size_t)(x.v * 3 + axes[0]) >= vsize || (size_t)(x.v * 3 + axes[1]) >= vsize)
                 continue;
             if (pnpoly3(vx, vy, v[x.v * 3 + axes[0]], v[x.v * 3 + axes[1]])) {
                 overlap = true;
@@ -399,7 +427,7 @@ void triangulate(const Face &f, int mat, const std::vector<float> &v, std::vecto
             guess += 1;
             continue;
         }
-        out.push_back({ind[0], ind[1], ind[2], mat, f.smooth});
+        out.push_back({ind[0], ind[1], ind[2], mat, smooth});
         size_t r = (guess + 1) % np;
         while (r + 1 < np) {
             rem[r] = rem[r + 1];
@@ -407,7 +435,7 @@ void triangulate(const Face &f, int mat, const std::vector<float> &v, std::vecto
         }
         rem.pop_back();
     }
-    if (rem.size() == 3) out.push_back({rem[0], rem[1], rem[2], mat, f.smooth});
+    if (rem.size() == 3) out.push_back({rem[0], rem[1], rem[2], mat, smooth});
 }
 
 struct ObjData {
@@ -416,145 +444,334 @@ struct ObjData {
     std::vector<MtlMaterial> mats;
 };
 
-kgk_status parse_obj(const std::string &path, ObjData &d) {
+// ---------------------------------------------------------------------------
+// Parallel parse.  The text is cut into chunks at line ends.  A pre-pass counts
+// each chunk's lines and v / vn / vt records, so every chunk knows the counts
+// before its first line and resolves relative indices exactly as a sequential
+// reader would.  Chunks then parse their numbers and face indices in parallel;
+// the state-changing lines (g, o, usemtl, mtllib, s, l, p) are kept, in order,
+// as events with the face and vertex counts they occur at.  A sequential pass
+// replays the events and faces in file order - shapes, materials, smoothing
+// groups, triangulation (which sees only the vertices read so far) - so the
+// result does not depend on the thread count.
+
+// Line cursor over [p, e): '\n', '\r\n' or '\r' ends a line; the line is
+// copied into a reused buffer so the token readers see a C string.
+struct LineRange {
+    const char *p, *e;
+    bool next(std::string &line) {
+        if (p >= e) return false;
+        const char *q = p;
+        while (q < e && *q != '\n' && *q != '\r') ++q;
+        line.assign(p, q);
+        if (q < e && *q == '\r' && q + 1 < e && q[1] == '\n') ++q;
+        p = q < e ? q + 1 : e;
+        return true;
+    }
+};
+
+enum LineKind { kLineSkip, kLineV, kLineVN, kLineVT, kLineLP, kLineF, kLineUsemtl, kLineMtllib, kLineGO, kLineS,
+                kLineOther };
+
+// Classifies a line by its first token (leading spaces and tabs skipped).
+LineKind classify(const char *t) {
+    if (t[0] == '\0' || t[0] == '#') return kLineSkip;
+    if (t[0] == 'v' && is_space(t[1])) return kLineV;
+    if (t[0] == 'v' && t[1] == 'n' && is_space(t[2])) return kLineVN;
+    if (t[0] == 'v' && t[1] == 't' && is_space(t[2])) return kLineVT;
+    if ((t[0] == 'l' || t[0] == 'p') && is_space(t[1])) return kLineLP;
+    if (t[0] == 'f' && is_space(t[1])) return kLineF;
+    if (!strncmp(t, "usemtl", 6)) return kLineUsemtl;
+    if (!strncmp(t, "mtllib", 6) && is_space(t[6])) return kLineMtllib;
+    if ((t[0] == 'g' || t[0] == 'o') && is_space(t[1])) return kLineGO;
+    if (t[0] == 's' && is_space(t[1])) return kLineS;
+    return kLineOther;
+}
+
+struct Counts {
+    size_t lines = 0, nv = 0, nvn = 0, nvt = 0;
+};
+
+struct Event {
+    LineKind kind;
+    size_t nfaces;  // faces of the chunk before this line
+    size_t nv;      // vertices of the file before this line
+    std::string text;
+};
+
+struct Chunk {
+    const char *p = nullptr, *e = nullptr;
+    Counts cnt, base;  // this chunk's counts; the counts before it
+    std::vector<float> v, vn, vt;
+    std::vector<VIdx> idx;          // face corners
+    std::vector<size_t> face_end;   // end of each face in idx
+    std::vector<Event> events;
+    size_t err_line = 0;            // 1-based line of the first bad index, 0 = none
+    bool err_face = false;
+};
+
+void count_chunk(Chunk &c) {
+    LineRange lr{c.p, c.e};
+    std::string ln;
+    while (lr.next(ln)) {
+        ++c.cnt.lines;
+        const char *t = ln.c_str();
+        t += strspn(t, " \t");
+        switch (classify(t)) {
+            case kLineV: ++c.cnt.nv; break;
+            case kLineVN: ++c.cnt.nvn; break;
+            case kLineVT: ++c.cnt.nvt; break;
+            default: break;
+        }
+    }
+}
+
+void parse_chunk(Chunk &c) {
+    LineRange lr{c.p, c.e};
+    std::string ln;
+    size_t line_no = c.base.lines;
+    c.v.reserve(3 * c.cnt.nv);
+    c.vn.reserve(3 * c.cnt.nvn);
+    c.vt.reserve(2 * c.cnt.nvt);
+    while (lr.next(ln)) {
+        ++line_no;
+        const char *t = ln.c_str();
+        t += strspn(t, " \t");
+        const LineKind k = classify(t);
+        const int nv = (int)(c.base.nv + c.v.size() / 3), nvn = (int)(c.base.nvn + c.vn.size() / 3),
+                  nvt = (int)(c.base.nvt + c.vt.size() / 2);
+        switch (k) {
+            case kLineSkip:
+            case kLineOther:
+                break;
+            case kLineV: {
+                t += 2;
+                const float x = read_real(&t), y = read_real(&t), z = read_real(&t);
+                c.v.push_back(x);
+                c.v.push_back(y);
+                c.v.push_back(z);
+                break;
+            }
+            case kLineVN: {
+                t += 3;
+                const float x = read_real(&t), y = read_real(&t), z = read_real(&t);
+                c.vn.push_back(x);
+                c.vn.push_back(y);
+                c.vn.push_back(z);
+                break;
+            }
+            case kLineVT: {
+                t += 3;
+                const float x = read_real(&t), y = read_real(&t);
+                c.vt.push_back(x);
+                c.vt.push_back(y);
+                break;
+            }
+            case kLineLP: {
+                const char *u = t + 2;
+                while (!is_newline(u[0])) {
+                    VIdx vi;
+                    if (!parse_triple(&u, nv, nvn, nvt, &vi)) {
+                        c.err_line = line_no;
+                        return;
+                    }
+                    u += strspn(u, " \t\r");
+                }
+                c.events.push_back({k, c.face_end.size(), (size_t)nv, std::string()});
+                break;
+            }
+            case kLineF: {
+                t += 2;
+                t += strspn(t, " \t");
+                while (!is_newline(t[0])) {
+                    VIdx vi;
+                    if (!parse_triple(&t, nv, nvn, nvt, &vi)) {
+                        c.err_line = line_no;
+                        c.err_face = true;
+                        return;
+                    }
+                    c.idx.push_back(vi);
+                    t += strspn(t, " \t\r");
+                }
+                c.face_end.push_back(c.idx.size());
+                break;
+            }
+            default:
+                c.events.push_back({k, c.face_end.size(), (size_t)nv, std::string(t)});
+                break;
+        }
+    }
+}
+
+// Runs f(i) for i in [0, n) on up to `threads` threads.
+template <class F>
+void parallel_for(size_t n, int threads, F f) {
+    const size_t nt = std::min<size_t>(n, (size_t)std::max(threads, 1));
+    if (nt <= 1) {
+        for (size_t i = 0; i < n; ++i) f(i);
+        return;
+    }
+    std::atomic<size_t> next{0};
+    std::vector<std::thread> pool;
+    for (size_t w = 0; w < nt; ++w)
+        pool.emplace_back([&]() {
+            for (size_t i; (i = next.fetch_add(1)) < n;) f(i);
+        });
+    for (std::thread &th : pool) th.join();
+}
+
+int resolve_threads(int threads) {
+    if (threads > 0) return std::min(threads, 256);
+    const unsigned hw = std::thread::hardware_concurrency();
+    return (int)std::min(std::max(hw, 1u), 64u);
+}
+
+kgk_status parse_obj(const std::string &path, ObjData &d, int threads) {
     std::string text;
     if (!read_text(path, text)) return fail(KGK_ERR_IO, "cannot open OBJ file " + path);
     const std::string base = dir_of(path);
+    // one chunk per call with one thread; else chunks of at least 256 KB, about four per thread
+    const size_t min_chunk = (size_t)256 << 10;
+    const size_t want =
+        threads == 1 ? 1 : std::max<size_t>(1, std::min<size_t>((size_t)threads * 4, text.size() / min_chunk));
+    std::vector<Chunk> chunks;
+    const char *p = text.data(), *const e = text.data() + text.size();
+    for (size_t k = 1; k <= want && p < e; ++k) {
+        const char *q = k == want ? e : std::max<const char *>(p, text.data() + text.size() * k / want);
+        while (q < e && *q != '\n' && *q != '\r') ++q;  // move to the end of a line
+        if (q < e) {
+            if (*q == '\r' && q + 1 < e && q[1] == '\n') ++q;
+            ++q;
+        }
+        Chunk c;
+        c.p = p;
+        c.e = q;
+        chunks.push_back(std::move(c));
+        p = q;
+    }
+    parallel_for(chunks.size(), threads, [&](size_t i) { count_chunk(chunks[i]); });
+    Counts run;
+    for (Chunk &c : chunks) {
+        c.base = run;
+        run.lines += c.cnt.lines;
+        run.nv += c.cnt.nv;
+        run.nvn += c.cnt.nvn;
+        run.nvt += c.cnt.nvt;
+    }
+    parallel_for(chunks.size(), threads, [&](size_t i) { parse_chunk(chunks[i]); });
+    for (const Chunk &c : chunks)
+        if (c.err_line)
+            return fail(KGK_ERR_PARSE, path + ":" + std::to_string(c.err_line) +
+                                           (c.err_face ? ": bad face index" : ": bad index"));
+    d.v.reserve(3 * run.nv);
+    d.vn.reserve(3 * run.nvn);
+    d.vt.reserve(2 * run.nvt);
+    for (const Chunk &c : chunks) {
+        d.v.insert(d.v.end(), c.v.begin(), c.v.end());
+        d.vn.insert(d.vn.end(), c.vn.begin(), c.vn.end());
+        d.vt.insert(d.vt.end(), c.vt.begin(), c.vt.end());
+    }
+    // sequential replay in file order
     std::map<std::string, int> mat_by_name;
     std::set<std::string> mtl_files;
-    std::vector<Face> faces;
+    struct FaceRef {
+        const VIdx *vi;
+        size_t n;
+        unsigned smooth;
+    };
+    std::vector<FaceRef> faces;
     bool other = false;  // lines / points in the current primitive group
     int material = -1;
     unsigned smooth = 0;
     Shape shape;
-    auto export_group = [&]() {
+    auto export_group = [&](size_t nv) {
         if (faces.empty() && !other) return false;
-        for (const Face &f : faces) triangulate(f, material, d.v, shape.tris);
+        shape.tris.reserve(shape.tris.size() + faces.size());
+        for (const FaceRef &f : faces) triangulate(f.vi, f.n, f.smooth, material, d.v, 3 * nv, shape.tris);
         if (other) shape.other_prims = true;
         return true;
     };
-    Lines lines{text};
-    std::string ln;
-    size_t line_no = 0;
-    while (lines.next(ln)) {
-        ++line_no;
-        if (!ln.empty() && ln.back() == '\n') ln.pop_back();
-        if (!ln.empty() && ln.back() == '\r') ln.pop_back();
-        if (ln.empty()) continue;
-        const char *t = ln.c_str();
-        t += strspn(t, " \t");
-        if (t[0] == '\0' || t[0] == '#') continue;
-        if (t[0] == 'v' && is_space(t[1])) {
-            t += 2;
-            const float x = read_real(&t), y = read_real(&t), z = read_real(&t);
-            d.v.push_back(x);
-            d.v.push_back(y);
-            d.v.push_back(z);
-            continue;
-        }
-        if (t[0] == 'v' && t[1] == 'n' && is_space(t[2])) {
-            t += 3;
-            const float x = read_real(&t), y = read_real(&t), z = read_real(&t);
-            d.vn.push_back(x);
-            d.vn.push_back(y);
-            d.vn.push_back(z);
-            continue;
-        }
-        if (t[0] == 'v' && t[1] == 't' && is_space(t[2])) {
-            t += 3;
-            const float x = read_real(&t), y = read_real(&t);
-            d.vt.push_back(x);
-            d.vt.push_back(y);
-            continue;
-        }
-        if ((t[0] == 'l' || t[0] == 'p') && is_space(t[1])) {
-            t += 2;
-            while (!is_newline(t[0])) {
-                VIdx vi;
-                if (!parse_triple(&t, (int)(d.v.size() / 3), (int)(d.vn.size() / 3), (int)(d.vt.size() / 2), &vi))
-                    return fail(KGK_ERR_PARSE, path + ":" + std::to_string(line_no) + ": bad index");
-                t += strspn(t, " \t\r");
+    for (const Chunk &c : chunks) {
+        size_t f = 0;
+        auto take_faces = [&](size_t upto) {
+            for (; f < upto; ++f) {
+                const size_t b = f ? c.face_end[f - 1] : 0;
+                faces.push_back({c.idx.data() + b, c.face_end[f] - b, smooth});
             }
-            other = true;
-            continue;
-        }
-        if (t[0] == 'f' && is_space(t[1])) {
-            t += 2;
-            t += strspn(t, " \t");
-            Face f;
-            f.smooth = smooth;
-            while (!is_newline(t[0])) {
-                VIdx vi;
-                if (!parse_triple(&t, (int)(d.v.size() / 3), (int)(d.vn.size() / 3), (int)(d.vt.size() / 2), &vi))
-                    return fail(KGK_ERR_PARSE, path + ":" + std::to_string(line_no) + ": bad face index");
-                f.vi.push_back(vi);
-                t += strspn(t, " \t\r");
-            }
-            faces.push_back(std::move(f));
-            continue;
-        }
-        if (!strncmp(t, "usemtl", 6)) {
-            t += 6;
-            const std::string name = read_string(&t);
-            auto it = mat_by_name.find(name);
-            const int id = it != mat_by_name.end() ? it->second : -1;
-            if (id != material) {
-                export_group();
-                faces.clear();
-                material = id;
-            }
-            continue;
-        }
-        if (!strncmp(t, "mtllib", 6) && is_space(t[6])) {
-            t += 7;
-            // file names separated by spaces ('\' escapes a space)
-            std::vector<std::string> names;
-            std::string cur;
-            for (const char *c = t; *c; ++c) {
-                if (*c == '\\' && c[1]) {
-                    cur += *++c;
-                } else if (*c == ' ') {
-                    if (!cur.empty()) names.push_back(cur);
-                    cur.clear();
-                } else {
-                    cur += *c;
-                }
-            }
-            if (!cur.empty()) names.push_back(cur);
-            for (const std::string &nm : names) {
-                if (mtl_files.count(nm)) break;
-                std::string mt;
-                if (read_text(base + nm, mt)) {
-                    parse_mtl(mt, d.mats, mat_by_name);
-                    mtl_files.insert(nm);
+        };
+        for (const Event &ev : c.events) {
+            take_faces(ev.nfaces);
+            const char *t = ev.text.c_str();
+            switch (ev.kind) {
+                case kLineLP:
+                    other = true;
+                    break;
+                case kLineUsemtl: {
+                    t += 6;
+                    const std::string name = read_string(&t);
+                    auto it = mat_by_name.find(name);
+                    const int id = it != mat_by_name.end() ? it->second : -1;
+                    if (id != material) {
+                        export_group(ev.nv);
+                        faces.clear();
+                        material = id;
+                    }
                     break;
                 }
+                case kLineMtllib: {
+                    t += 7;
+                    // file names separated by spaces ('\' escapes a space)
+                    std::vector<std::string> names;
+                    std::string cur;
+                    for (const char *ch = t; *ch; ++ch) {
+                        if (*ch == '\\' && ch[1]) {
+                            cur += *++ch;
+                        } else if (*ch == ' ') {
+                            if (!cur.empty()) names.push_back(cur);
+                            cur.clear();
+                        } else {
+                            cur += *ch;
+                        }
+                    }
+                    if (!cur.empty()) names.push_back(cur);
+                    for (const std::string &nm : names) {
+                        if (mtl_files.count(nm)) break;
+                        std::string mt;
+                        if (read_text(base + nm, mt)) {
+                            parse_mtl(mt, d.mats, mat_by_name);
+                            mtl_files.insert(nm);
+                            break;
+                        }
+                    }
+                    break;
+                }
+                case kLineGO:
+                    export_group(ev.nv);
+                    if (!shape.tris.empty() || (t[0] == 'o' && shape.other_prims)) d.shapes.push_back(std::move(shape));
+                    shape = Shape();
+                    faces.clear();
+                    other = false;
+                    break;
+                case kLineS: {
+                    t += 2;
+                    t += strspn(t, " \t");
+                    if (t[0] == '\0') break;
+                    if (t[0] == '\r' || t[1] == '\n') break;
+                    if (strlen(t) >= 3 && t[0] == 'o' && t[1] == 'f' && t[2] == 'f') {
+                        smooth = 0;
+                    } else {
+                        const int g = atoi(t);
+                        smooth = g < 0 ? 0u : (unsigned)g;
+                    }
+                    break;
+                }
+                default:
+                    break;
             }
-            continue;
         }
-        if ((t[0] == 'g' || t[0] == 'o') && is_space(t[1])) {
-            export_group();
-            if (!shape.tris.empty() || (t[0] == 'o' && shape.other_prims)) d.shapes.push_back(std::move(shape));
-            shape = Shape();
-            faces.clear();
-            other = false;
-            continue;
-        }
-        if (t[0] == 's' && is_space(t[1])) {
-            t += 2;
-            t += strspn(t, " \t");
-            if (t[0] == '\0') continue;
-            if (t[0] == '\r' || t[1] == '\n') continue;
-            if (strlen(t) >= 3 && t[0] == 'o' && t[1] == 'f' && t[2] == 'f') {
-                smooth = 0;
-            } else {
-                const int g = atoi(t);
-                smooth = g < 0 ? 0u : (unsigned)g;
-            }
-            continue;
-        }
+        take_faces(c.face_end.size());
     }
-    const bool ret = export_group();
+    const bool ret = export_group(run.nv);
     if (ret || !shape.tris.empty()) d.shapes.push_back(std::move(shape));
     return KGK_OK;
 }
@@ -599,34 +816,58 @@ kgk_material make_mat(int type, int tex, kgk_vec diffuse, kgk_vec emission, floa
 
 extern "C" {
 
-kgk_status kgk_load_obj(const char *obj_path, const char *hdr_path, kgk_host_scene *out) {
+kgk_status kgk_load_obj_ex(const char *obj_path, const char *hdr_path, const kgk_load_options *opt,
+                           kgk_host_scene *out) {
     if (!obj_path || !out) return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_load_obj: NULL argument");
     memset(out, 0, sizeof *out);
+    const int model = opt ? opt->material_model : KGK_MATERIALS_REFERENCE;
+    if (model != KGK_MATERIALS_REFERENCE && model != KGK_MATERIALS_PBR)
+        return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_load_obj: unknown material_model");
+    const int threads = resolve_threads(opt ? opt->threads : 0);
     ObjData d;
-    KGK_TRY(parse_obj(obj_path, d));
+    KGK_TRY(parse_obj(obj_path, d, threads));
     const std::string base = dir_of(obj_path);
-    // triangles (IO_load_WavefrontObj.cuh:32-88)
-    std::vector<kgk_triangle> tris;
+    // triangles (IO_load_WavefrontObj.cuh:32-88), converted in parallel
+    std::vector<size_t> shape_off(d.shapes.size() + 1, 0);
+    for (size_t s = 0; s < d.shapes.size(); ++s) shape_off[s + 1] = shape_off[s] + d.shapes[s].tris.size();
+    const size_t n_tris = shape_off.back();
+    if (n_tris == 0) return fail(KGK_ERR_PARSE, std::string(obj_path) + ": no triangles");
+    kgk_triangle *tri_out = (kgk_triangle *)malloc(n_tris * sizeof(kgk_triangle));
+    if (!tri_out) return fail(KGK_ERR_OUT_OF_MEMORY, "kgk_load_obj: out of host memory");
     const size_t nv = d.v.size() / 3, nvn = d.vn.size() / 3, nvt = d.vt.size() / 2;
-    for (size_t s = 0; s < d.shapes.size(); ++s) {
-        for (const Tri &tr : d.shapes[s].tris) {
+    const size_t block = 1 << 16;
+    const size_t n_blocks = (n_tris + block - 1) / block;
+    // first bad index per block (triangle index, kind): the earliest is reported
+    std::vector<std::pair<size_t, int>> bad(n_blocks, {SIZE_MAX, 0});
+    parallel_for(n_blocks, threads, [&](size_t blk) {
+        const size_t i0 = blk * block, i1 = std::min(n_tris, i0 + block);
+        size_t s = std::upper_bound(shape_off.begin(), shape_off.end(), i0) - shape_off.begin() - 1;
+        for (size_t i = i0; i < i1; ++i) {
+            while (i >= shape_off[s + 1]) ++s;
+            const Tri &tr = d.shapes[s].tris[i - shape_off[s]];
             const VIdx *ix[3] = {&tr.a, &tr.b, &tr.c};
             kgk_vec p[3], n[3], uv[3];
             bool all_n = true;
             for (int k = 0; k < 3; ++k) {
-                if (ix[k]->v < 0 || (size_t)ix[k]->v >= nv)
-                    return fail(KGK_ERR_PARSE, std::string(obj_path) + ": vertex index out of range");
+                if (ix[k]->v < 0 || (size_t)ix[k]->v >= nv) {
+                    bad[blk] = {i, 0};
+                    return;
+                }
                 p[k] = vec3(d.v[3 * ix[k]->v], d.v[3 * ix[k]->v + 1], d.v[3 * ix[k]->v + 2]);
                 if (ix[k]->vn >= 0) {
-                    if ((size_t)ix[k]->vn >= nvn)
-                        return fail(KGK_ERR_PARSE, std::string(obj_path) + ": normal index out of range");
+                    if ((size_t)ix[k]->vn >= nvn) {
+                        bad[blk] = {i, 1};
+                        return;
+                    }
                     n[k] = vec3(d.vn[3 * ix[k]->vn], d.vn[3 * ix[k]->vn + 1], d.vn[3 * ix[k]->vn + 2]);
                 } else {
                     all_n = false;
                 }
                 if (ix[k]->vt >= 0) {
-                    if ((size_t)ix[k]->vt >= nvt)
-                        return fail(KGK_ERR_PARSE, std::string(obj_path) + ": texcoord index out of range");
+                    if ((size_t)ix[k]->vt >= nvt) {
+                        bad[blk] = {i, 2};
+                        return;
+                    }
                     uv[k] = vec3(d.vt[2 * ix[k]->vt], d.vt[2 * ix[k]->vt + 1], 0.0f);
                 } else {
                     uv[k] = vec3(0, 0, 0);
@@ -638,7 +879,7 @@ kgk_status kgk_load_obj(const char *obj_path, const char *hdr_path, kgk_host_sce
                 const kgk_vec c = vec3(e1.y * e2.z - e1.z * e2.y, e1.z * e2.x - e1.x * e2.z, e1.x * e2.y - e1.y * e2.x);
                 n[0] = n[1] = n[2] = c;
             }
-            kgk_triangle t;
+            kgk_triangle &t = tri_out[i];
             memset(&t, 0, sizeof t);
             t.v0 = p[0];
             t.v1 = p[1];
@@ -652,10 +893,16 @@ kgk_status kgk_load_obj(const char *obj_path, const char *hdr_path, kgk_host_sce
             t.material_id = tr.mat + 1;
             t.is_SmoothNormal = tr.smooth != 0;
             t.shape_id = (int32_t)s;
-            tris.push_back(t);
         }
+    });
+    for (const auto &b : bad) {
+        if (b.first == SIZE_MAX) continue;
+        free(tri_out);
+        static const char *what[3] = {"vertex", "normal", "texcoord"};
+        return fail(KGK_ERR_PARSE, std::string(obj_path) + ": " + what[b.second] + " index out of range");
     }
-    if (tris.empty()) return fail(KGK_ERR_PARSE, std::string(obj_path) + ": no triangles");
+    d.shapes.clear();
+    d.shapes.shrink_to_fit();
     // materials (scene.cuh:14-18, IO_load_WavefrontObj.cuh:90-124)
     std::vector<kgk_material> mats;
     mats.push_back(make_mat(0, -1, vec3(0.75f, 0.75f, 0.75f), vec3(0, 0, 0), 0.0f, 0.0f, 0.0f, 0.0f, 1.0f, 0.0f, 0.0f,
@@ -669,6 +916,7 @@ kgk_status kgk_load_obj(const char *obj_path, const char *hdr_path, kgk_host_sce
             diffuse = vec3(diffuse.x + 1e-4f, diffuse.y + 1e-4f, diffuse.z + 1e-4f);
         const float spec = sqrtf(m.specular[0] * m.specular[0] + m.specular[1] * m.specular[1] +
                                  m.specular[2] * m.specular[2]);
+        int tex = -1;
         if (!m.diffuse_tex.empty()) {
             const size_t k = m.diffuse_tex.find_last_of("/\\");
             const std::string name = k == std::string::npos ? m.diffuse_tex : m.diffuse_tex.substr(k + 1);
@@ -676,30 +924,58 @@ kgk_status kgk_load_obj(const char *obj_path, const char *hdr_path, kgk_host_sce
                 tex_id[name] = (int)tex_id.size();
                 tex_names.push_back(name);
             }
-            mats.push_back(make_mat(0, tex_id[name], diffuse, emission, 0.0f, spec, 0.0f, m.metallic, m.roughness,
-                                    0.0f, 0.0f, 0.0f, 0.0f, 0.0f, m.ior, 0.0f, 0.0f, 0.5f));
+            tex = tex_id[name];
+        }
+        if (model == KGK_MATERIALS_PBR && m.has_pbr) {
+            // Disney from the MTL PBR extension: Pr roughness, Pm metallic,
+            // Ps sheen, Pc clearcoat, Pcr clearcoat roughness (gloss = 1 - Pcr),
+            // aniso; specular from Ni as F0 / 0.08 (F0 = ((Ni-1)/(Ni+1))^2),
+            // 0.5 (F0 = 4 %) without Ni
+            auto clamp01 = [](float x) { return std::min(std::max(x, 0.0f), 1.0f); };
+            float specular = 0.5f;
+            if (m.has_ni && m.ior > 0.0f) {
+                const float f0 = ((m.ior - 1.0f) / (m.ior + 1.0f)) * ((m.ior - 1.0f) / (m.ior + 1.0f));
+                specular = clamp01(f0 / 0.08f);
+            }
+            mats.push_back(make_mat(1, tex, diffuse, emission, 0.0f, specular, 0.0f, clamp01(m.metallic),
+                                    clamp01(m.roughness), clamp01(m.anisotropy), clamp01(m.sheen), 0.0f,
+                                    clamp01(m.clearcoat), 1.0f - clamp01(m.clearcoat_roughness),
+                                    m.has_ni ? m.ior : 1.45f, 0.0f, 0.0f, 0.5f));
+        } else if (tex >= 0) {
+            mats.push_back(make_mat(0, tex, diffuse, emission, 0.0f, spec, 0.0f, m.metallic, m.roughness, 0.0f, 0.0f,
+                                    0.0f, 0.0f, 0.0f, m.ior, 0.0f, 0.0f, 0.5f));
         } else {
             mats.push_back(make_mat(0, -1, diffuse, emission, 0.0f, spec, 0.0f, m.metallic, m.roughness, 0.0f, 0.0f,
                                     0.0f, 1.0f, 0.0f, m.ior, 0.01f, 0.01f, 0.0f));
         }
     }
-    for (const kgk_triangle &t : tris)
-        if (t.material_id < 0 || (size_t)t.material_id >= mats.size())
+    for (size_t i = 0; i < n_tris; ++i)
+        if (tri_out[i].material_id < 0 || (size_t)tri_out[i].material_id >= mats.size()) {
+            free(tri_out);
             return fail(KGK_ERR_PARSE, std::string(obj_path) + ": material id out of range");
-    // textures (IO_load_images.cuh:9-15: every value + 1e-4)
+        }
+    // textures (IO_load_images.cuh:9-15: every value + 1e-4), decoded in parallel
     std::vector<kgk_texture> texs(tex_names.size());
-    auto free_all = [&]() {
-        for (kgk_texture &x : texs) free(x.pixels);
-    };
-    for (size_t i = 0; i < tex_names.size(); ++i) {
-        const kgk_status st = load_image_float((base + tex_names[i]).c_str(), &texs[i]);
-        if (st != KGK_OK) {
-            free_all();
-            return st;
+    std::vector<kgk_status> tex_st(tex_names.size(), KGK_OK);
+    std::vector<std::string> tex_err(tex_names.size());
+    parallel_for(tex_names.size(), threads, [&](size_t i) {
+        tex_st[i] = load_image_float((base + tex_names[i]).c_str(), &texs[i]);
+        if (tex_st[i] != KGK_OK) {
+            tex_err[i] = kgk::last_error_message();
+            return;
         }
         const size_t cnt = (size_t)texs[i].width * texs[i].height * texs[i].bpp;
         for (size_t k = 0; k < cnt; ++k) texs[i].pixels[k] = (float)((double)texs[i].pixels[k] + 1e-4);
-    }
+    });
+    auto free_all = [&]() {
+        for (kgk_texture &x : texs) free(x.pixels);
+        free(tri_out);
+    };
+    for (size_t i = 0; i < tex_names.size(); ++i)
+        if (tex_st[i] != KGK_OK) {
+            free_all();
+            return fail(tex_st[i], tex_err[i]);
+        }
     kgk_texture hdr{nullptr, 0, 0, 0};
     if (hdr_path && hdr_path[0]) {
         const kgk_status st = load_image_float(hdr_path, &hdr);
@@ -708,11 +984,9 @@ kgk_status kgk_load_obj(const char *obj_path, const char *hdr_path, kgk_host_sce
             return st;
         }
     }
-    out->triangles = (kgk_triangle *)malloc(tris.size() * sizeof(kgk_triangle));
     out->materials = (kgk_material *)malloc(mats.size() * sizeof(kgk_material));
     out->textures = texs.empty() ? nullptr : (kgk_texture *)malloc(texs.size() * sizeof(kgk_texture));
-    if (!out->triangles || !out->materials || (!texs.empty() && !out->textures)) {
-        free(out->triangles);
+    if (!out->materials || (!texs.empty() && !out->textures)) {
         free(out->materials);
         free(out->textures);
         free_all();
@@ -720,14 +994,18 @@ kgk_status kgk_load_obj(const char *obj_path, const char *hdr_path, kgk_host_sce
         memset(out, 0, sizeof *out);
         return fail(KGK_ERR_OUT_OF_MEMORY, "kgk_load_obj: out of host memory");
     }
-    memcpy(out->triangles, tris.data(), tris.size() * sizeof(kgk_triangle));
+    out->triangles = tri_out;
     memcpy(out->materials, mats.data(), mats.size() * sizeof(kgk_material));
     if (!texs.empty()) memcpy(out->textures, texs.data(), texs.size() * sizeof(kgk_texture));
-    out->n_triangles = tris.size();
+    out->n_triangles = n_tris;
     out->n_materials = mats.size();
     out->n_textures = texs.size();
     out->hdr = hdr;
     return KGK_OK;
+}
+
+kgk_status kgk_load_obj(const char *obj_path, const char *hdr_path, kgk_host_scene *out) {
+    return kgk_load_obj_ex(obj_path, hdr_path, nullptr, out);
 }
 
 void kgk_host_scene_free(kgk_host_scene *s) {
@@ -740,14 +1018,19 @@ void kgk_host_scene_free(kgk_host_scene *s) {
     memset(s, 0, sizeof *s);
 }
 
-kgk_status kgk_scene_load_obj(const char *obj_path, const char *hdr_path, kgk_scene **out) {
+kgk_status kgk_scene_load_obj_ex(const char *obj_path, const char *hdr_path, const kgk_load_options *opt,
+                                 kgk_scene **out) {
     if (!obj_path || !out) return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_scene_load_obj: NULL argument");
     kgk_host_scene hs;
-    KGK_TRY(kgk_load_obj(obj_path, hdr_path, &hs));
+    KGK_TRY(kgk_load_obj_ex(obj_path, hdr_path, opt, &hs));
     const kgk_status st = kgk_scene_create(hs.triangles, hs.n_triangles, hs.materials, hs.n_materials, hs.textures,
                                            hs.n_textures, hs.hdr.pixels ? &hs.hdr : nullptr, out);
     kgk_host_scene_free(&hs);
     return st;
+}
+
+kgk_status kgk_scene_load_obj(const char *obj_path, const char *hdr_path, kgk_scene **out) {
+    return kgk_scene_load_obj_ex(obj_path, hdr_path, nullptr, out);
 }
 
 }  // extern "C"

@@ -104,6 +104,15 @@ class KgkHostScene(ctypes.Structure):
                 ("hdr", KgkTexture)]
 
 
+MATERIALS_REFERENCE = 0
+MATERIALS_PBR = 1
+
+
+class KgkLoadOptions(ctypes.Structure):
+    _fields_ = [("material_model", ctypes.c_int32), ("threads", ctypes.c_int32),
+                ("reserved", ctypes.c_int32 * 6)]
+
+
 class KgkNrcConfig(ctypes.Structure):
     _fields_ = [("width", ctypes.c_int32), ("hidden_layers", ctypes.c_int32),
                 ("learning_rate", ctypes.c_float), ("train_paths", ctypes.c_int32),

@@ -301,6 +301,57 @@ def write_obj_scene(d):
     return os.path.join(d, "OBJ.obj")
 
 
+def write_big_obj(d, n_blocks=2000, seed=5, full_indices=False):
+    """A large seeded OBJ for the parallel parser: blocks of vertices and
+    faces (triangles to hexagons, absolute and relative indices, with and
+    without vt / vn) separated by group, object, material, smoothing, line and
+    point records, comments and blank lines, with \\n, \\r\\n and \\r line ends
+    mixed.  full_indices: every corner has v/vt/vn (the reference's loader
+    needs both).  Uses scene.mtl of write_obj_scene."""
+    rng = np.random.default_rng(seed)
+    out = ["mtllib scene.mtl\n"]
+    nv = nvt = nvn = 0
+    ends = ["\n", "\r\n", "\r"]
+    mats = ["red", "tex_rgb", "emissive", "tex_ga", "no_such_material"]
+    for b in range(n_blocks):
+        le = ends[int(rng.integers(0, 3))]
+        k = int(rng.integers(8, 40))
+        pts = rng.normal(0, 10, (k, 3)) + rng.normal(0, 100, 3)
+        out.append("".join(f"v {x:.6f} {y:.6f} {z:.6f}{le}" for x, y, z in pts))
+        out.append("".join(f"vt {u:.5f} {v:.5f}{le}" for u, v in rng.random((k // 2, 2))))
+        out.append("".join(f"vn {x:.4f} {y:.4f} {z:.4f}{le}" for x, y, z in rng.normal(0, 1, (k // 3, 3))))
+        nv += k
+        nvt += k // 2
+        nvn += k // 3
+        for f in range(int(rng.integers(10, 60))):
+            r = rng.random()
+            if r < 0.03:
+                out.append(rng.choice([f"g grp{b}_{f}", f"o obj{b}_{f}", "g", "# comment", "", "   "]) + le)
+            elif r < 0.07:
+                out.append(f"usemtl {mats[int(rng.integers(0, len(mats)))]}{le}")
+            elif r < 0.10:
+                out.append(rng.choice(["s 1", "s off", "s 0", "s 3"]) + le)
+            elif r < 0.11:
+                out.append(f"l {int(rng.integers(1, nv + 1))} {int(rng.integers(1, nv + 1))}{le}")
+            elif r < 0.115:
+                out.append(f"p {-int(rng.integers(1, k + 1))}{le}")
+            n = int(rng.choice([3, 3, 3, 4, 4, 5, 6]))
+            corners = []
+            style = int(rng.integers(0, 4)) if not full_indices else 3
+            for c in range(n):
+                rel = rng.random() < 0.3
+                iv = int(rng.integers(1, k + 1))  # within this block, so convex-ish faces stay local
+                v = -iv if rel else nv - k + iv
+                t = -int(rng.integers(1, k // 2 + 1)) if rel else int(rng.integers(1, nvt + 1))
+                m = -int(rng.integers(1, k // 3 + 1)) if rel else int(rng.integers(1, nvn + 1))
+                corners.append([f"{v}", f"{v}/{t}", f"{v}//{m}", f"{v}/{t}/{m}"][style])
+            out.append("f " + " ".join(corners) + le)
+    path = os.path.join(d, "big.obj")
+    with open(path, "w", newline="") as f:
+        f.write("".join(out))
+    return path
+
+
 def write_images(d):
     names = []
     for name, data in image_cases():

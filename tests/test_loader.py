@@ -98,3 +98,61 @@ def test_errors(tmp_path):
     (tmp_path / "x.jpg").write_bytes(b"\xff\xd8\xff\xe0" + bytes(64))
     with pytest.raises(KgkError, match="JPEG"):
         load_image(tmp_path / "x.jpg")
+
+
+def test_parallel_parse_is_independent_of_threads(tmp_path):
+    """The chunked parallel parse (relative indices, groups, materials and
+    smoothing groups crossing chunk boundaries, mixed line ends) gives the
+    sequential parse's result bit for bit."""
+    scene_files.write_obj_scene(str(tmp_path))
+    path = scene_files.write_big_obj(str(tmp_path), n_blocks=1500)
+    assert os.path.getsize(path) > 3 << 20  # several 256 KB chunks at every thread count below
+    t1, m1, x1, _ = load_obj(path, threads=1)  # one chunk: the sequential reader
+    assert len(t1) > 50000 and len(np.unique(t1["shape_id"])) > 20
+    for th in (2, 3, 7):
+        t, m, x, _ = load_obj(path, threads=th)
+        assert same_bits(scenes.canonical(t), scenes.canonical(t1)), th
+        assert same_bits(m, m1)
+        assert len(x) == len(x1) and all(same_bits(a, b) for a, b in zip(x, x1))
+
+
+@pytest.mark.skipif(not os.path.exists(os.path.join(os.path.dirname(GOLDEN), "..", "oracle", "_ref",
+                                                    "libkgkref.so")), reason="reference build not present")
+def test_large_file_against_reference_build(tmp_path):
+    from oracle import orc
+    scene_files.write_obj_scene(str(tmp_path))
+    path = scene_files.write_big_obj(str(tmp_path), n_blocks=600, seed=9, full_indices=True)
+    os.replace(path, tmp_path / "OBJ.obj")  # the reference reads OBJ.obj from its directory
+    rt, rm, _ = orc.ref_load_obj(str(tmp_path))
+    tris, mats, _, _ = load_obj(tmp_path / "OBJ.obj", threads=4)
+    assert same_bits(scenes.canonical(tris), scenes.canonical(rt))
+    assert same_bits(mats, rm)
+
+
+def test_pbr_materials_map_to_disney(tmp_path):
+    from kagayaki_gb300 import MATERIALS_PBR, structs
+    path = scene_files.write_obj_scene(str(tmp_path))
+    with open(tmp_path / "scene.mtl", "a") as f:
+        f.write("\nnewmtl coat\nKd 0.2 0.4 0.8\nPr 0.3\nPc 1.5\nPcr 0.25\nPs 0.5\naniso 0.7\n")
+    with open(path, "a") as f:
+        f.write("usemtl coat\nf 1 2 3\n")
+    _, ref_m, _, _ = load_obj(path)
+    tris, m, _, _ = load_obj(path, materials=MATERIALS_PBR)
+    names = ["red", "tex_rgb", "emissive", "tex_ga", "tex_pal", "coat"]
+    assert len(m) == len(ref_m) == len(names) + 1
+    for i, name in enumerate(names, start=1):
+        if name not in ("red", "coat"):  # no PBR key: converted as the reference does
+            assert same_bits(m[i], ref_m[i]), name
+    red, coat = m[1], m[6]
+    assert red["MATERIAL_TYPE_ID"] == structs.DISNEY and coat["MATERIAL_TYPE_ID"] == structs.DISNEY
+    np.testing.assert_allclose(red["diffuse"][:3], [0.63, 0.065, 0.05], rtol=1e-6)
+    assert red["roughness"] == np.float32(0.5) and red["metallic"] == np.float32(0.25)
+    f0 = ((1.33 - 1) / (1.33 + 1)) ** 2
+    np.testing.assert_allclose(red["specular"], f0 / 0.08, rtol=1e-5)
+    assert red["IOR"] == np.float32(1.33)
+    assert coat["clearcoat"] == 1.0 and coat["cloearcoatGloss"] == np.float32(0.75)  # Pc clamped to 1
+    assert coat["sheen"] == np.float32(0.5) and coat["anisotropic"] == np.float32(0.7)
+    assert coat["specular"] == np.float32(0.5) and coat["IOR"] == np.float32(1.45)
+    assert tris["material_id"][-1] == 6
+    with pytest.raises(KgkError, match="material_model"):
+        load_obj(path, materials=7)
