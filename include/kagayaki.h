@@ -314,7 +314,9 @@ kgk_status kgk_camera_setup(kgk_vec origin, float cam_to_screen_dist, float rota
  * this call's samples (x,y,z; align = 1).  Replaces render<<<>>>
  * (render.cuh:21-49, main.cu:199) with a wavefront pipeline.  prev_cam may be
  * NULL (no reprojection).  When cfg->accumulate is set, the samples are also
- * added to the scene's FP64 accumulator (see kgk_accum_*). */
+ * added to the scene's FP64 accumulator (see kgk_accum_*).  out may be host
+ * or device memory, or NULL: the frame then stays on the device, in the
+ * scene, for kgk_svgf_output(noisy = NULL) (no counterpart in the reference). */
 kgk_status kgk_render(kgk_scene *scene, const kgk_camera *cam, const kgk_camera *prev_cam,
                       const kgk_render_config *cfg, kgk_vec *out, kgk_stats *stats);
 
@@ -356,6 +358,31 @@ typedef struct kgk_svgf_config {
  * filter keeps its history in the scene handle. */
 kgk_status kgk_svgf(kgk_scene *scene, const kgk_svgf_config *cfg, const kgk_vec *noisy,
                     kgk_vec *filtered);
+
+/* kgk_svgf for a frame loop (no counterpart in the reference, whose main.cu
+ * filters, then gamma-converts and writes PNGs on the host, IO_save_png.cuh).
+ *   noisy    NULL = the frame the last kgk_render kept on the device (out = NULL)
+ *   filtered NULL = not written (else host or device, as kgk_svgf)
+ *   rgba8    NULL = not written; else width*height*4 bytes (host or device):
+ *            the filtered frame with save_png's tone mapping (powf(x, 1/2.2f),
+ *            clamp, x255 truncated, alpha 255; bytes equal to
+ *            kgk_tonemap_rgba8's), written in the filter's last pass
+ *   async    0 = return when every output is written.  1 = return once the
+ *            work is queued: a host rgba8 buffer is filled by a copy on a
+ *            second stream that overlaps the scene's next calls, and is
+ *            complete when kgk_scene_sync returns; the buffer must stay valid
+ *            until then.  The copy overlaps only when rgba8 is pinned memory
+ *            (kgk_host_alloc, or cudaHostAlloc / cudaHostRegister); pageable
+ *            memory is copied before the call returns.  A host `filtered`
+ *            buffer makes the call wait.
+ * At least one of filtered and rgba8 must be given. */
+kgk_status kgk_svgf_output(kgk_scene *scene, const kgk_svgf_config *cfg, const kgk_vec *noisy,
+                           kgk_vec *filtered, uint8_t *rgba8, int32_t async);
+/* Waits for the scene's queued work and output copies. */
+kgk_status kgk_scene_sync(kgk_scene *scene);
+/* Page-locked host memory for overlapped output copies; free with kgk_host_free. */
+kgk_status kgk_host_alloc(size_t bytes, void **out);
+void kgk_host_free(void *ptr);
 
 /* struct_SVGFBuffers.cuh:7-23 `SVGFBuffer`, 112 B: the reference's per-pixel
  * G-buffer and filter state. */
@@ -455,7 +482,9 @@ kgk_status kgk_nrc_loss_scale(kgk_scene *scene, float *scale);
 /* ------------------------------------------------------------------------- */
 
 /* gamma 1/2.2, then clamp to [0,1], then x255 truncated, alpha 255
- * (IO_save_png.cuh:26,7,47-52): out = width*height*4 bytes. */
+ * (IO_save_png.cuh:26,7,47-52): out = width*height*4 bytes.  A NaN (also from
+ * a negative value) gives 0.  A device img is tone-mapped on the device (the
+ * same bytes); out may then be host or device memory. */
 kgk_status kgk_tonemap_rgba8(const kgk_vec *img, int32_t width, int32_t height, uint8_t *out);
 /* Writes the tone-mapped image as an RGBA8 PNG. */
 kgk_status kgk_save_png(const kgk_vec *img, int32_t width, int32_t height, const char *path);

@@ -37,6 +37,10 @@ PROTOTYPES = {
     "kgk_accum_reset": (_st, [_vp, _i32, _i32]),
     "kgk_accum_read": (_st, [_vp, _vp, _vp, ctypes.POINTER(ctypes.c_uint64)]),
     "kgk_svgf": (_st, [_vp, ctypes.POINTER(KgkSvgfConfig), _vp, _vp]),
+    "kgk_svgf_output": (_st, [_vp, ctypes.POINTER(KgkSvgfConfig), _vp, _vp, _vp, _i32]),
+    "kgk_scene_sync": (_st, [_vp]),
+    "kgk_host_alloc": (_st, [_sz, ctypes.POINTER(_vp)]),
+    "kgk_host_free": (None, [_vp]),
     "kgk_svgf_apply": (_st, [_vp, _vp, _vp, _vp, _i32, _i32, _i32]),
     "kgk_svgf_apply_noalloc": (_st, [_vp, _vp, _vp, _vp, _i32, _i32, _i32, _vp]),
     "kgk_nrc_init": (_st, [_vp, _vp]),

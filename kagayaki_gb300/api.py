@@ -25,7 +25,12 @@ ESTIMATOR_UNBIASED = 1
 
 
 def _p(a):
-    return ctypes.c_void_p(a.ctypes.data) if a is not None else None
+    """A numpy array's data pointer; an int is taken as a (device) pointer."""
+    if a is None:
+        return None
+    if isinstance(a, int):
+        return ctypes.c_void_p(a)
+    return ctypes.c_void_p(a.ctypes.data)
 
 
 def _as(a, dtype):
@@ -129,20 +134,35 @@ class Scene:
     def render(self, cam, width, height, spp=1, max_depth=0, rr_start_depth=3,
                estimator=ESTIMATOR_COMPAT, seed=1, frame_index=0, accumulate=False,
                count_work=False, write_gbuffer=False, use_cache=False, wave_paths=0, prev_cam=None,
-               out=None, profile_stages=False, texture_filter=0):
+               out=None, profile_stages=False, texture_filter=0, keep_on_device=False):
+        """kgk_render.  out: a (height, width, 4) float32 host array (allocated
+        when None) or a device pointer (int); keep_on_device: the frame stays
+        in the scene for svgf_output(noisy=None) and None is returned for it."""
         cfg = KgkRenderConfig(width=width, height=height, spp=spp, max_depth=max_depth,
                               rr_start_depth=rr_start_depth, estimator=estimator, seed=seed,
                               frame_index=frame_index, accumulate=int(accumulate),
                               wave_paths=wave_paths, count_work=int(count_work),
                               write_gbuffer=int(write_gbuffer), use_cache=int(use_cache),
                               profile_stages=int(profile_stages), texture_filter=int(texture_filter))
-        if out is None:
+        if keep_on_device:
+            out = None
+        elif out is None:
             out = np.empty((height, width, 4), np.float32)
         st = KgkStats()
         check(lib().kgk_render(self._h, ctypes.byref(cam),
                                ctypes.byref(prev_cam) if prev_cam is not None else None,
                                ctypes.byref(cfg), _p(out), ctypes.byref(st)))
         return out, stats_dict(st)
+
+    def svgf_output(self, cfg, noisy=None, filtered=None, rgba8=None, async_=False):
+        """kgk_svgf_output: noisy None = the frame kept by render(keep_on_device=True);
+        filtered / rgba8: host arrays, device pointers (int) or None."""
+        check(lib().kgk_svgf_output(self._h, ctypes.byref(cfg), _p(noisy), _p(filtered), _p(rgba8),
+                                    int(async_)))
+
+    def sync(self):
+        """kgk_scene_sync: waits for queued work and output copies."""
+        check(lib().kgk_scene_sync(self._h))
 
     def set_textures_rgba8(self, textures):
         """Replaces the scene's textures with RGBA8 ones: (height, width, 4) uint8 arrays."""
@@ -172,6 +192,30 @@ class Scene:
         n = ctypes.c_uint64()
         check(lib().kgk_accum_read(self._h, _p(mean), _p(var), ctypes.byref(n)))
         return mean, var, n.value
+
+
+class PinnedBuffer:
+    """Page-locked host memory from kgk_host_alloc, viewed as a numpy array."""
+
+    def __init__(self, shape, dtype):
+        dtype = np.dtype(dtype)
+        n = int(np.prod(shape)) * dtype.itemsize
+        self._ptr = ctypes.c_void_p()
+        check(lib().kgk_host_alloc(n, ctypes.byref(self._ptr)))
+        raw = (ctypes.c_uint8 * n).from_address(self._ptr.value)
+        self.array = np.frombuffer(raw, np.uint8).view(dtype).reshape(shape)
+
+    def free(self):
+        if self._ptr:
+            self.array = None
+            lib().kgk_host_free(self._ptr)
+            self._ptr = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
 
 
 def _texture_array(t):

@@ -171,6 +171,7 @@ void kgk_scene_destroy(kgk_scene *s) {
     if (!s) return;
     cudaSetDevice(s->device);
     if (s->stream) cudaStreamSynchronize(s->stream);
+    output_state_free(s);
     render_state_free(s);
     svgf_state_free(s);
     nrc_state_free(s);

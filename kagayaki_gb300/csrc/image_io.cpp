@@ -5,6 +5,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <mutex>
 #include <vector>
 
 #include "kgk_scene.h"
@@ -45,14 +46,44 @@ void chunk(std::vector<uint8_t> &out, const char *type, const std::vector<uint8_
     put32(out, crc32(&out[start], out.size() - start) ^ 0xffffffffu);
 }
 
-// gamma 1/2.2 -> clamp [0,1] -> x255 truncated (IO_save_png.cuh:26,7,47-52)
-inline uint8_t tone(float x) {
+inline uint8_t tone(float x) { return kgk::tone_host(x); }
+
+}  // namespace
+
+namespace kgk {
+
+// gamma 1/2.2 -> clamp [0,1] -> x255 truncated (IO_save_png.cuh:26,7,47-52);
+// a NaN (also powf of a negative number) gives 0 instead of the reference's
+// undefined float-to-char conversion.
+uint8_t tone_host(float x) {
     float g = powf(x, 1 / 2.2f);
+    if (g != g) return 0;
     g = g < 0.0f ? 0.0f : (g > 1.0f ? 1.0f : g);
     return (uint8_t)(g * 255);
 }
 
-}  // namespace
+const float *tone_thresholds() {
+    static float t[255];
+    static std::once_flag once;
+    std::call_once(once, []() {
+        // floats >= 0 are ordered like their bit patterns: binary search over
+        // [+0, +inf] for the first pattern whose byte reaches k
+        for (int k = 1; k <= 255; ++k) {
+            uint32_t lo = 0u, hi = 0x7f800000u;  // tone_host(+inf) = 255 >= k
+            while (lo < hi) {
+                const uint32_t mid = lo + (hi - lo) / 2;
+                float x;
+                memcpy(&x, &mid, 4);
+                if (tone_host(x) >= k) hi = mid;
+                else lo = mid + 1;
+            }
+            memcpy(&t[k - 1], &lo, 4);
+        }
+    });
+    return t;
+}
+
+}  // namespace kgk
 
 extern "C" {
 
@@ -60,12 +91,23 @@ kgk_status kgk_tonemap_rgba8(const kgk_vec *img, int32_t w, int32_t h, uint8_t *
     if (!img || !out) return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_tonemap_rgba8: NULL buffer");
     if (w <= 0 || h <= 0) return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_tonemap_rgba8: empty image");
     const size_t npx = (size_t)w * h;
-    std::vector<kgk_vec> host;
     const kgk_vec *src = img;
     if (is_device_ptr(img)) {
-        host.resize(npx);
-        KGK_CUDA(cudaMemcpy(host.data(), img, npx * sizeof(kgk_vec), cudaMemcpyDeviceToHost));
-        src = host.data();
+        // on the device; the bytes go to `out` (device or host)
+        uchar4 *dout = reinterpret_cast<uchar4 *>(out);
+        const bool od = is_device_ptr(out);
+        if (!od) KGK_CUDA(cudaMalloc(reinterpret_cast<void **>(&dout), npx * sizeof(uchar4)));
+        kgk_status st = tonemap_device(reinterpret_cast<const float4 *>(img), npx, dout, nullptr);
+        if (st == KGK_OK && !od) {
+            const cudaError_t e = cudaMemcpy(out, dout, npx * sizeof(uchar4), cudaMemcpyDeviceToHost);
+            if (e != cudaSuccess) st = cuda_fail(e, "kgk_tonemap_rgba8 copy");
+        }
+        if (st == KGK_OK) {
+            const cudaError_t e = cudaDeviceSynchronize();
+            if (e != cudaSuccess) st = cuda_fail(e, "kgk_tonemap_rgba8");
+        }
+        if (!od) cudaFree(dout);
+        return st;
     }
     for (size_t i = 0; i < npx; ++i) {
         out[4 * i] = tone(src[i].x);

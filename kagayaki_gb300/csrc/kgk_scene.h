@@ -36,6 +36,30 @@ void nrc_state_free(kgk_scene *s);
 // The G-buffer and camera of the last frame rendered with write_gbuffer=1.
 bool svgf_gbuffer(kgk_scene *s, int *W, int *H, const float4 **pos, const float4 **nrm, const float4 **alb,
                   const float4 **emi, kgk_camera *cam);
+// The frame the last kgk_render kept on the device (called with out == NULL).
+bool render_kept_frame(kgk_scene *s, int *W, int *H, const float4 **frame);
+
+// RGBA8 frame output (svgf.cu): two device buffers used in turn, and a copy
+// stream that brings a finished one to host memory while the next frame is
+// computed on the scene's stream.
+struct OutputState {
+    size_t npx = 0;
+    uchar4 *rgba8[2] = {nullptr, nullptr};
+    int slot = 0;
+    cudaStream_t copy = nullptr;
+    cudaEvent_t done[2] = {nullptr, nullptr}, copied[2] = {nullptr, nullptr};
+};
+void output_state_free(kgk_scene *s);
+
+// save_png's tone mapping (IO_save_png.cuh:26,7,47-52) on the host:
+// powf(x, 1/2.2f), clamp to [0,1], x255 truncated (NaN gives 0).
+uint8_t tone_host(float x);
+// Thresholds of tone_host: entry k-1 is the smallest float x >= 0 with
+// tone_host(x) >= k (k = 1..255), computed once with this machine's powf, so
+// a device lookup gives tone_host's bytes exactly.
+const float *tone_thresholds();
+// Tone-maps npx pixels on the device (in, out: device pointers) on stream st.
+kgk_status tonemap_device(const float4 *in, size_t npx, uchar4 *out, cudaStream_t st);
 
 }  // namespace kgk
 
@@ -48,4 +72,5 @@ struct kgk_scene {
     kgk::RenderState *rs = nullptr;
     kgk::SvgfState *svgf = nullptr;
     kgk::NrcState *nrc = nullptr;
+    kgk::OutputState *out = nullptr;
 };

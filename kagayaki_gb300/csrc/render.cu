@@ -35,6 +35,8 @@ struct RenderState {
     int W = 0, H = 0;                         // per-pixel buffers
     unsigned long long *seeds = nullptr;      // compat per-pixel seed chain (render.cuh:19,29,42)
     float4 *frame = nullptr;                  // per-call radiance sum
+    float4 *kept = nullptr;                   // the output frame kept on the device (kgk_render out == NULL)
+    bool kept_valid = false;
     double *acc_sum = nullptr, *acc_sq = nullptr;  // FP64 accumulator (3 per pixel)
     unsigned long long acc_n = 0;
     int acc_W = 0, acc_H = 0;
@@ -1016,6 +1018,8 @@ kgk_status ensure_pixels(RenderState &R, int W, int H) {
     KGK_TRY(ensure(&R.seeds, npx, "per-pixel seeds"));
     KGK_CUDA(cudaMemset(R.seeds, 0, npx * sizeof(unsigned long long)));
     KGK_TRY(ensure(&R.frame, npx, "frame buffer"));
+    KGK_TRY(ensure(&R.kept, npx, "frame buffer"));
+    R.kept_valid = false;
     KGK_TRY(ensure(&R.gb_pos, npx, "G-buffer"));
     KGK_TRY(ensure(&R.gb_nrm, npx, "G-buffer"));
     KGK_TRY(ensure(&R.gb_alb, npx, "G-buffer"));
@@ -1065,7 +1069,7 @@ kgk_status ensure_train(RenderState &R, int tcap) {
 void render_state_free(kgk_scene *s) {
     RenderState *R = s->rs;
     if (!R) return;
-    void *ptrs[] = {R->seeds, R->frame, R->acc_sum, R->acc_sq, R->gb_pos, R->gb_nrm, R->gb_alb, R->gb_emi,
+    void *ptrs[] = {R->seeds, R->frame, R->kept, R->acc_sum, R->acc_sq, R->gb_pos, R->gb_nrm, R->gb_alb, R->gb_emi,
                     R->o, R->d, R->thr, R->rad, R->hit, R->rng, R->depth, R->aq[0], R->aq[1], R->sq[0],
                     R->sq[1], R->sq[2], R->sh_o[0], R->sh_o[1], R->sh_d[0], R->sh_d[1], R->sh_c[0],
                     R->sh_c[1], R->cnt, R->stats, R->spread, R->pflags, R->qrec, R->trec, R->ttgt};
@@ -1077,6 +1081,15 @@ void render_state_free(kgk_scene *s) {
 RenderState *render_state(kgk_scene *s) {
     if (!s->rs) s->rs = new RenderState();
     return s->rs;
+}
+
+bool render_kept_frame(kgk_scene *s, int *W, int *H, const float4 **frame) {
+    RenderState *R = s->rs;
+    if (!R || !R->kept_valid) return false;
+    *W = R->W;
+    *H = R->H;
+    *frame = R->kept;
+    return true;
 }
 
 bool svgf_gbuffer(kgk_scene *s, int *W, int *H, const float4 **pos, const float4 **nrm, const float4 **alb,
@@ -1102,7 +1115,7 @@ extern "C" {
 kgk_status kgk_render(kgk_scene *s, const kgk_camera *cam, const kgk_camera *prev_cam,
                       const kgk_render_config *cfg, kgk_vec *out, kgk_stats *stats) {
     (void)prev_cam;
-    if (!s || !cam || !cfg || !out) return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_render: NULL argument");
+    if (!s || !cam || !cfg) return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_render: NULL argument");
     if (!s->built) return fail(KGK_ERR_NOT_BUILT, "kgk_render: call kgk_build_bvh first");
     if (cfg->width <= 0 || cfg->height <= 0 || (long long)cfg->width * cfg->height > (1LL << 26))
         return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_render: image size out of range");
@@ -1318,10 +1331,14 @@ kgk_status kgk_render(kgk_scene *s, const kgk_camera *cam, const kgk_camera *pre
         R.gbuffer_valid = true;
         R.gbuffer_cam = *cam;
     }
-    // output
-    const bool od = is_device_ptr(out);
+    // output: the caller's device buffer, the scene's kept frame (out == NULL),
+    // or staging copied to the caller's host buffer
+    const bool od = out == nullptr || is_device_ptr(out);
     float4 *dout;
-    if (od) {
+    R.kept_valid = out == nullptr;
+    if (!out) {
+        dout = R.kept;
+    } else if (od) {
         dout = reinterpret_cast<float4 *>(out);
     } else {
         KGK_TRY(s->staging.reserve((size_t)npx * sizeof(float4)));

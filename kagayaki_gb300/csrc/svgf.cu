@@ -79,6 +79,41 @@ struct CompatArgs {
 
 #define FOR_PIXELS(n) for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < (n); p += gridDim.x * blockDim.x)
 
+// save_png's tone mapping on the device.  tone_host's bytes are a step
+// function of x; T holds its 255 steps (the smallest x reaching each byte,
+// computed with the host's powf), so counting the steps at or below x gives
+// tone_host(x) exactly.  NaN and negative x give 0 (powf is NaN there), except
+// -inf, where powf(-inf, 1/2.2f) = +inf gives 255.
+struct ToneTable {
+    float t[255];
+};
+
+__device__ __forceinline__ unsigned tone_byte(float x, const ToneTable &T) {
+    if (!(x >= 0.0f)) return x == -__int_as_float(0x7f800000) ? 255u : 0u;
+    unsigned i = 0;
+#pragma unroll
+    for (unsigned step = 128; step; step >>= 1)
+        if (T.t[i + step - 1] <= x) i += step;
+    return i;
+}
+
+__device__ __forceinline__ uchar4 tone_rgba8(float4 c, const ToneTable &T) {
+    return make_uchar4((unsigned char)tone_byte(c.x, T), (unsigned char)tone_byte(c.y, T),
+                       (unsigned char)tone_byte(c.z, T), 255);
+}
+
+__global__ void k_tonemap(const float4 *__restrict__ in, size_t npx, uchar4 *__restrict__ out,
+                          const __grid_constant__ ToneTable T) {
+    for (size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x; p < npx; p += (size_t)gridDim.x * blockDim.x)
+        out[p] = tone_rgba8(in[p], T);
+}
+
+ToneTable tone_table() {
+    ToneTable T;
+    memcpy(T.t, tone_thresholds(), sizeof T.t);
+    return T;
+}
+
 __global__ void k_c_prologue(CompatArgs a) {
     FOR_PIXELS(a.W * a.H) {
         float3 r = v3(a.R[p]);
@@ -662,18 +697,23 @@ __global__ void k_s_feedback(StdArgs a, const float4 *filtered) {
     }
 }
 
-__global__ void k_s_output(StdArgs a, const float4 *filtered, float4 *out) {
+// The last pass: re-modulates the filtered colour by the albedo and writes
+// the frame (out, when not null) and its save_png bytes (rgba8, when not null).
+__global__ void k_s_output(StdArgs a, const float4 *filtered, float4 *out, uchar4 *rgba8,
+                           const __grid_constant__ ToneTable T) {
     FOR_PIXELS(a.W * a.H) {
         const float4 nr = a.nrm[p];
-        if (__float_as_int(nr.w) < 0) {
-            const float4 c = filtered[p];
-            out[p] = make_float4(c.x, c.y, c.z, 1.0f);
-            continue;
-        }
-        const float3 al = f3(a.alb[p]) + f3(kS, kS, kS);
         const float4 c = filtered[p];
-        const float3 e = f3(a.emi[p]);
-        out[p] = make_float4(c.x * al.x + 0.0f * e.x, c.y * al.y, c.z * al.z, 1.0f);
+        float4 o;
+        if (__float_as_int(nr.w) < 0) {
+            o = make_float4(c.x, c.y, c.z, 1.0f);
+        } else {
+            const float3 al = f3(a.alb[p]) + f3(kS, kS, kS);
+            const float3 e = f3(a.emi[p]);
+            o = make_float4(c.x * al.x + 0.0f * e.x, c.y * al.y, c.z * al.z, 1.0f);
+        }
+        if (out) out[p] = o;
+        if (rgba8) rgba8[p] = tone_rgba8(o, T);
     }
 }
 
@@ -710,6 +750,53 @@ void svgf_state_free(kgk_scene *s) {
 SvgfState *svgf_state(kgk_scene *s) {
     if (!s->svgf) s->svgf = new SvgfState();
     return s->svgf;
+}
+
+kgk_status tonemap_device(const float4 *in, size_t npx, uchar4 *out, cudaStream_t st) {
+    const int g = (int)std::min<size_t>((npx + 255) / 256, 4096);
+    k_tonemap<<<g, 256, 0, st>>>(in, npx, out, tone_table());
+    KGK_CUDA(cudaGetLastError());
+    return KGK_OK;
+}
+
+void output_state_free(kgk_scene *s) {
+    OutputState *O = s->out;
+    if (!O) return;
+    if (O->copy) cudaStreamSynchronize(O->copy);
+    for (int k = 0; k < 2; ++k) {
+        dfree(O->rgba8[k]);
+        if (O->done[k]) cudaEventDestroy(O->done[k]);
+        if (O->copied[k]) cudaEventDestroy(O->copied[k]);
+    }
+    if (O->copy) cudaStreamDestroy(O->copy);
+    delete O;
+    s->out = nullptr;
+}
+
+// The output double buffer for npx pixels (created on first use).
+kgk_status output_state(kgk_scene *s, size_t npx, OutputState **out) {
+    if (!s->out) {
+        OutputState *O = new OutputState();
+        s->out = O;
+        KGK_CUDA(cudaStreamCreateWithFlags(&O->copy, cudaStreamNonBlocking));
+        for (int k = 0; k < 2; ++k) {
+            KGK_CUDA(cudaEventCreateWithFlags(&O->done[k], cudaEventDisableTiming));
+            KGK_CUDA(cudaEventCreateWithFlags(&O->copied[k], cudaEventDisableTiming));
+        }
+    }
+    OutputState &O = *s->out;
+    if (O.npx < npx) {
+        KGK_CUDA(cudaStreamSynchronize(O.copy));
+        for (int k = 0; k < 2; ++k) {
+            dfree(O.rgba8[k]);
+            O.rgba8[k] = nullptr;
+        }
+        O.npx = 0;
+        for (int k = 0; k < 2; ++k) KGK_TRY(dalloc(&O.rgba8[k], npx, "RGBA8 output"));
+        O.npx = npx;
+    }
+    *out = &O;
+    return KGK_OK;
 }
 
 }  // namespace kgk
@@ -762,6 +849,13 @@ kgk_status kgk_svgf_apply(kgk_vec *result, kgk_vec *filtered, kgk_svgf_buffer *p
 
 kgk_status kgk_svgf(kgk_scene *s, const kgk_svgf_config *cfg, const kgk_vec *noisy, kgk_vec *filtered) {
     if (!s || !cfg || !noisy || !filtered) return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_svgf: NULL argument");
+    return kgk_svgf_output(s, cfg, noisy, filtered, nullptr, 0);
+}
+
+kgk_status kgk_svgf_output(kgk_scene *s, const kgk_svgf_config *cfg, const kgk_vec *noisy, kgk_vec *filtered,
+                           uint8_t *rgba8, int32_t async) {
+    if (!s || !cfg) return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_svgf: NULL argument");
+    if (!filtered && !rgba8) return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_svgf: no output buffer");
     KGK_CUDA(cudaSetDevice(s->device));
     int W, H;
     const float4 *gpos, *gnrm, *galb, *gemi;
@@ -793,12 +887,39 @@ kgk_status kgk_svgf(kgk_scene *s, const kgk_svgf_config *cfg, const kgk_vec *noi
         S.H = H;
         S.has_prev = false;
     }
-    // staging of host images
-    const bool dn = is_device_ptr(noisy), dfo = is_device_ptr(filtered);
+    // input: the frame kept on the device by kgk_render(out = NULL), a device
+    // image, or a host image staged here
+    const float4 *kept = nullptr;
+    if (!noisy) {
+        int kW = 0, kH = 0;
+        if (!render_kept_frame(s, &kW, &kH, &kept) || kW != W || kH != H)
+            return fail(KGK_ERR_INVALID_ARGUMENT,
+                        "kgk_svgf: noisy == NULL needs the last kgk_render to keep its frame (out == NULL)");
+    }
+    const bool dn = noisy && is_device_ptr(noisy), dfo = filtered && is_device_ptr(filtered);
     KGK_TRY(s->staging.reserve(2 * npx * sizeof(float4) + 256));
-    float4 *in = dn ? (float4 *)noisy : (float4 *)s->staging.ptr;
+    float4 *in = kept ? (float4 *)kept : (dn ? (float4 *)noisy : (float4 *)s->staging.ptr);
+    // the filtered frame: the caller's device buffer, else staging (copied to a
+    // host buffer below, or only tone-mapped)
     float4 *out = dfo ? (float4 *)filtered : (float4 *)((char *)s->staging.ptr + npx * sizeof(float4));
-    if (!dn) KGK_CUDA(cudaMemcpyAsync(in, noisy, npx * sizeof(float4), cudaMemcpyHostToDevice, st));
+    if (noisy && !dn) KGK_CUDA(cudaMemcpyAsync(in, noisy, npx * sizeof(float4), cudaMemcpyHostToDevice, st));
+    // RGBA8 output: the caller's device buffer, else this scene's double buffer
+    const bool d8 = rgba8 && is_device_ptr(rgba8);
+    OutputState *O = nullptr;
+    uchar4 *out8 = nullptr;
+    int slot = 0;
+    if (rgba8) {
+        if (d8) {
+            out8 = reinterpret_cast<uchar4 *>(rgba8);
+        } else {
+            KGK_TRY(output_state(s, npx, &O));
+            slot = O->slot;
+            O->slot ^= 1;
+            out8 = O->rgba8[slot];
+            // the copy that last read this buffer has finished
+            KGK_CUDA(cudaStreamWaitEvent(st, O->copied[slot], 0));
+        }
+    }
     const int g = (int)std::min<size_t>((npx + 255) / 256, 65535);
     if (cfg->mode == KGK_SVGF_COMPAT) {
         k_gbuffer_to_records<<<g, 256, 0, st>>>(gpos, gnrm, galb, gemi, (int)npx, S.cur);
@@ -810,6 +931,7 @@ kgk_status kgk_svgf(kgk_scene *s, const kgk_svgf_config *cfg, const kgk_vec *noi
         KGK_TRY(run_compat((kgk_vec *)R, (kgk_vec *)out, S.prev, S.cur, W, H, cfg->frame_index, reps, stages, st));
         // main.cu:232: the current buffer becomes the previous one
         KGK_CUDA(cudaMemcpyAsync(S.prev, S.cur, npx * sizeof(kgk_svgf_buffer), cudaMemcpyDeviceToDevice, st));
+        if (out8) KGK_TRY(tonemap_device(out, npx, out8, st));
     } else if (cfg->mode == KGK_SVGF_STANDARD) {
         if (cfg->frame_index == 0) S.has_prev = false;
         StdArgs a;
@@ -835,7 +957,7 @@ kgk_status kgk_svgf(kgk_scene *s, const kgk_svgf_config *cfg, const kgk_vec *noi
             if (i == 0) k_s_feedback<<<g, 256, 0, st>>>(a, dst);
             std::swap(src, dst);
         }
-        k_s_output<<<g, 256, 0, st>>>(a, src, out);
+        k_s_output<<<g, 256, 0, st>>>(a, src, filtered ? out : nullptr, out8, tone_table());
         k_s_save_prev<<<g, 256, 0, st>>>(a);
         KGK_CUDA(cudaGetLastError());
         std::swap(S.hist, S.hist_prev);
@@ -845,9 +967,40 @@ kgk_status kgk_svgf(kgk_scene *s, const kgk_svgf_config *cfg, const kgk_vec *noi
     } else {
         return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_svgf: unknown mode");
     }
-    if (!dfo) KGK_CUDA(cudaMemcpyAsync(filtered, out, npx * sizeof(float4), cudaMemcpyDeviceToHost, st));
-    KGK_CUDA(cudaStreamSynchronize(st));
+    if (O) {
+        // bring the bytes back on the copy stream, after this frame's filter
+        KGK_CUDA(cudaEventRecord(O->done[slot], st));
+        KGK_CUDA(cudaStreamWaitEvent(O->copy, O->done[slot], 0));
+        KGK_CUDA(cudaMemcpyAsync(rgba8, out8, npx * sizeof(uchar4), cudaMemcpyDeviceToHost, O->copy));
+        KGK_CUDA(cudaEventRecord(O->copied[slot], O->copy));
+        if (!async) KGK_CUDA(cudaStreamSynchronize(O->copy));
+    }
+    if (filtered && !dfo) KGK_CUDA(cudaMemcpyAsync(filtered, out, npx * sizeof(float4), cudaMemcpyDeviceToHost, st));
+    if (!async || (filtered && !dfo)) KGK_CUDA(cudaStreamSynchronize(st));
     return KGK_OK;
+}
+
+kgk_status kgk_scene_sync(kgk_scene *s) {
+    if (!s) return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_scene_sync: NULL scene");
+    KGK_CUDA(cudaSetDevice(s->device));
+    KGK_CUDA(cudaStreamSynchronize(s->stream));
+    if (s->out) KGK_CUDA(cudaStreamSynchronize(s->out->copy));
+    return KGK_OK;
+}
+
+kgk_status kgk_host_alloc(size_t bytes, void **out) {
+    if (!out) return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_host_alloc: NULL argument");
+    *out = nullptr;
+    const cudaError_t e = cudaHostAlloc(out, bytes ? bytes : 1, cudaHostAllocPortable);
+    if (e != cudaSuccess) {
+        *out = nullptr;
+        return cuda_fail(e, "kgk_host_alloc");
+    }
+    return KGK_OK;
+}
+
+void kgk_host_free(void *p) {
+    if (p) cudaFreeHost(p);
 }
 
 }  // extern "C"
