@@ -682,6 +682,83 @@ def run_c4(args):
     print(json.dumps(line), flush=True)
 
 
+def run_trace(args):
+    """Closest-hit queries alone (kgk_trace_closest, the batch form of
+    willIntersectWithTriangle_nonRecursive): the seeded parity ray sets of the
+    Cornell box (2^20 rays) and of the 5.2M-triangle field (2^22 rays), rays
+    and results in host memory.  value: the field's rays per device second;
+    e2e: the same call's wall clock with the host copies.  Beside it: the
+    GPU BVH build and the scene upload of the field (kgk_scene_create), and
+    the oracle's CPU traversal on all host threads (brute force for the box,
+    whose reference BVH is a single leaf; the oracle's CPU BVH for the field,
+    on a bounded sample of the rays)."""
+    from kagayaki_gb300 import Scene, scenes
+    from oracle import orc
+    res = {}
+    tris_f, mats_f, info = scenes.icosphere_field()
+    cases = [("cornell", *scenes.cornell_box()[:2], 1 << 20, None),
+             ("field", tris_f, mats_f, 1 << 22, info)]
+    for name, tris, mats, n, inf in cases:
+        lo, hi = (inf["lo"], inf["hi"]) if inf else scenes.scene_bounds(tris)
+        rays = scenes.parity_rays(n, lo, hi, seed=1)
+        t0 = time.perf_counter()
+        scene = Scene(tris, mats)
+        upload_s = time.perf_counter() - t0
+        bvh = scene.build_bvh()
+        for _ in range(args.warmup):
+            scene.trace_closest(rays)
+        dev_ms = 0.0
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            ids, t, st = scene.trace_closest(rays, with_stats=True)
+            dev_ms += st["ms_device"]
+        wall = time.perf_counter() - t0
+        scene.close()
+        r = {"rays": n, "triangles": len(tris), "mrays_per_s_device": round(n * args.steps / (dev_ms / 1e3) / 1e6, 1),
+             "mrays_per_s_e2e": round(n * args.steps / wall / 1e6, 1), "ms_device": round(dev_ms / args.steps, 3),
+             "bvh_build_ms": round(bvh["ms_build"], 1), "scene_upload_ms": round(1e3 * upload_s, 1),
+             "hits": int((ids >= 0).sum())}
+        if not args.no_cpu:
+            thr = orc.nthreads()
+            if name == "cornell":
+                t0 = time.perf_counter()
+                oids, ot = orc.closest_brute(tris, rays)
+                cs = time.perf_counter() - t0
+                ncpu = n
+                kind = "brute force over the 36 triangles (the reference's C1 BVH is one leaf)"
+            else:
+                ncpu = 1 << 20
+                L = orc.orc()
+                t0 = time.perf_counter()
+                b = L.orc_bvh_build(orc._ptr(tris), len(tris))
+                r["cpu_bvh_build_ms_1_thread"] = round(1e3 * (time.perf_counter() - t0), 1)
+                try:
+                    oids = np.empty(ncpu, np.int32)
+                    ot = np.empty(ncpu, np.float32)
+                    t0 = time.perf_counter()
+                    L.orc_bvh_closest(b, orc._ptr(rays), ncpu, orc._ptr(oids), orc._ptr(ot), thr)
+                    cs = time.perf_counter() - t0
+                finally:
+                    L.orc_bvh_free(b)
+                kind = f"the oracle's CPU BVH, first {ncpu} rays (build timed apart)"
+            r["cpu"] = {"mrays_per_s": round(ncpu / cs / 1e6, 3), "threads": thr, "sample": kind,
+                        "ids_equal": int((oids == ids[:ncpu]).sum()), "of": ncpu}
+        res[name] = r
+    f = res["field"]
+    line = {"metric": "Mrays/s", "value": f["mrays_per_s_device"], "unit": "Mrays/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": f["ms_device"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "seeded parity ray sets",
+            "config": {"workload": "closest-hit-parity-rays", "field_rays": 1 << 22, "cornell_rays": 1 << 20,
+                       "l2": "inputs larger than L2 (0.7 GB BVH+triangles for the field)"},
+            "e2e": {"value": f["mrays_per_s_e2e"], "unit": "Mrays/s", "h2d_bytes_per_step": 40 * (1 << 22),
+                    "d2h_bytes_per_step": 8 * (1 << 22)},
+            "cases": res}
+    if "cpu" in f:
+        line["cpu_baseline"] = {"value": f["cpu"]["mrays_per_s"], "unit": "Mrays/s", "cores": f["cpu"]["threads"],
+                                "kind": "port", "sample": f["cpu"]["sample"]}
+    print(json.dumps(line), flush=True)
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -719,11 +796,12 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
     ap.add_argument("--no-relmse", action="store_true", help="skip the plain-vs-cache relMSE study")
     ap.add_argument("--wave-paths", type=int, default=0, help="paths per wave (0 = the library default)")
-    ap.add_argument("--workload", default="frame", choices=["frame", "c1", "svgf-orbit", "c4", "mlp", "c5"],
+    ap.add_argument("--workload", default="frame",
+                    choices=["frame", "c1", "svgf-orbit", "c4", "mlp", "c5", "trace"],
                     help="frame: the 64-spp Mrays/s benchmark; c1: the Cornell box with the reference's "
                          "estimator (also with --impl reference); svgf-orbit: 60 frames at 1 spp + SVGF; c4: the "
                          "cache along the orbit; mlp: the radiance-cache network alone; c5: 10.6M triangles, 4K, "
-                         "textures, cache")
+                         "textures, cache; trace: closest-hit queries on the parity ray sets")
     ap.add_argument("--width", type=int, default=0, help="override the frame width (profiling cases)")
     ap.add_argument("--height", type=int, default=0, help="override the frame height")
     ap.add_argument("--spp", type=int, default=0, help="override the samples per pixel")
@@ -741,6 +819,8 @@ def main():
         run_c4(args)
     elif args.workload == "c5":
         run_c5(args)
+    elif args.workload == "trace":
+        run_trace(args)
     else:
         run_ours(args)
 

@@ -7,8 +7,11 @@
 // ImageBasedLighting.cuh:59-73) computed on the host in input order; this file
 // is compiled with -ffp-contract=off so the sums round the same way on every
 // host.  The unbiased estimator gets normalised CDFs accumulated in double.
+#include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
+#include <thread>
 #include <vector>
 
 #include "kgk_device.cuh"
@@ -62,6 +65,41 @@ template <class T> kgk_status upload(T **dst, const T *src, size_t n, const char
     return KGK_OK;
 }
 
+// Triangle records (156 B, the reference's layout) to the device layout:
+// vertices (3 float4) and attributes (normals, texcoords, material id with
+// the smooth-normal flag in bit 31; 4 float4).  A repacking, no arithmetic.
+__global__ void k_tri_soa(const kgk_triangle *__restrict__ raw, size_t n, float4 *__restrict__ verts,
+                          float4 *__restrict__ attr) {
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const kgk_triangle &t = raw[i];
+        verts[3 * i] = make_float4(t.v0.x, t.v0.y, t.v0.z, 0.0f);
+        verts[3 * i + 1] = make_float4(t.v1.x, t.v1.y, t.v1.z, 0.0f);
+        verts[3 * i + 2] = make_float4(t.v2.x, t.v2.y, t.v2.z, 0.0f);
+        const unsigned char smooth = reinterpret_cast<const unsigned char *>(&t)[148];
+        const unsigned bits = ((unsigned)t.material_id & 0x7fffffffu) | (smooth ? 0x80000000u : 0u);
+        attr[4 * i] = make_float4(t.v0_vn.x, t.v0_vn.y, t.v0_vn.z, t.v0_vt.x);
+        attr[4 * i + 1] = make_float4(t.v1_vn.x, t.v1_vn.y, t.v1_vn.z, t.v0_vt.y);
+        attr[4 * i + 2] = make_float4(t.v2_vn.x, t.v2_vn.y, t.v2_vn.z, t.v1_vt.x);
+        attr[4 * i + 3] = make_float4(t.v1_vt.y, t.v2_vt.x, t.v2_vt.y, __uint_as_float(bits));
+    }
+}
+
+// Runs f(begin, end) over [0, n) in blocks on the host's threads.
+template <class F>
+void host_blocks(size_t n, size_t block, F f) {
+    const size_t nb = (n + block - 1) / block;
+    const unsigned hw = std::max(1u, std::min(64u, std::thread::hardware_concurrency()));
+    const size_t nt = std::min<size_t>(nb, hw);
+    std::atomic<size_t> next{0};
+    auto work = [&]() {
+        for (size_t b; (b = next.fetch_add(1)) < nb;) f(b * block, std::min(n, (b + 1) * block));
+    };
+    std::vector<std::thread> pool;
+    for (size_t k = 1; k < nt; ++k) pool.emplace_back(work);
+    work();
+    for (std::thread &th : pool) th.join();
+}
+
 }  // namespace
 
 kgk_status scene_upload(DevScene &s, const kgk_triangle *tris_in, size_t n, const kgk_material *mats_in,
@@ -71,71 +109,109 @@ kgk_status scene_upload(DevScene &s, const kgk_triangle *tris_in, size_t n, cons
     if (!mats_in || nm == 0) return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_scene_create: no materials");
     if (n > (size_t)600000000) return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_scene_create: too many triangles");
     if (ntex > 0 && !tex) return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_scene_create: textures == NULL");
-    std::vector<kgk_triangle> tris;
+    // Host triangle records are read in place: copied as they are to the
+    // device (and repacked there by k_tri_soa) while host threads check the
+    // material ids and compute the bounds and the per-triangle light terms.
+    std::vector<kgk_triangle> tris_copy;
+    const kgk_triangle *tris = tris_in;
+    const bool tris_dev = is_device_ptr(tris_in);
+    if (tris_dev) {
+        KGK_TRY(to_host(tris_in, n, tris_copy));
+        tris = tris_copy.data();
+    }
     std::vector<kgk_material> mats;
-    KGK_TRY(to_host(tris_in, n, tris));
     KGK_TRY(to_host(mats_in, nm, mats));
-    for (size_t i = 0; i < n; ++i)
-        if (tris[i].material_id < 0 || (size_t)tris[i].material_id >= nm)
-            return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_scene_create: triangle " + std::to_string(i) +
-                                                      " has material_id " + std::to_string(tris[i].material_id) +
-                                                      " outside [0, " + std::to_string(nm) + ")");
     for (size_t i = 0; i < nm; ++i)
         if (mats[i].TEXTURE_BASECOLOR_ID >= (int)ntex || mats[i].TEXTURE_BASECOLOR_ID < -1)
             return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_scene_create: material " + std::to_string(i) +
                                                       " names a missing texture");
-
+    struct DevBuf {
+        kgk_triangle *p = nullptr;
+        ~DevBuf() { dfree(p); }
+    } raw;
+    KGK_TRY(dalloc(&raw.p, n, "triangle records (upload)"));
+    KGK_TRY(dalloc(&s.verts, 3 * n, "triangle vertices"));
+    KGK_TRY(dalloc(&s.attr, 4 * n, "triangle attributes"));
+    // emission length per material; per-triangle term area * |emission|
+    // (calculate_Lss's summand, the same float expression)
+    std::vector<float> elen(nm), term(n);
+    for (size_t m = 0; m < nm; ++m) elen[m] = hlen(hv(mats[m].emission));
+    const size_t block = 1 << 16;
+    const size_t nb = (n + block - 1) / block;
+    std::vector<size_t> bad(nb, SIZE_MAX);
+    std::vector<float> blo(3 * nb, INFINITY), bhi(3 * nb, -INFINITY);
+    auto host_pass = [&]() {
+    host_blocks(n, block, [&](size_t i0, size_t i1) {
+        const size_t b = i0 / block;
+        float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+        for (size_t i = i0; i < i1; ++i) {
+            const kgk_triangle &t = tris[i];
+            if (t.material_id < 0 || (size_t)t.material_id >= nm) {
+                if (bad[b] == SIZE_MAX) bad[b] = i;
+                continue;
+            }
+            const kgk_vec *vs[3] = {&t.v0, &t.v1, &t.v2};
+            for (const kgk_vec *v : vs) {
+                const float c[3] = {v->x, v->y, v->z};
+                for (int a = 0; a < 3; ++a) {
+                    lo[a] = std::fmin(lo[a], c[a]);
+                    hi[a] = std::fmax(hi[a], c[a]);
+                }
+            }
+            term[i] = tri_area(t) * elen[t.material_id];
+        }
+        for (int a = 0; a < 3; ++a) {
+            blo[3 * b + a] = lo[a];
+            bhi[3 * b + a] = hi[a];
+        }
+    });
+    };
+    {
+        // the host pass runs while this thread copies the records (a copy
+        // from pageable memory holds the calling thread until it is staged)
+        std::thread pass(host_pass);
+        const cudaError_t e1 = cudaMemcpyAsync(raw.p, tris_in, n * sizeof(kgk_triangle),
+                                               tris_dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, st);
+        if (e1 == cudaSuccess)
+            k_tri_soa<<<(int)std::min<size_t>((n + 255) / 256, 8192), 256, 0, st>>>(raw.p, n, s.verts, s.attr);
+        const cudaError_t e2 = cudaGetLastError();
+        pass.join();
+        if (e1 != cudaSuccess) return cuda_fail(e1, "triangle upload");
+        if (e2 != cudaSuccess) return cuda_fail(e2, "k_tri_soa");
+    }
+    for (size_t b = 0; b < nb; ++b)
+        if (bad[b] != SIZE_MAX) {
+            cudaStreamSynchronize(st);
+            const size_t i = bad[b];
+            return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_scene_create: triangle " + std::to_string(i) +
+                                                      " has material_id " + std::to_string(tris[i].material_id) +
+                                                      " outside [0, " + std::to_string(nm) + ")");
+        }
     s.n_tris = (int32_t)n;
     s.n_mats = (int32_t)nm;
     for (int a = 0; a < 3; ++a) {
         s.lo[a] = INFINITY;
         s.hi[a] = -INFINITY;
-    }
-    for (size_t i = 0; i < n; ++i) {
-        const kgk_vec *vs[3] = {&tris[i].v0, &tris[i].v1, &tris[i].v2};
-        for (const kgk_vec *v : vs) {
-            const float c[3] = {v->x, v->y, v->z};
-            for (int a = 0; a < 3; ++a) {
-                s.lo[a] = std::fmin(s.lo[a], c[a]);
-                s.hi[a] = std::fmax(s.hi[a], c[a]);
-            }
+        for (size_t b = 0; b < nb; ++b) {
+            s.lo[a] = std::fmin(s.lo[a], blo[3 * b + a]);
+            s.hi[a] = std::fmax(s.hi[a], bhi[3 * b + a]);
         }
-    }
-    // vertices and attributes
-    {
-        std::vector<float4> verts(3 * n), attr(4 * n);
-        for (size_t i = 0; i < n; ++i) {
-            const kgk_triangle &t = tris[i];
-            verts[3 * i] = make_float4(t.v0.x, t.v0.y, t.v0.z, 0.0f);
-            verts[3 * i + 1] = make_float4(t.v1.x, t.v1.y, t.v1.z, 0.0f);
-            verts[3 * i + 2] = make_float4(t.v2.x, t.v2.y, t.v2.z, 0.0f);
-            unsigned bits = ((unsigned)t.material_id & 0x7fffffffu) | (t.is_SmoothNormal ? 0x80000000u : 0u);
-            float fb;
-            memcpy(&fb, &bits, 4);
-            attr[4 * i] = make_float4(t.v0_vn.x, t.v0_vn.y, t.v0_vn.z, t.v0_vt.x);
-            attr[4 * i + 1] = make_float4(t.v1_vn.x, t.v1_vn.y, t.v1_vn.z, t.v0_vt.y);
-            attr[4 * i + 2] = make_float4(t.v2_vn.x, t.v2_vn.y, t.v2_vn.z, t.v1_vt.x);
-            attr[4 * i + 3] = make_float4(t.v1_vt.y, t.v2_vt.x, t.v2_vt.y, fb);
-        }
-        KGK_TRY(upload(&s.verts, verts.data(), verts.size(), "triangle vertices", st));
-        KGK_TRY(upload(&s.attr, attr.data(), attr.size(), "triangle attributes", st));
-        KGK_CUDA(cudaStreamSynchronize(st));
     }
     KGK_TRY(upload(&s.mats, mats.data(), nm, "materials", st));
-
-    // face lights: the reference's running FP32 sum (calculate_Lss)
+    // face lights: the reference's running FP32 sum (calculate_Lss), in input order
     {
         std::vector<float> cdf(n);
         std::vector<int32_t> ids;
         std::vector<double> w;
-        auto emis_len = [&](int m) { return hlen(hv(mats[m].emission)); };
-        cdf[0] = tri_area(tris[0]) * emis_len(tris[0].material_id);
-        for (size_t i = 1; i < n; ++i) cdf[i] = cdf[i - 1] + tri_area(tris[i]) * emis_len(tris[i].material_id);
+        cdf[0] = term[0];
+        for (size_t i = 1; i < n; ++i) cdf[i] = cdf[i - 1] + term[i];
         s.no_light = cdf[n - 1] == 0.0f ? 1 : 0;
         KGK_TRY(upload(&s.light_cdf_ref, cdf.data(), n, "light CDF", st));
         double total = 0.0;
         for (size_t i = 0; i < n; ++i) {
-            double wi = (double)tri_area(tris[i]) * (double)emis_len(tris[i].material_id);
+            const float e = elen[tris[i].material_id];
+            if (!(e > 0.0f)) continue;  // the weight would be 0 (or NaN): not an emitter
+            const double wi = (double)tri_area(tris[i]) * (double)e;
             if (wi > 0.0) {
                 ids.push_back((int32_t)i);
                 w.push_back(wi);
