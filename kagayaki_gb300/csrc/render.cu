@@ -1,19 +1,24 @@
 // render.cu - wavefront path tracer.  Replaces the per-pixel megakernel
 // render<<<W*H/256, 256>>> (render.cuh:21-49, RayTrace.cuh:9-109).
 //
-// One wave = one path per (pixel, sample) pair, state in SoA arrays indexed by
-// path id.  Per bounce:
-//   extend  closest hit of every active path; paths are appended to one of
-//           three shade queues (miss, Lambert, Disney) with warp-ballot
-//           compaction, so shading warps are material-coherent;
-//   shade   emission, Russian roulette, next-event estimation (shadow-ray
-//           records with their contribution precomputed), BSDF sampling;
-//           continuing paths are compacted into the next active queue;
+// One wave = one path per (pixel, sample) pair.  The live paths' state sits
+// densely in SoA arrays (two buffers, used in turn): slot i of the current
+// buffer holds the i-th live path, with its id (pixel + sample * pixels).
+// Per bounce:
+//   extend  closest hit of every live path, written to hit[slot]; the slot
+//           goes to the hit or the miss queue (warp-ballot appends);
+//   shade   misses: the sky lookup, the path ends; hits: emission, Russian
+//           roulette, next-event estimation (shadow-ray records with their
+//           contribution precomputed), BSDF sampling.  A continuing path's
+//           state moves to the next buffer at the slot a warp-ballot append
+//           gives it, a finished path's radiance goes to fin[id] - so the
+//           kernels read and write the state of neighbouring slots together;
 //   shadow  two passes (face lights, environment) - at most one record per
-//           path per pass, so each adds to its path's radiance without atomics
-//           and in the reference's order (face light, then environment).
-// Kernels are persistent grid-stride loops that read their queue length from
-// device memory: the host never waits inside a wave.
+//           path per pass, so each adds to its path's radiance (in the next
+//           buffer, or in fin) without atomics and in the reference's order
+//           (face light, then environment).
+// Kernels are persistent grid-stride loops that read their counts from device
+// memory: the host only reads the live count between bounces.
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -25,11 +30,25 @@
 
 namespace kgk {
 
-// Device bytes per path in flight (ensure_wave): 5 float4 of state, rng,
-// depth, two alive queues, three shade queues, two shadow queues of three
-// float4; with the cache also its spread, flags and query record.
-constexpr size_t kPathStateBytes = 5 * 16 + 8 + 4 + 2 * 4 + 3 * 4 + 2 * 3 * 16;
-constexpr size_t kCachePathBytes = 8 + 4 + 20 * 4;
+// Device bytes per path in flight (ensure_wave): two buffers of state (4
+// float4, rng, depth, id), the final radiance and the hit (float4 each), the
+// hit and miss slot queues, two shadow queues of three float4; with the cache
+// also its spread and flags (two buffers) and a query record.
+constexpr size_t kPathStateBytes = 2 * (4 * 16 + 8 + 4 + 4) + 2 * 16 + 2 * 4 + 2 * 3 * 16;
+constexpr size_t kCachePathBytes = 2 * (8 + 4) + 20 * 4;
+
+// Live path state, one buffer (slot = position among the live paths).
+struct PathBuf {
+    float4 *o = nullptr;              // origin
+    float4 *d = nullptr;              // direction, w: pdf of the sampled direction (0 = no MIS)
+    float4 *thr = nullptr;            // throughput
+    float4 *rad = nullptr;            // radiance gathered so far
+    unsigned long long *rng = nullptr;
+    int *depth = nullptr;
+    int *id = nullptr;                // path id: pixel + sample * pixels
+    float2 *spread = nullptr;         // cache: (sqrt-summed path spread, primary footprint)
+    int *pflags = nullptr;            // cache: bit 0 training path, bit 1 queried, bits 8.. suffix bounces
+};
 
 struct RenderState {
     int W = 0, H = 0;                         // per-pixel buffers
@@ -47,17 +66,14 @@ struct RenderState {
     float4 *gb_emi = nullptr;   // emission, hit flag
     // wave state (capacity cap paths)
     int cap = 0;
-    float4 *o = nullptr, *d = nullptr, *thr = nullptr, *rad = nullptr, *hit = nullptr;
-    unsigned long long *rng = nullptr;
-    int *depth = nullptr;
-    int *aq[2] = {nullptr, nullptr};
-    int *sq[3] = {nullptr, nullptr, nullptr};
+    PathBuf pb[2];                            // live path state, used in turn
+    float4 *fin = nullptr;                    // final radiance by path id
+    float4 *hit = nullptr;                    // closest hit by slot (t, u, v, triangle id or -1)
+    int *hq = nullptr, *mq = nullptr;         // slots whose ray hit / missed the scene
     float4 *sh_o[2] = {nullptr, nullptr}, *sh_d[2] = {nullptr, nullptr}, *sh_c[2] = {nullptr, nullptr};
     int *cnt = nullptr;                       // queue counters
     unsigned long long *stats = nullptr;      // rays_closest, rays_shadow, overflow, nodes, tris
-    // radiance cache (capacity cap paths)
-    float2 *spread = nullptr;                 // (sqrt-summed path spread, primary footprint)
-    int *pflags = nullptr;                    // bit 0 training path, bit 1 queried, bits 8.. suffix bounces
+    // radiance cache (capacity cap paths; spread and flags are in pb)
     float *qrec = nullptr;                    // query records, kQRec floats each
     float *trec = nullptr;                    // training records, kQRec floats each
     float *ttgt = nullptr;                    // training targets (3 per record)
@@ -72,12 +88,12 @@ struct RenderState {
 
 namespace {
 
-// Device counters: alive-queue sizes (double-buffered), shade-queue sizes,
-// shadow-queue sizes, dynamic-fetch cursors of the extend and shadow kernels
-// (zeroed before every bounce together with the queues), cache record counts.
+// Device counters: live paths in each state buffer, shadow-queue sizes,
+// dynamic-fetch cursors of the extend and shadow kernels, hit and miss queue
+// sizes (zeroed before every bounce together with the shadow queues), cache
+// record counts.
 enum Cnt {
-    kA0 = 0, kA1 = 1, kSQ0 = 2, kSQ1 = 3, kSQ2 = 4, kSH0 = 5, kSH1 = 6, kFE = 7, kFS0 = 8, kFS1 = 9,
-    kQN = 10, kTN = 11, kNCnt = 12
+    kA0 = 0, kA1 = 1, kSH0 = 2, kSH1 = 3, kFE = 4, kFS0 = 5, kFS1 = 6, kHQ = 7, kMQ = 8, kQN = 9, kTN = 10, kNCnt = 11
 };
 // Lanes of a warp that must be idle before the warp fetches new rays.
 constexpr int kRefill = 8;
@@ -102,23 +118,60 @@ struct Params {
     int count_work;
     unsigned long long seed;
     int frame_index;
-    // state
-    float4 *o, *d, *thr, *rad, *hit;
-    unsigned long long *rng;
-    int *depth;
+    // state: the bounce's live paths (cur), the next bounce's (nxt)
+    PathBuf cur, nxt;
+    float4 *fin, *hit;
     unsigned long long *seeds;
     float4 *gb_pos, *gb_nrm, *gb_alb, *gb_emi;
     int *cnt;
     unsigned long long *stats;
     // radiance cache
     int use_cache;
-    float2 *spread;
-    int *pflags;
     float *qrec, *trec;
     int tcap;
     int train_stride, train_offset, suffix_max;
     float spread_c;
 };
+
+// One live path in registers.
+struct PathState {
+    float3 o, d, T, rad;
+    float pdf;                 // of the sampled direction d (0 = no MIS)
+    unsigned long long rs;
+    int depth, id;
+    float2 sp;                 // cache only
+    int fl;                    // cache only
+};
+
+__device__ __forceinline__ PathState load_path(const PathBuf &b, int i, bool cache) {
+    PathState s;
+    const float4 o = b.o[i], d = b.d[i], t = b.thr[i], r = b.rad[i];
+    s.o = f3(o);
+    s.d = f3(d);
+    s.pdf = d.w;
+    s.T = f3(t);
+    s.rad = f3(r);
+    s.rs = b.rng[i];
+    s.depth = b.depth[i];
+    s.id = b.id[i];
+    s.sp = cache ? b.spread[i] : make_float2(0.0f, 0.0f);
+    s.fl = cache ? b.pflags[i] : 0;
+    return s;
+}
+
+__device__ __forceinline__ void store_path(const PathBuf &b, int k, const PathState &s, bool cache) {
+    b.o[k] = make_float4(s.o.x, s.o.y, s.o.z, 0.0f);
+    b.d[k] = make_float4(s.d.x, s.d.y, s.d.z, s.pdf);
+    b.thr[k] = make_float4(s.T.x, s.T.y, s.T.z, 0.0f);
+    b.rad[k] = make_float4(s.rad.x, s.rad.y, s.rad.z, 0.0f);
+    b.rng[k] = s.rs;
+    b.depth[k] = s.depth;
+    b.id[k] = s.id;
+    if (cache) {
+        b.spread[k] = s.sp;
+        b.pflags[k] = s.fl;
+    }
+}
 
 __device__ __forceinline__ int warp_append(int *counter, bool pred) {
     const unsigned m = __ballot_sync(~0u, pred);
@@ -175,30 +228,33 @@ __global__ void k_raygen(Params P) {
             const float jx = rnd_u(s) - 0.5f, jy = rnd_u(s) - 0.5f;
             dir = primary_dir(P.cam, P.W, P.H, (float)X + jx, (float)Y + jy);
         }
-        P.o[i] = make_float4(P.cam.CamOrg.x, P.cam.CamOrg.y, P.cam.CamOrg.z, 0.0f);
-        P.d[i] = make_float4(dir.x, dir.y, dir.z, 0.0f);  // w: pdf of the sampled direction (0 = no MIS)
-        P.thr[i] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
+        const PathBuf &b = P.cur;
+        b.o[i] = make_float4(P.cam.CamOrg.x, P.cam.CamOrg.y, P.cam.CamOrg.z, 0.0f);
+        b.d[i] = make_float4(dir.x, dir.y, dir.z, 0.0f);  // w: pdf of the sampled direction (0 = no MIS)
+        b.thr[i] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
         const float r0 = P.estimator == KGK_ESTIMATOR_COMPAT ? kSINF : 0.0f;  // RayTrace.cuh:14
-        P.rad[i] = make_float4(r0, r0, r0, 0.0f);
-        P.rng[i] = s;
-        P.depth[i] = 0;
+        b.rad[i] = make_float4(r0, r0, r0, 0.0f);
+        b.rng[i] = s;
+        b.depth[i] = 0;
+        b.id[i] = i;
         if (P.use_cache) {
-            P.spread[i] = make_float2(0.0f, 0.0f);
+            b.spread[i] = make_float2(0.0f, 0.0f);
             const bool train = P.train_stride > 0 && i < P.npx && (i % P.train_stride) == P.train_offset;
-            P.pflags[i] = train ? 1 : 0;
+            b.pflags[i] = train ? 1 : 0;
         }
     }
 }
 
 // ---------------------------------------------------------------------------
-// Closest hit for every ray of the queue (q == nullptr: paths 0..dense_n-1),
-// then the path goes to the miss, Lambert or Disney shade queue.  Each warp
-// keeps its lanes busy: when kRefill or more lanes have finished, they take
-// the next rays from the queue (one atomic per warp).
+// Closest hit of every live path (slots 0..n-1 of the current buffer; n from
+// counter cnt_idx, or dense_n when cnt_idx < 0), written to hit[slot]; the
+// slot goes to the hit or the miss queue (warp-ballot appends), so shading
+// warps are either all surface hits or all misses.  Each warp keeps its lanes
+// busy: when kRefill or more lanes have finished, they take the next rays
+// (one atomic per warp).
 template <bool kCount>
-__global__ void __launch_bounds__(128) k_extend(Params P, const int *__restrict__ q, int qcnt_idx, int dense_n,
-                                                int *sq0, int *sq1, int *sq2) {
-    const int n = q ? P.cnt[qcnt_idx] : dense_n;
+__global__ void __launch_bounds__(128) k_extend(Params P, int cnt_idx, int dense_n, int *hq, int *mq) {
+    const int n = cnt_idx >= 0 ? P.cnt[cnt_idx] : dense_n;
     const DevScene &s = P.sc;
     int *fetch = &P.cnt[kFE];
     const unsigned lane = threadIdx.x & 31u;
@@ -220,8 +276,8 @@ __global__ void __launch_bounds__(128) k_extend(Params P, const int *__restrict_
             if (!active) {
                 const int i = base + __popc(idle & lt);
                 if (i < n) {
-                    p = q ? q[i] : i;
-                    const float4 o = P.o[p], d = P.d[p];
+                    p = i;
+                    const float4 o = P.cur.o[p], d = P.cur.d[p];
                     r = make_ray(f3(o), f3(d));
                     trav_init(c, kBigT);
                     active = true;
@@ -234,23 +290,15 @@ __global__ void __launch_bounds__(128) k_extend(Params P, const int *__restrict_
                                         false, st)) {
             active = false;
             ++rays;
-            if (c.hit_slot < 0) {
-                cls = 0;
-                P.hit[p] = make_float4(kBigT, 0.0f, 0.0f, __int_as_float(-1));
-            } else {
-                P.hit[p] = make_float4(c.best_t, c.bu, c.bv, __int_as_float(c.best_id));
-                const unsigned bits = __float_as_uint(__ldg(&s.attr[4 * c.best_id + 3].w));
-                const int mid = (int)(bits & 0x7fffffffu);
-                cls = __ldg(&s.mats[mid].MATERIAL_TYPE_ID) == 1 ? 2 : 1;
-            }
+            cls = c.hit_slot < 0 ? 0 : 1;
+            P.hit[p] = c.hit_slot < 0 ? make_float4(kBigT, 0.0f, 0.0f, __int_as_float(-1))
+                                      : make_float4(c.best_t, c.bu, c.bv, __int_as_float(c.best_id));
         }
         if (__any_sync(~0u, cls >= 0)) {
-            const int a0 = warp_append(&P.cnt[kSQ0], cls == 0);
-            const int a1 = warp_append(&P.cnt[kSQ1], cls == 1);
-            const int a2 = warp_append(&P.cnt[kSQ2], cls == 2);
-            if (cls == 0) sq0[a0] = p;
-            if (cls == 1) sq1[a1] = p;
-            if (cls == 2) sq2[a2] = p;
+            const int am = warp_append(&P.cnt[kMQ], cls == 0);
+            const int ah = warp_append(&P.cnt[kHQ], cls == 1);
+            if (cls == 0) mq[am] = p;
+            if (cls == 1) hq[ah] = p;
         }
     }
     warp_add_u64(&P.stats[kRaysC], rays);
@@ -309,12 +357,12 @@ __device__ __forceinline__ float3 diffuse_of(const kgk_material &m) { return f3(
 
 __device__ __forceinline__ void push_shadow(const Params &P, float4 *so, float4 *sd, float4 *sc, int cidx,
                                             bool pred, float3 org, float3 dir, float tmax, int light,
-                                            float3 contrib, int path) {
+                                            float3 contrib, int target) {
     const int k = warp_append(&P.cnt[cidx], pred);
     if (pred) {
         so[k] = make_float4(org.x, org.y, org.z, tmax);
         sd[k] = make_float4(dir.x, dir.y, dir.z, __int_as_float(light));
-        sc[k] = make_float4(contrib.x, contrib.y, contrib.z, __int_as_float(path));
+        sc[k] = make_float4(contrib.x, contrib.y, contrib.z, __int_as_float(target));
     }
 }
 
@@ -349,8 +397,35 @@ struct ShadeOut {
     int f_light;
 };
 
-// One shading event of path p in the reference's estimator (see shade_unbiased_core).
-__device__ __forceinline__ void shade_compat_core(const Params &P, int p, ShadeOut &out) {
+// A path that left the scene (either estimator): its G-buffer record when it
+// is a first-sample camera ray, and the sky (or background) radiance it
+// gathers - RayTrace.cuh:21-35 for the reference's estimator; with the
+// environment's MIS weight against the sampled direction's pdf for the
+// unbiased one.
+template <int kEst>
+__device__ __forceinline__ void shade_miss(const Params &P, float3 d, float prev_pdf, float3 T, float3 &rad,
+                                           int depth, int path) {
+    const DevScene &s = P.sc;
+    const int px = path % P.npx;
+    if (depth == 0 && P.write_gbuffer && path < P.npx) write_gbuffer(P, px, nullptr);
+    if (kEst == KGK_ESTIMATOR_COMPAT) {
+        rad += T * env_or_bg_ref(s, d);
+    } else if (s.env) {
+        const float3 Le = env_lookup_u(s, d);
+        float wgt = 1.0f;
+        if (prev_pdf > 0.0f) {
+            const float pe = env_pdf_u(s, d);
+            wgt = prev_pdf / (prev_pdf + pe);
+        }
+        rad += T * Le * wgt;
+    } else {
+        rad += T;  // background (1,1,1), no light sampling for it
+    }
+}
+
+// One shading event of path ps (hit h) in the reference's estimator (see
+// shade_unbiased_core).
+__device__ __forceinline__ void shade_compat_core(const Params &P, PathState &ps, float4 h, ShadeOut &out) {
     const DevScene &s = P.sc;
     bool cont = false;
     bool f_pred = false, e_pred = false;
@@ -360,21 +435,16 @@ __device__ __forceinline__ void shade_compat_core(const Params &P, int p, ShadeO
     float3 npos, ndir, T;
     unsigned long long rs = 0;
     {
-        const float4 o4 = P.o[p], d4 = P.d[p], h = P.hit[p];
-        const float3 o = f3(o4), d = f3(d4);
-        T = f3(P.thr[p]);
-        float3 rad = f3(P.rad[p]);
-        rs = P.rng[p];
-        const int depth = P.depth[p];
+        const float3 o = ps.o, d = ps.d;
+        T = ps.T;
+        float3 rad = ps.rad;
+        rs = ps.rs;
+        const int depth = ps.depth;
         const int id = __float_as_int(h.w);
-        const int px = p % P.npx;
-        const bool first_sample = p < P.npx;
+        const int px = ps.id % P.npx;
+        const bool first_sample = ps.id < P.npx;
         if (id < 0) {
-            if (depth == 0 && P.write_gbuffer && first_sample) {
-                write_gbuffer(P, px, nullptr);
-                P.gb_nrm[px] = make_float4(0.0f, 0.0f, 0.0f, __int_as_float(-1));
-            }
-            rad += T * env_or_bg_ref(s, d);  // RayTrace.cuh:21-35
+            shade_miss<KGK_ESTIMATOR_COMPAT>(P, d, 0.0f, T, rad, depth, ps.id);
         } else {
             Surface S = load_surface(s, id, h, o, d);
             const float3 n = S.n;
@@ -534,14 +604,15 @@ __device__ __forceinline__ void shade_compat_core(const Params &P, int p, ShadeO
                 cont = P.max_depth <= 0 || depth + 1 < P.max_depth;
             }
         }
-        P.rad[p] = make_float4(rad.x, rad.y, rad.z, 0.0f);
+        ps.rad = rad;
         if (cont) {
-            P.o[p] = make_float4(npos.x, npos.y, npos.z, 0.0f);
-            P.d[p] = make_float4(ndir.x, ndir.y, ndir.z, 0.0f);
-            P.thr[p] = make_float4(T.x, T.y, T.z, 0.0f);
-            P.depth[p] = depth + 1;
+            ps.o = npos;
+            ps.d = ndir;
+            ps.pdf = 0.0f;
+            ps.T = T;
+            ps.depth = depth + 1;
         }
-        P.rng[p] = rs;
+        ps.rs = rs;
         if (!cont) P.seeds[px] = rs;  // randSeeds[pos] = rand.seed (render.cuh:42)
     }
     out.cont = cont;
@@ -555,16 +626,6 @@ __device__ __forceinline__ void shade_compat_core(const Params &P, int p, ShadeO
     out.e_c = e_c;
     out.f_tmax = f_tmax;
     out.f_light = f_light;
-}
-
-__device__ void shade_compat(const Params &P, int p, bool valid, int *next_q, int next_cnt, float4 *so0,
-                             float4 *sd0, float4 *sc0, float4 *so1, float4 *sd1, float4 *sc1) {
-    ShadeOut o{};
-    if (valid) shade_compat_core(P, p, o);
-    const int k = warp_append(&P.cnt[next_cnt], o.cont);
-    if (o.cont) next_q[k] = p;
-    push_shadow(P, so0, sd0, sc0, kSH0, o.f_pred, o.f_org, o.f_dir, o.f_tmax, o.f_light, o.f_c, p);
-    push_shadow(P, so1, sd1, sc1, kSH1, o.e_pred, o.spos, o.e_dir, kBigT, -1, o.e_c, p);
 }
 
 // ---------------------------------------------------------------------------
@@ -613,10 +674,10 @@ __device__ __forceinline__ void write_cache_record(const Params &P, float *rec, 
     rec[17] = rad.x; rec[18] = rad.y; rec[19] = rad.z;
 }
 
-// One unbiased shading event of path p (its hit is in P.hit): emission, the
-// cache decisions, Russian roulette, the two NEE samples (returned in `o` as
-// shadow-ray records, not traced) and the BSDF sample (path state updated).
-__device__ __forceinline__ void shade_unbiased_core(const Params &P, int p, ShadeOut &out) {
+// One unbiased shading event of path ps (hit h): emission, the cache
+// decisions, Russian roulette, the two NEE samples (returned in `out` as
+// shadow-ray records, not traced) and the BSDF sample (ps updated).
+__device__ __forceinline__ void shade_unbiased_core(const Params &P, PathState &ps, float4 h, ShadeOut &out) {
     const DevScene &s = P.sc;
     bool cont = false, f_pred = false, e_pred = false;
     float3 spos = f3(0.0f, 0.0f, 0.0f), f_dir = spos, f_c = spos, e_dir = spos, e_c = spos;
@@ -624,29 +685,17 @@ __device__ __forceinline__ void shade_unbiased_core(const Params &P, int p, Shad
     float3 ndir = spos, T = spos;
     unsigned long long rs = 0;
     {
-        const float4 o4 = P.o[p], d4 = P.d[p], h = P.hit[p];
-        const float3 o = f3(o4), d = f3(d4);
-        const float prev_pdf = d4.w;  // 0: no MIS (camera ray)
-        T = f3(P.thr[p]);
-        float3 rad = f3(P.rad[p]);
-        rs = P.rng[p];
-        const int depth = P.depth[p];
+        const float3 o = ps.o, d = ps.d;
+        const float prev_pdf = ps.pdf;  // 0: no MIS (camera ray)
+        T = ps.T;
+        float3 rad = ps.rad;
+        rs = ps.rs;
+        const int depth = ps.depth;
         const int id = __float_as_int(h.w);
-        const int px = p % P.npx;
-        const bool first_sample = p < P.npx;
+        const int px = ps.id % P.npx;
+        const bool first_sample = ps.id < P.npx;
         if (id < 0) {
-            if (depth == 0 && P.write_gbuffer && first_sample) write_gbuffer(P, px, nullptr);
-            if (s.env) {
-                const float3 Le = env_lookup_u(s, d);
-                float wgt = 1.0f;
-                if (prev_pdf > 0.0f) {
-                    const float pe = env_pdf_u(s, d);
-                    wgt = prev_pdf / (prev_pdf + pe);
-                }
-                rad += T * Le * wgt;
-            } else {
-                rad += T;  // background (1,1,1), no light sampling for it
-            }
+            shade_miss<KGK_ESTIMATOR_UNBIASED>(P, d, prev_pdf, T, rad, depth, ps.id);
         } else {
             Surface S = load_surface(s, id, h, o, d);
             const float3 n = S.n, wo = -d;
@@ -669,32 +718,32 @@ __device__ __forceinline__ void shade_unbiased_core(const Params &P, int p, Shad
             bool to_cache = false;
             if (P.use_cache) {
                 // path spread (sqrt-summed) against the primary footprint
-                float2 sp = P.spread[p];
+                float2 sp = ps.sp;
                 const float cosl = fmaxf(fabsf(dot3(S.ng, d)), 1e-4f);
                 if (depth == 0) sp.y = S.t * S.t / (4.0f * kPI * cosl);
                 else sp.x += sqrtf(S.t * S.t / (fmaxf(prev_pdf, 1e-8f) * cosl));
-                P.spread[p] = sp;
-                int fl = P.pflags[p];
+                ps.sp = sp;
+                int fl = ps.fl;
                 const bool wide = depth >= 1 && sp.x * sp.x > P.spread_c * sp.y;
                 if (fl & 1) {
                     if (!(fl & 2)) {
                         if (wide) {  // training path: record the query vertex, keep going
                             const int k = atomicAdd(&P.cnt[kTN], 1);
-                            if (k < P.tcap) write_cache_record(P, P.trec + (size_t)k * kQRec, S, -d, T, p, rad);
+                            if (k < P.tcap) write_cache_record(P, P.trec + (size_t)k * kQRec, S, -d, T, ps.id, rad);
                             fl |= 2;
                         }
                     } else {
                         fl += 256;
                         if ((fl >> 8) >= P.suffix_max) to_cache = true;  // suffix end: bootstrap from the cache
                     }
-                    P.pflags[p] = fl;
+                    ps.fl = fl;
                 } else if (wide) {
                     to_cache = true;
                 }
             }
             if (to_cache) {
                 const int k = atomicAdd(&P.cnt[kQN], 1);
-                write_cache_record(P, P.qrec + (size_t)k * kQRec, S, -d, T, p, rad);
+                write_cache_record(P, P.qrec + (size_t)k * kQRec, S, -d, T, ps.id, rad);
                 alive = false;
             }
             if (alive && depth >= P.rr_start) {
@@ -784,14 +833,15 @@ __device__ __forceinline__ void shade_unbiased_core(const Params &P, int p, Shad
                 }
             }
         }
-        P.rad[p] = make_float4(rad.x, rad.y, rad.z, 0.0f);
+        ps.rad = rad;
         if (cont) {
-            P.o[p] = make_float4(spos.x, spos.y, spos.z, 0.0f);
-            P.d[p] = make_float4(ndir.x, ndir.y, ndir.z, npdf);
-            P.thr[p] = make_float4(T.x, T.y, T.z, 0.0f);
-            P.depth[p] = depth + 1;
+            ps.o = spos;
+            ps.d = ndir;
+            ps.pdf = npdf;
+            ps.T = T;
+            ps.depth = depth + 1;
         }
-        P.rng[p] = rs;
+        ps.rs = rs;
     }
     out.cont = cont;
     out.f_pred = f_pred;
@@ -806,45 +856,81 @@ __device__ __forceinline__ void shade_unbiased_core(const Params &P, int p, Shad
     out.f_light = -1;
 }
 
-__device__ void shade_unbiased(const Params &P, int p, bool valid, int *next_q, int next_cnt, float4 *so0,
-                               float4 *sd0, float4 *sc0, float4 *so1, float4 *sd1, float4 *sc1) {
-    ShadeOut o{};
-    if (valid) shade_unbiased_core(P, p, o);
-    const int k = warp_append(&P.cnt[next_cnt], o.cont);
-    if (o.cont) next_q[k] = p;
-    push_shadow(P, so0, sd0, sc0, kSH0, o.f_pred, o.spos, o.f_dir, o.f_tmax, -1, o.f_c, p);
-    push_shadow(P, so1, sd1, sc1, kSH1, o.e_pred, o.spos, o.e_dir, kBigT, -1, o.e_c, p);
+// Shades the live paths of the current buffer with the hits k_extend wrote:
+// first the miss queue (shade_miss: the sky lookup, then the path ends), then
+// the hit queue (the surface shading, on warps that are all hits).
+// Continuing paths move to the next buffer (counter next_cnt), finished ones
+// leave their radiance in fin[id].  A shadow record names where its
+// contribution goes: the path's slot in the next buffer (>= 0) or -(id + 1)
+// for fin.
+template <int kEst>
+__global__ void __launch_bounds__(128) k_shade(Params P, const int *__restrict__ hq, const int *__restrict__ mq,
+                                               int next_cnt, float4 *so0, float4 *sd0, float4 *sc0, float4 *so1,
+                                               float4 *sd1, float4 *sc1) {
+    const int nm = P.cnt[kMQ], nh = P.cnt[kHQ];
+    const int n = nm + nh;
+    const bool cache = P.use_cache != 0;
+    for (int base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+        const int j = base + threadIdx.x;
+        if (j < nm) {  // a miss: the path ends here
+            const int i = mq[j];
+            const PathBuf &b = P.cur;
+            const float4 d4 = b.d[i];
+            float3 rad = f3(b.rad[i]);
+            const int path = b.id[i], depth = b.depth[i];
+            shade_miss<kEst>(P, f3(d4), d4.w, f3(b.thr[i]), rad, depth, path);
+            P.fin[path] = make_float4(rad.x, rad.y, rad.z, 0.0f);
+            if (kEst == KGK_ESTIMATOR_COMPAT) P.seeds[path % P.npx] = b.rng[i];  // render.cuh:42
+        }
+        if (base + (int)blockDim.x <= nm) continue;  // the whole block was misses
+        const bool go = j >= nm && j < n;
+        PathState ps;
+        ps.id = 0;
+        ShadeOut o{};
+        if (go) {
+            const int i = hq[j - nm];
+            ps = load_path(P.cur, i, cache);
+            if (kEst == KGK_ESTIMATOR_COMPAT) shade_compat_core(P, ps, P.hit[i], o);
+            else shade_unbiased_core(P, ps, P.hit[i], o);
+        }
+        const int k = warp_append(&P.cnt[next_cnt], o.cont);
+        if (o.cont) store_path(P.nxt, k, ps, cache);
+        else if (go) P.fin[ps.id] = make_float4(ps.rad.x, ps.rad.y, ps.rad.z, 0.0f);
+        const int target = o.cont ? k : -(ps.id + 1);
+        push_shadow(P, so0, sd0, sc0, kSH0, o.f_pred, o.f_org, o.f_dir, o.f_tmax, o.f_light, o.f_c, target);
+        push_shadow(P, so1, sd1, sc1, kSH1, o.e_pred, o.spos, o.e_dir, kBigT, -1, o.e_c, target);
+    }
 }
 
 // The tail of a wave: once few paths are alive (or the whole wave is small),
-// each thread carries one path through all of its remaining bounces - closest
-// hit, shading, then its face-light and environment shadow rays in that order
-// (the order of the wavefront's passes, so the radiance sums are the same) -
-// instead of four kernel launches per bounce that each wait for their slowest
-// ray.  q == nullptr: paths 0..dense_n-1 from their primary rays.  A path
-// runs at most `bounces` more bounces, the wavefront's bounce limit.
+// each thread carries one path of the current buffer (slots 0..n-1, n from
+// counter cnt_idx, or dense_n when cnt_idx < 0) through all of its remaining
+// bounces in registers - closest hit, shading, then its face-light and
+// environment shadow rays in that order (the order of the wavefront's passes,
+// so the radiance sums are the same) - instead of four kernel launches per
+// bounce that each wait for their slowest ray.  A path runs at most `bounces`
+// more bounces, the wavefront's limit.
 template <int kEst>
-__global__ void __launch_bounds__(128) k_tail(Params P, const int *__restrict__ q, int qcnt_idx, int dense_n,
-                                              int bounces) {
-    const int n = q ? P.cnt[qcnt_idx] : dense_n;
+__global__ void __launch_bounds__(128) k_tail(Params P, int cnt_idx, int dense_n, int bounces) {
+    const int n = cnt_idx >= 0 ? P.cnt[cnt_idx] : dense_n;
     const DevScene &s = P.sc;
+    const bool cache = P.use_cache != 0;
     unsigned rays_c = 0, rays_s = 0, overflow = 0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const int p = q ? q[i] : i;
+        PathState ps = load_path(P.cur, i, cache);
         for (int k = 0; k < bounces; ++k) {
-            const float4 o4 = P.o[p], d4 = P.d[p];
-            const RayPre r = make_ray(f3(o4), f3(d4));
+            const RayPre r = make_ray(ps.o, ps.d);
             float bt = kBigT, u = 0.0f, v = 0.0f;
             int bid = 0x7fffffff;
             TravStats st{0, 0, 0};
             const int slot = trace_closest<false>(s.nodes, (unsigned)s.n_nodes, s.tri_rec, (unsigned)s.n_tris, r, bt,
                                                   bid, u, v, st);
-            P.hit[p] = slot < 0 ? make_float4(kBigT, 0.0f, 0.0f, __int_as_float(-1))
-                                : make_float4(bt, u, v, __int_as_float(bid));
+            const float4 h = slot < 0 ? make_float4(kBigT, 0.0f, 0.0f, __int_as_float(-1))
+                                      : make_float4(bt, u, v, __int_as_float(bid));
             ++rays_c;
             ShadeOut so{};
-            if (kEst == KGK_ESTIMATOR_COMPAT) shade_compat_core(P, p, so);
-            else shade_unbiased_core(P, p, so);
+            if (kEst == KGK_ESTIMATOR_COMPAT) shade_compat_core(P, ps, h, so);
+            else shade_unbiased_core(P, ps, h, so);
             if (so.f_pred) {
                 const RayPre rs = make_ray(so.f_org, so.f_dir);
                 bool vis;
@@ -858,25 +944,19 @@ __global__ void __launch_bounds__(128) k_tail(Params P, const int *__restrict__ 
                     vis = !trace_any<false>(s.nodes, (unsigned)s.n_nodes, s.tri_rec, (unsigned)s.n_tris, rs,
                                             so.f_tmax, st);
                 }
-                if (vis) {
-                    float4 rr = P.rad[p];
-                    rr.x += so.f_c.x; rr.y += so.f_c.y; rr.z += so.f_c.z;
-                    P.rad[p] = rr;
-                }
+                if (vis) ps.rad = ps.rad + so.f_c;
                 ++rays_s;
             }
             if (so.e_pred) {
                 const RayPre rs = make_ray(so.spos, so.e_dir);
-                if (!trace_any<false>(s.nodes, (unsigned)s.n_nodes, s.tri_rec, (unsigned)s.n_tris, rs, kBigT, st)) {
-                    float4 rr = P.rad[p];
-                    rr.x += so.e_c.x; rr.y += so.e_c.y; rr.z += so.e_c.z;
-                    P.rad[p] = rr;
-                }
+                if (!trace_any<false>(s.nodes, (unsigned)s.n_nodes, s.tri_rec, (unsigned)s.n_tris, rs, kBigT, st))
+                    ps.rad = ps.rad + so.e_c;
                 ++rays_s;
             }
             overflow += st.overflow;
             if (!so.cont) break;
         }
+        P.fin[ps.id] = make_float4(ps.rad.x, ps.rad.y, ps.rad.z, 0.0f);
     }
     warp_add_u64(&P.stats[kRaysC], rays_c);
     warp_add_u64(&P.stats[kRaysS], rays_s);
@@ -884,22 +964,12 @@ __global__ void __launch_bounds__(128) k_tail(Params P, const int *__restrict__ 
     warp_add_u64(&P.stats[kOverflow], overflow);
 }
 
-template <int kEst>
-__global__ void __launch_bounds__(128) k_shade(Params P, const int *sq0, const int *sq1, const int *sq2,
-                                               int *next_q, int next_cnt, float4 *so0, float4 *sd0, float4 *sc0,
-                                               float4 *so1, float4 *sd1, float4 *sc1) {
-    const int n0 = P.cnt[kSQ0], n1 = P.cnt[kSQ1], n2 = P.cnt[kSQ2];
-    const int n = n0 + n1 + n2;
-    for (int base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
-        const int i = base + threadIdx.x;
-        const bool valid = i < n;
-        int p = 0;
-        if (valid) p = i < n0 ? sq0[i] : (i < n0 + n1 ? sq1[i - n0] : sq2[i - n0 - n1]);
-        if (kEst == KGK_ESTIMATOR_COMPAT)
-            shade_compat(P, p, valid, next_q, next_cnt, so0, sd0, sc0, so1, sd1, sc1);
-        else
-            shade_unbiased(P, p, valid, next_q, next_cnt, so0, sd0, sc0, so1, sd1, sc1);
-    }
+// Paths still live when the bounce limit ends the wavefront: their radiance
+// so far is final.
+__global__ void k_flush(Params P, int cnt_idx) {
+    const int n = P.cnt[cnt_idx];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        P.fin[P.cur.id[i]] = P.cur.rad[i];
 }
 
 // ---------------------------------------------------------------------------
@@ -907,8 +977,9 @@ __global__ void __launch_bounds__(128) k_shade(Params P, const int *sq0, const i
 // when the closest hit within its range is that light (the reference's test,
 // NextEventEstimation_FaceLight.cuh:69-71); an environment record when nothing
 // lies in (kTMin, range).  Visible records add their contribution to the
-// path's radiance (one record per path per queue, so no atomics).  Lanes are
-// refilled like k_extend's.
+// path's radiance - in the next buffer, or in fin for a finished path (one
+// record per path per queue, so no atomics).  Lanes are refilled like
+// k_extend's.
 __global__ void __launch_bounds__(128) k_shadow(Params P, int cidx, int fidx, const float4 *__restrict__ so,
                                                 const float4 *__restrict__ sd, const float4 *__restrict__ sc) {
     const int n = P.cnt[cidx];
@@ -949,12 +1020,13 @@ __global__ void __launch_bounds__(128) k_shadow(Params P, int cidx, int fidx, co
             const bool vis = light >= 0 ? (c.hit_slot >= 0 && c.best_id == light) : c.hit_slot < 0;
             if (vis) {
                 const float4 cc = sc[i];
-                const int p = __float_as_int(cc.w);
-                float4 rr = P.rad[p];
+                const int t = __float_as_int(cc.w);
+                float4 *dst = t >= 0 ? P.nxt.rad + t : P.fin + (-t - 1);
+                float4 rr = *dst;
                 rr.x += cc.x;
                 rr.y += cc.y;
                 rr.z += cc.z;
-                P.rad[p] = rr;
+                *dst = rr;
             }
         }
     }
@@ -982,7 +1054,7 @@ __global__ void k_finish(Params P, float4 *frame, double *acc_sum, double *acc_s
         float4 f = first_wave ? make_float4(0.0f, 0.0f, 0.0f, 0.0f) : frame[px];
         double s0 = 0, s1 = 0, s2 = 0, q0 = 0, q1 = 0, q2 = 0;
         for (int k = 0; k < P.spp_wave; ++k) {
-            const float4 r = P.rad[k * P.npx + px];
+            const float4 r = P.fin[k * P.npx + px];
             f.x += r.x;
             f.y += r.y;
             f.z += r.z;
@@ -1032,21 +1104,28 @@ kgk_status ensure_pixels(RenderState &R, int W, int H) {
 kgk_status ensure_wave(RenderState &R, int cap, bool cache) {
     if (R.cap >= cap && (!cache || R.qrec_cap >= cap)) return KGK_OK;
     if (cache && R.qrec_cap < cap) {
-        KGK_TRY(ensure(&R.spread, cap, "cache path state"));
-        KGK_TRY(ensure(&R.pflags, cap, "cache path state"));
+        for (int k = 0; k < 2; ++k) {
+            KGK_TRY(ensure(&R.pb[k].spread, cap, "cache path state"));
+            KGK_TRY(ensure(&R.pb[k].pflags, cap, "cache path state"));
+        }
         KGK_TRY(ensure(&R.qrec, (size_t)cap * kQRec, "cache query records"));
         R.qrec_cap = cap;
     }
     if (R.cap >= cap) return KGK_OK;
-    KGK_TRY(ensure(&R.o, cap, "path state"));
-    KGK_TRY(ensure(&R.d, cap, "path state"));
-    KGK_TRY(ensure(&R.thr, cap, "path state"));
-    KGK_TRY(ensure(&R.rad, cap, "path state"));
-    KGK_TRY(ensure(&R.hit, cap, "path state"));
-    KGK_TRY(ensure(&R.rng, cap, "path state"));
-    KGK_TRY(ensure(&R.depth, cap, "path state"));
-    for (int k = 0; k < 2; ++k) KGK_TRY(ensure(&R.aq[k], cap, "path queue"));
-    for (int k = 0; k < 3; ++k) KGK_TRY(ensure(&R.sq[k], cap, "shade queue"));
+    for (int k = 0; k < 2; ++k) {
+        PathBuf &b = R.pb[k];
+        KGK_TRY(ensure(&b.o, cap, "path state"));
+        KGK_TRY(ensure(&b.d, cap, "path state"));
+        KGK_TRY(ensure(&b.thr, cap, "path state"));
+        KGK_TRY(ensure(&b.rad, cap, "path state"));
+        KGK_TRY(ensure(&b.rng, cap, "path state"));
+        KGK_TRY(ensure(&b.depth, cap, "path state"));
+        KGK_TRY(ensure(&b.id, cap, "path state"));
+    }
+    KGK_TRY(ensure(&R.fin, cap, "path radiance"));
+    KGK_TRY(ensure(&R.hit, cap, "path hits"));
+    KGK_TRY(ensure(&R.hq, cap, "hit queue"));
+    KGK_TRY(ensure(&R.mq, cap, "miss queue"));
     for (int k = 0; k < 2; ++k) {
         KGK_TRY(ensure(&R.sh_o[k], cap, "shadow queue"));
         KGK_TRY(ensure(&R.sh_d[k], cap, "shadow queue"));
@@ -1070,10 +1149,13 @@ void render_state_free(kgk_scene *s) {
     RenderState *R = s->rs;
     if (!R) return;
     void *ptrs[] = {R->seeds, R->frame, R->kept, R->acc_sum, R->acc_sq, R->gb_pos, R->gb_nrm, R->gb_alb, R->gb_emi,
-                    R->o, R->d, R->thr, R->rad, R->hit, R->rng, R->depth, R->aq[0], R->aq[1], R->sq[0],
-                    R->sq[1], R->sq[2], R->sh_o[0], R->sh_o[1], R->sh_d[0], R->sh_d[1], R->sh_c[0],
-                    R->sh_c[1], R->cnt, R->stats, R->spread, R->pflags, R->qrec, R->trec, R->ttgt};
+                    R->fin, R->hit, R->hq, R->mq, R->sh_o[0], R->sh_o[1], R->sh_d[0], R->sh_d[1], R->sh_c[0],
+                    R->sh_c[1], R->cnt, R->stats, R->qrec, R->trec, R->ttgt};
     for (void *p : ptrs) dfree(p);
+    for (PathBuf &b : R->pb) {
+        void *bp[] = {b.o, b.d, b.thr, b.rad, b.rng, b.depth, b.id, b.spread, b.pflags};
+        for (void *p : bp) dfree(p);
+    }
     delete R;
     s->rs = nullptr;
 }
@@ -1178,7 +1260,10 @@ kgk_status kgk_render(kgk_scene *s, const kgk_camera *cam, const kgk_camera *pre
     P.count_work = cfg->count_work;
     P.seed = cfg->seed;
     P.frame_index = cfg->frame_index;
-    P.o = R.o; P.d = R.d; P.thr = R.thr; P.rad = R.rad; P.hit = R.hit; P.rng = R.rng; P.depth = R.depth;
+    P.cur = R.pb[0];
+    P.nxt = R.pb[1];
+    P.fin = R.fin;
+    P.hit = R.hit;
     P.seeds = R.seeds;
     P.gb_pos = R.gb_pos; P.gb_nrm = R.gb_nrm; P.gb_alb = R.gb_alb; P.gb_emi = R.gb_emi;
     P.cnt = R.cnt;
@@ -1187,8 +1272,6 @@ kgk_status kgk_render(kgk_scene *s, const kgk_camera *cam, const kgk_camera *pre
     if (P.use_cache) {
         const kgk_nrc_config &nc = s->nrc->cfg;
         KGK_TRY(ensure_train(R, nc.train_paths));
-        P.spread = R.spread;
-        P.pflags = R.pflags;
         P.qrec = R.qrec;
         P.trec = R.trec;
         P.tcap = R.tcap;
@@ -1234,43 +1317,50 @@ kgk_status kgk_render(kgk_scene *s, const kgk_camera *cam, const kgk_camera *pre
             KGK_CUDA(cudaMemsetAsync(R.cnt + kQN, 0, 2 * sizeof(int), st));
             if (wave > 0) P.train_stride = 0;  // training paths only in the first wave
         }
+        P.cur = R.pb[0];
+        P.nxt = R.pb[1];
         k_raygen<<<grid, 128, 0, st>>>(P);
         ++launches;
-        // a small wave (the reference's estimator renders one sample per
-        // pixel per wave) runs in the tail kernel from its primary rays
-        if (n <= kTailPaths) {
+        auto launch_tail = [&](int cnt_idx, int dense_n, int bounces, int threads) -> kgk_status {
             KGK_TRY(stage_begin(3));
-            const int tg = std::max(1, std::min((n + 127) / 128, R.sms * 16));
+            const int tg = std::max(1, std::min((threads + 127) / 128, R.sms * 16));
             if (cfg->estimator == KGK_ESTIMATOR_COMPAT)
-                k_tail<KGK_ESTIMATOR_COMPAT><<<tg, 128, 0, st>>>(P, nullptr, 0, n, max_bounces);
+                k_tail<KGK_ESTIMATOR_COMPAT><<<tg, 128, 0, st>>>(P, cnt_idx, dense_n, bounces);
             else
-                k_tail<KGK_ESTIMATOR_UNBIASED><<<tg, 128, 0, st>>>(P, nullptr, 0, n, max_bounces);
+                k_tail<KGK_ESTIMATOR_UNBIASED><<<tg, 128, 0, st>>>(P, cnt_idx, dense_n, bounces);
             KGK_TRY(stage_end());
             KGK_CUDA(cudaGetLastError());
             ++launches;
+            return KGK_OK;
+        };
+        // a small wave (the reference's estimator renders one sample per
+        // pixel per wave) runs in the tail kernel from its primary rays
+        bool drained = false;
+        if (n <= kTailPaths) {
+            KGK_TRY(launch_tail(-1, n, max_bounces, n));
+            drained = true;
         }
-        int cur = 0;
-        for (int b = 0; b < max_bounces && n > kTailPaths; ++b) {
-            KGK_CUDA(cudaMemsetAsync(R.cnt + kSQ0, 0, (kFS1 + 1 - kSQ0) * sizeof(int), st));
-            KGK_CUDA(cudaMemsetAsync(R.cnt + (cur ^ 1), 0, sizeof(int), st));
-            const int *q = b == 0 ? nullptr : R.aq[cur];
+        int c = 0;  // the buffer holding this bounce's live paths
+        for (int b = 0; b < max_bounces && !drained; ++b) {
+            P.cur = R.pb[c];
+            P.nxt = R.pb[c ^ 1];
+            const int cidx = b == 0 ? -1 : kA0 + c, nidx = kA0 + (c ^ 1);
+            KGK_CUDA(cudaMemsetAsync(R.cnt + kSH0, 0, (kMQ + 1 - kSH0) * sizeof(int), st));
+            KGK_CUDA(cudaMemsetAsync(R.cnt + nidx, 0, sizeof(int), st));
             KGK_TRY(stage_begin(0));
             if (cfg->count_work)
-                k_extend<true><<<grid, 128, 0, st>>>(P, q, cur, n, R.sq[0], R.sq[1], R.sq[2]);
+                k_extend<true><<<grid, 128, 0, st>>>(P, cidx, n, R.hq, R.mq);
             else
-                k_extend<false><<<grid, 128, 0, st>>>(P, q, cur, n, R.sq[0], R.sq[1], R.sq[2]);
+                k_extend<false><<<grid, 128, 0, st>>>(P, cidx, n, R.hq, R.mq);
             KGK_TRY(stage_end());
             ++extend_launches;
             KGK_TRY(stage_begin(1));
             if (cfg->estimator == KGK_ESTIMATOR_COMPAT)
-                k_shade<KGK_ESTIMATOR_COMPAT><<<grid, 128, 0, st>>>(P, R.sq[0], R.sq[1], R.sq[2], R.aq[cur ^ 1],
-                                                                  cur ^ 1, R.sh_o[0], R.sh_d[0], R.sh_c[0],
-                                                                  R.sh_o[1], R.sh_d[1], R.sh_c[1]);
+                k_shade<KGK_ESTIMATOR_COMPAT><<<grid, 128, 0, st>>>(P, R.hq, R.mq, nidx, R.sh_o[0], R.sh_d[0],
+                                                                  R.sh_c[0], R.sh_o[1], R.sh_d[1], R.sh_c[1]);
             else
-                k_shade<KGK_ESTIMATOR_UNBIASED><<<grid, 128, 0, st>>>(P, R.sq[0], R.sq[1], R.sq[2],
-                                                                    R.aq[cur ^ 1], cur ^ 1, R.sh_o[0],
-                                                                    R.sh_d[0], R.sh_c[0], R.sh_o[1],
-                                                                    R.sh_d[1], R.sh_c[1]);
+                k_shade<KGK_ESTIMATOR_UNBIASED><<<grid, 128, 0, st>>>(P, R.hq, R.mq, nidx, R.sh_o[0], R.sh_d[0],
+                                                                    R.sh_c[0], R.sh_o[1], R.sh_d[1], R.sh_c[1]);
             KGK_TRY(stage_end());
             KGK_TRY(stage_begin(2));
             k_shadow<<<grid, 128, 0, st>>>(P, kSH0, kFS0, R.sh_o[0], R.sh_d[0], R.sh_c[0]);
@@ -1278,34 +1368,37 @@ kgk_status kgk_render(kgk_scene *s, const kgk_camera *cam, const kgk_camera *pre
             KGK_TRY(stage_end());
             KGK_CUDA(cudaGetLastError());
             launches += 4;
-            cur ^= 1;
-            // from the second bounce on, check the alive count every bounce,
+            c ^= 1;
+            P.cur = R.pb[c];
+            P.nxt = R.pb[c ^ 1];
+            // from the second bounce on, check the live count every bounce,
             // to hand the last few paths to the tail kernel
             if (b >= 1) {
                 int alive = 0;
-                KGK_CUDA(cudaMemcpyAsync(&alive, R.cnt + cur, sizeof(int), cudaMemcpyDeviceToHost, st));
+                KGK_CUDA(cudaMemcpyAsync(&alive, R.cnt + kA0 + c, sizeof(int), cudaMemcpyDeviceToHost, st));
                 KGK_CUDA(cudaStreamSynchronize(st));
-                if (alive == 0) break;
+                if (alive == 0) {
+                    drained = true;
+                    break;
+                }
                 if (alive <= kTailPaths && b + 1 < max_bounces) {
-                    KGK_TRY(stage_begin(3));
-                    const int tg = std::max(1, std::min((alive + 127) / 128, R.sms * 16));
-                    if (cfg->estimator == KGK_ESTIMATOR_COMPAT)
-                        k_tail<KGK_ESTIMATOR_COMPAT><<<tg, 128, 0, st>>>(P, R.aq[cur], cur, 0, max_bounces - b - 1);
-                    else
-                        k_tail<KGK_ESTIMATOR_UNBIASED><<<tg, 128, 0, st>>>(P, R.aq[cur], cur, 0,
-                                                                          max_bounces - b - 1);
-                    KGK_TRY(stage_end());
-                    KGK_CUDA(cudaGetLastError());
-                    ++launches;
+                    KGK_TRY(launch_tail(kA0 + c, 0, max_bounces - b - 1, alive));
+                    drained = true;
                     break;
                 }
             }
         }
+        if (!drained) {
+            // the bounce limit ended the wavefront with paths still live
+            k_flush<<<grid, 128, 0, st>>>(P, kA0 + c);
+            KGK_CUDA(cudaGetLastError());
+            ++launches;
+        }
         if (P.use_cache) {
             // terminate into the cache, then learn from this wave's training paths
             NrcState &N = *s->nrc;
-            KGK_TRY(nrc_infer_dev(N, R.qrec, kQRec, R.cap, R.cnt + kQN, nullptr, R.rad, st));
-            k_cache_targets<<<64, 256, 0, st>>>(R.trec, R.cnt + kTN, R.tcap, R.rad, R.ttgt);
+            KGK_TRY(nrc_infer_dev(N, R.qrec, kQRec, R.cap, R.cnt + kQN, nullptr, R.fin, st));
+            k_cache_targets<<<64, 256, 0, st>>>(R.trec, R.cnt + kTN, R.tcap, R.fin, R.ttgt);
             KGK_CUDA(cudaGetLastError());
             launches += 2;
             if (wave == 0) {
