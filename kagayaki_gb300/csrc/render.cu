@@ -248,10 +248,44 @@ __global__ void k_raygen(Params P) {
 // ---------------------------------------------------------------------------
 // Closest hit of every live path (slots 0..n-1 of the current buffer; n from
 // counter cnt_idx, or dense_n when cnt_idx < 0), written to hit[slot]; the
-// slot goes to the hit or the miss queue (warp-ballot appends), so shading
-// warps are either all surface hits or all misses.  Each warp keeps its lanes
-// busy: when kRefill or more lanes have finished, they take the next rays
-// (one atomic per warp).
+// slot goes to the hit or the miss queue, so shading warps are either all
+// surface hits or all misses.  Each warp gathers its finished slots in shared
+// memory and appends them 32 at a time (one atomic, one coalesced store).
+// Each warp keeps its lanes busy: when kRefill or more lanes have finished,
+// they take the next rays (one atomic per warp).
+struct QueueBatch {
+    int *buf;       // this warp's 64 shared-memory entries
+    int n = 0;      // entries held (warp-uniform, < 32 between calls)
+    // Adds the lanes' slots where pred holds; writes out full batches of 32.
+    __device__ __forceinline__ void add(bool pred, int slot, int *queue, int *counter) {
+        const unsigned lane = threadIdx.x & 31u;
+        const unsigned m = __ballot_sync(~0u, pred);
+        if (pred) buf[n + __popc(m & ((1u << lane) - 1u))] = slot;
+        n += __popc(m);
+        __syncwarp();
+        if (n >= 32) {
+            int base = 0;
+            if (lane == 0) base = atomicAdd(counter, 32);
+            base = __shfl_sync(~0u, base, 0);
+            queue[base + lane] = buf[lane];
+            __syncwarp();
+            if ((int)lane < n - 32) buf[lane] = buf[32 + lane];
+            n -= 32;
+            __syncwarp();
+        }
+    }
+    // Writes out what is left.
+    __device__ __forceinline__ void flush(int *queue, int *counter) {
+        const unsigned lane = threadIdx.x & 31u;
+        if (n == 0) return;
+        int base = 0;
+        if (lane == 0) base = atomicAdd(counter, n);
+        base = __shfl_sync(~0u, base, 0);
+        if ((int)lane < n) queue[base + lane] = buf[lane];
+        n = 0;
+    }
+};
+
 template <bool kCount>
 __global__ void __launch_bounds__(128) k_extend(Params P, int cnt_idx, int dense_n, int *hq, int *mq) {
     const int n = cnt_idx >= 0 ? P.cnt[cnt_idx] : dense_n;
@@ -259,6 +293,10 @@ __global__ void __launch_bounds__(128) k_extend(Params P, int cnt_idx, int dense
     int *fetch = &P.cnt[kFE];
     const unsigned lane = threadIdx.x & 31u;
     const unsigned lt = (1u << lane) - 1u;
+    __shared__ int s_q[2][4][64];  // per warp: hit and miss batches (blocks of 128 threads)
+    QueueBatch hb, mb;
+    hb.buf = s_q[0][threadIdx.x >> 5];
+    mb.buf = s_q[1][threadIdx.x >> 5];
     bool active = false, exhausted = false;
     int p = 0;
     unsigned rays = 0;
@@ -295,12 +333,12 @@ __global__ void __launch_bounds__(128) k_extend(Params P, int cnt_idx, int dense
                                       : make_float4(c.best_t, c.bu, c.bv, __int_as_float(c.best_id));
         }
         if (__any_sync(~0u, cls >= 0)) {
-            const int am = warp_append(&P.cnt[kMQ], cls == 0);
-            const int ah = warp_append(&P.cnt[kHQ], cls == 1);
-            if (cls == 0) mq[am] = p;
-            if (cls == 1) hq[ah] = p;
+            hb.add(cls == 1, p, hq, &P.cnt[kHQ]);
+            mb.add(cls == 0, p, mq, &P.cnt[kMQ]);
         }
     }
+    hb.flush(hq, &P.cnt[kHQ]);
+    mb.flush(mq, &P.cnt[kMQ]);
     warp_add_u64(&P.stats[kRaysC], rays);
     if (kCount) {
         warp_add_u64(&P.stats[kNodes], st.nodes);
