@@ -370,6 +370,19 @@ __global__ void k_copy_range(const Chunk *chunks, const int *src, int *dst) {
     for (int i = ch.begin + threadIdx.x; i < ch.end; i += blockDim.x) dst[i] = src[i];
 }
 
+// The material class of each BVH-ordered triangle goes into the .w of its
+// second record (1 = Disney BRDF, 0 = any other type; the intersection test
+// reads only .xyz there), so a closest hit tells the shading queues apart
+// without a material lookup.
+__global__ void k_tri_class(float4 *tri_rec, int n, const float4 *attr, const kgk_material *mats, int n_mats) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int prim = __float_as_int(tri_rec[3 * i].w);
+        const unsigned mid = __float_as_uint(attr[4 * prim + 3].w) & 0x7fffffffu;
+        const int cls = mid < (unsigned)n_mats && mats[mid].MATERIAL_TYPE_ID == 1 ? 1 : 0;
+        tri_rec[3 * i + 1].w = __int_as_float(cls);
+    }
+}
+
 __global__ void k_write_nodes(const int *ids, const BinNode *vals, const int *firsts,
                               const int *counts, int m, BinNode *nodes, int *bfirst, int *bcount,
                               int cap, int *err) {
@@ -1098,6 +1111,10 @@ kgk_status bvh_build(DevScene &s, cudaStream_t st, BvhBuildStats *out) {
         tri_start += level_tris;
         ntasks = next_n;
         std::swap(tasks_a, tasks_b);
+    }
+    if (tri_start == n) {
+        k_tri_class<<<std::min((n + 255) / 256, 4096), 256, 0, st>>>(tri_rec, n, s.attr, s.mats, s.n_mats);
+        KGK_CUDA(cudaGetLastError());
     }
     KGK_CUDA(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, st));
     KGK_CUDA(cudaEventRecord(e1, st));

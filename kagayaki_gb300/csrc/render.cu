@@ -32,9 +32,9 @@ namespace kgk {
 
 // Device bytes per path in flight (ensure_wave): two buffers of state (4
 // float4, rng, depth, id), the final radiance and the hit (float4 each), the
-// hit and miss slot queues, two shadow queues of three float4; with the cache
+// miss / Lambert / Disney slot queues, two shadow queues of three float4; with the cache
 // also its spread and flags (two buffers) and a query record.
-constexpr size_t kPathStateBytes = 2 * (4 * 16 + 8 + 4 + 4) + 2 * 16 + 2 * 4 + 2 * 3 * 16;
+constexpr size_t kPathStateBytes = 2 * (4 * 16 + 8 + 4 + 4) + 2 * 16 + 3 * 4 + 2 * 3 * 16;
 constexpr size_t kCachePathBytes = 2 * (8 + 4) + 20 * 4;
 
 // Live path state, one buffer (slot = position among the live paths).
@@ -69,7 +69,8 @@ struct RenderState {
     PathBuf pb[2];                            // live path state, used in turn
     float4 *fin = nullptr;                    // final radiance by path id
     float4 *hit = nullptr;                    // closest hit by slot (t, u, v, triangle id or -1)
-    int *hq = nullptr, *mq = nullptr;         // slots whose ray hit / missed the scene
+    int *mq = nullptr;                        // slots whose ray missed the scene
+    int *lq = nullptr, *dq = nullptr;         // slots whose ray hit a Disney / another material
     float4 *sh_o[2] = {nullptr, nullptr}, *sh_d[2] = {nullptr, nullptr}, *sh_c[2] = {nullptr, nullptr};
     int *cnt = nullptr;                       // queue counters
     unsigned long long *stats = nullptr;      // rays_closest, rays_shadow, overflow, nodes, tris
@@ -89,11 +90,12 @@ struct RenderState {
 namespace {
 
 // Device counters: live paths in each state buffer, shadow-queue sizes,
-// dynamic-fetch cursors of the extend and shadow kernels, hit and miss queue
-// sizes (zeroed before every bounce together with the shadow queues), cache
-// record counts.
+// dynamic-fetch cursors of the extend and shadow kernels, miss / Lambert /
+// Disney queue sizes (zeroed before every bounce together with the shadow
+// queues), cache record counts.
 enum Cnt {
-    kA0 = 0, kA1 = 1, kSH0 = 2, kSH1 = 3, kFE = 4, kFS0 = 5, kFS1 = 6, kHQ = 7, kMQ = 8, kQN = 9, kTN = 10, kNCnt = 11
+    kA0 = 0, kA1 = 1, kSH0 = 2, kSH1 = 3, kFE = 4, kFS0 = 5, kFS1 = 6, kMQ = 7, kLQ = 8, kDQ = 9, kQN = 10,
+    kTN = 11, kNCnt = 12
 };
 // Lanes of a warp that must be idle before the warp fetches new rays.
 constexpr int kRefill = 8;
@@ -248,9 +250,11 @@ __global__ void k_raygen(Params P) {
 // ---------------------------------------------------------------------------
 // Closest hit of every live path (slots 0..n-1 of the current buffer; n from
 // counter cnt_idx, or dense_n when cnt_idx < 0), written to hit[slot]; the
-// slot goes to the hit or the miss queue, so shading warps are either all
-// surface hits or all misses.  Each warp gathers its finished slots in shared
-// memory and appends them 32 at a time (one atomic, one coalesced store).
+// slot goes to the miss, the Lambert or the Disney queue (the hit triangle's
+// material class is in its BVH record, read by the traversal anyway), so
+// shading warps are material-coherent.  Each warp gathers its finished slots
+// in shared memory and appends them 32 at a time (one atomic, one coalesced
+// store).
 // Each warp keeps its lanes busy: when kRefill or more lanes have finished,
 // they take the next rays (one atomic per warp).
 struct QueueBatch {
@@ -287,16 +291,17 @@ struct QueueBatch {
 };
 
 template <bool kCount>
-__global__ void __launch_bounds__(128) k_extend(Params P, int cnt_idx, int dense_n, int *hq, int *mq) {
+__global__ void __launch_bounds__(128) k_extend(Params P, int cnt_idx, int dense_n, int *mq, int *lq, int *dq) {
     const int n = cnt_idx >= 0 ? P.cnt[cnt_idx] : dense_n;
     const DevScene &s = P.sc;
     int *fetch = &P.cnt[kFE];
     const unsigned lane = threadIdx.x & 31u;
     const unsigned lt = (1u << lane) - 1u;
-    __shared__ int s_q[2][4][64];  // per warp: hit and miss batches (blocks of 128 threads)
-    QueueBatch hb, mb;
-    hb.buf = s_q[0][threadIdx.x >> 5];
-    mb.buf = s_q[1][threadIdx.x >> 5];
+    __shared__ int s_q[3][4][64];  // per warp: miss, Lambert, Disney batches (blocks of 128 threads)
+    QueueBatch mb, lb, db;
+    mb.buf = s_q[0][threadIdx.x >> 5];
+    lb.buf = s_q[1][threadIdx.x >> 5];
+    db.buf = s_q[2][threadIdx.x >> 5];
     bool active = false, exhausted = false;
     int p = 0;
     unsigned rays = 0;
@@ -328,17 +333,19 @@ __global__ void __launch_bounds__(128) k_extend(Params P, int cnt_idx, int dense
                                         false, st)) {
             active = false;
             ++rays;
-            cls = c.hit_slot < 0 ? 0 : 1;
+            cls = c.hit_slot < 0 ? 0 : 1 + (c.hit_slot & 1);
             P.hit[p] = c.hit_slot < 0 ? make_float4(kBigT, 0.0f, 0.0f, __int_as_float(-1))
                                       : make_float4(c.best_t, c.bu, c.bv, __int_as_float(c.best_id));
         }
         if (__any_sync(~0u, cls >= 0)) {
-            hb.add(cls == 1, p, hq, &P.cnt[kHQ]);
             mb.add(cls == 0, p, mq, &P.cnt[kMQ]);
+            lb.add(cls == 1, p, lq, &P.cnt[kLQ]);
+            db.add(cls == 2, p, dq, &P.cnt[kDQ]);
         }
     }
-    hb.flush(hq, &P.cnt[kHQ]);
     mb.flush(mq, &P.cnt[kMQ]);
+    lb.flush(lq, &P.cnt[kLQ]);
+    db.flush(dq, &P.cnt[kDQ]);
     warp_add_u64(&P.stats[kRaysC], rays);
     if (kCount) {
         warp_add_u64(&P.stats[kNodes], st.nodes);
@@ -896,17 +903,18 @@ __device__ __forceinline__ void shade_unbiased_core(const Params &P, PathState &
 
 // Shades the live paths of the current buffer with the hits k_extend wrote:
 // first the miss queue (shade_miss: the sky lookup, then the path ends), then
-// the hit queue (the surface shading, on warps that are all hits).
+// the Lambert and the Disney queues (the surface shading, on warps of one
+// material class).
 // Continuing paths move to the next buffer (counter next_cnt), finished ones
 // leave their radiance in fin[id].  A shadow record names where its
 // contribution goes: the path's slot in the next buffer (>= 0) or -(id + 1)
 // for fin.
 template <int kEst>
-__global__ void __launch_bounds__(128) k_shade(Params P, const int *__restrict__ hq, const int *__restrict__ mq,
-                                               int next_cnt, float4 *so0, float4 *sd0, float4 *sc0, float4 *so1,
-                                               float4 *sd1, float4 *sc1) {
-    const int nm = P.cnt[kMQ], nh = P.cnt[kHQ];
-    const int n = nm + nh;
+__global__ void __launch_bounds__(128) k_shade(Params P, const int *__restrict__ mq, const int *__restrict__ lq,
+                                               const int *__restrict__ dq, int next_cnt, float4 *so0, float4 *sd0,
+                                               float4 *sc0, float4 *so1, float4 *sd1, float4 *sc1) {
+    const int nm = P.cnt[kMQ], nl = P.cnt[kLQ], nd = P.cnt[kDQ];
+    const int n = nm + nl + nd;
     const bool cache = P.use_cache != 0;
     for (int base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
         const int j = base + threadIdx.x;
@@ -926,7 +934,8 @@ __global__ void __launch_bounds__(128) k_shade(Params P, const int *__restrict__
         ps.id = 0;
         ShadeOut o{};
         if (go) {
-            const int i = hq[j - nm];
+            const int jh = j - nm;
+            const int i = jh < nl ? lq[jh] : dq[jh - nl];
             ps = load_path(P.cur, i, cache);
             if (kEst == KGK_ESTIMATOR_COMPAT) shade_compat_core(P, ps, P.hit[i], o);
             else shade_unbiased_core(P, ps, P.hit[i], o);
@@ -1162,8 +1171,9 @@ kgk_status ensure_wave(RenderState &R, int cap, bool cache) {
     }
     KGK_TRY(ensure(&R.fin, cap, "path radiance"));
     KGK_TRY(ensure(&R.hit, cap, "path hits"));
-    KGK_TRY(ensure(&R.hq, cap, "hit queue"));
     KGK_TRY(ensure(&R.mq, cap, "miss queue"));
+    KGK_TRY(ensure(&R.lq, cap, "Lambert queue"));
+    KGK_TRY(ensure(&R.dq, cap, "Disney queue"));
     for (int k = 0; k < 2; ++k) {
         KGK_TRY(ensure(&R.sh_o[k], cap, "shadow queue"));
         KGK_TRY(ensure(&R.sh_d[k], cap, "shadow queue"));
@@ -1187,7 +1197,7 @@ void render_state_free(kgk_scene *s) {
     RenderState *R = s->rs;
     if (!R) return;
     void *ptrs[] = {R->seeds, R->frame, R->kept, R->acc_sum, R->acc_sq, R->gb_pos, R->gb_nrm, R->gb_alb, R->gb_emi,
-                    R->fin, R->hit, R->hq, R->mq, R->sh_o[0], R->sh_o[1], R->sh_d[0], R->sh_d[1], R->sh_c[0],
+                    R->fin, R->hit, R->mq, R->lq, R->dq, R->sh_o[0], R->sh_o[1], R->sh_d[0], R->sh_d[1], R->sh_c[0],
                     R->sh_c[1], R->cnt, R->stats, R->qrec, R->trec, R->ttgt};
     for (void *p : ptrs) dfree(p);
     for (PathBuf &b : R->pb) {
@@ -1383,21 +1393,21 @@ kgk_status kgk_render(kgk_scene *s, const kgk_camera *cam, const kgk_camera *pre
             P.cur = R.pb[c];
             P.nxt = R.pb[c ^ 1];
             const int cidx = b == 0 ? -1 : kA0 + c, nidx = kA0 + (c ^ 1);
-            KGK_CUDA(cudaMemsetAsync(R.cnt + kSH0, 0, (kMQ + 1 - kSH0) * sizeof(int), st));
+            KGK_CUDA(cudaMemsetAsync(R.cnt + kSH0, 0, (kDQ + 1 - kSH0) * sizeof(int), st));
             KGK_CUDA(cudaMemsetAsync(R.cnt + nidx, 0, sizeof(int), st));
             KGK_TRY(stage_begin(0));
             if (cfg->count_work)
-                k_extend<true><<<grid, 128, 0, st>>>(P, cidx, n, R.hq, R.mq);
+                k_extend<true><<<grid, 128, 0, st>>>(P, cidx, n, R.mq, R.lq, R.dq);
             else
-                k_extend<false><<<grid, 128, 0, st>>>(P, cidx, n, R.hq, R.mq);
+                k_extend<false><<<grid, 128, 0, st>>>(P, cidx, n, R.mq, R.lq, R.dq);
             KGK_TRY(stage_end());
             ++extend_launches;
             KGK_TRY(stage_begin(1));
             if (cfg->estimator == KGK_ESTIMATOR_COMPAT)
-                k_shade<KGK_ESTIMATOR_COMPAT><<<grid, 128, 0, st>>>(P, R.hq, R.mq, nidx, R.sh_o[0], R.sh_d[0],
+                k_shade<KGK_ESTIMATOR_COMPAT><<<grid, 128, 0, st>>>(P, R.mq, R.lq, R.dq, nidx, R.sh_o[0], R.sh_d[0],
                                                                   R.sh_c[0], R.sh_o[1], R.sh_d[1], R.sh_c[1]);
             else
-                k_shade<KGK_ESTIMATOR_UNBIASED><<<grid, 128, 0, st>>>(P, R.hq, R.mq, nidx, R.sh_o[0], R.sh_d[0],
+                k_shade<KGK_ESTIMATOR_UNBIASED><<<grid, 128, 0, st>>>(P, R.mq, R.lq, R.dq, nidx, R.sh_o[0], R.sh_d[0],
                                                                     R.sh_c[0], R.sh_o[1], R.sh_d[1], R.sh_c[1]);
             KGK_TRY(stage_end());
             KGK_TRY(stage_begin(2));

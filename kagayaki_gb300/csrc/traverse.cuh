@@ -320,7 +320,8 @@ __device__ __forceinline__ void trav_init(Trav &c, float tmax) {
 // Visits one node and the triangles of its hit leaves.  any_mode: stop at the
 // first triangle with kTMin <= t < best_t (occlusion); otherwise keep the
 // closest hit (ties to the smaller id).  Returns true when the traversal is
-// finished; then c.hit_slot is the BVH-order triangle index hit, or -1.
+// finished; then c.hit_slot is -1 (no hit) or, for the BVH-order triangle ti
+// hit, 2 * ti + its material class (the .w of its second record: 1 = Disney).
 template <bool kCount>
 __device__ __forceinline__ bool trav_step(const WideNode *__restrict__ nodes, unsigned n_nodes,
                                           const float4 *__restrict__ tri, unsigned n_tris, const RayPre &r,
@@ -366,7 +367,7 @@ __device__ __forceinline__ bool trav_step(const WideNode *__restrict__ nodes, un
                 if (t < c.best_t) {
                     c.best_t = t;
                     c.best_id = id;
-                    c.hit_slot = ti;
+                    c.hit_slot = 2 * ti + __float_as_int(b.w);
                     return true;
                 }
             } else if (t < c.best_t || (t == c.best_t && id < c.best_id)) {
@@ -374,7 +375,7 @@ __device__ __forceinline__ bool trav_step(const WideNode *__restrict__ nodes, un
                 c.best_id = id;
                 c.bu = u;
                 c.bv = v;
-                c.hit_slot = ti;
+                c.hit_slot = 2 * ti + __float_as_int(b.w);
             }
         }
     }
