@@ -212,8 +212,9 @@ typedef struct kgk_host_scene {
  * semantics of load_object (FileIO/IO_load_WavefrontObj.cuh:10-127, which
  * parses with tinyobjloader v2.0.0rc10) and load_Textures / load_HDR
  * (FileIO/IO_load_images.cuh:9-29).  MTL files and textures are looked up in
- * the OBJ file's directory.  Vertices without vn take the face normal and
- * without vt (0,0,0), where the reference would read past its arrays.
+ * the OBJ file's directory.  Vertices without vn (or whose vn index is past
+ * the file's normals) take the face normal and without vt (0,0,0), where the
+ * reference would read past its arrays.
  * Images: PNG, binary PNM and Radiance .hdr (KGK_ERR_UNSUPPORTED for JPEG and
  * other formats). */
 kgk_status kgk_load_obj(const char *obj_path, const char *hdr_path, kgk_host_scene *out);

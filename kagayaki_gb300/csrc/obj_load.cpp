@@ -24,8 +24,9 @@
 //   texcoords (u, v, 0); diffuse + 1e-4 when a component is 0; Lambert;
 //   specular = |Ks|; textured and untextured materials take the two parameter
 //   sets of IO_load_WavefrontObj.cuh:114-122; texture pixels + 1e-4.
-// Differences by design: vertices without vn take the face's geometric normal
-// and without vt take (0, 0, 0) (the reference indexes missing entries); MTL
+// Differences by design: vertices without vn (or with an index past the vn
+// records) take the face's geometric normal and without vt take (0, 0, 0)
+// (the reference indexes missing entries); MTL
 // files and textures are looked up in the OBJ file's directory (the reference
 // uses the working directory); malformed input returns an error instead of
 // exiting.
@@ -854,20 +855,15 @@ kgk_status kgk_load_obj_ex(const char *obj_path, const char *hdr_path, const kgk
                     return;
                 }
                 p[k] = vec3(d.v[3 * ix[k]->v], d.v[3 * ix[k]->v + 1], d.v[3 * ix[k]->v + 2]);
-                if (ix[k]->vn >= 0) {
-                    if ((size_t)ix[k]->vn >= nvn) {
-                        bad[blk] = {i, 1};
-                        return;
-                    }
+                // a normal or texcoord index past the file's records counts as
+                // absent (tinyobjloader keeps it; load_object would read past
+                // its arrays)
+                if (ix[k]->vn >= 0 && (size_t)ix[k]->vn < nvn) {
                     n[k] = vec3(d.vn[3 * ix[k]->vn], d.vn[3 * ix[k]->vn + 1], d.vn[3 * ix[k]->vn + 2]);
                 } else {
                     all_n = false;
                 }
-                if (ix[k]->vt >= 0) {
-                    if ((size_t)ix[k]->vt >= nvt) {
-                        bad[blk] = {i, 2};
-                        return;
-                    }
+                if (ix[k]->vt >= 0 && (size_t)ix[k]->vt < nvt) {
                     uv[k] = vec3(d.vt[2 * ix[k]->vt], d.vt[2 * ix[k]->vt + 1], 0.0f);
                 } else {
                     uv[k] = vec3(0, 0, 0);
@@ -898,8 +894,7 @@ kgk_status kgk_load_obj_ex(const char *obj_path, const char *hdr_path, const kgk
     for (const auto &b : bad) {
         if (b.first == SIZE_MAX) continue;
         free(tri_out);
-        static const char *what[3] = {"vertex", "normal", "texcoord"};
-        return fail(KGK_ERR_PARSE, std::string(obj_path) + ": " + what[b.second] + " index out of range");
+        return fail(KGK_ERR_PARSE, std::string(obj_path) + ": vertex index out of range");
     }
     d.shapes.clear();
     d.shapes.shrink_to_fit();

@@ -226,6 +226,10 @@ def ref():
         L.ref_obj_texture.argtypes = [_i32, _vp, _vp, _vp, ctypes.POINTER(ctypes.POINTER(ctypes.c_float))]
         L.ref_load_image.argtypes = [ctypes.c_char_p, _vp, _vp, _vp]
         L.ref_load_image.restype = ctypes.POINTER(ctypes.c_float)
+        L.ref_tinyobj_parse.argtypes = [ctypes.c_char_p, ctypes.c_char_p, _vp]
+        L.ref_tinyobj_parse.restype = _i32
+        L.ref_tinyobj_copy.argtypes = [_vp, _vp, _vp, _vp, _vp]
+        L.ref_source_dir.restype = ctypes.c_char_p
         _ref = L
     return _ref
 
@@ -248,6 +252,35 @@ def ref_load_obj(directory):
         n = w.value * h.value * b.value
         texs.append(np.ctypeslib.as_array(px, (n,)).copy().reshape(h.value, w.value, b.value))
     return tris, mats, texs
+
+
+def ref_models_dir():
+    """tinyobjloader's vendored test models in the reference checkout the
+    reference build came from, or None when that checkout is not here."""
+    if not ref_available():
+        return None
+    d = os.path.join(ref().ref_source_dir().decode(), "external_lib", "tinyobjloader", "models")
+    return d if os.path.isdir(d) else None
+
+
+def ref_tinyobj(path):
+    """tinyobjloader's own parse of `path` (MTL files beside it), as the
+    reference's load_object configures it.  None when the reader rejects the
+    file; else a dict: v (n,3), vn (n,3), vt (n,2), corners (t,3,3) of
+    (vertex, texcoord, normal) indices, -1 = none, and per triangle
+    material, smoothing group and shape index (t,3), and the material count."""
+    counts = np.zeros(5, np.int64)
+    d = os.path.dirname(os.path.abspath(path)) + "/"
+    if not ref().ref_tinyobj_parse(path.encode(), d.encode(), _ptr(counts)):
+        return None
+    nv, nn, nt, ntri, nmat = (int(c) for c in counts)
+    v = np.zeros((nv, 3), np.float32)
+    vn = np.zeros((nn, 3), np.float32)
+    vt = np.zeros((nt, 2), np.float32)
+    corners = np.zeros((ntri, 3, 3), np.int32)
+    face = np.zeros((ntri, 3), np.int32)
+    ref().ref_tinyobj_copy(_ptr(v), _ptr(vn), _ptr(vt), _ptr(corners), _ptr(face))
+    return dict(v=v, vn=vn, vt=vt, corners=corners, face=face, n_materials=nmat)
 
 
 def ref_load_image(path):

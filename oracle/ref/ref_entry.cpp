@@ -17,6 +17,9 @@
  *   ref_disney_eval    evaluate_Disney_BRDF / _pdf (Disney_BRDF.cuh:118-183).
  *   ref_camera_setup   Camera_SetUpCamera (struct_Camera.cuh:27-35).
  *   ref_light_cdf      calculate_Lss / calculate_Lss_HDR.
+ *   ref_load_obj       load_object (IO_load_WavefrontObj.cuh:10-127).
+ *   ref_tinyobj_parse  tinyobjloader's raw parse, as load_object configures it.
+ *   ref_load_image     stbi_loadf.
  *
  * The traversal-call counter replaces struct_stack.cuh (a 37-line fixed-size
  * stack) with an equivalent class whose constructor counts one ray per
@@ -324,6 +327,65 @@ void ref_obj_texture(int i, int *w, int *h, int *bpp, const float **pixels) {
     *bpp = HOST_TexturesData[i].bpp;
     *pixels = HOST_TexturesData[i].pixels;
 }
+
+/* tinyobjloader's own parse of one OBJ (the library load_object calls,
+ * IO_load_WavefrontObj.cuh:11-28, with its default reader configuration:
+ * triangulation on), MTL files looked up in mtl_dir.  Returns 1 when the
+ * reader accepts the file, 0 when it rejects it; counts[0..4] = vertices,
+ * normals, texcoords, triangles, materials.  ref_tinyobj_copy then gives the
+ * attribute arrays, per corner (vertex, texcoord, normal) indices (-1 = none)
+ * and per triangle (material, smoothing group, shape). */
+static std::vector<float> g_to_v, g_to_vn, g_to_vt;
+static std::vector<int> g_to_corner, g_to_face;
+int ref_tinyobj_parse(const char *path, const char *mtl_dir, long long *counts) {
+    tinyobj::ObjReaderConfig cfg;
+    cfg.mtl_search_path = mtl_dir;
+    tinyobj::ObjReader reader;
+    g_to_v.clear(); g_to_vn.clear(); g_to_vt.clear(); g_to_corner.clear(); g_to_face.clear();
+    for (int k = 0; k < 5; ++k) counts[k] = 0;
+    if (!reader.ParseFromFile(path, cfg)) return 0;
+    const auto &a = reader.GetAttrib();
+    g_to_v.assign(a.vertices.begin(), a.vertices.end());
+    g_to_vn.assign(a.normals.begin(), a.normals.end());
+    g_to_vt.assign(a.texcoords.begin(), a.texcoords.end());
+    const auto &shapes = reader.GetShapes();
+    for (size_t s = 0; s < shapes.size(); ++s) {
+        const auto &m = shapes[s].mesh;
+        size_t off = 0;
+        for (size_t f = 0; f < m.num_face_vertices.size(); ++f) {
+            const size_t fv = m.num_face_vertices[f];
+            if (fv == 3) {
+                for (size_t v = 0; v < 3; ++v) {
+                    const tinyobj::index_t ix = m.indices[off + v];
+                    g_to_corner.push_back(ix.vertex_index);
+                    g_to_corner.push_back(ix.texcoord_index);
+                    g_to_corner.push_back(ix.normal_index);
+                }
+                g_to_face.push_back(m.material_ids[f]);
+                g_to_face.push_back((int)m.smoothing_group_ids[f]);
+                g_to_face.push_back((int)s);
+            }
+            off += fv;
+        }
+    }
+    counts[0] = (long long)g_to_v.size() / 3;
+    counts[1] = (long long)g_to_vn.size() / 3;
+    counts[2] = (long long)g_to_vt.size() / 2;
+    counts[3] = (long long)g_to_face.size() / 3;
+    counts[4] = (long long)reader.GetMaterials().size();
+    return 1;
+}
+void ref_tinyobj_copy(float *v, float *vn, float *vt, int *corner, int *face) {
+    std::memcpy(v, g_to_v.data(), g_to_v.size() * sizeof(float));
+    std::memcpy(vn, g_to_vn.data(), g_to_vn.size() * sizeof(float));
+    std::memcpy(vt, g_to_vt.data(), g_to_vt.size() * sizeof(float));
+    std::memcpy(corner, g_to_corner.data(), g_to_corner.size() * sizeof(int));
+    std::memcpy(face, g_to_face.data(), g_to_face.size() * sizeof(int));
+}
+
+/* The reference checkout this library was built from (its vendored test
+ * models are read from there). */
+const char *ref_source_dir(void) { return KGK_REF_DIR; }
 
 /* stbi_loadf of one file (load_image without the +1e-4, and load_HDR). */
 const float *ref_load_image(const char *path, int *w, int *h, int *bpp) {

@@ -156,3 +156,66 @@ def test_pbr_materials_map_to_disney(tmp_path):
     assert tris["material_id"][-1] == 6
     with pytest.raises(KgkError, match="material_model"):
         load_obj(path, materials=7)
+
+
+def _normalize_ref(a):
+    """Vec normalize (struct_Vec.cuh:40-46) in float32: a zero vector becomes (10000, 0, 0)."""
+    a = a.astype(np.float32)
+    x, y, z = a[..., 0], a[..., 1], a[..., 2]
+    ln = np.sqrt(x * x + y * y + z * z)
+    safe = np.where(ln == 0, np.float32(1), ln)
+    out = a / safe[..., None]
+    out[ln == 0] = np.array([10000, 0, 0], np.float32)
+    return out
+
+
+def test_vendored_models_parse_like_tinyobjloader():
+    """Every test model vendored with tinyobjloader, parsed by the reference's
+    own tinyobjloader build and by kgk_load_obj: the same accept / reject
+    decision, and for accepted files the same triangles bit for bit -
+    positions, normals (the file's when all three corners have one, else the
+    face normal), texcoords, material ids (+1 for the reserved material),
+    smooth flags and shape ids.  Models whose MTL names a texture image that
+    is not among the models are skipped (the reference loads its textures
+    too), as are files with no triangles (the library rejects those)."""
+    from oracle import orc
+    models = orc.ref_models_dir()
+    if models is None:
+        pytest.skip("reference build or checkout not present")
+    compared = skipped_tex = 0
+    for name in sorted(os.listdir(models)):
+        if not name.endswith(".obj"):
+            continue
+        path = os.path.join(models, name)
+        ref = orc.ref_tinyobj(path)
+        try:
+            tris, mats, _, _ = load_obj(path)
+        except KgkError as e:
+            if "cannot open image" in str(e):
+                skipped_tex += 1
+                continue
+            assert ref is None or len(ref["face"]) == 0, (name, str(e))
+            continue
+        assert ref is not None and len(ref["face"]) == len(tris), name
+        c = ref["corners"]
+        P = ref["v"][c[:, :, 0]]
+        assert same_bits(tris["verts"][:, 0:3, :3], P), name
+        nn, nt = len(ref["vn"]), len(ref["vt"])
+        ok_n = ((c[:, :, 2] >= 0) & (c[:, :, 2] < nn)).all(1)
+        raw_n = ref["vn"][np.clip(c[:, :, 2], 0, max(nn - 1, 0))] if nn else np.zeros_like(P)
+        e1, e2 = P[:, 1] - P[:, 0], P[:, 2] - P[:, 0]
+        face = np.stack([e1[:, 1] * e2[:, 2] - e1[:, 2] * e2[:, 1], e1[:, 2] * e2[:, 0] - e1[:, 0] * e2[:, 2],
+                         e1[:, 0] * e2[:, 1] - e1[:, 1] * e2[:, 0]], 1)
+        exp_n = np.where(ok_n[:, None, None], _normalize_ref(raw_n), _normalize_ref(face)[:, None, :])
+        assert same_bits(tris["verts"][:, 3:6, :3], exp_n), name
+        ok_t = (c[:, :, 1] >= 0) & (c[:, :, 1] < nt)
+        raw_t = ref["vt"][np.clip(c[:, :, 1], 0, max(nt - 1, 0))] if nt else np.zeros(c.shape[:2] + (2,), np.float32)
+        exp_t = np.zeros(c.shape[:2] + (3,), np.float32)
+        exp_t[..., :2] = np.where(ok_t[..., None], raw_t, 0)
+        assert same_bits(tris["verts"][:, 6:9, :3], exp_t), name
+        assert np.array_equal(tris["material_id"], ref["face"][:, 0] + 1), name
+        assert np.array_equal(tris["is_SmoothNormal"], ref["face"][:, 1] != 0), name
+        assert np.array_equal(tris["shape_id"], ref["face"][:, 2]), name
+        assert len(mats) == ref["n_materials"] + 1, name
+        compared += 1
+    assert compared >= 25 and skipped_tex <= 10, (compared, skipped_tex)
