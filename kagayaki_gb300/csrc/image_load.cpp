@@ -10,8 +10,9 @@
 //     float, alpha (the last channel when the count is even) = byte / 255;
 //   * 16-bit images are first reduced to 8 bits (the high byte).
 // This file decodes PNG (every colour type and bit depth, tRNS, Adam7),
-// binary PNM (P5 / P6) and Radiance .hdr, and converts them by those rules.
-// JPEG, BMP, TGA, PSD, GIF and PIC are not decoded (KGK_ERR_UNSUPPORTED).
+// binary PNM (P5 / P6) and Radiance .hdr, takes JPEG from jpeg_load.cpp, and
+// converts them by those rules.  BMP, TGA, PSD, GIF and PIC are not decoded
+// (KGK_ERR_UNSUPPORTED).
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -536,9 +537,20 @@ kgk_status decode_hdr(const std::vector<uint8_t> &f, kgk_texture *out, const cha
     return KGK_OK;
 }
 
+// A JPEG starts with 0xff (more 0xff fill bytes may follow) and the SOI marker.
+bool is_jpeg(const std::vector<uint8_t> &f) {
+    if (f.empty() || f[0] != 0xff) return false;
+    size_t i = 1;
+    while (i < f.size() && f[i] == 0xff) ++i;
+    return i < f.size() && f[i] == 0xd8;
+}
+
 }  // namespace
 
 namespace kgk {
+
+kgk_status decode_jpeg(const std::vector<uint8_t> &f, int *w_out, int *h_out, int *n_out, std::vector<uint8_t> &pix,
+                       const char *path);
 
 // stbi_loadf: decode and convert to float (see the file comment).
 kgk_status load_image_float(const char *path, kgk_texture *out) {
@@ -556,10 +568,11 @@ kgk_status load_image_float(const char *path, kgk_texture *out) {
         KGK_TRY(decode_png(f, &w, &h, &n, pix, path));
     } else if (f.size() >= 3 && f[0] == 'P' && (f[1] == '5' || f[1] == '6')) {
         KGK_TRY(decode_pnm(f, &w, &h, &n, pix, path));
-    } else if (f.size() >= 3 && f[0] == 0xff && f[1] == 0xd8) {
-        return fail(KGK_ERR_UNSUPPORTED, std::string("JPEG is not decoded (convert to PNG): ") + path);
+    } else if (is_jpeg(f)) {
+        KGK_TRY(decode_jpeg(f, &w, &h, &n, pix, path));
     } else {
-        return fail(KGK_ERR_UNSUPPORTED, std::string("unknown image format (PNG, PNM and .hdr are decoded): ") + path);
+        return fail(KGK_ERR_UNSUPPORTED,
+                    std::string("unknown image format (PNG, JPEG, PNM and .hdr are decoded): ") + path);
     }
     const size_t npx = (size_t)w * h;
     float *px = (float *)malloc(npx * n * sizeof(float));

@@ -196,8 +196,416 @@ def pnm_cases():
             ("rgb16.ppm", b"P6\n6 4\n65535\n" + c16.tobytes())]
 
 
+# ---------------------------------------------------------------------------
+# JPEG (a small encoder for the fixtures: any sampling factors, sequential
+# interleaved or per-component scans, progressive spectral selection and
+# successive approximation, restart intervals, Adobe / JFIF segments)
+# ---------------------------------------------------------------------------
+def _zigzag():
+    order = []
+    for s in range(15):
+        rng_ = range(s + 1)
+        for k in rng_:
+            x = s - k if s % 2 else k
+            y = s - x
+            if x < 8 and y < 8:
+                order.append(y * 8 + x)
+    return np.array(order)
+
+
+ZIGZAG = _zigzag()
+
+
+def _dct_matrix():
+    m = np.zeros((8, 8))
+    for k in range(8):
+        a = np.sqrt(1 / 8) if k == 0 else np.sqrt(2 / 8)
+        for n in range(8):
+            m[k, n] = a * np.cos((2 * n + 1) * k * np.pi / 16)
+    return m
+
+
+DCT8 = _dct_matrix()
+
+
+def _huff_table(freq):
+    """Code lengths (counts per length 1..16, symbols in order) for symbol
+    frequencies by the JPEG standard's procedure (Annex K.2): a reserved
+    dummy symbol keeps any code from being all ones, lengths above 16 are
+    folded back."""
+    freq = dict(freq)
+    syms = sorted(freq)
+    f = {k: v for k, v in freq.items() if v > 0}
+    if not f:
+        f = {0: 1}
+    f[256] = 1  # reserved
+    size = {k: 0 for k in f}
+    others = {k: -1 for k in f}
+    fr = dict(f)
+    while True:
+        live = [k for k in fr if fr[k] > 0]
+        if len(live) < 2:
+            break
+        live.sort(key=lambda k: (fr[k], -k))
+        c1, c2 = live[0], live[1]
+        # c1: the least frequent (largest value on ties), c2: the next
+        fr[c1] += fr[c2]
+        fr[c2] = 0
+        size[c1] += 1
+        while others[c1] != -1:
+            c1 = others[c1]
+            size[c1] += 1
+        others[c1] = c2
+        size[c2] += 1
+        while others[c2] != -1:
+            c2 = others[c2]
+            size[c2] += 1
+    bits = [0] * 33
+    for k, sz in size.items():
+        bits[sz] += 1
+    i = 32
+    while i > 16:
+        while bits[i] > 0:
+            j = i - 2
+            while bits[j] == 0:
+                j -= 1
+            bits[i] -= 2
+            bits[i - 1] += 1
+            bits[j + 1] += 2
+            bits[j] -= 1
+        i -= 1
+    while bits[i] == 0:
+        i -= 1
+    bits[i] -= 1  # remove the reserved code
+    vals = sorted((k for k in size if k != 256), key=lambda k: (size[k], k))
+    counts = bits[1:17]
+    # canonical codes
+    codes = {}
+    code = 0
+    k = 0
+    for ln in range(1, 17):
+        for _ in range(counts[ln - 1]):
+            codes[vals[k]] = (code, ln)
+            code += 1
+            k += 1
+        code <<= 1
+    return counts, vals, codes
+
+
+class _BitWriter:
+    def __init__(self):
+        self.out = bytearray()
+        self.acc = 0
+        self.n = 0
+
+    def put(self, code, length):
+        for i in range(length - 1, -1, -1):
+            self.acc = (self.acc << 1) | ((code >> i) & 1)
+            self.n += 1
+            if self.n == 8:
+                self.out.append(self.acc)
+                if self.acc == 0xff:
+                    self.out.append(0)
+                self.acc = 0
+                self.n = 0
+
+    def flush(self):
+        while self.n:
+            self.put(1, 1)
+
+
+def _mag(v):
+    a = abs(int(v))
+    n = a.bit_length()
+    bits = a if v >= 0 else (~a) & ((1 << n) - 1)
+    return n, bits
+
+
+def jpeg_bytes(planes, samp, qscale=1.0, scans=None, progressive=False, restart=0, adobe=None, jfif=True,
+               ids=None, dqt16=False, pad_ff=False):
+    """planes: component sample planes (uint8 arrays, component sizes of the
+    image (W, H) for the sampling factors `samp` [(h, v), ...]).  scans:
+    [(component indices, Ss, Se, Ah, Al)] (sequential: Ss=0, Se=63, A=0)."""
+    nc = len(planes)
+    hmax = max(h for h, _ in samp)
+    vmax = max(v for _, v in samp)
+    Hc = planes[0].shape[0] * vmax // samp[0][1] if False else None
+    # image size from the first component (chosen with h = hmax, v = vmax by the callers)
+    H, W = planes[0].shape
+    mcux = -(-W // (8 * hmax))
+    mcuy = -(-H // (8 * vmax))
+    ids = ids or list(range(1, nc + 1))
+    # quantisation: two procedural tables
+    uu, vv = np.meshgrid(np.arange(8), np.arange(8))
+    qt = [np.clip(np.round((2 + (uu + vv) * 2.5) * qscale), 1, 65535 if dqt16 else 255).astype(np.int64),
+          np.clip(np.round((3 + (uu + vv) * 4.0) * qscale), 1, 65535 if dqt16 else 255).astype(np.int64)]
+    tq = [0 if c == 0 else 1 for c in range(nc)]
+    # coefficients per component: padded to whole MCUs with edge replication
+    coefs = []
+    for c in range(nc):
+        h, v = samp[c]
+        bw, bh = mcux * h, mcuy * v
+        pl = planes[c].astype(np.float64)
+        pad = np.pad(pl, ((0, bh * 8 - pl.shape[0]), (0, bw * 8 - pl.shape[1])), mode="edge")
+        blocks = pad.reshape(bh, 8, bw, 8).transpose(0, 2, 1, 3) - 128.0
+        d = np.einsum("ki,abij,lj->abkl", DCT8, blocks, DCT8)
+        q = qt[tq[c]][None, None]
+        coefs.append(np.round(d / q).astype(np.int64).reshape(bh, bw, 64))
+    if scans is None:
+        scans = [(list(range(nc)), 0, 63, 0, 0)]
+
+    def blocks_of(comps):
+        """(component, block row, block col) in scan order, MCU by MCU."""
+        if len(comps) == 1:
+            c = comps[0]
+            h, v = samp[c]
+            cw = -(-W * h // hmax)
+            ch = -(-H * v // vmax)
+            for by in range(-(-ch // 8)):
+                for bx in range(-(-cw // 8)):
+                    yield [(c, by, bx)]
+        else:
+            for my in range(mcuy):
+                for mx in range(mcux):
+                    unit = []
+                    for c in comps:
+                        h, v = samp[c]
+                        for y in range(v):
+                            for x in range(h):
+                                unit.append((c, my * v + y, mx * h + x))
+                    yield unit
+
+    def pt_ac(val, al):  # point transform of an AC coefficient (magnitude shift)
+        return -((-val) >> al) if val < 0 else val >> al
+
+    def encode_scan(comps, ss, se, ah, al, tables=None):
+        """Symbols of one scan: returns (dc freq, ac freq, writer) - with
+        tables=None only counts symbols."""
+        dcf, acf = {}, {}
+        bw = _BitWriter()
+        emit = tables is not None
+
+        def sym(kind, s, extra=0, nbits=0):
+            (dcf if kind == 0 else acf)[s] = (dcf if kind == 0 else acf).get(s, 0) + 1
+            if emit:
+                code, ln = tables[kind][s]
+                bw.put(code, ln)
+                if nbits:
+                    bw.put(extra, nbits)
+
+        state = {"eobrun": 0, "be": []}
+
+        def flush_eob():
+            r = state["eobrun"]
+            if r:
+                nb = r.bit_length() - 1
+                sym(1, nb << 4, r - (1 << nb), nb)
+                state["eobrun"] = 0
+            if emit:
+                for bit in state["be"]:
+                    bw.put(bit, 1)
+            state["be"] = []
+
+        pred = {c: 0 for c in comps}
+        units = list(blocks_of(comps))
+        for ui, unit in enumerate(units):
+            if restart and ui and ui % restart == 0:
+                flush_eob()
+                if emit:
+                    bw.flush()
+                    bw.out += bytes([0xff, 0xd0 + ((ui // restart - 1) % 8)])
+                pred = {c: 0 for c in comps}
+            for (c, by, bx) in unit:
+                z = coefs[c][by, bx][ZIGZAG]
+                if ss == 0:  # DC
+                    if ah == 0:
+                        dcv = int(z[0]) >> al
+                        diff = dcv - pred[c]
+                        pred[c] = dcv
+                        n, bits = _mag(diff)
+                        sym(0, n, bits, n)
+                    else:
+                        if emit:
+                            bw.put((int(z[0]) >> al) & 1, 1)
+                    if not progressive:  # sequential: the AC terms follow
+                        r = 0
+                        for k in range(1, 64):
+                            v = int(z[k])
+                            if v == 0:
+                                r += 1
+                                continue
+                            while r > 15:
+                                sym(1, 0xf0)
+                                r -= 16
+                            n, bits = _mag(v)
+                            sym(1, (r << 4) | n, bits, n)
+                            r = 0
+                        if r:
+                            sym(1, 0)
+                    continue
+                if ah == 0:  # AC first scan of the band
+                    vals = [pt_ac(int(z[k]), al) for k in range(ss, se + 1)]
+                    if not any(vals):
+                        state["eobrun"] += 1
+                        if state["eobrun"] == 0x7fff:
+                            flush_eob()
+                        continue
+                    flush_eob()
+                    r = 0
+                    last = max(i for i, v in enumerate(vals) if v)
+                    for i, v in enumerate(vals):
+                        if i > last:
+                            break
+                        if v == 0:
+                            r += 1
+                            continue
+                        while r > 15:
+                            sym(1, 0xf0)
+                            r -= 16
+                        n, bits = _mag(v)
+                        sym(1, (r << 4) | n, bits, n)
+                        r = 0
+                    if last < se - ss:
+                        state["eobrun"] += 1
+                        if state["eobrun"] == 0x7fff:
+                            flush_eob()
+                    continue
+                # AC refinement scan (the standard's correction-bit scheme)
+                absv = [abs(int(z[k])) >> al for k in range(ss, se + 1)]
+                sign = [int(z[k]) >= 0 for k in range(ss, se + 1)]
+                eob = max([i for i, v in enumerate(absv) if v == 1], default=-1)
+                r = 0
+                br = []
+                for i, v in enumerate(absv):
+                    if v == 0:
+                        r += 1
+                        continue
+                    while r > 15 and i <= eob:
+                        flush_eob()
+                        sym(1, 0xf0)
+                        r -= 16
+                        if emit:
+                            for bit in br:
+                                bw.put(bit, 1)
+                        br = []
+                    if v > 1:
+                        br.append(v & 1)
+                        continue
+                    flush_eob()
+                    sym(1, (r << 4) | 1, 1 if sign[i] else 0, 1)
+                    if emit:
+                        for bit in br:
+                            bw.put(bit, 1)
+                    br = []
+                    r = 0
+                if r > 0 or br:
+                    state["eobrun"] += 1
+                    state["be"] += br
+                    if state["eobrun"] == 0x7fff or len(state["be"]) > 937:
+                        flush_eob()
+        flush_eob()
+        if emit:
+            bw.flush()
+        return dcf, acf, bw
+
+    out = bytearray(b"\xff\xd8")
+    if pad_ff:
+        out += b"\xff"
+    if jfif:
+        out += b"\xff\xe0" + struct.pack(">H", 16) + b"JFIF\x00" + bytes([1, 1, 0, 0, 1, 0, 1, 0, 0])
+    if adobe is not None:
+        out += b"\xff\xee" + struct.pack(">H", 14) + b"Adobe\x00" + bytes([100, 0, 0, 0, 0, adobe])
+    out += b"\xff\xfe" + struct.pack(">H", 2 + 9) + b"seeded!!!"
+    for t in range(2):
+        if dqt16:
+            out += b"\xff\xdb" + struct.pack(">H", 2 + 129) + bytes([0x10 | t]) + \
+                b"".join(struct.pack(">H", int(x)) for x in qt[t].reshape(64)[ZIGZAG])
+        else:
+            out += b"\xff\xdb" + struct.pack(">H", 2 + 65) + bytes([t]) + bytes(int(x) for x in qt[t].reshape(64)[ZIGZAG])
+    sof = 0xc2 if progressive else (0xc1 if dqt16 else 0xc0)
+    out += bytes([0xff, sof]) + struct.pack(">HBHHB", 8 + 3 * nc, 8, H, W, nc)
+    for c in range(nc):
+        out += bytes([ids[c], (samp[c][0] << 4) | samp[c][1], tq[c]])
+    if restart:
+        out += b"\xff\xdd" + struct.pack(">HH", 4, restart)
+    for (comps, ss, se, ah, al) in scans:
+        dcf, acf, _ = encode_scan(comps, ss, se, ah, al)
+        dct = _huff_table(dcf) if dcf else None
+        act = _huff_table(acf) if acf else None
+        seg = bytearray()
+        if dct:
+            seg += bytes([0x00]) + bytes(dct[0]) + bytes(dct[1])
+        if act:
+            seg += bytes([0x10]) + bytes(act[0]) + bytes(act[1])
+        if seg:
+            out += b"\xff\xc4" + struct.pack(">H", 2 + len(seg)) + seg
+        out += b"\xff\xda" + struct.pack(">HB", 6 + 2 * len(comps), len(comps))
+        for c in comps:
+            out += bytes([ids[c], 0x00])
+        out += bytes([ss, se, (ah << 4) | al])
+        tabs = ({k: v for k, v in dct[2].items()} if dct else {}, {k: v for k, v in act[2].items()} if act else {})
+        _, _, bw = encode_scan(comps, ss, se, ah, al, tabs)
+        out += bw.out
+    out += b"\xff\xd9"
+    return bytes(out)
+
+
+def _smooth(rng, h, w):
+    """A smooth seeded plane with some detail (uint8)."""
+    y, x = np.mgrid[0:h, 0:w]
+    v = 128 + 60 * np.sin(x / (2 + rng.uniform(0, 5)) + rng.uniform(0, 6)) * np.cos(y / (3 + rng.uniform(0, 5)))
+    v += rng.normal(0, 12, (h, w))
+    return np.clip(np.round(v), 0, 255).astype(np.uint8)
+
+
+def jpeg_cases():
+    rng = np.random.default_rng(15)
+    cases = []
+
+    def planes(W, H, samp):
+        hmax = max(h for h, _ in samp)
+        vmax = max(v for _, v in samp)
+        return [_smooth(rng, -(-H * v // vmax), -(-W * h // hmax)) for h, v in samp]
+
+    s444 = [(1, 1)] * 3
+    s420 = [(2, 2), (1, 1), (1, 1)]
+    s422 = [(2, 1), (1, 1), (1, 1)]
+    s440 = [(1, 2), (1, 1), (1, 1)]
+    s411 = [(4, 1), (1, 1), (1, 1)]
+    cases.append(("gray.jpg", jpeg_bytes(planes(37, 29, [(1, 1)]), [(1, 1)])))
+    cases.append(("ycc444.jpg", jpeg_bytes(planes(33, 21, s444), s444)))
+    cases.append(("ycc420.jpg", jpeg_bytes(planes(45, 33, s420), s420, qscale=2.0)))
+    cases.append(("ycc420_1px.jpg", jpeg_bytes(planes(1, 1, s420), s420)))
+    cases.append(("ycc420_2x3.jpg", jpeg_bytes(planes(2, 3, s420), s420)))
+    cases.append(("ycc422.jpg", jpeg_bytes(planes(40, 17, s422), s422)))
+    cases.append(("ycc440.jpg", jpeg_bytes(planes(23, 40, s440), s440)))
+    cases.append(("ycc411.jpg", jpeg_bytes(planes(50, 12, s411), s411)))
+    cases.append(("ycc420_restart.jpg", jpeg_bytes(planes(70, 50, s420), s420, restart=3)))
+    cases.append(("ycc420_planar.jpg", jpeg_bytes(planes(41, 35, s420), s420,
+                                                 scans=[([0], 0, 63, 0, 0), ([1], 0, 63, 0, 0), ([2], 0, 63, 0, 0)])))
+    cases.append(("ycc_dqt16.jpg", jpeg_bytes(planes(24, 18, s444), s444, qscale=0.5, dqt16=True)))
+    cases.append(("rgb_ids.jpg", jpeg_bytes(planes(19, 13, s444), s444, ids=[ord("R"), ord("G"), ord("B")])))
+    cases.append(("rgb_adobe.jpg", jpeg_bytes(planes(19, 13, s444), s444, adobe=0, jfif=False)))
+    cases.append(("cmyk.jpg", jpeg_bytes(planes(21, 14, [(1, 1)] * 4), [(1, 1)] * 4, adobe=0, jfif=False)))
+    cases.append(("ycck.jpg", jpeg_bytes(planes(21, 14, [(2, 2), (1, 1), (1, 1), (2, 2)]),
+                                         [(2, 2), (1, 1), (1, 1), (2, 2)], adobe=2, jfif=False)))
+    prog = [([0, 1, 2], 0, 0, 0, 1),
+            ([0], 1, 5, 0, 2), ([2], 1, 63, 0, 1), ([1], 1, 63, 0, 1), ([0], 6, 63, 0, 2),
+            ([0], 1, 63, 2, 1), ([0, 1, 2], 0, 0, 1, 0), ([2], 1, 63, 1, 0), ([1], 1, 63, 1, 0),
+            ([0], 1, 63, 1, 0)]
+    cases.append(("prog420.jpg", jpeg_bytes(planes(53, 37, s420), s420, scans=prog, progressive=True,
+                                            qscale=0.7)))
+    cases.append(("prog420_restart.jpg", jpeg_bytes(planes(53, 37, s420), s420, scans=prog, progressive=True,
+                                                    restart=2, pad_ff=True)))
+    cases.append(("prog_gray.jpg", jpeg_bytes(planes(30, 26, [(1, 1)]), [(1, 1)], progressive=True, qscale=0.4,
+                                              scans=[([0], 0, 0, 0, 2), ([0], 1, 63, 0, 3), ([0], 0, 0, 2, 1),
+                                                     ([0], 1, 63, 3, 2), ([0], 1, 63, 2, 1), ([0], 0, 0, 1, 0),
+                                                     ([0], 1, 63, 1, 0)])))
+    return cases
+
+
 def image_cases():
-    return png_cases() + hdr_cases() + pnm_cases()
+    return png_cases() + hdr_cases() + pnm_cases() + jpeg_cases()
 
 
 # ---------------------------------------------------------------------------
@@ -250,6 +658,8 @@ usemtl tex_ga
 f 9/1/5 10/2/5 11/3/5 12/4/5 13/5/5 14/1/5 15/2/5 16/3/5
 usemtl tex_pal
 f 9/1/5 11/3/5 13/5/5
+usemtl tex_jpg
+f 10/2/5 12/4/5 14/1/5
 l 1 2 3
 o lines_only
 l 9 10
@@ -282,6 +692,9 @@ map_Kd some/dir/tex_ga.png
 newmtl tex_pal
 Kd 0.2 0.3 0.4
 map_Kd -blendu off -s 1 1 1 tex_pal.png
+
+newmtl tex_jpg
+map_Kd tex_jpg.jpg
 """
 
 
@@ -298,6 +711,9 @@ def write_obj_scene(d):
     with open(os.path.join(d, "tex_pal.png"), "wb") as f:
         f.write(png_bytes(rng.integers(0, 12, (5, 11, 1)), 3, 4, palette=rng.integers(0, 256, (12, 3)),
                           trns=bytes([0, 128, 255]), seed=3))
+    with open(os.path.join(d, "tex_jpg.jpg"), "wb") as f:
+        s420 = [(2, 2), (1, 1), (1, 1)]
+        f.write(jpeg_bytes([_smooth(rng, 14, 22), _smooth(rng, 7, 11), _smooth(rng, 7, 11)], s420))
     return os.path.join(d, "OBJ.obj")
 
 

@@ -138,12 +138,12 @@ def test_pbr_materials_map_to_disney(tmp_path):
         f.write("usemtl coat\nf 1 2 3\n")
     _, ref_m, _, _ = load_obj(path)
     tris, m, _, _ = load_obj(path, materials=MATERIALS_PBR)
-    names = ["red", "tex_rgb", "emissive", "tex_ga", "tex_pal", "coat"]
+    names = ["red", "tex_rgb", "emissive", "tex_ga", "tex_pal", "tex_jpg", "coat"]
     assert len(m) == len(ref_m) == len(names) + 1
     for i, name in enumerate(names, start=1):
         if name not in ("red", "coat"):  # no PBR key: converted as the reference does
             assert same_bits(m[i], ref_m[i]), name
-    red, coat = m[1], m[6]
+    red, coat = m[1], m[7]
     assert red["MATERIAL_TYPE_ID"] == structs.DISNEY and coat["MATERIAL_TYPE_ID"] == structs.DISNEY
     np.testing.assert_allclose(red["diffuse"][:3], [0.63, 0.065, 0.05], rtol=1e-6)
     assert red["roughness"] == np.float32(0.5) and red["metallic"] == np.float32(0.25)
@@ -153,7 +153,7 @@ def test_pbr_materials_map_to_disney(tmp_path):
     assert coat["clearcoat"] == 1.0 and coat["cloearcoatGloss"] == np.float32(0.75)  # Pc clamped to 1
     assert coat["sheen"] == np.float32(0.5) and coat["anisotropic"] == np.float32(0.7)
     assert coat["specular"] == np.float32(0.5) and coat["IOR"] == np.float32(1.45)
-    assert tris["material_id"][-1] == 6
+    assert tris["material_id"][-1] == 7
     with pytest.raises(KgkError, match="material_model"):
         load_obj(path, materials=7)
 
