@@ -687,6 +687,86 @@ __global__ void k_s_atrous(StdArgs a, const float4 *__restrict__ in, float4 *out
     }
 }
 
+// The a-trous pass for the small steps (1, 2, 4) on shared-memory tiles: a
+// block stages its 32 x 8 pixels and a halo of 2 * step (the 5 x 5 taps at
+// that step, the 3 x 3 variance blur and the depth gradient all fall inside)
+// - normal and depth, material id (-1: no hit, -2: outside the image),
+// colour and variance - then filters from shared memory with the 3 x 3
+// variance blur of k_s_gauss_var computed in place.  Same arithmetic, in the
+// same order, as k_s_gauss_var + k_s_atrous, so the result is the same.
+template <int kStep>
+__global__ void __launch_bounds__(256) k_s_atrous_tile(StdArgs a, const float4 *__restrict__ in, float4 *out) {
+    constexpr int TX = 32, TY = 8, R = 2 * kStep, SX = TX + 2 * R, SY = TY + 2 * R;
+    __shared__ float4 s_nd[SY][SX];  // normal, depth
+    __shared__ float4 s_c[SY][SX];   // colour, variance
+    __shared__ int s_m[SY][SX];      // material id, -1 no hit, -2 outside
+    const int W = a.W, H = a.H;
+    const int x0 = blockIdx.x * TX - R, y0 = blockIdx.y * TY - R;
+    for (int i = threadIdx.y * TX + threadIdx.x; i < SX * SY; i += TX * TY) {
+        const int sx = i % SX, sy = i / SX, gx = x0 + sx, gy = y0 + sy;
+        if (gx >= 0 && gx < W && gy >= 0 && gy < H) {
+            const int q = W * gy + gx;
+            const float4 nr = a.nrm[q];
+            s_nd[sy][sx] = make_float4(nr.x, nr.y, nr.z, a.pos[q].w);
+            s_c[sy][sx] = in[q];
+            s_m[sy][sx] = __float_as_int(nr.w) < 0 ? -1 : max(__float_as_int(a.alb[q].w), 0);
+        } else {
+            s_nd[sy][sx] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            s_c[sy][sx] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            s_m[sy][sx] = -2;
+        }
+    }
+    __syncthreads();
+    const int x = blockIdx.x * TX + threadIdx.x, y = blockIdx.y * TY + threadIdx.y;
+    if (x >= W || y >= H) return;
+    const int p = W * y + x, cx = threadIdx.x + R, cy = threadIdx.y + R;
+    const float4 c = s_c[cy][cx];
+    const int mat = s_m[cy][cx];
+    if (mat < 0) {
+        out[p] = c;
+        return;
+    }
+    // k_s_gauss_var's 3 x 3 blur of the variance over the pixels in the image
+    float gs = 0, gw = 0;
+    for (int ky = -1; ky <= 1; ++ky)
+        for (int kx = -1; kx <= 1; ++kx) {
+            if (s_m[cy + ky][cx + kx] == -2) continue;
+            const float k = cKG[kx + 1] * cKG[ky + 1];
+            gs += k * s_c[cy + ky][cx + kx].w;
+            gw += k;
+        }
+    const float gvar = gs / gw;
+    const float4 nd = s_nd[cy][cx];
+    const float d = nd.w;
+    const float gx = (x + 1 < W ? s_nd[cy][cx + 1].w : d) - (x > 0 ? s_nd[cy][cx - 1].w : d);
+    const float gy = (y + 1 < H ? s_nd[cy + 1][cx].w : d) - (y > 0 ? s_nd[cy - 1][cx].w : d);
+    const float grad = 0.5f * fmaxf(fabsf(gx), fabsf(gy));
+    const float l = lumf(f3(c));
+    const float sdl = a.sl * sqrtf(fmaxf(gvar, 0.0f)) + 1e-6f;
+    float3 sc = f3(c) * (36.0f / 256.0f);
+    float sv = (36.0f / 256.0f) * (36.0f / 256.0f) * c.w;
+    float sw = 36.0f / 256.0f;
+#pragma unroll
+    for (int ki = 0; ki < 25; ++ki) {
+        if (ki == 12) continue;
+        const int ox = ki % 5 - 2, oy = ki / 5 - 2;
+        const int qy = cy + oy * kStep, qx = cx + ox * kStep;
+        const int qm = s_m[qy][qx];
+        if (qm != mat) continue;  // outside, no hit or another material
+        const float4 qn = s_nd[qy][qx];
+        const float4 qc = s_c[qy][qx];
+        const float dist = (float)kStep * sqrtf((float)(ox * ox + oy * oy));
+        const float wz = depth_weight_std(d, qn.w, grad, dist, a.sz);
+        const float wn = normal_weight(dot3(f3(nd), f3(qn)), a.sn, a.sn_log2);
+        const float wl = __expf(-fabsf(l - lumf(f3(qc))) / sdl);
+        const float w = cKW[ki] * wz * wn * wl;
+        sc += f3(qc) * w;
+        sv += w * w * qc.w;
+        sw += w;
+    }
+    out[p] = make_float4(sc.x / sw, sc.y / sw, sc.z / sw, sv / (sw * sw));
+}
+
 __global__ void k_s_feedback(StdArgs a, const float4 *filtered) {
     FOR_PIXELS(a.W * a.H) {
         if (__float_as_int(a.nrm[p].w) < 0) continue;
@@ -951,9 +1031,18 @@ kgk_status kgk_svgf_output(kgk_scene *s, const kgk_svgf_config *cfg, const kgk_v
         k_s_variance<<<g, 256, 0, st>>>(a);
         const int iters = cfg->atrous_iterations > 0 ? cfg->atrous_iterations : 5;
         float4 *src = S.col, *dst = S.tmp;
+        const dim3 tiles((W + 31) / 32, (H + 7) / 8), tile_threads(32, 8);
         for (int i = 0; i < iters; ++i) {
-            k_s_gauss_var<<<g, 256, 0, st>>>(a, src);
-            k_s_atrous<<<g, 256, 0, st>>>(a, src, dst, 1 << i);
+            if (i == 0) {
+                k_s_atrous_tile<1><<<tiles, tile_threads, 0, st>>>(a, src, dst);
+            } else if (i == 1) {
+                k_s_atrous_tile<2><<<tiles, tile_threads, 0, st>>>(a, src, dst);
+            } else if (i == 2) {
+                k_s_atrous_tile<4><<<tiles, tile_threads, 0, st>>>(a, src, dst);
+            } else {
+                k_s_gauss_var<<<g, 256, 0, st>>>(a, src);
+                k_s_atrous<<<g, 256, 0, st>>>(a, src, dst, 1 << i);
+            }
             if (i == 0) k_s_feedback<<<g, 256, 0, st>>>(a, dst);
             std::swap(src, dst);
         }
