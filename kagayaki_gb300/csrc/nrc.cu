@@ -61,6 +61,34 @@ __device__ __forceinline__ float encode_col(const float *raw, int c) {
     return 1.0f;
 }
 
+// All 64 input features of a raw query (the values of encode_col, with each
+// sincospif computed once).
+__device__ __forceinline__ void encode_row(const float *raw, float (&f)[64]) {
+#pragma unroll
+    for (int ax = 0; ax < 3; ++ax) {
+#pragma unroll
+        for (int k = 0; k < 6; ++k) {
+            float s, co;
+            sincospif(raw[ax] * (float)(1 << k), &s, &co);
+            f[ax * 12 + 2 * k] = s;
+            f[ax * 12 + 2 * k + 1] = co;
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < 6; ++j) f[36 + j] = raw[3 + j];  // normal, view
+#pragma unroll
+    for (int j = 0; j < 6; ++j) {
+        float s, co;
+        sincospif(raw[3 + j], &s, &co);
+        f[42 + 2 * j] = s;
+        f[42 + 2 * j + 1] = co;
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) f[54 + j] = raw[9 + j];  // roughness, albedo
+#pragma unroll
+    for (int j = 58; j < 64; ++j) f[j] = 1.0f;
+}
+
 // Input-layer A fragments of the warp's 16 samples (rows g and g + 8).
 __device__ __forceinline__ void encode_frags(const float *ra, const float *rb, uint32_t (&a)[4][4]) {
     const int t = threadIdx.x & 3;
@@ -333,13 +361,15 @@ __global__ void __launch_bounds__(128) k_infer_tc(const unsigned short *__restri
             float rw[kRaw];
 #pragma unroll
             for (int k = 0; k < kRaw; ++k) rw[k] = live ? raw[(size_t)q * stride_floats + k] : 0.0f;
+            float f[64];
+            encode_row(rw, f);
 #pragma unroll
             for (int c = 0; c < 8; ++c) {
                 uint4 v;
-                v.x = pack2(encode_col(rw, 8 * c + 0), encode_col(rw, 8 * c + 1));
-                v.y = pack2(encode_col(rw, 8 * c + 2), encode_col(rw, 8 * c + 3));
-                v.z = pack2(encode_col(rw, 8 * c + 4), encode_col(rw, 8 * c + 5));
-                v.w = pack2(encode_col(rw, 8 * c + 6), encode_col(rw, 8 * c + 7));
+                v.x = pack2(f[8 * c + 0], f[8 * c + 1]);
+                v.y = pack2(f[8 * c + 2], f[8 * c + 3]);
+                v.z = pack2(f[8 * c + 4], f[8 * c + 5]);
+                v.w = pack2(f[8 * c + 6], f[8 * c + 7]);
                 *reinterpret_cast<uint4 *>(A + sw_off(tid, c)) = v;
             }
         }
