@@ -221,15 +221,17 @@ __global__ void __launch_bounds__(256) k_infer(const unsigned short *__restrict_
 // ---------------------------------------------------------------------------
 // inference on the 5th-generation tensor cores (tcgen05 + TMEM)
 //
-// One CTA of 128 threads carries tiles of 128 queries through the network:
-// thread r owns row r.  Per layer the CTA writes the BF16 activations
-// (128 x 64) to shared memory in the 128-byte-swizzled K-major layout, one
-// elected thread issues four tcgen05.mma (M=128, N=64, K=16 each) against the
-// layer's weights (64 x 64, same layout, resident in shared memory) into a
-// 128 x 64 FP32 accumulator in tensor memory, and commits to an mbarrier; the
-// threads then read their row back from tensor memory (tcgen05.ld 32x32b),
-// apply the ReLU and round to BF16 for the next layer.  The output layer uses
-// N=16 (3 live rows of the padded weights).
+// A CTA holds the weights once (64 x 64 per layer, BF16, 128-byte-swizzled
+// K-major, in shared memory) for four warpgroups, each carrying its own tiles
+// of 128 queries through the network: thread r of a warpgroup owns row r.
+// Per layer a warpgroup writes the BF16 activations (128 x 64) to its
+// shared-memory tile in the same layout, one elected thread issues four
+// tcgen05.mma (M=128, N=64, K=16 each) into the warpgroup's 128 x 64 FP32
+// accumulator in tensor memory and commits to the warpgroup's mbarrier; the
+// threads then read their row back (tcgen05.ld 32x32b), apply the ReLU and
+// round to BF16 for the next layer.  The warpgroups synchronise on their own
+// named barriers, so the CUDA-core work of one overlaps the MMAs of another.
+// The output layer uses N=16 (3 live rows of the padded weights).
 // Every wait is bounded: on a timeout the CTA raises *err, stops issuing and
 // frees its tensor memory.
 // ---------------------------------------------------------------------------
@@ -240,11 +242,13 @@ constexpr uint32_t kLayerBytes = 64 * 128;       // 64 rows x 128 B (64 BF16)
 constexpr uint32_t kOutBytes = 16 * 128;         // padded output layer
 constexpr uint32_t kWOff = 0;                    // hidden layers at l * kLayerBytes
 constexpr uint32_t kOutOff = kLayers * kLayerBytes;
-constexpr uint32_t kAOff = kOutOff + kOutBytes;  // activation tile, 16 KB (1024-aligned)
-constexpr uint32_t kBarOff = kAOff + kRows * 128;
-constexpr uint32_t kSlotOff = kBarOff + 8;
+constexpr int kGroups = 4;                       // warpgroups per CTA, one tile each at a time
+constexpr uint32_t kAOff = kOutOff + kOutBytes;  // activation tiles, 16 KB each (1024-aligned)
+constexpr uint32_t kATile = kRows * 128;
+constexpr uint32_t kBarOff = kAOff + kGroups * kATile;  // one mbarrier per warpgroup
+constexpr uint32_t kSlotOff = kBarOff + 8 * kGroups;
 constexpr uint32_t kSmemBytes = kSlotOff + 8 + 1024;  // + room to align the base to 1024 B
-constexpr uint32_t kTmemCols = 64;
+constexpr uint32_t kTmemCols = 64 * kGroups;          // a 64-column accumulator per warpgroup
 static_assert(kAOff % 1024 == 0, "swizzle atoms need 1024-byte alignment");
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -314,15 +318,32 @@ __device__ __forceinline__ uint32_t sw_off(int r, int c) { return (uint32_t)r * 
 
 }  // namespace tc
 
-__global__ void __launch_bounds__(128) k_infer_tc(const unsigned short *__restrict__ img, const float *__restrict__ raw,
-                                                  int stride_floats, int n, const int *n_dev, float *out, float4 *rad,
-                                                  int *err) {
+// Named barrier of one warpgroup (ids 1..4; 0 is __syncthreads), and its OR
+// reduction.
+__device__ __forceinline__ void wg_sync(int id) { asm volatile("bar.sync %0, 128;" ::"r"(id) : "memory"); }
+__device__ __forceinline__ bool wg_sync_or(int id, bool v) {
+    uint32_t r;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\tsetp.ne.u32 p, %1, 0;\n\tbar.red.or.pred q, %2, 128, p;\n\t"
+        "selp.u32 %0, 1, 0, q;\n\t}\n"
+        : "=r"(r)
+        : "r"((uint32_t)v), "r"(id)
+        : "memory");
+    return r != 0;
+}
+
+__global__ void __launch_bounds__(128 * tc::kGroups) k_infer_tc(const unsigned short *__restrict__ img,
+                                                                const float *__restrict__ raw, int stride_floats,
+                                                                int n, const int *n_dev, float *out, float4 *rad,
+                                                                int *err) {
     using namespace tc;
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     const uint32_t pad = (1024u - (smem_u32(smem_raw) & 1023u)) & 1023u;
     unsigned char *sm = smem_raw + pad;
     const uint32_t s0 = smem_u32(sm);
     const int tid = threadIdx.x, warp = tid >> 5;
+    const int g = tid >> 7, r = tid & 127;  // warpgroup, row
+    const int wgbar = 1 + g;                // its named barrier
     // weights: BF16 image rows (pitch kPitch) -> swizzled K-major tiles
     for (int i = tid; i < (kLayers * 64 + 16) * 8; i += blockDim.x) {
         const int row = i >> 3, c = i & 7;  // row over all layers (64 per hidden layer, then 16)
@@ -332,8 +353,8 @@ __global__ void __launch_bounds__(128) k_infer_tc(const unsigned short *__restri
         else dst = kOutOff + sw_off(row - kLayers * 64, c);
         *reinterpret_cast<uint4 *>(sm + dst) = v;
     }
-    const uint32_t bar = s0 + kBarOff;
-    if (tid == 0) {
+    const uint32_t bar = s0 + kBarOff + 8u * (uint32_t)g;
+    if (r == 0) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
@@ -347,16 +368,17 @@ __global__ void __launch_bounds__(128) k_infer_tc(const unsigned short *__restri
     fence_before();
     __syncthreads();
     fence_after();
-    const uint32_t tmem = *reinterpret_cast<volatile uint32_t *>(sm + kSlotOff);
-    const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);  // this warp's 32 TMEM lanes
+    const uint32_t tmem = *reinterpret_cast<volatile uint32_t *>(sm + kSlotOff) + 64u * (uint32_t)g;
+    const uint32_t trow = tmem + ((uint32_t)((warp & 3) * 32) << 16);  // this warp's 32 TMEM lanes
     const int total = n_dev ? min(*n_dev, n) : n;
     uint32_t phase = 0;
     bool failed = false;
-    unsigned char *A = sm + kAOff;
-    for (int tile = blockIdx.x; tile * kRows < total; tile += gridDim.x) {
-        const int q = tile * kRows + tid;
+    unsigned char *A = sm + kAOff + (uint32_t)g * kATile;
+    const uint32_t a_addr = s0 + kAOff + (uint32_t)g * kATile;
+    for (int tile = blockIdx.x * kGroups + g; tile * kRows < total; tile += gridDim.x * kGroups) {
+        const int q = tile * kRows + r;
         const bool live = q < total;
-        // input encoding of row tid
+        // input encoding of row r
         {
             float rw[kRaw];
 #pragma unroll
@@ -370,7 +392,7 @@ __global__ void __launch_bounds__(128) k_infer_tc(const unsigned short *__restri
                 v.y = pack2(f[8 * c + 2], f[8 * c + 3]);
                 v.z = pack2(f[8 * c + 4], f[8 * c + 5]);
                 v.w = pack2(f[8 * c + 6], f[8 * c + 7]);
-                *reinterpret_cast<uint4 *>(A + sw_off(tid, c)) = v;
+                *reinterpret_cast<uint4 *>(A + sw_off(r, c)) = v;
             }
         }
         float y[3] = {0.0f, 0.0f, 0.0f};
@@ -378,10 +400,10 @@ __global__ void __launch_bounds__(128) k_infer_tc(const unsigned short *__restri
             const bool last = l == kLayers;
             fence_async_smem();
             fence_before();
-            __syncthreads();
-            if (tid == 0) {
+            wg_sync(wgbar);
+            if (r == 0) {
                 fence_after();
-                const uint64_t ad = sw128_desc(s0 + kAOff);
+                const uint64_t ad = sw128_desc(a_addr);
                 const uint64_t bd = sw128_desc(s0 + (last ? kOutOff : kWOff + (uint32_t)l * kLayerBytes));
                 const uint32_t id = last ? idesc_bf16(128, 16) : idesc_bf16(128, 64);
 #pragma unroll
@@ -390,7 +412,7 @@ __global__ void __launch_bounds__(128) k_infer_tc(const unsigned short *__restri
             }
             const bool ok = bar_wait(bar, phase);
             phase ^= 1u;
-            if (__syncthreads_or(!ok)) {
+            if (wg_sync_or(wgbar, !ok)) {
                 failed = true;
                 break;
             }
@@ -410,8 +432,8 @@ __global__ void __launch_bounds__(128) k_infer_tc(const unsigned short *__restri
                     hi.y = pack2(fmaxf(v[10], 0.0f), fmaxf(v[11], 0.0f));
                     hi.z = pack2(fmaxf(v[12], 0.0f), fmaxf(v[13], 0.0f));
                     hi.w = pack2(fmaxf(v[14], 0.0f), fmaxf(v[15], 0.0f));
-                    *reinterpret_cast<uint4 *>(A + sw_off(tid, 2 * cb)) = lo;
-                    *reinterpret_cast<uint4 *>(A + sw_off(tid, 2 * cb + 1)) = hi;
+                    *reinterpret_cast<uint4 *>(A + sw_off(r, 2 * cb)) = lo;
+                    *reinterpret_cast<uint4 *>(A + sw_off(r, 2 * cb + 1)) = hi;
                 }
             } else {
                 float v[16];
@@ -433,11 +455,11 @@ __global__ void __launch_bounds__(128) k_infer_tc(const unsigned short *__restri
                 // cache termination: rad[path] += T * max(y, 0)
                 const float *rec = raw + (size_t)q * stride_floats;
                 const int path = __float_as_int(rec[16]);
-                float4 r = rad[path];
-                r.x += rec[13] * fmaxf(y[0], 0.0f);
-                r.y += rec[14] * fmaxf(y[1], 0.0f);
-                r.z += rec[15] * fmaxf(y[2], 0.0f);
-                rad[path] = r;
+                float4 rr = rad[path];
+                rr.x += rec[13] * fmaxf(y[0], 0.0f);
+                rr.y += rec[14] * fmaxf(y[1], 0.0f);
+                rr.z += rec[15] * fmaxf(y[2], 0.0f);
+                rad[path] = rr;
             }
         }
     }
@@ -445,13 +467,15 @@ __global__ void __launch_bounds__(128) k_infer_tc(const unsigned short *__restri
         // the MMAs of the timed-out phase may still be in flight: wait once
         // more (bounded) before the tensor memory is released
         bar_wait(bar, phase ^ 1u);
-        if (tid == 0) atomicExch(err, 1);
+        if (r == 0) atomicExch(err, 1);
     }
     fence_before();
     __syncthreads();
     if (warp == 0) {
         fence_after();
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem - 64u * (uint32_t)g),
+                     "r"(kTmemCols)
+                     : "memory");
     }
 }
 
@@ -810,8 +834,8 @@ kgk_status nrc_check_error(NrcState &N) {
 
 kgk_status nrc_infer_dev(NrcState &N, const float *raw, int stride, int n, const int *n_dev, float *out, float4 *rad,
                          cudaStream_t st) {
-    const int grid = N.sms * 3;  // three ~60 KB CTAs fit an SM; 3 x 64 TMEM columns of 512
-    k_infer_tc<<<grid, 128, tc::kSmemBytes, st>>>(N.img, raw, stride, n, n_dev, out, rad, N.ints + 2);
+    const int grid = N.sms * 2;  // two ~108 KB CTAs of four warpgroups per SM, 2 x 256 TMEM columns of 512
+    k_infer_tc<<<grid, 128 * tc::kGroups, tc::kSmemBytes, st>>>(N.img, raw, stride, n, n_dev, out, rad, N.ints + 2);
     KGK_CUDA(cudaGetLastError());
     return KGK_OK;
 }
