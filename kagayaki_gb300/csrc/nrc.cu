@@ -28,6 +28,13 @@ __device__ __forceinline__ uint32_t pack2(float lo, float hi) {
     __nv_bfloat162 h = __floats2bfloat162_rn(lo, hi);
     return *reinterpret_cast<uint32_t *>(&h);
 }
+// ReLU and BF16 rounding of two values in one conversion (negative values,
+// and only those, become 0; lo in the low half).
+__device__ __forceinline__ uint32_t pack2_relu(float lo, float hi) {
+    uint32_t d;
+    asm("cvt.rn.relu.bf16x2.f32 %0, %1, %2;" : "=r"(d) : "f"(hi), "f"(lo));
+    return d;
+}
 __device__ __forceinline__ uint32_t pack_raw(unsigned short lo, unsigned short hi) {
     return (uint32_t)lo | ((uint32_t)hi << 16);
 }
@@ -424,14 +431,14 @@ __global__ void __launch_bounds__(128 * tc::kGroups) k_infer_tc(const unsigned s
                     tmem_ld16(trow + 16 * cb, v);
                     tmem_wait_ld();
                     uint4 lo, hi;
-                    lo.x = pack2(fmaxf(v[0], 0.0f), fmaxf(v[1], 0.0f));
-                    lo.y = pack2(fmaxf(v[2], 0.0f), fmaxf(v[3], 0.0f));
-                    lo.z = pack2(fmaxf(v[4], 0.0f), fmaxf(v[5], 0.0f));
-                    lo.w = pack2(fmaxf(v[6], 0.0f), fmaxf(v[7], 0.0f));
-                    hi.x = pack2(fmaxf(v[8], 0.0f), fmaxf(v[9], 0.0f));
-                    hi.y = pack2(fmaxf(v[10], 0.0f), fmaxf(v[11], 0.0f));
-                    hi.z = pack2(fmaxf(v[12], 0.0f), fmaxf(v[13], 0.0f));
-                    hi.w = pack2(fmaxf(v[14], 0.0f), fmaxf(v[15], 0.0f));
+                    lo.x = pack2_relu(v[0], v[1]);
+                    lo.y = pack2_relu(v[2], v[3]);
+                    lo.z = pack2_relu(v[4], v[5]);
+                    lo.w = pack2_relu(v[6], v[7]);
+                    hi.x = pack2_relu(v[8], v[9]);
+                    hi.y = pack2_relu(v[10], v[11]);
+                    hi.z = pack2_relu(v[12], v[13]);
+                    hi.w = pack2_relu(v[14], v[15]);
                     *reinterpret_cast<uint4 *>(A + sw_off(r, 2 * cb)) = lo;
                     *reinterpret_cast<uint4 *>(A + sw_off(r, 2 * cb + 1)) = hi;
                 }
