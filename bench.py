@@ -441,61 +441,73 @@ def run_svgf_orbit(args):
 
 
 def run_mlp(args):
-    """The radiance-cache MLP alone (64 -> 5 x 64 -> 3, BF16 in, FP32
-    accumulate): inference of 2^21 queries (tcgen05 kernel) and training
-    steps on 65,536 samples (forward + backward + dW + Adam), device buffers.
-    TFLOP/s over algorithmic FLOPs: 2 x 20,672 per query, 3 x that per
+    """The radiance-cache MLP alone (64 inputs -> 5 hidden layers of width W ->
+    3, BF16 in, FP32 accumulate), at width 64 (the 1080p cache: training
+    batch 65,536) and width 128 (the 4K cache: batch 2^18): inference of 2^21
+    queries (tcgen05 kernel) and training steps (forward + backward + dW +
+    Adam), device buffers.  TFLOP/s over algorithmic FLOPs: 2 x (64 W + 4 W^2
+    + 3 W) per query (20,672 MACs at width 64, 74,112 at 128), 3 x that per
     training sample."""
     import ctypes
     import torch
     from kagayaki_gb300 import Scene, scenes
     from kagayaki_gb300._lib import check, lib
-    tris, mats, _ = scenes.cornell_box()
-    scene = Scene(tris, mats)
-    check(lib().kgk_nrc_init(scene._h, None))
-    g = torch.Generator(device="cpu").manual_seed(1)
-    n = 1 << 21
-    raw = torch.rand((n, 13), generator=g).cuda()
-    out = torch.empty((n, 3), device="cuda")
-    nt = 65536
-    traw = torch.rand((nt, 13), generator=g).cuda()
-    tgt = torch.rand((nt, 3), generator=g).cuda()
-    loss = np.zeros(1, np.float32)  # host: the call returns the last step's loss
-    vp = lambda t: ctypes.c_void_p(t.data_ptr())  # noqa: E731
-
-    def infer():
-        check(lib().kgk_nrc_infer(scene._h, vp(raw), n, vp(out)))
-
-    def train(k):
-        check(lib().kgk_nrc_train(scene._h, vp(traw), vp(tgt), nt, k, ctypes.c_void_p(loss.ctypes.data)))
-
-    for _ in range(args.warmup):
-        infer()
-        train(4)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        infer()
-    ti = (time.perf_counter() - t0) / args.steps
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        train(4)
-    tt = (time.perf_counter() - t0) / args.steps / 4
-    scene.close()
+    from kagayaki_gb300.structs import KgkNrcConfig
     peaks = json.load(open(os.path.join(HERE, "MEASURED_PEAKS.json"))) if os.path.exists(
         os.path.join(HERE, "MEASURED_PEAKS.json")) else {}
     peak = peaks.get("bf16_tflops", 1900.0)
-    fl = 2 * 20672
-    inf_tf = fl * n / ti / 1e12
-    trn_tf = 3 * fl * nt / tt / 1e12
-    line = {"metric": "Mqueries/s", "value": round(n / ti / 1e6, 1), "unit": "Mqueries/s", "n_gpus": 1,
+    vp = lambda t: ctypes.c_void_p(t.data_ptr())  # noqa: E731
+    tris, mats, _ = scenes.cornell_box()
+
+    def measure(width, nt):
+        scene = Scene(tris, mats)
+        cfg = KgkNrcConfig(width=width)
+        check(lib().kgk_nrc_init(scene._h, ctypes.byref(cfg)))
+        g = torch.Generator(device="cpu").manual_seed(1)
+        n = 1 << 21
+        raw = torch.rand((n, 13), generator=g).cuda()
+        out = torch.empty((n, 3), device="cuda")
+        traw = torch.rand((nt, 13), generator=g).cuda()
+        tgt = torch.rand((nt, 3), generator=g).cuda()
+        loss = np.zeros(1, np.float32)  # host: the call returns the last step's loss
+
+        def infer():
+            check(lib().kgk_nrc_infer(scene._h, vp(raw), n, vp(out)))
+
+        def train(k):
+            check(lib().kgk_nrc_train(scene._h, vp(traw), vp(tgt), nt, k, ctypes.c_void_p(loss.ctypes.data)))
+
+        for _ in range(args.warmup):
+            infer()
+            train(4)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            infer()
+        ti = (time.perf_counter() - t0) / args.steps
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            train(4)
+        tt = (time.perf_counter() - t0) / args.steps / 4
+        scene.close()
+        fl = 2 * (64 * width + 4 * width * width + 3 * width)
+        inf_tf = fl * n / ti / 1e12
+        trn_tf = 3 * fl * nt / tt / 1e12
+        return n, ti, {"queries": n, "train_batch": nt, "mqueries_per_s": round(n / ti / 1e6, 1),
+                       "inference": {"tflops": round(inf_tf, 2), "frac_of_bf16_peak": round(inf_tf / peak, 4),
+                                     "kernel": "k_infer_tc (tcgen05)"},
+                       "training_step": {"ms": round(tt * 1e3, 3), "tflops": round(trn_tf, 2),
+                                         "frac_of_bf16_peak": round(trn_tf / peak, 4),
+                                         "kernel": "k_train_fb + k_train_dw (mma.sync)"}}
+
+    n, ti, w64 = measure(64, 65536)
+    _, _, w128 = measure(128, 1 << 18)
+    line = {"metric": "Mqueries/s", "value": w64["mqueries_per_s"], "unit": "Mqueries/s", "n_gpus": 1,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ti * 1e3, 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "bf16 (fp32 accumulate)", "data": "uniform random queries",
-            "config": {"workload": "cache-mlp", "queries": n, "train_batch": nt, "timing": "wall clock per call"},
-            "inference": {"tflops": round(inf_tf, 2), "frac_of_bf16_peak": round(inf_tf / peak, 4),
-                          "kernel": "k_infer_tc (tcgen05)"},
-            "training_step": {"ms": round(tt * 1e3, 3), "tflops": round(trn_tf, 2),
-                              "frac_of_bf16_peak": round(trn_tf / peak, 4), "kernel": "k_train (mma.sync)"}}
+            "config": {"workload": "cache-mlp", "width": 64, "queries": n, "train_batch": w64["train_batch"],
+                       "timing": "wall clock per call"},
+            "inference": w64["inference"], "training_step": w64["training_step"], "width_128": w128}
     print(json.dumps(line), flush=True)
 
 
@@ -503,8 +515,8 @@ def run_c5(args):
     """The scaled config: 10.6 M triangles (128 displaced icospheres on a
     256 x 256-tile terrain), 64 RGBA8 1024^2 textures sampled bilinearly, a
     4096 x 2048 HDR sky, 3840 x 2160 at 1 spp per frame over a 120-frame orbit
-    with the radiance cache (2^18 training paths per frame; the network is the
-    64-wide one), then plain vs cache at equal time and at equal relMSE against
+    with the radiance cache widened to 128 (2^18 training paths per frame),
+    then plain vs cache at equal time and at equal relMSE against
     a 4096-spp FP64-accumulated frame."""
     from kagayaki_gb300 import ESTIMATOR_UNBIASED, Scene, scenes
     W, H = args.width or 3840, args.height or 2160
@@ -522,7 +534,7 @@ def run_c5(args):
     res = {}
     for mode in ("plain", "cache"):
         if mode == "cache":
-            scene.cache_init(train_paths=1 << 18, seed=1)
+            scene.cache_init(width=128, train_paths=1 << 18, seed=1)
         for f in range(3):
             scene.render(cam_of(f), W, H, spp=1, seed=1, frame_index=f, use_cache=mode == "cache", out=out, **kw)
         dev = 0.0
@@ -540,7 +552,7 @@ def run_c5(args):
     for k in range(64):
         scene.render(cam, W, H, spp=64, seed=7, frame_index=900_000 + k, accumulate=True, **kw)
     ref, _, nref = scene.accum_read(W, H)
-    scene.cache_init(train_paths=1 << 18, seed=1)
+    scene.cache_init(width=128, train_paths=1 << 18, seed=1)
     for f in range(32):
         scene.render(cam, W, H, spp=1, seed=5, frame_index=f, use_cache=True, out=out, **kw)
     acc = np.zeros((H, W, 3))
@@ -570,7 +582,7 @@ def run_c5(args):
             "data": "synthetic seeded scene",
             "config": {"workload": "c5-10.6M-4k-1spp-orbit", "triangles": int(len(tris)), "width": W, "height": H,
                        "textures": "64 x 1024^2 RGBA8, bilinear", "env": "4096x2048 float32 sky + sun 1e4",
-                       "cache": "width 64, 2^18 training paths per frame", "scene_generation_s": round(gen_s, 1),
+                       "cache": "width 128, 2^18 training paths per frame", "scene_generation_s": round(gen_s, 1),
                        "bvh_build_ms": round(bvh["ms_build"], 1)},
             "orbit": res,
             "relmse_static": {"reference_spp": int(nref),

@@ -449,7 +449,7 @@ kgk_status kgk_svgf_apply_noalloc(kgk_vec *result, kgk_vec *filtered, kgk_svgf_b
  * Raw query = 13 floats: position normalised to the scene box (3), shading
  * normal (3), direction toward the viewer (3), roughness, albedo (3). */
 typedef struct kgk_nrc_config {
-    int32_t width;              /* hidden width: 64                              */
+    int32_t width;              /* hidden width: 64 (0 = 64) or 128              */
     int32_t hidden_layers;      /* 5                                             */
     float learning_rate;        /* Adam, 1e-2                                    */
     int32_t train_paths;        /* training paths per frame, 65,536              */
@@ -462,14 +462,16 @@ typedef struct kgk_nrc_config {
 
 /* (Re)initialises the scene's cache with He-uniform weights. */
 kgk_status kgk_nrc_init(kgk_scene *scene, const kgk_nrc_config *cfg);
-/* FP32 master weights, layer by layer, each (out, in) row-major: 5 x (64 x 64)
- * then 3 x 64 (20,672 floats). */
+/* FP32 master weights, layer by layer, each (out, in) row-major: W x 64,
+ * 4 x (W x W), then 3 x W for hidden width W (20,672 floats at width 64,
+ * 74,112 at width 128). */
 kgk_status kgk_nrc_set_weights(kgk_scene *scene, const float *w, size_t n);
 kgk_status kgk_nrc_get_weights(kgk_scene *scene, float *w, size_t n);
 /* Predictions (n x 3) for n raw queries (n x 13). */
 kgk_status kgk_nrc_infer(kgk_scene *scene, const float *raw, size_t n, float *out);
 /* Gradient of the mean relative-L2 loss over the batch w.r.t. the weights
- * (20,672 floats, loss scale removed) and the loss; weights unchanged. */
+ * (as many floats as the weights, loss scale removed) and the loss; weights
+ * unchanged. */
 kgk_status kgk_nrc_gradients(kgk_scene *scene, const float *raw, const float *target, size_t n,
                              float *grad, float *loss);
 /* `steps` Adam steps on one batch; loss = the last step's loss. */

@@ -5,13 +5,28 @@
 
 namespace kgk {
 namespace nrc {
-constexpr int kWidth = 64;      // hidden width
-constexpr int kLayers = 5;      // hidden layers
+constexpr int kIn = 64;         // encoded input features
+constexpr int kLayers = 5;      // hidden layers (ReLU): kIn -> W, then 4 x (W -> W)
 constexpr int kRaw = 13;        // raw query floats: p(3, normalised) n(3) v(3) roughness albedo(3)
-constexpr int kPitch = 72;      // BF16 row pitch of the shared-memory weight image
 constexpr int kOutRows = 16;    // output layer rows, padded (3 live)
-constexpr int kImgElems = kLayers * kWidth * kPitch + kOutRows * kPitch;
-constexpr int kParams = kLayers * kWidth * kWidth + 3 * kWidth;  // 20,672
+
+// Sizes of the network of hidden width W (64 or 128).  Master weights, FP32,
+// layer by layer, each (out, in) row-major: W x 64, 4 x (W x W), 3 x W.
+template <int W>
+struct Net {
+    static constexpr int kPitch = W + 8;  // BF16 row pitch of the shared-memory weight image
+    static constexpr int kImg = kLayers * W * kPitch + kOutRows * kPitch;  // image elements
+    static constexpr int kParams = W * kIn + (kLayers - 1) * W * W + 3 * W;
+    // inputs of layer l (l == kLayers: the output layer)
+    __host__ __device__ static constexpr int in(int l) { return l == 0 ? kIn : W; }
+    // offset of layer l in the master weights
+    __host__ __device__ static constexpr int woff(int l) { return l == 0 ? 0 : W * kIn + (l - 1) * W * W; }
+};
+static_assert(Net<64>::kParams == 20672 && Net<128>::kParams == 74112, "network sizes");
+
+inline bool width_ok(int w) { return w == 64 || w == 128; }
+inline int params_of(int w) { return w == 128 ? Net<128>::kParams : Net<64>::kParams; }
+inline int img_elems_of(int w) { return w == 128 ? Net<128>::kImg : Net<64>::kImg; }
 constexpr float kEpsRel = 0.01f;
 constexpr float kInitScale = 128.0f;
 constexpr int kScaleGrowth = 1000;
@@ -21,14 +36,15 @@ struct NrcState {
     kgk_nrc_config cfg{};
     float *w = nullptr, *m = nullptr, *v = nullptr, *g = nullptr;  // FP32 master weights, Adam, gradient
     unsigned short *img = nullptr;   // BF16 weight image (shared-memory layout)
-    unsigned short *trH = nullptr;   // training scratch: activations H_l, [layer][row][64]
-    unsigned short *trD = nullptr;   // training scratch: output gradients dZ_l, [layer][row][64]
+    unsigned short *trH = nullptr;   // training scratch: activations H_l, [layer][row][width]
+    unsigned short *trD = nullptr;   // training scratch: output gradients dZ_l, [layer][row][width]
     int tr_cap = 0;                  // rows the scratch holds
     float *scal = nullptr;           // [0] loss scale, [1] last loss
     int *ints = nullptr;             // [0] non-finite flag, [1] clean steps since the last scale change,
                                      // [2] inference timeout flag
     int step = 0;
     int sms = 0;
+    int params = 0;                  // master weights (20,672 at width 64, 74,112 at 128)
     bool ready = false;
 };
 

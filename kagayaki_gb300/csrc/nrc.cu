@@ -1,18 +1,21 @@
-// nrc.cu - learned radiance cache: a fully fused MLP (64 -> 5 x 64 ReLU -> 3,
-// no biases) in BF16 on the tensor cores with FP32 accumulation.
+// nrc.cu - learned radiance cache: an MLP of hidden width W = 64 or 128
+// (64 inputs -> W, 4 x (W -> W), ReLU after each, -> 3 linear outputs, no
+// biases) in BF16 on the tensor cores with FP32 accumulation.
 //
-// One warp carries 16 samples through every layer with mma.sync m16n8k16:
-// the FP32 accumulator fragment of one layer, rounded to BF16 after the
-// ReLU, is exactly the A-operand fragment of the next layer, so activations
-// stay in registers.  Weights live in shared memory as a BF16 image with a
-// 72-element row pitch (bank-conflict-free fragment loads).
-// Training fuses forward, relative-L2 loss (scaled by a dynamic loss scale),
-// backward and the weight-gradient GEMMs; each CTA accumulates dW in shared
-// memory (FP32) and adds it to the global gradient once.  Adam updates FP32
-// master weights and rewrites the BF16 image.
+// Inference runs on the 5th-generation tensor cores (tcgen05, accumulators in
+// tensor memory).  Training runs on mma.sync m16n8k16: one warp carries 16
+// samples through every layer, and the FP32 accumulator fragment of one
+// layer, rounded to BF16 after the ReLU, is exactly the A-operand fragment of
+// the next layer, so activations stay in registers.  Its weights live in
+// shared memory as a BF16 image with a (W + 8)-element row pitch
+// (bank-conflict-free fragment loads).  Forward, relative-L2 loss (times a
+// dynamic loss scale) and backward run in one kernel, the weight-gradient
+// GEMMs in a second; Adam updates FP32 master weights and rewrites the BF16
+// image.
 // No counterpart in the reference.
 #include <cuda_bf16.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -109,16 +112,17 @@ __device__ __forceinline__ void encode_frags(const float *ra, const float *rb, u
     }
 }
 
-// acc[nt] = A (16 x 64) * W^T (64 x 64) for one hidden layer; W row-major
-// [out][in] in shared memory with pitch kPitch.
-__device__ __forceinline__ void layer_fwd(const unsigned short *W, const uint32_t (&a)[4][4], float (&acc)[8][4]) {
+// acc[nt] = A (16 x 16 KT) * W^T for output rows 8 nt .. 8 nt + 7 of a weight
+// matrix [out][in] in shared memory (BF16, row pitch P).
+template <int P, int KT, int NT>
+__device__ __forceinline__ void layer_fwd(const unsigned short *Wm, const uint32_t (&a)[KT][4], float (&acc)[NT][4]) {
     const int g = (threadIdx.x & 31) >> 2, t = threadIdx.x & 3;
 #pragma unroll
-    for (int nt = 0; nt < 8; ++nt) {
+    for (int nt = 0; nt < NT; ++nt) {
         acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.0f;
-        const unsigned short *row = W + (nt * 8 + g) * kPitch;
+        const unsigned short *row = Wm + (nt * 8 + g) * P;
 #pragma unroll
-        for (int kt = 0; kt < 4; ++kt) {
+        for (int kt = 0; kt < KT; ++kt) {
             const uint32_t b0 = *reinterpret_cast<const uint32_t *>(row + kt * 16 + 2 * t);
             const uint32_t b1 = *reinterpret_cast<const uint32_t *>(row + kt * 16 + 8 + 2 * t);
             mma16816(acc[nt], a[kt], b0, b1);
@@ -126,137 +130,97 @@ __device__ __forceinline__ void layer_fwd(const unsigned short *W, const uint32_
     }
 }
 
-__device__ __forceinline__ void out_fwd(const unsigned short *W, const uint32_t (&a)[4][4], float (&acc)[4]) {
+// C fragments -> BF16 A fragments of the next layer, after the ReLU.  Returns
+// the ReLU derivative as bits: bit 4 nt + i is set when acc[nt][i] > 0.
+template <int NT>
+__device__ __forceinline__ unsigned long long relu_to_frags(const float (&acc)[NT][4], uint32_t (&a)[NT / 2][4]) {
+    static_assert(NT <= 16, "64 mask bits");
+    unsigned long long m = 0;
+#pragma unroll
+    for (int nt = 0; nt < NT; ++nt)
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+            if (acc[nt][i] > 0.0f) m |= 1ull << (4 * nt + i);
+#pragma unroll
+    for (int kt = 0; kt < NT / 2; ++kt) {
+        a[kt][0] = pack2_relu(acc[2 * kt][0], acc[2 * kt][1]);
+        a[kt][1] = pack2_relu(acc[2 * kt][2], acc[2 * kt][3]);
+        a[kt][2] = pack2_relu(acc[2 * kt + 1][0], acc[2 * kt + 1][1]);
+        a[kt][3] = pack2_relu(acc[2 * kt + 1][2], acc[2 * kt + 1][3]);
+    }
+    return m;
+}
+
+// The warp's A fragments (16 rows x 16 KT BF16 columns) as rows base + g and
+// base + g + 8 of a global [row][ld] array.
+template <int KT>
+__device__ __forceinline__ void frags_to_global(const uint32_t (&a)[KT][4], unsigned short *dst, int ld, int base) {
     const int g = (threadIdx.x & 31) >> 2, t = threadIdx.x & 3;
-    acc[0] = acc[1] = acc[2] = acc[3] = 0.0f;
-    const unsigned short *row = W + g * kPitch;
+    unsigned short *r0 = dst + (size_t)(base + g) * ld + 2 * t, *r1 = r0 + (size_t)8 * ld;
 #pragma unroll
-    for (int kt = 0; kt < 4; ++kt) {
-        const uint32_t b0 = *reinterpret_cast<const uint32_t *>(row + kt * 16 + 2 * t);
-        const uint32_t b1 = *reinterpret_cast<const uint32_t *>(row + kt * 16 + 8 + 2 * t);
-        mma16816(acc, a[kt], b0, b1);
+    for (int kt = 0; kt < KT; ++kt) {
+        *reinterpret_cast<uint32_t *>(r0 + kt * 16) = a[kt][0];
+        *reinterpret_cast<uint32_t *>(r1 + kt * 16) = a[kt][1];
+        *reinterpret_cast<uint32_t *>(r0 + kt * 16 + 8) = a[kt][2];
+        *reinterpret_cast<uint32_t *>(r1 + kt * 16 + 8) = a[kt][3];
     }
 }
 
-// C fragments (after ReLU) -> BF16 A fragments of the next layer.
-__device__ __forceinline__ void relu_to_frags(const float (&acc)[8][4], uint32_t (&a)[4][4]) {
-#pragma unroll
-    for (int kt = 0; kt < 4; ++kt) {
-        a[kt][0] = pack2(fmaxf(acc[2 * kt][0], 0.0f), fmaxf(acc[2 * kt][1], 0.0f));
-        a[kt][1] = pack2(fmaxf(acc[2 * kt][2], 0.0f), fmaxf(acc[2 * kt][3], 0.0f));
-        a[kt][2] = pack2(fmaxf(acc[2 * kt + 1][0], 0.0f), fmaxf(acc[2 * kt + 1][1], 0.0f));
-        a[kt][3] = pack2(fmaxf(acc[2 * kt + 1][2], 0.0f), fmaxf(acc[2 * kt + 1][3], 0.0f));
-    }
-}
-
-// Stores A fragments (16 x 64 BF16) into a [16][kPitch] shared tile.
-__device__ __forceinline__ void store_frags(unsigned short *T, const uint32_t (&a)[4][4]) {
-    const int g = (threadIdx.x & 31) >> 2, t = threadIdx.x & 3;
-#pragma unroll
-    for (int kt = 0; kt < 4; ++kt) {
-        const int c = kt * 16 + 2 * t;
-        *reinterpret_cast<uint32_t *>(T + g * kPitch + c) = a[kt][0];
-        *reinterpret_cast<uint32_t *>(T + (g + 8) * kPitch + c) = a[kt][1];
-        *reinterpret_cast<uint32_t *>(T + g * kPitch + c + 8) = a[kt][2];
-        *reinterpret_cast<uint32_t *>(T + (g + 8) * kPitch + c + 8) = a[kt][3];
-    }
-}
-
+template <int W>
 __device__ __forceinline__ void load_image(unsigned short *dst, const unsigned short *src) {
-    const int n16 = kImgElems * 2 / 16;
+    constexpr int n16 = Net<W>::kImg * 2 / 16;
+    static_assert(Net<W>::kImg * 2 % 16 == 0, "16-byte copies");
     const uint4 *s = reinterpret_cast<const uint4 *>(src);
     uint4 *d = reinterpret_cast<uint4 *>(dst);
     for (int i = threadIdx.x; i < n16; i += blockDim.x) d[i] = s[i];
 }
 
 // ---------------------------------------------------------------------------
-// inference
-// ---------------------------------------------------------------------------
-// Query record: raw[13], T[3] (path throughput), path id, pad -> 5 float4.
-__global__ void __launch_bounds__(256) k_infer(const unsigned short *__restrict__ img, const float *__restrict__ raw,
-                                               int stride_floats, int n, const int *n_dev, float *out, float4 *rad) {
-    extern __shared__ __align__(16) unsigned short sW[];
-    load_image(sW, img);
-    __syncthreads();
-    const int total = n_dev ? *n_dev : n;
-    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nwarps = (gridDim.x * blockDim.x) >> 5;
-    for (int base = warp * 16; base < total; base += nwarps * 16) {
-        const int sa = base + g, sb = base + g + 8;
-        float ra[kRaw], rb[kRaw];
-#pragma unroll
-        for (int k = 0; k < kRaw; ++k) {
-            ra[k] = sa < total ? raw[(size_t)sa * stride_floats + k] : 0.0f;
-            rb[k] = sb < total ? raw[(size_t)sb * stride_floats + k] : 0.0f;
-        }
-        uint32_t a[4][4];
-        encode_frags(ra, rb, a);
-        float acc[8][4];
-#pragma unroll 1
-        for (int l = 0; l < kLayers; ++l) {
-            layer_fwd(sW + l * kWidth * kPitch, a, acc);
-            relu_to_frags(acc, a);
-        }
-        float y[4];
-        out_fwd(sW + kLayers * kWidth * kPitch, a, y);
-        // lanes t = 0, 1 hold outputs 0..3 of samples g and g + 8
-        if (t < 2) {
-            const int cols[2] = {2 * t, 2 * t + 1};
-            const int s2[2] = {sa, sb};
-            for (int r = 0; r < 2; ++r) {
-                const int s = s2[r];
-                if (s >= total) continue;
-                for (int k = 0; k < 2; ++k) {
-                    const int c = cols[k];
-                    if (c > 2) continue;
-                    const float v = y[2 * r + k];
-                    if (out) out[(size_t)s * 3 + c] = v;
-                    if (rad) {
-                        // cache termination: rad[path] += T * max(y, 0)
-                        const float *rec = raw + (size_t)s * stride_floats;
-                        const int path = __float_as_int(rec[16]);
-                        const float add = rec[13 + c] * fmaxf(v, 0.0f);
-                        float *rp = reinterpret_cast<float *>(rad + path) + c;
-                        *rp += add;
-                    }
-                }
-            }
-        }
-    }
-}
-
-// ---------------------------------------------------------------------------
 // inference on the 5th-generation tensor cores (tcgen05 + TMEM)
 //
-// A CTA holds the weights once (64 x 64 per layer, BF16, 128-byte-swizzled
-// K-major, in shared memory) for four warpgroups, each carrying its own tiles
-// of 128 queries through the network: thread r of a warpgroup owns row r.
-// Per layer a warpgroup writes the BF16 activations (128 x 64) to its
-// shared-memory tile in the same layout, one elected thread issues four
-// tcgen05.mma (M=128, N=64, K=16 each) into the warpgroup's 128 x 64 FP32
-// accumulator in tensor memory and commits to the warpgroup's mbarrier; the
-// threads then read their row back (tcgen05.ld 32x32b), apply the ReLU and
-// round to BF16 for the next layer.  The warpgroups synchronise on their own
-// named barriers, so the CUDA-core work of one overlaps the MMAs of another.
-// The output layer uses N=16 (3 live rows of the padded weights).
+// A CTA holds the weights once (BF16, 128-byte-swizzled K-major, in shared
+// memory; each layer as K sub-tiles of 64 inputs) for its warpgroups, each
+// carrying its own tiles of 128 queries through the network: thread r of a
+// warpgroup owns row r.  Per layer a warpgroup writes the BF16 activations
+// (128 x W) to its shared-memory tile in the same layout, one elected thread
+// issues the tcgen05.mma (M=128, N=W, K=16 each) into the warpgroup's
+// 128 x W FP32 accumulator in tensor memory and commits to the warpgroup's
+// mbarrier; the threads then read their row back (tcgen05.ld 32x32b) and
+// apply the ReLU and the BF16 rounding for the next layer in one conversion.
+// The warpgroups synchronise on their own named barriers, so the CUDA-core
+// work of one overlaps the MMAs of another.  Width 64: four warpgroups per
+// CTA, two CTAs per SM; width 128: two warpgroups, one CTA per SM (shared
+// memory).  The output layer uses N=16 (3 live rows of the padded weights).
 // Every wait is bounded: on a timeout the CTA raises *err, stops issuing and
 // frees its tensor memory.
 // ---------------------------------------------------------------------------
 namespace tc {
 
-constexpr int kRows = 128;                       // M of every MMA, queries per tile
-constexpr uint32_t kLayerBytes = 64 * 128;       // 64 rows x 128 B (64 BF16)
-constexpr uint32_t kOutBytes = 16 * 128;         // padded output layer
-constexpr uint32_t kWOff = 0;                    // hidden layers at l * kLayerBytes
-constexpr uint32_t kOutOff = kLayers * kLayerBytes;
-constexpr int kGroups = 4;                       // warpgroups per CTA, one tile each at a time
-constexpr uint32_t kAOff = kOutOff + kOutBytes;  // activation tiles, 16 KB each (1024-aligned)
-constexpr uint32_t kATile = kRows * 128;
-constexpr uint32_t kBarOff = kAOff + kGroups * kATile;  // one mbarrier per warpgroup
-constexpr uint32_t kSlotOff = kBarOff + 8 * kGroups;
-constexpr uint32_t kSmemBytes = kSlotOff + 8 + 1024;  // + room to align the base to 1024 B
-constexpr uint32_t kTmemCols = 64 * kGroups;          // a 64-column accumulator per warpgroup
-static_assert(kAOff % 1024 == 0, "swizzle atoms need 1024-byte alignment");
+constexpr int kRows = 128;                  // M of every MMA, queries per tile
+constexpr uint32_t kSub = kRows * 128;      // activation K sub-tile: 128 rows x 64 BF16
+constexpr uint32_t kOutSub = kOutRows * 128;  // output-layer K sub-tile: 16 rows x 64 BF16
+
+template <int W>
+struct Tc {
+    static constexpr int kGroups = W == 64 ? 4 : 2;  // warpgroups per CTA, one tile each at a time
+    static constexpr int kCtasPerSm = W == 64 ? 2 : 1;
+    static constexpr uint32_t kKSubs = W / 64;       // K sub-tiles of a W-input layer
+    static constexpr uint32_t kWSub = (uint32_t)W * 128;  // weight K sub-tile: W rows x 64 BF16
+    // layer l's weights: in(l) / 64 sub-tiles (layer 0: one)
+    __host__ __device__ static constexpr uint32_t layer_off(int l) {
+        return l == 0 ? 0u : kWSub + (uint32_t)(l - 1) * kKSubs * kWSub;
+    }
+    static constexpr uint32_t kOutOff = layer_off(kLayers);
+    static constexpr uint32_t kAOff = kOutOff + kKSubs * kOutSub;  // activation tiles (1024-aligned)
+    static constexpr uint32_t kATile = kKSubs * kSub;
+    static constexpr uint32_t kBarOff = kAOff + kGroups * kATile;   // one mbarrier per warpgroup
+    static constexpr uint32_t kSlotOff = kBarOff + 8 * kGroups;
+    static constexpr uint32_t kSmemBytes = kSlotOff + 8 + 1024;     // + room to align the base to 1024 B
+    static constexpr uint32_t kTmemCols = (uint32_t)W * kGroups;    // a W-column accumulator per warpgroup
+    static_assert(kAOff % 1024 == 0, "swizzle atoms need 1024-byte alignment");
+    static_assert(kSmemBytes <= 227 * 1024, "shared memory per CTA");
+    static_assert(kTmemCols * kCtasPerSm <= 512, "tensor memory per SM");
+};
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -339,11 +303,14 @@ __device__ __forceinline__ bool wg_sync_or(int id, bool v) {
     return r != 0;
 }
 
-__global__ void __launch_bounds__(128 * tc::kGroups) k_infer_tc(const unsigned short *__restrict__ img,
-                                                                const float *__restrict__ raw, int stride_floats,
-                                                                int n, const int *n_dev, float *out, float4 *rad,
-                                                                int *err) {
+template <int W>
+__global__ void __launch_bounds__(128 * tc::Tc<W>::kGroups) k_infer_tc(const unsigned short *__restrict__ img,
+                                                                       const float *__restrict__ raw,
+                                                                       int stride_floats, int n, const int *n_dev,
+                                                                       float *out, float4 *rad, int *err) {
     using namespace tc;
+    using T = Tc<W>;
+    constexpr int kG = T::kGroups, P = Net<W>::kPitch;
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     const uint32_t pad = (1024u - (smem_u32(smem_raw) & 1023u)) & 1023u;
     unsigned char *sm = smem_raw + pad;
@@ -351,23 +318,28 @@ __global__ void __launch_bounds__(128 * tc::kGroups) k_infer_tc(const unsigned s
     const int tid = threadIdx.x, warp = tid >> 5;
     const int g = tid >> 7, r = tid & 127;  // warpgroup, row
     const int wgbar = 1 + g;                // its named barrier
-    // weights: BF16 image rows (pitch kPitch) -> swizzled K-major tiles
-    for (int i = tid; i < (kLayers * 64 + 16) * 8; i += blockDim.x) {
-        const int row = i >> 3, c = i & 7;  // row over all layers (64 per hidden layer, then 16)
-        const uint4 v = *reinterpret_cast<const uint4 *>(img + (size_t)row * kPitch + c * 8);
+    // weights: BF16 image rows (pitch P) -> swizzled K-major sub-tiles
+    constexpr int kChunks = W / 8;  // 16-byte chunks of a W-input row
+    for (int i = tid; i < (kLayers * W + kOutRows) * kChunks; i += blockDim.x) {
+        const int row = i / kChunks, c = i % kChunks;
         uint32_t dst;
-        if (row < kLayers * 64) dst = kWOff + (uint32_t)(row >> 6) * kLayerBytes + sw_off(row & 63, c);
-        else dst = kOutOff + sw_off(row - kLayers * 64, c);
-        *reinterpret_cast<uint4 *>(sm + dst) = v;
+        if (row < kLayers * W) {
+            const int l = row / W;
+            if (c >= Net<W>::in(l) / 8) continue;
+            dst = T::layer_off(l) + (uint32_t)(c >> 3) * T::kWSub + sw_off(row % W, c & 7);
+        } else {
+            dst = T::kOutOff + (uint32_t)(c >> 3) * kOutSub + sw_off(row - kLayers * W, c & 7);
+        }
+        *reinterpret_cast<uint4 *>(sm + dst) = *reinterpret_cast<const uint4 *>(img + (size_t)row * P + c * 8);
     }
-    const uint32_t bar = s0 + kBarOff + 8u * (uint32_t)g;
+    const uint32_t bar = s0 + T::kBarOff + 8u * (uint32_t)g;
     if (r == 0) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 0) {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(s0 + kSlotOff),
-                     "r"(kTmemCols)
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(s0 + T::kSlotOff),
+                     "r"(T::kTmemCols)
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
@@ -375,17 +347,17 @@ __global__ void __launch_bounds__(128 * tc::kGroups) k_infer_tc(const unsigned s
     fence_before();
     __syncthreads();
     fence_after();
-    const uint32_t tmem = *reinterpret_cast<volatile uint32_t *>(sm + kSlotOff) + 64u * (uint32_t)g;
+    const uint32_t tmem = *reinterpret_cast<volatile uint32_t *>(sm + T::kSlotOff) + (uint32_t)W * (uint32_t)g;
     const uint32_t trow = tmem + ((uint32_t)((warp & 3) * 32) << 16);  // this warp's 32 TMEM lanes
     const int total = n_dev ? min(*n_dev, n) : n;
     uint32_t phase = 0;
     bool failed = false;
-    unsigned char *A = sm + kAOff + (uint32_t)g * kATile;
-    const uint32_t a_addr = s0 + kAOff + (uint32_t)g * kATile;
-    for (int tile = blockIdx.x * kGroups + g; tile * kRows < total; tile += gridDim.x * kGroups) {
+    unsigned char *A = sm + T::kAOff + (uint32_t)g * T::kATile;
+    const uint32_t a_addr = s0 + T::kAOff + (uint32_t)g * T::kATile;
+    for (int tile = blockIdx.x * kG + g; tile * kRows < total; tile += gridDim.x * kG) {
         const int q = tile * kRows + r;
         const bool live = q < total;
-        // input encoding of row r
+        // input encoding of row r (the first K sub-tile)
         {
             float rw[kRaw];
 #pragma unroll
@@ -410,11 +382,15 @@ __global__ void __launch_bounds__(128 * tc::kGroups) k_infer_tc(const unsigned s
             wg_sync(wgbar);
             if (r == 0) {
                 fence_after();
-                const uint64_t ad = sw128_desc(a_addr);
-                const uint64_t bd = sw128_desc(s0 + (last ? kOutOff : kWOff + (uint32_t)l * kLayerBytes));
-                const uint32_t id = last ? idesc_bf16(128, 16) : idesc_bf16(128, 64);
-#pragma unroll
-                for (int kk = 0; kk < 4; ++kk) mma_bf16(tmem, ad + 2 * kk, bd + 2 * kk, id, kk > 0 ? 1u : 0u);
+                const int nk = Net<W>::in(l) / 16;
+                const uint32_t boff = last ? T::kOutOff : T::layer_off(l);
+                const uint32_t bsub = last ? kOutSub : T::kWSub;
+                const uint32_t id = last ? idesc_bf16(128, 16) : idesc_bf16(128, W);
+                for (int kk = 0; kk < nk; ++kk) {
+                    const uint32_t j = (uint32_t)kk >> 2, o = 2u * (uint32_t)(kk & 3);  // sub-tile, 32 B steps
+                    mma_bf16(tmem, sw128_desc(a_addr + j * kSub) + o, sw128_desc(s0 + boff + j * bsub) + o, id,
+                             kk > 0 ? 1u : 0u);
+                }
                 commit(bar);
             }
             const bool ok = bar_wait(bar, phase);
@@ -426,7 +402,7 @@ __global__ void __launch_bounds__(128 * tc::kGroups) k_infer_tc(const unsigned s
             fence_after();
             if (!last) {
 #pragma unroll
-                for (int cb = 0; cb < 4; ++cb) {  // 16 columns = two 16-byte chunks of BF16
+                for (int cb = 0; cb < W / 16; ++cb) {  // 16 columns = two 16-byte chunks of BF16
                     float v[16];
                     tmem_ld16(trow + 16 * cb, v);
                     tmem_wait_ld();
@@ -439,8 +415,9 @@ __global__ void __launch_bounds__(128 * tc::kGroups) k_infer_tc(const unsigned s
                     hi.y = pack2_relu(v[10], v[11]);
                     hi.z = pack2_relu(v[12], v[13]);
                     hi.w = pack2_relu(v[14], v[15]);
-                    *reinterpret_cast<uint4 *>(A + sw_off(r, 2 * cb)) = lo;
-                    *reinterpret_cast<uint4 *>(A + sw_off(r, 2 * cb + 1)) = hi;
+                    unsigned char *At = A + (uint32_t)(cb >> 2) * kSub;
+                    *reinterpret_cast<uint4 *>(At + sw_off(r, (2 * cb) & 7)) = lo;
+                    *reinterpret_cast<uint4 *>(At + sw_off(r, (2 * cb + 1) & 7)) = hi;
                 }
             } else {
                 float v[16];
@@ -480,8 +457,8 @@ __global__ void __launch_bounds__(128 * tc::kGroups) k_infer_tc(const unsigned s
     __syncthreads();
     if (warp == 0) {
         fence_after();
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem - 64u * (uint32_t)g),
-                     "r"(kTmemCols)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem - (uint32_t)W * (uint32_t)g),
+                     "r"(T::kTmemCols)
                      : "memory");
     }
 }
@@ -489,37 +466,36 @@ __global__ void __launch_bounds__(128 * tc::kGroups) k_infer_tc(const unsigned s
 // ---------------------------------------------------------------------------
 // training, split form: k_train_fb runs forward, loss and backward for tiles
 // of 16 samples per warp and stores every layer's input activations H_l and
-// output gradients dZ_l (BF16 rows of 64) to global scratch; k_train_dw then
-// forms dW_l = dZ_l^T H_l over the batch as a split-K GEMM (each CTA a chunk
-// of samples, accumulating in registers, one atomic add per element per CTA).
-// Layer 5 is the output layer (dZ_5 has 3 live columns of 64).
+// output gradients dZ_l (BF16 rows of W, H_0 with 64 live columns) to global
+// scratch; k_train_dw then forms dW_l = dZ_l^T H_l over the batch as a
+// split-K GEMM (each CTA a chunk of samples, accumulating in registers, one
+// atomic add per element per CTA).  Layer 5 is the output layer (dZ_5 has 3
+// live columns).  The ReLU derivatives of the forward pass stay on chip as
+// one 64-bit mask per lane and layer.
 // ---------------------------------------------------------------------------
-constexpr int kFbWarps = 4;
-constexpr size_t kFbPerWarp = (size_t)(kLayers + 1) * 16 * kPitch * 2;  // H_0..H_5 tiles
-constexpr size_t kFbSmem = (((size_t)kImgElems * 2 + 15) & ~(size_t)15) + kFbPerWarp * kFbWarps;
+constexpr int kMaskBytes = kLayers * 32 * 8;  // per warp
 
-// Copies a warp's [16][kPitch] BF16 tile (64 live columns) to global rows
-// dst[row * 64 + c], rows base..base+15 (16-byte stores).
-__device__ __forceinline__ void tile_to_global(const unsigned short *T, unsigned short *dst, int base) {
-    const int lane = threadIdx.x & 31;
-    for (int i = lane; i < 16 * 8; i += 32) {
-        const int r = i >> 3, c = i & 7;
-        const uint4 v = *reinterpret_cast<const uint4 *>(T + r * kPitch + c * 8);
-        *reinterpret_cast<uint4 *>(dst + (size_t)(base + r) * kWidth + c * 8) = v;
-    }
-}
+template <int W>
+struct Fb {
+    static constexpr int kWarps = W == 64 ? 4 : 8;
+    static constexpr int kCtasPerSm = W == 64 ? 2 : 1;
+    static constexpr size_t kImgBytes = ((size_t)Net<W>::kImg * 2 + 15) & ~(size_t)15;
+    static constexpr size_t kSmem = kImgBytes + (size_t)kMaskBytes * kWarps;
+    static_assert(kSmem * kCtasPerSm <= 227 * 1024, "shared memory per SM");
+};
 
-__global__ void __launch_bounds__(128) k_train_fb(const unsigned short *__restrict__ img, const float *__restrict__ raw,
-                                                  int raw_stride, const float *__restrict__ target, int tgt_stride,
-                                                  int n, const int *n_dev, const float *scale_p,
-                                                  unsigned short *Hs, unsigned short *Ds, size_t layer_stride,
-                                                  float *loss_sum) {
+template <int W>
+__global__ void __launch_bounds__(32 * Fb<W>::kWarps) k_train_fb(
+    const unsigned short *__restrict__ img, const float *__restrict__ raw, int raw_stride,
+    const float *__restrict__ target, int tgt_stride, int n, const int *n_dev, const float *scale_p,
+    unsigned short *Hs, unsigned short *Ds, size_t layer_stride, float *loss_sum) {
+    constexpr int P = Net<W>::kPitch, NT = W / 8, KT = W / 16;
     extern __shared__ __align__(16) unsigned char smem[];
     unsigned short *sW = reinterpret_cast<unsigned short *>(smem);
     const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3, wid = threadIdx.x >> 5;
-    unsigned short *acts = reinterpret_cast<unsigned short *>(smem + (((size_t)kImgElems * 2 + 15) & ~(size_t)15) +
-                                                              kFbPerWarp * wid);
-    load_image(sW, img);
+    unsigned long long *msk =
+        reinterpret_cast<unsigned long long *>(smem + Fb<W>::kImgBytes + (size_t)kMaskBytes * wid) + lane;
+    load_image<W>(sW, img);
     __syncthreads();
     const int total = n_dev ? min(*n_dev, n) : n;
     const int padded = (total + 15) & ~15;
@@ -529,26 +505,31 @@ __global__ void __launch_bounds__(128) k_train_fb(const unsigned short *__restri
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nwarps = (gridDim.x * blockDim.x) >> 5;
     for (int base = warp * 16; base < padded; base += nwarps * 16) {
         const int sa = base + g, sb = base + g + 8;
-        float ra[kRaw], rb[kRaw];
+        float acc[NT][4];
+        uint32_t a[KT][4];
+        {
+            float ra[kRaw], rb[kRaw];
 #pragma unroll
-        for (int k = 0; k < kRaw; ++k) {
-            ra[k] = sa < total ? raw[(size_t)sa * raw_stride + k] : 0.0f;
-            rb[k] = sb < total ? raw[(size_t)sb * raw_stride + k] : 0.0f;
+            for (int k = 0; k < kRaw; ++k) {
+                ra[k] = sa < total ? raw[(size_t)sa * raw_stride + k] : 0.0f;
+                rb[k] = sb < total ? raw[(size_t)sb * raw_stride + k] : 0.0f;
+            }
+            uint32_t a0[4][4];
+            encode_frags(ra, rb, a0);
+            frags_to_global<4>(a0, Hs, W, base);  // H_0: the 64 input columns
+            layer_fwd<P, 4, NT>(sW, a0, acc);
         }
-        uint32_t a[4][4];
-        encode_frags(ra, rb, a);
-        store_frags(acts, a);
-        float acc[8][4];
+        msk[0] = relu_to_frags<NT>(acc, a);
+        frags_to_global<KT>(a, Hs + layer_stride, W, base);
 #pragma unroll 1
-        for (int l = 0; l < kLayers; ++l) {
-            layer_fwd(sW + l * kWidth * kPitch, a, acc);
-            relu_to_frags(acc, a);
-            store_frags(acts + (l + 1) * 16 * kPitch, a);
+        for (int l = 1; l < kLayers; ++l) {
+            layer_fwd<P, KT, NT>(sW + l * W * P, a, acc);
+            msk[32 * l] = relu_to_frags<NT>(acc, a);
+            frags_to_global<KT>(a, Hs + (size_t)(l + 1) * layer_stride, W, base);
         }
-        float y[4];
-        out_fwd(sW + kLayers * kWidth * kPitch, a, y);
-        __syncwarp();
-        for (int l = 0; l <= kLayers; ++l) tile_to_global(acts + l * 16 * kPitch, Hs + l * layer_stride, base);
+        float y1[1][4];
+        layer_fwd<P, KT, 1>(sW + kLayers * W * P, a, y1);
+        const float *y = y1[0];
         // relative L2: d/dy (y - t)^2 / (y^2 + eps), denominator held constant
         float dy[4] = {0.0f, 0.0f, 0.0f, 0.0f};
 #pragma unroll
@@ -566,77 +547,68 @@ __global__ void __launch_bounds__(128) k_train_fb(const unsigned short *__restri
                 dy[2 * r + k] = 2.0f * d / den * inv_n * S;
             }
         }
-        // dZ of the output layer: columns 0..3 of the rows (3 live)
+        // dZ of the output layer: columns 0..7 of the rows (3 live); columns
+        // 8.. stay zero (cleared when the scratch is allocated)
         {
             unsigned short *drow = Ds + (size_t)kLayers * layer_stride;
-            const uint32_t d0 = pack2(dy[0], dy[1]), d1 = pack2(dy[2], dy[3]);
-            if (t < 2) {
-                *reinterpret_cast<uint32_t *>(drow + (size_t)sa * kWidth + 2 * t) = d0;
-                *reinterpret_cast<uint32_t *>(drow + (size_t)sb * kWidth + 2 * t) = d1;
-            } else {
-                *reinterpret_cast<uint32_t *>(drow + (size_t)sa * kWidth + 2 * t) = 0u;
-                *reinterpret_cast<uint32_t *>(drow + (size_t)sb * kWidth + 2 * t) = 0u;
-            }
-            // columns 8..63 of the output-layer rows stay zero (written once per call)
+            const uint32_t d0 = t < 2 ? pack2(dy[0], dy[1]) : 0u, d1 = t < 2 ? pack2(dy[2], dy[3]) : 0u;
+            *reinterpret_cast<uint32_t *>(drow + (size_t)sa * W + 2 * t) = d0;
+            *reinterpret_cast<uint32_t *>(drow + (size_t)sb * W + 2 * t) = d1;
         }
-        // dA_4 = dZ_out (16 x 16, cols >= 8 zero) * W_out (16 x 64)
-        uint32_t dza[4];
-        dza[0] = pack2(dy[0], dy[1]);
-        dza[1] = pack2(dy[2], dy[3]);
-        dza[2] = 0u;
-        dza[3] = 0u;
+        // dA_4 = dZ_out (16 x 16, columns >= 8 zero) * W_out (16 x W)
         {
-            const unsigned short *Wo = sW + kLayers * kWidth * kPitch;
+            uint32_t dza[4];
+            dza[0] = pack2(dy[0], dy[1]);
+            dza[1] = pack2(dy[2], dy[3]);
+            dza[2] = 0u;
+            dza[3] = 0u;
+            const unsigned short *Wo = sW + kLayers * W * P;
 #pragma unroll
-            for (int nt = 0; nt < 8; ++nt) {
+            for (int nt = 0; nt < NT; ++nt) {
                 acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.0f;
                 const int i = nt * 8 + g;
-                const uint32_t b0 = pack_raw(Wo[(2 * t) * kPitch + i], Wo[(2 * t + 1) * kPitch + i]);
-                const uint32_t b1 = pack_raw(Wo[(2 * t + 8) * kPitch + i], Wo[(2 * t + 9) * kPitch + i]);
+                const uint32_t b0 = pack_raw(Wo[(2 * t) * P + i], Wo[(2 * t + 1) * P + i]);
+                const uint32_t b1 = pack_raw(Wo[(2 * t + 8) * P + i], Wo[(2 * t + 9) * P + i]);
                 mma16816(acc[nt], dza, b0, b1);
             }
         }
 #pragma unroll 1
         for (int l = kLayers - 1; l >= 0; --l) {
-            // dZ_l = dA_l * relu'(h_l); h_l is activation l + 1 in `acts`
-            const unsigned short *Hl = acts + (l + 1) * 16 * kPitch;
+            // dZ_l = dA_l * relu'(z_l)
+            const unsigned long long m = msk[32 * l];
 #pragma unroll
-            for (int nt = 0; nt < 8; ++nt) {
-                const int c = nt * 8 + 2 * t;
-                if (bf2f(Hl[g * kPitch + c]) <= 0.0f) acc[nt][0] = 0.0f;
-                if (bf2f(Hl[g * kPitch + c + 1]) <= 0.0f) acc[nt][1] = 0.0f;
-                if (bf2f(Hl[(g + 8) * kPitch + c]) <= 0.0f) acc[nt][2] = 0.0f;
-                if (bf2f(Hl[(g + 8) * kPitch + c + 1]) <= 0.0f) acc[nt][3] = 0.0f;
-            }
+            for (int nt = 0; nt < NT; ++nt)
+#pragma unroll
+                for (int i = 0; i < 4; ++i)
+                    if (!((m >> (4 * nt + i)) & 1ull)) acc[nt][i] = 0.0f;
             // dZ_l rows to global (BF16)
             unsigned short *drow = Ds + (size_t)l * layer_stride;
 #pragma unroll
-            for (int nt = 0; nt < 8; ++nt) {
+            for (int nt = 0; nt < NT; ++nt) {
                 const int c = nt * 8 + 2 * t;
-                *reinterpret_cast<uint32_t *>(drow + (size_t)sa * kWidth + c) = pack2(acc[nt][0], acc[nt][1]);
-                *reinterpret_cast<uint32_t *>(drow + (size_t)sb * kWidth + c) = pack2(acc[nt][2], acc[nt][3]);
+                *reinterpret_cast<uint32_t *>(drow + (size_t)sa * W + c) = pack2(acc[nt][0], acc[nt][1]);
+                *reinterpret_cast<uint32_t *>(drow + (size_t)sb * W + c) = pack2(acc[nt][2], acc[nt][3]);
             }
             if (l == 0) break;
-            // dA_{l-1} = dZ_l (16 x 64) * W_l (64 x 64)
-            uint32_t da[4][4];
+            // dA_{l-1} = dZ_l (16 x W) * W_l (W x W)
 #pragma unroll
-            for (int kt = 0; kt < 4; ++kt) {
-                da[kt][0] = pack2(acc[2 * kt][0], acc[2 * kt][1]);
-                da[kt][1] = pack2(acc[2 * kt][2], acc[2 * kt][3]);
-                da[kt][2] = pack2(acc[2 * kt + 1][0], acc[2 * kt + 1][1]);
-                da[kt][3] = pack2(acc[2 * kt + 1][2], acc[2 * kt + 1][3]);
+            for (int kt = 0; kt < KT; ++kt) {
+                a[kt][0] = pack2(acc[2 * kt][0], acc[2 * kt][1]);
+                a[kt][1] = pack2(acc[2 * kt][2], acc[2 * kt][3]);
+                a[kt][2] = pack2(acc[2 * kt + 1][0], acc[2 * kt + 1][1]);
+                a[kt][3] = pack2(acc[2 * kt + 1][2], acc[2 * kt + 1][3]);
             }
-            const unsigned short *Wl = sW + l * kWidth * kPitch;
+            const unsigned short *Wl = sW + l * W * P;
 #pragma unroll
-            for (int nt = 0; nt < 8; ++nt) {
+            for (int nt = 0; nt < NT; ++nt) {
                 acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.0f;
                 const int i = nt * 8 + g;
 #pragma unroll
-                for (int kt = 0; kt < 4; ++kt) {
+                for (int kt = 0; kt < KT; ++kt) {
                     const int o = kt * 16 + 2 * t;
-                    const uint32_t b0 = pack_raw(Wl[o * kPitch + i], Wl[(o + 1) * kPitch + i]);
-                    const uint32_t b1 = pack_raw(Wl[(o + 8) * kPitch + i], Wl[(o + 9) * kPitch + i]);
-                    mma16816(acc[nt], da[kt], b0, b1);
+                    const uint32_t b0 = pack_raw(Wl[o * P + i], Wl[(o + 1) * P + i]);
+                    const uint32_t b1 = pack_raw(Wl[(o + 8) * P + i], Wl[(o + 9) * P + i]);
+                    mma16816(acc[nt], a[kt], b0, b1);
                 }
             }
         }
@@ -647,80 +619,94 @@ __global__ void __launch_bounds__(128) k_train_fb(const unsigned short *__restri
     if (lane == 0 && loss_sum) atomicAdd(loss_sum, lsum * inv_n);
 }
 
-// dW_l[o][i] += sum over a chunk of samples of dZ_l[s][o] * H_l[s][i].
-// blockIdx.y = layer (0..4 hidden, 5 output); blockIdx.x = sample chunk.
-// Warp w owns output rows 16w..16w+15 (the output layer only warp 0).
-constexpr int kDwChunk = 1024;
-__global__ void __launch_bounds__(128) k_train_dw(const unsigned short *__restrict__ Hs,
-                                                  const unsigned short *__restrict__ Ds, size_t layer_stride, int n,
-                                                  const int *n_dev, float *dW_glob) {
-    __shared__ __align__(16) unsigned short sD[16 * kPitch], sH[16 * kPitch];
-    const int l = blockIdx.y;
+// dW_l[o][i] += sum over the samples s0..s1-1 of dZ_l[s][o] * H_l[s][i] for
+// the layer's IN = 8 NT inputs.  Warp w owns output rows 16w..16w+15 (the
+// output layer only warp 0).
+template <int W, int NT>
+__device__ __forceinline__ void dw_chunk(const unsigned short *D, const unsigned short *H, int s0, int s1, int l,
+                                        float *dW, unsigned short *sD, unsigned short *sH) {
+    constexpr int P = Net<W>::kPitch, IN = NT * 8;
     const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3, wid = threadIdx.x >> 5;
-    const int total = n_dev ? min(*n_dev, n) : n;
-    const int padded = (total + 15) & ~15;
-    const int s0 = blockIdx.x * kDwChunk, s1 = min(s0 + kDwChunk, padded);
-    if (s0 >= s1) return;
-    const unsigned short *D = Ds + (size_t)l * layer_stride, *Hl = Hs + (size_t)l * layer_stride;
     const bool active = l < kLayers || wid == 0;
-    float acc[8][4];
+    float acc[NT][4];
 #pragma unroll
-    for (int nt = 0; nt < 8; ++nt) acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.0f;
+    for (int nt = 0; nt < NT; ++nt) acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.0f;
     for (int sb = s0; sb < s1; sb += 16) {
         __syncthreads();
         {
-            const int r = threadIdx.x >> 3, c = threadIdx.x & 7;  // 128 threads = 16 rows x 8 chunks
-            *reinterpret_cast<uint4 *>(sD + r * kPitch + c * 8) =
-                *reinterpret_cast<const uint4 *>(D + (size_t)(sb + r) * kWidth + c * 8);
-            *reinterpret_cast<uint4 *>(sH + r * kPitch + c * 8) =
-                *reinterpret_cast<const uint4 *>(Hl + (size_t)(sb + r) * kWidth + c * 8);
+            const int r = threadIdx.x / (W / 8), c = threadIdx.x % (W / 8);  // 16 rows x W/8 chunks
+            *reinterpret_cast<uint4 *>(sD + r * P + c * 8) =
+                *reinterpret_cast<const uint4 *>(D + (size_t)(sb + r) * W + c * 8);
+            if (c < IN / 8)
+                *reinterpret_cast<uint4 *>(sH + r * P + c * 8) =
+                    *reinterpret_cast<const uint4 *>(H + (size_t)(sb + r) * W + c * 8);
         }
         __syncthreads();
         if (!active) continue;
-        // A = dZ^T rows o (16 of them) x 16 samples; B = H samples x 64 inputs
+        // A = dZ^T rows o (16 of them) x 16 samples; B = H samples x IN inputs
         uint32_t a[4];
         const int o0 = wid * 16 + g, o1 = o0 + 8;
-        a[0] = pack_raw(sD[(2 * t) * kPitch + o0], sD[(2 * t + 1) * kPitch + o0]);
-        a[1] = pack_raw(sD[(2 * t) * kPitch + o1], sD[(2 * t + 1) * kPitch + o1]);
-        a[2] = pack_raw(sD[(2 * t + 8) * kPitch + o0], sD[(2 * t + 9) * kPitch + o0]);
-        a[3] = pack_raw(sD[(2 * t + 8) * kPitch + o1], sD[(2 * t + 9) * kPitch + o1]);
+        a[0] = pack_raw(sD[(2 * t) * P + o0], sD[(2 * t + 1) * P + o0]);
+        a[1] = pack_raw(sD[(2 * t) * P + o1], sD[(2 * t + 1) * P + o1]);
+        a[2] = pack_raw(sD[(2 * t + 8) * P + o0], sD[(2 * t + 9) * P + o0]);
+        a[3] = pack_raw(sD[(2 * t + 8) * P + o1], sD[(2 * t + 9) * P + o1]);
 #pragma unroll
-        for (int nt = 0; nt < 8; ++nt) {
+        for (int nt = 0; nt < NT; ++nt) {
             const int i = nt * 8 + g;
-            const uint32_t b0 = pack_raw(sH[(2 * t) * kPitch + i], sH[(2 * t + 1) * kPitch + i]);
-            const uint32_t b1 = pack_raw(sH[(2 * t + 8) * kPitch + i], sH[(2 * t + 9) * kPitch + i]);
+            const uint32_t b0 = pack_raw(sH[(2 * t) * P + i], sH[(2 * t + 1) * P + i]);
+            const uint32_t b1 = pack_raw(sH[(2 * t + 8) * P + i], sH[(2 * t + 9) * P + i]);
             mma16816(acc[nt], a, b0, b1);
         }
     }
     if (!active) return;
     const int o0 = wid * 16 + g, o1 = o0 + 8;
-    const int rows = l < kLayers ? kWidth : 3;
-    float *dW = dW_glob + (size_t)l * kWidth * kWidth;
+    const int rows = l < kLayers ? W : 3;
 #pragma unroll
-    for (int nt = 0; nt < 8; ++nt) {
+    for (int nt = 0; nt < NT; ++nt) {
         const int col = nt * 8 + 2 * t;
         if (o0 < rows) {
-            atomicAdd(&dW[o0 * kWidth + col], acc[nt][0]);
-            atomicAdd(&dW[o0 * kWidth + col + 1], acc[nt][1]);
+            atomicAdd(&dW[o0 * IN + col], acc[nt][0]);
+            atomicAdd(&dW[o0 * IN + col + 1], acc[nt][1]);
         }
         if (o1 < rows) {
-            atomicAdd(&dW[o1 * kWidth + col], acc[nt][2]);
-            atomicAdd(&dW[o1 * kWidth + col + 1], acc[nt][3]);
+            atomicAdd(&dW[o1 * IN + col], acc[nt][2]);
+            atomicAdd(&dW[o1 * IN + col + 1], acc[nt][3]);
         }
     }
 }
 
-// Master weights [l][out][in] -> padded BF16 image.
+// blockIdx.y = layer (0..4 hidden, 5 output); blockIdx.x = sample chunk of
+// `chunk` (a multiple of 16) samples.
+template <int W>
+__global__ void __launch_bounds__(2 * W) k_train_dw(const unsigned short *__restrict__ Hs,
+                                                    const unsigned short *__restrict__ Ds, size_t layer_stride,
+                                                    int n, const int *n_dev, int chunk, float *dW_glob) {
+    __shared__ __align__(16) unsigned short sD[16 * Net<W>::kPitch], sH[16 * Net<W>::kPitch];
+    const int l = blockIdx.y;
+    const int total = n_dev ? min(*n_dev, n) : n;
+    const int padded = (total + 15) & ~15;
+    const int s0 = blockIdx.x * chunk, s1 = min(s0 + chunk, padded);
+    if (s0 >= s1) return;
+    const unsigned short *D = Ds + (size_t)l * layer_stride, *H = Hs + (size_t)l * layer_stride;
+    float *dW = dW_glob + Net<W>::woff(l);
+    if (l == 0) dw_chunk<W, kIn / 8>(D, H, s0, s1, l, dW, sD, sH);
+    else dw_chunk<W, W / 8>(D, H, s0, s1, l, dW, sD, sH);
+}
+
+// Master weights -> padded BF16 image: row r of layer l at (l W + r) P, the
+// output layer's 16 rows (3 live) after the hidden layers.
+template <int W>
 __global__ void k_make_image(const float *w, unsigned short *img) {
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < kImgElems; i += gridDim.x * blockDim.x) {
+    constexpr int P = Net<W>::kPitch;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < Net<W>::kImg; i += gridDim.x * blockDim.x) {
+        const int row = i / P, c = i % P;
         float v = 0.0f;
-        const int hid = kLayers * kWidth * kPitch;
-        if (i < hid) {
-            const int l = i / (kWidth * kPitch), r = (i / kPitch) % kWidth, c = i % kPitch;
-            if (c < kWidth) v = w[(size_t)l * kWidth * kWidth + r * kWidth + c];
+        if (row < kLayers * W) {
+            const int l = row / W, r = row % W, in = Net<W>::in(l);
+            if (c < in) v = w[Net<W>::woff(l) + r * in + c];
         } else {
-            const int j = i - hid, r = j / kPitch, c = j % kPitch;
-            if (r < 3 && c < kWidth) v = w[(size_t)kLayers * kWidth * kWidth + r * kWidth + c];
+            const int r = row - kLayers * W;
+            if (r < 3 && c < W) v = w[Net<W>::woff(kLayers) + r * W + c];
         }
         __nv_bfloat16 b = __float2bfloat16_rn(v);
         img[i] = *reinterpret_cast<unsigned short *>(&b);
@@ -772,45 +758,84 @@ __global__ void k_unscale(const float *g, int n, const float *scale_p, float *ou
 // ---------------------------------------------------------------------------
 using namespace nrc;
 
+namespace {
+// BF16 image of the master weights, on stream st
+void make_image(NrcState &N, cudaStream_t st) {
+    if (N.cfg.width == 128) k_make_image<128><<<64, 256, 0, st>>>(N.w, N.img);
+    else k_make_image<64><<<64, 256, 0, st>>>(N.w, N.img);
+}
+
+template <int W>
+void launch_infer(NrcState &N, const float *raw, int stride, int n, const int *n_dev, float *out, float4 *rad,
+                  cudaStream_t st) {
+    using T = tc::Tc<W>;
+    k_infer_tc<W><<<N.sms * T::kCtasPerSm, 128 * T::kGroups, T::kSmemBytes, st>>>(N.img, raw, stride, n, n_dev, out,
+                                                                                  rad, N.ints + 2);
+}
+
+template <int W>
+void launch_grad(NrcState &N, const float *raw, int raw_stride, const float *tgt, int tgt_stride, int n,
+                 const int *n_dev, int rows, cudaStream_t st) {
+    const size_t ls = (size_t)N.tr_cap * W;
+    k_train_fb<W><<<N.sms * Fb<W>::kCtasPerSm, 32 * Fb<W>::kWarps, Fb<W>::kSmem, st>>>(
+        N.img, raw, raw_stride, tgt, tgt_stride, n, n_dev, N.scal, N.trH, N.trD, ls, N.scal + 1);
+    // split K: chunks of at least 1024 samples, about four CTAs per SM over the six layers
+    const int want = std::max(1, 4 * N.sms / (kLayers + 1));
+    int chunk = std::max(1024, (rows + want - 1) / want);
+    chunk = (chunk + 15) & ~15;
+    const dim3 gdw((unsigned)((rows + chunk - 1) / chunk), kLayers + 1);
+    k_train_dw<W><<<gdw, 2 * W, 0, st>>>(N.trH, N.trD, ls, n, n_dev, chunk, N.g);
+}
+}  // namespace
+
 kgk_status nrc_init(NrcState &N, const kgk_nrc_config *cfg, int device) {
     nrc_free(N);
     if (cfg) N.cfg = *cfg;
-    if (N.cfg.width == 0) N.cfg.width = kWidth;
+    if (N.cfg.width == 0) N.cfg.width = 64;
     if (N.cfg.hidden_layers == 0) N.cfg.hidden_layers = kLayers;
-    if (N.cfg.width != kWidth || N.cfg.hidden_layers != kLayers)
-        return fail(KGK_ERR_UNSUPPORTED, "radiance cache: this build has 5 hidden layers of width 64");
+    if (!width_ok(N.cfg.width) || N.cfg.hidden_layers != kLayers)
+        return fail(KGK_ERR_UNSUPPORTED, "radiance cache: this build has 5 hidden layers of width 64 or 128");
+    const int W = N.cfg.width;
+    N.params = params_of(W);
     if (N.cfg.learning_rate <= 0.0f) N.cfg.learning_rate = 1e-2f;
     if (N.cfg.train_paths <= 0) N.cfg.train_paths = 65536;
     if (N.cfg.train_suffix_max <= 0) N.cfg.train_suffix_max = 4;
     if (N.cfg.train_steps <= 0) N.cfg.train_steps = 4;
     if (N.cfg.spread_c <= 0.0f) N.cfg.spread_c = 0.01f;
-    KGK_TRY(dalloc(&N.w, kParams, "cache weights"));
-    KGK_TRY(dalloc(&N.m, kParams, "cache Adam state"));
-    KGK_TRY(dalloc(&N.v, kParams, "cache Adam state"));
-    KGK_TRY(dalloc(&N.g, kParams, "cache gradient"));
-    KGK_TRY(dalloc(&N.img, (size_t)kImgElems, "cache BF16 weights"));
+    KGK_TRY(dalloc(&N.w, (size_t)N.params, "cache weights"));
+    KGK_TRY(dalloc(&N.m, (size_t)N.params, "cache Adam state"));
+    KGK_TRY(dalloc(&N.v, (size_t)N.params, "cache Adam state"));
+    KGK_TRY(dalloc(&N.g, (size_t)N.params, "cache gradient"));
+    KGK_TRY(dalloc(&N.img, (size_t)img_elems_of(W), "cache BF16 weights"));
     KGK_TRY(dalloc(&N.scal, 4, "cache scalars"));
     KGK_TRY(dalloc(&N.ints, 4, "cache scalars"));
-    // He-uniform initialisation from a seeded stream
-    std::vector<float> h(kParams);
+    // He-uniform initialisation (bound sqrt(6 / inputs of the layer)) from a
+    // seeded stream
+    std::vector<float> h(N.params);
     unsigned long long s = N.cfg.seed ? N.cfg.seed : 0x1234567ull;
     auto nxt = [&]() {
         s ^= s << 13; s ^= s >> 7; s ^= s << 17;
         return (double)(s >> 11) * (1.0 / 9007199254740992.0);
     };
-    const double lim = std::sqrt(6.0 / kWidth);
-    for (int i = 0; i < kParams; ++i) h[i] = (float)((2.0 * nxt() - 1.0) * lim);
-    KGK_CUDA(cudaMemcpy(N.w, h.data(), kParams * sizeof(float), cudaMemcpyHostToDevice));
-    KGK_CUDA(cudaMemset(N.m, 0, kParams * sizeof(float)));
-    KGK_CUDA(cudaMemset(N.v, 0, kParams * sizeof(float)));
+    for (int i = 0; i < N.params; ++i) {
+        const int fan_in = i < W * kIn ? kIn : W;
+        h[i] = (float)((2.0 * nxt() - 1.0) * std::sqrt(6.0 / fan_in));
+    }
+    KGK_CUDA(cudaMemcpy(N.w, h.data(), N.params * sizeof(float), cudaMemcpyHostToDevice));
+    KGK_CUDA(cudaMemset(N.m, 0, N.params * sizeof(float)));
+    KGK_CUDA(cudaMemset(N.v, 0, N.params * sizeof(float)));
     const float sc[4] = {kInitScale, 0.0f, 0.0f, 0.0f};
     KGK_CUDA(cudaMemcpy(N.scal, sc, sizeof sc, cudaMemcpyHostToDevice));
     KGK_CUDA(cudaMemset(N.ints, 0, 4 * sizeof(int)));
-    k_make_image<<<64, 256>>>(N.w, N.img);
+    make_image(N, 0);
     KGK_CUDA(cudaGetLastError());
     KGK_CUDA(cudaDeviceSynchronize());
-    KGK_CUDA(cudaFuncSetAttribute(k_train_fb, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFbSmem));
-    KGK_CUDA(cudaFuncSetAttribute(k_infer_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc::kSmemBytes));
+    KGK_CUDA(cudaFuncSetAttribute(k_train_fb<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Fb<64>::kSmem));
+    KGK_CUDA(cudaFuncSetAttribute(k_train_fb<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Fb<128>::kSmem));
+    KGK_CUDA(cudaFuncSetAttribute(k_infer_tc<64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)tc::Tc<64>::kSmemBytes));
+    KGK_CUDA(cudaFuncSetAttribute(k_infer_tc<128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)tc::Tc<128>::kSmemBytes));
     cudaDeviceProp p;
     KGK_CUDA(cudaGetDeviceProperties(&p, device));
     N.sms = p.multiProcessorCount;
@@ -841,8 +866,10 @@ kgk_status nrc_check_error(NrcState &N) {
 
 kgk_status nrc_infer_dev(NrcState &N, const float *raw, int stride, int n, const int *n_dev, float *out, float4 *rad,
                          cudaStream_t st) {
-    const int grid = N.sms * 2;  // two ~108 KB CTAs of four warpgroups per SM, 2 x 256 TMEM columns of 512
-    k_infer_tc<<<grid, 128 * tc::kGroups, tc::kSmemBytes, st>>>(N.img, raw, stride, n, n_dev, out, rad, N.ints + 2);
+    // width 64: two ~107 KB CTAs of four warpgroups per SM (2 x 256 TMEM columns of 512);
+    // width 128: one ~213 KB CTA of two warpgroups per SM
+    if (N.cfg.width == 128) launch_infer<128>(N, raw, stride, n, n_dev, out, rad, st);
+    else launch_infer<64>(N, raw, stride, n, n_dev, out, rad, st);
     KGK_CUDA(cudaGetLastError());
     return KGK_OK;
 }
@@ -851,38 +878,36 @@ kgk_status nrc_grad_dev(NrcState &N, const float *raw, int raw_stride, const flo
                         const int *n_dev, cudaStream_t st) {
     const int rows = (n + 15) & ~15;
     if (N.tr_cap < rows) {
-        // per-sample activations and output gradients of every layer (BF16 rows of 64)
+        // per-sample activations and output gradients of every layer (BF16 rows of W)
         dfree(N.trH);
         dfree(N.trD);
         N.trH = N.trD = nullptr;
         N.tr_cap = 0;
-        const size_t cnt = (size_t)(kLayers + 1) * rows * kWidth;
+        const size_t cnt = (size_t)(kLayers + 1) * rows * N.cfg.width;
         KGK_TRY(dalloc(&N.trH, cnt, "cache training scratch"));
         KGK_TRY(dalloc(&N.trD, cnt, "cache training scratch"));
+        KGK_CUDA(cudaMemset(N.trH, 0, cnt * sizeof(unsigned short)));
         KGK_CUDA(cudaMemset(N.trD, 0, cnt * sizeof(unsigned short)));  // output-layer columns >= 8 stay 0
         N.tr_cap = rows;
     }
-    const size_t ls = (size_t)N.tr_cap * kWidth;
-    KGK_CUDA(cudaMemsetAsync(N.g, 0, kParams * sizeof(float), st));
+    KGK_CUDA(cudaMemsetAsync(N.g, 0, N.params * sizeof(float), st));
     KGK_CUDA(cudaMemsetAsync(N.scal + 1, 0, sizeof(float), st));  // loss
-    k_train_fb<<<N.sms * 2, 32 * kFbWarps, kFbSmem, st>>>(N.img, raw, raw_stride, tgt, tgt_stride, n, n_dev, N.scal,
-                                                          N.trH, N.trD, ls, N.scal + 1);
-    const dim3 gdw((unsigned)((rows + kDwChunk - 1) / kDwChunk), kLayers + 1);
-    k_train_dw<<<gdw, 128, 0, st>>>(N.trH, N.trD, ls, n, n_dev, N.g);
+    if (N.cfg.width == 128) launch_grad<128>(N, raw, raw_stride, tgt, tgt_stride, n, n_dev, rows, st);
+    else launch_grad<64>(N, raw, raw_stride, tgt, tgt_stride, n, n_dev, rows, st);
     KGK_CUDA(cudaGetLastError());
     return KGK_OK;
 }
 
 kgk_status nrc_step_dev(NrcState &N, cudaStream_t st) {
     KGK_CUDA(cudaMemsetAsync(N.ints, 0, sizeof(int), st));  // bad flag
-    k_check_finite<<<64, 256, 0, st>>>(N.g, kParams, N.ints);
+    k_check_finite<<<64, 256, 0, st>>>(N.g, N.params, N.ints);
     ++N.step;
     const float b1 = 0.9f, b2 = 0.99f;
     const float bc1 = 1.0f - std::pow(b1, (float)N.step), bc2 = 1.0f - std::pow(b2, (float)N.step);
-    k_adam<<<64, 256, 0, st>>>(N.w, N.m, N.v, N.g, kParams, N.ints, N.scal, N.cfg.learning_rate, b1, b2, 1e-10f,
+    k_adam<<<64, 256, 0, st>>>(N.w, N.m, N.v, N.g, N.params, N.ints, N.scal, N.cfg.learning_rate, b1, b2, 1e-10f,
                                bc1, bc2);
     k_scale_update<<<1, 1, 0, st>>>(N.scal, N.ints + 1, N.ints);
-    k_make_image<<<64, 256, 0, st>>>(N.w, N.img);
+    make_image(N, st);
     KGK_CUDA(cudaGetLastError());
     return KGK_OK;
 }
@@ -942,11 +967,11 @@ kgk_status kgk_nrc_init(kgk_scene *s, const kgk_nrc_config *cfg) {
 
 kgk_status kgk_nrc_set_weights(kgk_scene *s, const float *w, size_t n) {
     KGK_TRY(need(s));
-    if (!w || n != (size_t)kParams)
-        return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_nrc_set_weights: expected " + std::to_string(kParams) + " floats");
     NrcState &N = *s->nrc;
+    if (!w || n != (size_t)N.params)
+        return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_nrc_set_weights: expected " + std::to_string(N.params) + " floats");
     KGK_CUDA(cudaMemcpy(N.w, w, n * sizeof(float), is_device_ptr(w) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice));
-    k_make_image<<<64, 256, 0, s->stream>>>(N.w, N.img);
+    make_image(N, s->stream);
     KGK_CUDA(cudaGetLastError());
     KGK_CUDA(cudaStreamSynchronize(s->stream));
     return KGK_OK;
@@ -954,8 +979,9 @@ kgk_status kgk_nrc_set_weights(kgk_scene *s, const float *w, size_t n) {
 
 kgk_status kgk_nrc_get_weights(kgk_scene *s, float *w, size_t n) {
     KGK_TRY(need(s));
-    if (!w || n != (size_t)kParams)
-        return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_nrc_get_weights: expected " + std::to_string(kParams) + " floats");
+    if (!w || n != (size_t)s->nrc->params)
+        return fail(KGK_ERR_INVALID_ARGUMENT,
+                    "kgk_nrc_get_weights: expected " + std::to_string(s->nrc->params) + " floats");
     KGK_CUDA(cudaStreamSynchronize(s->stream));
     KGK_CUDA(cudaMemcpy(w, s->nrc->w, n * sizeof(float), is_device_ptr(w) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost));
     return KGK_OK;
@@ -991,11 +1017,11 @@ kgk_status kgk_nrc_gradients(kgk_scene *s, const float *raw, const float *target
     NrcState &N = *s->nrc;
     KGK_TRY(nrc_grad_dev(N, (const float *)draw, kRaw, (const float *)dt, 3, (int)n, nullptr, s->stream));
     void *dg;
-    KGK_TRY(dmalloc(&dg, kParams * sizeof(float), "cache staging"));
+    KGK_TRY(dmalloc(&dg, N.params * sizeof(float), "cache staging"));
     o.v.push_back(dg);
-    k_unscale<<<64, 256, 0, s->stream>>>(N.g, kParams, N.scal, (float *)dg);
+    k_unscale<<<64, 256, 0, s->stream>>>(N.g, N.params, N.scal, (float *)dg);
     KGK_CUDA(cudaGetLastError());
-    KGK_CUDA(cudaMemcpyAsync(grad, dg, kParams * sizeof(float), cudaMemcpyDeviceToHost, s->stream));
+    KGK_CUDA(cudaMemcpyAsync(grad, dg, N.params * sizeof(float), cudaMemcpyDeviceToHost, s->stream));
     float hl = 0.0f;
     KGK_CUDA(cudaMemcpyAsync(&hl, N.scal + 1, sizeof(float), cudaMemcpyDeviceToHost, s->stream));
     KGK_CUDA(cudaStreamSynchronize(s->stream));
