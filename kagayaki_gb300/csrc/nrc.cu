@@ -51,6 +51,25 @@ __device__ __forceinline__ void mma16816(float (&d)[4], const uint32_t (&a)[4], 
         : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
 }
 
+__device__ __forceinline__ uint32_t smem_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// Four 8 x 8 BF16 matrices from shared memory; lanes 8j..8j+7 give the row
+// addresses of matrix j, register j receives it in the mma fragment layout
+// (thread T: row T/4, columns 2 (T%4), +1).
+__device__ __forceinline__ void ldsm_x4(const unsigned short *p, uint32_t &r0, uint32_t &r1, uint32_t &r2,
+                                        uint32_t &r3) {
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];"
+                 : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
+                 : "r"(smem_addr(p)));
+}
+// The same, transposed: thread T receives rows 2 (T%4), +1 of column T/4.
+__device__ __forceinline__ void ldsm_x4_t(const unsigned short *p, uint32_t &r0, uint32_t &r1, uint32_t &r2,
+                                          uint32_t &r3) {
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];"
+                 : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
+                 : "r"(smem_addr(p)));
+}
+
 // One input feature (column c of the 64-float encoding) of a raw query.
 __device__ __forceinline__ float encode_col(const float *raw, int c) {
     if (c < 36) {
@@ -113,19 +132,45 @@ __device__ __forceinline__ void encode_frags(const float *ra, const float *rb, u
 }
 
 // acc[nt] = A (16 x 16 KT) * W^T for output rows 8 nt .. 8 nt + 7 of a weight
-// matrix [out][in] in shared memory (BF16, row pitch P).
+// matrix [out][in] in shared memory (BF16, row pitch P).  The B fragments of
+// two K steps come from one ldmatrix.x4: matrices (kt, low 8), (kt, high 8),
+// (kt + 1, low 8), (kt + 1, high 8) of the rows 8 nt..8 nt + 7.
 template <int P, int KT, int NT>
 __device__ __forceinline__ void layer_fwd(const unsigned short *Wm, const uint32_t (&a)[KT][4], float (&acc)[NT][4]) {
-    const int g = (threadIdx.x & 31) >> 2, t = threadIdx.x & 3;
+    static_assert(KT % 2 == 0, "K steps in pairs");
+    const int lane = threadIdx.x & 31, j = lane >> 3, rr = lane & 7;
+    const unsigned short *base = Wm + rr * P + (j >> 1) * 16 + (j & 1) * 8;
 #pragma unroll
     for (int nt = 0; nt < NT; ++nt) {
         acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.0f;
-        const unsigned short *row = Wm + (nt * 8 + g) * P;
 #pragma unroll
-        for (int kt = 0; kt < KT; ++kt) {
-            const uint32_t b0 = *reinterpret_cast<const uint32_t *>(row + kt * 16 + 2 * t);
-            const uint32_t b1 = *reinterpret_cast<const uint32_t *>(row + kt * 16 + 8 + 2 * t);
+        for (int kt = 0; kt < KT; kt += 2) {
+            uint32_t b0, b1, b2, b3;
+            ldsm_x4(base + nt * 8 * P + kt * 16, b0, b1, b2, b3);
             mma16816(acc[nt], a[kt], b0, b1);
+            mma16816(acc[nt], a[kt + 1], b2, b3);
+        }
+    }
+}
+
+// acc[nt] = dZ (16 x 16 KT, K = output rows of W) * W for input columns
+// 8 nt .. 8 nt + 7 of a weight matrix [out][in] (pitch P): the B fragments
+// are W's 8 x 8 blocks transposed, two K steps per ldmatrix.x4.trans
+// (blocks (kt, low 8 rows), (kt, high 8), (kt + 1, low 8), (kt + 1, high 8)).
+template <int P, int KT, int NT>
+__device__ __forceinline__ void layer_bwd(const unsigned short *Wm, const uint32_t (&a)[KT][4], float (&acc)[NT][4]) {
+    static_assert(KT % 2 == 0, "K steps in pairs");
+    const int lane = threadIdx.x & 31, j = lane >> 3, rr = lane & 7;
+    const unsigned short *base = Wm + ((j >> 1) * 16 + (j & 1) * 8 + rr) * P;
+#pragma unroll
+    for (int nt = 0; nt < NT; ++nt) {
+        acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.0f;
+#pragma unroll
+        for (int kt = 0; kt < KT; kt += 2) {
+            uint32_t b0, b1, b2, b3;
+            ldsm_x4_t(base + kt * 16 * P + nt * 8, b0, b1, b2, b3);
+            mma16816(acc[nt], a[kt], b0, b1);
+            mma16816(acc[nt], a[kt + 1], b2, b3);
         }
     }
 }
@@ -478,7 +523,7 @@ constexpr int kMaskBytes = kLayers * 32 * 8;  // per warp
 template <int W>
 struct Fb {
     static constexpr int kWarps = W == 64 ? 4 : 8;
-    static constexpr int kCtasPerSm = W == 64 ? 2 : 1;
+    static constexpr int kCtasPerSm = W == 64 ? 4 : 1;
     static constexpr size_t kImgBytes = ((size_t)Net<W>::kImg * 2 + 15) & ~(size_t)15;
     static constexpr size_t kSmem = kImgBytes + (size_t)kMaskBytes * kWarps;
     static_assert(kSmem * kCtasPerSm <= 227 * 1024, "shared memory per SM");
@@ -562,14 +607,18 @@ __global__ void __launch_bounds__(32 * Fb<W>::kWarps) k_train_fb(
             dza[1] = pack2(dy[2], dy[3]);
             dza[2] = 0u;
             dza[3] = 0u;
-            const unsigned short *Wo = sW + kLayers * W * P;
+            // B: the 16 padded output rows of W_out, 8 x 8 blocks transposed;
+            // blocks (rows 0-7, nt), (8-15, nt), (0-7, nt + 1), (8-15, nt + 1)
+            const int j = lane >> 3, rr = lane & 7;
+            const unsigned short *Wo = sW + kLayers * W * P + ((j & 1) * 8 + rr) * P + (j >> 1) * 8;
 #pragma unroll
-            for (int nt = 0; nt < NT; ++nt) {
+            for (int nt = 0; nt < NT; nt += 2) {
+                uint32_t b0, b1, b2, b3;
+                ldsm_x4_t(Wo + nt * 8, b0, b1, b2, b3);
                 acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.0f;
-                const int i = nt * 8 + g;
-                const uint32_t b0 = pack_raw(Wo[(2 * t) * P + i], Wo[(2 * t + 1) * P + i]);
-                const uint32_t b1 = pack_raw(Wo[(2 * t + 8) * P + i], Wo[(2 * t + 9) * P + i]);
+                acc[nt + 1][0] = acc[nt + 1][1] = acc[nt + 1][2] = acc[nt + 1][3] = 0.0f;
                 mma16816(acc[nt], dza, b0, b1);
+                mma16816(acc[nt + 1], dza, b2, b3);
             }
         }
 #pragma unroll 1
@@ -598,19 +647,7 @@ __global__ void __launch_bounds__(32 * Fb<W>::kWarps) k_train_fb(
                 a[kt][2] = pack2(acc[2 * kt + 1][0], acc[2 * kt + 1][1]);
                 a[kt][3] = pack2(acc[2 * kt + 1][2], acc[2 * kt + 1][3]);
             }
-            const unsigned short *Wl = sW + l * W * P;
-#pragma unroll
-            for (int nt = 0; nt < NT; ++nt) {
-                acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.0f;
-                const int i = nt * 8 + g;
-#pragma unroll
-                for (int kt = 0; kt < KT; ++kt) {
-                    const int o = kt * 16 + 2 * t;
-                    const uint32_t b0 = pack_raw(Wl[o * P + i], Wl[(o + 1) * P + i]);
-                    const uint32_t b1 = pack_raw(Wl[(o + 8) * P + i], Wl[(o + 9) * P + i]);
-                    mma16816(acc[nt], a[kt], b0, b1);
-                }
-            }
+            layer_bwd<P, KT, NT>(sW + l * W * P, a, acc);
         }
         __syncwarp();
     }
@@ -621,42 +658,77 @@ __global__ void __launch_bounds__(32 * Fb<W>::kWarps) k_train_fb(
 
 // dW_l[o][i] += sum over the samples s0..s1-1 of dZ_l[s][o] * H_l[s][i] for
 // the layer's IN = 8 NT inputs.  Warp w owns output rows 16w..16w+15 (the
-// output layer only warp 0).
+// output layer only warp 0).  Samples arrive in stages of kDwStage rows of
+// dZ and H, double-buffered with cp.async; both operands are read with
+// ldmatrix.trans (A = dZ^T, B = H with K = samples).
+constexpr int kDwStage = 64;
+
+template <int W>
+struct Dw {
+    static constexpr size_t kBuf = (size_t)kDwStage * Net<W>::kPitch;  // elements of one operand stage
+    static constexpr size_t kSmem = 4 * kBuf * sizeof(unsigned short);  // dZ and H, two stages
+};
+
+__device__ __forceinline__ void cp_async16(void *dst, const void *src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_addr(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+
 template <int W, int NT>
 __device__ __forceinline__ void dw_chunk(const unsigned short *D, const unsigned short *H, int s0, int s1, int l,
-                                        float *dW, unsigned short *sD, unsigned short *sH) {
+                                        float *dW, unsigned short *sm) {
     constexpr int P = Net<W>::kPitch, IN = NT * 8;
+    constexpr size_t kBuf = Dw<W>::kBuf;
+    static_assert(NT % 2 == 0, "column blocks in pairs");
     const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3, wid = threadIdx.x >> 5;
+    const int j = lane >> 3, rr = lane & 7;
     const bool active = l < kLayers || wid == 0;
     float acc[NT][4];
 #pragma unroll
     for (int nt = 0; nt < NT; ++nt) acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.0f;
-    for (int sb = s0; sb < s1; sb += 16) {
-        __syncthreads();
-        {
-            const int r = threadIdx.x / (W / 8), c = threadIdx.x % (W / 8);  // 16 rows x W/8 chunks
-            *reinterpret_cast<uint4 *>(sD + r * P + c * 8) =
-                *reinterpret_cast<const uint4 *>(D + (size_t)(sb + r) * W + c * 8);
-            if (c < IN / 8)
-                *reinterpret_cast<uint4 *>(sH + r * P + c * 8) =
-                    *reinterpret_cast<const uint4 *>(H + (size_t)(sb + r) * W + c * 8);
+    auto load = [&](int sb, int buf) {
+        unsigned short *sD = sm + (size_t)buf * 2 * kBuf, *sH = sD + kBuf;
+        const int rows = min(kDwStage, s1 - sb);
+        for (int i = threadIdx.x; i < kDwStage * (W / 8); i += blockDim.x) {
+            const int r = i / (W / 8), c = i % (W / 8);
+            if (r < rows) cp_async16(sD + r * P + c * 8, D + (size_t)(sb + r) * W + c * 8);
         }
+        for (int i = threadIdx.x; i < kDwStage * (IN / 8); i += blockDim.x) {
+            const int r = i / (IN / 8), c = i % (IN / 8);
+            if (r < rows) cp_async16(sH + r * P + c * 8, H + (size_t)(sb + r) * W + c * 8);
+        }
+        cp_async_commit();
+    };
+    int buf = 0;
+    load(s0, 0);
+    for (int sb = s0; sb < s1; sb += kDwStage) {
+        if (sb + kDwStage < s1) load(sb + kDwStage, buf ^ 1);
+        else cp_async_commit();  // an empty group keeps the wait count uniform
+        cp_async_wait1();
         __syncthreads();
-        if (!active) continue;
-        // A = dZ^T rows o (16 of them) x 16 samples; B = H samples x IN inputs
-        uint32_t a[4];
-        const int o0 = wid * 16 + g, o1 = o0 + 8;
-        a[0] = pack_raw(sD[(2 * t) * P + o0], sD[(2 * t + 1) * P + o0]);
-        a[1] = pack_raw(sD[(2 * t) * P + o1], sD[(2 * t + 1) * P + o1]);
-        a[2] = pack_raw(sD[(2 * t + 8) * P + o0], sD[(2 * t + 9) * P + o0]);
-        a[3] = pack_raw(sD[(2 * t + 8) * P + o1], sD[(2 * t + 9) * P + o1]);
+        if (active) {
+            const unsigned short *sD = sm + (size_t)buf * 2 * kBuf, *sH = sD + kBuf;
+            const int ksteps = min(kDwStage, s1 - sb) / 16;
+            for (int ks = 0; ks < ksteps; ++ks) {
+                // A = dZ^T (rows o = 16 wid..16 wid + 15, K = 16 samples): blocks
+                // (samples 0-7, o 0-7), (0-7, 8-15), (8-15, 0-7), (8-15, 8-15)
+                uint32_t a[4];
+                ldsm_x4_t(sD + (ks * 16 + (j >> 1) * 8 + rr) * P + wid * 16 + (j & 1) * 8, a[0], a[1], a[2], a[3]);
+                // B = H (K = 16 samples, N = 8 inputs): blocks (0-7, nt), (8-15, nt),
+                // (0-7, nt + 1), (8-15, nt + 1)
+                const unsigned short *hb = sH + (ks * 16 + (j & 1) * 8 + rr) * P + (j >> 1) * 8;
 #pragma unroll
-        for (int nt = 0; nt < NT; ++nt) {
-            const int i = nt * 8 + g;
-            const uint32_t b0 = pack_raw(sH[(2 * t) * P + i], sH[(2 * t + 1) * P + i]);
-            const uint32_t b1 = pack_raw(sH[(2 * t + 8) * P + i], sH[(2 * t + 9) * P + i]);
-            mma16816(acc[nt], a, b0, b1);
+                for (int nt = 0; nt < NT; nt += 2) {
+                    uint32_t b0, b1, b2, b3;
+                    ldsm_x4_t(hb + nt * 8, b0, b1, b2, b3);
+                    mma16816(acc[nt], a, b0, b1);
+                    mma16816(acc[nt + 1], a, b2, b3);
+                }
+            }
         }
+        __syncthreads();
+        buf ^= 1;
     }
     if (!active) return;
     const int o0 = wid * 16 + g, o1 = o0 + 8;
@@ -681,7 +753,7 @@ template <int W>
 __global__ void __launch_bounds__(2 * W) k_train_dw(const unsigned short *__restrict__ Hs,
                                                     const unsigned short *__restrict__ Ds, size_t layer_stride,
                                                     int n, const int *n_dev, int chunk, float *dW_glob) {
-    __shared__ __align__(16) unsigned short sD[16 * Net<W>::kPitch], sH[16 * Net<W>::kPitch];
+    extern __shared__ __align__(16) unsigned short dw_smem[];
     const int l = blockIdx.y;
     const int total = n_dev ? min(*n_dev, n) : n;
     const int padded = (total + 15) & ~15;
@@ -689,8 +761,8 @@ __global__ void __launch_bounds__(2 * W) k_train_dw(const unsigned short *__rest
     if (s0 >= s1) return;
     const unsigned short *D = Ds + (size_t)l * layer_stride, *H = Hs + (size_t)l * layer_stride;
     float *dW = dW_glob + Net<W>::woff(l);
-    if (l == 0) dw_chunk<W, kIn / 8>(D, H, s0, s1, l, dW, sD, sH);
-    else dw_chunk<W, W / 8>(D, H, s0, s1, l, dW, sD, sH);
+    if (l == 0) dw_chunk<W, kIn / 8>(D, H, s0, s1, l, dW, dw_smem);
+    else dw_chunk<W, W / 8>(D, H, s0, s1, l, dW, dw_smem);
 }
 
 // Master weights -> padded BF16 image: row r of layer l at (l W + r) P, the
@@ -784,7 +856,7 @@ void launch_grad(NrcState &N, const float *raw, int raw_stride, const float *tgt
     int chunk = std::max(1024, (rows + want - 1) / want);
     chunk = (chunk + 15) & ~15;
     const dim3 gdw((unsigned)((rows + chunk - 1) / chunk), kLayers + 1);
-    k_train_dw<W><<<gdw, 2 * W, 0, st>>>(N.trH, N.trD, ls, n, n_dev, chunk, N.g);
+    k_train_dw<W><<<gdw, 2 * W, Dw<W>::kSmem, st>>>(N.trH, N.trD, ls, n, n_dev, chunk, N.g);
 }
 }  // namespace
 
@@ -832,6 +904,8 @@ kgk_status nrc_init(NrcState &N, const kgk_nrc_config *cfg, int device) {
     KGK_CUDA(cudaDeviceSynchronize());
     KGK_CUDA(cudaFuncSetAttribute(k_train_fb<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Fb<64>::kSmem));
     KGK_CUDA(cudaFuncSetAttribute(k_train_fb<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Fb<128>::kSmem));
+    KGK_CUDA(cudaFuncSetAttribute(k_train_dw<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Dw<64>::kSmem));
+    KGK_CUDA(cudaFuncSetAttribute(k_train_dw<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Dw<128>::kSmem));
     KGK_CUDA(cudaFuncSetAttribute(k_infer_tc<64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)tc::Tc<64>::kSmemBytes));
     KGK_CUDA(cudaFuncSetAttribute(k_infer_tc<128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
