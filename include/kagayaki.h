@@ -215,8 +215,9 @@ typedef struct kgk_host_scene {
  * the OBJ file's directory.  Vertices without vn (or whose vn index is past
  * the file's normals) take the face normal and without vt (0,0,0), where the
  * reference would read past its arrays.
- * Images: PNG, JPEG (baseline and progressive), binary PNM and Radiance .hdr
- * (KGK_ERR_UNSUPPORTED for BMP, TGA, PSD, GIF and PIC). */
+ * Images: every format stbi_loadf reads: PNG, JPEG (baseline and progressive),
+ * BMP, TGA, GIF (first frame), PSD, Softimage PIC, binary PNM and Radiance
+ * .hdr. */
 kgk_status kgk_load_obj(const char *obj_path, const char *hdr_path, kgk_host_scene *out);
 void kgk_host_scene_free(kgk_host_scene *scene);
 

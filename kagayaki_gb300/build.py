@@ -19,7 +19,7 @@ LIB = os.path.join(HERE, "libkagayaki_gb300.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 CU_SOURCES = ["bvh.cu", "scene.cu", "trace.cu", "render.cu", "svgf.cu", "nrc.cu"]
-CPP_SOURCES = ["capi.cpp", "image_io.cpp", "image_load.cpp", "jpeg_load.cpp", "obj_load.cpp"]
+CPP_SOURCES = ["capi.cpp", "image_io.cpp", "image_load.cpp", "image_formats.cpp", "jpeg_load.cpp", "obj_load.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

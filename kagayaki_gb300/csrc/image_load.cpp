@@ -10,9 +10,11 @@
 //     float, alpha (the last channel when the count is even) = byte / 255;
 //   * 16-bit images are first reduced to 8 bits (the high byte).
 // This file decodes PNG (every colour type and bit depth, tRNS, Adam7),
-// binary PNM (P5 / P6) and Radiance .hdr, takes JPEG from jpeg_load.cpp, and
-// converts them by those rules.  BMP, TGA, PSD, GIF and PIC are not decoded
-// (KGK_ERR_UNSUPPORTED).
+// binary PNM (P5 / P6) and Radiance .hdr, takes JPEG from jpeg_load.cpp and
+// BMP, GIF, PSD, PIC and TGA from image_formats.cpp, tries the formats in
+// stb's order (stbi__load_main: PNG, BMP, GIF, PSD, PIC, JPEG, PNM, then the
+// weak TGA test last; .hdr first, as stbi_loadf does) and converts the bytes
+// by those rules.
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -551,6 +553,17 @@ namespace kgk {
 
 kgk_status decode_jpeg(const std::vector<uint8_t> &f, int *w_out, int *h_out, int *n_out, std::vector<uint8_t> &pix,
                        const char *path);
+// image_formats.cpp
+bool is_bmp(const std::vector<uint8_t> &f);
+bool is_gif(const std::vector<uint8_t> &f);
+bool is_psd(const std::vector<uint8_t> &f);
+bool is_pic(const std::vector<uint8_t> &f);
+bool is_tga(const std::vector<uint8_t> &f);
+kgk_status decode_bmp(const std::vector<uint8_t> &f, int *w, int *h, int *n, std::vector<uint8_t> &pix, const char *path);
+kgk_status decode_gif(const std::vector<uint8_t> &f, int *w, int *h, int *n, std::vector<uint8_t> &pix, const char *path);
+kgk_status decode_psd(const std::vector<uint8_t> &f, int *w, int *h, int *n, std::vector<uint8_t> &pix, const char *path);
+kgk_status decode_pic(const std::vector<uint8_t> &f, int *w, int *h, int *n, std::vector<uint8_t> &pix, const char *path);
+kgk_status decode_tga(const std::vector<uint8_t> &f, int *w, int *h, int *n, std::vector<uint8_t> &pix, const char *path);
 
 // stbi_loadf: decode and convert to float (see the file comment).
 kgk_status load_image_float(const char *path, kgk_texture *out) {
@@ -566,13 +579,22 @@ kgk_status load_image_float(const char *path, kgk_texture *out) {
     static const uint8_t kPng[8] = {137, 80, 78, 71, 13, 10, 26, 10};
     if (f.size() >= 8 && !memcmp(f.data(), kPng, 8)) {
         KGK_TRY(decode_png(f, &w, &h, &n, pix, path));
-    } else if (f.size() >= 3 && f[0] == 'P' && (f[1] == '5' || f[1] == '6')) {
-        KGK_TRY(decode_pnm(f, &w, &h, &n, pix, path));
+    } else if (is_bmp(f)) {
+        KGK_TRY(decode_bmp(f, &w, &h, &n, pix, path));
+    } else if (is_gif(f)) {
+        KGK_TRY(decode_gif(f, &w, &h, &n, pix, path));
+    } else if (is_psd(f)) {
+        KGK_TRY(decode_psd(f, &w, &h, &n, pix, path));
+    } else if (is_pic(f)) {
+        KGK_TRY(decode_pic(f, &w, &h, &n, pix, path));
     } else if (is_jpeg(f)) {
         KGK_TRY(decode_jpeg(f, &w, &h, &n, pix, path));
+    } else if (f.size() >= 3 && f[0] == 'P' && (f[1] == '5' || f[1] == '6')) {
+        KGK_TRY(decode_pnm(f, &w, &h, &n, pix, path));
+    } else if (is_tga(f)) {
+        KGK_TRY(decode_tga(f, &w, &h, &n, pix, path));
     } else {
-        return fail(KGK_ERR_UNSUPPORTED,
-                    std::string("unknown image format (PNG, JPEG, PNM and .hdr are decoded): ") + path);
+        return fail(KGK_ERR_UNSUPPORTED, std::string("unknown image format: ") + path);
     }
     const size_t npx = (size_t)w * h;
     float *px = (float *)malloc(npx * n * sizeof(float));

@@ -6,7 +6,11 @@ library and tests/golden/make_golden.py reads with the reference's own loader
 
   images: PNG in every colour type and bit depth (random row filters, zlib
           compression, Adam7 interlacing, tRNS), binary PNM, Radiance .hdr
-          (flat and run-length scanlines)
+          (flat and run-length scanlines), JPEG, BMP (every header size and
+          bit depth, bit fields), TGA (raw / run-length, grey, paletted,
+          15/16-bit), GIF (LZW with table restarts, interlacing, local
+          palettes, transparency, background fill), PSD (raw / RLE, 8 and 16
+          bits) and Softimage PIC (raw, pure and mixed run-length packets)
   OBJ.obj + scene.mtl + textures: triangles, quads, convex and concave
           polygons, negative indices, groups / objects, smoothing groups,
           usemtl switches (including an unknown material), numbers in several
@@ -604,8 +608,392 @@ def jpeg_cases():
     return cases
 
 
+# ---------------------------------------------------------------------------
+# BMP, TGA, GIF, PSD, Softimage PIC (small writers for the fixtures)
+# ---------------------------------------------------------------------------
+def bmp_bytes(img, bpp, hsz=40, top_down=False, compress=0, masks=None, palette=None):
+    """img: (h, w, 3|4) uint8 for bpp >= 16, or (h, w) palette indices for
+    bpp <= 8 (palette: (n, 3) RGB).  masks: (r, g, b[, a]) for compress 3 or
+    the V4/V5 header's mask fields."""
+    h, w = img.shape[:2]
+    rows = []
+    for y in range(h):
+        if bpp == 24:
+            row = img[y, :, 2::-1].tobytes()
+        elif bpp == 32 and masks is None:
+            px = img[y]
+            a = px[:, 3] if px.shape[1] == 4 else np.zeros(w, np.uint8)
+            row = np.stack([px[:, 2], px[:, 1], px[:, 0], a], 1).astype(np.uint8).tobytes()
+        elif bpp in (16, 32):
+            m = list(masks) + [0] * (4 - len(masks))
+            vals = np.zeros(w, np.uint64)
+            for c in range(4 if img.shape[2] == 4 else 3):
+                mk = m[c]
+                if not mk:
+                    continue
+                lo = (mk & -mk).bit_length() - 1
+                nb = bin(mk).count("1")
+                vals |= ((img[y, :, c].astype(np.uint64) >> np.uint64(8 - nb)) << np.uint64(lo))
+            row = vals.astype("<u2" if bpp == 16 else "<u4").tobytes()
+        elif bpp == 8:
+            row = img[y].astype(np.uint8).tobytes()
+        elif bpp == 4:
+            v = list(img[y]) + ([0] if w % 2 else [])
+            row = bytes((v[i] << 4) | v[i + 1] for i in range(0, len(v), 2))
+        elif bpp == 1:
+            v = list(img[y]) + [0] * ((-w) % 8)
+            row = bytes(sum(v[i + k] << (7 - k) for k in range(8)) for i in range(0, len(v), 8))
+        rows.append(row + b"\0" * ((-len(row)) % 4))
+    if not top_down:
+        rows = rows[::-1]
+    data = b"".join(rows)
+    pal = b""
+    if palette is not None:
+        for r, g, b in palette:
+            pal += bytes([b, g, r]) + (b"" if hsz == 12 else b"\0")
+    if hsz == 12:
+        info = struct.pack("<IHHHH", 12, w, h, 1, bpp)
+    else:
+        hh = -h if top_down else h
+        info = struct.pack("<IiiHHIIiiII", hsz, w, hh, 1, bpp, compress, len(data), 2835, 2835, 0, 0)
+        if hsz == 40 and compress == 3:
+            info += struct.pack("<III", *masks[:3])
+        elif hsz == 56:
+            info += struct.pack("<IIII", *(list(masks or [0, 0, 0, 0]) + [0] * 4)[:4])
+        elif hsz in (108, 124):
+            info += struct.pack("<IIII", *(list(masks or [0, 0, 0, 0]) + [0] * 4)[:4])
+            info += struct.pack("<I", 0x73524742) + b"\0" * 48
+            if hsz == 124:
+                info += b"\0" * 16
+    offset = 14 + len(info) + len(pal)
+    head = b"BM" + struct.pack("<IHHI", offset + len(data), 0, 0, offset)
+    return head + info + pal + data
+
+
+def bmp_cases():
+    rng = np.random.default_rng(21)
+    rgb = rng.integers(0, 256, (7, 13, 3), np.uint8)
+    rgba = rng.integers(0, 256, (6, 9, 4), np.uint8)
+    zero_a = rgba.copy()
+    zero_a[..., 3] = 0
+    pal = rng.integers(0, 256, (256, 3), np.uint8)
+    idx8 = rng.integers(0, 256, (5, 11), np.uint8)
+    idx4 = rng.integers(0, 16, (6, 9), np.uint8)
+    idx1 = rng.integers(0, 2, (4, 19), np.uint8)
+    os2_idx = rng.integers(0, 200, (5, 6), np.uint8)  # the OS/2 palette size formula reads 4 entries fewer
+    return [("rgb24.bmp", bmp_bytes(rgb, 24)),
+            ("rgb24_topdown.bmp", bmp_bytes(rgb, 24, top_down=True)),
+            ("rgba32_bi_rgb.bmp", bmp_bytes(rgba, 32)),
+            ("rgba32_v4.bmp", bmp_bytes(rgba, 32, hsz=108)),
+            ("rgba32_v5_zero_alpha.bmp", bmp_bytes(zero_a, 32, hsz=124, top_down=True)),
+            ("rgb32_bitfields.bmp", bmp_bytes(rgba[..., :3], 32, compress=3,
+                                              masks=(0xff000000, 0x00ff0000, 0x0000ff00))),
+            ("rgb16_555.bmp", bmp_bytes(rgb, 16, masks=(0x7c00, 0x03e0, 0x001f))),
+            ("rgb16_565.bmp", bmp_bytes(rgb, 16, compress=3, masks=(0xf800, 0x07e0, 0x001f))),
+            ("rgba16_4444_v4.bmp", bmp_bytes(rgba, 16, hsz=108, compress=3,
+                                             masks=(0x0f00, 0x00f0, 0x000f, 0xf000))),
+            ("pal8.bmp", bmp_bytes(idx8, 8, palette=pal)),
+            ("pal4.bmp", bmp_bytes(idx4, 4, palette=pal[:16])),
+            ("pal1.bmp", bmp_bytes(idx1, 1, palette=pal[:2])),
+            ("os2_rgb24.bmp", bmp_bytes(rgb, 24, hsz=12)),
+            ("os2_pal8.bmp", bmp_bytes(os2_idx, 8, hsz=12, palette=pal))]
+
+
+def _tga_rle(pixels):
+    """pixels: list of byte strings; run-length packets (runs of >= 2)."""
+    out, i, n = [], 0, len(pixels)
+    while i < n:
+        j = i
+        while j + 1 < n and pixels[j + 1] == pixels[i] and j - i < 127:
+            j += 1
+        if j > i:
+            out.append(bytes([0x80 | (j - i)]) + pixels[i])
+            i = j + 1
+            continue
+        j = i
+        while j + 1 < n and pixels[j + 1] != pixels[j] and j - i < 127:
+            j += 1
+        out.append(bytes([j - i]) + b"".join(pixels[i:j + 1]))
+        i = j + 1
+    return b"".join(out)
+
+
+def tga_bytes(pix, image_type, bpp, top_down=False, palette=None, pal_bits=0, image_id=b""):
+    """pix: (h, w, c) raw pixel bytes in file order (B, G, R[, A]), or (h, w)
+    indices / grey; palette: (n, pal_bits / 8) entry bytes in file order."""
+    h, w = pix.shape[:2]
+    rows = [pix[y] for y in range(h)]
+    if not top_down:
+        rows = rows[::-1]
+    bpx = bpp // 8 if bpp != 15 else 2
+    flat = []
+    for row in rows:
+        if row.ndim == 1:
+            if bpx == 2:
+                flat += [struct.pack("<H", int(v)) for v in row]
+            else:
+                flat += [bytes([int(v)]) for v in row]
+        else:
+            flat += [row[x].astype(np.uint8).tobytes() for x in range(w)]
+    data = _tga_rle(flat) if image_type >= 8 else b"".join(flat)
+    cmap = 1 if palette is not None else 0
+    n_pal = 0 if palette is None else len(palette)
+    head = struct.pack("<BBBHHBHHHHBB", len(image_id), cmap, image_type, 0, n_pal, pal_bits, 0, 0, w, h, bpp,
+                       0x20 if top_down else 0)
+    pal = b"" if palette is None else np.asarray(palette, np.uint8).tobytes()
+    return head + image_id + pal + data
+
+
+def tga_cases():
+    rng = np.random.default_rng(22)
+    bgr = rng.integers(0, 256, (6, 7, 3), np.uint8)
+    bgra = rng.integers(0, 256, (5, 8, 4), np.uint8)
+    grey = rng.integers(0, 256, (4, 9), np.uint8)
+    ga = rng.integers(0, 256, (5, 6, 2), np.uint8)
+    # images with runs for the RLE forms (runs cross row ends)
+    runs = rng.integers(0, 4, (9, 10), np.uint8)
+    run_cols = rng.integers(0, 256, (4, 3), np.uint8)
+    bgr_runs = run_cols[runs]
+    grey_runs = (runs * 60).astype(np.uint8)
+    pal24 = rng.integers(0, 256, (40, 3), np.uint8)
+    pal32 = rng.integers(0, 256, (16, 4), np.uint8)
+    pal16 = rng.integers(0, 1 << 15, 20).astype("<u2").view(np.uint8).reshape(20, 2)
+    idx = rng.integers(0, 40, (6, 5), np.uint8)
+    idx_bad = idx.copy()
+    idx_bad[0, 0] = 250  # out of the palette: entry 0
+    c16 = rng.integers(0, 1 << 15, (4, 5)).astype(np.uint16)
+    return [("bgr24.tga", tga_bytes(bgr, 2, 24)),
+            ("bgra32_topdown.tga", tga_bytes(bgra, 2, 32, top_down=True, image_id=b"kagayaki")),
+            ("grey8.tga", tga_bytes(grey, 3, 8)),
+            ("grey_alpha16.tga", tga_bytes(ga, 3, 16, top_down=True)),
+            ("rgb15.tga", tga_bytes(c16, 2, 16)),
+            ("rle_bgr24.tga", tga_bytes(bgr_runs, 10, 24)),
+            ("rle_grey8.tga", tga_bytes(grey_runs, 11, 8, top_down=True)),
+            ("pal24.tga", tga_bytes(idx_bad, 1, 8, palette=pal24, pal_bits=24)),
+            ("rle_pal32.tga", tga_bytes((runs * 3).astype(np.uint8), 9, 8, palette=pal32, pal_bits=32)),
+            ("pal16.tga", tga_bytes((idx % 20).astype(np.uint8), 1, 8, palette=pal16, pal_bits=16))]
+
+
+def _lzw_codes(indices, min_size):
+    """GIF LZW codes with the widths a reader uses: (code, width) pairs."""
+    clear, end = 1 << min_size, (1 << min_size) + 1
+    out = []
+    size = min_size + 1
+    table, nxt, avail, k = {}, clear + 2, clear + 2, 0
+
+    def reset():
+        nonlocal table, nxt, avail, size, k
+        table = {(i,): i for i in range(clear)}
+        nxt, avail, size, k = clear + 2, clear + 2, min_size + 1, 0
+
+    def emit(code):
+        nonlocal avail, size, k
+        out.append((code, size))
+        k += 1
+        if k >= 2:  # the reader adds an entry for every code after the first
+            avail += 1
+            if (avail & ((1 << size) - 1)) == 0 and avail <= 0xfff:
+                size += 1
+
+    out.append((clear, size))
+    reset()
+    w = ()
+    for c in indices:
+        wc = w + (int(c),)
+        if wc in table:
+            w = wc
+            continue
+        emit(table[w])
+        table[wc] = nxt
+        nxt += 1
+        w = (int(c),)
+        if nxt >= 4000:
+            emit(table[w])
+            w = ()
+            out.append((clear, size))
+            reset()
+    if w:
+        emit(table[w])
+    out.append((end, size))
+    return out
+
+
+def _gif_raster(indices, min_size):
+    acc = nbits = 0
+    data = bytearray()
+    for code, width in _lzw_codes(indices, min_size):
+        acc |= code << nbits
+        nbits += width
+        while nbits >= 8:
+            data.append(acc & 0xff)
+            acc >>= 8
+            nbits -= 8
+    if nbits:
+        data.append(acc & 0xff)
+    blocks = b"".join(bytes([len(data[i:i + 255])]) + bytes(data[i:i + 255]) for i in range(0, len(data), 255))
+    return bytes([min_size]) + blocks + b"\0"
+
+
+def gif_bytes(W, H, gpal=None, bg=0, frame=None, gce=None, exts=()):
+    """frame: (x, y, idx (h, w), lpal or None, interlaced)."""
+    def table_bits(pal):
+        n = 2
+        k = 0
+        while n < len(pal):
+            n *= 2
+            k += 1
+        return k, n
+
+    out = b"GIF89a" + struct.pack("<HH", W, H)
+    if gpal is not None:
+        k, n = table_bits(gpal)
+        out += bytes([0x80 | k, bg, 0])
+        out += np.asarray(gpal, np.uint8).tobytes() + b"\0" * (3 * (n - len(gpal)))
+    else:
+        out += bytes([0, bg, 0])
+    for e in exts:
+        out += e
+    if gce is not None:  # (transparent index or None)
+        out += b"\x21\xf9\x04" + bytes([1 if gce[0] is not None else 0]) + b"\0\0" + \
+            bytes([gce[0] or 0]) + b"\0"
+    x, y, idx, lpal, interlaced = frame
+    h, w = idx.shape
+    flags = 0x40 if interlaced else 0
+    pal_used = gpal
+    if lpal is not None:
+        k, n = table_bits(lpal)
+        flags |= 0x80 | k
+        pal_used = lpal
+    out += b"\x2c" + struct.pack("<HHHH", x, y, w, h) + bytes([flags])
+    if lpal is not None:
+        out += np.asarray(lpal, np.uint8).tobytes() + b"\0" * (3 * (n - len(lpal)))
+    rows = list(range(h))
+    if interlaced:
+        rows = list(range(0, h, 8)) + list(range(4, h, 8)) + list(range(2, h, 4)) + list(range(1, h, 2))
+    seq = np.concatenate([idx[r] for r in rows])
+    min_size = max(2, int(np.ceil(np.log2(max(len(pal_used), 2)))))
+    return out + _gif_raster(seq, min_size) + b"\x3b"
+
+
+def gif_cases():
+    rng = np.random.default_rng(23)
+    pal = rng.integers(0, 256, (256, 3), np.uint8)
+    noisy = rng.integers(0, 256, (70, 64), np.uint8)  # the code table fills and restarts
+    smooth = (np.add.outer(np.arange(21), np.arange(17)) // 3 % 16).astype(np.uint8)
+    two = rng.integers(0, 2, (9, 14), np.uint8)
+    comment = b"\x21\xfe\x05hello\x00"
+    app = b"\x21\xff\x0bNETSCAPE2.0\x03\x01\x00\x00\x00"
+    return [("noisy256.gif", gif_bytes(64, 70, pal, frame=(0, 0, noisy, None, False))),
+            ("interlaced.gif", gif_bytes(17, 21, pal[:16], frame=(0, 0, smooth, None, True), exts=(comment,))),
+            ("local_transparent.gif", gif_bytes(17, 21, None, frame=(0, 0, smooth, pal[16:32], False),
+                                                gce=(5,), exts=(app,))),
+            ("sub_frame_bg.gif", gif_bytes(20, 15, pal[:32], bg=7, frame=(3, 2, smooth[:9, :11] + 8, None, False),
+                                           gce=(9,))),
+            ("two_colour.gif", gif_bytes(14, 9, pal[100:102], frame=(0, 0, two, None, False)))]
+
+
+def _psd_rle_row(row):
+    out, i, n = bytearray(), 0, len(row)
+    while i < n:
+        j = i
+        while j + 1 < n and row[j + 1] == row[i] and j - i < 127:
+            j += 1
+        if j > i:
+            out += bytes([257 - (j - i + 1), row[i]])
+            i = j + 1
+            continue
+        j = i
+        while j + 1 < n and row[j + 1] != row[j] and j - i < 127:
+            j += 1
+        out += bytes([j - i]) + bytes(row[i:j + 1])
+        i = j + 1
+    return bytes(out)
+
+
+def psd_bytes(planes, depth=8, rle=False):
+    """planes: (c, h, w) channel planes (uint8, or uint16 for depth 16)."""
+    c, h, w = planes.shape
+    head = b"8BPS" + struct.pack(">H", 1) + b"\0" * 6 + struct.pack(">HIIHH", c, h, w, depth, 3)
+    head += struct.pack(">I", 0) + struct.pack(">I", 6) + b"\0" * 6 + struct.pack(">I", 0)
+    if not rle:
+        body = planes.astype(">u2" if depth == 16 else np.uint8).tobytes()
+        return head + struct.pack(">H", 0) + body
+    rows = [_psd_rle_row(bytes(planes[k, y].astype(np.uint8))) for k in range(c) for y in range(h)]
+    counts = b"".join(struct.pack(">H", len(r)) for r in rows)
+    return head + struct.pack(">H", 1) + counts + b"".join(rows)
+
+
+def psd_cases():
+    rng = np.random.default_rng(24)
+    rgb = rng.integers(0, 256, (3, 5, 7), np.uint8)
+    rgba = rng.integers(0, 256, (4, 6, 5), np.uint8)
+    rgba[3, 0, :3] = [0, 255, 128]
+    runs = rng.integers(0, 3, (5, 6, 40)).astype(np.uint8) * 80
+    deep = rng.integers(0, 65536, (4, 3, 4)).astype(np.uint16)
+    one = rng.integers(0, 256, (1, 4, 4), np.uint8)
+    return [("rgb8.psd", psd_bytes(rgb)),
+            ("rgba8_matte.psd", psd_bytes(rgba)),
+            ("rle5.psd", psd_bytes(runs, rle=True)),
+            ("rgba16.psd", psd_bytes(deep, depth=16)),
+            ("one_channel.psd", psd_bytes(one))]
+
+
+def pic_bytes(img, packets):
+    """img: (h, w, 4) RGBA; packets: [(channel mask, type)], chained in order.
+    Types: 0 raw, 1 pure run-length, 2 mixed run-length."""
+    h, w = img.shape[:2]
+    head = bytes([0x53, 0x80, 0xF6, 0x34]) + struct.pack(">f", 3.71) + b"kagayaki".ljust(80, b"\0") + b"PICT"
+    head += struct.pack(">HHfHH", w, h, 1.0, 3, 0)
+    for i, (ch, t) in enumerate(packets):
+        head += bytes([1 if i + 1 < len(packets) else 0, 8, t, ch])
+    sel = lambda ch: [k for k in range(4) if ch & (0x80 >> k)]  # noqa: E731
+    body = bytearray()
+    for y in range(h):
+        for ch, t in packets:
+            ks = sel(ch)
+            vals = [bytes(img[y, x, ks]) for x in range(w)]
+            if t == 0:
+                body += b"".join(vals)
+            elif t == 1:
+                x = 0
+                while x < w:
+                    n = 1
+                    while x + n < w and vals[x + n] == vals[x] and n < 255:
+                        n += 1
+                    body += bytes([n]) + vals[x]
+                    x += n
+            else:
+                x = 0
+                while x < w:
+                    n = 1
+                    while x + n < w and vals[x + n] == vals[x] and n < 300:
+                        n += 1
+                    if n >= 2:
+                        body += (bytes([n + 127]) if n <= 127 else b"\x80" + struct.pack(">H", n)) + vals[x]
+                        x += n
+                    else:
+                        m = 1
+                        while x + m < w and m < 128 and (x + m + 1 >= w or vals[x + m + 1] != vals[x + m]):
+                            m += 1
+                        body += bytes([m - 1]) + b"".join(vals[x:x + m])
+                        x += m
+    return head + bytes(body)
+
+
+def pic_cases():
+    rng = np.random.default_rng(25)
+    img = rng.integers(0, 256, (5, 9, 4), np.uint8)
+    runs = (rng.integers(0, 3, (6, 150, 4)) * 100).astype(np.uint8)
+    runs[:, :140] = runs[:, :1]  # long runs: the 16-bit count form
+    return [("raw_rgb.pic", pic_bytes(img, [(0xE0, 0)])),
+            ("pure_rle_rgba.pic", pic_bytes(runs[:, :20], [(0xE0, 1), (0x10, 1)])),
+            ("mixed_rle_rgba.pic", pic_bytes(runs, [(0xF0, 2)])),
+            ("split_channels.pic", pic_bytes(img, [(0x80, 0), (0x60, 2), (0x10, 1)]))]
+
+
 def image_cases():
-    return png_cases() + hdr_cases() + pnm_cases() + jpeg_cases()
+    return png_cases() + hdr_cases() + pnm_cases() + jpeg_cases() + bmp_cases() + tga_cases() + gif_cases() + \
+        psd_cases() + pic_cases()
 
 
 # ---------------------------------------------------------------------------

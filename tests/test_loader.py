@@ -100,6 +100,31 @@ def test_errors(tmp_path):
         load_image(tmp_path / "x.jpg")
 
 
+def test_image_format_errors(tmp_path):
+    """The cases stb_image rejects are errors here too (no partial image)."""
+    rng = np.random.default_rng(3)
+    rgb = rng.integers(0, 256, (4, 5, 3), np.uint8)
+    bmp = bytearray(scene_files.bmp_bytes(rgb, 24))
+    bmp[30:34] = (1).to_bytes(4, "little")  # BI_RLE8
+    cases = [("rle.bmp", bytes(bmp), "RLE"),
+             ("gap.bmp", bytes(bmp[:10]) + (60).to_bytes(4, "little") + bytes(bmp[14:30]) + bytes(4) +
+              bytes(bmp[34:54]) + bytes(6) + bytes(bmp[54:]), "offset"),
+             ("cmyk.psd", scene_files.psd_bytes(rng.integers(0, 256, (4, 3, 3), np.uint8))[:24] +
+              (4).to_bytes(2, "big") + scene_files.psd_bytes(rng.integers(0, 256, (4, 3, 3), np.uint8))[26:],
+              "RGB"),
+             ("noclear.gif", b"GIF89a\x02\x00\x02\x00\x80\x00\x00" + bytes(6) +
+              b"\x2c\x00\x00\x00\x00\x02\x00\x02\x00\x00\x02\x02\x01\x00\x00\x3b", "clear code"),
+             ("empty.gif", b"GIF89a\x02\x00\x02\x00\x00\x00\x00\x3b", "no image"),
+             ("shortpal.tga", scene_files.tga_bytes(rng.integers(0, 4, (3, 3), np.uint8), 1, 8,
+                                                    palette=rng.integers(0, 256, (4, 3), np.uint8),
+                                                    pal_bits=24)[:24], "palette"),
+             ("noise.bin", bytes(rng.integers(0, 256, 64, np.uint8)) + b"", "unknown image format")]
+    for name, data, msg in cases:
+        (tmp_path / name).write_bytes(data)
+        with pytest.raises(KgkError, match=msg):
+            load_image(tmp_path / name)
+
+
 def test_parallel_parse_is_independent_of_threads(tmp_path):
     """The chunked parallel parse (relative indices, groups, materials and
     smoothing groups crossing chunk boundaries, mixed line ends) gives the
