@@ -492,6 +492,11 @@ kgk_status kgk_nrc_loss_scale(kgk_scene *scene, float *scale);
 kgk_status kgk_tonemap_rgba8(const kgk_vec *img, int32_t width, int32_t height, uint8_t *out);
 /* Writes the tone-mapped image as an RGBA8 PNG. */
 kgk_status kgk_save_png(const kgk_vec *img, int32_t width, int32_t height, const char *path);
+/* Writes the image's linear RGB (no tone mapping) as an OpenEXR file: one
+ * part, scanlines without compression, channels B, G, R as FP32 (half == 0)
+ * or FP16 (half != 0, rounded to nearest even, overflow to infinity).  img
+ * may be host or device memory.  No counterpart in the reference. */
+kgk_status kgk_save_exr(const kgk_vec *img, int32_t width, int32_t height, int32_t half, const char *path);
 
 #ifdef __cplusplus
 } /* extern "C" */

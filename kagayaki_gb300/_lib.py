@@ -58,6 +58,7 @@ PROTOTYPES = {
     "kgk_image_free": (None, [_vp]),
     "kgk_tonemap_rgba8": (_st, [_vp, _i32, _i32, _vp]),
     "kgk_save_png": (_st, [_vp, _i32, _i32, ctypes.c_char_p]),
+    "kgk_save_exr": (_st, [_vp, _i32, _i32, _i32, ctypes.c_char_p]),
 }
 
 _lib = None

@@ -291,6 +291,14 @@ def tonemap(img):
     return out
 
 
+def save_exr(img, path, half=False):
+    """kgk_save_exr: the linear RGB of a (height, width, 4) float32 host image
+    as an uncompressed OpenEXR file, FP32 or (half=True) FP16 channels."""
+    img = np.ascontiguousarray(img, np.float32)
+    h, w = img.shape[:2]
+    check(lib().kgk_save_exr(_p(img), w, h, int(bool(half)), str(path).encode()))
+
+
 def save_png(img, path):
     img = np.ascontiguousarray(img, np.float32)
     h, w = img.shape[:2]

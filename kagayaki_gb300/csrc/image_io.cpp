@@ -166,3 +166,117 @@ kgk_status kgk_save_png(const kgk_vec *img, int32_t w, int32_t h, const char *pa
 }
 
 }  // extern "C"
+
+// OpenEXR output: a single-part scanline file, no compression, channels B, G,
+// R (the spec's alphabetical order) as FP32 or FP16, linear values as given.
+// No counterpart in the reference (it writes PNG only).
+namespace {
+
+// FP32 -> FP16, round to nearest even; overflow to infinity, NaN kept quiet.
+uint16_t to_half(float f) {
+    uint32_t x;
+    memcpy(&x, &f, 4);
+    const uint32_t sign = (x >> 16) & 0x8000u;
+    const uint32_t ax = x & 0x7fffffffu;
+    if (ax >= 0x7f800000u) return (uint16_t)(sign | 0x7c00u | (ax > 0x7f800000u ? 0x200u | ((ax >> 13) & 0x3ffu) : 0u));
+    if (ax >= 0x477ff000u) return (uint16_t)(sign | 0x7c00u);  // rounds to >= 65520: infinity
+    if (ax < 0x38800000u) {                                    // below the smallest normal half
+        if (ax < 0x33000000u) return (uint16_t)sign;            // below half of the smallest subnormal
+        const uint32_t e = ax >> 23, m = (ax & 0x7fffffu) | 0x800000u;
+        const uint32_t shift = 126u - e;                        // 14..24
+        const uint32_t q = m >> shift, rem = m & ((1u << shift) - 1u), half = 1u << (shift - 1u);
+        const uint32_t r = q + (rem > half || (rem == half && (q & 1u)));
+        return (uint16_t)(sign | r);
+    }
+    const uint32_t base = ax - 0x38000000u;  // rebias 127 -> 15
+    const uint32_t q = base >> 13, rem = base & 0x1fffu;
+    const uint32_t r = q + (rem > 0x1000u || (rem == 0x1000u && (q & 1u)));
+    return (uint16_t)(sign | r);
+}
+
+void put_le(std::vector<uint8_t> &v, uint64_t x, int bytes) {
+    for (int i = 0; i < bytes; ++i) v.push_back((uint8_t)(x >> (8 * i)));
+}
+
+void attr(std::vector<uint8_t> &v, const char *name, const char *type, const std::vector<uint8_t> &val) {
+    v.insert(v.end(), name, name + strlen(name) + 1);
+    v.insert(v.end(), type, type + strlen(type) + 1);
+    put_le(v, val.size(), 4);
+    v.insert(v.end(), val.begin(), val.end());
+}
+
+}  // namespace
+
+extern "C" kgk_status kgk_save_exr(const kgk_vec *img, int32_t w, int32_t h, int32_t half, const char *path) {
+    if (!path || !img) return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_save_exr: NULL argument");
+    if (w <= 0 || h <= 0) return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_save_exr: empty image");
+    const size_t n = (size_t)w * h;
+    std::vector<kgk_vec> host;
+    const kgk_vec *src = img;
+    if (is_device_ptr(img)) {
+        host.resize(n);
+        KGK_CUDA(cudaMemcpy(host.data(), img, n * sizeof(kgk_vec), cudaMemcpyDeviceToHost));
+        src = host.data();
+    }
+    const int ptype = half ? 1 : 2, bpc = half ? 2 : 4;
+    std::vector<uint8_t> out = {0x76, 0x2f, 0x31, 0x01, 2, 0, 0, 0};
+    std::vector<uint8_t> v;
+    for (const char *ch : {"B", "G", "R"}) {
+        v.insert(v.end(), ch, ch + 2);
+        put_le(v, (uint64_t)ptype, 4);
+        v.insert(v.end(), {0, 0, 0, 0});  // pLinear, reserved
+        put_le(v, 1, 4);
+        put_le(v, 1, 4);
+    }
+    v.push_back(0);
+    attr(out, "channels", "chlist", v);
+    attr(out, "compression", "compression", {0});
+    v.clear();
+    for (int32_t c : {0, 0, w - 1, h - 1}) put_le(v, (uint32_t)c, 4);
+    attr(out, "dataWindow", "box2i", v);
+    attr(out, "displayWindow", "box2i", v);
+    attr(out, "lineOrder", "lineOrder", {0});
+    v.clear();
+    const float one = 1.0f, zero = 0.0f;
+    uint32_t bits;
+    memcpy(&bits, &one, 4);
+    put_le(v, bits, 4);
+    attr(out, "pixelAspectRatio", "float", v);
+    v.clear();
+    memcpy(&bits, &zero, 4);
+    put_le(v, bits, 4);
+    put_le(v, bits, 4);
+    attr(out, "screenWindowCenter", "v2f", v);
+    v.clear();
+    memcpy(&bits, &one, 4);
+    put_le(v, bits, 4);
+    attr(out, "screenWindowWidth", "float", v);
+    out.push_back(0);  // end of header
+    const size_t line_bytes = (size_t)w * 3 * bpc;
+    const size_t table = out.size(), first = table + 8 * (size_t)h;
+    for (int y = 0; y < h; ++y) put_le(out, first + (size_t)y * (8 + line_bytes), 8);
+    out.reserve(first + (size_t)h * (8 + line_bytes));
+    for (int y = 0; y < h; ++y) {
+        put_le(out, (uint32_t)y, 4);
+        put_le(out, line_bytes, 4);
+        const kgk_vec *row = src + (size_t)y * w;
+        for (int c = 0; c < 3; ++c) {  // B, G, R
+            for (int x = 0; x < w; ++x) {
+                const float f = c == 0 ? row[x].z : (c == 1 ? row[x].y : row[x].x);
+                if (half) {
+                    put_le(out, to_half(f), 2);
+                } else {
+                    memcpy(&bits, &f, 4);
+                    put_le(out, bits, 4);
+                }
+            }
+        }
+    }
+    FILE *f = fopen(path, "wb");
+    if (!f) return fail(KGK_ERR_IO, std::string("kgk_save_exr: cannot open ") + path);
+    const size_t wr = fwrite(out.data(), 1, out.size(), f);
+    const int cl = fclose(f);
+    if (wr != out.size() || cl != 0) return fail(KGK_ERR_IO, std::string("kgk_save_exr: write failed for ") + path);
+    return KGK_OK;
+}
+

@@ -153,3 +153,18 @@ def test_svgf_output_needs_a_kept_frame():
             s.svgf_output(cfg, rgba8=np.empty((H, W, 4), np.uint8))
         with pytest.raises(KgkError, match="no output"):
             s.svgf_output(cfg)
+
+
+def test_exr_from_device_memory_equals_host(tmp_path):
+    """kgk_save_exr from a device image writes the same file as from the host copy."""
+    torch = pytest.importorskip("torch")
+    import ctypes
+    from kagayaki_gb300 import save_exr
+    from kagayaki_gb300._lib import check, lib
+    rng = np.random.default_rng(5)
+    img = rng.lognormal(0, 2, (24, 31, 4)).astype(np.float32)
+    dev = torch.from_numpy(img).cuda()
+    for half in (0, 1):
+        save_exr(img, tmp_path / "host.exr", half=bool(half))
+        check(lib().kgk_save_exr(ctypes.c_void_p(dev.data_ptr()), 31, 24, half, str(tmp_path / "dev.exr").encode()))
+        assert (tmp_path / "host.exr").read_bytes() == (tmp_path / "dev.exr").read_bytes()
