@@ -23,12 +23,15 @@
 #include <cstring>
 #include <vector>
 
+#include <cooperative_groups.h>
+
 #include "kgk_nrc.h"
 #include "kgk_scene.h"
 #include "shading.cuh"
 #include "traverse.cuh"
 
 namespace kgk {
+namespace cg = cooperative_groups;
 
 // Device bytes per path in flight (ensure_wave): two buffers of state (4
 // float4, rng, depth, id), the final radiance and the hit (float4 each), the
@@ -80,6 +83,11 @@ struct RenderState {
     float *ttgt = nullptr;                    // training targets (3 per record)
     int tcap = 0;
     int qrec_cap = 0;                         // paths the cache arrays above hold
+    // deferred tail shadow rays (kDeferSlots slots)
+    float4 *td_o = nullptr, *td_d = nullptr, *td_c = nullptr;
+    int *td_list = nullptr;
+    unsigned *td_mask = nullptr;
+    unsigned char *td_vis = nullptr;
     // device bytes held for `cap` paths (they count as available when sizing the wave)
     size_t cap_bytes_held() const { return (size_t)cap * kPathStateBytes + (size_t)qrec_cap * kCachePathBytes; }
     int sms = 0;
@@ -95,7 +103,7 @@ namespace {
 // queues), cache record counts.
 enum Cnt {
     kA0 = 0, kA1 = 1, kSH0 = 2, kSH1 = 3, kFE = 4, kFS0 = 5, kFS1 = 6, kMQ = 7, kLQ = 8, kDQ = 9, kQN = 10,
-    kTN = 11, kNCnt = 12
+    kTN = 11, kTD = 12, kTDF = 13, kNCnt = 14
 };
 // Lanes of a warp that must be idle before the warp fetches new rays.
 constexpr int kRefill = 8;
@@ -106,6 +114,13 @@ constexpr int kQRec = 20;
 enum Stat { kRaysC = 0, kRaysS = 1, kOverflow = 2, kNodes = 3, kTris = 4, kRaysT = 5, kNStat = 8 };
 // Paths few enough to finish in the tail kernel (one thread per path).
 constexpr int kTailPaths = 1 << 17;
+// Deferred shadow rays of the tail (unbiased estimator without the cache):
+// the first kDeferBounces bounces of a tail path leave their face-light and
+// environment shadow rays in fixed slots (path, bounce, kind) instead of
+// tracing them on the path's chain; a parallel pass traces them and another
+// adds the visible contributions in slot order.
+constexpr int kDeferBounces = 16;
+constexpr size_t kDeferSlots = (size_t)kTailPaths * kDeferBounces * 2;
 
 struct Params {
     DevScene sc;
@@ -127,6 +142,11 @@ struct Params {
     float4 *gb_pos, *gb_nrm, *gb_alb, *gb_emi;
     int *cnt;
     unsigned long long *stats;
+    // deferred tail shadow rays (null: traced inline)
+    float4 *td_o, *td_d, *td_c;
+    int *td_list;
+    unsigned *td_mask;
+    unsigned char *td_vis;
     // radiance cache
     int use_cache;
     float *qrec, *trec;
@@ -957,14 +977,31 @@ __global__ void __launch_bounds__(128) k_shade(Params P, const int *__restrict__
 // so the radiance sums are the same) - instead of four kernel launches per
 // bounce that each wait for their slowest ray.  A path runs at most `bounces`
 // more bounces, the wavefront's limit.
+// One deferred shadow record: slot (path i, bounce k, kind j) and its id in
+// the list (warp-aggregated append; the list order does not matter).
+__device__ __forceinline__ void defer_shadow(const Params &P, int i, int k, int j, float3 org, float3 dir,
+                                             float tmax, float3 c) {
+    const size_t slot = ((size_t)i * kDeferBounces + k) * 2 + j;
+    P.td_o[slot] = make_float4(org.x, org.y, org.z, tmax);
+    P.td_d[slot] = make_float4(dir.x, dir.y, dir.z, 0.0f);
+    P.td_c[slot] = make_float4(c.x, c.y, c.z, 0.0f);
+    cg::coalesced_group g = cg::coalesced_threads();
+    int base = 0;
+    if (g.thread_rank() == 0) base = atomicAdd(&P.cnt[kTD], (int)g.size());
+    base = g.shfl(base, 0);
+    P.td_list[base + (int)g.thread_rank()] = (int)slot;
+}
+
 template <int kEst>
 __global__ void __launch_bounds__(128) k_tail(Params P, int cnt_idx, int dense_n, int bounces) {
     const int n = cnt_idx >= 0 ? P.cnt[cnt_idx] : dense_n;
     const DevScene &s = P.sc;
     const bool cache = P.use_cache != 0;
+    const bool defer = kEst == KGK_ESTIMATOR_UNBIASED && P.td_o != nullptr && n <= kTailPaths;
     unsigned rays_c = 0, rays_s = 0, overflow = 0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         PathState ps = load_path(P.cur, i, cache);
+        unsigned dmask = 0;  // bit 2k + j: deferred record (bounce k, kind j)
         for (int k = 0; k < bounces; ++k) {
             const RayPre r = make_ray(ps.o, ps.d);
             float bt = kBigT, u = 0.0f, v = 0.0f;
@@ -978,6 +1015,17 @@ __global__ void __launch_bounds__(128) k_tail(Params P, int cnt_idx, int dense_n
             ShadeOut so{};
             if (kEst == KGK_ESTIMATOR_COMPAT) shade_compat_core(P, ps, h, so);
             else shade_unbiased_core(P, ps, h, so);
+            if (defer && k < kDeferBounces) {
+                if (so.f_pred) {
+                    defer_shadow(P, i, k, 0, so.f_org, so.f_dir, so.f_tmax, so.f_c);
+                    dmask |= 1u << (2 * k);
+                }
+                if (so.e_pred) {
+                    defer_shadow(P, i, k, 1, so.spos, so.e_dir, kBigT, so.e_c);
+                    dmask |= 2u << (2 * k);
+                }
+                so.f_pred = so.e_pred = false;
+            }
             if (so.f_pred) {
                 const RayPre rs = make_ray(so.f_org, so.f_dir);
                 bool vis;
@@ -1004,6 +1052,7 @@ __global__ void __launch_bounds__(128) k_tail(Params P, int cnt_idx, int dense_n
             if (!so.cont) break;
         }
         P.fin[ps.id] = make_float4(ps.rad.x, ps.rad.y, ps.rad.z, 0.0f);
+        if (defer) P.td_mask[i] = dmask;
     }
     warp_add_u64(&P.stats[kRaysC], rays_c);
     warp_add_u64(&P.stats[kRaysS], rays_s);
@@ -1017,6 +1066,77 @@ __global__ void k_flush(Params P, int cnt_idx) {
     const int n = P.cnt[cnt_idx];
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
         P.fin[P.cur.id[i]] = P.cur.rad[i];
+}
+
+// The tail's deferred shadow rays (any-hit: nothing in (kTMin, range)), from
+// the list of filled slots, lanes refilled like k_extend's; the visibility
+// of slot s goes to td_vis[s].
+__global__ void __launch_bounds__(128) k_tail_shadow(Params P) {
+    const int n = P.cnt[kTD];
+    const DevScene &s = P.sc;
+    int *fetch = &P.cnt[kTDF];
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned lt = (1u << lane) - 1u;
+    bool active = false, exhausted = false;
+    int slot = 0;
+    unsigned rays = 0;
+    RayPre r;
+    Trav c;
+    TravStack stk;
+    TravStats st{0, 0, 0};
+    while (true) {
+        const unsigned idle = __ballot_sync(~0u, !active);
+        if (!exhausted && __popc(idle) >= kRefill) {
+            int base = 0;
+            if (lane == 0) base = atomicAdd(fetch, __popc(idle));
+            base = __shfl_sync(~0u, base, 0);
+            if (base + __popc(idle) >= n) exhausted = true;
+            if (!active) {
+                const int i = base + __popc(idle & lt);
+                if (i < n) {
+                    slot = P.td_list[i];
+                    const float4 o = P.td_o[slot], d = P.td_d[slot];
+                    r = make_ray(f3(o), f3(d));
+                    trav_init(c, o.w);
+                    active = true;
+                }
+            }
+        }
+        if (!__any_sync(~0u, active)) break;
+        if (active && trav_step<false>(s.nodes, (unsigned)s.n_nodes, s.tri_rec, (unsigned)s.n_tris, r, c, stk, true,
+                                       st)) {
+            active = false;
+            ++rays;
+            P.td_vis[slot] = c.hit_slot < 0 ? 1 : 0;
+        }
+    }
+    warp_add_u64(&P.stats[kRaysS], rays);
+    warp_add_u64(&P.stats[kOverflow], st.overflow);
+}
+
+// Adds each tail path's visible deferred contributions to its radiance, in
+// slot order (bounce by bounce, face light before environment): the same sum
+// on every run.
+__global__ void k_tail_resolve(Params P, int cnt_idx, int dense_n) {
+    const int n = min(cnt_idx >= 0 ? P.cnt[cnt_idx] : dense_n, kTailPaths);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        unsigned m = P.td_mask[i];
+        if (!m) continue;
+        const int id = P.cur.id[i];
+        float4 rad = P.fin[id];
+        while (m) {
+            const int b = __ffs(m) - 1;
+            m &= m - 1u;
+            const size_t slot = (size_t)i * kDeferBounces * 2 + b;
+            if (P.td_vis[slot]) {
+                const float4 cc = P.td_c[slot];
+                rad.x += cc.x;
+                rad.y += cc.y;
+                rad.z += cc.z;
+            }
+        }
+        P.fin[id] = rad;
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -1183,6 +1303,17 @@ kgk_status ensure_wave(RenderState &R, int cap, bool cache) {
     return KGK_OK;
 }
 
+kgk_status ensure_tail_defer(RenderState &R) {
+    if (R.td_o) return KGK_OK;
+    KGK_TRY(ensure(&R.td_o, kDeferSlots, "deferred shadow rays"));
+    KGK_TRY(ensure(&R.td_d, kDeferSlots, "deferred shadow rays"));
+    KGK_TRY(ensure(&R.td_c, kDeferSlots, "deferred shadow rays"));
+    KGK_TRY(ensure(&R.td_list, kDeferSlots, "deferred shadow rays"));
+    KGK_TRY(ensure(&R.td_vis, kDeferSlots, "deferred shadow rays"));
+    KGK_TRY(ensure(&R.td_mask, (size_t)kTailPaths, "deferred shadow rays"));
+    return KGK_OK;
+}
+
 kgk_status ensure_train(RenderState &R, int tcap) {
     if (R.tcap >= tcap) return KGK_OK;
     KGK_TRY(ensure(&R.trec, (size_t)tcap * kQRec, "cache training records"));
@@ -1198,7 +1329,8 @@ void render_state_free(kgk_scene *s) {
     if (!R) return;
     void *ptrs[] = {R->seeds, R->frame, R->kept, R->acc_sum, R->acc_sq, R->gb_pos, R->gb_nrm, R->gb_alb, R->gb_emi,
                     R->fin, R->hit, R->mq, R->lq, R->dq, R->sh_o[0], R->sh_o[1], R->sh_d[0], R->sh_d[1], R->sh_c[0],
-                    R->sh_c[1], R->cnt, R->stats, R->qrec, R->trec, R->ttgt};
+                    R->sh_c[1], R->cnt, R->stats, R->qrec, R->trec, R->ttgt, R->td_o, R->td_d, R->td_c,
+                    R->td_list, R->td_mask, R->td_vis};
     for (void *p : ptrs) dfree(p);
     for (PathBuf &b : R->pb) {
         void *bp[] = {b.o, b.d, b.thr, b.rad, b.rng, b.depth, b.id, b.spread, b.pflags};
@@ -1317,6 +1449,19 @@ kgk_status kgk_render(kgk_scene *s, const kgk_camera *cam, const kgk_camera *pre
     P.cnt = R.cnt;
     P.stats = R.stats;
     P.use_cache = cfg->use_cache ? 1 : 0;
+    P.td_o = P.td_d = P.td_c = nullptr;
+    P.td_list = nullptr;
+    P.td_mask = nullptr;
+    P.td_vis = nullptr;
+    if (cfg->estimator != KGK_ESTIMATOR_COMPAT && !P.use_cache) {
+        KGK_TRY(ensure_tail_defer(R));
+        P.td_o = R.td_o;
+        P.td_d = R.td_d;
+        P.td_c = R.td_c;
+        P.td_list = R.td_list;
+        P.td_mask = R.td_mask;
+        P.td_vis = R.td_vis;
+    }
     if (P.use_cache) {
         const kgk_nrc_config &nc = s->nrc->cfg;
         KGK_TRY(ensure_train(R, nc.train_paths));
@@ -1372,10 +1517,17 @@ kgk_status kgk_render(kgk_scene *s, const kgk_camera *cam, const kgk_camera *pre
         auto launch_tail = [&](int cnt_idx, int dense_n, int bounces, int threads) -> kgk_status {
             KGK_TRY(stage_begin(3));
             const int tg = std::max(1, std::min((threads + 127) / 128, R.sms * 16));
-            if (cfg->estimator == KGK_ESTIMATOR_COMPAT)
+            if (cfg->estimator == KGK_ESTIMATOR_COMPAT) {
                 k_tail<KGK_ESTIMATOR_COMPAT><<<tg, 128, 0, st>>>(P, cnt_idx, dense_n, bounces);
-            else
+            } else {
+                if (P.td_o) KGK_CUDA(cudaMemsetAsync(R.cnt + kTD, 0, 2 * sizeof(int), st));
                 k_tail<KGK_ESTIMATOR_UNBIASED><<<tg, 128, 0, st>>>(P, cnt_idx, dense_n, bounces);
+                if (P.td_o) {
+                    k_tail_shadow<<<grid, 128, 0, st>>>(P);
+                    k_tail_resolve<<<tg, 128, 0, st>>>(P, cnt_idx, dense_n);
+                    launches += 2;
+                }
+            }
             KGK_TRY(stage_end());
             KGK_CUDA(cudaGetLastError());
             ++launches;
