@@ -19,6 +19,8 @@
 namespace kgk {
 
 constexpr int kTravStack = 32;
+// Node visits a resumable traversal step may make before it tests triangles.
+constexpr int kNodesPerStep = 2;
 // Conservative widening of box exit distances: 1 + 2 * gamma(3) covers the
 // rounding of the quantised plane, the origin offset and the multiply.
 constexpr float kBoxWiden = 1.0000004f;
@@ -327,7 +329,12 @@ __device__ __forceinline__ bool trav_step(const WideNode *__restrict__ nodes, un
                                           const float4 *__restrict__ tri, unsigned n_tris, const RayPre &r,
                                           Trav &c, TravStack &stk, bool any_mode, TravStats &st) {
     uint2 tg = make_uint2(0u, 0u);
-    if (c.group.y & 0xff000000u) {
+#pragma unroll 1
+    for (int visit = 0; visit < kNodesPerStep && tg.y == 0u; ++visit) {
+        if ((c.group.y & 0xff000000u) == 0u) {
+            if (c.sp == 0) break;
+            c.group = stk.e[--c.sp];
+        }
         const unsigned hits_imask = c.group.y;
         const int child_bit = 31 - __clz(hits_imask & 0xff000000u);
         const unsigned base = c.group.x;
@@ -347,9 +354,6 @@ __device__ __forceinline__ bool trav_step(const WideNode *__restrict__ nodes, un
         const unsigned imask = __float_as_uint(n0.w) >> 24;
         c.group = make_uint2(__float_as_uint(n1.x), (hm & 0xff000000u) | imask);
         tg = make_uint2(__float_as_uint(n1.y), hm & 0x00ffffffu);
-    } else {
-        tg = c.group;
-        c.group = make_uint2(0u, 0u);
     }
     while (tg.y != 0u) {
         const int k = __ffs(tg.y) - 1;
