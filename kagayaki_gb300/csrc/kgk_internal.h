@@ -148,6 +148,7 @@ kgk_status bvh_validate(const DevScene &s, cudaStream_t st);
 
 struct TraceCounters {
     unsigned long long rays, overflows, nodes, tris;
+    unsigned long long fetch;  // next ray to hand out (persistent kernels)
 };
 kgk_status trace_closest_dev(const DevScene &s, const kgk_ray *rays, size_t n, int32_t *id,
                              float *t, bool count, TraceCounters *ctr_dev, cudaStream_t st);

@@ -1,5 +1,8 @@
 // trace.cu - batch closest-hit and occlusion queries (the parity entry
-// points kgk_trace_closest / kgk_trace_any).  One thread per ray.
+// points kgk_trace_closest / kgk_trace_any): persistent kernels, one ray per
+// lane at a time, lanes refilled from a shared counter.
+#include <algorithm>
+
 #include "kgk_internal.h"
 #include "traverse.cuh"
 
@@ -32,42 +35,68 @@ __device__ __forceinline__ void flush_counters(TraceCounters *ctr, unsigned node
     }
 }
 
-template <bool kCount>
-__global__ void __launch_bounds__(128) k_trace_closest(const WideNode *__restrict__ nodes, unsigned n_nodes,
-                                                       const float4 *__restrict__ tri, unsigned n_tris,
-                                                       const kgk_ray *__restrict__ rays, int n,
-                                                       int32_t *id_out, float *t_out,
-                                                       TraceCounters *ctr) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+// Lanes take new rays (one atomic per warp) whenever kRefill or more of them
+// are idle, so a warp does not wait for its longest ray; trav_step keeps the
+// same node and triangle order as trace_closest / trace_any, so the answers
+// are the same.
+constexpr int kRefill = 8;
+
+template <bool kAny, bool kCount>
+__global__ void __launch_bounds__(128) k_trace(const WideNode *__restrict__ nodes, unsigned n_nodes,
+                                               const float4 *__restrict__ tri, unsigned n_tris,
+                                               const kgk_ray *__restrict__ rays, const float *__restrict__ tmax,
+                                               int n, int32_t *id_out, float *t_out, uint8_t *occ,
+                                               TraceCounters *ctr) {
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned lt = (1u << lane) - 1u;
+    bool active = false, exhausted = false;
+    int i = 0;
+    unsigned done = 0;
+    RayPre r;
+    Trav c;
+    TravStack stk;
     TravStats st{0, 0, 0};
-    if (i < n) {
-        float3 o, d;
-        load_ray(rays, i, o, d);
-        const RayPre r = make_ray(o, d);
-        float best_t = kBigT, u = 0.0f, v = 0.0f;
-        int best_id = 0x7fffffff;
-        int slot = trace_closest<kCount>(nodes, n_nodes, tri, n_tris, r, best_t, best_id, u, v, st);
-        id_out[i] = slot >= 0 ? best_id : -1;
-        t_out[i] = slot >= 0 ? best_t : kBigT;
+    while (true) {
+        const unsigned idle = __ballot_sync(~0u, !active);
+        if (!exhausted && __popc(idle) >= kRefill) {
+            int base = 0;
+            if (lane == 0) base = (int)atomicAdd(&ctr->fetch, (unsigned long long)__popc(idle));
+            base = __shfl_sync(~0u, base, 0);
+            if (base + __popc(idle) >= n) exhausted = true;
+            if (!active) {
+                i = base + __popc(idle & lt);
+                if (i < n) {
+                    float3 o, d;
+                    load_ray(rays, i, o, d);
+                    r = make_ray(o, d);
+                    trav_init(c, kAny && tmax ? tmax[i] : kBigT);
+                    active = true;
+                }
+            }
+        }
+        if (!__any_sync(~0u, active)) break;
+        if (active && trav_step<kCount>(nodes, n_nodes, tri, n_tris, r, c, stk, kAny, st)) {
+            active = false;
+            ++done;
+            if (kAny) {
+                occ[i] = c.hit_slot >= 0 ? 1 : 0;
+            } else {
+                id_out[i] = c.hit_slot >= 0 ? c.best_id : -1;
+                t_out[i] = c.hit_slot >= 0 ? c.best_t : kBigT;
+            }
+        }
     }
-    flush_counters(ctr, st.nodes, st.tris, st.overflow, i < n ? 1u : 0u);
+    flush_counters(ctr, st.nodes, st.tris, st.overflow, done);
 }
 
-__global__ void __launch_bounds__(128) k_trace_any(const WideNode *__restrict__ nodes, unsigned n_nodes,
-                                                   const float4 *__restrict__ tri, unsigned n_tris,
-                                                   const kgk_ray *__restrict__ rays,
-                                                   const float *__restrict__ tmax, int n,
-                                                   uint8_t *occ, TraceCounters *ctr) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    TravStats st{0, 0, 0};
-    if (i < n) {
-        float3 o, d;
-        load_ray(rays, i, o, d);
-        const RayPre r = make_ray(o, d);
-        const float tm = tmax ? tmax[i] : kBigT;
-        occ[i] = trace_any<false>(nodes, n_nodes, tri, n_tris, r, tm, st) ? 1 : 0;
+int grid_for(size_t n) {
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) sms = 1;
     }
-    flush_counters(ctr, st.nodes, st.tris, st.overflow, i < n ? 1u : 0u);
+    return (int)std::min<size_t>((size_t)sms * 8, (n + 127) / 128);
 }
 
 }  // namespace
@@ -76,11 +105,13 @@ kgk_status trace_closest_dev(const DevScene &s, const kgk_ray *rays, size_t n, i
                              bool count, TraceCounters *ctr, cudaStream_t st) {
     if (n == 0) return KGK_OK;
     if (n > 0x7fffffff) return fail(KGK_ERR_INVALID_ARGUMENT, "trace: too many rays");
-    const int g = (int)((n + 127) / 128);
+    const int g = grid_for(n);
     if (count)
-        k_trace_closest<true><<<g, 128, 0, st>>>(s.nodes, (unsigned)s.n_nodes, s.tri_rec, (unsigned)s.n_tris, rays, (int)n, id, t, ctr);
+        k_trace<false, true><<<g, 128, 0, st>>>(s.nodes, (unsigned)s.n_nodes, s.tri_rec, (unsigned)s.n_tris, rays,
+                                                 nullptr, (int)n, id, t, nullptr, ctr);
     else
-        k_trace_closest<false><<<g, 128, 0, st>>>(s.nodes, (unsigned)s.n_nodes, s.tri_rec, (unsigned)s.n_tris, rays, (int)n, id, t, ctr);
+        k_trace<false, false><<<g, 128, 0, st>>>(s.nodes, (unsigned)s.n_nodes, s.tri_rec, (unsigned)s.n_tris, rays,
+                                                  nullptr, (int)n, id, t, nullptr, ctr);
     KGK_CUDA(cudaGetLastError());
     return KGK_OK;
 }
@@ -89,8 +120,8 @@ kgk_status trace_any_dev(const DevScene &s, const kgk_ray *rays, const float *tm
                          TraceCounters *ctr, cudaStream_t st) {
     if (n == 0) return KGK_OK;
     if (n > 0x7fffffff) return fail(KGK_ERR_INVALID_ARGUMENT, "trace: too many rays");
-    const int g = (int)((n + 127) / 128);
-    k_trace_any<<<g, 128, 0, st>>>(s.nodes, (unsigned)s.n_nodes, s.tri_rec, (unsigned)s.n_tris, rays, tmax, (int)n, occ, ctr);
+    k_trace<true, false><<<grid_for(n), 128, 0, st>>>(s.nodes, (unsigned)s.n_nodes, s.tri_rec, (unsigned)s.n_tris,
+                                                       rays, tmax, (int)n, nullptr, nullptr, occ, ctr);
     KGK_CUDA(cudaGetLastError());
     return KGK_OK;
 }

@@ -319,7 +319,9 @@ __device__ __forceinline__ void trav_init(Trav &c, float tmax) {
     c.hit_slot = -1;
 }
 
-// Visits one node and the triangles of its hit leaves.  any_mode: stop at the
+// Visits nodes until one has hit leaf triangles (at most kNodesPerStep
+// nodes), then tests those triangles: the same order as trace_closest /
+// trace_any, in fewer, more even steps.  any_mode: stop at the
 // first triangle with kTMin <= t < best_t (occlusion); otherwise keep the
 // closest hit (ties to the smaller id).  Returns true when the traversal is
 // finished; then c.hit_slot is -1 (no hit) or, for the BVH-order triangle ti
