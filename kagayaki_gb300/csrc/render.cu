@@ -227,29 +227,39 @@ __device__ __forceinline__ float3 primary_dir(const kgk_camera &c, int W, int H,
 }
 
 // ---------------------------------------------------------------------------
+// Primary ray of wave path i (pixel i % npx, sample sample_base + i / npx):
+// origin, direction and the path's rng state.
+__device__ __forceinline__ void primary_ray(const Params &P, int i, float3 &dir_out, unsigned long long &s_out) {
+    const int px = i % P.npx;
+    const int smp = P.sample_base + i / P.npx;
+    const int X = px % P.W, Y = px / P.W;
+    unsigned long long s;
+    float3 dir;
+    if (P.estimator == KGK_ESTIMATOR_COMPAT) {
+        // render.cuh:29 seeding; pixel 0 divides by zero there, its terms are 0 here
+        const int pos = px;
+        const int m1 = (int)((unsigned)142857u * (unsigned)pos);
+        const long long q = pos > 0 ? 998244353 / pos : 0;
+        const long long r = pos > 0 ? 1000000007 % pos : 0;
+        s = P.seeds[px] + (unsigned long long)(long long)m1 + (unsigned long long)q + (unsigned long long)r;
+        dir = primary_dir(P.cam, P.W, P.H, (float)X, (float)Y);
+    } else {
+        s = splitmix64(P.seed ^ splitmix64(((unsigned long long)P.frame_index << 40) ^
+                                           ((unsigned long long)smp << 26) ^ (unsigned long long)px));
+        if (s == 0ull) s = 1ull;
+        const float jx = rnd_u(s) - 0.5f, jy = rnd_u(s) - 0.5f;
+        dir = primary_dir(P.cam, P.W, P.H, (float)X + jx, (float)Y + jy);
+    }
+    dir_out = dir;
+    s_out = s;
+}
+
 __global__ void k_raygen(Params P) {
     const int n = P.npx * P.spp_wave;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const int px = i % P.npx;
-        const int smp = P.sample_base + i / P.npx;
-        const int X = px % P.W, Y = px / P.W;
-        unsigned long long s;
         float3 dir;
-        if (P.estimator == KGK_ESTIMATOR_COMPAT) {
-            // render.cuh:29 seeding; pixel 0 divides by zero there, its terms are 0 here
-            const int pos = px;
-            const int m1 = (int)((unsigned)142857u * (unsigned)pos);
-            const long long q = pos > 0 ? 998244353 / pos : 0;
-            const long long r = pos > 0 ? 1000000007 % pos : 0;
-            s = P.seeds[px] + (unsigned long long)(long long)m1 + (unsigned long long)q + (unsigned long long)r;
-            dir = primary_dir(P.cam, P.W, P.H, (float)X, (float)Y);
-        } else {
-            s = splitmix64(P.seed ^ splitmix64(((unsigned long long)P.frame_index << 40) ^
-                                               ((unsigned long long)smp << 26) ^ (unsigned long long)px));
-            if (s == 0ull) s = 1ull;
-            const float jx = rnd_u(s) - 0.5f, jy = rnd_u(s) - 0.5f;
-            dir = primary_dir(P.cam, P.W, P.H, (float)X + jx, (float)Y + jy);
-        }
+        unsigned long long s;
+        primary_ray(P, i, dir, s);
         const PathBuf &b = P.cur;
         b.o[i] = make_float4(P.cam.CamOrg.x, P.cam.CamOrg.y, P.cam.CamOrg.z, 0.0f);
         b.d[i] = make_float4(dir.x, dir.y, dir.z, 0.0f);  // w: pdf of the sampled direction (0 = no MIS)
@@ -992,65 +1002,77 @@ __device__ __forceinline__ void defer_shadow(const Params &P, int i, int k, int 
     P.td_list[base + (int)g.thread_rank()] = (int)slot;
 }
 
+// All remaining bounces (at most `bounces`) of one path in registers: closest
+// hit, shading, then its face-light and environment shadow rays in that
+// order (the order of the wavefront's passes, so the radiance sums are the
+// same); with `defer`, the shadow rays of its first kDeferBounces bounces go
+// to slots of tail path i instead.  Returns the deferred-record mask.
+template <int kEst>
+__device__ __forceinline__ unsigned run_path(const Params &P, PathState &ps, int i, int bounces, bool defer,
+                                             unsigned &rays_c, unsigned &rays_s, unsigned &overflow) {
+    const DevScene &s = P.sc;
+    unsigned dmask = 0;  // bit 2k + j: deferred record (bounce k, kind j)
+    for (int k = 0; k < bounces; ++k) {
+        const RayPre r = make_ray(ps.o, ps.d);
+        float bt = kBigT, u = 0.0f, v = 0.0f;
+        int bid = 0x7fffffff;
+        TravStats st{0, 0, 0};
+        const int slot = trace_closest<false>(s.nodes, (unsigned)s.n_nodes, s.tri_rec, (unsigned)s.n_tris, r, bt,
+                                              bid, u, v, st);
+        const float4 h = slot < 0 ? make_float4(kBigT, 0.0f, 0.0f, __int_as_float(-1))
+                                  : make_float4(bt, u, v, __int_as_float(bid));
+        ++rays_c;
+        ShadeOut so{};
+        if (kEst == KGK_ESTIMATOR_COMPAT) shade_compat_core(P, ps, h, so);
+        else shade_unbiased_core(P, ps, h, so);
+        if (defer && k < kDeferBounces) {
+            if (so.f_pred) {
+                defer_shadow(P, i, k, 0, so.f_org, so.f_dir, so.f_tmax, so.f_c);
+                dmask |= 1u << (2 * k);
+            }
+            if (so.e_pred) {
+                defer_shadow(P, i, k, 1, so.spos, so.e_dir, kBigT, so.e_c);
+                dmask |= 2u << (2 * k);
+            }
+            so.f_pred = so.e_pred = false;
+        }
+        if (so.f_pred) {
+            const RayPre rs = make_ray(so.f_org, so.f_dir);
+            bool vis;
+            if (so.f_light >= 0) {  // the reference's test: the closest hit is the light
+                float lt = so.f_tmax, lu, lv;
+                int lid = 0x7fffffff;
+                const int ls = trace_closest<false>(s.nodes, (unsigned)s.n_nodes, s.tri_rec, (unsigned)s.n_tris,
+                                                    rs, lt, lid, lu, lv, st);
+                vis = ls >= 0 && lid == so.f_light;
+            } else {
+                vis = !trace_any<false>(s.nodes, (unsigned)s.n_nodes, s.tri_rec, (unsigned)s.n_tris, rs,
+                                        so.f_tmax, st);
+            }
+            if (vis) ps.rad = ps.rad + so.f_c;
+            ++rays_s;
+        }
+        if (so.e_pred) {
+            const RayPre rs = make_ray(so.spos, so.e_dir);
+            if (!trace_any<false>(s.nodes, (unsigned)s.n_nodes, s.tri_rec, (unsigned)s.n_tris, rs, kBigT, st))
+                ps.rad = ps.rad + so.e_c;
+            ++rays_s;
+        }
+        overflow += st.overflow;
+        if (!so.cont) break;
+    }
+    return dmask;
+}
+
 template <int kEst>
 __global__ void __launch_bounds__(128) k_tail(Params P, int cnt_idx, int dense_n, int bounces) {
     const int n = cnt_idx >= 0 ? P.cnt[cnt_idx] : dense_n;
-    const DevScene &s = P.sc;
     const bool cache = P.use_cache != 0;
     const bool defer = kEst == KGK_ESTIMATOR_UNBIASED && P.td_o != nullptr && n <= kTailPaths;
     unsigned rays_c = 0, rays_s = 0, overflow = 0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         PathState ps = load_path(P.cur, i, cache);
-        unsigned dmask = 0;  // bit 2k + j: deferred record (bounce k, kind j)
-        for (int k = 0; k < bounces; ++k) {
-            const RayPre r = make_ray(ps.o, ps.d);
-            float bt = kBigT, u = 0.0f, v = 0.0f;
-            int bid = 0x7fffffff;
-            TravStats st{0, 0, 0};
-            const int slot = trace_closest<false>(s.nodes, (unsigned)s.n_nodes, s.tri_rec, (unsigned)s.n_tris, r, bt,
-                                                  bid, u, v, st);
-            const float4 h = slot < 0 ? make_float4(kBigT, 0.0f, 0.0f, __int_as_float(-1))
-                                      : make_float4(bt, u, v, __int_as_float(bid));
-            ++rays_c;
-            ShadeOut so{};
-            if (kEst == KGK_ESTIMATOR_COMPAT) shade_compat_core(P, ps, h, so);
-            else shade_unbiased_core(P, ps, h, so);
-            if (defer && k < kDeferBounces) {
-                if (so.f_pred) {
-                    defer_shadow(P, i, k, 0, so.f_org, so.f_dir, so.f_tmax, so.f_c);
-                    dmask |= 1u << (2 * k);
-                }
-                if (so.e_pred) {
-                    defer_shadow(P, i, k, 1, so.spos, so.e_dir, kBigT, so.e_c);
-                    dmask |= 2u << (2 * k);
-                }
-                so.f_pred = so.e_pred = false;
-            }
-            if (so.f_pred) {
-                const RayPre rs = make_ray(so.f_org, so.f_dir);
-                bool vis;
-                if (so.f_light >= 0) {  // the reference's test: the closest hit is the light
-                    float lt = so.f_tmax, lu, lv;
-                    int lid = 0x7fffffff;
-                    const int ls = trace_closest<false>(s.nodes, (unsigned)s.n_nodes, s.tri_rec, (unsigned)s.n_tris,
-                                                        rs, lt, lid, lu, lv, st);
-                    vis = ls >= 0 && lid == so.f_light;
-                } else {
-                    vis = !trace_any<false>(s.nodes, (unsigned)s.n_nodes, s.tri_rec, (unsigned)s.n_tris, rs,
-                                            so.f_tmax, st);
-                }
-                if (vis) ps.rad = ps.rad + so.f_c;
-                ++rays_s;
-            }
-            if (so.e_pred) {
-                const RayPre rs = make_ray(so.spos, so.e_dir);
-                if (!trace_any<false>(s.nodes, (unsigned)s.n_nodes, s.tri_rec, (unsigned)s.n_tris, rs, kBigT, st))
-                    ps.rad = ps.rad + so.e_c;
-                ++rays_s;
-            }
-            overflow += st.overflow;
-            if (!so.cont) break;
-        }
+        const unsigned dmask = run_path<kEst>(P, ps, i, bounces, defer, rays_c, rays_s, overflow);
         P.fin[ps.id] = make_float4(ps.rad.x, ps.rad.y, ps.rad.z, 0.0f);
         if (defer) P.td_mask[i] = dmask;
     }
