@@ -752,6 +752,7 @@ __device__ __forceinline__ void write_cache_record(const Params &P, float *rec, 
 // One unbiased shading event of path ps (hit h): emission, the cache
 // decisions, Russian roulette, the two NEE samples (returned in `out` as
 // shadow-ray records, not traced) and the BSDF sample (ps updated).
+template <bool kCache>
 __device__ __forceinline__ void shade_unbiased_core(const Params &P, PathState &ps, float4 h, ShadeOut &out) {
     const DevScene &s = P.sc;
     bool cont = false, f_pred = false, e_pred = false;
@@ -791,7 +792,7 @@ __device__ __forceinline__ void shade_unbiased_core(const Params &P, PathState &
             }
             bool alive = true;
             bool to_cache = false;
-            if (P.use_cache) {
+            if (kCache) {
                 // path spread (sqrt-summed) against the primary footprint
                 float2 sp = ps.sp;
                 const float cosl = fmaxf(fabsf(dot3(S.ng, d)), 1e-4f);
@@ -939,13 +940,13 @@ __device__ __forceinline__ void shade_unbiased_core(const Params &P, PathState &
 // leave their radiance in fin[id].  A shadow record names where its
 // contribution goes: the path's slot in the next buffer (>= 0) or -(id + 1)
 // for fin.
-template <int kEst>
+template <int kEst, bool kCache>
 __global__ void __launch_bounds__(128) k_shade(Params P, const int *__restrict__ mq, const int *__restrict__ lq,
                                                const int *__restrict__ dq, int next_cnt, float4 *so0, float4 *sd0,
                                                float4 *sc0, float4 *so1, float4 *sd1, float4 *sc1) {
     const int nm = P.cnt[kMQ], nl = P.cnt[kLQ], nd = P.cnt[kDQ];
     const int n = nm + nl + nd;
-    const bool cache = P.use_cache != 0;
+    const bool cache = kCache;
     for (int base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
         const int j = base + threadIdx.x;
         if (j < nm) {  // a miss: the path ends here
@@ -968,7 +969,7 @@ __global__ void __launch_bounds__(128) k_shade(Params P, const int *__restrict__
             const int i = jh < nl ? lq[jh] : dq[jh - nl];
             ps = load_path(P.cur, i, cache);
             if (kEst == KGK_ESTIMATOR_COMPAT) shade_compat_core(P, ps, P.hit[i], o);
-            else shade_unbiased_core(P, ps, P.hit[i], o);
+            else shade_unbiased_core<kCache>(P, ps, P.hit[i], o);
         }
         const int k = warp_append(&P.cnt[next_cnt], o.cont);
         if (o.cont) store_path(P.nxt, k, ps, cache);
@@ -1007,7 +1008,7 @@ __device__ __forceinline__ void defer_shadow(const Params &P, int i, int k, int 
 // order (the order of the wavefront's passes, so the radiance sums are the
 // same); with `defer`, the shadow rays of its first kDeferBounces bounces go
 // to slots of tail path i instead.  Returns the deferred-record mask.
-template <int kEst>
+template <int kEst, bool kCache>
 __device__ __forceinline__ unsigned run_path(const Params &P, PathState &ps, int i, int bounces, bool defer,
                                              unsigned &rays_c, unsigned &rays_s, unsigned &overflow) {
     const DevScene &s = P.sc;
@@ -1024,7 +1025,7 @@ __device__ __forceinline__ unsigned run_path(const Params &P, PathState &ps, int
         ++rays_c;
         ShadeOut so{};
         if (kEst == KGK_ESTIMATOR_COMPAT) shade_compat_core(P, ps, h, so);
-        else shade_unbiased_core(P, ps, h, so);
+        else shade_unbiased_core<kCache>(P, ps, h, so);
         if (defer && k < kDeferBounces) {
             if (so.f_pred) {
                 defer_shadow(P, i, k, 0, so.f_org, so.f_dir, so.f_tmax, so.f_c);
@@ -1064,15 +1065,15 @@ __device__ __forceinline__ unsigned run_path(const Params &P, PathState &ps, int
     return dmask;
 }
 
-template <int kEst>
+template <int kEst, bool kCache>
 __global__ void __launch_bounds__(128) k_tail(Params P, int cnt_idx, int dense_n, int bounces) {
     const int n = cnt_idx >= 0 ? P.cnt[cnt_idx] : dense_n;
-    const bool cache = P.use_cache != 0;
+    const bool cache = kCache;
     const bool defer = kEst == KGK_ESTIMATOR_UNBIASED && P.td_o != nullptr && n <= kTailPaths;
     unsigned rays_c = 0, rays_s = 0, overflow = 0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         PathState ps = load_path(P.cur, i, cache);
-        const unsigned dmask = run_path<kEst>(P, ps, i, bounces, defer, rays_c, rays_s, overflow);
+        const unsigned dmask = run_path<kEst, kCache>(P, ps, i, bounces, defer, rays_c, rays_s, overflow);
         P.fin[ps.id] = make_float4(ps.rad.x, ps.rad.y, ps.rad.z, 0.0f);
         if (defer) P.td_mask[i] = dmask;
     }
@@ -1540,10 +1541,13 @@ kgk_status kgk_render(kgk_scene *s, const kgk_camera *cam, const kgk_camera *pre
             KGK_TRY(stage_begin(3));
             const int tg = std::max(1, std::min((threads + 127) / 128, R.sms * 16));
             if (cfg->estimator == KGK_ESTIMATOR_COMPAT) {
-                k_tail<KGK_ESTIMATOR_COMPAT><<<tg, 128, 0, st>>>(P, cnt_idx, dense_n, bounces);
+                k_tail<KGK_ESTIMATOR_COMPAT, false><<<tg, 128, 0, st>>>(P, cnt_idx, dense_n, bounces);
             } else {
                 if (P.td_o) KGK_CUDA(cudaMemsetAsync(R.cnt + kTD, 0, 2 * sizeof(int), st));
-                k_tail<KGK_ESTIMATOR_UNBIASED><<<tg, 128, 0, st>>>(P, cnt_idx, dense_n, bounces);
+                if (P.use_cache)
+                    k_tail<KGK_ESTIMATOR_UNBIASED, true><<<tg, 128, 0, st>>>(P, cnt_idx, dense_n, bounces);
+                else
+                    k_tail<KGK_ESTIMATOR_UNBIASED, false><<<tg, 128, 0, st>>>(P, cnt_idx, dense_n, bounces);
                 if (P.td_o) {
                     k_tail_shadow<<<grid, 128, 0, st>>>(P);
                     k_tail_resolve<<<tg, 128, 0, st>>>(P, cnt_idx, dense_n);
@@ -1578,11 +1582,17 @@ kgk_status kgk_render(kgk_scene *s, const kgk_camera *cam, const kgk_camera *pre
             ++extend_launches;
             KGK_TRY(stage_begin(1));
             if (cfg->estimator == KGK_ESTIMATOR_COMPAT)
-                k_shade<KGK_ESTIMATOR_COMPAT><<<grid, 128, 0, st>>>(P, R.mq, R.lq, R.dq, nidx, R.sh_o[0], R.sh_d[0],
-                                                                  R.sh_c[0], R.sh_o[1], R.sh_d[1], R.sh_c[1]);
+                k_shade<KGK_ESTIMATOR_COMPAT, false><<<grid, 128, 0, st>>>(P, R.mq, R.lq, R.dq, nidx, R.sh_o[0],
+                                                                         R.sh_d[0], R.sh_c[0], R.sh_o[1], R.sh_d[1],
+                                                                         R.sh_c[1]);
+            else if (P.use_cache)
+                k_shade<KGK_ESTIMATOR_UNBIASED, true><<<grid, 128, 0, st>>>(P, R.mq, R.lq, R.dq, nidx, R.sh_o[0],
+                                                                          R.sh_d[0], R.sh_c[0], R.sh_o[1], R.sh_d[1],
+                                                                          R.sh_c[1]);
             else
-                k_shade<KGK_ESTIMATOR_UNBIASED><<<grid, 128, 0, st>>>(P, R.mq, R.lq, R.dq, nidx, R.sh_o[0], R.sh_d[0],
-                                                                    R.sh_c[0], R.sh_o[1], R.sh_d[1], R.sh_c[1]);
+                k_shade<KGK_ESTIMATOR_UNBIASED, false><<<grid, 128, 0, st>>>(P, R.mq, R.lq, R.dq, nidx, R.sh_o[0],
+                                                                           R.sh_d[0], R.sh_c[0], R.sh_o[1], R.sh_d[1],
+                                                                           R.sh_c[1]);
             KGK_TRY(stage_end());
             KGK_TRY(stage_begin(2));
             k_shadow<<<grid, 128, 0, st>>>(P, kSH0, kFS0, R.sh_o[0], R.sh_d[0], R.sh_c[0]);
