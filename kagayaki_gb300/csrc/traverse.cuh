@@ -292,7 +292,7 @@ __device__ __forceinline__ bool trace_any(const WideNode *__restrict__ nodes, un
 }
 
 // ---------------------------------------------------------------------------
-// Resumable traversal, one node visit per call, for kernels that refill
+// Resumable traversal, a few node visits per call, for kernels that refill
 // finished lanes with new rays (dynamic ray fetch) instead of letting a warp
 // wait for its longest ray.  Same node order, culling and hit rules as
 // trace_closest / trace_any, so the results are the same.
