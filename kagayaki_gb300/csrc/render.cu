@@ -103,7 +103,7 @@ namespace {
 // queues), cache record counts.
 enum Cnt {
     kA0 = 0, kA1 = 1, kSH0 = 2, kSH1 = 3, kFE = 4, kFS0 = 5, kFS1 = 6, kMQ = 7, kLQ = 8, kDQ = 9, kQN = 10,
-    kTN = 11, kTD = 12, kTDF = 13, kNCnt = 14
+    kTN = 11, kTD = 12, kTDF = 13, kTF = 14, kNCnt = 15
 };
 // Lanes of a warp that must be idle before the warp fetches new rays.
 constexpr int kRefill = 8;
@@ -1071,7 +1071,9 @@ __global__ void __launch_bounds__(128) k_tail(Params P, int cnt_idx, int dense_n
     const bool cache = kCache;
     const bool defer = kEst == KGK_ESTIMATOR_UNBIASED && P.td_o != nullptr && n <= kTailPaths;
     unsigned rays_c = 0, rays_s = 0, overflow = 0;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    // a thread takes the next path as soon as its own has ended (the grid is
+    // what fits on the GPU at once), so no path waits for a whole block
+    for (int i = atomicAdd(&P.cnt[kTF], 1); i < n; i = atomicAdd(&P.cnt[kTF], 1)) {
         PathState ps = load_path(P.cur, i, cache);
         const unsigned dmask = run_path<kEst, kCache>(P, ps, i, bounces, defer, rays_c, rays_s, overflow);
         P.fin[ps.id] = make_float4(ps.rad.x, ps.rad.y, ps.rad.z, 0.0f);
@@ -1503,6 +1505,22 @@ kgk_status kgk_render(kgk_scene *s, const kgk_camera *cam, const kgk_camera *pre
     KGK_CUDA(cudaEventRecord(e0, st));
     const int max_bounces = cfg->max_depth > 0 ? cfg->max_depth : 1024;
     uint64_t launches = 0, extend_launches = 0;
+    // resident blocks per SM of the tail kernel used by this render
+    int tail_blocks_per_sm = 1;
+    {
+        cudaError_t e;
+        if (cfg->estimator == KGK_ESTIMATOR_COMPAT)
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&tail_blocks_per_sm,
+                                                              k_tail<KGK_ESTIMATOR_COMPAT, false>, 128, 0);
+        else if (cfg->use_cache)
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&tail_blocks_per_sm,
+                                                              k_tail<KGK_ESTIMATOR_UNBIASED, true>, 128, 0);
+        else
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&tail_blocks_per_sm,
+                                                              k_tail<KGK_ESTIMATOR_UNBIASED, false>, 128, 0);
+        KGK_CUDA(e);
+        tail_blocks_per_sm = std::max(1, tail_blocks_per_sm);
+    }
     // optional per-stage timing: an event before and after every stage launch
     const bool prof = cfg->profile_stages != 0;
     std::vector<cudaEvent_t> ev;
@@ -1539,7 +1557,8 @@ kgk_status kgk_render(kgk_scene *s, const kgk_camera *cam, const kgk_camera *pre
         ++launches;
         auto launch_tail = [&](int cnt_idx, int dense_n, int bounces, int threads) -> kgk_status {
             KGK_TRY(stage_begin(3));
-            const int tg = std::max(1, std::min((threads + 127) / 128, R.sms * 16));
+            const int tg = std::max(1, std::min((threads + 127) / 128, R.sms * tail_blocks_per_sm));
+            KGK_CUDA(cudaMemsetAsync(R.cnt + kTF, 0, sizeof(int), st));
             if (cfg->estimator == KGK_ESTIMATOR_COMPAT) {
                 k_tail<KGK_ESTIMATOR_COMPAT, false><<<tg, 128, 0, st>>>(P, cnt_idx, dense_n, bounces);
             } else {
