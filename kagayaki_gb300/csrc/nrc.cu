@@ -90,15 +90,24 @@ __device__ __forceinline__ float encode_col(const float *raw, int c) {
     return 1.0f;
 }
 
-// All 64 input features of a raw query (the values of encode_col, with each
-// sincospif computed once).
+// sin(pi x) and cos(pi x) for the inference encoding: x reduced exactly to
+// [-1, 1] (x - 2 rint(x / 2)), then the hardware sine and cosine of pi times
+// it, whose absolute error (about 1e-6) lies far below the BF16 rounding
+// every feature gets before the first layer.
+__device__ __forceinline__ void sincospi_feature(float x, float *s, float *c) {
+    const float r = x - 2.0f * rintf(0.5f * x);
+    __sincosf(r * 3.14159265358979f, s, c);
+}
+
+// All 64 input features of a raw query (the values of encode_col, each sine
+// and cosine pair computed once).
 __device__ __forceinline__ void encode_row(const float *raw, float (&f)[64]) {
 #pragma unroll
     for (int ax = 0; ax < 3; ++ax) {
 #pragma unroll
         for (int k = 0; k < 6; ++k) {
             float s, co;
-            sincospif(raw[ax] * (float)(1 << k), &s, &co);
+            sincospi_feature(raw[ax] * (float)(1 << k), &s, &co);
             f[ax * 12 + 2 * k] = s;
             f[ax * 12 + 2 * k + 1] = co;
         }
@@ -108,7 +117,7 @@ __device__ __forceinline__ void encode_row(const float *raw, float (&f)[64]) {
 #pragma unroll
     for (int j = 0; j < 6; ++j) {
         float s, co;
-        sincospif(raw[3 + j], &s, &co);
+        sincospi_feature(raw[3 + j], &s, &co);
         f[42 + 2 * j] = s;
         f[42 + 2 * j + 1] = co;
     }
