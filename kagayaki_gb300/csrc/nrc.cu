@@ -70,27 +70,7 @@ __device__ __forceinline__ void ldsm_x4_t(const unsigned short *p, uint32_t &r0,
                  : "r"(smem_addr(p)));
 }
 
-// One input feature (column c of the 64-float encoding) of a raw query.
-__device__ __forceinline__ float encode_col(const float *raw, int c) {
-    if (c < 36) {
-        const int ax = c / 12, k = (c % 12) >> 1;
-        float s, co;
-        sincospif(raw[ax] * (float)(1 << k), &s, &co);
-        return (c & 1) ? co : s;
-    }
-    if (c < 42) return raw[3 + (c - 36)];  // normal, view
-    if (c < 54) {
-        const int j = c - 42;
-        const float x = raw[3 + (j / 6) * 3 + ((j % 6) >> 1)];
-        float s, co;
-        sincospif(x, &s, &co);
-        return (j & 1) ? co : s;
-    }
-    if (c < 58) return raw[9 + (c - 54)];  // roughness, albedo
-    return 1.0f;
-}
-
-// sin(pi x) and cos(pi x) for the inference encoding: x reduced exactly to
+// sin(pi x) and cos(pi x) for the input encoding: x reduced exactly to
 // [-1, 1] (x - 2 rint(x / 2)), then the hardware sine and cosine of pi times
 // it, whose absolute error (about 1e-6) lies far below the BF16 rounding
 // every feature gets before the first layer.
@@ -98,6 +78,27 @@ __device__ __forceinline__ void sincospi_feature(float x, float *s, float *c) {
     const float r = x - 2.0f * rintf(0.5f * x);
     __sincosf(r * 3.14159265358979f, s, c);
 }
+
+// One input feature (column c of the 64-float encoding) of a raw query.
+__device__ __forceinline__ float encode_col(const float *raw, int c) {
+    if (c < 36) {
+        const int ax = c / 12, k = (c % 12) >> 1;
+        float s, co;
+        sincospi_feature(raw[ax] * (float)(1 << k), &s, &co);
+        return (c & 1) ? co : s;
+    }
+    if (c < 42) return raw[3 + (c - 36)];  // normal, view
+    if (c < 54) {
+        const int j = c - 42;
+        const float x = raw[3 + (j / 6) * 3 + ((j % 6) >> 1)];
+        float s, co;
+        sincospi_feature(x, &s, &co);
+        return (j & 1) ? co : s;
+    }
+    if (c < 58) return raw[9 + (c - 54)];  // roughness, albedo
+    return 1.0f;
+}
+
 
 // All 64 input features of a raw query (the values of encode_col, each sine
 // and cosine pair computed once).
