@@ -26,6 +26,9 @@ namespace {
 
 constexpr uint32_t kMaxDim = 1u << 24;  // stb's STBI_MAX_DIMENSIONS
 
+// stb's stbi__mad3sizes_valid: w * h * n bytes must fit in an int.
+bool too_large(uint64_t w, uint64_t h, uint64_t n) { return w * h * n > 0x7fffffffull; }
+
 // Sequential reader with stb's end-of-file behaviour.
 struct Rd {
     const uint8_t *p;
@@ -183,6 +186,7 @@ kgk_status decode_bmp(const std::vector<uint8_t> &f, int *w_out, int *h_out, int
     if (psize == 0 && (size_t)offset != r.pos) return fail(KGK_ERR_PARSE, where + "bad data offset");
     const int img_n = (bpp == 24 && ma == 0xff000000u) ? 3 : (ma ? 4 : 3);
     const int target = img_n;
+    if (too_large(w, h, target)) return fail(KGK_ERR_PARSE, where + "too large");
     pix.assign((size_t)w * h * target, 0);
     uint8_t *out = pix.data();
     size_t z = 0;
@@ -322,6 +326,7 @@ kgk_status decode_gif(const std::vector<uint8_t> &f, int *w_out, int *h_out, int
             p[i][3] = transp == i ? 0 : 255;
         }
     };
+    if (too_large((uint32_t)W, (uint32_t)H, 4)) return fail(KGK_ERR_PARSE, where + "too large");
     if (flags & 0x80) colortable(pal, 2 << (flags & 7), -1);
     const size_t pcount = (size_t)W * H;
     pix.assign(pcount * 4, 0);
@@ -503,6 +508,7 @@ kgk_status decode_psd(const std::vector<uint8_t> &f, int *w_out, int *h_out, int
     for (int k = 0; k < 3; ++k) r.skip((long long)(int32_t)r.be32());  // mode data, resources, reserved
     const uint32_t compression = r.be16();
     if (compression > 1) return fail(KGK_ERR_UNSUPPORTED, where + "compression");
+    if (too_large(w, h, 4)) return fail(KGK_ERR_PARSE, where + "too large");
     const size_t count = (size_t)w * h;
     pix.assign(count * 4, 0);
     if (compression) {
@@ -577,6 +583,7 @@ kgk_status decode_pic(const std::vector<uint8_t> &f, int *w_out, int *h_out, int
     r.skip(92);
     const uint32_t w = r.be16(), h = r.be16();
     if (r.eof()) return fail(KGK_ERR_PARSE, where + "file too short");
+    if (too_large(w, h, 4)) return fail(KGK_ERR_PARSE, where + "too large");
     r.skip(8);  // ratio, fields, pad
     struct Packet {
         int size, type, channel;
@@ -726,6 +733,7 @@ kgk_status decode_tga(const std::vector<uint8_t> &f, int *w_out, int *h_out, int
     bool rgb16 = false;
     const int comp = indexed ? tga_comp(pal_bits, false, &rgb16) : tga_comp(bpp, type == 3, &rgb16);
     if (!comp) return fail(KGK_ERR_PARSE, where + "pixel format");
+    if (too_large((uint32_t)w, (uint32_t)h, (uint32_t)comp)) return fail(KGK_ERR_PARSE, where + "too large");
     pix.assign((size_t)w * h * comp, 0);
     r.skip(offset);
     auto read_rgb16 = [&](uint8_t *out) {

@@ -118,7 +118,11 @@ def test_image_format_errors(tmp_path):
              ("shortpal.tga", scene_files.tga_bytes(rng.integers(0, 4, (3, 3), np.uint8), 1, 8,
                                                     palette=rng.integers(0, 256, (4, 3), np.uint8),
                                                     pal_bits=24)[:24], "palette"),
-             ("noise.bin", bytes(rng.integers(0, 256, 64, np.uint8)) + b"", "unknown image format")]
+             ("noise.bin", bytes(rng.integers(0, 256, 64, np.uint8)) + b"", "unknown image format"),
+             # stb's size rule: width * height * channels must fit in an int
+             ("huge.bmp", bytes(bmp[:18]) + (30000).to_bytes(4, "little") + (30000).to_bytes(4, "little") +
+              bytes(bmp[26:30]) + bytes(4) + bytes(bmp[34:]), "too large"),
+             ("huge.gif", b"GIF89a\xff\xff\xff\xff\x00\x00\x00\x3b", "too large")]
     for name, data, msg in cases:
         (tmp_path / name).write_bytes(data)
         with pytest.raises(KgkError, match=msg):
