@@ -89,16 +89,6 @@ Staging::~Staging() { dfree(ptr); }
 
 using namespace kgk;
 
-#define KGK_GUARD_BEGIN try {
-#define KGK_GUARD_END                                                        \
-    }                                                                        \
-    catch (const std::exception &ex) {                                       \
-        return fail(KGK_ERR_OUT_OF_MEMORY, std::string("host exception: ") + ex.what()); \
-    }                                                                        \
-    catch (...) {                                                            \
-        return fail(KGK_ERR_OUT_OF_MEMORY, "unknown host exception");      \
-    }
-
 extern "C" {
 
 const char *kgk_version(void) { return "kagayaki-gb300 0.1.0 (sm_103a)"; }

@@ -88,6 +88,7 @@ const float *tone_thresholds() {
 extern "C" {
 
 kgk_status kgk_tonemap_rgba8(const kgk_vec *img, int32_t w, int32_t h, uint8_t *out) {
+    KGK_GUARD_BEGIN
     if (!img || !out) return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_tonemap_rgba8: NULL buffer");
     if (w <= 0 || h <= 0) return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_tonemap_rgba8: empty image");
     const size_t npx = (size_t)w * h;
@@ -116,9 +117,11 @@ kgk_status kgk_tonemap_rgba8(const kgk_vec *img, int32_t w, int32_t h, uint8_t *
         out[4 * i + 3] = 255;
     }
     return KGK_OK;
+    KGK_GUARD_END
 }
 
 kgk_status kgk_save_png(const kgk_vec *img, int32_t w, int32_t h, const char *path) {
+    KGK_GUARD_BEGIN
     if (!path) return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_save_png: path == NULL");
     if (w <= 0 || h <= 0) return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_save_png: empty image");
     std::vector<uint8_t> rgba((size_t)w * h * 4);
@@ -163,6 +166,7 @@ kgk_status kgk_save_png(const kgk_vec *img, int32_t w, int32_t h, const char *pa
     int cl = fclose(f);
     if (wr != png.size() || cl != 0) return fail(KGK_ERR_IO, std::string("kgk_save_png: write failed for ") + path);
     return KGK_OK;
+    KGK_GUARD_END
 }
 
 }  // extern "C"
@@ -208,6 +212,7 @@ void attr(std::vector<uint8_t> &v, const char *name, const char *type, const std
 }  // namespace
 
 extern "C" kgk_status kgk_save_exr(const kgk_vec *img, int32_t w, int32_t h, int32_t half, const char *path) {
+    KGK_GUARD_BEGIN
     if (!path || !img) return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_save_exr: NULL argument");
     if (w <= 0 || h <= 0) return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_save_exr: empty image");
     const size_t n = (size_t)w * h;
@@ -278,5 +283,6 @@ extern "C" kgk_status kgk_save_exr(const kgk_vec *img, int32_t w, int32_t h, int
     const int cl = fclose(f);
     if (wr != out.size() || cl != 0) return fail(KGK_ERR_IO, std::string("kgk_save_exr: write failed for ") + path);
     return KGK_OK;
+    KGK_GUARD_END
 }
 

@@ -616,8 +616,10 @@ kgk_status load_image_float(const char *path, kgk_texture *out) {
 extern "C" {
 
 kgk_status kgk_load_image(const char *path, kgk_texture *out) {
+    KGK_GUARD_BEGIN
     if (!path || !out) return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_load_image: NULL argument");
     return load_image_float(path, out);
+    KGK_GUARD_END
 }
 
 void kgk_image_free(kgk_texture *t) {

@@ -146,6 +146,18 @@ void scene_free(DevScene &s);
 kgk_status bvh_build(DevScene &s, cudaStream_t st, BvhBuildStats *out);
 kgk_status bvh_validate(const DevScene &s, cudaStream_t st);
 
+// C-ABI entry points: no C++ exception crosses the boundary; a host
+// exception (allocation failure) becomes a status.
+#define KGK_GUARD_BEGIN try {
+#define KGK_GUARD_END                                                        \
+    }                                                                        \
+    catch (const std::exception &ex) {                                       \
+        return fail(KGK_ERR_OUT_OF_MEMORY, std::string("host exception: ") + ex.what()); \
+    }                                                                        \
+    catch (...) {                                                            \
+        return fail(KGK_ERR_OUT_OF_MEMORY, "unknown host exception");      \
+    }
+
 struct TraceCounters {
     unsigned long long rays, overflows, nodes, tris;
     unsigned long long fetch;  // next ray to hand out (persistent kernels)

@@ -819,6 +819,7 @@ extern "C" {
 
 kgk_status kgk_load_obj_ex(const char *obj_path, const char *hdr_path, const kgk_load_options *opt,
                            kgk_host_scene *out) {
+    KGK_GUARD_BEGIN
     if (!obj_path || !out) return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_load_obj: NULL argument");
     memset(out, 0, sizeof *out);
     const int model = opt ? opt->material_model : KGK_MATERIALS_REFERENCE;
@@ -997,6 +998,7 @@ kgk_status kgk_load_obj_ex(const char *obj_path, const char *hdr_path, const kgk
     out->n_textures = texs.size();
     out->hdr = hdr;
     return KGK_OK;
+    KGK_GUARD_END
 }
 
 kgk_status kgk_load_obj(const char *obj_path, const char *hdr_path, kgk_host_scene *out) {
