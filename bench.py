@@ -186,6 +186,9 @@ def run_ours(args):
         scene.render(cam, W, H, frame_index=w, out=out_host, **kw)
     # work counts + stage times (untimed pass)
     _, prof = scene.render(cam, W, H, frame_index=10_000, out=out_host, count_work=True, profile_stages=True, **kw)
+    # exclusive stage times (stages one after another, untimed): the extend
+    # kernel's duration for the roofline, and the stage breakdown
+    _, solo = scene.render(cam, W, H, frame_index=10_001, out=out_host, profile_stages=2, **kw)
     if dist:
         dist.barrier()
     clocks = ClockSampler()
@@ -202,10 +205,7 @@ def run_ours(args):
         rays += st["rays_closest"] + st["rays_shadow"]
         dev_ms += st["ms_device"]
         launches += st["kernel_launches"]
-        ext_ms += st["ms_extend"]
-        ext_rays += st["rays_closest"] - st["rays_tail"]  # the tail kernel's rays are not k_extend's
-        for key in stage_sum:
-            stage_sum[key] += st["ms_" + key]
+
     # end to end: host camera in, host frame out, wall clock
     t0 = time.perf_counter()
     e2e_rays = 0
@@ -227,14 +227,19 @@ def run_ours(args):
         return
     hbm, peak_kind = load_peaks()
     # roofline of the traversal (extend) stage: algorithmic bytes per ray
-    # (counted in the untimed counting pass) x rays of the timed frames /
-    # the extend launches' event-timed duration in the timed frames
+    # (counted in the untimed counting pass) x the extend rays of the frame
+    # with exclusive stage times / its extend launches' event-timed duration
     ext_rays_prof = prof["rays_closest"] - prof["rays_tail"]  # nodes / triangles are counted in k_extend only
     bytes_per_ray = (prof["nodes_visited"] * NODE_BYTES + prof["tris_tested"] * TRI_BYTES +
                      ext_rays_prof * RAY_BYTES) / max(ext_rays_prof, 1)
+    # the extend launches of the frame with exclusive stage times (the timed
+    # frames overlap each bounce's shadow passes with the next extend)
+    ext_ms = solo["ms_extend"]
+    ext_rays = solo["rays_closest"] - solo["rays_tail"]  # the tail kernel's rays are not k_extend's
+    stage_sum = {key: solo["ms_" + key] for key in stage_sum}
     ext_s = ext_ms / 1e3
     achieved = bytes_per_ray * ext_rays / ext_s / 1e9 if ext_s > 0 else None
-    n_ext = args.steps * prof["extend_launches"] if prof.get("extend_launches") else None
+    n_ext = solo["extend_launches"] if solo.get("extend_launches") else None
     traffic = None
     dram_per_ray = read_profile_value("k_extend_c2_traffic.md", "dram_bytes_per_ray")
     if dram_per_ray is not None and n_ext:
@@ -263,7 +268,7 @@ def run_ours(args):
                      "peak_source": peak_kind,
                      "bytes_per_ray": round(bytes_per_ray, 1),
                      "achieved_per_launch_bytes": round(bytes_per_ray * ext_rays / n_ext) if n_ext else None},
-        "stages_ms": {k: round(v / args.steps, 2) for k, v in stage_sum.items()},
+        "stages_ms": {k: round(v, 2) for k, v in stage_sum.items()},
         "rays_per_step": int(rays / args.steps),
         "bvh": {"wide_nodes": bvh["n_wide_nodes"], "build_ms": round(bvh["ms_build"], 1)},
         "clocks": ck,

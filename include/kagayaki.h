@@ -129,7 +129,10 @@ typedef struct kgk_render_config {
     int32_t count_work;      /* 1: count BVH nodes visited / triangles tested      */
     int32_t write_gbuffer;   /* 1: write the SVGF G-buffer from primary hits       */
     int32_t use_cache;       /* 1: terminate paths into the radiance cache         */
-    int32_t profile_stages;  /* 1: time each pipeline stage with CUDA events        */
+    int32_t profile_stages;  /* 1: time each pipeline stage with CUDA events (the
+                              * shadow passes overlap the next bounce's extend);
+                              * 2: the same with the stages one after another, so
+                              * each stage time is that stage's alone             */
     int32_t texture_filter;  /* 0: nearest (Texture::get_Color, struct_Texture.cuh:
                                 12-18); 1: bilinear with wrap-around addressing  */
     int32_t reserved[4];

@@ -54,6 +54,8 @@ struct PathBuf {
 };
 
 struct RenderState {
+    cudaStream_t st2 = nullptr;               // the shadow passes, overlapping the next bounce's extend
+    cudaEvent_t shaded = nullptr, shadowed = nullptr;
     int W = 0, H = 0;                         // per-pixel buffers
     unsigned long long *seeds = nullptr;      // compat per-pixel seed chain (render.cuh:19,29,42)
     float4 *frame = nullptr;                  // per-call radiance sum
@@ -1352,6 +1354,9 @@ kgk_status ensure_train(RenderState &R, int tcap) {
 void render_state_free(kgk_scene *s) {
     RenderState *R = s->rs;
     if (!R) return;
+    if (R->st2) cudaStreamDestroy(R->st2);
+    if (R->shaded) cudaEventDestroy(R->shaded);
+    if (R->shadowed) cudaEventDestroy(R->shadowed);
     void *ptrs[] = {R->seeds, R->frame, R->kept, R->acc_sum, R->acc_sq, R->gb_pos, R->gb_nrm, R->gb_alb, R->gb_emi,
                     R->fin, R->hit, R->mq, R->lq, R->dq, R->sh_o[0], R->sh_o[1], R->sh_d[0], R->sh_d[1], R->sh_c[0],
                     R->sh_c[1], R->cnt, R->stats, R->qrec, R->trec, R->ttgt, R->td_o, R->td_d, R->td_c,
@@ -1499,6 +1504,19 @@ kgk_status kgk_render(kgk_scene *s, const kgk_camera *cam, const kgk_camera *pre
         P.spread_c = nc.spread_c;
     }
     const int grid = R.sms * 8;   // persistent grid-stride launches, 128 threads per block
+    if (!R.st2) {
+        KGK_CUDA(cudaStreamCreateWithFlags(&R.st2, cudaStreamNonBlocking));
+        KGK_CUDA(cudaEventCreateWithFlags(&R.shaded, cudaEventDisableTiming));
+        KGK_CUDA(cudaEventCreateWithFlags(&R.shadowed, cudaEventDisableTiming));
+    }
+    // profile_stages == 2: stages one after another, so each stage time is its own
+    const cudaStream_t sh_st = cfg->profile_stages == 2 ? st : R.st2;
+    bool shadow_pending = false;  // shadow passes on st2 not yet waited for on st
+    auto join_shadow = [&]() -> kgk_status {
+        if (shadow_pending) KGK_CUDA(cudaStreamWaitEvent(st, R.shadowed, 0));
+        shadow_pending = false;
+        return KGK_OK;
+    };
     cudaEvent_t e0, e1;
     KGK_CUDA(cudaEventCreate(&e0));
     KGK_CUDA(cudaEventCreate(&e1));
@@ -1525,20 +1543,20 @@ kgk_status kgk_render(kgk_scene *s, const kgk_camera *cam, const kgk_camera *pre
     const bool prof = cfg->profile_stages != 0;
     std::vector<cudaEvent_t> ev;
     std::vector<int> ev_stage;  // 0 extend, 1 shade, 2 shadow, 3 tail
-    auto stage_begin = [&](int stage) -> kgk_status {
+    auto stage_begin = [&](int stage, cudaStream_t on = nullptr) -> kgk_status {
         if (!prof) return KGK_OK;
         cudaEvent_t a;
         KGK_CUDA(cudaEventCreate(&a));
-        KGK_CUDA(cudaEventRecord(a, st));
+        KGK_CUDA(cudaEventRecord(a, on ? on : st));
         ev.push_back(a);
         ev_stage.push_back(stage);
         return KGK_OK;
     };
-    auto stage_end = [&]() -> kgk_status {
+    auto stage_end = [&](cudaStream_t on = nullptr) -> kgk_status {
         if (!prof) return KGK_OK;
         cudaEvent_t b;
         KGK_CUDA(cudaEventCreate(&b));
-        KGK_CUDA(cudaEventRecord(b, st));
+        KGK_CUDA(cudaEventRecord(b, on ? on : st));
         ev.push_back(b);
         ev_stage.push_back(-1);
         return KGK_OK;
@@ -1590,7 +1608,9 @@ kgk_status kgk_render(kgk_scene *s, const kgk_camera *cam, const kgk_camera *pre
             P.cur = R.pb[c];
             P.nxt = R.pb[c ^ 1];
             const int cidx = b == 0 ? -1 : kA0 + c, nidx = kA0 + (c ^ 1);
-            KGK_CUDA(cudaMemsetAsync(R.cnt + kSH0, 0, (kDQ + 1 - kSH0) * sizeof(int), st));
+            // extend's counters only: the previous bounce's shadow passes may still run
+            KGK_CUDA(cudaMemsetAsync(R.cnt + kFE, 0, sizeof(int), st));
+            KGK_CUDA(cudaMemsetAsync(R.cnt + kMQ, 0, (kDQ + 1 - kMQ) * sizeof(int), st));
             KGK_CUDA(cudaMemsetAsync(R.cnt + nidx, 0, sizeof(int), st));
             KGK_TRY(stage_begin(0));
             if (cfg->count_work)
@@ -1599,6 +1619,11 @@ kgk_status kgk_render(kgk_scene *s, const kgk_camera *cam, const kgk_camera *pre
                 k_extend<false><<<grid, 128, 0, st>>>(P, cidx, n, R.mq, R.lq, R.dq);
             KGK_TRY(stage_end());
             ++extend_launches;
+            // shading adds to the radiance the previous shadow passes wrote and
+            // refills their queues: wait for them, then reset the queue counters
+            KGK_TRY(join_shadow());
+            KGK_CUDA(cudaMemsetAsync(R.cnt + kSH0, 0, 2 * sizeof(int), st));
+            KGK_CUDA(cudaMemsetAsync(R.cnt + kFS0, 0, 2 * sizeof(int), st));
             KGK_TRY(stage_begin(1));
             if (cfg->estimator == KGK_ESTIMATOR_COMPAT)
                 k_shade<KGK_ESTIMATOR_COMPAT, false><<<grid, 128, 0, st>>>(P, R.mq, R.lq, R.dq, nidx, R.sh_o[0],
@@ -1609,10 +1634,14 @@ kgk_status kgk_render(kgk_scene *s, const kgk_camera *cam, const kgk_camera *pre
                                                                           R.sh_d[0], R.sh_c[0], R.sh_o[1], R.sh_d[1],
                                                                           R.sh_c[1]);
             KGK_TRY(stage_end());
-            KGK_TRY(stage_begin(2));
-            k_shadow<<<grid, 128, 0, st>>>(P, kSH0, kFS0, R.sh_o[0], R.sh_d[0], R.sh_c[0]);
-            k_shadow<<<grid, 128, 0, st>>>(P, kSH1, kFS1, R.sh_o[1], R.sh_d[1], R.sh_c[1]);
-            KGK_TRY(stage_end());
+            KGK_CUDA(cudaEventRecord(R.shaded, st));
+            KGK_CUDA(cudaStreamWaitEvent(sh_st, R.shaded, 0));
+            KGK_TRY(stage_begin(2, sh_st));
+            k_shadow<<<grid, 128, 0, sh_st>>>(P, kSH0, kFS0, R.sh_o[0], R.sh_d[0], R.sh_c[0]);
+            k_shadow<<<grid, 128, 0, sh_st>>>(P, kSH1, kFS1, R.sh_o[1], R.sh_d[1], R.sh_c[1]);
+            KGK_TRY(stage_end(sh_st));
+            KGK_CUDA(cudaEventRecord(R.shadowed, sh_st));
+            shadow_pending = true;
             KGK_CUDA(cudaGetLastError());
             launches += 4;
             c ^= 1;
@@ -1629,12 +1658,14 @@ kgk_status kgk_render(kgk_scene *s, const kgk_camera *cam, const kgk_camera *pre
                     break;
                 }
                 if (alive <= kTailPaths && b + 1 < max_bounces) {
+                    KGK_TRY(join_shadow());  // the tail starts from the radiance they complete
                     KGK_TRY(launch_tail(kA0 + c, 0, max_bounces - b - 1, alive));
                     drained = true;
                     break;
                 }
             }
         }
+        KGK_TRY(join_shadow());
         if (!drained) {
             // the bounce limit ended the wavefront with paths still live
             k_flush<<<grid, 128, 0, st>>>(P, kA0 + c);
