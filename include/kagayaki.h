@@ -436,7 +436,9 @@ kgk_status kgk_svgf_apply(kgk_vec *result, kgk_vec *filtered, kgk_svgf_buffer *p
  *    does not matter.
  * The first call on each device looks the array's device address up
  * (cudaGetSymbolAddress) with that device current; make that first call
- * before any stream capture. */
+ * before any stream capture.  The address is kept for the life of the
+ * process: after cudaDeviceReset on a device, do not call this function on
+ * that device again. */
 kgk_status kgk_svgf_apply_noalloc(kgk_vec *result, kgk_vec *filtered, kgk_svgf_buffer *prev,
                                   kgk_svgf_buffer *cur, int32_t width, int32_t height, int32_t frame,
                                   void *cuda_stream);

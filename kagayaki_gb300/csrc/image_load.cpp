@@ -315,6 +315,10 @@ kgk_status decode_png(const std::vector<uint8_t> &f, int *w_out, int *h_out, int
     }
     const bool depth_ok = depth == 8 || depth == 16 || ((ctype == 0 || ctype == 3) && (depth == 1 || depth == 2 || depth == 4));
     if (!depth_ok || (ctype == 3 && depth == 16)) return fail(KGK_ERR_PARSE, where + "bad bit depth");
+    // stb_image's header rule (stbi__parse_png_file): width x height x channels
+    // (4 for a paletted image, which expands to RGBA) must stay within 2^30,
+    // checked before anything of the image's size is allocated.
+    if ((1u << 30) / W / (ctype == 3 ? 4u : (uint32_t)channels) < H) return fail(KGK_ERR_PARSE, where + "too large");
     std::vector<uint8_t> raw;
     std::string zerr;
     if (!zlib_inflate(idat, raw, zerr)) return fail(KGK_ERR_PARSE, where + zerr);
@@ -471,6 +475,8 @@ kgk_status decode_hdr(const std::vector<uint8_t> &f, kgk_texture *out, const cha
     if (strncmp(p, "+X ", 3) != 0) return fail(KGK_ERR_UNSUPPORTED, where + "unsupported data layout");
     const long W = strtol(p + 3, nullptr, 10);
     if (W <= 0 || H <= 0 || W > (1 << 24) || H > (1 << 24)) return fail(KGK_ERR_PARSE, where + "bad size");
+    // stb_image's stbi__mad4sizes_valid: width x height x 3 floats must fit in an int.
+    if ((uint64_t)W * (uint64_t)H * 3u * sizeof(float) > 0x7fffffffull) return fail(KGK_ERR_PARSE, where + "too large");
     float *px = (float *)malloc((size_t)W * H * 3 * sizeof(float));
     if (!px) return fail(KGK_ERR_OUT_OF_MEMORY, where + "out of host memory");
     auto bad = [&](const char *m) {

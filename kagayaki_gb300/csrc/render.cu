@@ -1420,6 +1420,10 @@ kgk_status kgk_render(kgk_scene *s, const kgk_camera *cam, const kgk_camera *pre
         return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_render: use_cache needs kgk_nrc_init");
     KGK_CUDA(cudaSetDevice(s->device));
     RenderState &R = *render_state(s);
+    // A render that returned early with an error may have left its last shadow
+    // passes running on the second stream; everything this call queues on the
+    // scene's stream (counter resets first) waits for them.
+    if (R.shadowed) KGK_CUDA(cudaStreamWaitEvent(s->stream, R.shadowed, 0));
     const int W = cfg->width, H = cfg->height, npx = W * H;
     KGK_TRY(ensure_pixels(R, W, H));
     if (cfg->estimator == KGK_ESTIMATOR_COMPAT && cfg->frame_index == 0)

@@ -393,17 +393,16 @@ __global__ void k_copy_vec(const kgk_vec *src, kgk_vec *dst, int n) {
     FOR_PIXELS(n) dst[p] = src[p];
 }
 
-// Runs the compat pipeline on device buffers (R, F, P, C all W*H records).
-kgk_status run_compat(kgk_vec *R, kgk_vec *F, kgk_svgf_buffer *P, kgk_svgf_buffer *C, int W, int H, int frame,
-                      int repeats, int stages, cudaStream_t st) {
-    const size_t npx = (size_t)W * H;
-    void *scratch = nullptr;
-    const size_t fl = npx * sizeof(float);
-    const size_t bytes = 9 * fl + npx + npx * sizeof(kgk_vec) + 1024;
-    KGK_TRY(dmalloc(&scratch, bytes, "SVGF scratch"));
-    char *b = (char *)scratch;
-    CompatArgs a;
-    a.W = W; a.H = H; a.frame = frame; a.R = R; a.F = F; a.P = P; a.C = C;
+// Scratch of the compat pipeline, carved from one block: M1, M2, sd, gz (two
+// arrays), s1, s2, sw, var, var2 at `fl` bytes each, then R2 (`vec` bytes),
+// then the per-pixel spatial flags; every array starts on a 256-byte boundary.
+// Returns var2, the second variance buffer of the a-trous passes.
+constexpr size_t scratch_up(size_t x) { return (x + 255) & ~(size_t)255; }
+constexpr size_t compat_fl(size_t npx) { return scratch_up(npx * sizeof(float)); }
+constexpr size_t compat_vec(size_t npx) { return scratch_up(npx * sizeof(kgk_vec)); }
+constexpr size_t compat_scratch_bytes(size_t npx) { return 10 * compat_fl(npx) + compat_vec(npx) + npx; }
+
+float *carve_compat(CompatArgs &a, unsigned char *b, size_t fl, size_t vec) {
     a.M1 = (float *)b; b += fl;
     a.M2 = (float *)b; b += fl;
     a.sd = (float *)b; b += fl;
@@ -412,11 +411,17 @@ kgk_status run_compat(kgk_vec *R, kgk_vec *F, kgk_svgf_buffer *P, kgk_svgf_buffe
     a.s2 = (float *)b; b += fl;
     a.sw = (float *)b; b += fl;
     a.var = (float *)b; b += fl;
-    a.R2 = (kgk_vec *)b; b += npx * sizeof(kgk_vec);
-    a.spatial = (unsigned char *)b;
-    float *var2 = nullptr;
-    kgk_status stt = dmalloc((void **)&var2, fl, "SVGF scratch");
-    if (stt != KGK_OK) { dfree(scratch); return stt; }
+    float *var2 = (float *)b; b += fl;
+    a.R2 = (kgk_vec *)b; b += vec;
+    a.spatial = b;
+    return var2;
+}
+
+// Queues the compat pipeline (SVGF.cuh:495-522, every __syncthreads a kernel
+// boundary) on `st` and waits for it.  Every scratch word is written by an
+// earlier kernel of the same call before any kernel reads it.
+kgk_status launch_compat(CompatArgs &a, float *var2, int repeats, int stages, cudaStream_t st) {
+    const size_t npx = (size_t)a.W * a.H;
     const int g = (int)std::min<size_t>((npx + 255) / 256, 65535);
     k_c_prologue<<<g, 256, 0, st>>>(a);
     k_c_temporal<<<g, 256, 0, st>>>(a);
@@ -427,7 +432,7 @@ kgk_status run_compat(kgk_vec *R, kgk_vec *F, kgk_svgf_buffer *P, kgk_svgf_buffe
     k_c_var5<<<g, 256, 0, st>>>(a);
     k_c_gauss1<<<g, 256, 0, st>>>(a);
     k_c_gauss2<<<g, 256, 0, st>>>(a);
-    kgk_vec *rin = R, *rout = a.R2;
+    kgk_vec *rin = a.R, *rout = a.R2;
     float *vin = a.var, *vout = var2;
     for (int k = 0; k < repeats; ++k)
         for (int s = 0; s < stages; ++s) {
@@ -435,14 +440,27 @@ kgk_status run_compat(kgk_vec *R, kgk_vec *F, kgk_svgf_buffer *P, kgk_svgf_buffe
             std::swap(rin, rout);
             std::swap(vin, vout);
         }
-    if (rin != R) k_copy_vec<<<g, 256, 0, st>>>(rin, R, (int)npx);
+    if (rin != a.R) k_copy_vec<<<g, 256, 0, st>>>(rin, a.R, (int)npx);
     k_c_final<<<g, 256, 0, st>>>(a, vin);
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    dfree(scratch);
-    dfree(var2);
     if (e != cudaSuccess) return cuda_fail(e, "SVGF compat kernels");
     return KGK_OK;
+}
+
+// Runs the compat pipeline on device buffers (R, F, P, C all W*H records),
+// with scratch allocated for the call.
+kgk_status run_compat(kgk_vec *R, kgk_vec *F, kgk_svgf_buffer *P, kgk_svgf_buffer *C, int W, int H, int frame,
+                      int repeats, int stages, cudaStream_t st) {
+    const size_t npx = (size_t)W * H;
+    void *scratch = nullptr;
+    KGK_TRY(dmalloc(&scratch, compat_scratch_bytes(npx), "SVGF scratch"));
+    CompatArgs a;
+    a.W = W; a.H = H; a.frame = frame; a.R = R; a.F = F; a.P = P; a.C = C;
+    float *var2 = carve_compat(a, (unsigned char *)scratch, compat_fl(npx), compat_vec(npx));
+    const kgk_status stt = launch_compat(a, var2, repeats, stages, st);
+    dfree(scratch);
+    return stt;
 }
 
 // Fills reference-layout records from the renderer's G-buffer, the way
@@ -1111,11 +1129,8 @@ namespace kgk {
 namespace {
 
 constexpr size_t kNaMax = (size_t)KGK_SVGF_NOALLOC_MAX_PIXELS;
-constexpr size_t kNaAlign = 256;
-constexpr size_t na_up(size_t x) { return (x + kNaAlign - 1) & ~(kNaAlign - 1); }
-constexpr size_t kNaFloats = na_up(kNaMax * sizeof(float));
-// M1, M2, sd, gz (x2), s1, s2, sw, var, var2 | R2 (kgk_vec) | spatial (bytes)
-constexpr size_t kNaBytes = 10 * kNaFloats + na_up(kNaMax * sizeof(kgk_vec)) + na_up(kNaMax);
+// run_compat's scratch layout at the maximum image size
+constexpr size_t kNaBytes = compat_scratch_bytes(kNaMax);
 
 __device__ __align__(256) static unsigned char g_svgf_scratch[kNaBytes];
 
@@ -1124,7 +1139,8 @@ std::mutex g_na_mu;
 unsigned char *g_na_addr[kNaMaxDevices] = {};
 
 // Device address of g_svgf_scratch on the current device; looked up once per
-// device (with that device current) and cached.
+// device (with that device current) and cached for the life of the process,
+// so it is stale after cudaDeviceReset on that device.
 kgk_status noalloc_scratch(unsigned char **out) {
     int dev = 0;
     KGK_CUDA(cudaGetDevice(&dev));
@@ -1159,47 +1175,10 @@ extern "C" kgk_status kgk_svgf_apply_noalloc(kgk_vec *result, kgk_vec *filtered,
                     "kgk_svgf_apply_noalloc: all four buffers must be device memory (host buffers would need staging)");
     unsigned char *base = nullptr;
     KGK_TRY(noalloc_scratch(&base));
-    cudaStream_t st = (cudaStream_t)cuda_stream;
-    const size_t npx = (size_t)W * H;
     CompatArgs a;
     a.W = W; a.H = H; a.frame = frame;
     a.R = result; a.F = filtered; a.P = prev; a.C = cur;
-    unsigned char *b = base;
-    a.M1 = (float *)b; b += kNaFloats;
-    a.M2 = (float *)b; b += kNaFloats;
-    a.sd = (float *)b; b += kNaFloats;
-    a.gz = (float *)b; b += 2 * kNaFloats;
-    a.s1 = (float *)b; b += kNaFloats;
-    a.s2 = (float *)b; b += kNaFloats;
-    a.sw = (float *)b; b += kNaFloats;
-    a.var = (float *)b; b += kNaFloats;
-    float *var2 = (float *)b; b += kNaFloats;
-    a.R2 = (kgk_vec *)b; b += na_up(kNaMax * sizeof(kgk_vec));
-    a.spatial = b;
-    // Every scratch word is written by an earlier kernel of this call before
-    // any kernel reads it, so the previous call's leftovers never matter.
-    const int g = (int)std::min<size_t>((npx + 255) / 256, 65535);
-    k_c_prologue<<<g, 256, 0, st>>>(a);
-    k_c_temporal<<<g, 256, 0, st>>>(a);
-    k_c_var1<<<g, 256, 0, st>>>(a);
-    k_c_var2<<<g, 256, 0, st>>>(a);
-    k_c_var3<<<g, 256, 0, st>>>(a);
-    k_c_var4<<<g, 256, 0, st>>>(a);
-    k_c_var5<<<g, 256, 0, st>>>(a);
-    k_c_gauss1<<<g, 256, 0, st>>>(a);
-    k_c_gauss2<<<g, 256, 0, st>>>(a);
-    kgk_vec *rin = result, *rout = a.R2;
-    float *vin = a.var, *vout = var2;
-    for (int k = 0; k < 5; ++k)
-        for (int s = 0; s < 5; ++s) {
-            k_c_atrous<<<g, 256, 0, st>>>(a, rin, rout, vin, vout, s);
-            std::swap(rin, rout);
-            std::swap(vin, vout);
-        }
-    if (rin != result) k_copy_vec<<<g, 256, 0, st>>>(rin, result, (int)npx);
-    k_c_final<<<g, 256, 0, st>>>(a, vin);
-    cudaError_t e = cudaGetLastError();
-    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    if (e != cudaSuccess) return cuda_fail(e, "kgk_svgf_apply_noalloc kernels");
-    return KGK_OK;
+    // run_compat's layout, each array at its size for the largest image
+    float *var2 = carve_compat(a, base, compat_fl(kNaMax), compat_vec(kNaMax));
+    return launch_compat(a, var2, 5, 5, (cudaStream_t)cuda_stream);
 }

@@ -13,6 +13,15 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ORC_SO = os.path.join(HERE, "_build", "liborc.so")
 REF_SO = os.path.join(HERE, "_ref", "libkgkref.so")
 
+
+def reference_dir():
+    """The reference checkout the `ref` build reads: $KGK_REFERENCE_DIR, else a
+    directory named `reference` beside this repository."""
+    d = os.environ.get("KGK_REFERENCE_DIR")
+    if d:
+        return d
+    return os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")
+
 _vp = ctypes.c_void_p
 _i64 = ctypes.c_int64
 _i32 = ctypes.c_int
@@ -20,11 +29,11 @@ _f32 = ctypes.c_float
 
 
 def build(ref=False):
-    """Builds liborc.so (and the reference library when ref=True and the
-    reference checkout exists)."""
+    """Builds liborc.so (and the reference library when ref=True; the caller
+    checks that the reference checkout exists)."""
     subprocess.run(["make", "-s", "-C", HERE, "orc"], check=True)
     if ref:
-        subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
+        subprocess.run(["make", "-s", "-C", HERE, "ref", "REF_DIR=" + reference_dir()], check=True)
 
 
 def _ptr(a):

@@ -100,6 +100,18 @@ def test_errors(tmp_path):
         load_image(tmp_path / "x.jpg")
 
 
+def png_header(w, h, ctype):
+    """A PNG signature, an IHDR chunk for w x h at 8 bits of colour type
+    `ctype`, and an empty IEND (no image data)."""
+    import struct
+    import zlib
+
+    def chunk(tag, data):
+        return struct.pack(">I", len(data)) + tag + data + struct.pack(">I", zlib.crc32(tag + data) & 0xffffffff)
+    return (b"\x89PNG\r\n\x1a\n" + chunk(b"IHDR", struct.pack(">IIBBBBB", w, h, 8, ctype, 0, 0, 0)) +
+            chunk(b"IEND", b""))
+
+
 def test_image_format_errors(tmp_path):
     """The cases stb_image rejects are errors here too (no partial image)."""
     rng = np.random.default_rng(3)
@@ -122,7 +134,10 @@ def test_image_format_errors(tmp_path):
              # stb's size rule: width * height * channels must fit in an int
              ("huge.bmp", bytes(bmp[:18]) + (30000).to_bytes(4, "little") + (30000).to_bytes(4, "little") +
               bytes(bmp[26:30]) + bytes(4) + bytes(bmp[34:]), "too large"),
-             ("huge.gif", b"GIF89a\xff\xff\xff\xff\x00\x00\x00\x3b", "too large")]
+             ("huge.gif", b"GIF89a\xff\xff\xff\xff\x00\x00\x00\x3b", "too large"),
+             # a few bytes claiming 40000 x 40000 RGBA: rejected before any allocation
+             ("huge.png", png_header(40000, 40000, 6), "too large"),
+             ("huge.hdr", b"#?RADIANCE\nFORMAT=32-bit_rle_rgbe\n\n-Y 30000 +X 30000\n" + bytes(16), "too large")]
     for name, data, msg in cases:
         (tmp_path / name).write_bytes(data)
         with pytest.raises(KgkError, match=msg):
