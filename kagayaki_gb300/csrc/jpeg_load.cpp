@@ -496,7 +496,12 @@ bool Decoder::block_prog_ac(int16_t *d, int ci) {
     return true;
 }
 
-// Integer inverse DCT of one 8x8 block into out (stride bytes per row).
+// Integer inverse DCT of one 8x8 block into out (stride bytes per row).  The
+// published method is the Independent JPEG Group's "islow" separable integer
+// IDCT (jidctint.c, after Loeffler, Ligtenberg and Moschytz 1989) with 12-bit
+// fixed-point constants, in the variant stb_image v2.27 uses (columns first,
+// its rounding biases and shifts), which every output bit of stbi_loadf
+// depends on.
 constexpr int fix12(double x) { return (int)(x * 4096 + 0.5); }
 
 struct Idct1 {

@@ -56,76 +56,57 @@ inline bool is_space(char c) { return c == ' ' || c == '\t'; }
 inline bool is_digit(char c) { return (unsigned)(c - '0') < 10u; }
 inline bool is_newline(char c) { return c == '\r' || c == '\n' || c == '\0'; }
 
-// tinyobjloader's number grammar (see the file comment).
+// 10^-k as the fraction digits of tinyobjloader's reader weigh them: the
+// nearest double for k < 8, std::pow beyond.
+double fraction_weight(int k) {
+    static const double w[8] = {1.0, 1e-1, 1e-2, 1e-3, 1e-4, 1e-5, 1e-6, 1e-7};
+    return k < 8 ? w[k] : std::pow(10.0, -k);
+}
+
+// A number as tinyobjloader v2.0.0rc10 reads one from [s, end):
+//   [+|-] ( digits [ '.' digits* ] | '.' digits* ) [ (e|E) [+|-] digits ]
+// The value is accumulated in double: integer digits as m = 10 m + d, the
+// k-th fraction digit adds d * 10^-k, and an exponent e != 0 scales by
+// ldexp(m * 5^e, e), and the sign multiplies the result.  Reading stops at the first character outside the
+// grammar (the value read so far stands), but an exponent marker must be
+// followed by digits, and an exponent above INT_MAX is rejected.  `end` must
+// point at a non-digit character (the callers end tokens at blanks).
 bool parse_double(const char *s, const char *end, double *out) {
-    if (s >= end) return false;
-    double mant = 0.0;
-    int expo = 0;
-    char sign = '+', esign = '+';
     const char *c = s;
-    int read = 0;
-    bool more = false, lead_dot = false;
-    if (*c == '+' || *c == '-') {
-        sign = *c++;
-        if (c != end && *c == '.') lead_dot = true;
-    } else if (is_digit(*c)) {
-    } else if (*c == '.') {
-        lead_dot = true;
-    } else {
-        return false;
+    auto here = [&](char a, char b) { return c != end && (*c == a || *c == b); };
+    auto digit_here = [&]() { return c != end && is_digit(*c); };
+    if (c == end || !(here('+', '-') || is_digit(*c) || *c == '.')) return false;
+    const bool negative = *c == '-';
+    if (here('+', '-')) ++c;
+    double m = 0.0;
+    if (!here('.', '.')) {  // an integer part is required unless a '.' leads
+        const char *first = c;
+        for (; digit_here(); ++c) m = m * 10 + (*c - '0');
+        if (c == first) return false;
     }
-    more = c != end;
-    if (!lead_dot) {
-        while (more && is_digit(*c)) {
-            mant *= 10;
-            mant += (int)(*c - '0');
-            ++c;
-            ++read;
-            more = c != end;
-        }
-        if (read == 0) return false;
-    }
-    if (!more) goto assemble;
-    if (*c == '.') {
+    if (here('.', '.')) {
         ++c;
-        read = 1;
-        more = c != end;
-        static const double kPow10Neg[8] = {1.0, 0.1, 0.01, 0.001, 0.0001, 0.00001, 0.000001, 0.0000001};
-        while (more && is_digit(*c)) {
-            mant += (int)(*c - '0') * (read < 8 ? kPow10Neg[read] : std::pow(10.0, -read));
-            ++read;
-            ++c;
-            more = c != end;
-        }
-    } else if (*c == 'e' || *c == 'E') {
-    } else {
-        goto assemble;
+        for (int k = 1; digit_here(); ++c, ++k) m += (double)(*c - '0') * fraction_weight(k);
     }
-    if (!more) goto assemble;
-    if (*c == 'e' || *c == 'E') {
+    int e = 0;
+    if (here('e', 'E')) {
         ++c;
-        more = c != end;
-        if (more && (*c == '+' || *c == '-')) {
-            esign = *c++;
-        } else if (is_digit(*c)) {
-        } else {
-            return false;
+        const bool e_negative = here('-', '-');
+        if (here('+', '-')) ++c;
+        const char *first = c;
+        for (; digit_here(); ++c) {
+            if (e > 2147483647 / 10) return false;
+            e = e * 10 + (*c - '0');
         }
-        read = 0;
-        more = c != end;
-        while (more && is_digit(*c)) {
-            if (expo > 2147483647 / 10) return false;
-            expo *= 10;
-            expo += (int)(*c - '0');
-            ++c;
-            ++read;
-            more = c != end;
-        }
-        expo *= (esign == '+' ? 1 : -1);
-        if (read == 0) return false;
+        if (c == first) return false;
+        if (e_negative) e = -e;
     }
-assemble:
-    *out = (sign == '+' ? 1 : -1) * (expo ? std::ldexp(mant * std::pow(5.0, expo), expo) : mant);
+    const double v = e != 0 ? std::ldexp(m * std::pow(5.0, e), e) : m;
+    // The sign is a factor, multiplied in: a NaN (0 * 5^e with 5^e overflowing)
+    // then keeps the sign bit the hardware gave it, where a negation would
+    // flip it.  Loaded from a table so the compiler keeps the multiplication.
+    static const double kSign[2] = {1.0, -1.0};
+    *out = kSign[negative] * v;
     return true;
 }
 
