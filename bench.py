@@ -106,16 +106,20 @@ def build_workload():
     return tris, mats, env, info
 
 
-def orbit_camera(frame, height, radius=25.0, start_deg=37.0, step_deg=6.0, z=6.0, target_z=8.0):
+def orbit_camera(frame, height, radius=25.0, start_deg=37.0, step_deg=6.0, z=6.0, target_z=8.0, setup=None):
     """Camera on a circle of `radius` around the field, looking at its centre
     (z up).  Camera_SetUpCamera's Euler convention: rotate X by 90 - pitch to
-    look horizontally, then Z to face the centre."""
-    from kagayaki_gb300 import camera_setup
+    look horizontally, then Z to face the centre.  `setup` is the
+    Camera_SetUpCamera to use: the library's (default) or, for the CPU legs,
+    the oracle's restatement (the same 18 floats bit for bit), so that those
+    legs never load the library."""
+    if setup is None:
+        from kagayaki_gb300 import camera_setup as setup
     ang = start_deg + step_deg * frame
     a = np.deg2rad(ang)
     org = (radius * np.cos(a), radius * np.sin(a), z)
     pitch = np.rad2deg(np.arctan2(z - target_z, radius))
-    return camera_setup(org, 28.0, (90.0 - pitch, 0.0, ang + 90.0), height)
+    return setup(org, 28.0, (90.0 - pitch, 0.0, ang + 90.0), height)
 
 
 def cpu_reference(tris, mats, env, threads, budget_s=10.0, chunk=65536):
@@ -124,9 +128,8 @@ def cpu_reference(tris, mats, env, threads, budget_s=10.0, chunk=65536):
     batches of `chunk` pixels spread over the 1920x1080 frame at 1 spp until
     `budget_s` seconds of work.  Returns (rays/s, rays, seconds, pixels)."""
     from oracle import orc
-    from kagayaki_gb300 import camera_array
     bvh = orc.CpuBvh(tris)
-    c = camera_array(orbit_camera(0, 1080))
+    c = orbit_camera(0, 1080, setup=orc.camera_setup)
     npx = 1920 * 1080
     order = np.random.default_rng(5).permutation(np.arange(1, npx, dtype=np.int32))
     rays, secs, done = 0, 0.0, 0
@@ -213,6 +216,15 @@ def run_ours(args):
         img, st = scene.render(cam, W, H, frame_index=100 + k, out=out_host, **kw)
         e2e_rays += st["rays_closest"] + st["rays_shadow"]
     e2e_s = time.perf_counter() - t0
+    # the same frame with the reference's estimator (compat: one sample per
+    # pixel per wave with its seed chain, no depth cap), for comparison with
+    # the reference arm, which runs that estimator
+    compat_ms, compat_rays, compat_steps = 0.0, 0, 2
+    for k in range(compat_steps + 1):
+        _, st = scene.render(cam, W, H, spp=spp, estimator=ESTIMATOR_COMPAT, frame_index=0, out=out_host)
+        if k > 0:  # the first call is a warm-up
+            compat_ms += st["ms_device"]
+            compat_rays += st["rays_closest"] + st["rays_shadow"]
     ck = clocks.stop(local)
     study = None
     if not args.no_relmse and rank == 0:
@@ -244,6 +256,16 @@ def run_ours(args):
     dram_per_ray = read_profile_value("k_extend_c2_traffic.md", "dram_bytes_per_ray")
     if dram_per_ray is not None and n_ext:
         traffic = round(dram_per_ray * ext_rays / n_ext)
+    # issue side of the same launches: FP32 operations per ray (a slab test is
+    # 12 per child of a visited node, a triangle test 30) against the FP32
+    # issue rate at the sampled clock (SMs x 128 lanes x clock)
+    ops_per_ray = (prof["nodes_visited"] * 8 * 12 + prof["tris_tested"] * 30) / max(ext_rays_prof, 1)
+    sm_mhz = (ck or {}).get("sm_mhz") or 2070.0
+    issue_peak = device_sms() * 128 * sm_mhz * 1e6 / 1e12  # Tops/s
+    issue_ach = ops_per_ray * ext_rays / ext_s / 1e12 if ext_s > 0 else None
+    issue_frac = issue_ach / issue_peak if issue_ach else None
+    byte_frac = achieved / hbm if achieved else None
+    wee = read_profile_value("stages_bounce1_480x270_4spp.md", "warp_exec_efficiency_extend")
     mrays = rays / (dev_ms / 1e3) / 1e6
     line = {
         "metric": "Mrays/s",
@@ -263,11 +285,26 @@ def run_ours(args):
                 "h2d_bytes_per_step": 72 + 96, "d2h_bytes_per_step": W * H * 16},
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1) if achieved else None,
-                     "peak": hbm, "unit": "GB/s", "frac": round(achieved / hbm, 4) if achieved else None,
+                     "peak": hbm, "unit": "GB/s",
+                     "frac": round(max(byte_frac or 0.0, issue_frac or 0.0), 4) if achieved else None,
                      "traffic": traffic, "kernel": "k_extend (closest-hit traversal)",
                      "peak_source": peak_kind,
                      "bytes_per_ray": round(bytes_per_ray, 1),
-                     "achieved_per_launch_bytes": round(bytes_per_ray * ext_rays / n_ext) if n_ext else None},
+                     "achieved_per_launch_bytes": round(bytes_per_ray * ext_rays / n_ext) if n_ext else None,
+                     "byte_frac": round(byte_frac, 4) if byte_frac else None,
+                     "issue": {"ops_per_ray": round(ops_per_ray, 1),
+                               "achieved": round(issue_ach, 3) if issue_ach else None,
+                               "peak": round(issue_peak, 2), "unit": "Tops/s (FP32 lanes)",
+                               "frac": round(issue_frac, 4) if issue_frac else None,
+                               "peak_source": f"{device_sms()} SMs x 128 FP32 lanes x {sm_mhz:.0f} MHz (sampled)"},
+                     "warp_exec_efficiency": wee,
+                     "warp_exec_efficiency_source": "ncu, k_extend at bounce 1 (profiles/stages_bounce1_480x270_4spp.md)",
+                     "frac_rule": "max(byte_frac, issue.frac)"},
+        "compat": {"value": round(compat_rays / (compat_ms / 1e3) / 1e6, 2) if compat_ms > 0 else None,
+                   "unit": "Mrays/s", "ms_per_step": round(compat_ms / compat_steps, 3),
+                   "rays_per_step": int(compat_rays / compat_steps), "steps": compat_steps,
+                   "estimator": "reference (compat): one sample per pixel per wave, Russian roulette only",
+                   "note": "the same frame with the estimator the reference arm runs"},
         "stages_ms": {k: round(v, 2) for k, v in stage_sum.items()},
         "rays_per_step": int(rays / args.steps),
         "bvh": {"wide_nodes": bvh["n_wide_nodes"], "build_ms": round(bvh["ms_build"], 1)},
@@ -282,6 +319,17 @@ def run_ours(args):
                                 "sample": f"{npx_done} random pixels of the frame at 1 spp, compat estimator "
                                           f"(oracle port, CPU BVH): {nr} rays in {dt:.1f} s"}
     print(json.dumps(line), flush=True)
+
+
+def device_sms():
+    """Streaming multiprocessors of GPU 0 (152 on a GB300)."""
+    try:
+        import torch
+        if torch.cuda.is_available():
+            return torch.cuda.get_device_properties(0).multi_processor_count
+    except Exception:
+        pass
+    return 152
 
 
 def read_profile_value(name, key):
@@ -603,15 +651,14 @@ def run_c1(args, reference=False):
     with its seed chain, Russian roulette only - the reference has no depth
     cap).  Ours on the GPU, or (reference=True) the oracle port of the
     reference's render on all host cores."""
-    from kagayaki_gb300 import ESTIMATOR_COMPAT, Scene, camera_array, camera_setup, scenes
+    from kagayaki_gb300 import scenes
     tris, mats, c = scenes.cornell_box()
     W = H = 256
     spp = 16
-    cam = camera_setup(c["origin"], c["dist"], c["rot"], H)
     if reference:
         from oracle import orc
         thr = os.cpu_count() or 1
-        ca = camera_array(cam)
+        ca = orc.camera_setup(c["origin"], c["dist"], c["rot"], H)
         orc.render_compat(tris, mats, ca, W, H, 1, threads=thr)  # warm-up
         t0 = time.perf_counter()
         rays = 0
@@ -624,6 +671,8 @@ def run_c1(args, reference=False):
                                   "kind": "port", "sample": f"{args.steps} full frames"}}
         ms = 1e3 * secs / args.steps
     else:
+        from kagayaki_gb300 import ESTIMATOR_COMPAT, Scene, camera_setup
+        cam = camera_setup(c["origin"], c["dist"], c["rot"], H)
         scene = Scene(tris, mats)
         scene.build_bvh()
         out = np.empty((H, W, 4), np.float32)
@@ -792,10 +841,12 @@ def run_reference(args):
             tot_rays += nr
     v = tot_rays / sum(per) / 1e6
     line = {"metric": "Mrays/s", "value": round(v, 4), "unit": "Mrays/s", "impl": "reference",
-            "n_gpus": int(os.environ.get("WORLD_SIZE", "1")), "steps": args.steps, "warmup": args.warmup,
+            "n_gpus": int(os.environ.get("WORLD_SIZE", str(args.gpus))), "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": round(1e3 * sum(per) / len(per), 1), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic seeded scene",
-            "config": dict(WORKLOAD, parallelism="host cores"),
+            "config": dict(WORKLOAD, parallelism="host cores",
+                           estimator="reference (compat): the reference's own estimator, Russian roulette only",
+                           traversal="the oracle's CPU BVH (the reference's 5000-entry table overflows here)"),
             "cpu_baseline": {"value": round(v, 4), "unit": "Mrays/s", "cores": thr, "kind": "port",
                              "sample": f"random pixels of the frame at 1 spp per step (~{budget:.0f} s of work), "
                                        "compat estimator, oracle port with a CPU BVH"},
