@@ -226,6 +226,13 @@ def run_ours(args):
             compat_ms += st["ms_device"]
             compat_rays += st["rays_closest"] + st["rays_shadow"]
     ck = clocks.stop(local)
+    c1 = None
+    if rank == 0:
+        c1_v, c1_ms, c1_rays = measure_c1_ours(3)
+        c1 = {"workload": "cornell-36tris-256x256-16spp-compat", "value": round(c1_v, 2), "unit": "Mrays/s",
+              "ms_per_frame": round(c1_ms, 3), "rays_per_frame": int(c1_rays),
+              "note": "config C1 with the reference's estimator; the reference arm times the reference's own "
+                      "GPU renderer on it (gpu_reference_c1)"}
     study = None
     if not args.no_relmse and rank == 0:
         try:
@@ -310,6 +317,8 @@ def run_ours(args):
         "bvh": {"wide_nodes": bvh["n_wide_nodes"], "build_ms": round(bvh["ms_build"], 1)},
         "clocks": ck,
     }
+    if c1:
+        line["c1"] = c1
     if study:
         line["relmse"] = study
     if not args.no_cpu:
@@ -387,9 +396,23 @@ def relmse_study(scene, W, H, max_depth, ref_spp=4096, train_frames=32, eval_fra
             cache1 = img[..., :3].astype(np.float64)
             cache1_ms = st["ms_device"]
     cache_img = acc / eval_frames
+    # equal time: the plain frame's samples per pixel are adjusted until its
+    # measured device time is within 2 % of the cached frames' (at most four
+    # tries; the closest one is kept)
     spp_eq = max(1, int(round(cache_ms / ms_per_spp)))
-    plain_eq, stp = scene.render(cam, W, H, spp=spp_eq, seed=9, frame_index=300_002, out=out, **kw)
-    plain_eq = plain_eq[..., :3].astype(np.float64)
+    best = None
+    for k in range(4):
+        img, stp = scene.render(cam, W, H, spp=spp_eq, seed=9, frame_index=300_002 + k, out=out, **kw)
+        err = stp["ms_device"] / cache_ms - 1.0
+        if best is None or abs(err) < abs(best[2]):
+            best = (img[..., :3].astype(np.float64), stp, err, spp_eq)
+        if abs(err) <= 0.02:
+            break
+        nxt = max(1, int(round(spp_eq * cache_ms / stp["ms_device"])))
+        if nxt == spp_eq:
+            nxt = spp_eq + (1 if err < 0 else -1)
+        spp_eq = max(1, nxt)
+    plain_eq, stp, _, spp_eq = best
     return {
         "reference": {"spp": int(nref), "accumulation": "fp64", "seconds": round(ref_s, 1)},
         "camera": "orbit frame 0 (static)",
@@ -399,7 +422,8 @@ def relmse_study(scene, W, H, max_depth, ref_spp=4096, train_frames=32, eval_fra
         "equal_time": {"ms": round(cache_ms, 2),
                        "cache": {"relmse": round(rel_mse(cache_img, ref), 5), "frames": eval_frames, "spp": eval_frames},
                        "plain": {"relmse": round(rel_mse(plain_eq, ref), 5), "spp": spp_eq,
-                                 "ms": round(stp["ms_device"], 2)}},
+                                 "ms": round(stp["ms_device"], 2),
+                                 "time_vs_cache": round(stp["ms_device"] / cache_ms, 4)}},
     }
 
 
@@ -645,6 +669,64 @@ def run_c5(args):
     print(json.dumps(line), flush=True)
 
 
+def c1_camera(H, oracle=False):
+    """The Cornell box camera for an H-row image (the oracle's
+    Camera_SetUpCamera for the CPU and reference legs)."""
+    from kagayaki_gb300 import scenes
+    _, _, c = scenes.cornell_box()
+    if oracle:
+        from oracle import orc
+        return orc.camera_setup(c["origin"], c["dist"], c["rot"], H)
+    from kagayaki_gb300 import camera_setup
+    return camera_setup(c["origin"], c["dist"], c["rot"], H)
+
+
+def measure_c1_ours(steps, warmup=2):
+    """Our compat estimator on config C1 (Cornell box, 256 x 256, 16 spp):
+    (Mrays/s, ms per frame, rays per frame), device time."""
+    from kagayaki_gb300 import ESTIMATOR_COMPAT, Scene, scenes
+    tris, mats, _ = scenes.cornell_box()
+    cam = c1_camera(256)
+    out = np.empty((256, 256, 4), np.float32)
+    with Scene(tris, mats) as scene:
+        scene.build_bvh()
+        for f in range(warmup):
+            scene.render(cam, 256, 256, spp=16, estimator=ESTIMATOR_COMPAT, frame_index=f, out=out)
+        dev, rays = 0.0, 0
+        for f in range(steps):
+            _, st = scene.render(cam, 256, 256, spp=16, estimator=ESTIMATOR_COMPAT, frame_index=warmup + f, out=out)
+            dev += st["ms_device"]
+            rays += st["rays_closest"] + st["rays_shadow"]
+    return rays / (dev / 1e3) / 1e6, dev / steps, rays // steps
+
+
+def gpu_reference_c1():
+    """The reference's own render kernel on this GPU at config C1 (the
+    Cornell box, 256 x 256, 16 one-sample launches with its seed chain), or
+    the reason it could not run.  Its first launch is checked against the
+    oracle's first frame."""
+    try:
+        from oracle import orc, ref_gpu
+        why = ref_gpu.available()
+        if why:
+            return {"unavailable": why}
+        from kagayaki_gb300 import scenes
+        tris, mats, _ = scenes.cornell_box()
+        cam = c1_camera(256, oracle=True)
+        first, _ = orc.render_compat(tris, mats, cam, 256, 256, 1)
+        px = np.random.default_rng(41).choice(np.arange(1, 256 * 256), 4096, replace=False)
+        r = ref_gpu.render_c1(cam, check_samples=(px, first[0][px]))
+    except Exception as e:
+        return {"unavailable": f"{type(e).__name__}: {e}"}
+    return {"workload": "cornell-36tris-256x256-16spp-compat", "value": round(r["mrays"], 2), "unit": "Mrays/s",
+            "ms_per_frame": round(r["ms_per_frame"], 3), "rays_per_frame": r["rays_per_frame"],
+            "first_launch_within_1e-3_of_oracle": r["first_launch_agreement"],
+            "registers": r["registers"], "stack_bytes": r["stack_bytes"],
+            "kind": "the reference's render kernel (render.cuh:21-49) compiled for sm_103a from its own headers "
+                    "(oracle/ref/ref_gpu.cu), launched as main.cu launches it, CUDA events around each launch; "
+                    "rays = traversal calls counted by a second build"}
+
+
 def run_c1(args, reference=False):
     """The reference's CPU-runnable case: the 36-triangle Cornell box, 256 x 256,
     16 spp, the reference's estimator (compat: one sample per pixel per pass
@@ -668,32 +750,24 @@ def run_c1(args, reference=False):
         secs = time.perf_counter() - t0
         extra = {"impl": "reference",
                  "cpu_baseline": {"value": round(rays / secs / 1e6, 3), "unit": "Mrays/s", "cores": thr,
-                                  "kind": "port", "sample": f"{args.steps} full frames"}}
+                                  "kind": "port", "sample": f"{args.steps} full frames"},
+                 "gpu_reference": gpu_reference_c1()}
+        extra["e2e"] = {"value": round(rays / secs / 1e6, 3), "unit": "Mrays/s", "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}
         ms = 1e3 * secs / args.steps
     else:
-        from kagayaki_gb300 import ESTIMATOR_COMPAT, Scene, camera_setup
-        cam = camera_setup(c["origin"], c["dist"], c["rot"], H)
-        scene = Scene(tris, mats)
-        scene.build_bvh()
-        out = np.empty((H, W, 4), np.float32)
-        for f in range(args.warmup):
-            scene.render(cam, W, H, spp=spp, estimator=ESTIMATOR_COMPAT, frame_index=f, out=out)
-        dev = 0.0
-        rays = 0
-        for f in range(args.steps):
-            _, st = scene.render(cam, W, H, spp=spp, estimator=ESTIMATOR_COMPAT, frame_index=args.warmup + f,
-                                 out=out)
-            dev += st["ms_device"]
-            rays += st["rays_closest"] + st["rays_shadow"]
-        scene.close()
-        secs = dev / 1e3
-        ms = dev / args.steps
+        _, ms, rays_per = measure_c1_ours(args.steps, args.warmup)
+        rays = rays_per * args.steps
+        secs = ms * args.steps / 1e3
         extra = {}
     line = {"metric": "Mrays/s", "value": round(rays / secs / 1e6, 3), "unit": "Mrays/s", "n_gpus": 1,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic seeded Cornell box",
             "config": {"workload": "cornell-36tris-256x256-16spp-compat", "estimator": "reference (compat)",
-                       "depth": "Russian roulette only, as the reference"}}
+                       "depth": "Russian roulette only, as the reference",
+                       "differs_from_config": "config C1 names max depth 8; the reference's estimator has no "
+                                              "depth cap (RayTrace.cuh:17-108 loops until Russian roulette "
+                                              "ends the path), so both arms run unbounded depth"}}
     line.update(extra)
     print(json.dumps(line), flush=True)
 
@@ -850,7 +924,11 @@ def run_reference(args):
             "cpu_baseline": {"value": round(v, 4), "unit": "Mrays/s", "cores": thr, "kind": "port",
                              "sample": f"random pixels of the frame at 1 spp per step (~{budget:.0f} s of work), "
                                        "compat estimator, oracle port with a CPU BVH"},
-            "e2e": {"value": round(v, 4), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "e2e": {"value": round(v, 4), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            # the reference's own CUDA renderer on this GPU, at the configuration
+            # its traversal handles (config C1); at this line's 5.2M triangles
+            # its 5000-entry traversal table overflows and reports misses
+            "gpu_reference_c1": gpu_reference_c1()}
     print(json.dumps(line), flush=True)
 
 

@@ -411,6 +411,25 @@ typedef struct kgk_svgf_buffer {
 kgk_status kgk_svgf_apply(kgk_vec *result, kgk_vec *filtered, kgk_svgf_buffer *prev,
                           kgk_svgf_buffer *cur, int32_t width, int32_t height, int32_t frame);
 
+/* evaluate_Disney_BRDF and evaluate_Disney_BRDF_pdf (Disney_BRDF.cuh:118-183)
+ * on the device, as the compat estimator evaluates them, with the parameters
+ * RayTrace derives from the material (RayTrace.cuh:85-92): for n direction
+ * triples (3 floats each) wo (toward the light), wi (toward the viewer) and
+ * the normal, brdf receives 3 floats and pdf 1 float per triple.  Buffers
+ * may be host or device memory; uses the current device; synchronous. */
+kgk_status kgk_disney_eval(const kgk_material *material, int32_t n, const float *wo, const float *wi,
+                           const float *normal, float *brdf, float *pdf);
+
+/* The reference-layout G-buffer of the frame last rendered with
+ * write_gbuffer = 1: the SVGFBuffer records the reference's render() fills
+ * for its caller (every record initialised as render.cuh:28 does, then at the
+ * primary hit Albedo after texture mapping, Emission, the normal facing the
+ * ray, ObjectID, MaterialID and Depth as RayTrace.cuh:66-82; ObjectID -1 on
+ * a miss; PosLastFrameI/F left at (-1, -1), where struct_Camera.cuh:109-110
+ * leaves them).  This is the `cur` argument kgk_svgf_apply takes.
+ * out = width*height records, host or device; synchronous. */
+kgk_status kgk_gbuffer_records(kgk_scene *scene, kgk_svgf_buffer *out);
+
 /* Largest image (width * height) kgk_svgf_apply_noalloc accepts. */
 #define KGK_SVGF_NOALLOC_MAX_PIXELS (512 * 512)
 

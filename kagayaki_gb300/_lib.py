@@ -42,6 +42,8 @@ PROTOTYPES = {
     "kgk_host_alloc": (_st, [_sz, ctypes.POINTER(_vp)]),
     "kgk_host_free": (None, [_vp]),
     "kgk_svgf_apply": (_st, [_vp, _vp, _vp, _vp, _i32, _i32, _i32]),
+    "kgk_gbuffer_records": (_st, [_vp, _vp]),
+    "kgk_disney_eval": (_st, [_vp, _i32, _vp, _vp, _vp, _vp, _vp]),
     "kgk_svgf_apply_noalloc": (_st, [_vp, _vp, _vp, _vp, _i32, _i32, _i32, _vp]),
     "kgk_nrc_init": (_st, [_vp, _vp]),
     "kgk_nrc_set_weights": (_st, [_vp, _vp, _sz]),

@@ -16,7 +16,7 @@ import numpy as np
 
 from . import _lib
 from ._lib import KgkError, check, lib
-from .structs import (MATERIAL, MATERIALS_PBR, MATERIALS_REFERENCE, RAY, TRIANGLE, KgkBvhInfo,  # noqa: F401
+from .structs import (MATERIAL, MATERIALS_PBR, MATERIALS_REFERENCE, RAY, SVGF_BUFFER, TRIANGLE, KgkBvhInfo,  # noqa: F401
                       KgkCamera, KgkHostScene, KgkLoadOptions, KgkNrcConfig, KgkRenderConfig, KgkStats,
                       KgkSvgfConfig, KgkTexture, KgkTextureRGBA8, KgkVec)
 
@@ -153,6 +153,13 @@ class Scene:
                                ctypes.byref(prev_cam) if prev_cam is not None else None,
                                ctypes.byref(cfg), _p(out), ctypes.byref(st)))
         return out, stats_dict(st)
+
+    def gbuffer_records(self, width, height):
+        """kgk_gbuffer_records: the last write_gbuffer frame as the reference's
+        SVGFBuffer records, a (height * width,) SVGF_BUFFER array."""
+        out = np.zeros(width * height, SVGF_BUFFER)
+        check(lib().kgk_gbuffer_records(self._h, _p(out)))
+        return out
 
     def svgf_output(self, cfg, noisy=None, filtered=None, rgba8=None, async_=False):
         """kgk_svgf_output: noisy None = the frame kept by render(keep_on_device=True);

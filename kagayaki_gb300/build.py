@@ -18,7 +18,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libkagayaki_gb300.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
-CU_SOURCES = ["bvh.cu", "scene.cu", "trace.cu", "render.cu", "svgf.cu", "nrc.cu"]
+CU_SOURCES = ["bvh.cu", "scene.cu", "trace.cu", "render.cu", "svgf.cu", "nrc.cu", "brdf.cu"]
 CPP_SOURCES = ["capi.cpp", "image_io.cpp", "image_load.cpp", "image_formats.cpp", "jpeg_load.cpp", "obj_load.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

@@ -409,8 +409,12 @@ __device__ __forceinline__ Surface load_surface(const DevScene &s, int id, float
     const float b1 = h.y, b2 = h.z, b0 = 1.0f - b1 - b2;
     const unsigned bits = __float_as_uint(a3.w);
     S.ns = (bits & 0x80000000u) ? normalize3(n1 * b1 + n2 * b2 + n0 * b0) : S.ng;
-    float uu = b1 * a1.z + b2 * a3.y + b0 * a0.w;   // vt.x of v1, v2, v0
-    float vv = b1 * a3.x + b2 * a3.z + b0 * a1.w;   // vt.y
+    // u * v1_vt + v * v2_vt + (1 - u - v) * v0_vt (struct_Triangle.cuh:61),
+    // rounded in the reference's order; k_tri_soa packs vt0 in a0.w / a1.w,
+    // vt1 in a2.w / a3.x and vt2 in a3.y / a3.z
+    const float w0 = __fsub_rn(__fsub_rn(1.0f, b1), b2);
+    float uu = __fadd_rn(__fadd_rn(__fmul_rn(b1, a2.w), __fmul_rn(b2, a3.y)), __fmul_rn(w0, a0.w));
+    float vv = __fadd_rn(__fadd_rn(__fmul_rn(b1, a3.x), __fmul_rn(b2, a3.z)), __fmul_rn(w0, a1.w));
     if (uu < 0.0f) uu += (float)((int)(-uu) + 1); else if (uu > 1.0f) uu -= (float)((int)uu);
     if (vv < 0.0f) vv += (float)((int)(-vv) + 1); else if (vv > 1.0f) vv -= (float)((int)vv);
     S.t = h.x;

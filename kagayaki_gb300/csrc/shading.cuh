@@ -183,7 +183,7 @@ __device__ float3 disney_eval(const kgk_material &m, const DisneyParams &p, floa
 
 // evaluate_Disney_BRDF_pdf (Disney_BRDF.cuh:168-183): the reference's mixture,
 // whose specular terms divide by 4|n.out| (not the half-vector Jacobian).
-__device__ float disney_pdf_ref(const DisneyParams &p, float3 in, float3 out, float3 n, float3 u,
+static __device__ float disney_pdf_ref(const DisneyParams &p, float3 in, float3 out, float3 n, float3 u,
                                 float3 v, float3 w) {
     const float3 h = normalize3(out + in);
     const float sw = p.wt[0] + p.wt[1] + p.wt[2] + p.wt[3] + p.wt[4];
@@ -195,7 +195,7 @@ __device__ float disney_pdf_ref(const DisneyParams &p, float3 in, float3 out, fl
 
 // Consistent mixture pdf of disney_sample_unbiased: lobe probabilities wt/sum,
 // half-vector Jacobian 1 / (4 |out.h|).
-__device__ float disney_pdf_unbiased(const DisneyParams &p, float3 in, float3 out, float3 n, float3 u,
+static __device__ float disney_pdf_unbiased(const DisneyParams &p, float3 in, float3 out, float3 n, float3 u,
                                      float3 v, float3 w) {
     const float ndo = dot3(n, out);
     if (ndo <= 0.0f || dot3(n, in) <= 0.0f) return 0.0f;

@@ -945,6 +945,30 @@ kgk_status kgk_svgf_apply(kgk_vec *result, kgk_vec *filtered, kgk_svgf_buffer *p
     return s;
 }
 
+kgk_status kgk_gbuffer_records(kgk_scene *s, kgk_svgf_buffer *out) {
+    if (!s || !out) return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_gbuffer_records: NULL argument");
+    KGK_CUDA(cudaSetDevice(s->device));
+    int W, H;
+    const float4 *gpos, *gnrm, *galb, *gemi;
+    kgk_camera cam;
+    if (!svgf_gbuffer(s, &W, &H, &gpos, &gnrm, &galb, &gemi, &cam))
+        return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_gbuffer_records: render a frame with write_gbuffer=1 first");
+    const size_t npx = (size_t)W * H;
+    cudaStream_t st = s->stream;
+    const bool dev = is_device_ptr(out);
+    kgk_svgf_buffer *dst = out;
+    if (!dev) {
+        KGK_TRY(s->staging.reserve(npx * sizeof(kgk_svgf_buffer)));
+        dst = (kgk_svgf_buffer *)s->staging.ptr;
+    }
+    const int g = (int)std::min<size_t>((npx + 255) / 256, 65535);
+    k_gbuffer_to_records<<<g, 256, 0, st>>>(gpos, gnrm, galb, gemi, (int)npx, dst);
+    KGK_CUDA(cudaGetLastError());
+    if (!dev) KGK_CUDA(cudaMemcpyAsync(out, dst, npx * sizeof(kgk_svgf_buffer), cudaMemcpyDeviceToHost, st));
+    KGK_CUDA(cudaStreamSynchronize(st));
+    return KGK_OK;
+}
+
 kgk_status kgk_svgf(kgk_scene *s, const kgk_svgf_config *cfg, const kgk_vec *noisy, kgk_vec *filtered) {
     if (!s || !cfg || !noisy || !filtered) return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_svgf: NULL argument");
     return kgk_svgf_output(s, cfg, noisy, filtered, nullptr, 0);

@@ -168,6 +168,61 @@ def cornell_box():
     return tris, mats, cam
 
 
+def parity_scene(kind):
+    """Small seeded scenes on which the reference's own estimator is compared
+    sample for sample with the reference's render.  Returns (triangles,
+    materials, camera args (origin, dist, rot), textures (list of (h, w, bpp)
+    float32 arrays, indexed by TEXTURE_BASECOLOR_ID), environment or None).
+
+      cornell   cornell_box() as it is: Lambert walls and boxes, a face light
+      disney    the same box with Disney boxes: the short one a rough metal,
+                the tall one a clearcoated dielectric with sheen, sheen tint,
+                specular tint and anisotropy
+      textured  the same box with a textured back wall (RGB, 64 x 48) and
+                floor (RGBA, 32 x 32), seeded; their uvs stay inside
+                [0.02, 0.98], where the reference's nearest fetch
+                (struct_Texture.cuh:12-18) reads inside the texel array
+      env       two displaced Disney icospheres (1,280 triangles each) over a
+                ground quad under a 64 x 32 float32 sky with a sun lobe of
+                peak 100, no face light
+    """
+    if kind == "env":
+        tris, mats, info = icosphere_field(n_meshes=2, subdiv=3, seed=5, box=6.0)
+        env, _ = sky_environment(64, 32, sun_peak=100.0, seed=3)
+        ang, radius, z, tz = 37.0, 12.0, 4.0, 2.5
+        a = np.deg2rad(ang)
+        org = (radius * np.cos(a), radius * np.sin(a), z)
+        pitch = np.rad2deg(np.arctan2(z - tz, radius))
+        cam = dict(origin=org, dist=28.0, rot=(90.0 - pitch, 0.0, ang + 90.0))
+        return tris, mats, cam, [], np.ascontiguousarray(env, np.float32)
+    tris, mats, cam = cornell_box()
+    tris = tris.copy()
+    textures = []
+    if kind == "disney":
+        metal = make_material(DISNEY, (0.9, 0.62, 0.3), metallic=1.0, roughness=0.35, specular=0.5)
+        coat = make_material(DISNEY, (0.2, 0.35, 0.75), roughness=0.6, specular=0.5, specularTint=0.4,
+                             sheen=0.7, sheenTint=0.5, clearcoat=0.8, cloearcoatGloss=0.7, anisotropic=0.4)
+        mats = np.concatenate([mats, np.stack([metal, coat])])
+        tris["material_id"][tris["shape_id"] == 5] = len(mats) - 2
+        tris["material_id"][tris["shape_id"] == 6] = len(mats) - 1
+    elif kind == "textured":
+        rng = CounterRng(17)
+        wall = rng.uniform(48 * 64 * 3, 0.05, 0.95).reshape(48, 64, 3).astype(np.float32)
+        floor = rng.uniform(32 * 32 * 4, 0.05, 0.95).reshape(32, 32, 4).astype(np.float32)
+        textures = [wall, floor]
+        mats = np.concatenate([mats, np.stack([make_material(LAMBERT, (0.8, 0.8, 0.8)),
+                                               make_material(LAMBERT, (0.8, 0.8, 0.8))])])
+        mats["TEXTURE_BASECOLOR_ID"][-2:] = (0, 1)
+        for shape, mat in ((2, len(mats) - 2), (0, len(mats) - 1)):  # back wall, floor
+            sel = tris["shape_id"] == shape
+            tris["material_id"][sel] = mat
+            uv = tris["verts"][sel, 6:9, :2]
+            tris["verts"][sel, 6:9, :2] = 0.02 + 0.96 * uv
+    elif kind != "cornell":
+        raise ValueError(f"unknown parity scene {kind!r}")
+    return canonical(tris), mats, cam, textures, None
+
+
 # --------------------------------------------------------------------------
 # Config 2: displaced icosphere field
 # --------------------------------------------------------------------------

@@ -32,11 +32,24 @@ MATERIAL = np.dtype([("MATERIAL_TYPE_ID", "<i4"), ("TEXTURE_BASECOLOR_ID", "<i4"
 # struct_Ray.cuh:12-15: dir, org, double pad.
 RAY = np.dtype([("dir", "<f4", (4,)), ("org", "<f4", (4,)), ("_dummy", "<f8")], align=True)
 
+# struct_SVGFBuffers.cuh:7-23 `SVGFBuffer` (112 B: two bytes of padding after
+# the two flags).
+SVGF_BUFFER = np.dtype({
+    "names": ["Albedo", "Emission", "Normal", "ColorHistory", "ObjectID", "MaterialID",
+              "PosLastFrameI", "PosLastFrameF", "sampleNum", "MomentOne", "MomentTwo", "Variance",
+              "Depth", "willApplyATrousFilter", "willApplyTemporalAccumulation"],
+    "formats": [("<f4", (4,)), ("<f4", (4,)), ("<f4", (4,)), ("<f4", (4,)), "<i4", "<i4",
+                ("<i4", (2,)), ("<f4", (2,)), "<i4", "<f4", "<f4", "<f4", "<f4", "u1", "u1"],
+    "offsets": [0, 16, 32, 48, 64, 68, 72, 80, 88, 92, 96, 100, 104, 108, 109],
+    "itemsize": 112,
+})
+
 # align=True keeps numpy from repacking the records (dropping the C padding)
 # when arrays are concatenated.
 assert TRIANGLE.itemsize == 156 and TRIANGLE.isalignedstruct
 assert MATERIAL.itemsize == 96
 assert RAY.itemsize == 40
+assert SVGF_BUFFER.itemsize == 112
 
 LAMBERT = 0
 DISNEY = 1

@@ -95,6 +95,54 @@ def classify(tris, rays, ids, t):
     return flags
 
 
+def exact_hit(tri, ray):
+    """The ray/triangle intersection of Triangle::intersectTest
+    (struct_Triangle.cuh:41-57: Cramer's rule, hit when u, v >= 0, u + v <= 1
+    and t >= 1e-5) in exact rational arithmetic on the float32 inputs:
+    (hit, t, u, v) with t, u, v as Fractions (None when the ray is parallel).
+    Settles which answer is geometrically right where the float expressions
+    disagree near an edge."""
+    from fractions import Fraction as Fr
+    f = [Fr(float(c)) for c in np.asarray(tri["verts"][:3, :3], np.float64).ravel()]
+    v0, v1, v2 = f[0:3], f[3:6], f[6:9]
+    o = [Fr(float(c)) for c in ray["org"][:3]]
+    d = [Fr(float(c)) for c in ray["dir"][:3]]
+
+    def sub(a, b):
+        return [a[0] - b[0], a[1] - b[1], a[2] - b[2]]
+
+    def cross(a, b):
+        return [a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0]]
+
+    def dot(a, b):
+        return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]
+    e1, e2, so = sub(v1, v0), sub(v2, v0), sub(o, v0)
+    de2 = cross(d, e2)
+    det = dot(de2, e1)
+    if det == 0:
+        return False, None, None, None
+    se1 = cross(so, e1)
+    t, u, v = dot(se1, e2) / det, dot(de2, so) / det, dot(se1, d) / det
+    return bool(u >= 0 and v >= 0 and u + v <= 1 and t >= Fr(1, 100000)), t, u, v
+
+
+def exact_winner(tris, ray, candidates):
+    """The candidate triangle (-1: none) the ray hits first in exact
+    arithmetic, and whether another candidate ties it exactly."""
+    best, bt, tie = -1, None, False
+    for k in candidates:
+        if k < 0:
+            continue
+        hit, t, _, _ = exact_hit(tris[k], ray)
+        if not hit:
+            continue
+        if bt is None or t < bt:
+            best, bt, tie = int(k), t, False
+        elif t == bt:
+            tie = True
+    return best, tie
+
+
 def closest_bvh(tris, rays):
     L = orc()
     b = L.orc_bvh_build(_ptr(tris), len(tris))
@@ -146,9 +194,25 @@ def env_cdf(env):
     return out
 
 
-def render_compat(tris, mats, cam, width, height, frames, env=None, threads=None):
+def _texture_table(textures):
+    """Reference `Texture` records (pixels, width, height, bpp) over a list of
+    (h, w, bpp) float32 arrays; returns (table or None, count, arrays kept)."""
+    if not textures:
+        return None, 0, []
+    from kagayaki_gb300.structs import KgkTexture
+    keep = [np.ascontiguousarray(t, np.float32) for t in textures]
+    table = (KgkTexture * len(keep))()
+    for i, t in enumerate(keep):
+        table[i].pixels = t.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+        table[i].height, table[i].width, table[i].bpp = t.shape
+    return table, len(keep), keep
+
+
+def render_compat(tris, mats, cam, width, height, frames, env=None, threads=None, textures=None):
     """Returns (frames, height*width, 3) float32 samples and the traversal
-    count.  Pixel 0 is NaN (the reference's seed divides by zero there)."""
+    count.  Pixel 0 is NaN (the reference's seed divides by zero there).
+    textures: list of (h, w, bpp) float32 arrays, indexed by the materials'
+    TEXTURE_BASECOLOR_ID."""
     out = np.empty((frames, width * height, 3), np.float32)
     env_p, hw, hh, hb = None, 0, 0, 0
     if env is not None:
@@ -156,7 +220,9 @@ def render_compat(tris, mats, cam, width, height, frames, env=None, threads=None
         hh, hw, hb = env.shape
         env_p = _ptr(env)
     cam = np.ascontiguousarray(cam, np.float32)
-    n = orc().orc_render_compat(_ptr(tris), len(tris), _ptr(mats), len(mats), None, 0, env_p, hw,
+    table, ntex, _keep = _texture_table(textures)
+    n = orc().orc_render_compat(_ptr(tris), len(tris), _ptr(mats), len(mats),
+                                ctypes.cast(table, _vp) if table is not None else None, ntex, env_p, hw,
                                 hh, hb, _ptr(cam), width, height, frames,
                                 threads or nthreads(), _ptr(out))
     return out, n
@@ -313,8 +379,11 @@ def ref_trace(tris, rays, threads=None):
     return ids, t, ok, nodes, bs.value
 
 
-def ref_render(tris, mats, cam, width, height, frames, env=None, threads=None, gbuf=False):
+def ref_render(tris, mats, cam, width, height, frames, env=None, threads=None, gbuf=False, textures=None):
+    """The reference's render() on the host: (frames, npx, 3) samples, the
+    traversal count and (gbuf=True) the last frame's SVGFBuffer records."""
     out = np.empty((frames, width * height, 3), np.float32)
+    table, ntex, _keep = _texture_table(textures)
     env_p, hw, hh, hb = None, 0, 0, 0
     if env is not None:
         env = np.ascontiguousarray(env, np.float32)
@@ -324,7 +393,8 @@ def ref_render(tris, mats, cam, width, height, frames, env=None, threads=None, g
     gb = None
     if gbuf:
         gb = np.zeros(width * height * ref().ref_sizeof_svgfbuffer(), np.uint8)
-    n = ref().ref_render(_ptr(tris), len(tris), _ptr(mats), len(mats), None, 0, env_p, hw, hh, hb,
+    n = ref().ref_render(_ptr(tris), len(tris), _ptr(mats), len(mats),
+                         ctypes.cast(table, _vp) if table is not None else None, ntex, env_p, hw, hh, hb,
                          _ptr(cam), _ptr(cam), width, height, frames, threads or nthreads(),
                          _ptr(out), _ptr(gb))
     return (out, n, gb) if gbuf else (out, n)

@@ -20,6 +20,8 @@
  *   ref_load_obj       load_object (IO_load_WavefrontObj.cuh:10-127).
  *   ref_tinyobj_parse  tinyobjloader's raw parse, as load_object configures it.
  *   ref_load_image     stbi_loadf.
+ *   ref_export_scene   a scene, its reference BVH and light CDF in a file
+ *                      for the reference's GPU render (oracle/ref_gpu.py).
  *
  * The traversal-call counter replaces struct_stack.cuh (a 37-line fixed-size
  * stack) with an equivalent class whose constructor counts one ray per
@@ -381,6 +383,44 @@ void ref_tinyobj_copy(float *v, float *vn, float *vt, int *corner, int *face) {
     std::memcpy(vt, g_to_vt.data(), g_to_vt.size() * sizeof(float));
     std::memcpy(corner, g_to_corner.data(), g_to_corner.size() * sizeof(int));
     std::memcpy(face, g_to_face.data(), g_to_face.size() * sizeof(int));
+}
+
+/* Writes what the reference's GPU render() needs of a scene to `path`, as
+ * render_prepare and main.cu prepare it (construct_BVH, calculate_Lss,
+ * Convert_BVHTreeFromHostToDevice): the file read by oracle/ref_gpu.py.
+ *   char[8] "KGKREFS1"; int32 n_tris, n_mats, n_nodes, n_faces, n_lss,
+ *   exists_nolight; Triangle[n_tris]; Material[n_mats];
+ *   BVH_node_Device[n_nodes] with face_list holding the int64 offset of the
+ *   node's entries in the face array (-1: none); int32[n_faces];
+ *   float[n_lss].  Returns 0, or -1 when the file cannot be written. */
+static_assert(sizeof(BVH_node_Device) == 72, "BVH_node_Device");
+int ref_export_scene(const Triangle *tris, int n, const Material *mats, int nm, const char *path) {
+    load_scene(tris, n, mats, nm);
+    HOST_Light_strength_sum.clear();
+    HOST_Exists_NoLight = false;
+    calculate_Lss();
+    std::vector<BVH_node_Device> nodes(g_tree.begin(), g_tree.end());
+    std::vector<int> faces;
+    for (auto &nd : nodes) {
+        long long off = -1;
+        if (nd.face_list) {
+            off = (long long)faces.size();
+            faces.insert(faces.end(), nd.face_list, nd.face_list + nd.face_list_size);
+        }
+        std::memcpy(&nd.face_list, &off, sizeof off);
+    }
+    FILE *f = std::fopen(path, "wb");
+    if (!f) return -1;
+    const int hdr[6] = {n, nm, (int)nodes.size(), (int)faces.size(), (int)HOST_Light_strength_sum.size(),
+                        HOST_Exists_NoLight ? 1 : 0};
+    bool ok = std::fwrite("KGKREFS1", 1, 8, f) == 8 && std::fwrite(hdr, sizeof hdr, 1, f) == 1;
+    ok = ok && std::fwrite(tris, sizeof(Triangle), (size_t)n, f) == (size_t)n;
+    ok = ok && std::fwrite(mats, sizeof(Material), (size_t)nm, f) == (size_t)nm;
+    ok = ok && std::fwrite(nodes.data(), sizeof(BVH_node_Device), nodes.size(), f) == nodes.size();
+    ok = ok && std::fwrite(faces.data(), sizeof(int), faces.size(), f) == faces.size();
+    ok = ok && std::fwrite(HOST_Light_strength_sum.data(), sizeof(float), HOST_Light_strength_sum.size(), f) ==
+                   HOST_Light_strength_sum.size();
+    return (std::fclose(f) == 0 && ok) ? 0 : -1;
 }
 
 /* The reference checkout this library was built from (its vendored test

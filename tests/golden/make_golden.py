@@ -16,11 +16,25 @@ Fixtures:
   camera_ref.npz        Camera_SetUpCamera for a few poses
   cdf_ref.npz           calculate_Lss / calculate_Lss_HDR for small inputs
   svgf_ref.npz          ApplySVGF (race-free reading) on two frames
+  parity_scenes_ref.npz per-sample compat renders of the Disney, textured and
+                        environment scenes of scenes.parity_scene (48x48, 6
+                        chained frames), their 256-frame mean/variance at
+                        32x32, and render()'s SVGFBuffer records at 32x32
+  c1_image_ref.npz      the Cornell box at config C1's size (256x256): the
+                        16-sample per-pixel mean and the per-pixel standard
+                        deviation of one sample (from 256 samples), float16,
+                        and all 16 samples of 2048 seeded pixels (float32)
   loader_ref.npz        load_object + load_Textures on the seeded OBJ scene of
                         tests/golden/scene_files.py, and stbi_loadf on its
                         seeded PNG / PNM / .hdr images
 
     python tests/golden/make_golden.py --only loader   # just loader_ref.npz
+    python tests/golden/make_golden.py --only parity   # the two files above
+
+The reference's sample_BXDF (sampling.cuh:15-19) adds into an uninitialised
+array, so its Disney lobe choice depends on stack contents; oracle/Makefile
+builds the reference with -ftrivial-auto-var-init=zero, which gives that
+array its zero-initialised reading and makes the renders reproducible.
 """
 import hashlib
 import os
@@ -68,14 +82,61 @@ def make_loader_golden():
     np.savez_compressed(os.path.join(HERE, "loader_ref.npz"), **out)
 
 
+PARITY_KINDS = ("disney", "textured", "env")
+# samples per pixel of the 32x32 statistics.  The environment scene stops at
+# 128: further on, a direction whose z rounds beyond 1 makes asin return NaN,
+# clamp passes it on and (int)NaN indexes the environment CDF far out of
+# bounds (ImageBasedLighting.cuh:6-31,85-90), which crashes the host build.
+PARITY_N32 = {"disney": 256, "textured": 256, "env": 128}
+
+
+def make_parity_golden():
+    """Reference renders of scenes.parity_scene's Disney, textured and
+    environment scenes, and of the Cornell box at C1's size."""
+    out = {}
+    for kind in PARITY_KINDS:
+        tris, mats, c, tex, env = scenes.parity_scene(kind)
+        cam = orc.camera_setup(c["origin"], c["dist"], c["rot"], 48)
+        frames, nrays = orc.ref_render(tris, mats, cam, 48, 48, 6, env=env, textures=tex)
+        cam32 = orc.camera_setup(c["origin"], c["dist"], c["rot"], 32)
+        many, _, gb = orc.ref_render(tris, mats, cam32, 32, 32, PARITY_N32[kind], env=env, textures=tex,
+                                     gbuf=True)
+        out[f"{kind}_frames"] = frames
+        out[f"{kind}_camera"] = cam
+        out[f"{kind}_rays"] = np.int64(nrays)
+        out[f"{kind}_mean32"] = np.nanmean(many, axis=0)
+        out[f"{kind}_var32"] = np.nanvar(many, axis=0, ddof=1)
+        out[f"{kind}_camera32"] = cam32
+        out[f"{kind}_gbuf32"] = gb
+        out[f"{kind}_n32"] = np.int32(PARITY_N32[kind])
+    np.savez_compressed(os.path.join(HERE, "parity_scenes_ref.npz"), **out)
+
+    tris, mats, c = scenes.cornell_box()
+    cam = orc.camera_setup(c["origin"], c["dist"], c["rot"], 256)
+    sixteen, rays16 = orc.ref_render(tris, mats, cam, 256, 256, 16)
+    many, _ = orc.ref_render(tris, mats, cam, 256, 256, 256)
+    # every sample of 2048 seeded pixels (1..65535) over the 16 chained frames
+    px = np.sort(np.random.default_rng(41).choice(np.arange(1, 256 * 256), 2048, replace=False)).astype(np.int32)
+    np.savez_compressed(os.path.join(HERE, "c1_image_ref.npz"), camera=cam, spp=np.int32(16),
+                        rays16=np.int64(rays16), mean16=np.nanmean(sixteen, axis=0).astype(np.float16),
+                        std1=np.nanstd(many, axis=0, ddof=1).astype(np.float16), n_std=np.int32(256),
+                        px_sample=px, samples16=sixteen[:, px])
+
+
 def main():
     orc.build(ref=True)
     assert orc.ref_available(), "oracle/_ref was not built (needs the reference checkout)"
-    if "--only" in sys.argv and sys.argv[sys.argv.index("--only") + 1] == "loader":
+    only = sys.argv[sys.argv.index("--only") + 1] if "--only" in sys.argv else None
+    if only == "loader":
         make_loader_golden()
         print("loader fixture written to", HERE)
         return
+    if only == "parity":
+        make_parity_golden()
+        print("parity fixtures written to", HERE)
+        return
     make_loader_golden()
+    make_parity_golden()
     assert orc.ref_available(), "oracle/_ref was not built (needs the reference checkout)"
 
     # --- closest hits, Cornell box ---

@@ -2,14 +2,15 @@
 
 compat estimator: per-sample comparison with the reference's own render of
 the Cornell box (golden frames: same xorshift stream, so most samples follow
-the same path and agree to FP32 rounding) and a 3-sigma test of the per-pixel
-mean against the reference's 256-sample statistics.
+the same path and agree to FP32 rounding; the bars are in tests/conftest.py)
+and a 3-sigma test of the per-pixel mean against the reference's 256-sample
+statistics.
 unbiased estimator: analytic furnace scenes (closed emissive box,
 constant-environment convex object)."""
 import numpy as np
 import pytest
 
-from conftest import golden
+from conftest import BAR_CLOSE, BAR_CLOSE_FRAME0, golden, sample_stats
 from kagayaki_gb300 import ESTIMATOR_COMPAT, ESTIMATOR_UNBIASED, Scene, scenes, structs
 from kagayaki_gb300.structs import KgkCamera
 
@@ -40,14 +41,13 @@ def test_compat_samples_follow_the_reference(cornell):
         img, st = cornell.render(cam, W, H, spp=1, estimator=ESTIMATOR_COMPAT, frame_index=f)
         assert st["traversal_overflows"] == 0
         ours.append(img.reshape(-1, 4)[:, :3])
-    ours = np.stack(ours)[:, 1:]
-    ref = ref[:, 1:]
-    rel = np.abs(ours - ref) / np.maximum(np.abs(ref), 1e-3)
-    close = (rel <= 1e-3).all(-1)
-    # FMA contraction and libm differences can flip a discrete decision (RR,
-    # light choice) on a few paths; those diverge for the rest of the chain
-    assert close[0].mean() > 0.97, close[0].mean()
-    assert close.mean() > 0.9, close.mean()
+    # per sample within 1e-4 relative (the bars and what explains the rest:
+    # tests/conftest.py)
+    st = sample_stats(np.stack(ours), ref)
+    print("Cornell 48x48 x 8 frames", st)
+    assert st["close_frame0"] > BAR_CLOSE_FRAME0, st
+    assert st["close"] > BAR_CLOSE, st
+    assert st["chains_in_step"] > 0.9, st
 
 
 def test_compat_mean_within_3_sigma_of_reference(cornell):

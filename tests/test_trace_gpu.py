@@ -116,13 +116,25 @@ def test_displaced_icosphere_field_full_size_property():
         ids, t, st = s.trace_closest(rays, with_stats=True)
     assert st["traversal_overflows"] == 0
     oids, ot = orc.closest_bvh(tris, rays)
-    # exact-t ties and edge grazes are rare on curved meshes; classify the
-    # disagreements by brute force over the triangles of both answers
+    # exact-t ties and edge grazes are rare on curved meshes: every ray whose
+    # answer differs is classified, by brute force over all 5.2M triangles
+    # (an exact-t tie, or a reference barycentric within 4 ulp of an edge) or
+    # else by exact rational arithmetic on the two candidate triangles (the
+    # ray really hits ours first: the reference expression's rounding put it
+    # on the other triangle); none may be left unexplained
     bad = np.nonzero(ids != oids)[0]
     assert len(bad) <= 1e-4 * len(rays), (len(bad), b)
+    if len(bad):
+        flags = orc.classify(tris, rays[bad], oids[bad], ot[bad])
+        exact = np.array([orc.exact_winner(tris, rays[i], (int(ids[i]), int(oids[i])))[0] == ids[i]
+                          for i in bad])
+        print(f"{len(bad)} of {len(rays)} rays differ: {int((flags & 1).sum())} exact-t ties, "
+              f"{int((flags & 2).sum())} edge grazes, {int((exact & (flags == 0)).sum())} where exact "
+              f"arithmetic confirms ours")
+        assert ((flags != 0) | exact).all(), f"{int(((flags == 0) & ~exact).sum())} unexplained id mismatches"
     hit = (oids >= 0) & (ids == oids)
     rel = np.abs(t[hit] - ot[hit]) / ot[hit]
-    assert np.quantile(rel, 0.9999) <= T_REL_TOL
+    assert rel.max() <= T_REL_TOL, rel.max()
 
 
 def test_watertight_closed_mesh():
