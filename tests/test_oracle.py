@@ -40,14 +40,15 @@ def test_exact_intersection_agrees_with_reference_test_away_from_edges():
     tris, _, _ = scenes.cornell_box()
     rays = scenes.parity_rays(64, C1_LO, C1_HI, seed=5)
     checked = 0
-    for r in rays:
+    for i in range(len(rays)):
+        r = rays[i:i + 1]
         for k in range(0, len(tris), 3):
             t, u, v = (np.zeros(1, np.float32) for _ in range(3))
             hit = orc.orc().orc_intersect_ref(tris[k:k + 1].ctypes.data, r.ctypes.data, t.ctypes.data,
                                               u.ctypes.data, v.ctypes.data)
             if min(abs(u[0]), abs(v[0]), abs(1 - u[0] - v[0])) < 1e-3 or abs(t[0]) < 1e-3:
                 continue
-            ehit, et, eu, ev = orc.exact_hit(tris[k], r)
+            ehit, et, eu, ev = orc.exact_hit(tris[k], r[0])
             assert bool(hit) == ehit
             if ehit:
                 assert abs(float(et) - t[0]) <= 1e-5 * abs(t[0])
