@@ -28,12 +28,42 @@ _i32 = ctypes.c_int
 _f32 = ctypes.c_float
 
 
+# The reference's vendored stb_image_write.h includes the C headers by
+# Windows paths relative to itself (external_lib/stb/stb_image_write.h:154,
+# 211-217, 244).  The `ref` build satisfies them with forwarding headers at
+# the same relative paths below an include directory six levels deep inside
+# oracle/_ref, so FileIO/IO_save_png.cuh compiles unchanged.
+WIN_HEADERS = {
+    "Program Files (x86)/Windows Kits/10/Include/10.0.22621.0/ucrt/stdlib.h": "stdlib.h",
+    "Program Files (x86)/Windows Kits/10/Include/10.0.22621.0/ucrt/stdio.h": "stdio.h",
+    "Program Files (x86)/Windows Kits/10/Include/10.0.22621.0/ucrt/string.h": "string.h",
+    "Program Files (x86)/Windows Kits/10/Include/10.0.22621.0/ucrt/math.h": "math.h",
+    "Program Files (x86)/Windows Kits/10/Include/10.0.22621.0/ucrt/assert.h": "assert.h",
+    "Program Files (x86)/Microsoft Visual Studio/2019/Community/VC/Tools/MSVC/14.29.30133/include/stdarg.h":
+        "stdarg.h",
+}
+
+
+def _win_include_shims():
+    """Writes the forwarding headers; returns the include directory."""
+    root = os.path.join(HERE, "_ref", "winshim")
+    inc = os.path.join(root, "i1", "i2", "i3", "i4", "i5", "i6")
+    os.makedirs(inc, exist_ok=True)
+    for rel, std in WIN_HEADERS.items():
+        path = os.path.join(root, rel)
+        os.makedirs(os.path.dirname(path), exist_ok=True)
+        with open(path, "w") as f:
+            f.write(f"#include <{std}>\n")
+    return inc
+
+
 def build(ref=False):
     """Builds liborc.so (and the reference library when ref=True; the caller
     checks that the reference checkout exists)."""
     subprocess.run(["make", "-s", "-C", HERE, "orc"], check=True)
     if ref:
-        subprocess.run(["make", "-s", "-C", HERE, "ref", "REF_DIR=" + reference_dir()], check=True)
+        subprocess.run(["make", "-s", "-C", HERE, "ref", "REF_DIR=" + reference_dir(),
+                        "WINSHIM=" + _win_include_shims()], check=True)
 
 
 def _ptr(a):
@@ -305,6 +335,12 @@ def ref():
         L.ref_tinyobj_parse.restype = _i32
         L.ref_tinyobj_copy.argtypes = [_vp, _vp, _vp, _vp, _vp]
         L.ref_source_dir.restype = ctypes.c_char_p
+        L.ref_export_scene.argtypes = [_vp, _i32, _vp, _i32, ctypes.c_char_p]
+        L.ref_export_scene.restype = _i32
+        L.ref_save_png_bytes.argtypes = [_vp, ctypes.c_char_p, _vp]
+        L.ref_save_png_bytes.restype = _i32
+        L.ref_image_size.argtypes = [_vp, _vp]
+        L.ref_image_size.restype = _i32
         _ref = L
     return _ref
 

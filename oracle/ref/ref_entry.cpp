@@ -20,6 +20,7 @@
  *   ref_load_obj       load_object (IO_load_WavefrontObj.cuh:10-127).
  *   ref_tinyobj_parse  tinyobjloader's raw parse, as load_object configures it.
  *   ref_load_image     stbi_loadf.
+ *   ref_save_png_bytes save_png's bytes for an image (written, read back).
  *   ref_export_scene   a scene, its reference BVH and light CDF in a file
  *                      for the reference's GPU render (oracle/ref_gpu.py).
  *
@@ -54,6 +55,7 @@ public:
 #include "NextEventEstimation.cuh"
 #include "render.cuh"
 #include "FileIO/IO_load_WavefrontObj.cuh"
+#include "FileIO/IO_save_png.cuh"
 
 #include <unistd.h>
 
@@ -421,6 +423,31 @@ int ref_export_scene(const Triangle *tris, int n, const Material *mats, int nm, 
     ok = ok && std::fwrite(HOST_Light_strength_sum.data(), sizeof(float), HOST_Light_strength_sum.size(), f) ==
                    HOST_Light_strength_sum.size();
     return (std::fclose(f) == 0 && ok) ? 0 : -1;
+}
+
+/* save_png (FileIO/IO_save_png.cuh:34-56) on a full image_sizeX x
+ * image_sizeY buffer of Vec (its gamma, clamp and truncation, then
+ * stbi_write_png), written as <prefix>000.png and read back with stbi_load:
+ * rgba receives the image's bytes (4 per pixel).  Returns 0, or -1 when the
+ * file could not be written or read. */
+int ref_save_png_bytes(const Vec *image, const char *prefix, unsigned char *rgba) {
+    const size_t npx = (size_t)image_sizeX * image_sizeY;
+    std::vector<Vec> buf(image, image + npx);   // save_png converts its argument in place
+    save_png(buf.data(), 1, prefix);
+    const std::string name = std::string(prefix) + "000.png";
+    int w = 0, h = 0, comp = 0;
+    unsigned char *px = stbi_load(name.c_str(), &w, &h, &comp, 4);
+    std::remove(name.c_str());
+    if (!px || w != image_sizeX || h != image_sizeY) return -1;
+    std::memcpy(rgba, px, npx * 4);
+    stbi_image_free(px);
+    return 0;
+}
+
+int ref_image_size(int *w, int *h) {
+    *w = image_sizeX;
+    *h = image_sizeY;
+    return 0;
 }
 
 /* The reference checkout this library was built from (its vendored test

@@ -24,12 +24,17 @@ Fixtures:
                         16-sample per-pixel mean and the per-pixel standard
                         deviation of one sample (from 256 samples), float16,
                         and all 16 samples of 2048 seeded pixels (float32)
+  tonemap_ref.npz       save_png's bytes (the reference's gamma, clamp and
+                        truncation, through its PNG writer and read back)
+                        for every step of the byte function +-8 ulp, special
+                        and random values
   loader_ref.npz        load_object + load_Textures on the seeded OBJ scene of
                         tests/golden/scene_files.py, and stbi_loadf on its
                         seeded PNG / PNM / .hdr images
 
     python tests/golden/make_golden.py --only loader   # just loader_ref.npz
     python tests/golden/make_golden.py --only parity   # the two files above
+    python tests/golden/make_golden.py --only tonemap  # tonemap_ref.npz
 
 The reference's sample_BXDF (sampling.cuh:15-19) adds into an uninitialised
 array, so its Disney lobe choice depends on stack contents; oracle/Makefile
@@ -45,6 +50,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.dirname(HERE))
 
 from kagayaki_gb300 import scenes, structs  # noqa: E402
 from oracle import orc  # noqa: E402
@@ -123,6 +129,54 @@ def make_parity_golden():
                         px_sample=px, samples16=sixteen[:, px])
 
 
+def tonemap_inputs():
+    """Inputs of the tone-map fixture: every step of the byte function (found
+    with the oracle's restatement) +-8 ulp, special values and seeded random
+    values, as (n, 3) float32."""
+    import ctypes
+
+    def byte(x):
+        img = np.zeros((1, 4), np.float32)
+        img[0, 0] = x
+        return int(orc.tonemap(img)[0, 0])
+    steps = []
+    for k in range(1, 256):
+        lo, hi = 0, 0x7f800000
+        while lo < hi:
+            mid = (lo + hi) // 2
+            if byte(np.uint32(mid).view(np.float32)) >= k:
+                hi = mid
+            else:
+                lo = mid + 1
+        steps.append(lo)
+    around = (np.array(steps, np.int64)[:, None] + np.arange(-8, 9)[None, :]).ravel()
+    around = around[(around >= 0) & (around <= 0x7f800000)].astype(np.uint32).view(np.float32)
+    rng = np.random.default_rng(12)
+    special = np.array([0.0, -0.0, 1e-45, 1e-38, 1.0, 1.0000001, 2.0, 1e30, np.inf, -1e-30, -3.0, -np.inf, np.nan],
+                       np.float32)
+    vals = np.concatenate([around, special, rng.uniform(0, 1.3, 12000).astype(np.float32),
+                           np.exp(rng.uniform(-20, 1, 4000)).astype(np.float32)])
+    vals = np.concatenate([vals, np.zeros((-len(vals)) % 3, np.float32)])
+    return vals.reshape(-1, 3)
+
+
+def make_tonemap_golden():
+    """save_png's bytes (FileIO/IO_save_png.cuh:34-56, the reference's own
+    code, its PNG read back) for the inputs of tonemap_inputs()."""
+    import ctypes
+    import tempfile
+    w, h = ctypes.c_int(), ctypes.c_int()
+    orc.ref().ref_image_size(ctypes.byref(w), ctypes.byref(h))
+    vals = tonemap_inputs()
+    img = np.zeros((w.value * h.value, 4), np.float32)
+    img[:len(vals), :3] = vals
+    out = np.zeros((w.value * h.value, 4), np.uint8)
+    with tempfile.TemporaryDirectory() as d:
+        rc = orc.ref().ref_save_png_bytes(img.ctypes.data, os.path.join(d, "ref").encode(), out.ctypes.data)
+    assert rc == 0
+    np.savez_compressed(os.path.join(HERE, "tonemap_ref.npz"), inputs=vals, rgba=out[:len(vals)])
+
+
 def main():
     orc.build(ref=True)
     assert orc.ref_available(), "oracle/_ref was not built (needs the reference checkout)"
@@ -135,6 +189,11 @@ def main():
         make_parity_golden()
         print("parity fixtures written to", HERE)
         return
+    if only == "tonemap":
+        make_tonemap_golden()
+        print("tone-map fixture written to", HERE)
+        return
+    make_tonemap_golden()
     make_loader_golden()
     make_parity_golden()
     assert orc.ref_available(), "oracle/_ref was not built (needs the reference checkout)"

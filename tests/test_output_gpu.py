@@ -70,6 +70,24 @@ def test_device_tonemap_matches_host_bytes():
     assert len(np.unique(host[..., :3])) == 256
 
 
+def test_device_tonemap_equals_reference_save_png():
+    """The device tone mapping against the bytes of the reference's own
+    save_png (tests/golden/tonemap_ref.npz)."""
+    torch = pytest.importorskip("torch")
+    import ctypes
+    from conftest import golden
+    from kagayaki_gb300._lib import check, lib
+    g = golden("tonemap_ref.npz")
+    img = np.zeros((1, len(g["inputs"]), 4), np.float32)
+    img[0, :, :3] = g["inputs"]
+    dev_in = torch.from_numpy(img).cuda()
+    dev_out = torch.zeros((1, len(g["inputs"]), 4), dtype=torch.uint8, device="cuda")
+    check(lib().kgk_tonemap_rgba8(ctypes.c_void_p(dev_in.data_ptr()), len(g["inputs"]), 1,
+                                  ctypes.c_void_p(dev_out.data_ptr())))
+    torch.cuda.synchronize()
+    assert np.array_equal(dev_out.cpu().numpy()[0], g["rgba"])
+
+
 def _scene_and_cams(H):
     tris, mats, c = scenes.cornell_box()
     cams = [camera_setup((c["origin"][0] + 0.03 * f, c["origin"][1], c["origin"][2]), c["dist"], c["rot"], H)

@@ -7,7 +7,7 @@ import numpy as np
 import pytest
 
 from conftest import golden
-from kagayaki_gb300 import ESTIMATOR_UNBIASED, Scene, camera_setup, scenes
+from kagayaki_gb300 import ESTIMATOR_COMPAT, ESTIMATOR_UNBIASED, Scene, camera_setup, scenes
 from kagayaki_gb300._lib import check, lib
 from kagayaki_gb300.structs import KgkSvgfConfig
 
@@ -54,6 +54,43 @@ def test_svgf_apply_matches_reference_two_frames():
     a, b = cur1.view(rec), g["out_cur1"].view(rec)
     assert np.array_equal(a["ids"], b["ids"])
     assert (a["fl"] == b["fl"]).mean() > 0.995
+
+
+def test_svgf_apply_follows_the_reference_over_an_orbit():
+    """Config C3's comparison, frame by frame: kgk_svgf_apply (ApplySVGF,
+    SVGF.cuh:495-522) over a 16-frame camera orbit of the Cornell box at
+    256 x 256 against the oracle's race-free restatement of the reference's
+    filter (orc.svgf_compat, bit-exact with the reference's own code on the
+    golden frames, tests/test_oracle.py).  Both take the same inputs each
+    frame - the compat frame and render()'s SVGFBuffer records
+    (kgk_gbuffer_records) - and carry their own state from frame to frame
+    as main.cu does (prev = this frame's records after filtering)."""
+    from oracle import orc
+    tris, mats, c = scenes.cornell_box()
+    W = H = 256
+    npx = W * H
+    prev_g = np.zeros(npx * 112, np.uint8)
+    prev_o = np.zeros(npx * 112, np.uint8)
+    worst = 1.0
+    with Scene(tris, mats) as s:
+        s.build_bvh()
+        for f in range(16):
+            # 0.25 degrees of yaw and 0.1 units of sideways motion per frame
+            org = (c["origin"][0] + 0.1 * f, c["origin"][1], c["origin"][2])
+            cam = camera_setup(org, c["dist"], (c["rot"][0], c["rot"][1] + 0.25 * f, c["rot"][2]), H)
+            noisy, _ = s.render(cam, W, H, spp=1, estimator=ESTIMATOR_COMPAT, frame_index=f, write_gbuffer=True)
+            recs = s.gbuffer_records(W, H).view(np.uint8)
+            res = np.ascontiguousarray(noisy.reshape(-1, 4))
+            res[:, 3] = 0.0
+            r_g, f_g, cur_g = res.copy(), np.zeros_like(res), recs.copy()
+            r_o, f_o, cur_o = res.copy(), np.zeros_like(res), recs.copy()
+            _run_apply(r_g, f_g, prev_g, cur_g, W, H, f)
+            orc.svgf_compat(W, H, r_o, f_o, prev_o, cur_o, f)
+            ok = _close(f_g[1:, :3], f_o[1:, :3])
+            worst = min(worst, float(ok.mean()))
+            assert ok.mean() > 0.995, (f, ok.mean())
+            prev_g, prev_o = cur_g, cur_o
+    print("SVGF orbit 256x256 x 16 frames: worst frame within 1e-4 of the race-free reference", worst)
 
 
 def test_svgf_apply_rejects_bad_sizes():
