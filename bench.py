@@ -713,14 +713,20 @@ def gpu_reference_c1():
         from kagayaki_gb300 import scenes
         tris, mats, _ = scenes.cornell_box()
         cam = c1_camera(256, oracle=True)
-        first, _ = orc.render_compat(tris, mats, cam, 256, 256, 1)
+        frames, _ = orc.render_compat(tris, mats, cam, 256, 256, 16)
         px = np.random.default_rng(41).choice(np.arange(1, 256 * 256), 4096, replace=False)
-        r = ref_gpu.render_c1(cam, check_samples=(px, first[0][px]))
+        r = ref_gpu.render_c1(cam, check_samples=(px, frames[0][px]))
     except Exception as e:
         return {"unavailable": f"{type(e).__name__}: {e}"}
+    # image check: the reference GPU frame's per-pixel 16-sample means against
+    # the oracle's, sigma from the oracle's 16 samples (two 16-sample means)
+    om = frames[:, 1:].mean(0)
+    sig = frames[:, 1:].std(0, ddof=1) * np.sqrt(2.0 / 16) + 1e-4
+    outside = float((np.abs(r["mean"][1:256 * 256] - om) > 3 * sig).any(-1).mean())
     return {"workload": "cornell-36tris-256x256-16spp-compat", "value": round(r["mrays"], 2), "unit": "Mrays/s",
             "ms_per_frame": round(r["ms_per_frame"], 3), "rays_per_frame": r["rays_per_frame"],
             "first_launch_within_1e-3_of_oracle": r["first_launch_agreement"],
+            "frame_pixels_outside_3sigma_of_oracle": outside,
             "registers": r["registers"], "stack_bytes": r["stack_bytes"],
             "kind": "the reference's render kernel (render.cuh:21-49) compiled for sm_103a from its own headers "
                     "(oracle/ref/ref_gpu.cu), launched as main.cu launches it, CUDA events around each launch; "

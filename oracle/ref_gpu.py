@@ -196,22 +196,24 @@ def _launch(cu, mod, args, W, H, stream=None):
     cu.ck(cu.L.cuLaunchKernel(mod.fn, grid, 1, 1, 256, 1, 1, 0, stream, params, None), "cuLaunchKernel")
 
 
-def render_c1(cam, W=256, H=256, spp=16, repeats=2, check_samples=None):
+def render_c1(cam, W=256, H=256, spp=16, repeats=2, check_samples=None, cubin=None):
     """Times the reference's render over `spp` chained one-sample launches of
     the Cornell box (one C1 frame), `repeats` times after a warm-up frame.
     check_samples: (pixel ids, first-frame samples (n, 3)) of the reference's
     host build, compared with the first launch's output.  Returns a dict:
     ms per frame (CUDA events around each launch, summed), rays per frame
     (traversal calls counted by the counting build), the agreement of the
-    first frame with the host build, the kernel's registers and stack."""
+    first frame with the host build, the warm-up frame's per-pixel mean
+    (W*H + 1, 3; position 0 unused), the kernel's registers and stack."""
     why = available()
     if why:
         raise RuntimeError(why)
     name = open(NAME_FILE).read().strip()
+    cubin = cubin or CUBIN
     sc = _read_scene(SCENE_C1)
     cu = _Cuda()
     try:
-        mod = _Module(cu, CUBIN, name)
+        mod = _Module(cu, cubin, name)
         regs, lmem = ctypes.c_int(), ctypes.c_int()
         cu.ck(cu.L.cuFuncGetAttribute(ctypes.byref(regs), 4, mod.fn), "registers")   # NUM_REGS
         cu.ck(cu.L.cuFuncGetAttribute(ctypes.byref(lmem), 3, mod.fn), "local size")  # LOCAL_SIZE_BYTES
@@ -223,17 +225,18 @@ def render_c1(cam, W=256, H=256, spp=16, repeats=2, check_samples=None):
         for e in ev:
             cu.ck(cu.L.cuEventCreate(ctypes.byref(e), 0), "cuEventCreate")
         agree = None
-        # warm-up frame (also the correctness check of its first launch)
+        # warm-up frame: its per-pixel mean, and the check of its first launch
+        mean = np.zeros((W * H + 1, 3), np.float64)
         for f in range(spp):
             _launch(cu, mod, args, W, H)
+            cu.ck(cu.L.cuCtxSynchronize(), "render (warm-up)")
+            res = cu.get(d_result, 16 * (W * H + 1), np.float32).reshape(-1, 4)[:, :3]
+            mean += res
             if f == 0 and check_samples is not None:
-                cu.ck(cu.L.cuCtxSynchronize(), "render (first launch)")
-                res = cu.get(d_result, 16 * (W * H + 1), np.float32).reshape(-1, 4)[:, :3]
                 px, ref = check_samples
-                ours = res[px]
-                rel = np.abs(ours - ref) / np.maximum(np.abs(ref), 1e-4)
+                rel = np.abs(res[px] - ref) / np.maximum(np.abs(ref), 1e-4)
                 agree = float((rel.max(-1) <= 1e-3).mean())
-        cu.ck(cu.L.cuCtxSynchronize(), "render (warm-up)")
+        mean /= spp
         ms = []
         for r in range(repeats):
             cu.ck(cu.L.cuMemsetD8_v2(_u64(seeds), 0, ctypes.c_size_t(8 * (W * H + 1))), "zero randSeeds")
@@ -264,7 +267,7 @@ def render_c1(cam, W=256, H=256, spp=16, repeats=2, check_samples=None):
         cu.close()
     best = min(ms)
     return dict(ms_per_frame=best, ms_all=ms, rays_per_frame=rays, mrays=rays / (best / 1e3) / 1e6,
-                first_launch_agreement=agree, registers=regs.value, stack_bytes=lmem.value,
+                first_launch_agreement=agree, mean=mean, registers=regs.value, stack_bytes=lmem.value,
                 launches_per_frame=spp, pixels=W * H)
 
 
