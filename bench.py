@@ -575,7 +575,7 @@ def run_mlp(args):
                                      "kernel": "k_infer_tc (tcgen05)"},
                        "training_step": {"ms": round(tt * 1e3, 3), "tflops": round(trn_tf, 2),
                                          "frac_of_bf16_peak": round(trn_tf / peak, 4),
-                                         "kernel": "k_train_fb + k_train_dw (mma.sync)"}}
+                                         "kernel": "k_train_fb_tc + k_train_dw_tc (tcgen05, TMA)"}}
 
     n, ti, w64 = measure(64, 65536)
     _, _, w128 = measure(128, 1 << 18)

@@ -496,10 +496,11 @@ kgk_status kgk_nrc_get_weights(kgk_scene *scene, float *w, size_t n);
 kgk_status kgk_nrc_infer(kgk_scene *scene, const float *raw, size_t n, float *out);
 /* Gradient of the mean relative-L2 loss over the batch w.r.t. the weights
  * (as many floats as the weights, loss scale removed) and the loss; weights
- * unchanged. */
+ * unchanged.  raw / target: host or device; grad and loss: host memory. */
 kgk_status kgk_nrc_gradients(kgk_scene *scene, const float *raw, const float *target, size_t n,
                              float *grad, float *loss);
-/* `steps` Adam steps on one batch; loss = the last step's loss. */
+/* `steps` Adam steps on one batch; loss (host memory, may be NULL) = the
+ * last step's loss. */
 kgk_status kgk_nrc_train(kgk_scene *scene, const float *raw, const float *target, size_t n,
                          int32_t steps, float *loss);
 /* Current dynamic loss scale. */

@@ -13,11 +13,15 @@
 // GEMMs in a second; Adam updates FP32 master weights and rewrites the BF16
 // image.
 // No counterpart in the reference.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_bf16.h>
 
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <mutex>
+#include <string>
 #include <vector>
 
 #include "kgk_device.cuh"
@@ -342,6 +346,19 @@ __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.
 // Row r of a 128B-swizzled K-major tile: 16-byte chunk c of the row.
 __device__ __forceinline__ uint32_t sw_off(int r, int c) { return (uint32_t)r * 128u + ((uint32_t)(c ^ (r & 7)) << 4); }
 
+// The same shared-memory bytes read as an MN-major operand: a 128-byte
+// swizzled tile whose rows run along K and whose 64 contiguous elements run
+// along M or N (the 128B-swizzle atom is 8 K-rows x 128 B either way).
+// lbo = byte distance between 64-element atoms along M / N, sbo = byte
+// distance between groups of 8 K-rows.
+__device__ __forceinline__ uint64_t sw128_desc_mn(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+    return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+           ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | ((uint64_t)1u << 46) | ((uint64_t)2u << 61);
+}
+
+// Instruction descriptor with B MN-major (bit 16, "transpose B").
+__host__ __device__ constexpr uint32_t idesc_bf16_bmn(int M, int N) { return idesc_bf16(M, N) | (1u << 16); }
+
 }  // namespace tc
 
 // Named barrier of one warpgroup (ids 1..4; 0 is __syncthreads), and its OR
@@ -508,6 +525,264 @@ __global__ void __launch_bounds__(128 * tc::Tc<W>::kGroups) k_infer_tc(const uns
         bar_wait(bar, phase ^ 1u);
         if (r == 0) atomicExch(err, 1);
     }
+    fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem - (uint32_t)W * (uint32_t)g),
+                     "r"(T::kTmemCols)
+                     : "memory");
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Training forward and backward on the 5th-generation tensor cores.  The CTA
+// layout is k_infer_tc's: the weights once in shared memory (K-major,
+// 128-byte swizzle), one 128-sample tile per warpgroup (thread r = row r =
+// tensor-memory lane r), a W-column FP32 accumulator per warpgroup.  Per tile:
+//   forward   Z_l = H_l W_l^T (A = H_l, B = W_l, both K-major), l = 0..4;
+//             H_{l+1} = bf16(relu(Z_l)), the ReLU derivative kept as bits;
+//             Y = H_5 W_5^T (N = 16, 3 live outputs);
+//   loss      relative L2 against the target, d/dY with the denominator held,
+//             times the loss scale: dZ_5 = (dy0, dy1, dy2, 0, ...);
+//   backward  dA_{l-1} = dZ_l W_l with the same weight tiles read as an
+//             MN-major B operand (K = the layer's outputs along the tile rows,
+//             N = its inputs along the swizzled 128-byte rows), and
+//             dZ_{l-1} = bf16(dA_{l-1} * relu'(Z_{l-1})), l = 5..1.
+// Each H_l and dZ_l row goes to the global scratch (BF16, W per row, the
+// layout k_train_dw_tc reads); the rows of the last tile past the sample
+// count are written too, with dY = 0.  Every mbarrier wait is bounded; a
+// timeout sets *err and ends the CTA after a last bounded wait for its MMAs,
+// freeing its tensor memory.
+// ---------------------------------------------------------------------------
+template <int W>
+__global__ void __launch_bounds__(128 * tc::Tc<W>::kGroups) k_train_fb_tc(
+    const unsigned short *__restrict__ img, const float *__restrict__ raw, int raw_stride,
+    const float *__restrict__ target, int tgt_stride, int n, const int *n_dev, const float *scale_p,
+    unsigned short *Hs, unsigned short *Ds, size_t layer_stride, float *loss_sum, int *err) {
+    using namespace tc;
+    using T = Tc<W>;
+    constexpr int kG = T::kGroups, P = Net<W>::kPitch, kMW = W / 32;
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    const uint32_t pad = (1024u - (smem_u32(smem_raw) & 1023u)) & 1023u;
+    unsigned char *sm = smem_raw + pad;
+    const uint32_t s0 = smem_u32(sm);
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int g = tid >> 7, r = tid & 127;
+    const int wgbar = 1 + g;
+    constexpr int kChunks = W / 8;
+    for (int i = tid; i < (kLayers * W + kOutRows) * kChunks; i += blockDim.x) {
+        const int row = i / kChunks, c = i % kChunks;
+        uint32_t dst;
+        if (row < kLayers * W) {
+            const int l = row / W;
+            if (c >= Net<W>::in(l) / 8) continue;
+            dst = T::layer_off(l) + (uint32_t)(c >> 3) * T::kWSub + sw_off(row % W, c & 7);
+        } else {
+            dst = T::kOutOff + (uint32_t)(c >> 3) * kOutSub + sw_off(row - kLayers * W, c & 7);
+        }
+        *reinterpret_cast<uint4 *>(sm + dst) = *reinterpret_cast<const uint4 *>(img + (size_t)row * P + c * 8);
+    }
+    const uint32_t bar = s0 + T::kBarOff + 8u * (uint32_t)g;
+    if (r == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(s0 + T::kSlotOff),
+                     "r"(T::kTmemCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    fence_async_smem();
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tmem = *reinterpret_cast<volatile uint32_t *>(sm + T::kSlotOff) + (uint32_t)W * (uint32_t)g;
+    const uint32_t trow = tmem + ((uint32_t)((warp & 3) * 32) << 16);
+    const int total = n_dev ? min(*n_dev, n) : n;
+    const int padded = (total + 127) & ~127;  // whole tiles: k_train_dw_tc reads 64-row boxes
+    const float S = *scale_p;
+    const float inv_n = 1.0f / (3.0f * (float)max(total, 1));
+    float lsum = 0.0f;
+    uint32_t phase = 0;
+    bool failed = false;
+    unsigned char *A = sm + T::kAOff + (uint32_t)g * T::kATile;
+    const uint32_t a_addr = s0 + T::kAOff + (uint32_t)g * T::kATile;
+    // Issues one layer's MMAs into the accumulator (forward: Z = A W^T;
+    // backward: dA = A W, the weights read MN-major), commits and waits
+    // (bounded); false when the wait timed out in any thread of the group.
+    auto run_mma = [&](bool backward, int l) -> bool {
+        fence_async_smem();
+        fence_before();
+        wg_sync(wgbar);
+        if (r == 0) {
+            fence_after();
+            const bool last = l == kLayers;
+            const uint32_t boff = last ? T::kOutOff : T::layer_off(l);
+            const uint32_t bsub = last ? kOutSub : T::kWSub;
+            if (!backward) {
+                const int nk = Net<W>::in(l) / 16;
+                const uint32_t id = last ? idesc_bf16(128, 16) : idesc_bf16(128, W);
+                for (int kk = 0; kk < nk; ++kk) {
+                    const uint32_t j = (uint32_t)kk >> 2, o = 2u * (uint32_t)(kk & 3);
+                    mma_bf16(tmem, sw128_desc(a_addr + j * kSub) + o, sw128_desc(s0 + boff + j * bsub) + o, id,
+                             kk > 0 ? 1u : 0u);
+                }
+            } else {
+                // K = layer l's outputs (16 rows of the output layer, else W),
+                // N = its W inputs in W / 64 atoms, the sub-tiles bsub apart
+                const int nk = last ? 1 : W / 16;
+                const uint32_t id = idesc_bf16_bmn(128, W);
+                for (int kk = 0; kk < nk; ++kk) {
+                    const uint32_t j = (uint32_t)kk >> 2, o = 2u * (uint32_t)(kk & 3);
+                    mma_bf16(tmem, sw128_desc(a_addr + j * kSub) + o,
+                             sw128_desc_mn(s0 + boff + (uint32_t)kk * 2048u, bsub, 1024u), id, kk > 0 ? 1u : 0u);
+                }
+            }
+            commit(bar);
+        }
+        const bool ok = bar_wait(bar, phase);
+        phase ^= 1u;
+        if (wg_sync_or(wgbar, !ok)) return false;
+        fence_after();
+        return true;
+    };
+    for (int tile = blockIdx.x * kG + g; tile * kRows < padded; tile += gridDim.x * kG) {
+        const int q = tile * kRows + r;
+        const bool live = q < total, store = q < padded;
+        unsigned short *hrow = Hs + (size_t)q * W, *drow = Ds + (size_t)q * W;
+        {
+            float rw[kRaw];
+#pragma unroll
+            for (int k = 0; k < kRaw; ++k) rw[k] = live ? raw[(size_t)q * raw_stride + k] : 0.0f;
+            float f[64];
+            encode_row(rw, f);
+#pragma unroll
+            for (int c = 0; c < 8; ++c) {
+                uint4 v;
+                v.x = pack2(f[8 * c + 0], f[8 * c + 1]);
+                v.y = pack2(f[8 * c + 2], f[8 * c + 3]);
+                v.z = pack2(f[8 * c + 4], f[8 * c + 5]);
+                v.w = pack2(f[8 * c + 6], f[8 * c + 7]);
+                *reinterpret_cast<uint4 *>(A + sw_off(r, c)) = v;
+                if (store) *reinterpret_cast<uint4 *>(hrow + 8 * c) = v;
+            }
+        }
+        uint32_t msk[kLayers][kMW];
+        float y[3] = {0.0f, 0.0f, 0.0f};
+        for (int l = 0; l <= kLayers; ++l) {
+            if (!run_mma(false, l)) {
+                failed = true;
+                break;
+            }
+            if (l < kLayers) {
+                unsigned short *hnext = hrow + (size_t)(l + 1) * layer_stride;
+#pragma unroll
+                for (int cb = 0; cb < W / 16; ++cb) {
+                    float v[16];
+                    tmem_ld16(trow + 16 * cb, v);
+                    tmem_wait_ld();
+                    uint32_t bits = 0;
+#pragma unroll
+                    for (int i = 0; i < 16; ++i) bits |= (v[i] > 0.0f ? 1u : 0u) << i;
+                    if (cb & 1) msk[l][cb >> 1] |= bits << 16;
+                    else msk[l][cb >> 1] = bits;
+                    uint4 lo, hi;
+                    lo.x = pack2_relu(v[0], v[1]);
+                    lo.y = pack2_relu(v[2], v[3]);
+                    lo.z = pack2_relu(v[4], v[5]);
+                    lo.w = pack2_relu(v[6], v[7]);
+                    hi.x = pack2_relu(v[8], v[9]);
+                    hi.y = pack2_relu(v[10], v[11]);
+                    hi.z = pack2_relu(v[12], v[13]);
+                    hi.w = pack2_relu(v[14], v[15]);
+                    unsigned char *At = A + (uint32_t)(cb >> 2) * kSub;
+                    *reinterpret_cast<uint4 *>(At + sw_off(r, (2 * cb) & 7)) = lo;
+                    *reinterpret_cast<uint4 *>(At + sw_off(r, (2 * cb + 1) & 7)) = hi;
+                    if (store) {
+                        *reinterpret_cast<uint4 *>(hnext + 16 * cb) = lo;
+                        *reinterpret_cast<uint4 *>(hnext + 16 * cb + 8) = hi;
+                    }
+                }
+            } else {
+                float v[16];
+                tmem_ld16(trow, v);
+                tmem_wait_ld();
+                y[0] = v[0];
+                y[1] = v[1];
+                y[2] = v[2];
+            }
+        }
+        if (failed) break;
+        // relative L2: d/dy (y - t)^2 / (y^2 + eps), denominator held constant
+        float dy[3] = {0.0f, 0.0f, 0.0f};
+        if (live) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const float tt = target[(size_t)q * tgt_stride + c];
+                const float den = y[c] * y[c] + kEpsRel;
+                const float d = y[c] - tt;
+                lsum += d * d / den;
+                dy[c] = 2.0f * d / den * inv_n * S;
+            }
+        }
+        {
+            // dZ_5: 16 columns (chunks 0 and 1 of the first sub-tile), 3 live
+            uint4 lo;
+            lo.x = pack2(dy[0], dy[1]);
+            lo.y = pack2(dy[2], 0.0f);
+            lo.z = 0u;
+            lo.w = 0u;
+            *reinterpret_cast<uint4 *>(A + sw_off(r, 0)) = lo;
+            *reinterpret_cast<uint4 *>(A + sw_off(r, 1)) = make_uint4(0u, 0u, 0u, 0u);
+            if (store) *reinterpret_cast<uint4 *>(drow + (size_t)kLayers * layer_stride) = lo;
+        }
+        for (int l = kLayers; l >= 1; --l) {
+            if (!run_mma(true, l)) {
+                failed = true;
+                break;
+            }
+            // dZ_{l-1} = dA_{l-1} * relu'(Z_{l-1})
+            unsigned short *dout = drow + (size_t)(l - 1) * layer_stride;
+#pragma unroll
+            for (int cb = 0; cb < W / 16; ++cb) {
+                float v[16];
+                tmem_ld16(trow + 16 * cb, v);
+                tmem_wait_ld();
+                const uint32_t bits = msk[l - 1][cb >> 1] >> (16 * (cb & 1));
+#pragma unroll
+                for (int i = 0; i < 16; ++i)
+                    if (!((bits >> i) & 1u)) v[i] = 0.0f;
+                uint4 lo, hi;
+                lo.x = pack2(v[0], v[1]);
+                lo.y = pack2(v[2], v[3]);
+                lo.z = pack2(v[4], v[5]);
+                lo.w = pack2(v[6], v[7]);
+                hi.x = pack2(v[8], v[9]);
+                hi.y = pack2(v[10], v[11]);
+                hi.z = pack2(v[12], v[13]);
+                hi.w = pack2(v[14], v[15]);
+                if (l > 1) {  // the A operand of the next backward MMA
+                    unsigned char *At = A + (uint32_t)(cb >> 2) * kSub;
+                    *reinterpret_cast<uint4 *>(At + sw_off(r, (2 * cb) & 7)) = lo;
+                    *reinterpret_cast<uint4 *>(At + sw_off(r, (2 * cb + 1) & 7)) = hi;
+                }
+                if (store) {
+                    *reinterpret_cast<uint4 *>(dout + 16 * cb) = lo;
+                    *reinterpret_cast<uint4 *>(dout + 16 * cb + 8) = hi;
+                }
+            }
+        }
+        if (failed) break;
+    }
+    if (failed) {
+        bar_wait(bar, phase ^ 1u);
+        if (r == 0) atomicExch(err, 1);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) lsum += __shfl_xor_sync(~0u, lsum, o);
+    if ((tid & 31) == 0 && loss_sum) atomicAdd(loss_sum, lsum * inv_n);
     fence_before();
     __syncthreads();
     if (warp == 0) {
@@ -775,6 +1050,157 @@ __global__ void __launch_bounds__(2 * W) k_train_dw(const unsigned short *__rest
     else dw_chunk<W, W / 8>(D, H, s0, s1, l, dW, dw_smem);
 }
 
+// ---------------------------------------------------------------------------
+// Weight gradients on the tensor cores: dW_l = dZ_l^T H_l over the batch, as
+// D[M = layer outputs x N = layer inputs] += A[M x K] B[K x N], K = samples.
+// Both operands come straight from the row-major scratch (one sample's W
+// outputs or inputs contiguous per row): read along K they are MN-major
+// tiles.  TMA loads boxes of 64 samples x 64 columns with the 128-byte
+// swizzle into a ring of stages; one thread feeds the ring, one issues the
+// MMAs (K = 16 per instruction, four per stage) and frees each stage with a
+// commit; the FP32 accumulator (M = 128 lanes, N <= 128 columns) stays in
+// tensor memory for the CTA's whole chunk of samples and is added to the
+// global gradient once at the end.  A layer with fewer than 128 outputs
+// (64 at width 64, 3 for the output layer) reads its 64-column box twice
+// (LBO 0) and keeps only its rows.  Every wait is bounded (~1 s); a timeout
+// sets *err, and the CTA waits (bounded) for its loads and MMAs in flight
+// before it frees its tensor memory.
+// ---------------------------------------------------------------------------
+namespace dwt {
+constexpr int kStages = 3;
+constexpr uint32_t kBox = 64u * 128u;  // 64 rows x 64 BF16, one swizzle-atom column
+template <int W>
+struct Cfg {
+    static constexpr int kBoxes = W / 64;  // boxes per operand per stage
+    static constexpr uint32_t kStage = 2u * kBoxes * kBox;
+    static constexpr uint32_t kBarOff = kStages * kStage;  // full[kStages], empty[kStages], done
+    static constexpr uint32_t kSlotOff = kBarOff + 8u * (2 * kStages + 1);
+    static constexpr uint32_t kSmem = kSlotOff + 16 + 1024;
+    static constexpr uint32_t kCols = 128;
+};
+
+__device__ __forceinline__ void arrive_expect_tx(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void tma_load3(uint32_t dst, const CUtensorMap *map, int c0, int c1, int c2,
+                                          uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+        "[%5];" ::"r"(dst),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(bar)
+        : "memory");
+}
+}  // namespace dwt
+
+template <int W>
+__global__ void __launch_bounds__(128) k_train_dw_tc(const __grid_constant__ CUtensorMap tmH,
+                                                     const __grid_constant__ CUtensorMap tmD, int n,
+                                                     const int *n_dev, int chunk, float *dW_glob, int *err) {
+    using namespace tc;
+    using C = dwt::Cfg<W>;
+    constexpr int S = dwt::kStages;
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    const uint32_t pad = (1024u - (smem_u32(smem_raw) & 1023u)) & 1023u;
+    unsigned char *sm = smem_raw + pad;
+    const uint32_t s0a = smem_u32(sm);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int l = blockIdx.y;
+    const int total = n_dev ? min(*n_dev, n) : n;
+    const int padded = (total + 127) & ~127;  // k_train_fb_tc writes whole 128-row tiles
+    const int r0 = blockIdx.x * chunk, r1 = min(r0 + chunk, padded);
+    if (r0 >= r1) return;
+    const int nst = (r1 - r0) / 64;
+    const bool out_layer = l == kLayers;
+    const int in = Net<W>::in(l), outs = out_layer ? 3 : W;
+    const int ma = out_layer ? 1 : W / 64, nb = in / 64;
+    const uint32_t tx = (uint32_t)(ma + nb) * dwt::kBox;
+    const uint32_t fullb = s0a + C::kBarOff, emptyb = fullb + 8u * S, doneb = fullb + 16u * S;
+    __shared__ int failed_sh;
+    if (tid == 0) {
+        failed_sh = 0;
+        for (int i = 0; i < 2 * S + 1; ++i)
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(fullb + 8u * i) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(s0a + C::kSlotOff),
+                     "r"(C::kCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tmem = *reinterpret_cast<volatile uint32_t *>(sm + C::kSlotOff);
+    if (tid == 0) {
+        // producer: stage i of the chunk into slot i % S
+        int issued = 0;
+        for (int i = 0; i < nst; ++i) {
+            const int s = i % S;
+            if (i >= S && !bar_wait(emptyb + 8u * s, (uint32_t)((i / S) - 1) & 1u)) {
+                atomicExch(&failed_sh, 1);
+                break;
+            }
+            if (*reinterpret_cast<volatile int *>(&failed_sh)) break;
+            const uint32_t st = s0a + (uint32_t)s * C::kStage;
+            dwt::arrive_expect_tx(fullb + 8u * s, tx);
+            const int row = r0 + 64 * i;
+            for (int b = 0; b < ma; ++b) dwt::tma_load3(st + (uint32_t)b * dwt::kBox, &tmD, 64 * b, row, l, fullb + 8u * s);
+            for (int b = 0; b < nb; ++b)
+                dwt::tma_load3(st + (uint32_t)(C::kBoxes + b) * dwt::kBox, &tmH, 64 * b, row, l, fullb + 8u * s);
+            issued = i + 1;
+        }
+        // every load issued has landed before the CTA's shared memory is released
+        for (int i = max(0, issued - S); i < issued; ++i) bar_wait(fullb + 8u * (i % S), (uint32_t)(i / S) & 1u);
+    } else if (tid == 32) {
+        // MMA issuer: A = dZ (M = outputs, MN-major), B = H (N = inputs, MN-major)
+        const uint32_t idesc = idesc_bf16(128, 64 * nb) | (1u << 15) | (1u << 16);
+        const uint32_t lboA = ma == 2 ? dwt::kBox : 0u, lboB = nb == 2 ? dwt::kBox : 0u;
+        for (int i = 0; i < nst; ++i) {
+            const int s = i % S;
+            if (!bar_wait(fullb + 8u * s, (uint32_t)(i / S) & 1u)) {
+                atomicExch(&failed_sh, 1);
+                break;
+            }
+            fence_after();
+            const uint32_t st = s0a + (uint32_t)s * C::kStage;
+            const uint32_t bs = st + (uint32_t)C::kBoxes * dwt::kBox;
+#pragma unroll
+            for (int kk = 0; kk < 4; ++kk)
+                mma_bf16(tmem, sw128_desc_mn(st + (uint32_t)kk * 2048u, lboA, 1024u),
+                         sw128_desc_mn(bs + (uint32_t)kk * 2048u, lboB, 1024u), idesc, (i > 0 || kk > 0) ? 1u : 0u);
+            commit(emptyb + 8u * s);
+        }
+        commit(doneb);  // completes once every MMA issued above has
+    }
+    __syncwarp();
+    const bool done_ok = bar_wait(doneb, 0u);
+    const bool ok = !__syncthreads_or(!done_ok || failed_sh);  // uniform over the CTA
+    fence_after();
+    // epilogue: warp w holds rows 32 w .. 32 w + 31 (tensor-memory lanes)
+    const int m = 32 * warp + lane;
+    float *dW = dW_glob + Net<W>::woff(l);
+    if (ok && 32 * warp < outs) {
+        for (int c = 0; c < 64 * nb; c += 16) {
+            float v[16];
+            tmem_ld16(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)c, v);
+            tmem_wait_ld();
+            if (m < outs) {
+#pragma unroll
+                for (int k = 0; k < 16; ++k) atomicAdd(dW + (size_t)m * in + c + k, v[k]);
+            }
+        }
+    }
+    if (!ok && tid == 0) atomicExch(err, 1);
+    fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(C::kCols) : "memory");
+    }
+}
+
 // Master weights -> padded BF16 image: row r of layer l at (l W + r) P, the
 // output layer's 16 rows (3 live) after the hidden layers.
 template <int W>
@@ -855,18 +1281,54 @@ void launch_infer(NrcState &N, const float *raw, int stride, int n, const int *n
                                                                                   rad, N.ints + 2);
 }
 
+// cuTensorMapEncodeTiled, through the runtime's driver entry point.
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    });
+    return fn;
+}
+
+// A training scratch (BF16 rows of W, kLayers + 1 layers of `cap` rows) as a
+// 3-D TMA tensor (columns, rows, layer) read in 64 x 64 boxes, 128-byte swizzle.
+kgk_status scratch_map(CUtensorMap *m, unsigned short *base, int W, int cap) {
+    PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+    if (!enc) return fail(KGK_ERR_CUDA, "radiance cache: cuTensorMapEncodeTiled is not available");
+    const cuuint64_t dims[3] = {(cuuint64_t)W, (cuuint64_t)cap, (cuuint64_t)(kLayers + 1)};
+    const cuuint64_t strides[2] = {(cuuint64_t)W * 2, (cuuint64_t)cap * W * 2};
+    const cuuint32_t box[3] = {64, 64, 1}, es[3] = {1, 1, 1};
+    const CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, base, dims, strides, box, es,
+                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS)
+        return fail(KGK_ERR_CUDA, "radiance cache: cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
+    return KGK_OK;
+}
+
 template <int W>
-void launch_grad(NrcState &N, const float *raw, int raw_stride, const float *tgt, int tgt_stride, int n,
-                 const int *n_dev, int rows, cudaStream_t st) {
+kgk_status launch_grad(NrcState &N, const float *raw, int raw_stride, const float *tgt, int tgt_stride, int n,
+                       const int *n_dev, int rows, cudaStream_t st) {
     const size_t ls = (size_t)N.tr_cap * W;
-    k_train_fb<W><<<N.sms * Fb<W>::kCtasPerSm, 32 * Fb<W>::kWarps, Fb<W>::kSmem, st>>>(
-        N.img, raw, raw_stride, tgt, tgt_stride, n, n_dev, N.scal, N.trH, N.trD, ls, N.scal + 1);
-    // split K: chunks of at least 1024 samples, about four CTAs per SM over the six layers
-    const int want = std::max(1, 4 * N.sms / (kLayers + 1));
+    using T = tc::Tc<W>;
+    k_train_fb_tc<W><<<N.sms * T::kCtasPerSm, 128 * T::kGroups, T::kSmemBytes, st>>>(
+        N.img, raw, raw_stride, tgt, tgt_stride, n, n_dev, N.scal, N.trH, N.trD, ls, N.scal + 1, N.ints + 2);
+    CUtensorMap mh, md;
+    KGK_TRY(scratch_map(&mh, N.trH, W, N.tr_cap));
+    KGK_TRY(scratch_map(&md, N.trD, W, N.tr_cap));
+    // split K: chunks of whole 64-row boxes, about two CTAs per SM over the six layers
+    const int want = std::max(1, 2 * N.sms / (kLayers + 1));
     int chunk = std::max(1024, (rows + want - 1) / want);
-    chunk = (chunk + 15) & ~15;
+    chunk = (chunk + 63) & ~63;
     const dim3 gdw((unsigned)((rows + chunk - 1) / chunk), kLayers + 1);
-    k_train_dw<W><<<gdw, 2 * W, Dw<W>::kSmem, st>>>(N.trH, N.trD, ls, n, n_dev, chunk, N.g);
+    k_train_dw_tc<W><<<gdw, 128, dwt::Cfg<W>::kSmem, st>>>(mh, md, n, n_dev, chunk, N.g, N.ints + 2);
+    return KGK_OK;
 }
 }  // namespace
 
@@ -916,6 +1378,14 @@ kgk_status nrc_init(NrcState &N, const kgk_nrc_config *cfg, int device) {
     KGK_CUDA(cudaFuncSetAttribute(k_train_fb<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Fb<128>::kSmem));
     KGK_CUDA(cudaFuncSetAttribute(k_train_dw<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Dw<64>::kSmem));
     KGK_CUDA(cudaFuncSetAttribute(k_train_dw<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Dw<128>::kSmem));
+    KGK_CUDA(cudaFuncSetAttribute(k_train_dw_tc<64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)dwt::Cfg<64>::kSmem));
+    KGK_CUDA(cudaFuncSetAttribute(k_train_dw_tc<128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)dwt::Cfg<128>::kSmem));
+    KGK_CUDA(cudaFuncSetAttribute(k_train_fb_tc<64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)tc::Tc<64>::kSmemBytes));
+    KGK_CUDA(cudaFuncSetAttribute(k_train_fb_tc<128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)tc::Tc<128>::kSmemBytes));
     KGK_CUDA(cudaFuncSetAttribute(k_infer_tc<64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)tc::Tc<64>::kSmemBytes));
     KGK_CUDA(cudaFuncSetAttribute(k_infer_tc<128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -960,7 +1430,7 @@ kgk_status nrc_infer_dev(NrcState &N, const float *raw, int stride, int n, const
 
 kgk_status nrc_grad_dev(NrcState &N, const float *raw, int raw_stride, const float *tgt, int tgt_stride, int n,
                         const int *n_dev, cudaStream_t st) {
-    const int rows = (n + 15) & ~15;
+    const int rows = (n + 127) & ~127;  // whole 128-row tiles
     if (N.tr_cap < rows) {
         // per-sample activations and output gradients of every layer (BF16 rows of W)
         dfree(N.trH);
@@ -976,8 +1446,8 @@ kgk_status nrc_grad_dev(NrcState &N, const float *raw, int raw_stride, const flo
     }
     KGK_CUDA(cudaMemsetAsync(N.g, 0, N.params * sizeof(float), st));
     KGK_CUDA(cudaMemsetAsync(N.scal + 1, 0, sizeof(float), st));  // loss
-    if (N.cfg.width == 128) launch_grad<128>(N, raw, raw_stride, tgt, tgt_stride, n, n_dev, rows, st);
-    else launch_grad<64>(N, raw, raw_stride, tgt, tgt_stride, n, n_dev, rows, st);
+    if (N.cfg.width == 128) KGK_TRY(launch_grad<128>(N, raw, raw_stride, tgt, tgt_stride, n, n_dev, rows, st));
+    else KGK_TRY(launch_grad<64>(N, raw, raw_stride, tgt, tgt_stride, n, n_dev, rows, st));
     KGK_CUDA(cudaGetLastError());
     return KGK_OK;
 }
@@ -1094,6 +1564,8 @@ kgk_status kgk_nrc_gradients(kgk_scene *s, const float *raw, const float *target
     KGK_TRY(need(s));
     if (!raw || !target || !grad || n == 0 || n > (1u << 30))
         return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_nrc_gradients: bad arguments");
+    if (is_device_ptr(grad) || (loss && is_device_ptr(loss)))
+        return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_nrc_gradients: grad and loss must be host memory");
     Owned o;
     void *draw, *dt;
     KGK_TRY(stage_in(s, raw, n * kRaw * sizeof(float), &draw, o.v));
@@ -1117,6 +1589,7 @@ kgk_status kgk_nrc_train(kgk_scene *s, const float *raw, const float *target, si
     KGK_TRY(need(s));
     if (!raw || !target || n == 0 || n > (1u << 30) || steps <= 0)
         return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_nrc_train: bad arguments");
+    if (loss && is_device_ptr(loss)) return fail(KGK_ERR_INVALID_ARGUMENT, "kgk_nrc_train: loss must be host memory");
     Owned o;
     void *draw, *dt;
     KGK_TRY(stage_in(s, raw, n * kRaw * sizeof(float), &draw, o.v));
