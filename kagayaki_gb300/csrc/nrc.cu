@@ -1,17 +1,17 @@
 // nrc.cu - learned radiance cache: an MLP of hidden width W = 64 or 128
 // (64 inputs -> W, 4 x (W -> W), ReLU after each, -> 3 linear outputs, no
-// biases) in BF16 on the tensor cores with FP32 accumulation.
+// biases) in BF16 on the 5th-generation tensor cores (tcgen05, accumulators
+// in tensor memory) with FP32 accumulation.
 //
-// Inference runs on the 5th-generation tensor cores (tcgen05, accumulators in
-// tensor memory).  Training runs on mma.sync m16n8k16: one warp carries 16
-// samples through every layer, and the FP32 accumulator fragment of one
-// layer, rounded to BF16 after the ReLU, is exactly the A-operand fragment of
-// the next layer, so activations stay in registers.  Its weights live in
-// shared memory as a BF16 image with a (W + 8)-element row pitch
-// (bank-conflict-free fragment loads).  Forward, relative-L2 loss (times a
-// dynamic loss scale) and backward run in one kernel, the weight-gradient
-// GEMMs in a second; Adam updates FP32 master weights and rewrites the BF16
-// image.
+// Inference (k_infer_tc) and the training forward / backward pass
+// (k_train_fb_tc) hold the weights once per CTA in shared memory, 128-byte
+// swizzled, and carry tiles of 128 samples per warpgroup through the layers;
+// the backward pass reads the same weight tiles as MN-major operands.  The
+// training pass writes every layer's activations and output gradients (BF16)
+// to a scratch by TMA; the weight-gradient GEMM (k_train_dw_tc) reads them
+// back by TMA as MN-major operands and accumulates dW in tensor memory.
+// Relative-L2 loss with a dynamic loss scale; Adam updates FP32 master
+// weights and rewrites the BF16 image.
 // No counterpart in the reference.
 #include <cuda.h>
 #include <cudaTypedefs.h>
@@ -42,38 +42,6 @@ __device__ __forceinline__ uint32_t pack2_relu(float lo, float hi) {
     asm("cvt.rn.relu.bf16x2.f32 %0, %1, %2;" : "=r"(d) : "f"(hi), "f"(lo));
     return d;
 }
-__device__ __forceinline__ uint32_t pack_raw(unsigned short lo, unsigned short hi) {
-    return (uint32_t)lo | ((uint32_t)hi << 16);
-}
-__device__ __forceinline__ float bf2f(unsigned short b) { return __uint_as_float((uint32_t)b << 16); }
-
-__device__ __forceinline__ void mma16816(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
-    asm volatile(
-        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-        "{%0,%1,%2,%3};\n"
-        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
-}
-
-__device__ __forceinline__ uint32_t smem_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-// Four 8 x 8 BF16 matrices from shared memory; lanes 8j..8j+7 give the row
-// addresses of matrix j, register j receives it in the mma fragment layout
-// (thread T: row T/4, columns 2 (T%4), +1).
-__device__ __forceinline__ void ldsm_x4(const unsigned short *p, uint32_t &r0, uint32_t &r1, uint32_t &r2,
-                                        uint32_t &r3) {
-    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];"
-                 : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
-                 : "r"(smem_addr(p)));
-}
-// The same, transposed: thread T receives rows 2 (T%4), +1 of column T/4.
-__device__ __forceinline__ void ldsm_x4_t(const unsigned short *p, uint32_t &r0, uint32_t &r1, uint32_t &r2,
-                                          uint32_t &r3) {
-    asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];"
-                 : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
-                 : "r"(smem_addr(p)));
-}
-
 // sin(pi x) and cos(pi x) for the input encoding: x reduced exactly to
 // [-1, 1] (x - 2 rint(x / 2)), then the hardware sine and cosine of pi times
 // it, whose absolute error (about 1e-6) lies far below the BF16 rounding
@@ -83,29 +51,9 @@ __device__ __forceinline__ void sincospi_feature(float x, float *s, float *c) {
     __sincosf(r * 3.14159265358979f, s, c);
 }
 
-// One input feature (column c of the 64-float encoding) of a raw query.
-__device__ __forceinline__ float encode_col(const float *raw, int c) {
-    if (c < 36) {
-        const int ax = c / 12, k = (c % 12) >> 1;
-        float s, co;
-        sincospi_feature(raw[ax] * (float)(1 << k), &s, &co);
-        return (c & 1) ? co : s;
-    }
-    if (c < 42) return raw[3 + (c - 36)];  // normal, view
-    if (c < 54) {
-        const int j = c - 42;
-        const float x = raw[3 + (j / 6) * 3 + ((j % 6) >> 1)];
-        float s, co;
-        sincospi_feature(x, &s, &co);
-        return (j & 1) ? co : s;
-    }
-    if (c < 58) return raw[9 + (c - 54)];  // roughness, albedo
-    return 1.0f;
-}
-
-
-// All 64 input features of a raw query (the values of encode_col, each sine
-// and cosine pair computed once).
+// All 64 input features of a raw query: 3 x 12 sine / cosine features of the
+// normalised position (6 octaves), normal and view direction, their sines and
+// cosines (12), roughness and albedo, six constant ones (the biases).
 __device__ __forceinline__ void encode_row(const float *raw, float (&f)[64]) {
 #pragma unroll
     for (int ax = 0; ax < 3; ++ax) {
@@ -130,108 +78,6 @@ __device__ __forceinline__ void encode_row(const float *raw, float (&f)[64]) {
     for (int j = 0; j < 4; ++j) f[54 + j] = raw[9 + j];  // roughness, albedo
 #pragma unroll
     for (int j = 58; j < 64; ++j) f[j] = 1.0f;
-}
-
-// Input-layer A fragments of the warp's 16 samples (rows g and g + 8).
-__device__ __forceinline__ void encode_frags(const float *ra, const float *rb, uint32_t (&a)[4][4]) {
-    const int t = threadIdx.x & 3;
-#pragma unroll
-    for (int kt = 0; kt < 4; ++kt) {
-        const int c0 = kt * 16 + 2 * t;
-        a[kt][0] = pack2(encode_col(ra, c0), encode_col(ra, c0 + 1));
-        a[kt][1] = pack2(encode_col(rb, c0), encode_col(rb, c0 + 1));
-        a[kt][2] = pack2(encode_col(ra, c0 + 8), encode_col(ra, c0 + 9));
-        a[kt][3] = pack2(encode_col(rb, c0 + 8), encode_col(rb, c0 + 9));
-    }
-}
-
-// acc[nt] = A (16 x 16 KT) * W^T for output rows 8 nt .. 8 nt + 7 of a weight
-// matrix [out][in] in shared memory (BF16, row pitch P).  The B fragments of
-// two K steps come from one ldmatrix.x4: matrices (kt, low 8), (kt, high 8),
-// (kt + 1, low 8), (kt + 1, high 8) of the rows 8 nt..8 nt + 7.
-template <int P, int KT, int NT>
-__device__ __forceinline__ void layer_fwd(const unsigned short *Wm, const uint32_t (&a)[KT][4], float (&acc)[NT][4]) {
-    static_assert(KT % 2 == 0, "K steps in pairs");
-    const int lane = threadIdx.x & 31, j = lane >> 3, rr = lane & 7;
-    const unsigned short *base = Wm + rr * P + (j >> 1) * 16 + (j & 1) * 8;
-#pragma unroll
-    for (int nt = 0; nt < NT; ++nt) {
-        acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.0f;
-#pragma unroll
-        for (int kt = 0; kt < KT; kt += 2) {
-            uint32_t b0, b1, b2, b3;
-            ldsm_x4(base + nt * 8 * P + kt * 16, b0, b1, b2, b3);
-            mma16816(acc[nt], a[kt], b0, b1);
-            mma16816(acc[nt], a[kt + 1], b2, b3);
-        }
-    }
-}
-
-// acc[nt] = dZ (16 x 16 KT, K = output rows of W) * W for input columns
-// 8 nt .. 8 nt + 7 of a weight matrix [out][in] (pitch P): the B fragments
-// are W's 8 x 8 blocks transposed, two K steps per ldmatrix.x4.trans
-// (blocks (kt, low 8 rows), (kt, high 8), (kt + 1, low 8), (kt + 1, high 8)).
-template <int P, int KT, int NT>
-__device__ __forceinline__ void layer_bwd(const unsigned short *Wm, const uint32_t (&a)[KT][4], float (&acc)[NT][4]) {
-    static_assert(KT % 2 == 0, "K steps in pairs");
-    const int lane = threadIdx.x & 31, j = lane >> 3, rr = lane & 7;
-    const unsigned short *base = Wm + ((j >> 1) * 16 + (j & 1) * 8 + rr) * P;
-#pragma unroll
-    for (int nt = 0; nt < NT; ++nt) {
-        acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.0f;
-#pragma unroll
-        for (int kt = 0; kt < KT; kt += 2) {
-            uint32_t b0, b1, b2, b3;
-            ldsm_x4_t(base + kt * 16 * P + nt * 8, b0, b1, b2, b3);
-            mma16816(acc[nt], a[kt], b0, b1);
-            mma16816(acc[nt], a[kt + 1], b2, b3);
-        }
-    }
-}
-
-// C fragments -> BF16 A fragments of the next layer, after the ReLU.  Returns
-// the ReLU derivative as bits: bit 4 nt + i is set when acc[nt][i] > 0.
-template <int NT>
-__device__ __forceinline__ unsigned long long relu_to_frags(const float (&acc)[NT][4], uint32_t (&a)[NT / 2][4]) {
-    static_assert(NT <= 16, "64 mask bits");
-    unsigned long long m = 0;
-#pragma unroll
-    for (int nt = 0; nt < NT; ++nt)
-#pragma unroll
-        for (int i = 0; i < 4; ++i)
-            if (acc[nt][i] > 0.0f) m |= 1ull << (4 * nt + i);
-#pragma unroll
-    for (int kt = 0; kt < NT / 2; ++kt) {
-        a[kt][0] = pack2_relu(acc[2 * kt][0], acc[2 * kt][1]);
-        a[kt][1] = pack2_relu(acc[2 * kt][2], acc[2 * kt][3]);
-        a[kt][2] = pack2_relu(acc[2 * kt + 1][0], acc[2 * kt + 1][1]);
-        a[kt][3] = pack2_relu(acc[2 * kt + 1][2], acc[2 * kt + 1][3]);
-    }
-    return m;
-}
-
-// The warp's A fragments (16 rows x 16 KT BF16 columns) as rows base + g and
-// base + g + 8 of a global [row][ld] array.
-template <int KT>
-__device__ __forceinline__ void frags_to_global(const uint32_t (&a)[KT][4], unsigned short *dst, int ld, int base) {
-    const int g = (threadIdx.x & 31) >> 2, t = threadIdx.x & 3;
-    unsigned short *r0 = dst + (size_t)(base + g) * ld + 2 * t, *r1 = r0 + (size_t)8 * ld;
-#pragma unroll
-    for (int kt = 0; kt < KT; ++kt) {
-        *reinterpret_cast<uint32_t *>(r0 + kt * 16) = a[kt][0];
-        *reinterpret_cast<uint32_t *>(r1 + kt * 16) = a[kt][1];
-        *reinterpret_cast<uint32_t *>(r0 + kt * 16 + 8) = a[kt][2];
-        *reinterpret_cast<uint32_t *>(r1 + kt * 16 + 8) = a[kt][3];
-    }
-}
-
-template <int W>
-__device__ __forceinline__ void load_image(unsigned short *dst, const unsigned short *src) {
-    constexpr int n16 = Net<W>::kImg * 2 / 16;
-    static_assert(Net<W>::kImg * 2 % 16 == 0, "16-byte copies");
-    const uint4 *s = reinterpret_cast<const uint4 *>(src);
-    uint4 *d = reinterpret_cast<uint4 *>(dst);
-    for (int i = threadIdx.x; i < n16; i += blockDim.x) d[i] = s[i];
 }
 
 // ---------------------------------------------------------------------------
@@ -358,6 +204,19 @@ __device__ __forceinline__ uint64_t sw128_desc_mn(uint32_t saddr, uint32_t lbo, 
 
 // Instruction descriptor with B MN-major (bit 16, "transpose B").
 __host__ __device__ constexpr uint32_t idesc_bf16_bmn(int M, int N) { return idesc_bf16(M, N) | (1u << 16); }
+
+// TMA store of one 3-D box from shared memory (bulk group of this thread).
+__device__ __forceinline__ void tma_store3(const CUtensorMap *map, uint32_t src, int c0, int c1, int c2) {
+    asm volatile("cp.async.bulk.tensor.3d.global.shared::cta.bulk_group [%0, {%1, %2, %3}], [%4];" ::"l"(
+                     reinterpret_cast<uint64_t>(map)),
+                 "r"(c0), "r"(c1), "r"(c2), "r"(src)
+                 : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+// the bulk stores of this thread have read their shared memory
+__device__ __forceinline__ void bulk_wait_read() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+// ... and completed
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
 
 }  // namespace tc
 
@@ -549,9 +408,11 @@ __global__ void __launch_bounds__(128 * tc::Tc<W>::kGroups) k_infer_tc(const uns
 //             MN-major B operand (K = the layer's outputs along the tile rows,
 //             N = its inputs along the swizzled 128-byte rows), and
 //             dZ_{l-1} = bf16(dA_{l-1} * relu'(Z_{l-1})), l = 5..1.
-// Each H_l and dZ_l row goes to the global scratch (BF16, W per row, the
-// layout k_train_dw_tc reads); the rows of the last tile past the sample
-// count are written too, with dY = 0.  Every mbarrier wait is bounded; a
+// Each H_l and dZ_l tile goes to the global scratch (BF16, W per row, the
+// layout k_train_dw_tc reads) by TMA stores of the shared-memory tile the
+// layer's MMAs read, issued while they run (dZ_5 and dZ_0, which no MMA
+// reads, by the threads); the rows of the last tile past the sample count
+// are written too, with dY = 0.  Every mbarrier wait is bounded; a
 // timeout sets *err and ends the CTA after a last bounded wait for its MMAs,
 // freeing its tensor memory.
 // ---------------------------------------------------------------------------
@@ -559,7 +420,8 @@ template <int W>
 __global__ void __launch_bounds__(128 * tc::Tc<W>::kGroups) k_train_fb_tc(
     const unsigned short *__restrict__ img, const float *__restrict__ raw, int raw_stride,
     const float *__restrict__ target, int tgt_stride, int n, const int *n_dev, const float *scale_p,
-    unsigned short *Hs, unsigned short *Ds, size_t layer_stride, float *loss_sum, int *err) {
+    unsigned short *Ds, size_t layer_stride, const __grid_constant__ CUtensorMap tmH,
+    const __grid_constant__ CUtensorMap tmD, float *loss_sum, int *err) {
     using namespace tc;
     using T = Tc<W>;
     constexpr int kG = T::kGroups, P = Net<W>::kPitch, kMW = W / 32;
@@ -610,9 +472,12 @@ __global__ void __launch_bounds__(128 * tc::Tc<W>::kGroups) k_train_fb_tc(
     unsigned char *A = sm + T::kAOff + (uint32_t)g * T::kATile;
     const uint32_t a_addr = s0 + T::kAOff + (uint32_t)g * T::kATile;
     // Issues one layer's MMAs into the accumulator (forward: Z = A W^T;
-    // backward: dA = A W, the weights read MN-major), commits and waits
-    // (bounded); false when the wait timed out in any thread of the group.
-    auto run_mma = [&](bool backward, int l) -> bool {
+    // backward: dA = A W, the weights read MN-major), then - while they run -
+    // the TMA stores of the A tile itself (H_l or dZ_l of the layer, `nsub`
+    // sub-tiles of 64 columns, two 64-row boxes each) into the scratch, waits
+    // for the MMAs (bounded) and for the stores to have read the tile;
+    // false when the wait timed out in any thread of the group.
+    auto run_mma = [&](bool backward, int l, const CUtensorMap *map, int nsub, int q0) -> bool {
         fence_async_smem();
         fence_before();
         wg_sync(wgbar);
@@ -641,17 +506,24 @@ __global__ void __launch_bounds__(128 * tc::Tc<W>::kGroups) k_train_fb_tc(
                 }
             }
             commit(bar);
+            if (map) {
+                for (int jj = 0; jj < nsub; ++jj)
+                    for (int h = 0; h < 2; ++h)
+                        tma_store3(map, a_addr + (uint32_t)jj * kSub + (uint32_t)h * 8192u, 64 * jj, q0 + 64 * h, l);
+                bulk_commit();
+            }
         }
         const bool ok = bar_wait(bar, phase);
         phase ^= 1u;
+        if (r == 0 && map) bulk_wait_read();  // the tile may be overwritten after the barrier below
         if (wg_sync_or(wgbar, !ok)) return false;
         fence_after();
         return true;
     };
     for (int tile = blockIdx.x * kG + g; tile * kRows < padded; tile += gridDim.x * kG) {
-        const int q = tile * kRows + r;
-        const bool live = q < total, store = q < padded;
-        unsigned short *hrow = Hs + (size_t)q * W, *drow = Ds + (size_t)q * W;
+        const int q0 = tile * kRows, q = q0 + r;
+        const bool live = q < total;
+        unsigned short *drow = Ds + (size_t)q * W;
         {
             float rw[kRaw];
 #pragma unroll
@@ -666,43 +538,43 @@ __global__ void __launch_bounds__(128 * tc::Tc<W>::kGroups) k_train_fb_tc(
                 v.z = pack2(f[8 * c + 4], f[8 * c + 5]);
                 v.w = pack2(f[8 * c + 6], f[8 * c + 7]);
                 *reinterpret_cast<uint4 *>(A + sw_off(r, c)) = v;
-                if (store) *reinterpret_cast<uint4 *>(hrow + 8 * c) = v;
             }
         }
         uint32_t msk[kLayers][kMW];
         float y[3] = {0.0f, 0.0f, 0.0f};
         for (int l = 0; l <= kLayers; ++l) {
-            if (!run_mma(false, l)) {
+            // H_l goes to the scratch while its layer's MMAs run
+            if (!run_mma(false, l, &tmH, l == 0 ? 1 : W / 64, q0)) {
                 failed = true;
                 break;
             }
             if (l < kLayers) {
-                unsigned short *hnext = hrow + (size_t)(l + 1) * layer_stride;
 #pragma unroll
-                for (int cb = 0; cb < W / 16; ++cb) {
-                    float v[16];
-                    tmem_ld16(trow + 16 * cb, v);
+                for (int hb = 0; hb < W / 64; ++hb) {  // 64 columns per tensor-memory wait
+                    float v[4][16];
+#pragma unroll
+                    for (int c = 0; c < 4; ++c) tmem_ld16(trow + 64 * hb + 16 * c, v[c]);
                     tmem_wait_ld();
-                    uint32_t bits = 0;
 #pragma unroll
-                    for (int i = 0; i < 16; ++i) bits |= (v[i] > 0.0f ? 1u : 0u) << i;
-                    if (cb & 1) msk[l][cb >> 1] |= bits << 16;
-                    else msk[l][cb >> 1] = bits;
-                    uint4 lo, hi;
-                    lo.x = pack2_relu(v[0], v[1]);
-                    lo.y = pack2_relu(v[2], v[3]);
-                    lo.z = pack2_relu(v[4], v[5]);
-                    lo.w = pack2_relu(v[6], v[7]);
-                    hi.x = pack2_relu(v[8], v[9]);
-                    hi.y = pack2_relu(v[10], v[11]);
-                    hi.z = pack2_relu(v[12], v[13]);
-                    hi.w = pack2_relu(v[14], v[15]);
-                    unsigned char *At = A + (uint32_t)(cb >> 2) * kSub;
-                    *reinterpret_cast<uint4 *>(At + sw_off(r, (2 * cb) & 7)) = lo;
-                    *reinterpret_cast<uint4 *>(At + sw_off(r, (2 * cb + 1) & 7)) = hi;
-                    if (store) {
-                        *reinterpret_cast<uint4 *>(hnext + 16 * cb) = lo;
-                        *reinterpret_cast<uint4 *>(hnext + 16 * cb + 8) = hi;
+                    for (int c = 0; c < 4; ++c) {
+                        const int cb = 4 * hb + c;
+                        uint32_t bits = 0;
+#pragma unroll
+                        for (int i = 0; i < 16; ++i) bits |= (v[c][i] > 0.0f ? 1u : 0u) << i;
+                        if (cb & 1) msk[l][cb >> 1] |= bits << 16;
+                        else msk[l][cb >> 1] = bits;
+                        uint4 lo, hi;
+                        lo.x = pack2_relu(v[c][0], v[c][1]);
+                        lo.y = pack2_relu(v[c][2], v[c][3]);
+                        lo.z = pack2_relu(v[c][4], v[c][5]);
+                        lo.w = pack2_relu(v[c][6], v[c][7]);
+                        hi.x = pack2_relu(v[c][8], v[c][9]);
+                        hi.y = pack2_relu(v[c][10], v[c][11]);
+                        hi.z = pack2_relu(v[c][12], v[c][13]);
+                        hi.w = pack2_relu(v[c][14], v[c][15]);
+                        unsigned char *At = A + (uint32_t)hb * kSub;
+                        *reinterpret_cast<uint4 *>(At + sw_off(r, (2 * cb) & 7)) = lo;
+                        *reinterpret_cast<uint4 *>(At + sw_off(r, (2 * cb + 1) & 7)) = hi;
                     }
                 }
             } else {
@@ -728,7 +600,8 @@ __global__ void __launch_bounds__(128 * tc::Tc<W>::kGroups) k_train_fb_tc(
             }
         }
         {
-            // dZ_5: 16 columns (chunks 0 and 1 of the first sub-tile), 3 live
+            // dZ_5: 16 columns (chunks 0 and 1 of the first sub-tile), 3 live;
+            // its scratch row by the thread (columns 0..7; 8.. stay zero)
             uint4 lo;
             lo.x = pack2(dy[0], dy[1]);
             lo.y = pack2(dy[2], 0.0f);
@@ -736,41 +609,47 @@ __global__ void __launch_bounds__(128 * tc::Tc<W>::kGroups) k_train_fb_tc(
             lo.w = 0u;
             *reinterpret_cast<uint4 *>(A + sw_off(r, 0)) = lo;
             *reinterpret_cast<uint4 *>(A + sw_off(r, 1)) = make_uint4(0u, 0u, 0u, 0u);
-            if (store) *reinterpret_cast<uint4 *>(drow + (size_t)kLayers * layer_stride) = lo;
+            *reinterpret_cast<uint4 *>(drow + (size_t)kLayers * layer_stride) = lo;
         }
         for (int l = kLayers; l >= 1; --l) {
-            if (!run_mma(true, l)) {
+            // dA_{l-1} = dZ_l W_l; dZ_l (l < kLayers) goes to the scratch meanwhile
+            if (!run_mma(true, l, l < kLayers ? &tmD : nullptr, W / 64, q0)) {
                 failed = true;
                 break;
             }
-            // dZ_{l-1} = dA_{l-1} * relu'(Z_{l-1})
+            // dZ_{l-1} = dA_{l-1} * relu'(Z_{l-1}): into the tile for the next
+            // backward MMA, or (dZ_0) straight to the scratch
             unsigned short *dout = drow + (size_t)(l - 1) * layer_stride;
 #pragma unroll
-            for (int cb = 0; cb < W / 16; ++cb) {
-                float v[16];
-                tmem_ld16(trow + 16 * cb, v);
-                tmem_wait_ld();
-                const uint32_t bits = msk[l - 1][cb >> 1] >> (16 * (cb & 1));
+            for (int hb = 0; hb < W / 64; ++hb) {
+                float v[4][16];
 #pragma unroll
-                for (int i = 0; i < 16; ++i)
-                    if (!((bits >> i) & 1u)) v[i] = 0.0f;
-                uint4 lo, hi;
-                lo.x = pack2(v[0], v[1]);
-                lo.y = pack2(v[2], v[3]);
-                lo.z = pack2(v[4], v[5]);
-                lo.w = pack2(v[6], v[7]);
-                hi.x = pack2(v[8], v[9]);
-                hi.y = pack2(v[10], v[11]);
-                hi.z = pack2(v[12], v[13]);
-                hi.w = pack2(v[14], v[15]);
-                if (l > 1) {  // the A operand of the next backward MMA
-                    unsigned char *At = A + (uint32_t)(cb >> 2) * kSub;
-                    *reinterpret_cast<uint4 *>(At + sw_off(r, (2 * cb) & 7)) = lo;
-                    *reinterpret_cast<uint4 *>(At + sw_off(r, (2 * cb + 1) & 7)) = hi;
-                }
-                if (store) {
-                    *reinterpret_cast<uint4 *>(dout + 16 * cb) = lo;
-                    *reinterpret_cast<uint4 *>(dout + 16 * cb + 8) = hi;
+                for (int c = 0; c < 4; ++c) tmem_ld16(trow + 64 * hb + 16 * c, v[c]);
+                tmem_wait_ld();
+#pragma unroll
+                for (int c = 0; c < 4; ++c) {
+                    const int cb = 4 * hb + c;
+                    const uint32_t bits = msk[l - 1][cb >> 1] >> (16 * (cb & 1));
+#pragma unroll
+                    for (int i = 0; i < 16; ++i)
+                        if (!((bits >> i) & 1u)) v[c][i] = 0.0f;
+                    uint4 lo, hi;
+                    lo.x = pack2(v[c][0], v[c][1]);
+                    lo.y = pack2(v[c][2], v[c][3]);
+                    lo.z = pack2(v[c][4], v[c][5]);
+                    lo.w = pack2(v[c][6], v[c][7]);
+                    hi.x = pack2(v[c][8], v[c][9]);
+                    hi.y = pack2(v[c][10], v[c][11]);
+                    hi.z = pack2(v[c][12], v[c][13]);
+                    hi.w = pack2(v[c][14], v[c][15]);
+                    if (l > 1) {
+                        unsigned char *At = A + (uint32_t)hb * kSub;
+                        *reinterpret_cast<uint4 *>(At + sw_off(r, (2 * cb) & 7)) = lo;
+                        *reinterpret_cast<uint4 *>(At + sw_off(r, (2 * cb + 1) & 7)) = hi;
+                    } else {
+                        *reinterpret_cast<uint4 *>(dout + 16 * cb) = lo;
+                        *reinterpret_cast<uint4 *>(dout + 16 * cb + 8) = hi;
+                    }
                 }
             }
         }
@@ -780,6 +659,7 @@ __global__ void __launch_bounds__(128 * tc::Tc<W>::kGroups) k_train_fb_tc(
         bar_wait(bar, phase ^ 1u);
         if (r == 0) atomicExch(err, 1);
     }
+    if (r == 0) bulk_wait_all();
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) lsum += __shfl_xor_sync(~0u, lsum, o);
     if ((tid & 31) == 0 && loss_sum) atomicAdd(loss_sum, lsum * inv_n);
@@ -791,263 +671,6 @@ __global__ void __launch_bounds__(128 * tc::Tc<W>::kGroups) k_train_fb_tc(
                      "r"(T::kTmemCols)
                      : "memory");
     }
-}
-
-// ---------------------------------------------------------------------------
-// training, split form: k_train_fb runs forward, loss and backward for tiles
-// of 16 samples per warp and stores every layer's input activations H_l and
-// output gradients dZ_l (BF16 rows of W, H_0 with 64 live columns) to global
-// scratch; k_train_dw then forms dW_l = dZ_l^T H_l over the batch as a
-// split-K GEMM (each CTA a chunk of samples, accumulating in registers, one
-// atomic add per element per CTA).  Layer 5 is the output layer (dZ_5 has 3
-// live columns).  The ReLU derivatives of the forward pass stay on chip as
-// one 64-bit mask per lane and layer.
-// ---------------------------------------------------------------------------
-constexpr int kMaskBytes = kLayers * 32 * 8;  // per warp
-
-template <int W>
-struct Fb {
-    static constexpr int kWarps = W == 64 ? 4 : 8;
-    static constexpr int kCtasPerSm = W == 64 ? 4 : 1;
-    static constexpr size_t kImgBytes = ((size_t)Net<W>::kImg * 2 + 15) & ~(size_t)15;
-    static constexpr size_t kSmem = kImgBytes + (size_t)kMaskBytes * kWarps;
-    static_assert(kSmem * kCtasPerSm <= 227 * 1024, "shared memory per SM");
-};
-
-template <int W>
-__global__ void __launch_bounds__(32 * Fb<W>::kWarps) k_train_fb(
-    const unsigned short *__restrict__ img, const float *__restrict__ raw, int raw_stride,
-    const float *__restrict__ target, int tgt_stride, int n, const int *n_dev, const float *scale_p,
-    unsigned short *Hs, unsigned short *Ds, size_t layer_stride, float *loss_sum) {
-    constexpr int P = Net<W>::kPitch, NT = W / 8, KT = W / 16;
-    extern __shared__ __align__(16) unsigned char smem[];
-    unsigned short *sW = reinterpret_cast<unsigned short *>(smem);
-    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3, wid = threadIdx.x >> 5;
-    unsigned long long *msk =
-        reinterpret_cast<unsigned long long *>(smem + Fb<W>::kImgBytes + (size_t)kMaskBytes * wid) + lane;
-    load_image<W>(sW, img);
-    __syncthreads();
-    const int total = n_dev ? min(*n_dev, n) : n;
-    const int padded = (total + 15) & ~15;
-    const float S = *scale_p;
-    const float inv_n = 1.0f / (3.0f * (float)max(total, 1));
-    float lsum = 0.0f;
-    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nwarps = (gridDim.x * blockDim.x) >> 5;
-    for (int base = warp * 16; base < padded; base += nwarps * 16) {
-        const int sa = base + g, sb = base + g + 8;
-        float acc[NT][4];
-        uint32_t a[KT][4];
-        {
-            float ra[kRaw], rb[kRaw];
-#pragma unroll
-            for (int k = 0; k < kRaw; ++k) {
-                ra[k] = sa < total ? raw[(size_t)sa * raw_stride + k] : 0.0f;
-                rb[k] = sb < total ? raw[(size_t)sb * raw_stride + k] : 0.0f;
-            }
-            uint32_t a0[4][4];
-            encode_frags(ra, rb, a0);
-            frags_to_global<4>(a0, Hs, W, base);  // H_0: the 64 input columns
-            layer_fwd<P, 4, NT>(sW, a0, acc);
-        }
-        msk[0] = relu_to_frags<NT>(acc, a);
-        frags_to_global<KT>(a, Hs + layer_stride, W, base);
-#pragma unroll 1
-        for (int l = 1; l < kLayers; ++l) {
-            layer_fwd<P, KT, NT>(sW + l * W * P, a, acc);
-            msk[32 * l] = relu_to_frags<NT>(acc, a);
-            frags_to_global<KT>(a, Hs + (size_t)(l + 1) * layer_stride, W, base);
-        }
-        float y1[1][4];
-        layer_fwd<P, KT, 1>(sW + kLayers * W * P, a, y1);
-        const float *y = y1[0];
-        // relative L2: d/dy (y - t)^2 / (y^2 + eps), denominator held constant
-        float dy[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-#pragma unroll
-        for (int r = 0; r < 2; ++r) {
-            const int s = r == 0 ? sa : sb;
-#pragma unroll
-            for (int k = 0; k < 2; ++k) {
-                const int c = 2 * t + k;
-                if (c > 2 || s >= total) continue;
-                const float yy = y[2 * r + k];
-                const float tt = target[(size_t)s * tgt_stride + c];
-                const float den = yy * yy + kEpsRel;
-                const float d = yy - tt;
-                lsum += d * d / den;
-                dy[2 * r + k] = 2.0f * d / den * inv_n * S;
-            }
-        }
-        // dZ of the output layer: columns 0..7 of the rows (3 live); columns
-        // 8.. stay zero (cleared when the scratch is allocated)
-        {
-            unsigned short *drow = Ds + (size_t)kLayers * layer_stride;
-            const uint32_t d0 = t < 2 ? pack2(dy[0], dy[1]) : 0u, d1 = t < 2 ? pack2(dy[2], dy[3]) : 0u;
-            *reinterpret_cast<uint32_t *>(drow + (size_t)sa * W + 2 * t) = d0;
-            *reinterpret_cast<uint32_t *>(drow + (size_t)sb * W + 2 * t) = d1;
-        }
-        // dA_4 = dZ_out (16 x 16, columns >= 8 zero) * W_out (16 x W)
-        {
-            uint32_t dza[4];
-            dza[0] = pack2(dy[0], dy[1]);
-            dza[1] = pack2(dy[2], dy[3]);
-            dza[2] = 0u;
-            dza[3] = 0u;
-            // B: the 16 padded output rows of W_out, 8 x 8 blocks transposed;
-            // blocks (rows 0-7, nt), (8-15, nt), (0-7, nt + 1), (8-15, nt + 1)
-            const int j = lane >> 3, rr = lane & 7;
-            const unsigned short *Wo = sW + kLayers * W * P + ((j & 1) * 8 + rr) * P + (j >> 1) * 8;
-#pragma unroll
-            for (int nt = 0; nt < NT; nt += 2) {
-                uint32_t b0, b1, b2, b3;
-                ldsm_x4_t(Wo + nt * 8, b0, b1, b2, b3);
-                acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.0f;
-                acc[nt + 1][0] = acc[nt + 1][1] = acc[nt + 1][2] = acc[nt + 1][3] = 0.0f;
-                mma16816(acc[nt], dza, b0, b1);
-                mma16816(acc[nt + 1], dza, b2, b3);
-            }
-        }
-#pragma unroll 1
-        for (int l = kLayers - 1; l >= 0; --l) {
-            // dZ_l = dA_l * relu'(z_l)
-            const unsigned long long m = msk[32 * l];
-#pragma unroll
-            for (int nt = 0; nt < NT; ++nt)
-#pragma unroll
-                for (int i = 0; i < 4; ++i)
-                    if (!((m >> (4 * nt + i)) & 1ull)) acc[nt][i] = 0.0f;
-            // dZ_l rows to global (BF16)
-            unsigned short *drow = Ds + (size_t)l * layer_stride;
-#pragma unroll
-            for (int nt = 0; nt < NT; ++nt) {
-                const int c = nt * 8 + 2 * t;
-                *reinterpret_cast<uint32_t *>(drow + (size_t)sa * W + c) = pack2(acc[nt][0], acc[nt][1]);
-                *reinterpret_cast<uint32_t *>(drow + (size_t)sb * W + c) = pack2(acc[nt][2], acc[nt][3]);
-            }
-            if (l == 0) break;
-            // dA_{l-1} = dZ_l (16 x W) * W_l (W x W)
-#pragma unroll
-            for (int kt = 0; kt < KT; ++kt) {
-                a[kt][0] = pack2(acc[2 * kt][0], acc[2 * kt][1]);
-                a[kt][1] = pack2(acc[2 * kt][2], acc[2 * kt][3]);
-                a[kt][2] = pack2(acc[2 * kt + 1][0], acc[2 * kt + 1][1]);
-                a[kt][3] = pack2(acc[2 * kt + 1][2], acc[2 * kt + 1][3]);
-            }
-            layer_bwd<P, KT, NT>(sW + l * W * P, a, acc);
-        }
-        __syncwarp();
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) lsum += __shfl_xor_sync(~0u, lsum, o);
-    if (lane == 0 && loss_sum) atomicAdd(loss_sum, lsum * inv_n);
-}
-
-// dW_l[o][i] += sum over the samples s0..s1-1 of dZ_l[s][o] * H_l[s][i] for
-// the layer's IN = 8 NT inputs.  Warp w owns output rows 16w..16w+15 (the
-// output layer only warp 0).  Samples arrive in stages of kDwStage rows of
-// dZ and H, double-buffered with cp.async; both operands are read with
-// ldmatrix.trans (A = dZ^T, B = H with K = samples).
-constexpr int kDwStage = 64;
-
-template <int W>
-struct Dw {
-    static constexpr size_t kBuf = (size_t)kDwStage * Net<W>::kPitch;  // elements of one operand stage
-    static constexpr size_t kSmem = 4 * kBuf * sizeof(unsigned short);  // dZ and H, two stages
-};
-
-__device__ __forceinline__ void cp_async16(void *dst, const void *src) {
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_addr(dst)), "l"(src) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
-
-template <int W, int NT>
-__device__ __forceinline__ void dw_chunk(const unsigned short *D, const unsigned short *H, int s0, int s1, int l,
-                                        float *dW, unsigned short *sm) {
-    constexpr int P = Net<W>::kPitch, IN = NT * 8;
-    constexpr size_t kBuf = Dw<W>::kBuf;
-    static_assert(NT % 2 == 0, "column blocks in pairs");
-    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3, wid = threadIdx.x >> 5;
-    const int j = lane >> 3, rr = lane & 7;
-    const bool active = l < kLayers || wid == 0;
-    float acc[NT][4];
-#pragma unroll
-    for (int nt = 0; nt < NT; ++nt) acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.0f;
-    auto load = [&](int sb, int buf) {
-        unsigned short *sD = sm + (size_t)buf * 2 * kBuf, *sH = sD + kBuf;
-        const int rows = min(kDwStage, s1 - sb);
-        for (int i = threadIdx.x; i < kDwStage * (W / 8); i += blockDim.x) {
-            const int r = i / (W / 8), c = i % (W / 8);
-            if (r < rows) cp_async16(sD + r * P + c * 8, D + (size_t)(sb + r) * W + c * 8);
-        }
-        for (int i = threadIdx.x; i < kDwStage * (IN / 8); i += blockDim.x) {
-            const int r = i / (IN / 8), c = i % (IN / 8);
-            if (r < rows) cp_async16(sH + r * P + c * 8, H + (size_t)(sb + r) * W + c * 8);
-        }
-        cp_async_commit();
-    };
-    int buf = 0;
-    load(s0, 0);
-    for (int sb = s0; sb < s1; sb += kDwStage) {
-        if (sb + kDwStage < s1) load(sb + kDwStage, buf ^ 1);
-        else cp_async_commit();  // an empty group keeps the wait count uniform
-        cp_async_wait1();
-        __syncthreads();
-        if (active) {
-            const unsigned short *sD = sm + (size_t)buf * 2 * kBuf, *sH = sD + kBuf;
-            const int ksteps = min(kDwStage, s1 - sb) / 16;
-            for (int ks = 0; ks < ksteps; ++ks) {
-                // A = dZ^T (rows o = 16 wid..16 wid + 15, K = 16 samples): blocks
-                // (samples 0-7, o 0-7), (0-7, 8-15), (8-15, 0-7), (8-15, 8-15)
-                uint32_t a[4];
-                ldsm_x4_t(sD + (ks * 16 + (j >> 1) * 8 + rr) * P + wid * 16 + (j & 1) * 8, a[0], a[1], a[2], a[3]);
-                // B = H (K = 16 samples, N = 8 inputs): blocks (0-7, nt), (8-15, nt),
-                // (0-7, nt + 1), (8-15, nt + 1)
-                const unsigned short *hb = sH + (ks * 16 + (j & 1) * 8 + rr) * P + (j >> 1) * 8;
-#pragma unroll
-                for (int nt = 0; nt < NT; nt += 2) {
-                    uint32_t b0, b1, b2, b3;
-                    ldsm_x4_t(hb + nt * 8, b0, b1, b2, b3);
-                    mma16816(acc[nt], a, b0, b1);
-                    mma16816(acc[nt + 1], a, b2, b3);
-                }
-            }
-        }
-        __syncthreads();
-        buf ^= 1;
-    }
-    if (!active) return;
-    const int o0 = wid * 16 + g, o1 = o0 + 8;
-    const int rows = l < kLayers ? W : 3;
-#pragma unroll
-    for (int nt = 0; nt < NT; ++nt) {
-        const int col = nt * 8 + 2 * t;
-        if (o0 < rows) {
-            atomicAdd(&dW[o0 * IN + col], acc[nt][0]);
-            atomicAdd(&dW[o0 * IN + col + 1], acc[nt][1]);
-        }
-        if (o1 < rows) {
-            atomicAdd(&dW[o1 * IN + col], acc[nt][2]);
-            atomicAdd(&dW[o1 * IN + col + 1], acc[nt][3]);
-        }
-    }
-}
-
-// blockIdx.y = layer (0..4 hidden, 5 output); blockIdx.x = sample chunk of
-// `chunk` (a multiple of 16) samples.
-template <int W>
-__global__ void __launch_bounds__(2 * W) k_train_dw(const unsigned short *__restrict__ Hs,
-                                                    const unsigned short *__restrict__ Ds, size_t layer_stride,
-                                                    int n, const int *n_dev, int chunk, float *dW_glob) {
-    extern __shared__ __align__(16) unsigned short dw_smem[];
-    const int l = blockIdx.y;
-    const int total = n_dev ? min(*n_dev, n) : n;
-    const int padded = (total + 15) & ~15;
-    const int s0 = blockIdx.x * chunk, s1 = min(s0 + chunk, padded);
-    if (s0 >= s1) return;
-    const unsigned short *D = Ds + (size_t)l * layer_stride, *H = Hs + (size_t)l * layer_stride;
-    float *dW = dW_glob + Net<W>::woff(l);
-    if (l == 0) dw_chunk<W, kIn / 8>(D, H, s0, s1, l, dW, dw_smem);
-    else dw_chunk<W, W / 8>(D, H, s0, s1, l, dW, dw_smem);
 }
 
 // ---------------------------------------------------------------------------
@@ -1067,11 +690,11 @@ __global__ void __launch_bounds__(2 * W) k_train_dw(const unsigned short *__rest
 // before it frees its tensor memory.
 // ---------------------------------------------------------------------------
 namespace dwt {
-constexpr int kStages = 3;
 constexpr uint32_t kBox = 64u * 128u;  // 64 rows x 64 BF16, one swizzle-atom column
 template <int W>
 struct Cfg {
     static constexpr int kBoxes = W / 64;  // boxes per operand per stage
+    static constexpr int kStages = W == 64 ? 6 : 3;  // 96 KB of stages either way: two CTAs per SM
     static constexpr uint32_t kStage = 2u * kBoxes * kBox;
     static constexpr uint32_t kBarOff = kStages * kStage;  // full[kStages], empty[kStages], done
     static constexpr uint32_t kSlotOff = kBarOff + 8u * (2 * kStages + 1);
@@ -1099,7 +722,7 @@ __global__ void __launch_bounds__(128) k_train_dw_tc(const __grid_constant__ CUt
                                                      const int *n_dev, int chunk, float *dW_glob, int *err) {
     using namespace tc;
     using C = dwt::Cfg<W>;
-    constexpr int S = dwt::kStages;
+    constexpr int S = C::kStages;
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     const uint32_t pad = (1024u - (smem_u32(smem_raw) & 1023u)) & 1023u;
     unsigned char *sm = smem_raw + pad;
@@ -1317,11 +940,13 @@ kgk_status launch_grad(NrcState &N, const float *raw, int raw_stride, const floa
                        const int *n_dev, int rows, cudaStream_t st) {
     const size_t ls = (size_t)N.tr_cap * W;
     using T = tc::Tc<W>;
-    k_train_fb_tc<W><<<N.sms * T::kCtasPerSm, 128 * T::kGroups, T::kSmemBytes, st>>>(
-        N.img, raw, raw_stride, tgt, tgt_stride, n, n_dev, N.scal, N.trH, N.trD, ls, N.scal + 1, N.ints + 2);
     CUtensorMap mh, md;
     KGK_TRY(scratch_map(&mh, N.trH, W, N.tr_cap));
     KGK_TRY(scratch_map(&md, N.trD, W, N.tr_cap));
+    // as many CTAs as the batch's 128-row tiles need (one per warpgroup), at most the resident count
+    const int fb_ctas = std::max(1, std::min(N.sms * T::kCtasPerSm, ((n + 127) / 128 + T::kGroups - 1) / T::kGroups));
+    k_train_fb_tc<W><<<fb_ctas, 128 * T::kGroups, T::kSmemBytes, st>>>(
+        N.img, raw, raw_stride, tgt, tgt_stride, n, n_dev, N.scal, N.trD, ls, mh, md, N.scal + 1, N.ints + 2);
     // split K: chunks of whole 64-row boxes, about two CTAs per SM over the six layers
     const int want = std::max(1, 2 * N.sms / (kLayers + 1));
     int chunk = std::max(1024, (rows + want - 1) / want);
@@ -1374,10 +999,6 @@ kgk_status nrc_init(NrcState &N, const kgk_nrc_config *cfg, int device) {
     make_image(N, 0);
     KGK_CUDA(cudaGetLastError());
     KGK_CUDA(cudaDeviceSynchronize());
-    KGK_CUDA(cudaFuncSetAttribute(k_train_fb<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Fb<64>::kSmem));
-    KGK_CUDA(cudaFuncSetAttribute(k_train_fb<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Fb<128>::kSmem));
-    KGK_CUDA(cudaFuncSetAttribute(k_train_dw<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Dw<64>::kSmem));
-    KGK_CUDA(cudaFuncSetAttribute(k_train_dw<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Dw<128>::kSmem));
     KGK_CUDA(cudaFuncSetAttribute(k_train_dw_tc<64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)dwt::Cfg<64>::kSmem));
     KGK_CUDA(cudaFuncSetAttribute(k_train_dw_tc<128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
