@@ -9,9 +9,10 @@ value: rays (closest + shadow) per second of device time, inputs resident.
 e2e:   the same through the C ABI with host buffers: the camera is read from
        host memory and the frame is copied back to host memory every step.
 --impl reference: the reference's estimator restated on the host CPU (the
-       oracle port; the reference's own GPU renderer is not run, see the
-       design notes), timed on a bounded sample of the same workload with all
-       host threads.
+       oracle port), timed on a bounded sample of the same workload with all
+       host threads; the line also carries the reference's own CUDA renderer
+       run on this GPU at the configuration its traversal handles (the
+       Cornell box, 256 x 256, 16 spp: gpu_reference_c1).
 relmse: equal-time image error against a converged 4096-spp frame (FP64
        accumulation on the GPU), plain path tracing vs the learned radiance
        cache, at the first camera of the orbit (static camera, 1 spp per
@@ -239,6 +240,12 @@ def run_ours(args):
             study = relmse_study(scene, W, H, WORKLOAD["max_depth"])
         except Exception as e:  # the throughput line is still printed
             study = {"error": f"{type(e).__name__}: {e}"}
+    probes = None
+    if rank == 0:
+        try:
+            probes = config_probes(scene, W, H)
+        except Exception as e:  # the throughput line is still printed
+            probes = {"error": f"{type(e).__name__}: {e}"}
     if dist:
         dev_ms, e2e_s, rays, e2e_rays = reduce_over_ranks(dist, dev_ms, e2e_s, rays, e2e_rays, "cuda")
     scene.close()
@@ -319,6 +326,8 @@ def run_ours(args):
     }
     if c1:
         line["c1"] = c1
+    if probes:
+        line["configs"] = probes
     if study:
         line["relmse"] = study
     if not args.no_cpu:
@@ -427,6 +436,95 @@ def relmse_study(scene, W, H, max_depth, ref_spp=4096, train_frames=32, eval_fra
     }
 
 
+def config_probes(scene, W, H, frames=20, warmup=3):
+    """Short runs of the other configurations, so that the default run records
+    them too: C3 (1-spp orbit + standard SVGF) and C4 (the width-64 cache
+    along the orbit) on this scene at W x H, C5 (10.6M triangles with
+    textures, 3840 x 2160, width-128 cache) on its own scene.  Each is the
+    frame loop of `--workload svgf-orbit | c4 | c5` over `frames` frames
+    after `warmup` (those workloads run 60 / 60 / 120 frames and add the
+    relMSE studies)."""
+    import ctypes
+    import torch
+    from kagayaki_gb300 import ESTIMATOR_UNBIASED, Scene, scenes
+    from kagayaki_gb300._lib import check, lib
+    from kagayaki_gb300.api import PinnedBuffer
+    from kagayaki_gb300.structs import KgkSvgfConfig
+    md = WORKLOAD["max_depth"]
+    out = {}
+    # C3: render (frame kept on the device) + standard SVGF writing RGBA8,
+    # copied asynchronously into pinned host memory; wall clock
+    kw = dict(spp=1, max_depth=md, estimator=ESTIMATOR_UNBIASED, write_gbuffer=True)
+    cfg = KgkSvgfConfig(mode=1, width=W, height=H, frame_index=0, atrous_iterations=5, alpha=0.2,
+                        sigma_z=1.0, sigma_n=128.0, sigma_l=4.0)
+    bufs = [PinnedBuffer((H, W, 4), np.uint8) for _ in range(2)]
+    t0 = 0.0
+    for f in range(warmup + frames):
+        if f == warmup:
+            scene.sync()
+            t0 = time.perf_counter()
+        scene.render(orbit_camera(f, H), W, H, seed=3, frame_index=f, keep_on_device=True, **kw)
+        cfg.frame_index = f
+        scene.svgf_output(cfg, rgba8=bufs[f % 2].array, async_=True)
+    scene.sync()
+    c3_s = time.perf_counter() - t0
+    for b in bufs:
+        b.free()
+    # the compat filter (kgk_svgf mode 0) alone on the same frames
+    cfg_c = KgkSvgfConfig(mode=0, width=W, height=H, frame_index=0)
+    dev_out = torch.empty((H, W, 4), dtype=torch.float32, device="cuda")
+    cs = []
+    for f in range(8):
+        scene.render(orbit_camera(f, H), W, H, seed=3, frame_index=f, keep_on_device=True, **kw)
+        scene.sync()
+        cfg_c.frame_index = f
+        t1 = time.perf_counter()
+        check(lib().kgk_svgf_output(scene._h, ctypes.byref(cfg_c), None, ctypes.c_void_p(dev_out.data_ptr()),
+                                    None, 0))
+        cs.append(time.perf_counter() - t1)
+    out["c3"] = {"workload": "svgf-orbit-1spp", "width": W, "height": H, "value": round(frames / c3_s, 2),
+                 "unit": "frames/s", "frames": frames,
+                 "compat_filter_ms": round(1e3 * float(np.median(cs[2:])), 3),
+                 "timing": "wall clock: render + standard SVGF + RGBA8 copy overlapping the next frame; "
+                           "compat filter: the synchronous kgk_svgf mode 0 call, device buffers"}
+
+    def cache_orbit(sc, w, h, cam_of, width, paths, kw2):
+        res = {}
+        o = np.empty((h, w, 4), np.float32)
+        for mode in ("plain", "cache"):
+            if mode == "cache":
+                sc.cache_init(width=width, train_paths=paths, seed=1)
+            dev = 0.0
+            for f in range(warmup + frames):
+                _, st = sc.render(cam_of(f), w, h, spp=1, seed=1, frame_index=f, use_cache=mode == "cache", out=o,
+                                  **kw2)
+                if f >= warmup:
+                    dev += st["ms_device"]
+            res[mode] = round(frames / (dev / 1e3), 2)
+        return res
+
+    kw4 = dict(max_depth=md, estimator=ESTIMATOR_UNBIASED)
+    r4 = cache_orbit(scene, W, H, lambda f: orbit_camera(f, H), 64, 1 << 16, kw4)
+    out["c4"] = {"workload": "cache-orbit-1080p-1spp", "value": r4["cache"], "unit": "frames/s",
+                 "plain_frames_per_s": r4["plain"], "frames": frames, "cache": "width 64, 65,536 training paths",
+                 "timing": "device time of the frames (CUDA events on the library's stream)"}
+    t1 = time.perf_counter()
+    tris5, mats5, tex5, _ = scenes.c5_scene()
+    env5, _ = scenes.sky_environment(4096, 2048, sun_peak=1e4, seed=3)
+    gen_s = time.perf_counter() - t1
+    W5, H5 = 3840, 2160
+    with Scene(tris5, mats5, textures=[np.zeros((1, 1, 3), np.float32)] * len(tex5), env=env5) as s5:
+        s5.set_textures_rgba8(tex5)
+        s5.build_bvh()
+        r5 = cache_orbit(s5, W5, H5, lambda f: orbit_camera(f, H5, radius=60.0, z=14.0, target_z=12.0), 128,
+                         1 << 18, dict(kw4, texture_filter=1))
+    out["c5"] = {"workload": "c5-10.6M-4k-1spp-orbit", "triangles": int(len(tris5)), "value": r5["cache"],
+                 "unit": "frames/s", "plain_frames_per_s": r5["plain"], "frames": frames,
+                 "cache": "width 128, 2^18 training paths per frame", "scene_generation_s": round(gen_s, 1),
+                 "timing": "device time of the frames (CUDA events on the library's stream)"}
+    return out
+
+
 def run_svgf_orbit(args):
     """The 1-spp orbit with SVGF: 1920x1080, 60 frames (6 degrees per frame) of
     the 5.2M-triangle scene, each rendered at 1 spp with its G-buffer and
@@ -440,7 +538,7 @@ def run_svgf_orbit(args):
     from kagayaki_gb300.structs import KgkSvgfConfig
     tris, mats, env, info = build_workload()
     W, H = args.width or 1920, args.height or 1080
-    frames = 60
+    frames = args.frames
     scene = Scene(tris, mats, env=env)
     scene.build_bvh()
     kw = dict(spp=1, max_depth=WORKLOAD["max_depth"], estimator=ESTIMATOR_UNBIASED, write_gbuffer=True)
@@ -489,6 +587,22 @@ def run_svgf_orbit(args):
     last_rgba = bufs[(frames - 1) % 2].array.copy()
     for b in bufs:
         b.free()
+    # the compat filter (ApplySVGF's race-free reading over the reference's
+    # records, kgk_svgf mode 0) on the same frames: the filter alone, frame
+    # and output on the device, each call synchronous
+    import torch
+    cfg_c = KgkSvgfConfig(mode=0, width=W, height=H, frame_index=0)
+    dev_out = torch.empty((H, W, 4), dtype=torch.float32, device="cuda")
+    compat_s = []
+    for f in range(13):
+        scene.render(orbit_camera(f, H), W, H, seed=3, frame_index=f, keep_on_device=True, **kw)
+        scene.sync()
+        cfg_c.frame_index = f
+        t0 = time.perf_counter()
+        check(lib().kgk_svgf_output(scene._h, ctypes.byref(cfg_c), None, ctypes.c_void_p(dev_out.data_ptr()),
+                                    None, 0))
+        compat_s.append(time.perf_counter() - t0)
+    compat_ms = 1e3 * float(np.median(compat_s[3:]))
     # the same frame through the float path, tone-mapped on the host
     from kagayaki_gb300 import tonemap
     rgba_match = bool(np.array_equal(last_rgba, tonemap(filt)))
@@ -510,6 +624,10 @@ def run_svgf_orbit(args):
             "e2e": {"value": round(frames / secs, 2), "unit": "frames/s", "h2d_bytes_per_step": 72 + 72,
                     "d2h_bytes_per_step": W * H * 4},
             "float_host_buffers_frames_per_s": round(frames / secs_float, 2),
+            "compat_filter_ms_per_frame": {"value": round(compat_ms, 3),
+                                           "what": "kgk_svgf mode 0 (ApplySVGF, 5 x 5 a-trous passes) at the "
+                                                   "same size, device buffers, wall clock of the synchronous "
+                                                   "call, median of 10 frames after 3"},
             "rgba8_equals_host_tonemap_of_float_path": rgba_match,
             "relmse_last_frame": {"reference_spp": int(nref),
                                   "noisy_1spp": round(rel_mse(noisy[..., :3].astype(np.float64), ref), 5),
@@ -957,6 +1075,7 @@ def main():
     ap.add_argument("--width", type=int, default=0, help="override the frame width (profiling cases)")
     ap.add_argument("--height", type=int, default=0, help="override the frame height")
     ap.add_argument("--spp", type=int, default=0, help="override the samples per pixel")
+    ap.add_argument("--frames", type=int, default=60, help="orbit frames of svgf-orbit (profiling cases)")
     args = ap.parse_args()
     if args.workload == "c1":
         if int(os.environ.get("RANK", "0")) == 0:

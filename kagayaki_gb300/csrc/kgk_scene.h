@@ -24,10 +24,11 @@ struct SvgfState {
     kgk_svgf_buffer *prev = nullptr, *cur = nullptr;   // compat: reference-layout records
     float4 *hist = nullptr, *hist_prev = nullptr;      // standard: demodulated colour, w = history length
     float2 *mom = nullptr, *mom_prev = nullptr;        // standard: luminance moments
-    float4 *nd_prev = nullptr;                         // previous normal + depth
-    int *mat_prev = nullptr;                           // previous material id (-1 = no hit)
-    float4 *col = nullptr, *tmp = nullptr;             // colour + variance ping-pong
-    float *gvar = nullptr;                             // 3x3-blurred variance
+    float4 *nd = nullptr, *nd_prev = nullptr;          // standard: normal + depth, this frame and the last
+    int *mat = nullptr, *mat_prev = nullptr;           // standard: material id (-1 = no hit), same
+    float *gz = nullptr;                               // standard: sigma_z |grad depth|
+    float4 *col = nullptr, *tmp = nullptr;             // standard: colour + variance ping-pong
+    unsigned char *compat_scratch = nullptr;           // compat: the filter's scratch (compat_scratch_bytes)
     kgk_camera prev_cam{};
     bool has_prev = false;
 };

@@ -75,6 +75,14 @@ struct CompatArgs {
     float *M1, *M2, *sd, *gz, *s1, *s2, *sw, *var;
     unsigned char *spatial;
     kgk_vec *R2;
+    // the a-trous passes' per-pixel guide, packed from the records once their
+    // fields are final (k_c_gauss2): normal and depth, ObjectID and MaterialID
+    float4 *gnd;
+    int2 *gom;
+    // each pass's input radiance divided by (albedo + sINF), with its
+    // luminance in w: written by the pass before (ping-pong), so a tap reads
+    // it instead of dividing
+    float4 *dm, *dm2;
 };
 
 #define FOR_PIXELS(n) for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < (n); p += gridDim.x * blockDim.x)
@@ -174,6 +182,9 @@ __global__ void k_c_var1(CompatArgs a) {
         const float d = c.Depth;
         a.gz[2 * p] = (a.C[W * y + x + dx].Depth - d) / (float)dx;
         a.gz[2 * p + 1] = (a.C[W * (y + dy) + x].Depth - d) / (float)dy;
+        // the guide k_c_var3 reads (the records as they are before k_c_var4)
+        a.gnd[p] = make_float4(c.Normal.x, c.Normal.y, c.Normal.z, d);
+        a.gom[p] = make_int2(c.ObjectID, c.MaterialID);
     }
 }
 
@@ -201,46 +212,66 @@ __constant__ float cKW[25] = {1 / 256.0f, 4 / 256.0f, 6 / 256.0f, 4 / 256.0f, 1 
                               4 / 256.0f, 16 / 256.0f, 24 / 256.0f, 16 / 256.0f, 4 / 256.0f,
                               1 / 256.0f, 4 / 256.0f, 6 / 256.0f, 4 / 256.0f, 1 / 256.0f};
 
-// 7x7 edge-stopped moment filter (SVGF.cuh:166-225)
-__global__ void k_c_var3(CompatArgs a) {
+// 7x7 edge-stopped moment filter (SVGF.cuh:166-225) on 32 x 8-pixel tiles:
+// a block stages the guide, ids and moments of its pixels and a halo of 3,
+// then sums in the reference's order (kx outer, ky inner).
+constexpr int kCTX = 32, kCTY = 8;
+__global__ void __launch_bounds__(256) k_c_var3(CompatArgs a) {
+    constexpr int R = 3, SX = kCTX + 2 * R, SY = kCTY + 2 * R;
+    __shared__ float4 s_nd[SY * SX];
+    __shared__ int2 s_om[SY * SX];
+    __shared__ float2 s_m[SY * SX];
     const int W = a.W, H = a.H;
-    FOR_PIXELS(W * H) {
-        a.sw[p] = a.s1[p] = a.s2[p] = 0.0f;
-        if (!a.spatial[p]) continue;
-        const int x = p % W, y = p / W;
-        const kgk_svgf_buffer &c = a.C[p];
-        const float3 n = v3(c.Normal);
-        float s1 = 0, s2 = 0, sw = 0;
-        for (int kx = -3; kx <= 3; ++kx) {
-            const int nx = x + kx;
-            if (nx < 0 || nx >= W) continue;
-            const float hx = cK7[kx + 3];
-            for (int ky = -3; ky <= 3; ++ky) {
-                const int ny = y + ky;
-                if (ny < 0 || ny >= H) continue;
-                const float hy = cK7[ky + 3];
-                if (kx == 0 && ky == 0) {
-                    s1 += hx * hy * a.M1[p];
-                    s2 += hx * hy * a.M2[p];
-                    sw += hx * hy;
-                    continue;
-                }
-                const int q = W * ny + nx;
-                const kgk_svgf_buffer &d = a.C[q];
-                if (d.ObjectID == -1) continue;
-                const float wm = c.MaterialID == d.MaterialID ? 1.0f : 0.0f;
-                const float wz = depth_w(c.Depth, d.Depth, kx, ky, a.gz[2 * p], a.gz[2 * p + 1]);
-                const float wn = normal_w(n, v3(d.Normal));
-                const float w = hx * hy * wz * wn * wm;
-                s1 += w * a.M1[q];
-                s2 += w * a.M2[q];
-                sw += w;
-            }
-        }
-        a.s1[p] = s1;
-        a.s2[p] = s2;
-        a.sw[p] = sw;
+    const int x0 = blockIdx.x * kCTX - R, y0 = blockIdx.y * kCTY - R;
+    for (int i = threadIdx.y * kCTX + threadIdx.x; i < SX * SY; i += kCTX * kCTY) {
+        const int gx = x0 + i % SX, gy = y0 + i / SX;
+        if (gx < 0 || gx >= W || gy < 0 || gy >= H) continue;
+        const int q = W * gy + gx;
+        s_nd[i] = a.gnd[q];
+        s_om[i] = a.gom[q];
+        s_m[i] = make_float2(a.M1[q], a.M2[q]);
     }
+    __syncthreads();
+    const int x = blockIdx.x * kCTX + threadIdx.x, y = blockIdx.y * kCTY + threadIdx.y;
+    if (x >= W || y >= H) return;
+    const int p = W * y + x, c = SX * (threadIdx.y + R) + threadIdx.x + R;
+    a.sw[p] = a.s1[p] = a.s2[p] = 0.0f;
+    if (!a.spatial[p]) return;
+    const float4 cn = s_nd[c];
+    const int cmat = s_om[c].y;
+    const float3 n = f3(cn);
+    const float gzx = a.gz[2 * p], gzy = a.gz[2 * p + 1];
+    float s1 = 0, s2 = 0, sw = 0;
+    for (int kx = -3; kx <= 3; ++kx) {
+        const int nx = x + kx;
+        if (nx < 0 || nx >= W) continue;
+        const float hx = cK7[kx + 3];
+        for (int ky = -3; ky <= 3; ++ky) {
+            const int ny = y + ky;
+            if (ny < 0 || ny >= H) continue;
+            const float hy = cK7[ky + 3];
+            if (kx == 0 && ky == 0) {
+                s1 += hx * hy * s_m[c].x;
+                s2 += hx * hy * s_m[c].y;
+                sw += hx * hy;
+                continue;
+            }
+            const int t = c + SX * ky + kx;
+            const int2 om = s_om[t];
+            if (om.x == -1) continue;
+            const float4 qn = s_nd[t];
+            const float wm = cmat == om.y ? 1.0f : 0.0f;
+            const float wz = depth_w(cn.w, qn.w, kx, ky, gzx, gzy);
+            const float wn = normal_w(n, f3(qn));
+            const float w = hx * hy * wz * wn * wm;
+            s1 += w * s_m[t].x;
+            s2 += w * s_m[t].y;
+            sw += w;
+        }
+    }
+    a.s1[p] = s1;
+    a.s2[p] = s2;
+    a.sw[p] = sw;
 }
 
 __global__ void k_c_var4(CompatArgs a) {
@@ -312,74 +343,225 @@ __global__ void k_c_gauss2(CompatArgs a) {
             a.sd[p] = sqrtf(a.s1[p] / a.sw[p]);
         }
         a.var[p] = c.Variance;
+        // the records' normal, depth, ids and albedo are final from here to
+        // the end of the a-trous passes, and so is R before the first pass
+        a.gnd[p] = make_float4(c.Normal.x, c.Normal.y, c.Normal.z, c.Depth);
+        a.gom[p] = make_int2(c.ObjectID, c.MaterialID);
+        const float3 dc = div3(v3(a.R[p]), v3(c.Albedo) + f3(kS, kS, kS));
+        a.dm[p] = make_float4(dc.x, dc.y, dc.z, lumf(dc));
+        // the a-trous passes' depth gradient (SVGF.cuh:366-372), from the
+        // records as k_c_var4 left them; k_c_var3 was the last reader of gz
+        const int W = a.W, x = p % W, y = p / W;
+        const int dx = x < W / 2 ? 1 : -1, dy = y < a.H / 2 ? 1 : -1;
+        a.gz[2 * p] = (a.C[W * y + x + dx].Depth - c.Depth) / (float)dx;
+        a.gz[2 * p + 1] = (a.C[W * (y + dy) + x].Depth - c.Depth) / (float)dy;
     }
 }
 
-// One a-trous stage (SVGF.cuh:347-474).  Reads Rin / var_in, writes Rout /
-// var_out (copies for untouched pixels keep the ping-pong consistent).
-__global__ void k_c_atrous(CompatArgs a, const kgk_vec *__restrict__ Rin, kgk_vec *Rout,
-                           const float *__restrict__ vin, float *vout, int stage) {
-    const int W = a.W, H = a.H;
-    FOR_PIXELS(W * H) {
-        const int x = p % W, y = p / W;
-        kgk_svgf_buffer &c = a.C[p];
-        const float3 alb = v3(c.Albedo);
-        const float3 dc = div3(v3(Rin[p]), alb + f3(kS, kS, kS));
-        const float l = lumf(dc);
-        const float d = c.Depth;
-        const int dx = x < W / 2 ? 1 : -1, dy = y < H / 2 ? 1 : -1;
-        const float gx = (a.C[W * y + x + dx].Depth - d) / (float)dx;
-        const float gy = (a.C[W * (y + dy) + x].Depth - d) / (float)dy;
-        const float3 n = v3(c.Normal);
-        const float sdv = a.sd[p];
-        float3 srad = f3(0.0f, 0.0f, 0.0f);
-        float svar = 0.0f, swt = 0.0f;
-        for (int ki = 0; ki < 25; ++ki) {
-            const float h = cKW[ki];
-            const int qx = x + ((ki % 5 - 2) * (1 << stage)), qy = y + ((ki / 5 - 2) * (1 << stage));
-            if (qx < 0 || qx >= W || qy < 0 || qy >= H) continue;
-            const int q = W * qy + qx;
-            if (ki == 12) {
-                svar += h * h * vin[p];
-                srad += dc * h;
-                swt += h;
-                continue;
-            }
-            const kgk_svgf_buffer &e = a.C[q];
-            if (e.ObjectID == -1) continue;
-            const float3 nr = div3(v3(Rin[q]), v3(e.Albedo) + f3(kS, kS, kS));
-            const float nl = lumf(nr);
-            if (((double)l > 0.5 && nl > 5 * l) || ((double)l > 0.1 && nl > 50 * l) || (l > kS && nl > 100 * l))
-                continue;
-            const float wm = c.MaterialID == e.MaterialID ? 1.0f : 0.0f;
-            const float wz = depth_w(d, e.Depth, qx, qy, gx, gy);  // absolute coordinates, SVGF.cuh:426
-            const float wn = normal_w(n, v3(e.Normal));
-            const float wl = lum_w(l, nl, sdv);
-            const float w = c.willApplyATrousFilter ? h * wz * wn * wl * wm : h * wz * wn * wm;
-            srad += nr * w;
-            svar += w * w * vin[q];
-            swt += w;
-        }
-        Rout[p] = Rin[p];
-        vout[p] = vin[p];
-        if (c.ObjectID == -1) continue;
-        if (swt < 1e-6f || swt * swt < 1e-6f) {
-            a.F[p] = Rin[p];
-            c.willApplyTemporalAccumulation = true;
+// One a-trous stage (SVGF.cuh:347-474) of pixel p = (x, y) at step 2^stage.
+// Reads go through Src: the global arrays (k_c_atrous) or a shared-memory
+// tile of them (k_c_atrous_tile); either way every tap is the reference's
+// expression in its order, so both give the same bits.  A tap's neighbour
+// radiance comes demodulated with its luminance (dm, written by the pass
+// before) instead of being divided by its albedo at every tap.
+struct CompatIO {
+    const kgk_vec *Rin;
+    kgk_vec *Rout;
+    const float4 *dmin;
+    float4 *dmout;
+    const float *vin;
+    float *vout;
+};
+
+template <class Src>
+__device__ __forceinline__ void compat_atrous_px(const CompatArgs &a, const CompatIO &io, const Src &S, int x, int y,
+                                                 int stage) {
+    const int W = a.W, H = a.H, p = W * y + x, step = 1 << stage;
+    kgk_svgf_buffer &c = a.C[p];
+    const float4 g = S.nd(0, 0);
+    const int2 om = S.om(0, 0);
+    const float4 dcl = S.dm(0, 0);
+    const float3 dc = f3(dcl);
+    const float l = dcl.w;
+    const float d = g.w;
+    const float gx = a.gz[2 * p], gy = a.gz[2 * p + 1];
+    const float3 n = f3(g);
+    const float sdv = a.sd[p];
+    const bool filt = c.willApplyATrousFilter;
+    float3 srad = f3(0.0f, 0.0f, 0.0f);
+    float svar = 0.0f, swt = 0.0f;
+#pragma unroll
+    for (int ki = 0; ki < 25; ++ki) {
+        const float h = cKW[ki];
+        const int ox = (ki % 5 - 2) * step, oy = (ki / 5 - 2) * step;
+        const int qx = x + ox, qy = y + oy;
+        if (qx < 0 || qx >= W || qy < 0 || qy >= H) continue;
+        if (ki == 12) {
+            svar += h * h * S.v(0, 0);
+            srad += dc * h;
+            swt += h;
             continue;
         }
-        const float3 fl = srad / swt;
-        const float fv = svar / (swt * swt);
-        const float cw = 0.2f;
-        const float3 o = (fl * alb) * cw + v3(Rin[p]) * (1 - cw);
-        a.F[p] = kv(o);
-        Rout[p] = kv(o);
-        if (c.willApplyATrousFilter) vout[p] = cw * vin[p] + (1 - cw) * fv;
-        if (stage == 0) {
-            c.ColorHistory = kv(o);
-            c.willApplyTemporalAccumulation = true;
-        }
+        const int2 eo = S.om(ox, oy);
+        if (eo.x == -1) continue;
+        const float4 em = S.dm(ox, oy);
+        const float3 nr = f3(em);
+        const float nl = em.w;
+        if (((double)l > 0.5 && nl > 5 * l) || ((double)l > 0.1 && nl > 50 * l) || (l > kS && nl > 100 * l))
+            continue;
+        const float4 eg = S.nd(ox, oy);
+        const float wm = om.y == eo.y ? 1.0f : 0.0f;
+        const float wz = depth_w(d, eg.w, qx, qy, gx, gy);  // absolute coordinates, SVGF.cuh:426
+        const float wn = normal_w(n, f3(eg));
+        const float wl = lum_w(l, nl, sdv);
+        const float w = filt ? h * wz * wn * wl * wm : h * wz * wn * wm;
+        srad += nr * w;
+        svar += w * w * S.v(ox, oy);
+        swt += w;
     }
+    const kgk_vec rin = io.Rin[p];
+    const float vc = S.v(0, 0);
+    if (om.x == -1 || swt < 1e-6f || swt * swt < 1e-6f) {
+        io.Rout[p] = rin;
+        io.vout[p] = vc;
+        io.dmout[p] = dcl;
+        if (om.x == -1) return;
+        a.F[p] = rin;
+        c.willApplyTemporalAccumulation = true;
+        return;
+    }
+    const float3 alb = v3(c.Albedo);
+    const float3 fl = srad / swt;
+    const float fv = svar / (swt * swt);
+    const float cw = 0.2f;
+    const float3 o = (fl * alb) * cw + v3(rin) * (1 - cw);
+    a.F[p] = kv(o);
+    io.Rout[p] = kv(o);
+    const float3 od = div3(o, alb + f3(kS, kS, kS));
+    io.dmout[p] = make_float4(od.x, od.y, od.z, lumf(od));
+    io.vout[p] = filt ? cw * vc + (1 - cw) * fv : vc;
+    if (stage == 0) {
+        c.ColorHistory = kv(o);
+        c.willApplyTemporalAccumulation = true;
+    }
+}
+
+// Taps read straight from the global arrays (offsets from pixel p).
+struct CompatGlobal {
+    const float4 *gnd_, *dm_;
+    const int2 *gom_;
+    const float *v_;
+    int p, W;
+    __device__ float4 nd(int ox, int oy) const { return gnd_[p + W * oy + ox]; }
+    __device__ int2 om(int ox, int oy) const { return gom_[p + W * oy + ox]; }
+    __device__ float4 dm(int ox, int oy) const { return dm_[p + W * oy + ox]; }
+    __device__ float v(int ox, int oy) const { return v_[p + W * oy + ox]; }
+};
+
+__global__ void k_c_atrous(CompatArgs a, CompatIO io, int stage) {
+    const int W = a.W;
+    FOR_PIXELS(W * a.H) {
+        const CompatGlobal S{a.gnd, io.dmin, a.gom, io.vin, p, W};
+        compat_atrous_px(a, io, S, p % W, p / W, stage);
+    }
+}
+
+// The same stage for steps 1, 2 and 4 on 32 x 8-pixel tiles: a block stages
+// its pixels and a halo of 2 * step (all 25 taps and the depth gradient's
+// neighbours) in shared memory - guide, ids, demodulated radiance, variance -
+// then filters from there.  Entries outside the image are never read (the
+// tap's bounds test comes first).
+template <int kStep> struct CTile {
+    static constexpr int R = 2 * kStep, SX = kCTX + 2 * R, SY = kCTY + 2 * R, N = SX * SY;
+    static constexpr size_t kSmem = (size_t)N * (2 * sizeof(float4) + sizeof(int2) + sizeof(float));
+};
+
+// Taps read from a tile of row length SX (offsets from entry c).
+template <int SX> struct CompatShared {
+    const float4 *snd, *sdm;
+    const int2 *som;
+    const float *sv;
+    int c;
+    __device__ float4 nd(int ox, int oy) const { return snd[c + SX * oy + ox]; }
+    __device__ int2 om(int ox, int oy) const { return som[c + SX * oy + ox]; }
+    __device__ float4 dm(int ox, int oy) const { return sdm[c + SX * oy + ox]; }
+    __device__ float v(int ox, int oy) const { return sv[c + SX * oy + ox]; }
+};
+
+template <int kStep>
+__global__ void __launch_bounds__(256) k_c_atrous_tile(CompatArgs a, CompatIO io) {
+    using T = CTile<kStep>;
+    extern __shared__ __align__(16) unsigned char smem[];
+    float4 *s_nd = (float4 *)smem;
+    float4 *s_dm = s_nd + T::N;
+    int2 *s_om = (int2 *)(s_dm + T::N);
+    float *s_v = (float *)(s_om + T::N);
+    const int W = a.W, H = a.H;
+    const int x0 = blockIdx.x * kCTX - T::R, y0 = blockIdx.y * kCTY - T::R;
+    for (int i = threadIdx.y * kCTX + threadIdx.x; i < T::N; i += kCTX * kCTY) {
+        const int gx = x0 + i % T::SX, gy = y0 + i / T::SX;
+        if (gx < 0 || gx >= W || gy < 0 || gy >= H) continue;
+        const int q = W * gy + gx;
+        s_nd[i] = a.gnd[q];
+        s_dm[i] = io.dmin[q];
+        s_om[i] = a.gom[q];
+        s_v[i] = io.vin[q];
+    }
+    __syncthreads();
+    const int x = blockIdx.x * kCTX + threadIdx.x, y = blockIdx.y * kCTY + threadIdx.y;
+    if (x >= W || y >= H) return;
+    const CompatShared<T::SX> S{s_nd, s_dm, s_om, s_v, T::SX * ((int)threadIdx.y + T::R) + (int)threadIdx.x + T::R};
+    compat_atrous_px(a, io, S, x, y, kStep == 1 ? 0 : kStep == 2 ? 1 : 2);
+}
+
+// The same stage for steps of 8 and more on row segments: a block of 256
+// threads takes 256 pixels of one row and stages the five rows its taps read
+// (y + {-2, -1, 0, 1, 2} step), each 256 + 4 step entries wide, so that every
+// tap comes from shared memory and the staging reads are coalesced.
+template <int kStep> struct CRows {
+    static constexpr int T = 256, R = 2 * kStep, SX = T + 2 * R, N = 5 * SX;
+    static constexpr size_t kSmem = (size_t)N * (2 * sizeof(float4) + sizeof(int2) + sizeof(float));
+};
+
+// Taps read from the five staged rows (row pitch SX, one row per step).
+template <int SX, int kStep> struct CompatRows {
+    const float4 *snd, *sdm;
+    const int2 *som;
+    const float *sv;
+    int c;
+    __device__ int at(int ox, int oy) const { return c + SX * (oy / kStep) + ox; }
+    __device__ float4 nd(int ox, int oy) const { return snd[at(ox, oy)]; }
+    __device__ int2 om(int ox, int oy) const { return som[at(ox, oy)]; }
+    __device__ float4 dm(int ox, int oy) const { return sdm[at(ox, oy)]; }
+    __device__ float v(int ox, int oy) const { return sv[at(ox, oy)]; }
+};
+
+template <int kStep>
+__global__ void __launch_bounds__(256) k_c_atrous_rows(CompatArgs a, CompatIO io) {
+    using T = CRows<kStep>;
+    extern __shared__ __align__(16) unsigned char smem[];
+    float4 *s_nd = (float4 *)smem;
+    float4 *s_dm = s_nd + T::N;
+    int2 *s_om = (int2 *)(s_dm + T::N);
+    float *s_v = (float *)(s_om + T::N);
+    const int W = a.W, H = a.H, y = blockIdx.y;
+    const int x0 = blockIdx.x * T::T - T::R;
+    for (int i = threadIdx.x; i < T::N; i += T::T) {
+        const int gx = x0 + i % T::SX, gy = y + (i / T::SX - 2) * kStep;
+        if (gx < 0 || gx >= W || gy < 0 || gy >= H) continue;
+        const int q = W * gy + gx;
+        s_nd[i] = a.gnd[q];
+        s_dm[i] = io.dmin[q];
+        s_om[i] = a.gom[q];
+        s_v[i] = io.vin[q];
+    }
+    __syncthreads();
+    const int x = blockIdx.x * T::T + threadIdx.x;
+    if (x >= W) return;
+    constexpr int stage = kStep == 8 ? 3 : kStep == 16 ? 4 : kStep == 32 ? 5 : 6;
+    static_assert((1 << stage) == kStep, "row-tile steps are 8, 16, 32 and 64");
+    const CompatRows<T::SX, kStep> S{s_nd, s_dm, s_om, s_v, 2 * T::SX + (int)threadIdx.x + T::R};
+    compat_atrous_px(a, io, S, x, y, stage);
 }
 
 __global__ void k_c_final(CompatArgs a, const float *var) {
@@ -395,12 +577,16 @@ __global__ void k_copy_vec(const kgk_vec *src, kgk_vec *dst, int n) {
 
 // Scratch of the compat pipeline, carved from one block: M1, M2, sd, gz (two
 // arrays), s1, s2, sw, var, var2 at `fl` bytes each, then R2 (`vec` bytes),
-// then the per-pixel spatial flags; every array starts on a 256-byte boundary.
-// Returns var2, the second variance buffer of the a-trous passes.
+// the guide (gnd, 16 B a pixel), the ids (gom, 8 B), the two demodulated
+// radiance buffers (dm, dm2, 16 B each), then the per-pixel spatial flags;
+// every array starts on a 256-byte boundary.  Returns var2, the second
+// variance buffer of the a-trous passes.
 constexpr size_t scratch_up(size_t x) { return (x + 255) & ~(size_t)255; }
 constexpr size_t compat_fl(size_t npx) { return scratch_up(npx * sizeof(float)); }
 constexpr size_t compat_vec(size_t npx) { return scratch_up(npx * sizeof(kgk_vec)); }
-constexpr size_t compat_scratch_bytes(size_t npx) { return 10 * compat_fl(npx) + compat_vec(npx) + npx; }
+constexpr size_t compat_scratch_bytes(size_t npx) {
+    return 10 * compat_fl(npx) + 4 * compat_vec(npx) + scratch_up(npx * sizeof(int2)) + npx;
+}
 
 float *carve_compat(CompatArgs &a, unsigned char *b, size_t fl, size_t vec) {
     a.M1 = (float *)b; b += fl;
@@ -413,6 +599,10 @@ float *carve_compat(CompatArgs &a, unsigned char *b, size_t fl, size_t vec) {
     a.var = (float *)b; b += fl;
     float *var2 = (float *)b; b += fl;
     a.R2 = (kgk_vec *)b; b += vec;
+    a.gnd = (float4 *)b; b += vec;
+    a.dm = (float4 *)b; b += vec;
+    a.dm2 = (float4 *)b; b += vec;
+    a.gom = (int2 *)b; b += scratch_up(vec / 2);
     a.spatial = b;
     return var2;
 }
@@ -423,21 +613,39 @@ float *carve_compat(CompatArgs &a, unsigned char *b, size_t fl, size_t vec) {
 kgk_status launch_compat(CompatArgs &a, float *var2, int repeats, int stages, cudaStream_t st) {
     const size_t npx = (size_t)a.W * a.H;
     const int g = (int)std::min<size_t>((npx + 255) / 256, 65535);
+    KGK_CUDA(cudaFuncSetAttribute(k_c_atrous_tile<4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)CTile<4>::kSmem));
+    KGK_CUDA(cudaFuncSetAttribute(k_c_atrous_rows<8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)CRows<8>::kSmem));
+    KGK_CUDA(cudaFuncSetAttribute(k_c_atrous_rows<16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)CRows<16>::kSmem));
     k_c_prologue<<<g, 256, 0, st>>>(a);
     k_c_temporal<<<g, 256, 0, st>>>(a);
     k_c_var1<<<g, 256, 0, st>>>(a);
     k_c_var2<<<g, 256, 0, st>>>(a);
-    k_c_var3<<<g, 256, 0, st>>>(a);
+    const dim3 tiles((a.W + kCTX - 1) / kCTX, (a.H + kCTY - 1) / kCTY), tile_threads(kCTX, kCTY);
+    k_c_var3<<<tiles, tile_threads, 0, st>>>(a);
     k_c_var4<<<g, 256, 0, st>>>(a);
     k_c_var5<<<g, 256, 0, st>>>(a);
     k_c_gauss1<<<g, 256, 0, st>>>(a);
     k_c_gauss2<<<g, 256, 0, st>>>(a);
     kgk_vec *rin = a.R, *rout = a.R2;
+    float4 *din = a.dm, *dout = a.dm2;
     float *vin = a.var, *vout = var2;
     for (int k = 0; k < repeats; ++k)
         for (int s = 0; s < stages; ++s) {
-            k_c_atrous<<<g, 256, 0, st>>>(a, rin, rout, vin, vout, s);
+            const CompatIO io{rin, rout, din, dout, vin, vout};
+            const dim3 rows((a.W + 255) / 256, a.H);
+            switch (s) {
+                case 0: k_c_atrous_tile<1><<<tiles, tile_threads, CTile<1>::kSmem, st>>>(a, io); break;
+                case 1: k_c_atrous_tile<2><<<tiles, tile_threads, CTile<2>::kSmem, st>>>(a, io); break;
+                case 2: k_c_atrous_tile<4><<<tiles, tile_threads, CTile<4>::kSmem, st>>>(a, io); break;
+                case 3: k_c_atrous_rows<8><<<rows, 256, CRows<8>::kSmem, st>>>(a, io); break;
+                case 4: k_c_atrous_rows<16><<<rows, 256, CRows<16>::kSmem, st>>>(a, io); break;
+                default: k_c_atrous<<<g, 256, 0, st>>>(a, io, s); break;
+            }
             std::swap(rin, rout);
+            std::swap(din, dout);
             std::swap(vin, vout);
         }
     if (rin != a.R) k_copy_vec<<<g, 256, 0, st>>>(rin, a.R, (int)npx);
@@ -449,38 +657,54 @@ kgk_status launch_compat(CompatArgs &a, float *var2, int repeats, int stages, cu
 }
 
 // Runs the compat pipeline on device buffers (R, F, P, C all W*H records),
-// with scratch allocated for the call.
+// with `scratch` (compat_scratch_bytes(W * H)), or scratch allocated for the
+// call when it is null.
 kgk_status run_compat(kgk_vec *R, kgk_vec *F, kgk_svgf_buffer *P, kgk_svgf_buffer *C, int W, int H, int frame,
-                      int repeats, int stages, cudaStream_t st) {
+                      int repeats, int stages, cudaStream_t st, unsigned char *scratch = nullptr) {
     const size_t npx = (size_t)W * H;
-    void *scratch = nullptr;
-    KGK_TRY(dmalloc(&scratch, compat_scratch_bytes(npx), "SVGF scratch"));
+    void *owned = nullptr;
+    if (!scratch) {
+        KGK_TRY(dmalloc(&owned, compat_scratch_bytes(npx), "SVGF scratch"));
+        scratch = (unsigned char *)owned;
+    }
     CompatArgs a;
     a.W = W; a.H = H; a.frame = frame; a.R = R; a.F = F; a.P = P; a.C = C;
-    float *var2 = carve_compat(a, (unsigned char *)scratch, compat_fl(npx), compat_vec(npx));
+    float *var2 = carve_compat(a, scratch, compat_fl(npx), compat_vec(npx));
     const kgk_status stt = launch_compat(a, var2, repeats, stages, st);
-    dfree(scratch);
+    if (owned) dfree(owned);
     return stt;
 }
 
 // Fills reference-layout records from the renderer's G-buffer, the way
-// render.cuh:28 (init) and RayTrace.cuh:66-82 fill them.
-__global__ void k_gbuffer_to_records(const float4 *pos, const float4 *nrm, const float4 *alb, const float4 *emi,
-                                     int npx, kgk_svgf_buffer *C) {
-    FOR_PIXELS(npx) {
+// render.cuh:28 (init) and RayTrace.cuh:66-82 fill them.  A block builds its
+// 256 records in shared memory and writes them out as consecutive words, so
+// that the 112-byte records are stored with coalesced writes.
+constexpr int kRecWords = (int)(sizeof(kgk_svgf_buffer) / 4);
+__global__ void __launch_bounds__(256) k_gbuffer_to_records(const float4 *pos, const float4 *nrm, const float4 *alb,
+                                                            const float4 *emi, size_t npx, kgk_svgf_buffer *C) {
+    __shared__ __align__(16) unsigned s_rec[256 * kRecWords];
+    const size_t base = (size_t)blockIdx.x * 256;
+    const int n = (int)min((size_t)256, npx - base);
+    if ((int)threadIdx.x < n) {
+        const size_t p = base + threadIdx.x;
         kgk_svgf_buffer b;
         sb_init(b);
-        const int obj = __float_as_int(nrm[p].w);
+        const float4 nr = nrm[p];
+        const int obj = __float_as_int(nr.w);
         if (obj >= 0) {
-            b.Albedo = kv(f3(alb[p]));
+            const float4 al = alb[p];
+            b.Albedo = kv(f3(al));
             b.Emission = kv(f3(emi[p]));
-            b.Normal = kv(f3(nrm[p]));
+            b.Normal = kv(f3(nr));
             b.ObjectID = obj;
-            b.MaterialID = __float_as_int(alb[p].w);
+            b.MaterialID = __float_as_int(al.w);
             b.Depth = pos[p].w;
         }
-        C[p] = b;
+        *reinterpret_cast<kgk_svgf_buffer *>(s_rec + threadIdx.x * kRecWords) = b;
     }
+    __syncthreads();
+    unsigned *dst = reinterpret_cast<unsigned *>(C + base);
+    for (int i = threadIdx.x; i < n * kRecWords; i += 256) dst[i] = s_rec[i];
 }
 
 // ---------------------------------------------------------------------------
@@ -488,15 +712,14 @@ __global__ void k_gbuffer_to_records(const float4 *pos, const float4 *nrm, const
 // ---------------------------------------------------------------------------
 struct StdArgs {
     int W, H;
-    int sn_log2;                           // log2(sigma_n) when it is a power of two <= 2^16, else -1
     const float4 *pos, *nrm, *alb, *emi;   // current G-buffer
     const float4 *noisy;                   // current frame (kgk_vec)
     float4 *hist, *hist_prev;
     float2 *mom, *mom_prev;
-    float4 *nd_prev;
-    int *mat_prev;
+    float4 *nd, *nd_prev;                  // normal + depth, this frame (written by k_s_temporal) and the last
+    int *mat, *mat_prev;                   // material id (>= 0) or -1 for no hit, same
+    float *gz;                             // sigma_z |grad depth| (k_s_variance)
     float4 *col, *tmp;
-    float *gvar;
     kgk_camera pcam;
     int has_prev;
     float alpha, sz, sn, sl;
@@ -518,20 +741,28 @@ __device__ __forceinline__ bool project_prev(const kgk_camera &c, int W, int H, 
     return true;
 }
 
+// Temporal integration; also writes this frame's guide (normal + depth,
+// material id) that the spatial passes read and the next frame reprojects
+// against.
 __global__ void k_s_temporal(StdArgs a) {
     const int W = a.W, H = a.H;
     FOR_PIXELS(W * H) {
         const float4 nr = a.nrm[p];
         const int obj = __float_as_int(nr.w);
         const float3 noisy = f3(a.noisy[p]);
+        const float4 ps = a.pos[p];
         if (obj < 0) {
             a.hist[p] = make_float4(noisy.x, noisy.y, noisy.z, 0.0f);
             a.mom[p] = make_float2(0.0f, 0.0f);
             a.col[p] = make_float4(noisy.x, noisy.y, noisy.z, 0.0f);
+            a.nd[p] = make_float4(nr.x, nr.y, nr.z, ps.w);
+            a.mat[p] = -1;
             continue;
         }
         const float4 al = a.alb[p];
-        const int mat = __float_as_int(al.w);
+        const int mat = max(__float_as_int(al.w), 0);
+        a.nd[p] = make_float4(nr.x, nr.y, nr.z, ps.w);
+        a.mat[p] = mat;
         const float3 albedo = f3(al);
         const float3 dl = div3(noisy, albedo + f3(kS, kS, kS));
         const float l = lumf(dl);
@@ -540,7 +771,6 @@ __global__ void k_s_temporal(StdArgs a) {
         float hl = 0.0f, wsum = 0.0f;
         if (a.has_prev) {
             float x, y;
-            const float4 ps = a.pos[p];
             if (project_prev(a.pcam, W, H, f3(ps), x, y)) {
                 // bilinear taps; pixel (X, Y)'s primary ray passes through
                 // integer screen coordinates (Generate1stRay)
@@ -559,10 +789,11 @@ __global__ void k_s_temporal(StdArgs a) {
                     if (fabsf(pn.w - exp_depth) > 0.05f * exp_depth + 1e-3f) continue;
                     const float w = ((k & 1) ? tx : 1.0f - tx) * ((k >> 1) ? ty : 1.0f - ty);
                     const float4 hp = a.hist_prev[q];
+                    const float2 mp = a.mom_prev[q];
                     hc += f3(hp) * w;
                     hl += hp.w * w;
-                    hm.x += a.mom_prev[q].x * w;
-                    hm.y += a.mom_prev[q].y * w;
+                    hm.x += mp.x * w;
+                    hm.y += mp.y * w;
                     wsum += w;
                 }
             }
@@ -576,9 +807,8 @@ __global__ void k_s_temporal(StdArgs a) {
             hm.y /= wsum;
             len = fminf(hl / wsum + 1.0f, 64.0f);
             const float ac = fmaxf(a.alpha, 1.0f / len);
-            const float am = fmaxf(a.alpha, 1.0f / len);
             c = hc * (1.0f - ac) + dl * ac;
-            m = make_float2(hm.x * (1.0f - am) + l * am, hm.y * (1.0f - am) + l * l * am);
+            m = make_float2(hm.x * (1.0f - ac) + l * ac, hm.y * (1.0f - ac) + l * l * ac);
         } else {
             c = dl;
             m = make_float2(l, l * l);
@@ -590,208 +820,291 @@ __global__ void k_s_temporal(StdArgs a) {
     }
 }
 
-__device__ __forceinline__ float depth_weight_std(float d, float dq, float grad, float dist, float sz) {
-    return __expf(-fabsf(d - dq) / (sz * fabsf(grad) * dist + 1e-3f));
+// The spatial passes' edge-stopping weight is one base-2 exponential:
+//   w = max(0, n.nq)^sigma_n * exp(-|d - dq| / (sigma_z |grad d| dist + 1e-3))
+//                            * exp(-|l - lq| / (sigma_l sqrt(var) + 1e-6))
+//     = 2^(sigma_n log2 max(0, n.nq) - |d - dq| rz(dist) - |l - lq| rl)
+// with rz(dist) = log2(e) / (sigma_z |grad d| dist + 1e-3) taken once per
+// pixel for each distinct tap distance, and rl likewise; lg2(0) = -inf gives
+// w = 0 for normals facing away.  Both are the hardware approximations
+// (ex2.approx / lg2.approx, relative error ~2^-22).
+constexpr float kLog2e = 1.44269504088896341f;
+__device__ __forceinline__ float ex2a(float x) {
+    float y;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float lg2a(float x) {
+    float y;
+    asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
 }
 
-// Normal weight max(0, n.nq)^sigma_n: repeated squaring when sigma_n is a
-// power of two (sn_log2 >= 0; 128 = seven squarings), else the fast power.
-__device__ __forceinline__ float normal_weight(float c, float sn, int sn_log2) {
-    c = fmaxf(0.0f, c);
-    if (sn_log2 >= 0) {
-        for (int i = 0; i < sn_log2; ++i) c *= c;
-        return c;
-    }
-    return c > 0.0f ? __powf(c, sn) : 0.0f;
-}
+// Tiles of the standard filter's spatial passes: 32 x 8 pixels and a halo of
+// R pixels.  Entries outside the image carry material -2, which matches no
+// pixel, so taps need no bounds test.
+constexpr int kSTX = 32, kSTY = 8;
 
-// Variance: temporal moments when the history is long enough, else a 7x7
-// edge-stopped spatial estimate.
-__global__ void k_s_variance(StdArgs a) {
+// Variance: temporal moments when the history is long enough (>= 4 frames),
+// else a 7 x 7 edge-stopped spatial estimate (normal and depth weights) on a
+// shared-memory tile with a halo of 3.
+__global__ void __launch_bounds__(256) k_s_variance(StdArgs a) {
+    constexpr int R = 3, SX = kSTX + 2 * R, SY = kSTY + 2 * R;
+    __shared__ float4 s_nd[SY * SX];
+    __shared__ float2 s_mo[SY * SX];
+    __shared__ int s_m[SY * SX];
     const int W = a.W, H = a.H;
-    FOR_PIXELS(W * H) {
-        const float4 nr = a.nrm[p];
-        if (__float_as_int(nr.w) < 0) continue;
-        const float len = a.hist[p].w;
-        float var;
-        if (len >= 4.0f) {
-            const float2 m = a.mom[p];
-            var = fmaxf(0.0f, m.y - m.x * m.x);
-        } else {
-            const int x = p % W, y = p / W;
-            const float d = a.pos[p].w;
-            const int mat = __float_as_int(a.alb[p].w);
-            const float gx = (x + 1 < W ? a.pos[p + 1].w : d) - (x > 0 ? a.pos[p - 1].w : d);
-            const float gy = (y + 1 < H ? a.pos[p + W].w : d) - (y > 0 ? a.pos[p - W].w : d);
-            const float grad = 0.5f * fmaxf(fabsf(gx), fabsf(gy));
-            float s1 = 0, s2 = 0, sw = 0;
-            for (int ky = -3; ky <= 3; ++ky)
-                for (int kx = -3; kx <= 3; ++kx) {
-                    const int qx = x + kx, qy = y + ky;
-                    if (qx < 0 || qx >= W || qy < 0 || qy >= H) continue;
-                    const int q = W * qy + qx;
-                    const float4 qn = a.nrm[q];
-                    if (__float_as_int(qn.w) < 0 || __float_as_int(a.alb[q].w) != mat) continue;
-                    const float w = depth_weight_std(d, a.pos[q].w, grad, sqrtf((float)(kx * kx + ky * ky)), a.sz) *
-                                    normal_weight(dot3(f3(nr), f3(qn)), a.sn, a.sn_log2);
-                    const float2 m = a.mom[q];
-                    s1 += w * m.x;
-                    s2 += w * m.y;
-                    sw += w;
-                }
-            var = sw > 0.0f ? fmaxf(0.0f, s2 / sw - (s1 / sw) * (s1 / sw)) : 0.0f;
-            var *= 4.0f / len;  // boost for short histories
-        }
-        a.col[p].w = var;
-    }
-}
-
-__global__ void k_s_gauss_var(StdArgs a, const float4 *col) {
-    const int W = a.W, H = a.H;
-    FOR_PIXELS(W * H) {
-        const int x = p % W, y = p / W;
-        float s = 0, w = 0;
-        for (int ky = -1; ky <= 1; ++ky)
-            for (int kx = -1; kx <= 1; ++kx) {
-                const int qx = x + kx, qy = y + ky;
-                if (qx < 0 || qx >= W || qy < 0 || qy >= H) continue;
-                const float k = cKG[kx + 1] * cKG[ky + 1];
-                s += k * col[W * qy + qx].w;
-                w += k;
-            }
-        a.gvar[p] = s / w;
-    }
-}
-
-__global__ void k_s_atrous(StdArgs a, const float4 *__restrict__ in, float4 *out, int step) {
-    const int W = a.W, H = a.H;
-    FOR_PIXELS(W * H) {
-        const float4 nr = a.nrm[p];
-        const float4 c = in[p];
-        if (__float_as_int(nr.w) < 0) {
-            out[p] = c;
-            continue;
-        }
-        const int x = p % W, y = p / W;
-        const float d = a.pos[p].w;
-        const int mat = __float_as_int(a.alb[p].w);
-        const float gx = (x + 1 < W ? a.pos[p + 1].w : d) - (x > 0 ? a.pos[p - 1].w : d);
-        const float gy = (y + 1 < H ? a.pos[p + W].w : d) - (y > 0 ? a.pos[p - W].w : d);
-        const float grad = 0.5f * fmaxf(fabsf(gx), fabsf(gy));
-        const float l = lumf(f3(c));
-        const float sdl = a.sl * sqrtf(fmaxf(a.gvar[p], 0.0f)) + 1e-6f;
-        float3 sc = f3(c) * (36.0f / 256.0f);
-        float sv = (36.0f / 256.0f) * (36.0f / 256.0f) * c.w;
-        float sw = 36.0f / 256.0f;
-        for (int ki = 0; ki < 25; ++ki) {
-            if (ki == 12) continue;
-            const int ox = ki % 5 - 2, oy = ki / 5 - 2;
-            const int qx = x + ox * step, qy = y + oy * step;
-            if (qx < 0 || qx >= W || qy < 0 || qy >= H) continue;
-            const int q = W * qy + qx;
-            const float4 qn = a.nrm[q];
-            if (__float_as_int(qn.w) < 0 || __float_as_int(a.alb[q].w) != mat) continue;
-            const float4 qc = in[q];
-            const float dist = (float)step * sqrtf((float)(ox * ox + oy * oy));
-            const float wz = depth_weight_std(d, a.pos[q].w, grad, dist, a.sz);
-            const float wn = normal_weight(dot3(f3(nr), f3(qn)), a.sn, a.sn_log2);
-            const float wl = __expf(-fabsf(l - lumf(f3(qc))) / sdl);
-            const float w = cKW[ki] * wz * wn * wl;
-            sc += f3(qc) * w;
-            sv += w * w * qc.w;
-            sw += w;
-        }
-        out[p] = make_float4(sc.x / sw, sc.y / sw, sc.z / sw, sv / (sw * sw));
-    }
-}
-
-// The a-trous pass for the small steps (1, 2, 4) on shared-memory tiles: a
-// block stages its 32 x 8 pixels and a halo of 2 * step (the 5 x 5 taps at
-// that step, the 3 x 3 variance blur and the depth gradient all fall inside)
-// - normal and depth, material id (-1: no hit, -2: outside the image),
-// colour and variance - then filters from shared memory with the 3 x 3
-// variance blur of k_s_gauss_var computed in place.  Same arithmetic, in the
-// same order, as k_s_gauss_var + k_s_atrous, so the result is the same.
-template <int kStep>
-__global__ void __launch_bounds__(256) k_s_atrous_tile(StdArgs a, const float4 *__restrict__ in, float4 *out) {
-    constexpr int TX = 32, TY = 8, R = 2 * kStep, SX = TX + 2 * R, SY = TY + 2 * R;
-    __shared__ float4 s_nd[SY][SX];  // normal, depth
-    __shared__ float4 s_c[SY][SX];   // colour, variance
-    __shared__ int s_m[SY][SX];      // material id, -1 no hit, -2 outside
-    const int W = a.W, H = a.H;
-    const int x0 = blockIdx.x * TX - R, y0 = blockIdx.y * TY - R;
-    for (int i = threadIdx.y * TX + threadIdx.x; i < SX * SY; i += TX * TY) {
-        const int sx = i % SX, sy = i / SX, gx = x0 + sx, gy = y0 + sy;
+    const int x0 = blockIdx.x * kSTX - R, y0 = blockIdx.y * kSTY - R;
+    for (int i = threadIdx.y * kSTX + threadIdx.x; i < SX * SY; i += kSTX * kSTY) {
+        const int gx = x0 + i % SX, gy = y0 + i / SX;
         if (gx >= 0 && gx < W && gy >= 0 && gy < H) {
             const int q = W * gy + gx;
-            const float4 nr = a.nrm[q];
-            s_nd[sy][sx] = make_float4(nr.x, nr.y, nr.z, a.pos[q].w);
-            s_c[sy][sx] = in[q];
-            s_m[sy][sx] = __float_as_int(nr.w) < 0 ? -1 : max(__float_as_int(a.alb[q].w), 0);
+            s_nd[i] = a.nd[q];
+            s_mo[i] = a.mom[q];
+            s_m[i] = a.mat[q];
         } else {
-            s_nd[sy][sx] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-            s_c[sy][sx] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-            s_m[sy][sx] = -2;
+            s_m[i] = -2;
         }
     }
     __syncthreads();
-    const int x = blockIdx.x * TX + threadIdx.x, y = blockIdx.y * TY + threadIdx.y;
+    const int x = blockIdx.x * kSTX + threadIdx.x, y = blockIdx.y * kSTY + threadIdx.y;
     if (x >= W || y >= H) return;
-    const int p = W * y + x, cx = threadIdx.x + R, cy = threadIdx.y + R;
-    const float4 c = s_c[cy][cx];
-    const int mat = s_m[cy][cx];
-    if (mat < 0) {
-        out[p] = c;
-        return;
+    const int p = W * y + x, c = SX * (threadIdx.y + R) + threadIdx.x + R;
+    const int mat = s_m[c];
+    if (mat < 0) return;
+    // sigma_z |grad d|: central differences of the depth (one-sided at the
+    // border), kept for the a-trous passes
+    const float4 nd = s_nd[c];
+    const float d = nd.w;
+    const float gx = (x + 1 < W ? s_nd[c + 1].w : d) - (x > 0 ? s_nd[c - 1].w : d);
+    const float gy = (y + 1 < H ? s_nd[c + SX].w : d) - (y > 0 ? s_nd[c - SX].w : d);
+    const float kz = a.sz * 0.5f * fmaxf(fabsf(gx), fabsf(gy));
+    a.gz[p] = kz;
+    const float len = a.hist[p].w;
+    float var;
+    if (len >= 4.0f) {
+        const float2 m = s_mo[c];
+        var = fmaxf(0.0f, m.y - m.x * m.x);
+    } else {
+        // rz for the 10 distinct squared distances of a 7 x 7 window
+        constexpr int kD2[10] = {0, 1, 2, 4, 5, 8, 9, 10, 13, 18};
+        float rz[10];
+#pragma unroll
+        for (int k = 0; k < 10; ++k) rz[k] = kLog2e / (kz * sqrtf((float)kD2[k]) + 1e-3f);
+        float s1 = 0, s2 = 0, sw = 0;
+#pragma unroll
+        for (int ky = -3; ky <= 3; ++ky)
+#pragma unroll
+            for (int kx = -3; kx <= 3; ++kx) {
+                const int t = c + SX * ky + kx;
+                if (s_m[t] != mat) continue;
+                const int d2 = kx * kx + ky * ky;
+                const int cls = d2 == 0 ? 0 : d2 == 1 ? 1 : d2 == 2 ? 2 : d2 == 4 ? 3 : d2 == 5 ? 4 : d2 == 8 ? 5
+                              : d2 == 9 ? 6 : d2 == 10 ? 7 : d2 == 13 ? 8 : 9;
+                const float4 qn = s_nd[t];
+                const float e = a.sn * lg2a(fmaxf(0.0f, dot3(f3(nd), f3(qn)))) - fabsf(d - qn.w) * rz[cls];
+                const float w = ex2a(e);
+                const float2 m = s_mo[t];
+                s1 += w * m.x;
+                s2 += w * m.y;
+                sw += w;
+            }
+        var = sw > 0.0f ? fmaxf(0.0f, s2 / sw - (s1 / sw) * (s1 / sw)) : 0.0f;
+        var *= 4.0f / len;  // boost for short histories
     }
-    // k_s_gauss_var's 3 x 3 blur of the variance over the pixels in the image
+    a.col[p].w = var;
+}
+
+// k_s_gauss_var's 3 x 3 blur of the variance over the pixels in the image,
+// read from global memory around pixel p = (x, y).
+__device__ __forceinline__ float gauss_var_global(const float4 *__restrict__ in, int W, int H, int x, int y) {
     float gs = 0, gw = 0;
+#pragma unroll
     for (int ky = -1; ky <= 1; ++ky)
+#pragma unroll
         for (int kx = -1; kx <= 1; ++kx) {
-            if (s_m[cy + ky][cx + kx] == -2) continue;
+            if (x + kx < 0 || x + kx >= W || y + ky < 0 || y + ky >= H) continue;
             const float k = cKG[kx + 1] * cKG[ky + 1];
-            gs += k * s_c[cy + ky][cx + kx].w;
+            gs += k * in[W * (y + ky) + x + kx].w;
             gw += k;
         }
-    const float gvar = gs / gw;
-    const float4 nd = s_nd[cy][cx];
+    return gs / gw;
+}
+
+// One a-trous pass of pixel p at `step` over colour + variance, given the
+// 3 x 3-blurred variance gvar.  Reads go through Src: a shared-memory tile
+// (k_s_atrous_tile), staged rows (k_s_atrous_rows) or the global arrays
+// (k_s_atrous).
+template <class Src>
+__device__ __forceinline__ float4 std_atrous_px(const StdArgs &a, const Src &S, int p, int step, float gvar) {
+    const float4 c = S.c(0, 0);
+    const int mat = S.m(0, 0);
+    const float4 nd = S.nd(0, 0);
     const float d = nd.w;
-    const float gx = (x + 1 < W ? s_nd[cy][cx + 1].w : d) - (x > 0 ? s_nd[cy][cx - 1].w : d);
-    const float gy = (y + 1 < H ? s_nd[cy + 1][cx].w : d) - (y > 0 ? s_nd[cy - 1][cx].w : d);
-    const float grad = 0.5f * fmaxf(fabsf(gx), fabsf(gy));
+    const float kz = a.gz[p] * (float)step;
     const float l = lumf(f3(c));
-    const float sdl = a.sl * sqrtf(fmaxf(gvar, 0.0f)) + 1e-6f;
+    const float rl = kLog2e / (a.sl * sqrtf(fmaxf(gvar, 0.0f)) + 1e-6f);
+    // rz for the squared tap distances 1, 2, 4, 5, 8 (in steps)
+    float rz[5];
+    constexpr int kD2[5] = {1, 2, 4, 5, 8};
+#pragma unroll
+    for (int k = 0; k < 5; ++k) rz[k] = kLog2e / (kz * sqrtf((float)kD2[k]) + 1e-3f);
     float3 sc = f3(c) * (36.0f / 256.0f);
     float sv = (36.0f / 256.0f) * (36.0f / 256.0f) * c.w;
     float sw = 36.0f / 256.0f;
 #pragma unroll
     for (int ki = 0; ki < 25; ++ki) {
         if (ki == 12) continue;
-        const int ox = ki % 5 - 2, oy = ki / 5 - 2;
-        const int qy = cy + oy * kStep, qx = cx + ox * kStep;
-        const int qm = s_m[qy][qx];
-        if (qm != mat) continue;  // outside, no hit or another material
-        const float4 qn = s_nd[qy][qx];
-        const float4 qc = s_c[qy][qx];
-        const float dist = (float)kStep * sqrtf((float)(ox * ox + oy * oy));
-        const float wz = depth_weight_std(d, qn.w, grad, dist, a.sz);
-        const float wn = normal_weight(dot3(f3(nd), f3(qn)), a.sn, a.sn_log2);
-        const float wl = __expf(-fabsf(l - lumf(f3(qc))) / sdl);
-        const float w = cKW[ki] * wz * wn * wl;
+        const int ox = (ki % 5 - 2) * step, oy = (ki / 5 - 2) * step;
+        if (!S.inside(ox, oy)) continue;
+        if (S.m(ox, oy) != mat) continue;  // no hit, another material, or outside a tile's image
+        const float4 qn = S.nd(ox, oy);
+        const float4 qc = S.c(ox, oy);
+        const int d2 = (ki % 5 - 2) * (ki % 5 - 2) + (ki / 5 - 2) * (ki / 5 - 2);
+        const int cls = d2 == 1 ? 0 : d2 == 2 ? 1 : d2 == 4 ? 2 : d2 == 5 ? 3 : 4;
+        const float e = a.sn * lg2a(fmaxf(0.0f, dot3(f3(nd), f3(qn)))) - fabsf(d - qn.w) * rz[cls] -
+                        fabsf(l - lumf(f3(qc))) * rl;
+        const float w = cKW[ki] * ex2a(e);
         sc += f3(qc) * w;
         sv += w * w * qc.w;
         sw += w;
     }
-    out[p] = make_float4(sc.x / sw, sc.y / sw, sc.z / sw, sv / (sw * sw));
+    return make_float4(sc.x / sw, sc.y / sw, sc.z / sw, sv / (sw * sw));
 }
 
-__global__ void k_s_feedback(StdArgs a, const float4 *filtered) {
-    FOR_PIXELS(a.W * a.H) {
-        if (__float_as_int(a.nrm[p].w) < 0) continue;
-        const float4 f = filtered[p];
-        a.hist[p].x = f.x;
-        a.hist[p].y = f.y;
-        a.hist[p].z = f.z;
+// The small steps (1, 2, 4) on shared-memory tiles with a halo of 2 * step:
+// guide (normal, depth), material and colour + variance.  The first pass
+// (kFeedback) also writes its colour back into the history, which the next
+// frame integrates.
+template <int kStep, bool kFeedback>
+__global__ void __launch_bounds__(256) k_s_atrous_tile(StdArgs a, const float4 *__restrict__ in, float4 *out) {
+    constexpr int R = 2 * kStep, SX = kSTX + 2 * R, SY = kSTY + 2 * R;
+    __shared__ float4 s_nd[SY * SX];
+    __shared__ float4 s_c[SY * SX];
+    __shared__ int s_m[SY * SX];
+    const int W = a.W, H = a.H;
+    const int x0 = blockIdx.x * kSTX - R, y0 = blockIdx.y * kSTY - R;
+    for (int i = threadIdx.y * kSTX + threadIdx.x; i < SX * SY; i += kSTX * kSTY) {
+        const int gx = x0 + i % SX, gy = y0 + i / SX;
+        if (gx >= 0 && gx < W && gy >= 0 && gy < H) {
+            const int q = W * gy + gx;
+            s_nd[i] = a.nd[q];
+            s_c[i] = in[q];
+            s_m[i] = a.mat[q];
+        } else {
+            s_m[i] = -2;
+        }
+    }
+    __syncthreads();
+    const int x = blockIdx.x * kSTX + threadIdx.x, y = blockIdx.y * kSTY + threadIdx.y;
+    if (x >= W || y >= H) return;
+    struct {
+        const float4 *snd, *sc;
+        const int *sm;
+        int o;  // this pixel's entry
+        __device__ bool inside(int ox, int oy) const { return sm[o + SX * oy + ox] != -2; }
+        __device__ int m(int ox, int oy) const { return sm[o + SX * oy + ox]; }
+        __device__ float4 nd(int ox, int oy) const { return snd[o + SX * oy + ox]; }
+        __device__ float4 c(int ox, int oy) const { return sc[o + SX * oy + ox]; }
+    } S{s_nd, s_c, s_m, SX * ((int)threadIdx.y + R) + (int)threadIdx.x + R};
+    const int p = W * y + x;
+    if (s_m[S.o] < 0) {
+        out[p] = s_c[S.o];
+        return;
+    }
+    // k_s_gauss_var's 3 x 3 blur of the variance over the pixels in the image
+    float gs = 0, gw = 0;
+#pragma unroll
+    for (int ky = -1; ky <= 1; ++ky)
+#pragma unroll
+        for (int kx = -1; kx <= 1; ++kx) {
+            if (!S.inside(kx, ky)) continue;
+            const float k = cKG[kx + 1] * cKG[ky + 1];
+            gs += k * S.c(kx, ky).w;
+            gw += k;
+        }
+    const float4 o = std_atrous_px(a, S, p, kStep, gs / gw);
+    out[p] = o;
+    if (kFeedback) {
+        const float len = a.hist[p].w;
+        a.hist[p] = make_float4(o.x, o.y, o.z, len);
+    }
+}
+
+// The large steps (8 and 16) on row segments: a block of 256 threads takes
+// 256 pixels of one row and stages the five rows its taps read (y + {-2, -1,
+// 0, 1, 2} step, 256 + 4 step entries each); the variance blur's neighbours
+// come from global memory (coalesced: consecutive threads, consecutive
+// pixels).
+template <int kStep> struct SRows {
+    static constexpr int T = 256, R = 2 * kStep, SX = T + 2 * R, N = 5 * SX;
+    static constexpr size_t kSmem = (size_t)N * (2 * sizeof(float4) + sizeof(int));
+};
+
+template <int kStep>
+__global__ void __launch_bounds__(256) k_s_atrous_rows(StdArgs a, const float4 *__restrict__ in, float4 *out) {
+    using T = SRows<kStep>;
+    extern __shared__ __align__(16) unsigned char smem[];
+    float4 *s_nd = (float4 *)smem;
+    float4 *s_c = s_nd + T::N;
+    int *s_m = (int *)(s_c + T::N);
+    const int W = a.W, H = a.H, y = blockIdx.y;
+    const int x0 = blockIdx.x * T::T - T::R;
+    for (int i = threadIdx.x; i < T::N; i += T::T) {
+        const int gx = x0 + i % T::SX, gy = y + (i / T::SX - 2) * kStep;
+        if (gx >= 0 && gx < W && gy >= 0 && gy < H) {
+            const int q = W * gy + gx;
+            s_nd[i] = a.nd[q];
+            s_c[i] = in[q];
+            s_m[i] = a.mat[q];
+        } else {
+            s_m[i] = -2;
+        }
+    }
+    __syncthreads();
+    const int x = blockIdx.x * T::T + threadIdx.x;
+    if (x >= W) return;
+    struct {
+        const float4 *snd, *sc;
+        const int *sm;
+        int o;  // this pixel's entry
+        __device__ int at(int ox, int oy) const { return o + T::SX * (oy / kStep) + ox; }
+        __device__ bool inside(int ox, int oy) const { return sm[at(ox, oy)] != -2; }
+        __device__ int m(int ox, int oy) const { return sm[at(ox, oy)]; }
+        __device__ float4 nd(int ox, int oy) const { return snd[at(ox, oy)]; }
+        __device__ float4 c(int ox, int oy) const { return sc[at(ox, oy)]; }
+    } S{s_nd, s_c, s_m, 2 * T::SX + (int)threadIdx.x + T::R};
+    const int p = W * y + x;
+    if (s_m[S.o] < 0) {
+        out[p] = s_c[S.o];
+        return;
+    }
+    out[p] = std_atrous_px(a, S, p, kStep, gauss_var_global(in, W, H, x, y));
+}
+
+// Steps of 32 and more (more than five a-trous passes): taps read global
+// memory (through L1 and L2).  kStep = 0: the step is `step`.
+template <int kStep>
+__global__ void k_s_atrous(StdArgs a, const float4 *__restrict__ in, float4 *out, int step) {
+    const int W = a.W, H = a.H;
+    FOR_PIXELS(W * H) {
+        const int x = p % W, y = p / W;
+        struct {
+            const float4 *gnd, *gc;
+            const int *gm;
+            int p, x, y, W, H;
+            __device__ bool inside(int ox, int oy) const {
+                return x + ox >= 0 && x + ox < W && y + oy >= 0 && y + oy < H;
+            }
+            __device__ int m(int ox, int oy) const { return gm[p + W * oy + ox]; }
+            __device__ float4 nd(int ox, int oy) const { return gnd[p + W * oy + ox]; }
+            __device__ float4 c(int ox, int oy) const { return gc[p + W * oy + ox]; }
+        } S{a.nd, in, a.mat, p, x, y, W, H};
+        if (a.mat[p] < 0) {
+            out[p] = in[p];
+            continue;
+        }
+        out[p] = std_atrous_px(a, S, p, kStep ? kStep : step, gauss_var_global(in, W, H, x, y));
     }
 }
 
@@ -800,27 +1113,16 @@ __global__ void k_s_feedback(StdArgs a, const float4 *filtered) {
 __global__ void k_s_output(StdArgs a, const float4 *filtered, float4 *out, uchar4 *rgba8,
                            const __grid_constant__ ToneTable T) {
     FOR_PIXELS(a.W * a.H) {
-        const float4 nr = a.nrm[p];
         const float4 c = filtered[p];
         float4 o;
-        if (__float_as_int(nr.w) < 0) {
+        if (a.mat[p] < 0) {
             o = make_float4(c.x, c.y, c.z, 1.0f);
         } else {
             const float3 al = f3(a.alb[p]) + f3(kS, kS, kS);
-            const float3 e = f3(a.emi[p]);
-            o = make_float4(c.x * al.x + 0.0f * e.x, c.y * al.y, c.z * al.z, 1.0f);
+            o = make_float4(c.x * al.x, c.y * al.y, c.z * al.z, 1.0f);
         }
         if (out) out[p] = o;
         if (rgba8) rgba8[p] = tone_rgba8(o, T);
-    }
-}
-
-__global__ void k_s_save_prev(StdArgs a) {
-    FOR_PIXELS(a.W * a.H) {
-        const float4 nr = a.nrm[p];
-        const int obj = __float_as_int(nr.w);
-        a.nd_prev[p] = make_float4(nr.x, nr.y, nr.z, a.pos[p].w);
-        a.mat_prev[p] = obj < 0 ? -1 : __float_as_int(a.alb[p].w);
     }
 }
 
@@ -833,8 +1135,8 @@ template <class T> kgk_status realloc_d(T **p, size_t n, const char *what) {
 }  // namespace
 
 void svgf_state_free_impl(SvgfState *S) {
-    void *ptrs[] = {S->prev, S->cur, S->hist, S->hist_prev, S->mom, S->mom_prev, S->nd_prev, S->mat_prev,
-                    S->col, S->tmp, S->gvar};
+    void *ptrs[] = {S->prev, S->cur, S->hist, S->hist_prev, S->mom, S->mom_prev, S->nd, S->nd_prev,
+                    S->mat, S->mat_prev, S->gz, S->col, S->tmp, S->compat_scratch};
     for (void *p : ptrs) dfree(p);
 }
 
@@ -961,8 +1263,7 @@ kgk_status kgk_gbuffer_records(kgk_scene *s, kgk_svgf_buffer *out) {
         KGK_TRY(s->staging.reserve(npx * sizeof(kgk_svgf_buffer)));
         dst = (kgk_svgf_buffer *)s->staging.ptr;
     }
-    const int g = (int)std::min<size_t>((npx + 255) / 256, 65535);
-    k_gbuffer_to_records<<<g, 256, 0, st>>>(gpos, gnrm, galb, gemi, (int)npx, dst);
+    k_gbuffer_to_records<<<(unsigned)((npx + 255) / 256), 256, 0, st>>>(gpos, gnrm, galb, gemi, npx, dst);
     KGK_CUDA(cudaGetLastError());
     if (!dev) KGK_CUDA(cudaMemcpyAsync(out, dst, npx * sizeof(kgk_svgf_buffer), cudaMemcpyDeviceToHost, st));
     KGK_CUDA(cudaStreamSynchronize(st));
@@ -999,11 +1300,14 @@ kgk_status kgk_svgf_output(kgk_scene *s, const kgk_svgf_config *cfg, const kgk_v
         KGK_TRY(dalloc(&S.hist_prev, npx, "SVGF history"));
         KGK_TRY(dalloc(&S.mom, npx, "SVGF moments"));
         KGK_TRY(dalloc(&S.mom_prev, npx, "SVGF moments"));
+        KGK_TRY(dalloc(&S.nd, npx, "SVGF guide"));
         KGK_TRY(dalloc(&S.nd_prev, npx, "SVGF history"));
+        KGK_TRY(dalloc(&S.mat, npx, "SVGF guide"));
         KGK_TRY(dalloc(&S.mat_prev, npx, "SVGF history"));
+        KGK_TRY(dalloc(&S.gz, npx, "SVGF guide"));
         KGK_TRY(dalloc(&S.col, npx, "SVGF colour"));
         KGK_TRY(dalloc(&S.tmp, npx, "SVGF colour"));
-        KGK_TRY(dalloc(&S.gvar, npx, "SVGF variance"));
+        KGK_TRY(dalloc(&S.compat_scratch, compat_scratch_bytes(npx), "SVGF scratch"));
         KGK_CUDA(cudaMemset(S.prev, 0, npx * sizeof(kgk_svgf_buffer)));
         S.W = W;
         S.H = H;
@@ -1044,13 +1348,14 @@ kgk_status kgk_svgf_output(kgk_scene *s, const kgk_svgf_config *cfg, const kgk_v
     }
     const int g = (int)std::min<size_t>((npx + 255) / 256, 65535);
     if (cfg->mode == KGK_SVGF_COMPAT) {
-        k_gbuffer_to_records<<<g, 256, 0, st>>>(gpos, gnrm, galb, gemi, (int)npx, S.cur);
+        k_gbuffer_to_records<<<(unsigned)((npx + 255) / 256), 256, 0, st>>>(gpos, gnrm, galb, gemi, npx, S.cur);
         // result buffer: the noisy frame (copied, the reference rewrites it)
         float4 *R = S.col;
         KGK_CUDA(cudaMemcpyAsync(R, in, npx * sizeof(float4), cudaMemcpyDeviceToDevice, st));
         const int reps = cfg->atrous_repeats > 0 ? cfg->atrous_repeats : 5;
         const int stages = cfg->atrous_iterations > 0 ? cfg->atrous_iterations : 5;
-        KGK_TRY(run_compat((kgk_vec *)R, (kgk_vec *)out, S.prev, S.cur, W, H, cfg->frame_index, reps, stages, st));
+        KGK_TRY(run_compat((kgk_vec *)R, (kgk_vec *)out, S.prev, S.cur, W, H, cfg->frame_index, reps, stages, st,
+                           S.compat_scratch));
         // main.cu:232: the current buffer becomes the previous one
         KGK_CUDA(cudaMemcpyAsync(S.prev, S.cur, npx * sizeof(kgk_svgf_buffer), cudaMemcpyDeviceToDevice, st));
         if (out8) KGK_TRY(tonemap_device(out, npx, out8, st));
@@ -1059,38 +1364,40 @@ kgk_status kgk_svgf_output(kgk_scene *s, const kgk_svgf_config *cfg, const kgk_v
         StdArgs a;
         a.W = W; a.H = H; a.pos = gpos; a.nrm = gnrm; a.alb = galb; a.emi = gemi; a.noisy = in;
         a.hist = S.hist; a.hist_prev = S.hist_prev; a.mom = S.mom; a.mom_prev = S.mom_prev;
-        a.nd_prev = S.nd_prev; a.mat_prev = S.mat_prev; a.col = S.col; a.tmp = S.tmp; a.gvar = S.gvar;
+        a.nd = S.nd; a.nd_prev = S.nd_prev; a.mat = S.mat; a.mat_prev = S.mat_prev;
+        a.gz = S.gz; a.col = S.col; a.tmp = S.tmp;
         a.pcam = S.prev_cam;
         a.has_prev = S.has_prev ? 1 : 0;
         a.alpha = cfg->alpha > 0.0f ? cfg->alpha : 0.2f;
         a.sz = cfg->sigma_z > 0.0f ? cfg->sigma_z : 1.0f;
         a.sn = cfg->sigma_n > 0.0f ? cfg->sigma_n : 128.0f;
-        a.sn_log2 = -1;
-        for (int k = 0; k <= 16; ++k)
-            if (a.sn == (float)(1 << k)) a.sn_log2 = k;
         a.sl = cfg->sigma_l > 0.0f ? cfg->sigma_l : 4.0f;
+        const dim3 tiles((W + kSTX - 1) / kSTX, (H + kSTY - 1) / kSTY), tile_threads(kSTX, kSTY);
+        const dim3 rows((W + 255) / 256, H);
+        KGK_CUDA(cudaFuncSetAttribute(k_s_atrous_rows<8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)SRows<8>::kSmem));
+        KGK_CUDA(cudaFuncSetAttribute(k_s_atrous_rows<16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)SRows<16>::kSmem));
         k_s_temporal<<<g, 256, 0, st>>>(a);
-        k_s_variance<<<g, 256, 0, st>>>(a);
+        k_s_variance<<<tiles, tile_threads, 0, st>>>(a);
         const int iters = cfg->atrous_iterations > 0 ? cfg->atrous_iterations : 5;
         float4 *src = S.col, *dst = S.tmp;
-        const dim3 tiles((W + 31) / 32, (H + 7) / 8), tile_threads(32, 8);
         for (int i = 0; i < iters; ++i) {
-            if (i == 0) {
-                k_s_atrous_tile<1><<<tiles, tile_threads, 0, st>>>(a, src, dst);
-            } else if (i == 1) {
-                k_s_atrous_tile<2><<<tiles, tile_threads, 0, st>>>(a, src, dst);
-            } else if (i == 2) {
-                k_s_atrous_tile<4><<<tiles, tile_threads, 0, st>>>(a, src, dst);
-            } else {
-                k_s_gauss_var<<<g, 256, 0, st>>>(a, src);
-                k_s_atrous<<<g, 256, 0, st>>>(a, src, dst, 1 << i);
+            switch (i) {
+                case 0: k_s_atrous_tile<1, true><<<tiles, tile_threads, 0, st>>>(a, src, dst); break;
+                case 1: k_s_atrous_tile<2, false><<<tiles, tile_threads, 0, st>>>(a, src, dst); break;
+                case 2: k_s_atrous_tile<4, false><<<tiles, tile_threads, 0, st>>>(a, src, dst); break;
+                case 3: k_s_atrous_rows<8><<<rows, 256, SRows<8>::kSmem, st>>>(a, src, dst); break;
+                case 4: k_s_atrous_rows<16><<<rows, 256, SRows<16>::kSmem, st>>>(a, src, dst); break;
+                default: k_s_atrous<0><<<g, 256, 0, st>>>(a, src, dst, 1 << std::min(i, 24)); break;
             }
-            if (i == 0) k_s_feedback<<<g, 256, 0, st>>>(a, dst);
             std::swap(src, dst);
         }
         k_s_output<<<g, 256, 0, st>>>(a, src, filtered ? out : nullptr, out8, tone_table());
-        k_s_save_prev<<<g, 256, 0, st>>>(a);
         KGK_CUDA(cudaGetLastError());
+        // this frame's guide is the next frame's previous one
+        std::swap(S.nd, S.nd_prev);
+        std::swap(S.mat, S.mat_prev);
         std::swap(S.hist, S.hist_prev);
         std::swap(S.mom, S.mom_prev);
         S.prev_cam = cam;
@@ -1144,7 +1451,7 @@ void kgk_host_free(void *p) {
 // must not allocate because cudaMalloc / cudaFree synchronise the whole device
 // and stall the caller's other streams.  This entry point takes its scratch
 // from g_svgf_scratch, a file-scope device array sized for
-// KGK_SVGF_NOALLOC_MAX_PIXELS pixels (57 B per pixel, ~15 MB); every GPU that
+// KGK_SVGF_NOALLOC_MAX_PIXELS pixels (113 B per pixel, ~30 MB); every GPU that
 // loads the library holds that array until the process exits.
 // ---------------------------------------------------------------------------
 #include <mutex>

@@ -349,22 +349,43 @@ def icosphere_field(n_meshes=64, subdiv=6, seed=2, box=20.0, amplitude=0.05,
 def value_noise2(x, y, seed, octaves=3, base_freq=4.0):
     """2D value noise over arrays x, y in [0, 1): `octaves` bilinear octaves
     (freq base_freq * 2^k, amplitude 0.5^k), smoothstep-interpolated,
-    normalised to [-1, 1]."""
-    total = np.zeros(np.broadcast(x, y).shape)
+    normalised to [-1, 1].  The lattice points' hashes are computed once and
+    gathered; on a grid (x constant down columns, y along rows) the x
+    interpolation runs once per lattice row - the same operations on the same
+    values, so the same result."""
+    x, y = np.broadcast_arrays(np.asarray(x, np.float64), np.asarray(y, np.float64))
+    grid = x.ndim == 2 and bool((x == x[:1]).all()) and bool((y == y[:, :1]).all())
+    total = np.zeros(x.shape)
     norm = 0.0
     for k in range(octaves):
         freq = base_freq * (2 ** k)
         amp = 0.5 ** k
-        qx, qy = x * freq + 1000.0, y * freq + 1000.0
+        qx, qy = (x[0], y[:, 0]) if grid else (x, y)
+        qx, qy = qx * freq + 1000.0, qy * freq + 1000.0
         ix, iy = np.floor(qx).astype(np.int64), np.floor(qy).astype(np.int64)
         fx, fy = qx - ix, qy - iy
         fx, fy = fx * fx * (3.0 - 2.0 * fx), fy * fy * (3.0 - 2.0 * fy)
-        z = np.zeros_like(ix)
-        h00 = _lattice_hash(ix, iy, z, seed * 131 + k)
-        h10 = _lattice_hash(ix + 1, iy, z, seed * 131 + k)
-        h01 = _lattice_hash(ix, iy + 1, z, seed * 131 + k)
-        h11 = _lattice_hash(ix + 1, iy + 1, z, seed * 131 + k)
-        total += amp * ((h00 * (1 - fx) + h10 * fx) * (1 - fy) + (h01 * (1 - fx) + h11 * fx) * fy)
+        x0, y0 = int(ix.min()), int(iy.min())
+        nx, ny = int(ix.max()) - x0 + 2, int(iy.max()) - y0 + 2
+        if grid:
+            gy, gx = np.mgrid[y0:y0 + ny, x0:x0 + nx]
+            T = _lattice_hash(gx, gy, np.zeros_like(gx), seed * 131 + k)
+            jx, jy = ix - x0, iy - y0
+            B = T[:, jx] * (1 - fx) + T[:, jx + 1] * fx  # lattice rows interpolated in x
+            total += amp * (B[jy] * (1 - fy)[:, None] + B[jy + 1] * fy[:, None])
+        else:
+            if nx * ny <= ix.size:
+                gy, gx = np.mgrid[y0:y0 + ny, x0:x0 + nx]
+                T = _lattice_hash(gx, gy, np.zeros_like(gx), seed * 131 + k)
+                jx, jy = ix - x0, iy - y0
+                h00, h10, h01, h11 = T[jy, jx], T[jy, jx + 1], T[jy + 1, jx], T[jy + 1, jx + 1]
+            else:
+                z = np.zeros_like(ix)
+                h00 = _lattice_hash(ix, iy, z, seed * 131 + k)
+                h10 = _lattice_hash(ix + 1, iy, z, seed * 131 + k)
+                h01 = _lattice_hash(ix, iy + 1, z, seed * 131 + k)
+                h11 = _lattice_hash(ix + 1, iy + 1, z, seed * 131 + k)
+            total += amp * ((h00 * (1 - fx) + h10 * fx) * (1 - fy) + (h01 * (1 - fx) + h11 * fx) * fy)
         norm += amp
     return total / norm
 

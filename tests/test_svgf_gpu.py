@@ -127,3 +127,45 @@ def test_svgf_standard_reduces_error_over_an_orbit():
     # and the history never makes a later frame worse than the first
     assert all(f < 0.5 * n for f, n in zip(errs_filt, errs_noisy)), (errs_noisy, errs_filt)
     assert max(errs_filt[2:]) <= 1.5 * errs_filt[0], errs_filt
+
+
+@pytest.mark.parametrize("W,H", [(72, 56), (70, 53)])
+def test_svgf_standard_matches_restatement(W, H):
+    """kgk_svgf (standard) pixel by pixel against its numpy restatement
+    (tests/svgf_standard_ref.py) over six frames of a still camera: frame 0
+    runs the 7 x 7 spatial variance everywhere, frames 4 and 5 the temporal
+    moments; tile edges fall inside the image (W not a multiple of 32, H of
+    8 in the second case).  The frames come from the compat estimator, whose
+    primary rays pass through the pixel centres (the unbiased one jitters
+    them), so the G-buffer is the same every frame and each pixel reprojects
+    onto itself, as the restatement assumes.  The device's weights use ex2 / lg2
+    approximations (~2^-22 relative, x sigma_n = 128 in the exponent), so a
+    pixel agrees within 2e-3 relative; where the blurred variance is tiny the
+    luminance weight's exponent |l - lq| / sigma_l sqrt(var) magnifies FP32
+    rounding of l, so up to 2 % of pixels may leave that bound."""
+    from svgf_standard_ref import StandardSVGF
+    tris, mats, c = scenes.cornell_box()
+    ref = StandardSVGF(W, H)
+    cam = camera_setup(c["origin"], c["dist"], c["rot"], H)
+    cfg = KgkSvgfConfig(mode=1, width=W, height=H, frame_index=0, atrous_iterations=5, alpha=0.2,
+                        sigma_z=1.0, sigma_n=128.0, sigma_l=4.0)
+    worst = 1.0
+    with Scene(tris, mats) as s:
+        s.build_bvh()
+        for f in range(6):
+            noisy, _ = s.render(cam, W, H, spp=1, estimator=ESTIMATOR_COMPAT, frame_index=f, write_gbuffer=True)
+            recs = s.gbuffer_records(W, H)
+            cfg.frame_index = f
+            out = np.empty_like(noisy)
+            check(lib().kgk_svgf(s._h, ctypes.byref(cfg), _p(noisy), _p(out)))
+            n = recs["Normal"][:, :3].reshape(H, W, 3)
+            alb = recs["Albedo"][:, :3].reshape(H, W, 3)
+            mat = np.where(recs["ObjectID"] >= 0, np.maximum(recs["MaterialID"], 0), -1).reshape(H, W)
+            exp = ref.frame(noisy[..., :3], n, recs["Depth"].reshape(H, W), mat, alb)
+            got = out[..., :3].astype(np.float64)
+            rel = np.abs(got - exp) / np.maximum(np.abs(exp), 1e-3)
+            ok = (rel <= 2e-3).all(-1)
+            worst = min(worst, float(ok.mean()))
+            assert np.isfinite(got).all()
+            assert ok.mean() > 0.98, (f, ok.mean(), float(rel.max()))
+    print(f"standard SVGF {W}x{H} x 6 frames vs restatement: worst frame within 2e-3", worst)
