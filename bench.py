@@ -241,7 +241,7 @@ def run_ours(args):
         except Exception as e:  # the throughput line is still printed
             study = {"error": f"{type(e).__name__}: {e}"}
     probes = None
-    if rank == 0:
+    if rank == 0 and not args.no_probes:
         try:
             probes = config_probes(scene, W, H)
         except Exception as e:  # the throughput line is still printed
@@ -908,20 +908,40 @@ def run_c4(args):
     evals = (19, 39, 59)
     scene = Scene(tris, mats, env=env)
     scene.build_bvh()
+    import ctypes
+    import torch
+    from kagayaki_gb300._lib import check, lib
+    from kagayaki_gb300.structs import KgkSvgfConfig
     kw = dict(max_depth=WORKLOAD["max_depth"], estimator=ESTIMATOR_UNBIASED)
     out = np.empty((H, W, 4), np.float32)
     imgs = {}
     times = {}
+    # temporal reuse of the cached frames: the standard filter's reprojection
+    # and history alone (KGK_SVGF_TEMPORAL) on each cached frame, timed apart
+    cfg_t = KgkSvgfConfig(mode=2, width=W, height=H, frame_index=0, alpha=0.2)
+    noisy_dev = torch.empty((H, W, 4), dtype=torch.float32, device="cuda")
+    filt_dev = torch.empty_like(noisy_dev)
+    temporal_s = []
     for mode in ("plain", "cache"):
         if mode == "cache":
             scene.cache_init(seed=1)
         dev = 0.0
         for f in range(frames):
             img, st = scene.render(orbit_camera(f, H), W, H, spp=1, seed=3, frame_index=f, use_cache=mode == "cache",
-                                   out=out, **kw)
+                                   out=out, write_gbuffer=mode == "cache", **kw)
             dev += st["ms_device"]
             if f in evals:
                 imgs[(mode, f)] = img[..., :3].astype(np.float64)
+            if mode == "cache":
+                noisy_dev.copy_(torch.from_numpy(out))
+                torch.cuda.synchronize()
+                cfg_t.frame_index = f
+                t0 = time.perf_counter()
+                check(lib().kgk_svgf_output(scene._h, ctypes.byref(cfg_t), ctypes.c_void_p(noisy_dev.data_ptr()),
+                                            ctypes.c_void_p(filt_dev.data_ptr()), None, 0))
+                temporal_s.append(time.perf_counter() - t0)
+                if f in evals:
+                    imgs[("cache_temporal", f)] = filt_dev[..., :3].cpu().numpy().astype(np.float64)
         times[mode] = dev / frames
     res = []
     for f in evals:
@@ -934,6 +954,7 @@ def run_c4(args):
         eq, _ = scene.render(cam, W, H, spp=spp_eq, seed=9, frame_index=800_000 + f, out=out, **kw)
         res.append({"frame": f + 1, "plain_1spp": round(rel_mse(imgs[("plain", f)], ref), 4),
                     "cache_1spp": round(rel_mse(imgs[("cache", f)], ref), 4),
+                    "cache_1spp_temporal_reuse": round(rel_mse(imgs[("cache_temporal", f)], ref), 4),
                     "plain_equal_time": round(rel_mse(eq[..., :3].astype(np.float64), ref), 4),
                     "plain_equal_time_spp": spp_eq})
     scene.close()
@@ -942,6 +963,9 @@ def run_c4(args):
             "scaling": "weak", "vs_baseline": None, "dtype": "f32 (cache MLP bf16)", "data": "synthetic seeded scene",
             "config": {"workload": "cache-orbit-1080p-1spp", "frames": frames, "cache": "width 64, 65,536 training paths"},
             "plain_frames_per_s": round(1e3 / times["plain"], 2),
+            "temporal_reuse_ms": {"value": round(1e3 * float(np.median(temporal_s[3:])), 3),
+                                  "what": "kgk_svgf mode 2 (reprojection + history, no spatial pass) on the "
+                                          "cached frame: wall clock of the synchronous call, device buffers"},
             "relmse": res}
     print(json.dumps(line), flush=True)
 
@@ -1065,6 +1089,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU baseline work budget")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
     ap.add_argument("--no-relmse", action="store_true", help="skip the plain-vs-cache relMSE study")
+    ap.add_argument("--no-probes", action="store_true", help="skip the C3 / C4 / C5 probes of the default run")
     ap.add_argument("--wave-paths", type=int, default=0, help="paths per wave (0 = the library default)")
     ap.add_argument("--workload", default="frame",
                     choices=["frame", "c1", "svgf-orbit", "c4", "mlp", "c5", "trace"],

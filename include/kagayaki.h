@@ -343,7 +343,15 @@ typedef enum kgk_svgf_mode {
     KGK_SVGF_COMPAT = 0,
     /* Standard SVGF: working reprojection from the previous camera, temporal
      * alpha, n a-trous iterations with edge-stopping sigmas. */
-    KGK_SVGF_STANDARD = 1
+    KGK_SVGF_STANDARD = 1,
+    /* Temporal reuse alone: the standard filter's reprojection and history
+     * (alpha) with no spatial pass - for frames that are already smooth, such
+     * as those the radiance cache terminates into.  A sample whose
+     * demodulated luminance exceeds 4x the brightest of its eight neighbours
+     * (1e-3 added) is scaled down to that bound before it enters the
+     * history, and the reprojected history is clamped, per channel, to the
+     * range of the current 3x3 neighbourhood (pixels that hit). */
+    KGK_SVGF_TEMPORAL = 2
 } kgk_svgf_mode;
 
 typedef struct kgk_svgf_config {

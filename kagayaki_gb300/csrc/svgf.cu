@@ -12,6 +12,9 @@
 //   spatial variance fallback, `atrous_iterations` edge-stopping a-trous
 //   passes (sigma_z, sigma_n, sigma_l) on albedo-demodulated lighting, the
 //   first pass feeding the next frame's history.
+// temporal: the standard filter's reprojection and history alone, with
+//   isolated outlier samples clamped before they enter the history and the
+//   history clamped to the colour box of the current 3 x 3 neighbourhood.
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -722,6 +725,7 @@ struct StdArgs {
     float4 *col, *tmp;
     kgk_camera pcam;
     int has_prev;
+    int firefly;                           // clamp isolated samples before they enter the history
     float alpha, sz, sn, sl;
 };
 
@@ -740,6 +744,8 @@ __device__ __forceinline__ bool project_prev(const kgk_camera &c, int W, int H, 
     y = H / 2.0f - dot3(v, sy) * k / (c.PixelSize * dot3(sy, sy));
     return true;
 }
+
+constexpr float kFirefly = 4.0f;
 
 // Temporal integration; also writes this frame's guide (normal + depth,
 // material id) that the spatial passes read and the next frame reprojects
@@ -764,8 +770,40 @@ __global__ void k_s_temporal(StdArgs a) {
         a.nd[p] = make_float4(nr.x, nr.y, nr.z, ps.w);
         a.mat[p] = mat;
         const float3 albedo = f3(al);
-        const float3 dl = div3(noisy, albedo + f3(kS, kS, kS));
-        const float l = lumf(dl);
+        float3 dl = div3(noisy, albedo + f3(kS, kS, kS));
+        float l = lumf(dl);
+        // temporal mode: the colour box of the 3 x 3 neighbourhood (pixels
+        // that hit) that the reprojected history is clamped to
+        float3 bmin = f3(0.0f, 0.0f, 0.0f), bmax = f3(0.0f, 0.0f, 0.0f);
+        if (a.firefly) {
+            // an isolated sample more than kFirefly times as bright as the
+            // brightest of its eight neighbours (that hit) is scaled down to
+            // that bound before it enters the history, where alpha = 0.2
+            // would carry it for tens of frames
+            const int x = p % W, y = p / W;
+            float lmax = 0.0f;
+            bool any = false;
+            bmin = f3(3.0e38f, 3.0e38f, 3.0e38f);
+            bmax = f3(-3.0e38f, -3.0e38f, -3.0e38f);
+            for (int k = 0; k < 9; ++k) {
+                const int qx = x + k % 3 - 1, qy = y + k / 3 - 1;
+                if (k == 4 || qx < 0 || qx >= W || qy < 0 || qy >= H) continue;
+                const int q = W * qy + qx;
+                if (__float_as_int(a.nrm[q].w) < 0) continue;
+                any = true;
+                const float3 dq = div3(f3(a.noisy[q]), f3(a.alb[q]) + f3(kS, kS, kS));
+                lmax = fmaxf(lmax, lumf(dq));
+                bmin = f3(fminf(bmin.x, dq.x), fminf(bmin.y, dq.y), fminf(bmin.z, dq.z));
+                bmax = f3(fmaxf(bmax.x, dq.x), fmaxf(bmax.y, dq.y), fmaxf(bmax.z, dq.z));
+            }
+            const float cap = kFirefly * lmax + 1e-3f;
+            if (any && l > cap) {
+                dl = dl * (cap / l);
+                l = cap;
+            }
+            bmin = f3(fminf(bmin.x, dl.x), fminf(bmin.y, dl.y), fminf(bmin.z, dl.z));
+            bmax = f3(fmaxf(bmax.x, dl.x), fmaxf(bmax.y, dl.y), fmaxf(bmax.z, dl.z));
+        }
         float3 hc = f3(0.0f, 0.0f, 0.0f);
         float2 hm = make_float2(0.0f, 0.0f);
         float hl = 0.0f, wsum = 0.0f;
@@ -803,6 +841,9 @@ __global__ void k_s_temporal(StdArgs a) {
         float len;
         if (wsum > 1e-4f) {
             hc = hc / wsum;
+            if (a.firefly)  // history outside the current neighbourhood's box is stale (ghosting)
+                hc = f3(fminf(fmaxf(hc.x, bmin.x), bmax.x), fminf(fmaxf(hc.y, bmin.y), bmax.y),
+                        fminf(fmaxf(hc.z, bmin.z), bmax.z));
             hm.x /= wsum;
             hm.y /= wsum;
             len = fminf(hl / wsum + 1.0f, 64.0f);
@@ -1359,7 +1400,7 @@ kgk_status kgk_svgf_output(kgk_scene *s, const kgk_svgf_config *cfg, const kgk_v
         // main.cu:232: the current buffer becomes the previous one
         KGK_CUDA(cudaMemcpyAsync(S.prev, S.cur, npx * sizeof(kgk_svgf_buffer), cudaMemcpyDeviceToDevice, st));
         if (out8) KGK_TRY(tonemap_device(out, npx, out8, st));
-    } else if (cfg->mode == KGK_SVGF_STANDARD) {
+    } else if (cfg->mode == KGK_SVGF_STANDARD || cfg->mode == KGK_SVGF_TEMPORAL) {
         if (cfg->frame_index == 0) S.has_prev = false;
         StdArgs a;
         a.W = W; a.H = H; a.pos = gpos; a.nrm = gnrm; a.alb = galb; a.emi = gemi; a.noisy = in;
@@ -1368,6 +1409,7 @@ kgk_status kgk_svgf_output(kgk_scene *s, const kgk_svgf_config *cfg, const kgk_v
         a.gz = S.gz; a.col = S.col; a.tmp = S.tmp;
         a.pcam = S.prev_cam;
         a.has_prev = S.has_prev ? 1 : 0;
+        a.firefly = cfg->mode == KGK_SVGF_TEMPORAL ? 1 : 0;
         a.alpha = cfg->alpha > 0.0f ? cfg->alpha : 0.2f;
         a.sz = cfg->sigma_z > 0.0f ? cfg->sigma_z : 1.0f;
         a.sn = cfg->sigma_n > 0.0f ? cfg->sigma_n : 128.0f;
@@ -1379,8 +1421,8 @@ kgk_status kgk_svgf_output(kgk_scene *s, const kgk_svgf_config *cfg, const kgk_v
         KGK_CUDA(cudaFuncSetAttribute(k_s_atrous_rows<16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)SRows<16>::kSmem));
         k_s_temporal<<<g, 256, 0, st>>>(a);
-        k_s_variance<<<tiles, tile_threads, 0, st>>>(a);
-        const int iters = cfg->atrous_iterations > 0 ? cfg->atrous_iterations : 5;
+        const int iters = cfg->mode == KGK_SVGF_TEMPORAL ? 0 : cfg->atrous_iterations > 0 ? cfg->atrous_iterations : 5;
+        if (iters > 0) k_s_variance<<<tiles, tile_threads, 0, st>>>(a);
         float4 *src = S.col, *dst = S.tmp;
         for (int i = 0; i < iters; ++i) {
             switch (i) {

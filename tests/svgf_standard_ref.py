@@ -16,6 +16,7 @@ import numpy as np
 
 KS = 1e-4
 LOG2E = 1.4426950408889634
+FIREFLY = 4.0
 KG = np.array([0.25, 0.5, 0.25])
 KW1 = np.array([1, 4, 6, 4, 1]) / 16.0
 
@@ -52,9 +53,10 @@ def depth_gradient(d, sz, step):
 
 
 class StandardSVGF:
-    def __init__(self, W, H, alpha=0.2, sz=1.0, sn=128.0, sl=4.0, iterations=5):
+    def __init__(self, W, H, alpha=0.2, sz=1.0, sn=128.0, sl=4.0, iterations=5, firefly=False):
         self.W, self.H = W, H
         self.alpha, self.sz, self.sn, self.sl, self.iters = alpha, sz, sn, sl, iterations
+        self.firefly = firefly  # the temporal mode's outlier clamp
         self.prev = None  # (hist, mom, normal, depth, mat)
 
     def frame(self, noisy, normal, depth, mat, albedo):
@@ -65,6 +67,35 @@ class StandardSVGF:
         hit = mat >= 0
         dl = noisy / (albedo + KS)
         l = lum(dl)
+        if self.firefly:
+            # 4x the brightest of the eight neighbours that hit (+ 1e-3)
+            lmax = np.zeros((H, W))
+            anyn = np.zeros((H, W), bool)
+            for oy in (-1, 0, 1):
+                for ox in (-1, 0, 1):
+                    if ox == 0 and oy == 0:
+                        continue
+                    qh = shifted(hit, ox, oy, False)
+                    ql = shifted(l, ox, oy, 0.0)
+                    lmax = np.where(qh, np.maximum(lmax, ql), lmax)
+                    anyn |= qh
+            cap = FIREFLY * lmax + 1e-3
+            clamp = hit & anyn & (l > cap)
+            scale = np.where(clamp, cap / np.where(clamp, l, 1.0), 1.0)
+            dl0 = dl
+            dl = dl * scale[..., None]
+            l = np.where(clamp, cap, l)
+            # the 3 x 3 colour box (neighbours that hit, unclamped; the pixel
+            # itself clamped) that the history is clamped to
+            bmin, bmax = dl.copy(), dl.copy()
+            for oy in (-1, 0, 1):
+                for ox in (-1, 0, 1):
+                    if ox == 0 and oy == 0:
+                        continue
+                    qh = shifted(hit, ox, oy, False)[..., None]
+                    qd = shifted(dl0, ox, oy, 0.0)
+                    bmin = np.where(qh, np.minimum(bmin, qd), bmin)
+                    bmax = np.where(qh, np.maximum(bmax, qd), bmax)
         hist = np.zeros((H, W, 4))
         mom = np.zeros((H, W, 2))
         c = dl.copy()
@@ -75,7 +106,8 @@ class StandardSVGF:
             ok = hit & (pmat == mat) & ((pn * normal).sum(-1) >= 0.9) & (np.abs(pd - depth) <= 0.05 * depth + 1e-3)
             length = np.where(ok, np.minimum(ph[..., 3] + 1.0, 64.0), 1.0)
             ac = np.maximum(self.alpha, 1.0 / length)
-            c = np.where(ok[..., None], ph[..., :3] * (1 - ac[..., None]) + dl * ac[..., None], dl)
+            hc = np.clip(ph[..., :3], bmin, bmax) if self.firefly else ph[..., :3]
+            c = np.where(ok[..., None], hc * (1 - ac[..., None]) + dl * ac[..., None], dl)
             m = np.where(ok[..., None], np.stack([pm[..., 0] * (1 - ac) + l * ac, pm[..., 1] * (1 - ac) + l * l * ac], -1),
                          m)
         hist[..., :3] = np.where(hit[..., None], c, noisy)

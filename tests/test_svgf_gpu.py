@@ -129,8 +129,8 @@ def test_svgf_standard_reduces_error_over_an_orbit():
     assert max(errs_filt[2:]) <= 1.5 * errs_filt[0], errs_filt
 
 
-@pytest.mark.parametrize("W,H", [(72, 56), (70, 53)])
-def test_svgf_standard_matches_restatement(W, H):
+@pytest.mark.parametrize("W,H,mode", [(72, 56, 1), (70, 53, 1), (70, 53, 2)])
+def test_svgf_standard_matches_restatement(W, H, mode):
     """kgk_svgf (standard) pixel by pixel against its numpy restatement
     (tests/svgf_standard_ref.py) over six frames of a still camera: frame 0
     runs the 7 x 7 spatial variance everywhere, frames 4 and 5 the temporal
@@ -142,12 +142,14 @@ def test_svgf_standard_matches_restatement(W, H):
     approximations (~2^-22 relative, x sigma_n = 128 in the exponent), so a
     pixel agrees within 2e-3 relative; where the blurred variance is tiny the
     luminance weight's exponent |l - lq| / sigma_l sqrt(var) magnifies FP32
-    rounding of l, so up to 2 % of pixels may leave that bound."""
+    rounding of l, so up to 2 % of pixels may leave that bound.  mode 2
+    (KGK_SVGF_TEMPORAL) is the same reprojection and history with no spatial
+    pass, and isolated outliers clamped before they enter the history."""
     from svgf_standard_ref import StandardSVGF
     tris, mats, c = scenes.cornell_box()
-    ref = StandardSVGF(W, H)
+    ref = StandardSVGF(W, H, iterations=5 if mode == 1 else 0, firefly=mode == 2)
     cam = camera_setup(c["origin"], c["dist"], c["rot"], H)
-    cfg = KgkSvgfConfig(mode=1, width=W, height=H, frame_index=0, atrous_iterations=5, alpha=0.2,
+    cfg = KgkSvgfConfig(mode=mode, width=W, height=H, frame_index=0, atrous_iterations=5, alpha=0.2,
                         sigma_z=1.0, sigma_n=128.0, sigma_l=4.0)
     worst = 1.0
     with Scene(tris, mats) as s:
@@ -168,4 +170,4 @@ def test_svgf_standard_matches_restatement(W, H):
             worst = min(worst, float(ok.mean()))
             assert np.isfinite(got).all()
             assert ok.mean() > 0.98, (f, ok.mean(), float(rel.max()))
-    print(f"standard SVGF {W}x{H} x 6 frames vs restatement: worst frame within 2e-3", worst)
+    print(f"SVGF mode {mode} {W}x{H} x 6 frames vs restatement: worst frame within 2e-3", worst)
