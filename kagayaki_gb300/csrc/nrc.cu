@@ -122,9 +122,15 @@ struct Tc {
     static constexpr uint32_t kSlotOff = kBarOff + 8 * kGroups;
     static constexpr uint32_t kSmemBytes = kSlotOff + 8 + 1024;     // + room to align the base to 1024 B
     static constexpr uint32_t kTmemCols = (uint32_t)W * kGroups;    // a W-column accumulator per warpgroup
+    // inference: two accumulators per warpgroup when a layer has two K
+    // sub-tiles, so the next layer's MMAs on the first sub-tile run while the
+    // second is converted
+    static constexpr int kAccBufs = kKSubs > 1 ? 2 : 1;
+    static constexpr uint32_t kInferTmemCols = kTmemCols * kAccBufs;
     static_assert(kAOff % 1024 == 0, "swizzle atoms need 1024-byte alignment");
     static_assert(kSmemBytes <= 227 * 1024, "shared memory per CTA");
     static_assert(kTmemCols * kCtasPerSm <= 512, "tensor memory per SM");
+    static_assert(kInferTmemCols * kCtasPerSm <= 512, "tensor memory per SM (inference)");
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -270,7 +276,7 @@ __global__ void __launch_bounds__(128 * tc::Tc<W>::kGroups) k_infer_tc(const uns
     }
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(s0 + T::kSlotOff),
-                     "r"(T::kTmemCols)
+                     "r"(T::kInferTmemCols)
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
@@ -278,7 +284,8 @@ __global__ void __launch_bounds__(128 * tc::Tc<W>::kGroups) k_infer_tc(const uns
     fence_before();
     __syncthreads();
     fence_after();
-    const uint32_t tmem = *reinterpret_cast<volatile uint32_t *>(sm + T::kSlotOff) + (uint32_t)W * (uint32_t)g;
+    constexpr uint32_t kGroupCols = (uint32_t)W * T::kAccBufs;
+    const uint32_t tmem = *reinterpret_cast<volatile uint32_t *>(sm + T::kSlotOff) + kGroupCols * (uint32_t)g;
     const uint32_t trow = tmem + ((uint32_t)((warp & 3) * 32) << 16);  // this warp's 32 TMEM lanes
     const int total = n_dev ? min(*n_dev, n) : n;
     uint32_t phase = 0;
@@ -306,24 +313,30 @@ __global__ void __launch_bounds__(128 * tc::Tc<W>::kGroups) k_infer_tc(const uns
             }
         }
         float y[3] = {0.0f, 0.0f, 0.0f};
-        for (int l = 0; l <= kLayers; ++l) {
+        // the MMAs of layer l on K sub-tile h (k-steps 4h .. 4h + 3) into the
+        // layer's accumulator; issued by row 0 once the sub-tile is written
+        auto issue = [&](int l, int h) {
             const bool last = l == kLayers;
-            fence_async_smem();
-            fence_before();
-            wg_sync(wgbar);
-            if (r == 0) {
-                fence_after();
-                const int nk = Net<W>::in(l) / 16;
-                const uint32_t boff = last ? T::kOutOff : T::layer_off(l);
-                const uint32_t bsub = last ? kOutSub : T::kWSub;
-                const uint32_t id = last ? idesc_bf16(128, 16) : idesc_bf16(128, W);
-                for (int kk = 0; kk < nk; ++kk) {
-                    const uint32_t j = (uint32_t)kk >> 2, o = 2u * (uint32_t)(kk & 3);  // sub-tile, 32 B steps
-                    mma_bf16(tmem, sw128_desc(a_addr + j * kSub) + o, sw128_desc(s0 + boff + j * bsub) + o, id,
-                             kk > 0 ? 1u : 0u);
-                }
-                commit(bar);
+            const uint32_t boff = last ? T::kOutOff : T::layer_off(l);
+            const uint32_t bsub = last ? kOutSub : T::kWSub;
+            const uint32_t id = last ? idesc_bf16(128, 16) : idesc_bf16(128, W);
+            const uint32_t d = tmem + (uint32_t)W * (uint32_t)(l % T::kAccBufs);
+            const int nk = Net<W>::in(l) / 16;
+            for (int kk = 4 * h; kk < nk && kk < 4 * h + 4; ++kk) {
+                const uint32_t j = (uint32_t)kk >> 2, o = 2u * (uint32_t)(kk & 3);  // sub-tile, 32 B steps
+                mma_bf16(d, sw128_desc(a_addr + j * kSub) + o, sw128_desc(s0 + boff + j * bsub) + o, id,
+                         kk > 0 ? 1u : 0u);
             }
+        };
+        fence_async_smem();
+        fence_before();
+        wg_sync(wgbar);
+        if (r == 0) {
+            fence_after();
+            issue(0, 0);
+            commit(bar);
+        }
+        for (int l = 0; l <= kLayers; ++l) {
             const bool ok = bar_wait(bar, phase);
             phase ^= 1u;
             if (wg_sync_or(wgbar, !ok)) {
@@ -331,32 +344,53 @@ __global__ void __launch_bounds__(128 * tc::Tc<W>::kGroups) k_infer_tc(const uns
                 break;
             }
             fence_after();
-            if (!last) {
-#pragma unroll
-                for (int cb = 0; cb < W / 16; ++cb) {  // 16 columns = two 16-byte chunks of BF16
-                    float v[16];
-                    tmem_ld16(trow + 16 * cb, v);
-                    tmem_wait_ld();
-                    uint4 lo, hi;
-                    lo.x = pack2_relu(v[0], v[1]);
-                    lo.y = pack2_relu(v[2], v[3]);
-                    lo.z = pack2_relu(v[4], v[5]);
-                    lo.w = pack2_relu(v[6], v[7]);
-                    hi.x = pack2_relu(v[8], v[9]);
-                    hi.y = pack2_relu(v[10], v[11]);
-                    hi.z = pack2_relu(v[12], v[13]);
-                    hi.w = pack2_relu(v[14], v[15]);
-                    unsigned char *At = A + (uint32_t)(cb >> 2) * kSub;
-                    *reinterpret_cast<uint4 *>(At + sw_off(r, (2 * cb) & 7)) = lo;
-                    *reinterpret_cast<uint4 *>(At + sw_off(r, (2 * cb + 1) & 7)) = hi;
-                }
-            } else {
+            const uint32_t acc = trow + (uint32_t)W * (uint32_t)(l % T::kAccBufs);
+            if (l == kLayers) {
                 float v[16];
-                tmem_ld16(trow, v);
+                tmem_ld16(acc, v);
                 tmem_wait_ld();
                 y[0] = v[0];
                 y[1] = v[1];
                 y[2] = v[2];
+                break;
+            }
+            // tensor-memory loads per wait: four at width 128; one at width
+            // 64, whose two CTAs per SM leave 64 registers a thread
+            constexpr int kLd = W == 64 ? 1 : 4;
+#pragma unroll
+            for (int h = 0; h < (int)T::kKSubs; ++h) {  // 64-column K sub-tiles of H_{l+1}
+                unsigned char *At = A + (uint32_t)h * kSub;
+#pragma unroll
+                for (int c0 = 0; c0 < 4; c0 += kLd) {
+                    float v[kLd][16];
+#pragma unroll
+                    for (int c = 0; c < kLd; ++c) tmem_ld16(acc + 64 * h + 16 * (c0 + c), v[c]);
+                    tmem_wait_ld();
+#pragma unroll
+                    for (int c = 0; c < kLd; ++c) {
+                        uint4 lo, hi;
+                        lo.x = pack2_relu(v[c][0], v[c][1]);
+                        lo.y = pack2_relu(v[c][2], v[c][3]);
+                        lo.z = pack2_relu(v[c][4], v[c][5]);
+                        lo.w = pack2_relu(v[c][6], v[c][7]);
+                        hi.x = pack2_relu(v[c][8], v[c][9]);
+                        hi.y = pack2_relu(v[c][10], v[c][11]);
+                        hi.z = pack2_relu(v[c][12], v[c][13]);
+                        hi.w = pack2_relu(v[c][14], v[c][15]);
+                        *reinterpret_cast<uint4 *>(At + sw_off(r, 2 * (c0 + c))) = lo;
+                        *reinterpret_cast<uint4 *>(At + sw_off(r, 2 * (c0 + c) + 1)) = hi;
+                    }
+                }
+                // sub-tile h of H_{l+1} is written: layer l + 1's MMAs on it
+                // start while the next sub-tile is converted
+                fence_async_smem();
+                fence_before();
+                wg_sync(wgbar);
+                if (r == 0) {
+                    fence_after();
+                    issue(l + 1, h);
+                    if (h == (int)T::kKSubs - 1) commit(bar);
+                }
             }
         }
         if (failed) break;
@@ -388,8 +422,8 @@ __global__ void __launch_bounds__(128 * tc::Tc<W>::kGroups) k_infer_tc(const uns
     __syncthreads();
     if (warp == 0) {
         fence_after();
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem - (uint32_t)W * (uint32_t)g),
-                     "r"(T::kTmemCols)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem - kGroupCols * (uint32_t)g),
+                     "r"(T::kInferTmemCols)
                      : "memory");
     }
 }
