@@ -14,8 +14,8 @@
 //      <= log2(kSmall) deep; node ids come from a per-task reserved range, so
 //      the tree is deterministic;
 //   4. collapse: breadth first, every wide node opens the largest-area inner
-//      child until it has 8 children; children with <= 3 triangles become leaf
-//      children; slots are ordered by octant so traversal visits near
+//      child until it has 8 children; children with at most 1 (large scenes)
+//      or 3 (small ones) triangles become leaf children; slots are ordered by octant so traversal visits near
 //      children first; child boxes are quantised to 8 bits against the parent
 //      box (conservative rounding).
 // Every kernel bounds-checks its writes and raises an error flag instead of
@@ -35,7 +35,17 @@ namespace {
 constexpr int kBins = 32;
 constexpr int kChunk = 4096;   // primitives per block in the large-task path
 constexpr int kSmall = 2048;   // tasks up to this size build inside one block
-constexpr int kMaxLeaf = 3;    // triangles per leaf child of a wide node
+// Triangles per leaf child of a wide node, chosen per scene (bvh_build).
+// One for large scenes: a wide node's leaf children then hold a triangle
+// each, so its quantised child box culls that triangle alone, and a node
+// yields at most 8 triangle tests.  Measured on the C2 frame (5.2M
+// triangles): 3089 Mrays/s at 1, 2978 at 2, 2799 at 3 (extend 43.5 / 46.0 /
+// 50.3 ms), for 1.72M / 1.00M / 0.71M wide nodes and a 140 / 87 / 65 ms
+// build.  Three for small scenes, whose nodes and triangles stay in cache:
+// the 36-triangle Cornell box (C1) runs 1509 Mrays/s at 3, 1156 at 1.
+constexpr int kMaxLeaf = 3;                // the largest leaf the node format holds (8 x 3 = 24 bits)
+constexpr int kLeafLarge = 1;
+constexpr int kLargeSceneTris = 1 << 16;   // scenes above this use kLeafLarge
 constexpr int kThreads = 256;
 constexpr int kBinInts = 13;   // count, box lo/hi, centroid lo/hi (ordered ints)
 constexpr int kStack = 32;
@@ -408,7 +418,7 @@ __global__ void __launch_bounds__(kThreads) k_small_build(const Task *tasks, con
                                                           const float4 *__restrict__ plo,
                                                           const float4 *__restrict__ phi, int *ref,
                                                           BinNode *nodes, int *bfirst, int *bcount,
-                                                          int cap, int *err) {
+                                                          int cap, int max_leaf, int *err) {
     __shared__ int sref[kSmall];
     __shared__ int stmp[kSmall];
     __shared__ int bins[3 * kBins * kBinInts];
@@ -456,7 +466,7 @@ __global__ void __launch_bounds__(kThreads) k_small_build(const Task *tasks, con
             bfirst[e.node] = tk.begin + e.b;
             bcount[e.node] = e.c;
         }
-        if (e.c <= kMaxLeaf) {
+        if (e.c <= max_leaf) {
             if (threadIdx.x == 0) {
                 nodes[e.node].lo.w = __int_as_float(tk.begin + e.b);
                 nodes[e.node].hi.w = __int_as_float(-e.c);
@@ -606,7 +616,7 @@ __device__ __forceinline__ bool bn_leaf(const BinNode &n) { return __float_as_in
 
 __global__ void k_collapse_count(const int *tasks, int ntasks, const BinNode *nodes,
                                  const int *bcount, int *child_list, int *n_inner, int *n_tris,
-                                 int cap, int *err) {
+                                 int cap, int max_leaf, int *err) {
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= ntasks) return;
     int b = tasks[t];
@@ -614,7 +624,7 @@ __global__ void k_collapse_count(const int *tasks, int ntasks, const BinNode *no
     int nc = 0;
     if (b < 0 || b >= cap) { raise_err(err, kErrBadChild); return; }
     const BinNode nb = nodes[b];
-    if (bcount[b] <= kMaxLeaf || bn_leaf(nb)) {
+    if (bcount[b] <= max_leaf || bn_leaf(nb)) {
         C[nc++] = b;
     } else {
         C[nc++] = __float_as_int(nb.lo.w);
@@ -625,7 +635,7 @@ __global__ void k_collapse_count(const int *tasks, int ntasks, const BinNode *no
             for (int i = 0; i < nc; ++i) {
                 int c = C[i];
                 if (c < 0 || c >= cap) { raise_err(err, kErrBadChild); return; }
-                if (bcount[c] <= kMaxLeaf) continue;
+                if (bcount[c] <= max_leaf) continue;
                 const BinNode nn = nodes[c];
                 if (bn_leaf(nn)) continue;
                 float a = surface_area(f3(nn.lo), f3(nn.hi));
@@ -644,7 +654,7 @@ __global__ void k_collapse_count(const int *tasks, int ntasks, const BinNode *no
         if (c >= 0) {
             if (c >= cap) { raise_err(err, kErrBadChild); return; }
             int k = bcount[c];
-            if (k <= kMaxLeaf) nt += k;
+            if (k <= max_leaf) nt += k;
             else ni += 1;
         }
     }
@@ -671,7 +681,7 @@ __global__ void k_collapse_emit(const int *tasks, int ntasks, const int *child_l
                                 int next_start, int tri_start, const BinNode *nodes, int cap,
                                 const int *bfirst, const int *bcount, const int *ref,
                                 const float4 *verts, WideNode *wide, int wide_cap, float4 *tri_rec,
-                                int n_tris, int *next_tasks, int next_cap, int *err) {
+                                int n_tris, int *next_tasks, int next_cap, int max_leaf, int *err) {
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= ntasks) return;
     int C[8];
@@ -735,7 +745,7 @@ __global__ void k_collapse_emit(const int *tasks, int ntasks, const int *child_l
         q = ceilf((chi[i].x - plo.x) / sx); while (q < 255.0f && plo.x + q * sx < chi[i].x) q += 1.0f; qhx[s] = (unsigned)fminf(fmaxf(q, 0.0f), 255.0f);
         q = ceilf((chi[i].y - plo.y) / sy); while (q < 255.0f && plo.y + q * sy < chi[i].y) q += 1.0f; qhy[s] = (unsigned)fminf(fmaxf(q, 0.0f), 255.0f);
         q = ceilf((chi[i].z - plo.z) / sz); while (q < 255.0f && plo.z + q * sz < chi[i].z) q += 1.0f; qhz[s] = (unsigned)fminf(fmaxf(q, 0.0f), 255.0f);
-        if (k > kMaxLeaf) {
+        if (k > max_leaf) {
             int wid = child_base + inner_k;
             int pos = inner_scan[t] + inner_k;
             if (pos >= next_cap || wid >= wide_cap) { raise_err(err, kErrWideOverflow); return; }
@@ -864,6 +874,7 @@ struct DevBuf {
 kgk_status bvh_build(DevScene &s, cudaStream_t st, BvhBuildStats *out) {
     const int n = s.n_tris;
     if (n <= 0) return fail(KGK_ERR_INVALID_ARGUMENT, "bvh_build: scene has no triangles");
+    const int max_leaf = n > kLargeSceneTris ? kLeafLarge : kMaxLeaf;
     dfree(s.nodes);
     s.nodes = nullptr;
     dfree(s.tri_rec);
@@ -1049,7 +1060,7 @@ kgk_status bvh_build(DevScene &s, cudaStream_t st, BvhBuildStats *out) {
         KGK_CUDA(cudaMemcpyAsync(d_sb, sb.data(), sizeof(int) * ns, cudaMemcpyHostToDevice, st));
         KGK_CUDA(cudaMemcpyAsync(d_se, se.data(), sizeof(int) * ns, cudaMemcpyHostToDevice, st));
         k_small_build<<<ns, kThreads, 0, st>>>(d_small, d_sb, d_se, ns, plo, phi, ref, nodes, bfirst,
-                                               bcount, cap, err);
+                                               bcount, cap, max_leaf, err);
         KGK_CUDA(cudaGetLastError());
     }
     int herr = 0;
@@ -1083,7 +1094,7 @@ kgk_status bvh_build(DevScene &s, cudaStream_t st, BvhBuildStats *out) {
         ++wlevels;
         const int g = (ntasks + 127) / 128;
         k_collapse_count<<<g, 128, 0, st>>>(tasks_a, ntasks, nodes, bcount, child_list, n_inner, n_tri,
-                                            cap, err);
+                                            cap, max_leaf, err);
         KGK_CUDA(cudaGetLastError());
         KGK_TRY(scan_exclusive(n_inner, inner_scan, ntasks, scan_tmp, tot, st));
         KGK_TRY(scan_exclusive(n_tri, tri_scan, ntasks, scan_tmp, tot + 1, st));
@@ -1105,7 +1116,7 @@ kgk_status bvh_build(DevScene &s, cudaStream_t st, BvhBuildStats *out) {
         k_collapse_emit<<<g, 128, 0, st>>>(tasks_a, ntasks, child_list, inner_scan, tri_scan,
                                            level_start, next_start, tri_start, nodes, cap, bfirst, bcount,
                                            ref, s.verts, wide, wide_cap, tri_rec, n, tasks_b,
-                                           wide_cap, err);
+                                           wide_cap, max_leaf, err);
         KGK_CUDA(cudaGetLastError());
         level_start = next_start;
         tri_start += level_tris;
@@ -1134,7 +1145,7 @@ kgk_status bvh_build(DevScene &s, cudaStream_t st, BvhBuildStats *out) {
         out->n_binary = (uint64_t)node_counter;
         out->n_wide = (uint64_t)s.n_nodes;
         out->max_depth = (uint32_t)wlevels;
-        out->max_leaf = kMaxLeaf;
+        out->max_leaf = max_leaf;
         out->ms = ms;
         out->sah = 0;
     }
