@@ -735,6 +735,19 @@ __device__ __noinline__ float4 bsdf_eval_pdf(const kgk_material *__restrict__ mg
     return make_float4(f.x, f.y, f.z, fmaxf(c, 0.0f) / kPI);
 }
 
+// bsdf_eval_pdf for a material class known at compile time: kMat 1 = Lambert
+// (inline), otherwise the out-of-line evaluation of either class.
+template <int kMat>
+__device__ __forceinline__ float4 bsdf_eval_pdf_k(const kgk_material *__restrict__ mg, float3 diffuse, float3 n,
+                                                  float3 wo, float3 wi) {
+    if (kMat == 1) {
+        const float c = dot3(n, wi);
+        const float3 f = c > 0.0f ? diffuse / kPI : f3(0.0f, 0.0f, 0.0f);
+        return make_float4(f.x, f.y, f.z, fmaxf(c, 0.0f) / kPI);
+    }
+    return bsdf_eval_pdf(mg, diffuse, n, wo, wi);
+}
+
 // Writes a cache record for the surface point of a path: normalised position,
 // shading normal, direction to the viewer, roughness, albedo, then T, the
 // path id and the radiance gathered so far.
@@ -758,7 +771,9 @@ __device__ __forceinline__ void write_cache_record(const Params &P, float *rec, 
 // One unbiased shading event of path ps (hit h): emission, the cache
 // decisions, Russian roulette, the two NEE samples (returned in `out` as
 // shadow-ray records, not traced) and the BSDF sample (ps updated).
-template <bool kCache>
+// kMat: the material class of every path shaded here (1 Lambert, 2 Disney;
+// 0: read from the material).
+template <bool kCache, int kMat = 0>
 __device__ __forceinline__ void shade_unbiased_core(const Params &P, PathState &ps, float4 h, ShadeOut &out) {
     const DevScene &s = P.sc;
     bool cont = false, f_pred = false, e_pred = false;
@@ -856,7 +871,7 @@ __device__ __forceinline__ void shade_unbiased_core(const Params &P, PathState &
                         const float3 Le = emission_of(s.mats[lb & 0x7fffffffu]);
                         const float parea = len3(Le) / s.emit_total;
                         const float pl = parea * dist * dist / cosl;
-                        const float4 fp = bsdf_eval_pdf(&s.mats[S.mat_id], diffuse_of(S.m), n, wo, Ld);
+                        const float4 fp = bsdf_eval_pdf_k<kMat>(&s.mats[S.mat_id], diffuse_of(S.m), n, wo, Ld);
                         const float3 f = f3(fp);
                         const float pb = fp.w;
                         const float wgt = pl / (pl + pb);
@@ -873,7 +888,7 @@ __device__ __forceinline__ void shade_unbiased_core(const Params &P, PathState &
                     const float3 ed = env_sample_u(s, rs, pe, Le);
                     const float coss = dot3(n, ed);
                     if (coss > 0.0f && pe > 0.0f) {
-                        const float4 fp = bsdf_eval_pdf(&s.mats[S.mat_id], diffuse_of(S.m), n, wo, ed);
+                        const float4 fp = bsdf_eval_pdf_k<kMat>(&s.mats[S.mat_id], diffuse_of(S.m), n, wo, ed);
                         const float3 f = f3(fp);
                         const float pb = fp.w;
                         const float wgt = pe / (pe + pb);
@@ -887,7 +902,7 @@ __device__ __forceinline__ void shade_unbiased_core(const Params &P, PathState &
                     float3 u, v, w;
                     onb_ref(n, u, v, w);
                     float3 nd;
-                    if (S.m.MATERIAL_TYPE_ID == 1) {
+                    if (kMat == 2 || (kMat == 0 && S.m.MATERIAL_TYPE_ID == 1)) {
                         const float sw = dp.wt[0] + dp.wt[1] + dp.wt[2] + dp.wt[3] + dp.wt[4];
                         const float rl = rnd_u(rs) * sw, r1 = rnd_u(rs), r2 = rnd_u(rs);
                         const float c3 = dp.wt[0] + dp.wt[1] + dp.wt[2];
@@ -900,7 +915,7 @@ __device__ __forceinline__ void shade_unbiased_core(const Params &P, PathState &
                         const float r1 = rnd_u(rs), r2 = rnd_u(rs);
                         nd = sample_cos_u(r1, r2, u, v, w);
                     }
-                    const float4 fp = bsdf_eval_pdf(&s.mats[S.mat_id], diffuse_of(S.m), n, wo, nd);
+                    const float4 fp = bsdf_eval_pdf_k<kMat>(&s.mats[S.mat_id], diffuse_of(S.m), n, wo, nd);
                     const float3 f = f3(fp);
                     const float pb = fp.w;
                     const float c = dot3(n, nd);
@@ -946,16 +961,21 @@ __device__ __forceinline__ void shade_unbiased_core(const Params &P, PathState &
 // leave their radiance in fin[id].  A shadow record names where its
 // contribution goes: the path's slot in the next buffer (>= 0) or -(id + 1)
 // for fin.
-template <int kEst, bool kCache>
+// kPart: 0 = all three queues in one launch; 1, 2, 3 = the miss, Lambert or
+// Disney queue alone, each launch compiled for its class only (a smaller
+// kernel: the one-launch form spends its time fetching instructions).
+template <int kEst, bool kCache, int kPart = 0>
 __global__ void __launch_bounds__(128) k_shade(Params P, const int *__restrict__ mq, const int *__restrict__ lq,
                                                const int *__restrict__ dq, int next_cnt, float4 *so0, float4 *sd0,
                                                float4 *sc0, float4 *so1, float4 *sd1, float4 *sc1) {
     const int nm = P.cnt[kMQ], nl = P.cnt[kLQ], nd = P.cnt[kDQ];
-    const int n = nm + nl + nd;
+    // this launch's range of the list [misses, Lambert, Disney]
+    const int lo = kPart == 2 ? nm : kPart == 3 ? nm + nl : 0;
+    const int n = kPart == 1 ? nm : kPart == 2 ? nm + nl : nm + nl + nd;
     const bool cache = kCache && P.use_cache;
-    for (int base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+    for (int base = lo + blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
         const int j = base + threadIdx.x;
-        if (j < nm) {  // a miss: the path ends here
+        if (kPart <= 1 && j < nm) {  // a miss: the path ends here
             const int i = mq[j];
             const PathBuf &b = P.cur;
             const float4 d4 = b.d[i];
@@ -965,6 +985,7 @@ __global__ void __launch_bounds__(128) k_shade(Params P, const int *__restrict__
             P.fin[path] = make_float4(rad.x, rad.y, rad.z, 0.0f);
             if (kEst == KGK_ESTIMATOR_COMPAT) P.seeds[path % P.npx] = b.rng[i];  // render.cuh:42
         }
+        if (kPart == 1) continue;
         if (base + (int)blockDim.x <= nm) continue;  // the whole block was misses
         const bool go = j >= nm && j < n;
         PathState ps;
@@ -975,7 +996,7 @@ __global__ void __launch_bounds__(128) k_shade(Params P, const int *__restrict__
             const int i = jh < nl ? lq[jh] : dq[jh - nl];
             ps = load_path(P.cur, i, cache);
             if (kEst == KGK_ESTIMATOR_COMPAT) shade_compat_core(P, ps, P.hit[i], o);
-            else shade_unbiased_core<kCache>(P, ps, P.hit[i], o);
+            else shade_unbiased_core<kCache, kPart == 2 ? 1 : kPart == 3 ? 2 : 0>(P, ps, P.hit[i], o);
         }
         const int k = warp_append(&P.cnt[next_cnt], o.cont);
         if (o.cont) store_path(P.nxt, k, ps, cache);
@@ -1637,10 +1658,18 @@ kgk_status kgk_render(kgk_scene *s, const kgk_camera *cam, const kgk_camera *pre
                 k_shade<KGK_ESTIMATOR_COMPAT, false><<<grid, 128, 0, st>>>(P, R.mq, R.lq, R.dq, nidx, R.sh_o[0],
                                                                          R.sh_d[0], R.sh_c[0], R.sh_o[1], R.sh_d[1],
                                                                          R.sh_c[1]);
-            else  // one instance for both: the cache-free one measured slower (29.6 vs 29.2 ms)
-                k_shade<KGK_ESTIMATOR_UNBIASED, true><<<grid, 128, 0, st>>>(P, R.mq, R.lq, R.dq, nidx, R.sh_o[0],
-                                                                          R.sh_d[0], R.sh_c[0], R.sh_o[1], R.sh_d[1],
-                                                                          R.sh_c[1]);
+            else {  // one instance for both: the cache-free one measured slower (29.6 vs 29.2 ms)
+                k_shade<KGK_ESTIMATOR_UNBIASED, true, 1><<<grid, 128, 0, st>>>(P, R.mq, R.lq, R.dq, nidx, R.sh_o[0],
+                                                                             R.sh_d[0], R.sh_c[0], R.sh_o[1],
+                                                                             R.sh_d[1], R.sh_c[1]);
+                k_shade<KGK_ESTIMATOR_UNBIASED, true, 2><<<grid, 128, 0, st>>>(P, R.mq, R.lq, R.dq, nidx, R.sh_o[0],
+                                                                             R.sh_d[0], R.sh_c[0], R.sh_o[1],
+                                                                             R.sh_d[1], R.sh_c[1]);
+                k_shade<KGK_ESTIMATOR_UNBIASED, true, 3><<<grid, 128, 0, st>>>(P, R.mq, R.lq, R.dq, nidx, R.sh_o[0],
+                                                                             R.sh_d[0], R.sh_c[0], R.sh_o[1],
+                                                                             R.sh_d[1], R.sh_c[1]);
+                launches += 2;
+            }
             KGK_TRY(stage_end());
             KGK_CUDA(cudaEventRecord(R.shaded, st));
             KGK_CUDA(cudaStreamWaitEvent(sh_st, R.shaded, 0));
