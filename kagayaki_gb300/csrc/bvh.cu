@@ -13,9 +13,10 @@
 //      memory, always descending into the smaller child so its stack stays
 //      <= log2(kSmall) deep; node ids come from a per-task reserved range, so
 //      the tree is deterministic;
-//   4. collapse: breadth first, every wide node opens the largest-area inner
-//      child until it has 8 children; children with at most 1 (large scenes)
-//      or 3 (small ones) triangles become leaf children; slots are ordered by octant so traversal visits near
+//   4. collapse: a bottom-up pass fills the SAH cost table of the optimal
+//      collapse (k_dp_up); then breadth first, every wide node takes the 8
+//      children that table chose; children with at most 1 (large scenes) or 3
+//      (small ones) triangles are leaf children; slots are ordered by octant so traversal visits near
 //      children first; child boxes are quantised to 8 bits against the parent
 //      box (conservative rounding).
 // Every kernel bounds-checks its writes and raises an error flag instead of
@@ -614,9 +615,92 @@ __global__ void __launch_bounds__(kThreads) k_small_build(const Task *tasks, con
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ bool bn_leaf(const BinNode &n) { return __float_as_int(n.hi.w) < 0; }
 
+// SAH-optimal choice of each wide node's children (Ylitie, Karras and Laine,
+// "Efficient incoherent ray traversal on GPUs through compressed wide BVHs",
+// HPG 2017, section 3.1).  cost(n, i) is the least SAH cost of the binary
+// subtree at n represented as at most i children of a wide node:
+//   cost(n, 1) = leaf cost if n may be a leaf (at most max_leaf triangles:
+//                c_prim A(n) count), else A(n) c_node + D(n, 8);
+//   cost(n, i) = min(cost(n, i - 1), D(n, i)),
+//   D(n, j)    = min over 0 < k < j of cost(left, k) + cost(right, j - k).
+// The table is filled bottom up, a node by the second of its children to
+// finish; dec[n] keeps the argmin k of D(n, 8) (bits 0-2) and, for j = 2..8,
+// the k of D(n, j) when it beats cost(n, j - 1), else 0 (bits 3(j-1)..).
+constexpr float kCostNode = 1.0f;
+constexpr float kCostTri = 0.3f;
+constexpr float kCostInf = 3.0e38f;
+
+__global__ void k_dp_parents(const BinNode *nodes, int n_nodes, int *parent, int *err) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_nodes) return;
+    const BinNode nd = nodes[i];
+    if (bn_leaf(nd)) return;  // leaves, and slots no task used (filled with -1)
+    const int l = __float_as_int(nd.lo.w), r = __float_as_int(nd.hi.w);
+    if (l <= 0 || l >= n_nodes || r <= 0 || r >= n_nodes) { raise_err(err, kErrBadChild); return; }
+    parent[l] = i;
+    parent[r] = i;
+}
+
+__global__ void k_dp_up(const BinNode *nodes, const int *bcount, const int *parent, int n_nodes, int max_leaf,
+                        float *cost, unsigned *dec, int *visits, int *err) {
+    int node = blockIdx.x * blockDim.x + threadIdx.x;
+    if (node >= n_nodes) return;
+    if (!bn_leaf(nodes[node]) || (node != 0 && parent[node] < 0)) return;  // start at the tree's leaves
+    {
+        const BinNode nd = nodes[node];
+        const int cnt = bcount[node];
+        const float cl = cnt <= max_leaf ? kCostTri * surface_area(f3(nd.lo), f3(nd.hi)) * (float)cnt : kCostInf;
+        for (int j = 0; j < 8; ++j) cost[(size_t)node * 8 + j] = cl;
+        dec[node] = 0u;
+    }
+    for (int guard = 0; guard < 4096; ++guard) {
+        const int p = node == 0 ? -1 : parent[node];
+        if (p < 0) return;
+        __threadfence();
+        if (atomicAdd(&visits[p], 1) == 0) return;  // the other child is not done: it finishes p
+        __threadfence();
+        const BinNode nd = nodes[p];
+        const int l = __float_as_int(nd.lo.w), r = __float_as_int(nd.hi.w);
+        float cl8[8], cr8[8];
+        for (int j = 0; j < 8; ++j) {
+            cl8[j] = __ldcg(&cost[(size_t)l * 8 + j]);
+            cr8[j] = __ldcg(&cost[(size_t)r * 8 + j]);
+        }
+        float D[9];
+        int K[9];
+        D[1] = kCostInf;
+        K[1] = 0;
+        for (int j = 2; j <= 8; ++j) {
+            float best = kCostInf;
+            int bk = 1;
+            for (int k = 1; k < j; ++k) {
+                const float c = cl8[k - 1] + cr8[j - k - 1];
+                if (c < best) { best = c; bk = k; }
+            }
+            D[j] = best;
+            K[j] = bk;
+        }
+        const float area = surface_area(f3(nd.lo), f3(nd.hi));
+        const int cnt = bcount[p];
+        float c = cnt <= max_leaf ? kCostTri * area * (float)cnt : kCostNode * area + D[8];
+        unsigned d = (unsigned)K[8];
+        cost[(size_t)p * 8] = c;
+        for (int j = 2; j <= 8; ++j) {
+            if (D[j] < c) {
+                c = D[j];
+                d |= (unsigned)K[j] << (3 * (j - 1));
+            }
+            cost[(size_t)p * 8 + j - 1] = c;
+        }
+        dec[p] = d;
+        node = p;
+    }
+    raise_err(err, kErrStackOverflow);  // deeper than any tree this build makes
+}
+
 __global__ void k_collapse_count(const int *tasks, int ntasks, const BinNode *nodes,
-                                 const int *bcount, int *child_list, int *n_inner, int *n_tris,
-                                 int cap, int max_leaf, int *err) {
+                                 const int *bcount, const unsigned *dec, int *child_list, int *n_inner,
+                                 int *n_tris, int cap, int max_leaf, int *err) {
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= ntasks) return;
     int b = tasks[t];
@@ -627,24 +711,32 @@ __global__ void k_collapse_count(const int *tasks, int ntasks, const BinNode *no
     if (bcount[b] <= max_leaf || bn_leaf(nb)) {
         C[nc++] = b;
     } else {
-        C[nc++] = __float_as_int(nb.lo.w);
-        C[nc++] = __float_as_int(nb.hi.w);
-        while (nc < 8) {
-            int pick = -1;
-            float best = -1.0f;
-            for (int i = 0; i < nc; ++i) {
-                int c = C[i];
-                if (c < 0 || c >= cap) { raise_err(err, kErrBadChild); return; }
-                if (bcount[c] <= max_leaf) continue;
-                const BinNode nn = nodes[c];
-                if (bn_leaf(nn)) continue;
-                float a = surface_area(f3(nn.lo), f3(nn.hi));
-                if (a > best) { best = a; pick = i; }
+        // the 8 slots go to b's two children as the cost table chose, and on
+        // down until each share is one slot, a leaf or a node that keeps
+        // what it was given
+        int sn[16], sj[16];
+        int sp = 0;
+        const int k8 = (int)(dec[b] & 7u);
+        sn[sp] = __float_as_int(nb.lo.w); sj[sp++] = k8;
+        sn[sp] = __float_as_int(nb.hi.w); sj[sp++] = 8 - k8;
+        while (sp > 0) {
+            --sp;
+            const int c = sn[sp];
+            int j = sj[sp];
+            if (c < 0 || c >= cap || j < 1 || nc >= 8) { raise_err(err, kErrBadChild); return; }
+            const BinNode nn = nodes[c];
+            if (j > 1 && bcount[c] > max_leaf && !bn_leaf(nn)) {
+                const unsigned dc = dec[c];
+                while (j > 1 && ((dc >> (3 * (j - 1))) & 7u) == 0u) --j;
+                if (j > 1) {
+                    const int k = (int)((dc >> (3 * (j - 1))) & 7u);
+                    if (sp + 2 > 16 || k < 1 || k >= j) { raise_err(err, kErrBadChild); return; }
+                    sn[sp] = __float_as_int(nn.lo.w); sj[sp++] = k;
+                    sn[sp] = __float_as_int(nn.hi.w); sj[sp++] = j - k;
+                    continue;
+                }
             }
-            if (pick < 0) break;
-            const BinNode nn = nodes[C[pick]];
-            C[pick] = __float_as_int(nn.lo.w);
-            C[nc++] = __float_as_int(nn.hi.w);
+            C[nc++] = c;
         }
     }
     int ni = 0, nt = 0;
@@ -900,6 +992,9 @@ kgk_status bvh_build(DevScene &s, cudaStream_t st, BvhBuildStats *out) {
     KGK_TRY(buf.get(&nodes, cap, "bvh binary nodes"));
     KGK_TRY(buf.get(&bfirst, cap, "bvh binary nodes"));
     KGK_TRY(buf.get(&bcount, cap, "bvh binary nodes"));
+    // slots the small builder reserves but does not use read as leaves
+    // (hi.w = -1) that no node points to
+    KGK_CUDA(cudaMemsetAsync(nodes, 0xFF, (size_t)cap * sizeof(BinNode), st));
     KGK_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
 
     k_init_bounds<<<1, 32, 0, st>>>(gbounds);
@@ -1069,6 +1164,22 @@ kgk_status bvh_build(DevScene &s, cudaStream_t st, BvhBuildStats *out) {
     if (herr != 0)
         return fail(KGK_ERR_DEVICE_CHECK, "bvh_build: binary build check failed (code " + std::to_string(herr) + ")");
 
+    // the collapse's cost table, bottom up over the binary tree
+    const int n_bin = node_counter;
+    int *parent, *visits;
+    float *dp_cost;
+    unsigned *dec;
+    KGK_TRY(buf.get(&parent, n_bin, "bvh collapse table"));
+    KGK_TRY(buf.get(&visits, n_bin, "bvh collapse table"));
+    KGK_TRY(buf.get(&dp_cost, 8 * (size_t)n_bin, "bvh collapse table"));
+    KGK_TRY(buf.get(&dec, n_bin, "bvh collapse table"));
+    KGK_CUDA(cudaMemsetAsync(parent, 0xFF, (size_t)n_bin * sizeof(int), st));
+    KGK_CUDA(cudaMemsetAsync(visits, 0, (size_t)n_bin * sizeof(int), st));
+    KGK_CUDA(cudaMemsetAsync(dec, 0, (size_t)n_bin * sizeof(unsigned), st));
+    k_dp_parents<<<(n_bin + 255) / 256, 256, 0, st>>>(nodes, n_bin, parent, err);
+    k_dp_up<<<(n_bin + 255) / 256, 256, 0, st>>>(nodes, bcount, parent, n_bin, max_leaf, dp_cost, dec, visits, err);
+    KGK_CUDA(cudaGetLastError());
+
     // collapse
     WideNode *wide;
     float4 *tri_rec;
@@ -1093,7 +1204,7 @@ kgk_status bvh_build(DevScene &s, cudaStream_t st, BvhBuildStats *out) {
     while (ntasks > 0) {
         ++wlevels;
         const int g = (ntasks + 127) / 128;
-        k_collapse_count<<<g, 128, 0, st>>>(tasks_a, ntasks, nodes, bcount, child_list, n_inner, n_tri,
+        k_collapse_count<<<g, 128, 0, st>>>(tasks_a, ntasks, nodes, bcount, dec, child_list, n_inner, n_tri,
                                             cap, max_leaf, err);
         KGK_CUDA(cudaGetLastError());
         KGK_TRY(scan_exclusive(n_inner, inner_scan, ntasks, scan_tmp, tot, st));
