@@ -267,7 +267,7 @@ def run_ours(args):
     achieved = bytes_per_ray * ext_rays / ext_s / 1e9 if ext_s > 0 else None
     n_ext = solo["extend_launches"] if solo.get("extend_launches") else None
     traffic = None
-    dram_per_ray = read_profile_value("k_extend_c2_traffic.md", "dram_bytes_per_ray")
+    dram_per_ray = read_profile_value("k_extend_traffic_960x540_16spp.md", "dram_bytes_per_ray")
     if dram_per_ray is not None and n_ext:
         traffic = round(dram_per_ray * ext_rays / n_ext)
     # issue side of the same launches: FP32 operations per ray (a slab test is
@@ -305,6 +305,7 @@ def run_ours(args):
                      "peak_source": peak_kind,
                      "bytes_per_ray": round(bytes_per_ray, 1),
                      "achieved_per_launch_bytes": round(bytes_per_ray * ext_rays / n_ext) if n_ext else None,
+                     "extend_rays_per_frame": int(ext_rays), "extend_launches_per_frame": n_ext,
                      "byte_frac": round(byte_frac, 4) if byte_frac else None,
                      "issue": {"ops_per_ray": round(ops_per_ray, 1),
                                "achieved": round(issue_ach, 3) if issue_ach else None,
