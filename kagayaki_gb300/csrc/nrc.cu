@@ -878,16 +878,21 @@ __global__ void k_make_image(const float *w, unsigned short *img) {
     }
 }
 
-__global__ void k_check_finite(const float *g, int n, int *bad) {
+// One Adam step with the BF16 image kept in step: every block first checks
+// that all gradients are finite (n <= 74,112 floats, read from L2), block 0
+// records the verdict for k_scale_update, and if it is clean each updated
+// master weight is written to the image too (the image's padding never
+// changes).
+template <int W>
+__global__ void k_adam_image(float *w, float *m, float *v, const float *g, const float *scale_p, float lr, float b1,
+                             float b2, float eps, float bc1, float bc2, unsigned short *img, int *bad_out) {
+    constexpr int n = Net<W>::kParams, P = Net<W>::kPitch;
     int local = 0;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    for (int i = threadIdx.x; i < n; i += blockDim.x)
         if (!isfinite(g[i])) local = 1;
-    if (__any_sync(~0u, local) && (threadIdx.x & 31) == 0) atomicOr(bad, 1);
-}
-
-__global__ void k_adam(float *w, float *m, float *v, const float *g, int n, const int *bad, const float *scale_p,
-                       float lr, float b1, float b2, float eps, float bc1, float bc2) {
-    if (*bad) return;
+    const int bad = __syncthreads_or(local);
+    if (blockIdx.x == 0 && threadIdx.x == 0) *bad_out = bad;
+    if (bad) return;
     const float inv_s = 1.0f / *scale_p;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const float gi = g[i] * inv_s;
@@ -895,7 +900,24 @@ __global__ void k_adam(float *w, float *m, float *v, const float *g, int n, cons
         const float vi = b2 * v[i] + (1.0f - b2) * gi * gi;
         m[i] = mi;
         v[i] = vi;
-        w[i] -= lr * (mi / bc1) / (sqrtf(vi / bc2) + eps);
+        const float wi = w[i] - lr * (mi / bc1) / (sqrtf(vi / bc2) + eps);
+        w[i] = wi;
+        // its place in the image: layer l, row r, column c
+        int row, c;
+        if (i < Net<W>::woff(1)) {
+            row = i / kIn;
+            c = i % kIn;
+        } else if (i < Net<W>::woff(kLayers)) {
+            const int k = i - Net<W>::woff(1);
+            row = W + k / W;  // layers 1..4 follow layer 0's W rows
+            c = k % W;
+        } else {
+            const int k = i - Net<W>::woff(kLayers);
+            row = kLayers * W + k / W;
+            c = k % W;
+        }
+        __nv_bfloat16 bw = __float2bfloat16_rn(wi);
+        img[row * P + c] = *reinterpret_cast<unsigned short *>(&bw);
     }
 }
 
@@ -1108,15 +1130,18 @@ kgk_status nrc_grad_dev(NrcState &N, const float *raw, int raw_stride, const flo
 }
 
 kgk_status nrc_step_dev(NrcState &N, cudaStream_t st) {
-    KGK_CUDA(cudaMemsetAsync(N.ints, 0, sizeof(int), st));  // bad flag
-    k_check_finite<<<64, 256, 0, st>>>(N.g, N.params, N.ints);
     ++N.step;
     const float b1 = 0.9f, b2 = 0.99f;
     const float bc1 = 1.0f - std::pow(b1, (float)N.step), bc2 = 1.0f - std::pow(b2, (float)N.step);
-    k_adam<<<64, 256, 0, st>>>(N.w, N.m, N.v, N.g, N.params, N.ints, N.scal, N.cfg.learning_rate, b1, b2, 1e-10f,
-                               bc1, bc2);
+    // Adam and the image in one launch (the finite check in every block),
+    // then the loss scale from block 0's verdict in N.ints[0]
+    if (N.cfg.width == 128)
+        k_adam_image<128><<<64, 256, 0, st>>>(N.w, N.m, N.v, N.g, N.scal, N.cfg.learning_rate, b1, b2, 1e-10f, bc1,
+                                              bc2, N.img, N.ints);
+    else
+        k_adam_image<64><<<64, 256, 0, st>>>(N.w, N.m, N.v, N.g, N.scal, N.cfg.learning_rate, b1, b2, 1e-10f, bc1,
+                                             bc2, N.img, N.ints);
     k_scale_update<<<1, 1, 0, st>>>(N.scal, N.ints + 1, N.ints);
-    make_image(N, st);
     KGK_CUDA(cudaGetLastError());
     return KGK_OK;
 }
