@@ -256,12 +256,25 @@ __device__ __forceinline__ void primary_ray(const Params &P, int i, float3 &dir_
     s_out = s;
 }
 
+// The path that buffer slot i of a wave starts: slots run over 8 x 4-pixel
+// tiles (tiles in row order, pixels in row order inside a tile), so that a
+// warp's 32 primary rays - and the shadow and secondary rays that follow
+// them - leave one compact patch of the image.  The path index itself keeps
+// its meaning (pixel = index % npx, sample = index / npx); images whose sides
+// are not multiples of 8 and 4 keep scanline order.
+__device__ __forceinline__ int tiled_path(const Params &P, int i) {
+    if ((P.W & 7) || (P.H & 3)) return i;
+    const int q = i % P.npx, t = q >> 5, w = q & 31, tw = P.W >> 3;
+    return (i - q) + ((t / tw) * 4 + (w >> 3)) * P.W + (t % tw) * 8 + (w & 7);
+}
+
 __global__ void k_raygen(Params P) {
     const int n = P.npx * P.spp_wave;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    for (int slot = blockIdx.x * blockDim.x + threadIdx.x; slot < n; slot += gridDim.x * blockDim.x) {
+        const int i = slot, id = tiled_path(P, slot);
         float3 dir;
         unsigned long long s;
-        primary_ray(P, i, dir, s);
+        primary_ray(P, id, dir, s);
         const PathBuf &b = P.cur;
         b.o[i] = make_float4(P.cam.CamOrg.x, P.cam.CamOrg.y, P.cam.CamOrg.z, 0.0f);
         b.d[i] = make_float4(dir.x, dir.y, dir.z, 0.0f);  // w: pdf of the sampled direction (0 = no MIS)
@@ -270,10 +283,10 @@ __global__ void k_raygen(Params P) {
         b.rad[i] = make_float4(r0, r0, r0, 0.0f);
         b.rng[i] = s;
         b.depth[i] = 0;
-        b.id[i] = i;
+        b.id[i] = id;
         if (P.use_cache) {
             b.spread[i] = make_float2(0.0f, 0.0f);
-            const bool train = P.train_stride > 0 && i < P.npx && (i % P.train_stride) == P.train_offset;
+            const bool train = P.train_stride > 0 && id < P.npx && (id % P.train_stride) == P.train_offset;
             b.pflags[i] = train ? 1 : 0;
         }
     }
