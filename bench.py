@@ -604,6 +604,25 @@ def run_svgf_orbit(args):
                                     None, 0))
         compat_s.append(time.perf_counter() - t0)
     compat_ms = 1e3 * float(np.median(compat_s[3:]))
+    # the same filter on a 1920x1080 Cornell-box frame (the scene the reference
+    # arm times the reference's own ApplySVGF on)
+    from kagayaki_gb300 import ESTIMATOR_COMPAT, camera_setup, scenes
+    ctris, cmats, cc = scenes.cornell_box()
+    cornell_s = []
+    cb_out = torch.empty((1080, 1920, 4), dtype=torch.float32, device="cuda")
+    with Scene(ctris, cmats) as cs:
+        cs.build_bvh()
+        ccam = camera_setup(cc["origin"], cc["dist"], cc["rot"], 1080)
+        for f in range(8):
+            cs.render(ccam, 1920, 1080, spp=1, estimator=ESTIMATOR_COMPAT, frame_index=f, keep_on_device=True,
+                      write_gbuffer=True)
+            cs.sync()
+            cfg_cb = KgkSvgfConfig(mode=0, width=1920, height=1080, frame_index=f)
+            t0 = time.perf_counter()
+            check(lib().kgk_svgf_output(cs._h, ctypes.byref(cfg_cb), None, ctypes.c_void_p(cb_out.data_ptr()),
+                                        None, 0))
+            cornell_s.append(time.perf_counter() - t0)
+    compat_cornell_ms = 1e3 * float(np.median(cornell_s[2:]))
     # the same frame through the float path, tone-mapped on the host
     from kagayaki_gb300 import tonemap
     rgba_match = bool(np.array_equal(last_rgba, tonemap(filt)))
@@ -626,9 +645,13 @@ def run_svgf_orbit(args):
                     "d2h_bytes_per_step": W * H * 4},
             "float_host_buffers_frames_per_s": round(frames / secs_float, 2),
             "compat_filter_ms_per_frame": {"value": round(compat_ms, 3),
+                                           "cornell_1080p": round(compat_cornell_ms, 3),
                                            "what": "kgk_svgf mode 0 (ApplySVGF, 5 x 5 a-trous passes) at the "
                                                    "same size, device buffers, wall clock of the synchronous "
-                                                   "call, median of 10 frames after 3"},
+                                                   "call (records from the G-buffer included), median of 10 "
+                                                   "frames after 3; cornell_1080p: the same on 1920x1080 "
+                                                   "Cornell-box frames, the input the reference arm times the "
+                                                   "reference's own ApplySVGF on"},
             "rgba8_equals_host_tonemap_of_float_path": rgba_match,
             "relmse_last_frame": {"reference_spp": int(nref),
                                   "noisy_1spp": round(rel_mse(noisy[..., :3].astype(np.float64), ref), 5),
@@ -850,6 +873,30 @@ def gpu_reference_c1():
             "kind": "the reference's render kernel (render.cuh:21-49) compiled for sm_103a from its own headers "
                     "(oracle/ref/ref_gpu.cu), launched as main.cu launches it, CUDA events around each launch; "
                     "rays = traversal calls counted by a second build"}
+
+
+def gpu_reference_svgf(W=1920, H=1080, frames=4):
+    """The reference's own ApplySVGF kernel on this GPU at W x H (the
+    denoiser main.cu:160-166 runs on every frame), or the reason it could not
+    run.  Its input is a Cornell-box frame made on the CPU by the oracle (the
+    compat estimator's one-sample frame and render()'s SVGFBuffer records),
+    chained over `frames` launches as main.cu chains them.  Kernel time only
+    (CUDA events)."""
+    try:
+        from oracle import ref_gpu
+        why = ref_gpu.available()
+        if why:
+            return {"unavailable": why}
+        res, recs = ref_gpu.cornell_svgf_inputs(W, H)
+        ms, _ = ref_gpu.apply_svgf([(res, recs)] * frames, W, H)
+    except Exception as e:
+        return {"unavailable": f"{type(e).__name__}: {e}"}
+    return {"workload": f"ApplySVGF on a {W}x{H} Cornell-box frame (input made by the oracle on the CPU)",
+            "ms_per_call": round(float(np.median(ms)), 3), "ms_all": [round(x, 3) for x in ms], "unit": "ms",
+            "kind": "the reference's ApplySVGF (SVGF.cuh:495-522) compiled for sm_103a from its own headers "
+                    "(oracle/ref/ref_gpu.cu), launched as main.cu:160-166 launches it; it uses __syncthreads as a "
+                    "grid barrier, so blocks race on their neighbours' records (the launch ends: every barrier is at "
+                    "function scope and every neighbour read bounds-checked)"}
 
 
 def run_c1(args, reference=False):
@@ -1077,7 +1124,9 @@ def run_reference(args):
             # the reference's own CUDA renderer on this GPU, at the configuration
             # its traversal handles (config C1); at this line's 5.2M triangles
             # its 5000-entry traversal table overflows and reports misses
-            "gpu_reference_c1": gpu_reference_c1()}
+            "gpu_reference_c1": gpu_reference_c1(),
+            # its denoiser too, at the size the SVGF orbit runs
+            "gpu_reference_svgf": gpu_reference_svgf()}
     print(json.dumps(line), flush=True)
 
 

@@ -1,8 +1,8 @@
 /*
  * ref_gpu.cu - the reference's own render kernel (render.cuh:21-49, with
- * RayTrace and everything it calls) compiled for sm_103a into a cubin, so
- * that the reference's CUDA renderer can be timed on the GPU beside the new
- * one.  TEST AND MEASUREMENT INFRASTRUCTURE: oracle/Makefile (target
+ * RayTrace and everything it calls) and its ApplySVGF kernel (SVGF.cuh:495-522)
+ * compiled for sm_103a into a cubin, so that the reference's CUDA renderer and
+ * denoiser can be timed on the GPU beside the new ones.  TEST AND MEASUREMENT INFRASTRUCTURE: oracle/Makefile (target
  * `refgpu`) builds it from the reference headers where they lie, with
  * ref_gpu_shim.h force-included; oracle/ref_gpu.py loads the cubin through
  * the CUDA driver API.  Nothing in the product links it.
@@ -33,3 +33,6 @@ public:
 #include "struct_Xorshift.cuh"
 #include "NextEventEstimation.cuh"
 #include "render.cuh"
+// ApplySVGF (SVGF.cuh:495-522), the kernel main.cu:160-166 launches on each
+// rendered frame, timed beside the library's kgk_svgf_apply
+#include "SVGF.cuh"

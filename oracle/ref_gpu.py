@@ -7,11 +7,11 @@ the product imports it.
 
 Files (git-ignored, made by build() where the reference checkout is; device
 code and data only, so they load on the GPU machine's host architecture):
-  _ref/kgkref_render.cubin        render() (ref/ref_gpu.cu, oracle/Makefile)
+  _ref/kgkref_render.cubin        render() and ApplySVGF() (ref/ref_gpu.cu, oracle/Makefile)
   _ref/kgkref_render_count.cubin  the same, counting traversal calls
   _ref/c1_scene.bin               the Cornell box with the reference's BVH
                                   (construct_BVH) and light CDF (calculate_Lss)
-  _ref/kgkref_render.txt          the kernel's symbol name
+  _ref/kgkref_render.txt          the two kernels' symbol names
 
 Two guards keep the launch inside defined behaviour, both outside the
 reference's code:
@@ -53,11 +53,13 @@ def build():
     if rc != 0:
         raise RuntimeError("ref_export_scene failed")
     out = subprocess.run(["nm", "-D", orc.REF_SO], capture_output=True, text=True, check=True).stdout
-    names = [ln.split()[-1] for ln in out.splitlines() if ln.split()[-1].startswith("_Z6renderP6Camera")]
-    if len(names) != 1:
-        raise RuntimeError("render() symbol not found in the reference's host build")
+    syms = [ln.split()[-1] for ln in out.splitlines() if ln.split()]
+    names = [n for n in syms if n.startswith("_Z6renderP6Camera")]
+    svgf = [n for n in syms if n.startswith("_Z9ApplySVGF")]
+    if len(names) != 1 or len(svgf) != 1:
+        raise RuntimeError("render() / ApplySVGF() symbol not found in the reference's host build")
     with open(NAME_FILE, "w") as f:
-        f.write(names[0] + "\n")
+        f.write(names[0] + "\n" + svgf[0] + "\n")
 
 
 def available():
@@ -208,7 +210,7 @@ def render_c1(cam, W=256, H=256, spp=16, repeats=2, check_samples=None, cubin=No
     why = available()
     if why:
         raise RuntimeError(why)
-    name = open(NAME_FILE).read().strip()
+    name = open(NAME_FILE).read().split()[0]
     cubin = cubin or CUBIN
     sc = _read_scene(SCENE_C1)
     cu = _Cuda()
@@ -269,6 +271,126 @@ def render_c1(cam, W=256, H=256, spp=16, repeats=2, check_samples=None, cubin=No
     return dict(ms_per_frame=best, ms_all=ms, rays_per_frame=rays, mrays=rays / (best / 1e3) / 1e6,
                 first_launch_agreement=agree, mean=mean, registers=regs.value, stack_bytes=lmem.value,
                 launches_per_frame=spp, pixels=W * H)
+
+
+# struct_SVGFBuffers.cuh:7-23 `SVGFBuffer` (112 B)
+_SVGF_REC = np.dtype({
+    "names": ["Albedo", "Emission", "Normal", "ColorHistory", "ObjectID", "MaterialID", "PosLastFrameI",
+              "PosLastFrameF", "sampleNum", "MomentOne", "MomentTwo", "Variance", "Depth",
+              "willApplyATrousFilter", "willApplyTemporalAccumulation"],
+    "formats": [("<f4", (4,)), ("<f4", (4,)), ("<f4", (4,)), ("<f4", (4,)), "<i4", "<i4", ("<i4", (2,)),
+                ("<f4", (2,)), "<i4", "<f4", "<f4", "<f4", "<f4", "u1", "u1"],
+    "offsets": [0, 16, 32, 48, 64, 68, 72, 80, 88, 92, 96, 100, 104, 108, 109],
+    "itemsize": 112})
+
+
+def cornell_svgf_inputs(W, H):
+    """One frame of ApplySVGF input for the Cornell box at W x H, made on the
+    CPU by the oracle: the compat estimator's one-sample frame
+    (orc.render_compat) and the SVGFBuffer records render() fills at the
+    primary hits (RayTrace.cuh:66-82): albedo (sINF when below 1e-5),
+    emission, the normal turned against the ray, face and material ids, hit
+    distance, and the reprojection left at (-1, -1) as the reference leaves
+    it (struct_Camera.cuh:109-110); pixels that miss keep SVGFBuffer::init's
+    values.  Returns (result (W*H, 4) float32, records (W*H * 112,) uint8)."""
+    from kagayaki_gb300 import scenes
+    from oracle import orc
+    tris, mats, c = scenes.cornell_box()
+    cam = orc.camera_setup(c["origin"], c["dist"], c["rot"], H)
+    org, cdir, dist, sx, sy, psz = cam[0:3], cam[4:7], cam[8], cam[9:12], cam[13:16], cam[17]
+    Y, X = np.divmod(np.arange(W * H, dtype=np.int64), W)
+    d = (cdir[None, :] * dist + sx[None, :] * ((X - W / 2.0) * psz)[:, None].astype(np.float32) +
+         sy[None, :] * ((H / 2.0 - Y) * psz)[:, None].astype(np.float32)).astype(np.float32)
+    d /= np.sqrt((d * d).sum(1, keepdims=True))
+    rays = np.zeros(W * H, np.dtype([("dir", "<f4", (4,)), ("org", "<f4", (4,)), ("_dummy", "<f8")], align=True))
+    rays["dir"][:, :3] = d
+    rays["org"][:, :3] = org
+    ids, t = orc.closest_brute(tris, rays)
+    rec = np.zeros(W * H, _SVGF_REC)
+    rec["ObjectID"] = -1
+    rec["MaterialID"] = -1
+    rec["PosLastFrameI"] = -1
+    rec["PosLastFrameF"] = -1.0
+    rec["MomentOne"] = -1.0
+    rec["MomentTwo"] = -1.0
+    rec["willApplyATrousFilter"] = 1
+    hit = ids >= 0
+    h = ids[hit]
+    v = tris["verts"][h][:, :, :3].astype(np.float64)      # (k, 3 vertices, xyz)
+    n = np.cross(v[:, 1] - v[:, 0], v[:, 2] - v[:, 0])
+    n /= np.linalg.norm(n, axis=1, keepdims=True)
+    n = np.where(((n * d[hit]).sum(1) > 0)[:, None], -n, n)
+    mid = tris["material_id"][h]
+    dif = mats["diffuse"][mid][:, :3].astype(np.float32)
+    dif = np.where((np.linalg.norm(dif, axis=1) < 1e-5)[:, None], np.float32(1e-4), dif)
+    rec["Albedo"][hit, :3] = dif
+    rec["Emission"][hit, :3] = mats["emission"][mid][:, :3]
+    rec["Normal"][hit, :3] = n
+    rec["ObjectID"][hit] = h
+    rec["MaterialID"][hit] = mid
+    rec["Depth"][hit] = t[hit]
+    frames, _ = orc.render_compat(tris, mats, cam, W, H, 1)
+    res = np.zeros((W * H, 4), np.float32)
+    res[:, :3] = np.nan_to_num(frames[0], nan=0.0)
+    return res, rec.view(np.uint8)
+
+
+def apply_svgf(frames, W, H, repeats=3):
+    """The reference's ApplySVGF (SVGF.cuh:495-522) on the GPU, launched as
+    main.cu:160-166 launches it (W*H/256 blocks of 256 threads, LoopID 0)
+    over a chain of frames: `frames` is a list of (result, records) pairs -
+    the (W*H, 4) float32 radiance and the W*H 112-byte SVGFBuffer records of
+    one frame - and, as main.cu:182 does, each frame's filtered records
+    become the next frame's previous ones.  The kernel uses __syncthreads as
+    if it were a grid barrier, so blocks race on their neighbours' records:
+    the run ends (every barrier sits at function scope, every neighbour read
+    is bounds-checked), its output is not the filter's.  Returns the CUDA-event
+    time of each launch of the last repeat of the chain (ms) and the last
+    frame's filtered output (W*H, 4)."""
+    why = available()
+    if why:
+        raise RuntimeError(why)
+    npx = W * H
+    if npx % 256 or npx > 1920 * 1920:
+        raise ValueError("ApplySVGF needs W*H a multiple of 256 and at most 1920*1920 (its moment maps)")
+    name = open(NAME_FILE).read().split()[1]
+    cu = _Cuda()
+    try:
+        mod = _Module(cu, CUBIN, name)
+        mod.set("image_sizeX_device", W, ctypes.c_int)
+        mod.set("image_sizeY_device", H, ctypes.c_int)
+        d_res = cu.alloc(16 * npx)
+        d_filt = cu.alloc(16 * npx)
+        d_prev = cu.alloc(112 * npx)
+        d_cur = cu.alloc(112 * npx)
+        ev = [_vp(), _vp()]
+        for e in ev:
+            cu.ck(cu.L.cuEventCreate(ctypes.byref(e), 0), "cuEventCreate")
+        ms = []
+        for r in range(repeats):
+            ms = []
+            for f, (res, recs) in enumerate(frames):
+                for d, a in ((d_res, res), (d_cur, recs)):
+                    b = np.ascontiguousarray(a)
+                    cu.ck(cu.L.cuMemcpyHtoD_v2(_u64(d), b.ctypes.data_as(_vp), ctypes.c_size_t(b.nbytes)), "upload")
+                args = [_u64(d_res), _u64(d_filt), _u64(d_prev), _u64(d_cur), ctypes.c_int(0), ctypes.c_int(npx),
+                        ctypes.c_int(f)]
+                params = (_vp * len(args))(*[ctypes.addressof(a) for a in args])
+                cu.ck(cu.L.cuEventRecord(ev[0], None), "cuEventRecord")
+                cu.ck(cu.L.cuLaunchKernel(mod.fn, npx // 256, 1, 1, 256, 1, 1, 0, None, params, None), "ApplySVGF")
+                cu.ck(cu.L.cuEventRecord(ev[1], None), "cuEventRecord")
+                cu.ck(cu.L.cuEventSynchronize(ev[1]), "ApplySVGF")
+                t = ctypes.c_float()
+                cu.ck(cu.L.cuEventElapsedTime_v2(ctypes.byref(t), ev[0], ev[1]), "cuEventElapsedTime")
+                ms.append(t.value)
+                cu.ck(cu.L.cuMemcpyDtoD_v2(_u64(d_prev), _u64(d_cur), ctypes.c_size_t(112 * npx)), "prev = cur")
+        filt = cu.get(d_filt, 16 * npx, np.float32).reshape(-1, 4)
+        for e in ev:
+            cu.L.cuEventDestroy_v2(e)
+        mod.unload()
+    finally:
+        cu.close()
+    return ms, filt
 
 
 if __name__ == "__main__":
