@@ -455,7 +455,7 @@ kgk_status kgk_gbuffer_records(kgk_scene *scene, kgk_svgf_buffer *out);
  *    KGK_ERR_INVALID_ARGUMENT;
  *  - the work runs on `cuda_stream` (a cudaStream_t, NULL = the default
  *    stream) and the call returns when it has finished;
- *  - scratch comes from one fixed device array of ~30 MB inside the library,
+ *  - scratch comes from one fixed device array of ~34 MB inside the library,
  *    which every GPU that loads the library holds until the process exits.
  *    All calls share it: calls that overlap on the GPU (for instance from two
  *    host threads on two streams) race and give undefined results.  Each call

@@ -82,6 +82,10 @@ struct CompatArgs {
     // fields are final (k_c_gauss2): normal and depth, ObjectID and MaterialID
     float4 *gnd;
     int2 *gom;
+    // the center pixel's albedo and willApplyATrousFilter (w = 1 or 0),
+    // final from k_c_gauss2 on: a pass reads 16 B instead of two sectors of
+    // the 112-byte record
+    float4 *galf;
     // each pass's input radiance divided by (albedo + sINF), with its
     // luminance in w: written by the pass before (ping-pong), so a tap reads
     // it instead of dividing
@@ -350,6 +354,7 @@ __global__ void k_c_gauss2(CompatArgs a) {
         // the end of the a-trous passes, and so is R before the first pass
         a.gnd[p] = make_float4(c.Normal.x, c.Normal.y, c.Normal.z, c.Depth);
         a.gom[p] = make_int2(c.ObjectID, c.MaterialID);
+        a.galf[p] = make_float4(c.Albedo.x, c.Albedo.y, c.Albedo.z, c.willApplyATrousFilter ? 1.0f : 0.0f);
         const float3 dc = div3(v3(a.R[p]), v3(c.Albedo) + f3(kS, kS, kS));
         a.dm[p] = make_float4(dc.x, dc.y, dc.z, lumf(dc));
         // the a-trous passes' depth gradient (SVGF.cuh:366-372), from the
@@ -380,7 +385,7 @@ template <class Src>
 __device__ __forceinline__ void compat_atrous_px(const CompatArgs &a, const CompatIO &io, const Src &S, int x, int y,
                                                  int stage) {
     const int W = a.W, H = a.H, p = W * y + x, step = 1 << stage;
-    kgk_svgf_buffer &c = a.C[p];
+    const float4 af = a.galf[p];
     const float4 g = S.nd(0, 0);
     const int2 om = S.om(0, 0);
     const float4 dcl = S.dm(0, 0);
@@ -390,7 +395,7 @@ __device__ __forceinline__ void compat_atrous_px(const CompatArgs &a, const Comp
     const float gx = a.gz[2 * p], gy = a.gz[2 * p + 1];
     const float3 n = f3(g);
     const float sdv = a.sd[p];
-    const bool filt = c.willApplyATrousFilter;
+    const bool filt = af.w != 0.0f;
     float3 srad = f3(0.0f, 0.0f, 0.0f);
     float svar = 0.0f, swt = 0.0f;
 #pragma unroll
@@ -430,10 +435,10 @@ __device__ __forceinline__ void compat_atrous_px(const CompatArgs &a, const Comp
         io.dmout[p] = dcl;
         if (om.x == -1) return;
         a.F[p] = rin;
-        c.willApplyTemporalAccumulation = true;
+        a.C[p].willApplyTemporalAccumulation = true;
         return;
     }
-    const float3 alb = v3(c.Albedo);
+    const float3 alb = f3(af);
     const float3 fl = srad / swt;
     const float fv = svar / (swt * swt);
     const float cw = 0.2f;
@@ -444,8 +449,8 @@ __device__ __forceinline__ void compat_atrous_px(const CompatArgs &a, const Comp
     io.dmout[p] = make_float4(od.x, od.y, od.z, lumf(od));
     io.vout[p] = filt ? cw * vc + (1 - cw) * fv : vc;
     if (stage == 0) {
-        c.ColorHistory = kv(o);
-        c.willApplyTemporalAccumulation = true;
+        a.C[p].ColorHistory = kv(o);
+        a.C[p].willApplyTemporalAccumulation = true;
     }
 }
 
@@ -580,15 +585,16 @@ __global__ void k_copy_vec(const kgk_vec *src, kgk_vec *dst, int n) {
 
 // Scratch of the compat pipeline, carved from one block: M1, M2, sd, gz (two
 // arrays), s1, s2, sw, var, var2 at `fl` bytes each, then R2 (`vec` bytes),
-// the guide (gnd, 16 B a pixel), the ids (gom, 8 B), the two demodulated
-// radiance buffers (dm, dm2, 16 B each), then the per-pixel spatial flags;
+// the guide (gnd, 16 B a pixel), the two demodulated radiance buffers (dm,
+// dm2, 16 B each), albedo + filter flag (galf, 16 B), the ids (gom, 8 B),
+// then the per-pixel spatial flags;
 // every array starts on a 256-byte boundary.  Returns var2, the second
 // variance buffer of the a-trous passes.
 constexpr size_t scratch_up(size_t x) { return (x + 255) & ~(size_t)255; }
 constexpr size_t compat_fl(size_t npx) { return scratch_up(npx * sizeof(float)); }
 constexpr size_t compat_vec(size_t npx) { return scratch_up(npx * sizeof(kgk_vec)); }
 constexpr size_t compat_scratch_bytes(size_t npx) {
-    return 10 * compat_fl(npx) + 4 * compat_vec(npx) + scratch_up(npx * sizeof(int2)) + npx;
+    return 10 * compat_fl(npx) + 5 * compat_vec(npx) + scratch_up(npx * sizeof(int2)) + npx;
 }
 
 float *carve_compat(CompatArgs &a, unsigned char *b, size_t fl, size_t vec) {
@@ -605,6 +611,7 @@ float *carve_compat(CompatArgs &a, unsigned char *b, size_t fl, size_t vec) {
     a.gnd = (float4 *)b; b += vec;
     a.dm = (float4 *)b; b += vec;
     a.dm2 = (float4 *)b; b += vec;
+    a.galf = (float4 *)b; b += vec;
     a.gom = (int2 *)b; b += scratch_up(vec / 2);
     a.spatial = b;
     return var2;
@@ -1493,7 +1500,7 @@ void kgk_host_free(void *p) {
 // must not allocate because cudaMalloc / cudaFree synchronise the whole device
 // and stall the caller's other streams.  This entry point takes its scratch
 // from g_svgf_scratch, a file-scope device array sized for
-// KGK_SVGF_NOALLOC_MAX_PIXELS pixels (113 B per pixel, ~30 MB); every GPU that
+// KGK_SVGF_NOALLOC_MAX_PIXELS pixels (129 B per pixel, ~34 MB); every GPU that
 // loads the library holds that array until the process exits.
 // ---------------------------------------------------------------------------
 #include <mutex>
