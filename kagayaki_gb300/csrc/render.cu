@@ -1671,7 +1671,7 @@ kgk_status kgk_render(kgk_scene *s, const kgk_camera *cam, const kgk_camera *pre
                 k_shade<KGK_ESTIMATOR_COMPAT, false><<<grid, 128, 0, st>>>(P, R.mq, R.lq, R.dq, nidx, R.sh_o[0],
                                                                          R.sh_d[0], R.sh_c[0], R.sh_o[1], R.sh_d[1],
                                                                          R.sh_c[1]);
-            else {  // one instance for both: the cache-free one measured slower (29.6 vs 29.2 ms)
+            else if (P.use_cache) {
                 k_shade<KGK_ESTIMATOR_UNBIASED, true, 1><<<grid, 128, 0, st>>>(P, R.mq, R.lq, R.dq, nidx, R.sh_o[0],
                                                                              R.sh_d[0], R.sh_c[0], R.sh_o[1],
                                                                              R.sh_d[1], R.sh_c[1]);
@@ -1681,6 +1681,17 @@ kgk_status kgk_render(kgk_scene *s, const kgk_camera *cam, const kgk_camera *pre
                 k_shade<KGK_ESTIMATOR_UNBIASED, true, 3><<<grid, 128, 0, st>>>(P, R.mq, R.lq, R.dq, nidx, R.sh_o[0],
                                                                              R.sh_d[0], R.sh_c[0], R.sh_o[1],
                                                                              R.sh_d[1], R.sh_c[1]);
+                launches += 2;
+            } else {  // without the cache, instances without its code
+                k_shade<KGK_ESTIMATOR_UNBIASED, false, 1><<<grid, 128, 0, st>>>(P, R.mq, R.lq, R.dq, nidx, R.sh_o[0],
+                                                                              R.sh_d[0], R.sh_c[0], R.sh_o[1],
+                                                                              R.sh_d[1], R.sh_c[1]);
+                k_shade<KGK_ESTIMATOR_UNBIASED, false, 2><<<grid, 128, 0, st>>>(P, R.mq, R.lq, R.dq, nidx, R.sh_o[0],
+                                                                              R.sh_d[0], R.sh_c[0], R.sh_o[1],
+                                                                              R.sh_d[1], R.sh_c[1]);
+                k_shade<KGK_ESTIMATOR_UNBIASED, false, 3><<<grid, 128, 0, st>>>(P, R.mq, R.lq, R.dq, nidx, R.sh_o[0],
+                                                                              R.sh_d[0], R.sh_c[0], R.sh_o[1],
+                                                                              R.sh_d[1], R.sh_c[1]);
                 launches += 2;
             }
             KGK_TRY(stage_end());
