@@ -336,7 +336,7 @@ struct QueueBatch {
 };
 
 template <bool kCount>
-__global__ void __launch_bounds__(128) k_extend(Params P, int cnt_idx, int dense_n, int *mq, int *lq, int *dq) {
+__global__ void __launch_bounds__(128, 8) k_extend(Params P, int cnt_idx, int dense_n, int *mq, int *lq, int *dq) {
     const int n = cnt_idx >= 0 ? P.cnt[cnt_idx] : dense_n;
     const DevScene &s = P.sc;
     int *fetch = &P.cnt[kFE];
@@ -1136,7 +1136,7 @@ __global__ void k_flush(Params P, int cnt_idx) {
 // The tail's deferred shadow rays (any-hit: nothing in (kTMin, range)), from
 // the list of filled slots, lanes refilled like k_extend's; the visibility
 // of slot s goes to td_vis[s].
-__global__ void __launch_bounds__(128) k_tail_shadow(Params P) {
+__global__ void __launch_bounds__(128, 8) k_tail_shadow(Params P) {
     const int n = P.cnt[kTD];
     const DevScene &s = P.sc;
     int *fetch = &P.cnt[kTDF];
@@ -1212,7 +1212,7 @@ __global__ void k_tail_resolve(Params P, int cnt_idx, int dense_n) {
 // path's radiance - in the next buffer, or in fin for a finished path (one
 // record per path per queue, so no atomics).  Lanes are refilled like
 // k_extend's.
-__global__ void __launch_bounds__(128) k_shadow(Params P, int cidx, int fidx, const float4 *__restrict__ so,
+__global__ void __launch_bounds__(128, 8) k_shadow(Params P, int cidx, int fidx, const float4 *__restrict__ so,
                                                 const float4 *__restrict__ sd, const float4 *__restrict__ sc) {
     const int n = P.cnt[cidx];
     const DevScene &s = P.sc;

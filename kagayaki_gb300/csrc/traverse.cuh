@@ -21,9 +21,10 @@ namespace kgk {
 constexpr int kTravStack = 32;
 // Node visits a resumable traversal step may make before it tests triangles.
 constexpr int kNodesPerStep = 2;
-// Conservative widening of box exit distances: 1 + 2 * gamma(3) covers the
-// rounding of the quantised plane, the origin offset and the multiply.
-constexpr float kBoxWiden = 1.0000004f;
+// Conservative widening of box exit distances: 1 + 2 * gamma(5) covers the
+// rounding of the origin offset, the multiply, the two roundings of the
+// biased plane offset and the plane's multiply-add.
+constexpr float kBoxWiden = 1.0000006f;
 
 struct RayPre {
     float3 o, d, inv;
@@ -112,11 +113,13 @@ __device__ __forceinline__ void ref_distance(const RayPre &r, float4 a4, float4 
 }
 
 __device__ __forceinline__ unsigned byte_of(unsigned x, int i) { return (x >> (i * 8)) & 0xffu; }
-// Byte i of x as a float, exactly: one byte permute builds the bits of
-// 2^23 + byte, one subtraction removes 2^23 (no integer-to-float conversion).
-__device__ __forceinline__ float byte_as_float(unsigned x, int i) {
-    const unsigned bits = __byte_perm(x, 0x4Bu, (unsigned)i | 0x4550u);
-    return __uint_as_float(bits) - 8388608.0f;
+// 2^15 + (byte i of x) as a float, exactly, in one byte permute: the byte
+// becomes mantissa bits 8..15 under the exponent of 2^15 (bits 0x47000000).
+// The box test folds the bias into its per-node plane offsets, so a plane
+// costs one permute and one multiply-add (no integer-to-float conversion and
+// no subtraction).
+__device__ __forceinline__ float byte_biased(unsigned x, int i) {
+    return __uint_as_float(__byte_perm(x, 0x4700u, 0x5404u | ((unsigned)i << 4)));
 }
 __device__ __forceinline__ unsigned sign_extend_s8x4(unsigned x) { return ((x >> 7) & 0x01010101u) * 0xffu; }
 
@@ -129,9 +132,20 @@ __device__ __forceinline__ unsigned node_intersect(const RayPre &r, float tmin, 
     const float adx = __uint_as_float((e & 0xffu) << 23) * r.inv.x;
     const float ady = __uint_as_float(((e >> 8) & 0xffu) << 23) * r.inv.y;
     const float adz = __uint_as_float(((e >> 16) & 0xffu) << 23) * r.inv.z;
+    // Plane b of an axis lies at t = (2^15 + b) * ad + (o - 2^15 * ad),
+    // formed as one multiply-add with an exact product.  The offset is
+    // rounded twice (o - 2^15 ad, then -/+ the slack), each time by at most
+    // 2^-24 (|o| + 2^15 |ad|) = 2^-24 |o| + 2^-9 |ad|.  A slack of 1/64 of the
+    // axis's quantum (|ad| / 64: per axis, since |ad| is huge on an axis the
+    // ray nearly parallels) moves near planes down and far planes up, four
+    // times the |ad| parts; kBoxWiden covers the |o| parts.
     const float ox = (n0.x - r.o.x) * r.inv.x;
     const float oy = (n0.y - r.o.y) * r.inv.y;
     const float oz = (n0.z - r.o.z) * r.inv.z;
+    const float bx = fmaf(-32768.0f, adx, ox), by = fmaf(-32768.0f, ady, oy), bz = fmaf(-32768.0f, adz, oz);
+    const float sx = fabsf(adx) * 0.015625f, sy = fabsf(ady) * 0.015625f, sz = fabsf(adz) * 0.015625f;
+    const float oxn = bx - sx, oyn = by - sy, ozn = bz - sz;
+    const float oxf = bx + sx, oyf = by + sy, ozf = bz + sz;
     const float tm = tmax * kBoxWiden;
     unsigned hits = 0;
 #pragma unroll
@@ -149,12 +163,12 @@ __device__ __forceinline__ unsigned node_intersect(const RayPre &r, float tmin, 
         const unsigned zn = r.d.z < 0.0f ? qhz : qlz, zf = r.d.z < 0.0f ? qlz : qhz;
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
-            const float t0x = byte_as_float(xn, j) * adx + ox;
-            const float t0y = byte_as_float(yn, j) * ady + oy;
-            const float t0z = byte_as_float(zn, j) * adz + oz;
-            const float t1x = byte_as_float(xf, j) * adx + ox;
-            const float t1y = byte_as_float(yf, j) * ady + oy;
-            const float t1z = byte_as_float(zf, j) * adz + oz;
+            const float t0x = fmaf(byte_biased(xn, j), adx, oxn);
+            const float t0y = fmaf(byte_biased(yn, j), ady, oyn);
+            const float t0z = fmaf(byte_biased(zn, j), adz, ozn);
+            const float t1x = fmaf(byte_biased(xf, j), adx, oxf);
+            const float t1y = fmaf(byte_biased(yf, j), ady, oyf);
+            const float t1z = fmaf(byte_biased(zf, j), adz, ozf);
             const float lo = fmaxf(fmaxf(t0x, t0y), fmaxf(t0z, tmin));
             const float hi = fminf(fminf(t1x, t1y), fminf(t1z, tm)) * kBoxWiden;
             if (lo <= hi) hits |= byte_of(child_bits4, j) << byte_of(bit_index4, j);
