@@ -116,6 +116,8 @@ constexpr int kQRec = 20;
 enum Stat { kRaysC = 0, kRaysS = 1, kOverflow = 2, kNodes = 3, kTris = 4, kRaysT = 5, kNStat = 8 };
 // Paths few enough to finish in the tail kernel (one thread per path).
 constexpr int kTailPaths = 1 << 17;
+// Idle lanes of a tail warp that take new paths together.
+constexpr int kTailRefill = 8;
 // Deferred shadow rays of the tail (unbiased estimator without the cache):
 // the first kDeferBounces bounces of a tail path leave their face-light and
 // environment shadow rays in fixed slots (path, bounce, kind) instead of
@@ -1043,81 +1045,133 @@ __device__ __forceinline__ void defer_shadow(const Params &P, int i, int k, int 
     P.td_list[base + (int)g.thread_rank()] = (int)slot;
 }
 
-// All remaining bounces (at most `bounces`) of one path in registers: closest
-// hit, shading, then its face-light and environment shadow rays in that
-// order (the order of the wavefront's passes, so the radiance sums are the
-// same); with `defer`, the shadow rays of its first kDeferBounces bounces go
-// to slots of tail path i instead.  Returns the deferred-record mask.
+// Bounce k of tail path i in registers: closest hit, shading, then its
+// face-light and environment shadow rays in that order (the order of the
+// wavefront's passes, so the radiance sums are the same); with `defer`, the
+// shadow rays of its first kDeferBounces bounces go to slots of tail path i
+// instead, and bit 2k + j of dmask records record (bounce k, kind j).
+// Returns whether the path continues.
 template <int kEst, bool kCache>
-__device__ __forceinline__ unsigned run_path(const Params &P, PathState &ps, int i, int bounces, bool defer,
-                                             unsigned &rays_c, unsigned &rays_s, unsigned &overflow) {
+__device__ __forceinline__ bool tail_bounce(const Params &P, PathState &ps, int i, int k, bool defer,
+                                            unsigned &dmask, unsigned &rays_c, unsigned &rays_s,
+                                            unsigned &overflow) {
     const DevScene &s = P.sc;
-    unsigned dmask = 0;  // bit 2k + j: deferred record (bounce k, kind j)
-    for (int k = 0; k < bounces; ++k) {
-        const RayPre r = make_ray(ps.o, ps.d);
-        float bt = kBigT, u = 0.0f, v = 0.0f;
-        int bid = 0x7fffffff;
-        TravStats st{0, 0, 0};
-        const int slot = trace_closest<false>(s.nodes, (unsigned)s.n_nodes, s.tri_rec, (unsigned)s.n_tris, r, bt,
-                                              bid, u, v, st);
-        const float4 h = slot < 0 ? make_float4(kBigT, 0.0f, 0.0f, __int_as_float(-1))
-                                  : make_float4(bt, u, v, __int_as_float(bid));
-        ++rays_c;
-        ShadeOut so{};
-        if (kEst == KGK_ESTIMATOR_COMPAT) shade_compat_core(P, ps, h, so);
-        else shade_unbiased_core<kCache>(P, ps, h, so);
-        if (defer && k < kDeferBounces) {
-            if (so.f_pred) {
-                defer_shadow(P, i, k, 0, so.f_org, so.f_dir, so.f_tmax, so.f_c);
-                dmask |= 1u << (2 * k);
-            }
-            if (so.e_pred) {
-                defer_shadow(P, i, k, 1, so.spos, so.e_dir, kBigT, so.e_c);
-                dmask |= 2u << (2 * k);
-            }
-            so.f_pred = so.e_pred = false;
-        }
+    const RayPre r = make_ray(ps.o, ps.d);
+    float bt = kBigT, u = 0.0f, v = 0.0f;
+    int bid = 0x7fffffff;
+    TravStats st{0, 0, 0};
+    const int slot = trace_closest<false>(s.nodes, (unsigned)s.n_nodes, s.tri_rec, (unsigned)s.n_tris, r, bt,
+                                          bid, u, v, st);
+    const float4 h = slot < 0 ? make_float4(kBigT, 0.0f, 0.0f, __int_as_float(-1))
+                              : make_float4(bt, u, v, __int_as_float(bid));
+    ++rays_c;
+    ShadeOut so{};
+    if (kEst == KGK_ESTIMATOR_COMPAT) shade_compat_core(P, ps, h, so);
+    else shade_unbiased_core<kCache>(P, ps, h, so);
+    if (defer && k < kDeferBounces) {
         if (so.f_pred) {
-            const RayPre rs = make_ray(so.f_org, so.f_dir);
-            bool vis;
-            if (so.f_light >= 0) {  // the reference's test: the closest hit is the light
-                float lt = so.f_tmax, lu, lv;
-                int lid = 0x7fffffff;
-                const int ls = trace_closest<false>(s.nodes, (unsigned)s.n_nodes, s.tri_rec, (unsigned)s.n_tris,
-                                                    rs, lt, lid, lu, lv, st);
-                vis = ls >= 0 && lid == so.f_light;
-            } else {
-                vis = !trace_any<false>(s.nodes, (unsigned)s.n_nodes, s.tri_rec, (unsigned)s.n_tris, rs,
-                                        so.f_tmax, st);
-            }
-            if (vis) ps.rad = ps.rad + so.f_c;
-            ++rays_s;
+            defer_shadow(P, i, k, 0, so.f_org, so.f_dir, so.f_tmax, so.f_c);
+            dmask |= 1u << (2 * k);
         }
         if (so.e_pred) {
-            const RayPre rs = make_ray(so.spos, so.e_dir);
-            if (!trace_any<false>(s.nodes, (unsigned)s.n_nodes, s.tri_rec, (unsigned)s.n_tris, rs, kBigT, st))
-                ps.rad = ps.rad + so.e_c;
-            ++rays_s;
+            defer_shadow(P, i, k, 1, so.spos, so.e_dir, kBigT, so.e_c);
+            dmask |= 2u << (2 * k);
         }
-        overflow += st.overflow;
-        if (!so.cont) break;
+        so.f_pred = so.e_pred = false;
     }
-    return dmask;
+    if (so.f_pred) {
+        const RayPre rs = make_ray(so.f_org, so.f_dir);
+        bool vis;
+        if (so.f_light >= 0) {  // the reference's test: the closest hit is the light
+            float lt = so.f_tmax, lu, lv;
+            int lid = 0x7fffffff;
+            const int ls = trace_closest<false>(s.nodes, (unsigned)s.n_nodes, s.tri_rec, (unsigned)s.n_tris,
+                                                rs, lt, lid, lu, lv, st);
+            vis = ls >= 0 && lid == so.f_light;
+        } else {
+            vis = !trace_any<false>(s.nodes, (unsigned)s.n_nodes, s.tri_rec, (unsigned)s.n_tris, rs,
+                                    so.f_tmax, st);
+        }
+        if (vis) ps.rad = ps.rad + so.f_c;
+        ++rays_s;
+    }
+    if (so.e_pred) {
+        const RayPre rs = make_ray(so.spos, so.e_dir);
+        if (!trace_any<false>(s.nodes, (unsigned)s.n_nodes, s.tri_rec, (unsigned)s.n_tris, rs, kBigT, st))
+            ps.rad = ps.rad + so.e_c;
+        ++rays_s;
+    }
+    overflow += st.overflow;
+    return so.cont;
 }
 
+// Each thread carries one path at a time through at most `bounces` more
+// bounces; the grid is what fits on the GPU at once.
+// Unbiased estimator: one loop iteration runs one bounce of every lane's
+// path.  A lane whose path has ended stays idle until kTailRefill lanes of
+// its warp are idle (or the paths run out); then the idle lanes take the next
+// paths together (one atomic for the warp) and load them.  So a warp neither
+// waits for the longest of its 32 paths (most tail paths of a frame end after
+// one bounce there) nor pays a fetch's latency on every bounce.
+// Compat estimator: a loop over each thread's whole path, a new path from
+// the counter when it ends.  Its waves run entirely in the tail from the
+// primary rays (long paths that Russian roulette ends, on small scenes),
+// where the refill loop measured slower.
 template <int kEst, bool kCache>
 __global__ void __launch_bounds__(128) k_tail(Params P, int cnt_idx, int dense_n, int bounces) {
     const int n = cnt_idx >= 0 ? P.cnt[cnt_idx] : dense_n;
     const bool cache = kCache;
     const bool defer = kEst == KGK_ESTIMATOR_UNBIASED && P.td_o != nullptr && n <= kTailPaths;
+    const unsigned lane = threadIdx.x & 31u;
     unsigned rays_c = 0, rays_s = 0, overflow = 0;
-    // a thread takes the next path as soon as its own has ended (the grid is
-    // what fits on the GPU at once), so no path waits for a whole block
-    for (int i = atomicAdd(&P.cnt[kTF], 1); i < n; i = atomicAdd(&P.cnt[kTF], 1)) {
-        PathState ps = load_path(P.cur, i, cache);
-        const unsigned dmask = run_path<kEst, kCache>(P, ps, i, bounces, defer, rays_c, rays_s, overflow);
-        P.fin[ps.id] = make_float4(ps.rad.x, ps.rad.y, ps.rad.z, 0.0f);
-        if (defer) P.td_mask[i] = dmask;
+    if constexpr (kEst == KGK_ESTIMATOR_COMPAT) {
+        for (int i = atomicAdd(&P.cnt[kTF], 1); i < n; i = atomicAdd(&P.cnt[kTF], 1)) {
+            PathState ps = load_path(P.cur, i, cache);
+            unsigned dmask = 0;
+            for (int k = 0; k < bounces; ++k)
+                if (!tail_bounce<kEst, kCache>(P, ps, i, k, false, dmask, rays_c, rays_s, overflow)) break;
+            P.fin[ps.id] = make_float4(ps.rad.x, ps.rad.y, ps.rad.z, 0.0f);
+        }
+        warp_add_u64(&P.stats[kRaysC], rays_c);
+        warp_add_u64(&P.stats[kRaysS], rays_s);
+        warp_add_u64(&P.stats[kRaysT], rays_c);
+        warp_add_u64(&P.stats[kOverflow], overflow);
+        return;
+    }
+    PathState ps;
+    int i = -1, k = 0;
+    unsigned dmask = 0;
+    bool exhausted = false;
+    while (true) {
+        const unsigned idle = __ballot_sync(~0u, i < 0);
+        if (!exhausted && (__popc(idle) >= kTailRefill || idle == ~0u)) {
+            int base = 0;
+            if (lane == 0) base = atomicAdd(&P.cnt[kTF], __popc(idle));
+            base = __shfl_sync(~0u, base, 0);
+            if (base + __popc(idle) >= n) exhausted = true;
+            if (i < 0) {
+                const int j = base + __popc(idle & ((1u << lane) - 1u));
+                if (j < n) {
+                    i = j;
+                    ps = load_path(P.cur, i, cache);
+                    k = 0;
+                    dmask = 0;
+                }
+            }
+        }
+        if (!__any_sync(~0u, i >= 0)) {
+            if (exhausted) break;
+            continue;
+        }
+        if (i >= 0) {
+            const bool cont =
+                k < bounces && tail_bounce<kEst, kCache>(P, ps, i, k, defer, dmask, rays_c, rays_s, overflow);
+            if (!cont || ++k >= bounces) {
+                P.fin[ps.id] = make_float4(ps.rad.x, ps.rad.y, ps.rad.z, 0.0f);
+                if (defer) P.td_mask[i] = dmask;
+                i = -1;
+            }
+        }
     }
     warp_add_u64(&P.stats[kRaysC], rays_c);
     warp_add_u64(&P.stats[kRaysS], rays_s);
