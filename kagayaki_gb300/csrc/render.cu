@@ -809,6 +809,21 @@ __device__ __forceinline__ void shade_unbiased_core(const Params &P, PathState &
         if (id < 0) {
             shade_miss<KGK_ESTIMATOR_UNBIASED>(P, d, prev_pdf, T, rad, depth, ps.id);
         } else {
+            // The environment NEE sample, drawn ahead: its random numbers sit
+            // at a fixed place in the path's stream (after the Russian
+            // roulette draw at depth >= rr_start and the emitter sample's
+            // three), so it is drawn here on a copy of the state and its
+            // alias-table and texel loads overlap the surface's.  Used (and
+            // the state moved past it) only where the sequential order
+            // draws it.
+            unsigned long long rs_env = rs;
+            float pe_env = 0.0f;
+            float3 le_env = f3(0.0f, 0.0f, 0.0f), ed_env = le_env;
+            if (s.env) {
+                if (depth >= P.rr_start) rs_env = xorshift64(rs_env);
+                if (s.n_emit > 0) rs_env = xorshift64(xorshift64(xorshift64(rs_env)));
+                ed_env = env_sample_u(s, rs_env, pe_env, le_env);
+            }
             Surface S = load_surface(s, id, h, o, d);
             const float3 n = S.n, wo = -d;
             if (depth == 0 && P.write_gbuffer && first_sample) {
@@ -896,11 +911,11 @@ __device__ __forceinline__ void shade_unbiased_core(const Params &P, PathState &
                         f_tmax = dist * (1.0f - 1e-4f);
                     }
                 }
-                // NEE: one environment sample
+                // NEE: one environment sample (drawn ahead)
                 if (s.env) {
-                    float pe;
-                    float3 Le;
-                    const float3 ed = env_sample_u(s, rs, pe, Le);
+                    const float pe = pe_env;
+                    const float3 Le = le_env, ed = ed_env;
+                    rs = rs_env;
                     const float coss = dot3(n, ed);
                     if (coss > 0.0f && pe > 0.0f) {
                         const float4 fp = bsdf_eval_pdf_k<kMat>(&s.mats[S.mat_id], diffuse_of(S.m), n, wo, ed);
