@@ -539,7 +539,7 @@ def run_svgf_orbit(args):
     from kagayaki_gb300.structs import KgkSvgfConfig
     tris, mats, env, info = build_workload()
     W, H = args.width or 1920, args.height or 1080
-    frames = args.frames
+    frames = args.frames or 60
     scene = Scene(tris, mats, env=env)
     scene.build_bvh()
     kw = dict(spp=1, max_depth=WORKLOAD["max_depth"], estimator=ESTIMATOR_UNBIASED, write_gbuffer=True)
@@ -739,7 +739,7 @@ def run_c5(args):
     a 4096-spp FP64-accumulated frame."""
     from kagayaki_gb300 import ESTIMATOR_UNBIASED, Scene, scenes
     W, H = args.width or 3840, args.height or 2160
-    frames = 120
+    frames = args.frames or 120
     t0 = time.perf_counter()
     tris, mats, tex, info = scenes.c5_scene()
     env, _ = scenes.sky_environment(4096, 2048, sun_peak=1e4, seed=3)
@@ -765,7 +765,25 @@ def run_c5(args):
         wall = time.perf_counter() - t0
         res[mode] = {"frames_per_s_device": round(frames / (dev / 1e3), 2), "frames_per_s_wall": round(frames / wall, 2),
                      "ms_per_frame_device": round(dev / frames, 2)}
-    # static camera: converged reference, cache after training, plain at equal time and at equal relMSE
+    relmse_static = None if args.no_relmse else c5_static_relmse(scene, cam_of, W, H, kw)
+    scene.close()
+    line = {"metric": "frames/s", "value": res["cache"]["frames_per_s_device"], "unit": "frames/s", "n_gpus": 1,
+            "steps": frames, "warmup": 3, "ms_per_step": res["cache"]["ms_per_frame_device"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 (cache MLP bf16)",
+            "data": "synthetic seeded scene",
+            "config": {"workload": "c5-10.6M-4k-1spp-orbit", "triangles": int(len(tris)), "width": W, "height": H,
+                       "textures": "64 x 1024^2 RGBA8, bilinear", "env": "4096x2048 float32 sky + sun 1e4",
+                       "cache": "width 128, 2^18 training paths per frame", "scene_generation_s": round(gen_s, 1),
+                       "bvh_build_ms": round(bvh["ms_build"], 1)},
+            "orbit": res,
+            "relmse_static": relmse_static}
+    print(json.dumps(line), flush=True)
+
+
+def c5_static_relmse(scene, cam_of, W, H, kw):
+    """C5's static-camera study: a converged 4096-spp reference, the cache
+    after 32 training frames, plain at equal time and at equal relMSE."""
+    out = np.empty((H, W, 4), np.float32)
     cam = cam_of(0)
     scene.accum_reset(W, H)
     for k in range(64):
@@ -794,21 +812,10 @@ def run_c5(args):
             eq_relmse = {"plain_spp": spp, "plain_ms": round(stq["ms_device"], 2), "plain_relmse": round(e, 5),
                          "cache_ms": round(cache_ms, 2), "time_ratio": round(stq["ms_device"] / cache_ms, 2)}
             break
-    scene.close()
-    line = {"metric": "frames/s", "value": res["cache"]["frames_per_s_device"], "unit": "frames/s", "n_gpus": 1,
-            "steps": frames, "warmup": 3, "ms_per_step": res["cache"]["ms_per_frame_device"],
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 (cache MLP bf16)",
-            "data": "synthetic seeded scene",
-            "config": {"workload": "c5-10.6M-4k-1spp-orbit", "triangles": int(len(tris)), "width": W, "height": H,
-                       "textures": "64 x 1024^2 RGBA8, bilinear", "env": "4096x2048 float32 sky + sun 1e4",
-                       "cache": "width 128, 2^18 training paths per frame", "scene_generation_s": round(gen_s, 1),
-                       "bvh_build_ms": round(bvh["ms_build"], 1)},
-            "orbit": res,
-            "relmse_static": {"reference_spp": int(nref),
-                              "equal_time": {"ms": round(cache_ms, 2), "cache": round(e_cache, 5),
-                                             "plain": round(e_plain, 5), "plain_spp": spp_eq},
-                              "equal_relmse": eq_relmse}}
-    print(json.dumps(line), flush=True)
+    return {"reference_spp": int(nref),
+            "equal_time": {"ms": round(cache_ms, 2), "cache": round(e_cache, 5), "plain": round(e_plain, 5),
+                           "plain_spp": spp_eq},
+            "equal_relmse": eq_relmse}
 
 
 def c1_camera(H, oracle=False):
@@ -1150,7 +1157,8 @@ def main():
     ap.add_argument("--width", type=int, default=0, help="override the frame width (profiling cases)")
     ap.add_argument("--height", type=int, default=0, help="override the frame height")
     ap.add_argument("--spp", type=int, default=0, help="override the samples per pixel")
-    ap.add_argument("--frames", type=int, default=60, help="orbit frames of svgf-orbit (profiling cases)")
+    ap.add_argument("--frames", type=int, default=0,
+                    help="orbit frames of svgf-orbit (default 60) and c5 (default 120), for profiling cases")
     args = ap.parse_args()
     if args.workload == "c1":
         if int(os.environ.get("RANK", "0")) == 0:

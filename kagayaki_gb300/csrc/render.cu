@@ -1569,6 +1569,10 @@ kgk_status kgk_render(kgk_scene *s, const kgk_camera *cam, const kgk_camera *pre
     Params P;
     memset(&P, 0, sizeof P);
     P.sc = s->dev;
+    // whether shading can write face-light shadow records at all (the compat
+    // estimator samples the reference's light CDF, the unbiased one the
+    // emitter list); without, the face-light shadow pass is not launched
+    const bool face_lights = cfg->estimator == KGK_ESTIMATOR_COMPAT ? !s->dev.no_light : s->dev.n_emit > 0;
     P.sc.tex_filter = cfg->texture_filter == 1 ? 1 : 0;
     P.cam = *cam;
     P.W = W;
@@ -1767,13 +1771,16 @@ kgk_status kgk_render(kgk_scene *s, const kgk_camera *cam, const kgk_camera *pre
             KGK_CUDA(cudaEventRecord(R.shaded, st));
             KGK_CUDA(cudaStreamWaitEvent(sh_st, R.shaded, 0));
             KGK_TRY(stage_begin(2, sh_st));
-            k_shadow<<<grid, 128, 0, sh_st>>>(P, kSH0, kFS0, R.sh_o[0], R.sh_d[0], R.sh_c[0]);
+            if (face_lights) {
+                k_shadow<<<grid, 128, 0, sh_st>>>(P, kSH0, kFS0, R.sh_o[0], R.sh_d[0], R.sh_c[0]);
+                ++launches;
+            }
             k_shadow<<<grid, 128, 0, sh_st>>>(P, kSH1, kFS1, R.sh_o[1], R.sh_d[1], R.sh_c[1]);
             KGK_TRY(stage_end(sh_st));
             KGK_CUDA(cudaEventRecord(R.shadowed, sh_st));
             shadow_pending = true;
             KGK_CUDA(cudaGetLastError());
-            launches += 4;
+            launches += 3;
             c ^= 1;
             P.cur = R.pb[c];
             P.nxt = R.pb[c ^ 1];
