@@ -1237,8 +1237,8 @@ __global__ void __launch_bounds__(128, 8) k_tail_shadow(Params P) {
             }
         }
         if (!__any_sync(~0u, active)) break;
-        if (active && trav_step<false>(s.nodes, (unsigned)s.n_nodes, s.tri_rec, (unsigned)s.n_tris, r, c, stk, true,
-                                       st)) {
+        if (active && trav_step<false, kNodesPerStepShadow>(s.nodes, (unsigned)s.n_nodes, s.tri_rec,
+                                                            (unsigned)s.n_tris, r, c, stk, true, st)) {
             active = false;
             ++rays;
             P.td_vis[slot] = c.hit_slot < 0 ? 1 : 0;
@@ -1314,8 +1314,8 @@ __global__ void __launch_bounds__(128, 8) k_shadow(Params P, int cidx, int fidx,
             }
         }
         if (!__any_sync(~0u, active)) break;
-        if (active && trav_step<false>(s.nodes, (unsigned)s.n_nodes, s.tri_rec, (unsigned)s.n_tris, r, c, stk,
-                                       light < 0, st)) {
+        if (active && trav_step<false, kNodesPerStepShadow>(s.nodes, (unsigned)s.n_nodes, s.tri_rec,
+                                                            (unsigned)s.n_tris, r, c, stk, light < 0, st)) {
             active = false;
             ++rays;
             const bool vis = light >= 0 ? (c.hit_slot >= 0 && c.best_id == light) : c.hit_slot < 0;

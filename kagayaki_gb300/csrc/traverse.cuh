@@ -19,8 +19,10 @@
 namespace kgk {
 
 constexpr int kTravStack = 32;
-// Node visits a resumable traversal step may make before it tests triangles.
+// Node visits a resumable traversal step may make before it tests triangles
+// (the closest-hit rays of k_extend and the batch queries; the shadow passes).
 constexpr int kNodesPerStep = 2;
+constexpr int kNodesPerStepShadow = 2;
 // Conservative widening of box exit distances: 1 + 2 * gamma(5) covers the
 // rounding of the origin offset, the multiply, the two roundings of the
 // biased plane offset and the plane's multiply-add.
@@ -340,13 +342,13 @@ __device__ __forceinline__ void trav_init(Trav &c, float tmax) {
 // closest hit (ties to the smaller id).  Returns true when the traversal is
 // finished; then c.hit_slot is -1 (no hit) or, for the BVH-order triangle ti
 // hit, 2 * ti + its material class (the .w of its second record: 1 = Disney).
-template <bool kCount>
+template <bool kCount, int kVisits = kNodesPerStep>
 __device__ __forceinline__ bool trav_step(const WideNode *__restrict__ nodes, unsigned n_nodes,
                                           const float4 *__restrict__ tri, unsigned n_tris, const RayPre &r,
                                           Trav &c, TravStack &stk, bool any_mode, TravStats &st) {
     uint2 tg = make_uint2(0u, 0u);
 #pragma unroll 1
-    for (int visit = 0; visit < kNodesPerStep && tg.y == 0u; ++visit) {
+    for (int visit = 0; visit < kVisits && tg.y == 0u; ++visit) {
         if ((c.group.y & 0xff000000u) == 0u) {
             if (c.sp == 0) break;
             c.group = stk.e[--c.sp];
